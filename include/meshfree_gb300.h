@@ -1,0 +1,195 @@
+/*
+ * meshfree_gb300.h -- C ABI of libmeshfree_gb300.so, the GB300 (sm_103a) engine for
+ * the RBF-FD semidiscretization hot path of MeshfreeTrixi.jl.
+ *
+ * The reference selects its compute backend through the engine field of
+ * RBFSolver{Basis,Engine} (src/solvers/rbfsolver.jl:68-71), chosen with
+ * PointCloudSolver(basis; engine=...) (src/solvers/pointcloudsolver/types.jl:71-74).
+ * Its CUDA engine is an empty stub (RBFFDEngineCUDA, src/solvers/rbfsolver.jl:60-61).
+ * A Julia engine type `RBFFDEngineGB300 <: AbstractRBFEngine` binds the entry points
+ * below with ccall; each entry point names the reference function it replaces.
+ *
+ * Conventions
+ *  - Every function returns mft_status (0 = MFT_OK).  Nothing aborts, throws across
+ *    the ABI or traps on the device.  mft_last_error() describes the last failure.
+ *  - Host arrays are read during the call only; nothing is retained.
+ *  - Node indices are 0-based int32 unless a function says otherwise (mft_load_csc
+ *    takes the reference's 1-based Int64 CSC arrays as they are).
+ *  - State arrays follow the reference's StructArray layout: nvars separate arrays of
+ *    length n (one per conserved variable), passed as an array of nvars pointers.
+ *  - One context = one CUDA stream on one device; a context is not re-entrant.
+ */
+#ifndef MESHFREE_GB300_H
+#define MESHFREE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mft_ctx mft_ctx;
+typedef int mft_status;
+
+enum {
+  MFT_OK = 0,
+  MFT_ERR_ARG = 1,         /* invalid argument or inconsistent sizes */
+  MFT_ERR_CUDA = 2,        /* CUDA runtime error (message in mft_last_error) */
+  MFT_ERR_STATE = 3,       /* call out of order (e.g. rhs before operators) */
+  MFT_ERR_SINGULAR = 4,    /* a local saddle-point system had an exactly zero pivot */
+  MFT_ERR_NONFINITE = 5,   /* the device produced NaN/Inf (flag word set by kernels) */
+  MFT_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+  MFT_ERR_UNSUPPORTED = 7, /* configuration not provided by this engine */
+  MFT_ERR_NOMEM = 8        /* device or host allocation failed */
+};
+
+/* Equation kinds (Trixi equation types used with point clouds). */
+enum { MFT_EQ_EULER2D = 0, MFT_EQ_ADVECTION = 1 };
+
+/* Boundary-condition kinds (src/equations/PointCloudBCs.jl). */
+enum { MFT_BC_DIRICHLET = 0, MFT_BC_SLIP_WALL = 1, MFT_BC_DO_NOTHING = 2 };
+
+/* Source kinds (src/sources/hyperviscosity.jl). */
+enum { MFT_SRC_RV = 0, MFT_SRC_UPWIND = 1, MFT_SRC_HV_TOMINEC = 2, MFT_SRC_HV_FLYER = 3 };
+
+/* Operator slots. MFT_OP_GRAD holds D_1..D_dim (compute_flux_operator(solver, domain));
+ * MFT_OP_LAP holds sum_d D_d^(2) (Tominec HV builds lap'*lap from it);
+ * MFT_OP_HV holds a ready hyperviscosity operator sum_d D_d^(2k) (Flyer HV). */
+enum { MFT_OP_GRAD = 0, MFT_OP_LAP = 1, MFT_OP_HV = 2 };
+
+/* Arithmetic of the operator apply.  FP64: FP64 weights, states and sums.
+ * FP32: weights generated in FP64 and stored FP32, FP32 states and sums in the
+ * apply; the SSP-RK stage combination stays FP64 with compensated sums. */
+enum { MFT_PREC_FP64 = 0, MFT_PREC_FP32 = 1 };
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device`.  flags: reserved, pass 0. */
+mft_status mft_ctx_create(mft_ctx** ctx, int device, int flags);
+mft_status mft_ctx_destroy(mft_ctx* ctx);
+/* Text of the last error on this context (never NULL; "" if none). */
+const char* mft_last_error(const mft_ctx* ctx);
+mft_status mft_version(int* major, int* minor, int* patch);
+/* Blocks until all work queued on the context stream has finished. */
+mft_status mft_sync(mft_ctx* ctx);
+
+/* ---------------------------------------------------------------- geometry */
+
+/* Node coordinates, n x dim row-major (the reference's Vector{SVector{dim}}).
+ * period: dim box lengths for a periodic (minimum-image) metric, or NULL.
+ * Replaces the point input of PointData (src/domains/PointCloudDomain/
+ * geometry_primatives.jl:322-339).  Resets stencils and operators. */
+mft_status mft_set_points(mft_ctx* ctx, int dim, int64_t n, const double* xyz,
+                          const double* period);
+
+/* Exact k nearest neighbours of every node (self first), ordered by (squared
+ * distance, node index), computed on the GPU; they become the context stencils.
+ * Replaces KDTree + knn(tree, points, nv, true) and the dx_min / dx_avg statistics
+ * of PointData (geometry_primatives.jl:327-334).  out_idx (n*k, host) and
+ * out_dist (n*k, host) may be NULL. */
+mft_status mft_knn(mft_ctx* ctx, int k, int32_t* out_idx, double* out_dist, double* out_dx_min,
+                   double* out_dx_avg);
+
+/* Ragged stencils given by the caller (centre first): rowptr[n+1], cols[rowptr[n]].
+ * Replaces domain.pd.neighbors.  Stencil sizes may differ per node. */
+mft_status mft_set_stencils(mft_ctx* ctx, const int64_t* rowptr, const int32_t* cols);
+
+/* ---------------------------------------------------------------- weights */
+
+/* Batched FP64 polyharmonic-spline (r^rbf_pow) + polynomial (total degree polydeg)
+ * saddle-point solves, one per node, for pure derivatives of order deriv_order along
+ * every axis, in one persistent launch bucketed by stencil size.  Replaces
+ * compute_flux_operator(solver, domain) (compute_operators.jl:409-453, deriv_order 1)
+ * and compute_flux_operator(solver, domain, k) (:549-594).  The result is stored in
+ * operator slot `op`: MFT_OP_GRAD takes the dim components as they are, MFT_OP_LAP and
+ * MFT_OP_HV take their sum over axes (as `sum(...)` at hyperviscosity.jl:44,111).
+ * out_w (host, rowptr[n]*dim, [slot][axis]) may be NULL; out_max_resid receives
+ * max over nodes of ||M w - b||_inf / ||b||_inf when not NULL. */
+mft_status mft_weights(mft_ctx* ctx, int op, int rbf_pow, int polydeg, int deriv_order,
+                       double* out_w, double* out_max_resid);
+
+/* Loads one component of an operator from the reference's SparseMatrixCSC arrays
+ * (1-based colptr[n+1], rowval[nnz], nzval[nnz]), e.g.
+ * semi.cache.rbf_differentiation_matrices[comp+1] (rbfsolver.jl:139).  All loaded
+ * operators must share one sparsity pattern. */
+mft_status mft_load_csc(mft_ctx* ctx, int op, int comp, int64_t n, const int64_t* colptr,
+                        const int64_t* rowval, const double* nzval);
+
+/* ---------------------------------------------------------------- physics */
+
+/* kind MFT_EQ_EULER2D: params[0] = gamma (CompressibleEulerEquations2D);
+ * kind MFT_EQ_ADVECTION: params[0..dim-1] = advection velocity
+ * (LinearScalarAdvectionEquation2D). */
+mft_status mft_set_equations(mft_ctx* ctx, int kind, const double* params);
+
+/* Boundary conditions in the order of the reference's NamedTuple
+ * (calc_boundary_flux!, rbfsolver.jl:277-318): kinds[n_bc], node lists
+ * idx[ptr[b]..ptr[b+1]), outward normals normals[ptr[n_bc]*dim] (slip walls). */
+mft_status mft_set_bcs(mft_ctx* ctx, int n_bc, const int* kinds, const int64_t* ptr,
+                       const int32_t* idx, const double* normals);
+
+/* Boundary values g(x, t) for the Dirichlet-listed nodes (ptr order, nvars each),
+ * used by every following rhs evaluation until replaced
+ * (BoundaryConditionDirichlet, PointCloudBCs.jl:49-63). */
+mft_status mft_set_dirichlet_values(mft_ctx* ctx, const double* values);
+
+/* Host callback that fills Dirichlet values for time t (same layout as above); when
+ * set, the time integrator calls it before every stage instead of using fixed values. */
+typedef void (*mft_dirichlet_fn)(double t, int64_t n_nodes, int nvars, double* values,
+                                 void* user);
+mft_status mft_set_dirichlet_callback(mft_ctx* ctx, mft_dirichlet_fn fn, void* user);
+
+/* Sources in the order of SourceTerms (calc_sources!, rbfsolver.jl:388-395).
+ * params: 4 doubles per source.
+ *   MFT_SRC_RV      {c_rv, c_uw, h = dx_avg, mean_mode}  SourceResidualViscosityTominec
+ *   MFT_SRC_UPWIND  {c_uw, h = dx_avg, 0, 0}             SourceUpwindViscosityTominec
+ *   MFT_SRC_HV_TOMINEC {gamma = c*dx_min^4.5, 0, 0, 0}   SourceHyperviscosityTominec
+ *   MFT_SRC_HV_FLYER   {gamma = c*dx_min^(2k), 0, 0, 0}  SourceHyperviscosityFlyer
+ * mean_mode 0: ode_mean divides by n*nvars (Trixi recursive_length); 1: by n. */
+mft_status mft_set_sources(mft_ctx* ctx, int n_src, const int* kinds, const double* params);
+
+mft_status mft_set_precision(mft_ctx* ctx, int precision);
+
+/* ---------------------------------------------------------------- rhs! */
+
+/* du = rhs!(u, t) with host StructArray-style arrays (nvars pointers of length n).
+ * u is mutated at boundary nodes as the reference's strong BCs do.  Replaces
+ * Trixi.rhs!(du, u, t, domain, equations, ic, bcs, sources, solver, cache)
+ * (rbfsolver.jl:397-428), calc_fluxes! (:247-265) and the source functors. */
+mft_status mft_rhs(mft_ctx* ctx, double* const* du, double* const* u, int nvars, double t);
+
+/* Same on device memory owned by the caller: u and du are nvars x n (SoA) FP64. */
+mft_status mft_rhs_device(mft_ctx* ctx, double* du, double* u, double t);
+
+/* ---------------------------------------------------------------- time integration */
+
+/* Device-resident state: upload / download (host SoA pointers). */
+mft_status mft_set_state(mft_ctx* ctx, const double* const* u, int nvars, double t);
+mft_status mft_get_state(mft_ctx* ctx, double* const* u, int nvars, double* t);
+
+/* Enables the HistoryCallback (src/callbacks_step/history.jl:43-152) with the given
+ * reconstruction order; it runs after every accepted step. */
+mft_status mft_history_init(mft_ctx* ctx, int approx_order);
+
+/* Advances nsteps SSP-RK3 (Shu-Osher, FSAL) steps of size dt on the device state,
+ * each step captured as one CUDA graph when use_graph != 0. */
+mft_status mft_ssprk33(mft_ctx* ctx, double dt, int nsteps, int use_graph);
+
+/* One step from host memory: uploads u, advances nsteps, downloads u (in place). */
+mft_status mft_ssprk33_host(mft_ctx* ctx, double* const* u, int nvars, double* t, double dt,
+                            int nsteps);
+
+/* Sets the fields of the residual-viscosity cache that the HistoryCallback
+ * maintains: approx_du (host StructArray-style, may be NULL to keep it) and
+ * success_iter (SourceResidualViscosityTominec cache, hyperviscosity.jl:202-244;
+ * written by modify_cache!, history.jl:91-103). */
+mft_status mft_set_rv_state(mft_ctx* ctx, const double* const* approx_du, int nvars,
+                            int success_iter);
+
+/* Viscosity of the last RV/upwind source evaluation (host, n values). */
+mft_status mft_get_viscosity(mft_ctx* ctx, double* eps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1096 @@
+// C ABI of libmeshfree_gb300.so and the host-side orchestration of one rhs!
+// evaluation and of the SSP-RK3 integrator with the HistoryCallback.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "mft_ctx.h"
+
+using namespace mft;
+
+#define MFT_VERSION_MAJOR 0
+#define MFT_VERSION_MINOR 1
+#define MFT_VERSION_PATCH 0
+
+namespace {
+
+template <class F>
+mft_status guarded(mft_ctx* c, F&& f) {
+  if (!c) return MFT_ERR_ARG;
+  try {
+    c->err.clear();
+    f();
+    return MFT_OK;
+  } catch (const mft::Error& e) {
+    c->err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    c->err = "host allocation failed";
+    return MFT_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    c->err = e.what();
+    return MFT_ERR_ARG;
+  }
+}
+
+void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
+
+// ---------------------------------------------------------------- ELL layout
+
+// Builds a sliced ELL over rows of a CSR-like structure.  pos[e] receives the
+// ELL element of structure entry e.
+void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& cols,
+               EllBuf& ell, std::vector<int64_t>& pos, cudaStream_t s) {
+  const int64_t nsl = (n + kSlice - 1) / kSlice;
+  std::vector<int64_t> soff(nsl + 1, 0);
+  std::vector<int32_t> rlen(n);
+  int maxlen = 0;
+  for (int64_t sl = 0; sl < nsl; ++sl) {
+    int m = 0;
+    for (int64_t r = sl * kSlice; r < std::min<int64_t>(n, (sl + 1) * kSlice); ++r) {
+      const int len = (int)(rowptr[r + 1] - rowptr[r]);
+      rlen[r] = len;
+      m = std::max(m, len);
+    }
+    maxlen = std::max(maxlen, m);
+    soff[sl + 1] = soff[sl] + (int64_t)m * kSlice;
+  }
+  const int64_t ne = soff[nsl];
+  std::vector<int32_t> col(ne);
+  pos.assign(rowptr[n], 0);
+  for (int64_t sl = 0; sl < nsl; ++sl) {
+    const int m = (int)((soff[sl + 1] - soff[sl]) / kSlice);
+    for (int64_t lane = 0; lane < kSlice; ++lane) {
+      const int64_t r = sl * kSlice + lane;
+      for (int j = 0; j < m; ++j) {
+        const int64_t e = soff[sl] + (int64_t)j * kSlice + lane;
+        if (r < n && j < rlen[r]) {
+          col[e] = cols[rowptr[r] + j];
+          pos[rowptr[r] + j] = e;
+        } else {
+          col[e] = (int32_t)(r < n ? r : 0);  // padding: a valid index, never read
+        }
+      }
+    }
+  }
+  ell.n = n;
+  ell.n_elems = ne;
+  ell.max_len = maxlen;
+  ell.slice_off.upload(soff, s);
+  ell.row_len.upload(rlen, s);
+  ell.col.upload(col, s);
+}
+
+}  // namespace
+
+namespace mft {
+
+void finish_pattern(mft_ctx* c) {
+  const int64_t n = c->n;
+  const int64_t nnz = c->rp[n];
+  // CSC view (rows ascending inside each column) with the map to CSR entries.
+  c->cp.assign(n + 1, 0);
+  for (int64_t e = 0; e < nnz; ++e) c->cp[c->ci[e] + 1]++;
+  for (int64_t j = 0; j < n; ++j) c->cp[j + 1] += c->cp[j];
+  c->ri.assign(nnz, 0);
+  c->csc2csr.assign(nnz, 0);
+  std::vector<int64_t> fill(c->cp.begin(), c->cp.end() - 1);
+  for (int64_t r = 0; r < n; ++r)
+    for (int64_t e = c->rp[r]; e < c->rp[r + 1]; ++e) {
+      const int64_t p = fill[c->ci[e]]++;
+      c->ri[p] = (int32_t)r;
+      c->csc2csr[p] = e;
+    }
+  for (int k = 0; k < kSlots; ++k) {
+    c->val[k].clear();
+    c->have_val[k] = false;
+  }
+  c->have_pattern = true;
+  c->dev_dirty = true;
+  c->fsal_valid = false;
+}
+
+void pattern_from_stencils(mft_ctx* c) {
+  const int64_t n = c->n;
+  c->rp.assign(n + 1, 0);
+  c->ci.assign(c->st_ci.size(), 0);
+  c->st2csr.assign(c->st_ci.size(), 0);
+  std::vector<int64_t> ord;
+  for (int64_t r = 0; r < n; ++r) {
+    const int64_t b = c->st_rp[r], e = c->st_rp[r + 1];
+    ord.resize(e - b);
+    std::iota(ord.begin(), ord.end(), b);
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int64_t x, int64_t y) { return c->st_ci[x] < c->st_ci[y]; });
+    for (int64_t k = 0; k < e - b; ++k) {
+      MFT_REQUIRE(k == 0 || c->st_ci[ord[k]] != c->st_ci[ord[k - 1]], MFT_ERR_ARG,
+                  "stencil of node " + std::to_string(r) + " lists a node twice");
+      c->ci[b + k] = c->st_ci[ord[k]];
+      c->st2csr[ord[k]] = b + k;
+    }
+    c->rp[r + 1] = e;
+  }
+  finish_pattern(c);
+}
+
+void ensure_work(mft_ctx* c) {
+  const int64_t n = c->n;
+  const int V = c->nvars;
+  MFT_REQUIRE(V > 0, MFT_ERR_STATE, "equations not set");
+  const size_t nv = (size_t)n * V;
+  for (auto* b : {&c->U[0], &c->U[1], &c->U[2], &c->U[3]}) b->alloc(nv);
+  c->F.alloc((size_t)n * 2 * V);
+  c->du_p.alloc(nv);
+  c->du_p2.alloc(nv);
+  c->t.alloc((size_t)n * 2 * V);
+  c->q.alloc(nv);
+  c->hvf.alloc(nv);
+  c->eps.alloc(n);
+  if (c->approx_du.n != nv) {
+    c->approx_du.alloc(nv);
+    c->approx_du.zero(c->stream);
+  }
+  c->soa.alloc(nv);
+  c->soa2.alloc(nv);
+  c->work_u.alloc(nv);
+  c->work_du.alloc(nv);
+  if (c->red_blocks == 0) {
+    c->red_blocks = 512;
+    c->red_partial.alloc((size_t)c->red_blocks * 8);
+    c->red_counter.alloc(2);
+    c->red_counter.zero(c->stream);
+    c->mean.alloc(8);
+    c->norms.alloc(8);
+  }
+  if (c->precision == MFT_PREC_FP32) {
+    for (auto* b : {&c->U32[0], &c->U32[1], &c->U32[2], &c->U32[3]}) b->alloc(nv);
+    c->du_p32.alloc(nv);
+    c->du_p2_32.alloc(nv);
+    c->t32.alloc((size_t)n * 2 * V);
+    c->q32.alloc(nv);
+    c->work_u32.alloc(nv);
+  }
+}
+
+void ensure_device_ops(mft_ctx* c) {
+  MFT_REQUIRE(c->have_pattern, MFT_ERR_STATE, "no operator pattern: call mft_knn, mft_set_stencils or mft_load_csc");
+  for (int d = 0; d < c->dim; ++d)
+    MFT_REQUIRE(c->have_val[d], MFT_ERR_STATE,
+                "gradient operator component " + std::to_string(d) + " not set");
+  if (!c->dev_dirty) return;
+  cudaStream_t s = c->stream;
+  std::vector<int64_t> pos;
+  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s);
+  c->fwd_pos.upload(pos, s);
+  std::vector<int64_t> rpos_csc;
+  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s);
+  std::vector<int64_t> rpos(rpos_csc.size());
+  for (size_t p = 0; p < rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
+  c->rev_pos.upload(rpos, s);
+  const std::vector<int64_t>& fpos = pos;
+  for (int k = 0; k < kSlots; ++k) {
+    if (!c->have_val[k]) {
+      c->fw[k].release(); c->rw[k].release(); c->fw32[k].release(); c->rw32[k].release();
+      continue;
+    }
+    std::vector<double> f(c->fwd.n_elems, 0.0), r(c->rev.n_elems, 0.0);
+    std::vector<float> f32(c->fwd.n_elems, 0.0f), r32(c->rev.n_elems, 0.0f);
+    const std::vector<double>& v = c->val[k];
+    for (size_t e = 0; e < v.size(); ++e) {
+      f[fpos[e]] = v[e];
+      r[rpos[e]] = v[e];
+      f32[fpos[e]] = (float)v[e];
+      r32[rpos[e]] = (float)v[e];
+    }
+    c->fw[k].upload(f, s);
+    c->rw[k].upload(r, s);
+    c->fw32[k].upload(f32, s);
+    c->rw32[k].upload(r32, s);
+  }
+  MFT_CUDA(cudaStreamSynchronize(s));
+  c->dev_dirty = false;
+}
+
+static void ensure_bcs(mft_ctx* c) {
+  if (!c->bc_dirty) return;
+  cudaStream_t s = c->stream;
+  const int64_t n = c->n;
+  std::vector<int8_t> tag(n, 0);
+  std::vector<int32_t> slot(n, 0);
+  std::vector<int32_t> bnode;
+  const int64_t total = c->n_bc ? c->bc_ptr[c->n_bc] : 0;
+  for (int b = 0; b < c->n_bc; ++b) {
+    const int k = c->bc_kind[b];
+    for (int64_t p = c->bc_ptr[b]; p < c->bc_ptr[b + 1]; ++p) {
+      const int32_t i = c->bc_idx[p];
+      if (k == MFT_BC_DO_NOTHING) continue;
+      if (k == MFT_BC_SLIP_WALL && c->eq != MFT_EQ_EULER2D) continue;
+      MFT_REQUIRE(tag[i] == 0, MFT_ERR_UNSUPPORTED,
+                  "node " + std::to_string(i) + " carries two active boundary conditions");
+      tag[i] = k == MFT_BC_DIRICHLET ? 1 : 2;
+      slot[i] = (int32_t)p;
+      bnode.push_back(i);
+    }
+  }
+  c->nb = (int64_t)bnode.size();
+  c->d_tag.upload(tag, s);
+  c->d_slot.upload(slot, s);
+  std::vector<double> nrm((size_t)std::max<int64_t>(total, 1) * 2, 0.0);
+  for (int64_t p = 0; p < total && !c->bc_normal.empty(); ++p)
+    for (int d = 0; d < 2 && d < c->dim; ++d) nrm[p * 2 + d] = c->bc_normal[p * c->dim + d];
+  c->d_normal.upload(nrm, s);
+  if (bnode.empty()) bnode.push_back(0);
+  c->d_bnode.upload(bnode, s);
+  c->d_dvals.alloc((size_t)std::max<int64_t>(total, 1) * std::max(c->nvars, 1));
+  if (!c->dir_values.empty())
+    MFT_CUDA(cudaMemcpyAsync(c->d_dvals.p, c->dir_values.data(),
+                             c->dir_values.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+  MFT_CUDA(cudaStreamSynchronize(s));
+  c->bc_dirty = false;
+}
+
+// Dirichlet values for time t through the registered host callback.
+static void refresh_dirichlet(mft_ctx* c, double t) {
+  if (!c->dir_fn || c->n_bc == 0) return;
+  const int64_t total = c->bc_ptr[c->n_bc];
+  c->dir_scratch.assign((size_t)total * c->nvars, 0.0);
+  c->dir_fn(t, total, c->nvars, c->dir_scratch.data(), c->dir_user);
+  MFT_CUDA(cudaStreamSynchronize(c->stream));
+  MFT_CUDA(cudaMemcpyAsync(c->d_dvals.p, c->dir_scratch.data(),
+                           c->dir_scratch.size() * sizeof(double), cudaMemcpyHostToDevice,
+                           c->stream));
+  MFT_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void launch_fwd(mft_ctx* c, const FwdArgs& a) {
+  if (c->precision == MFT_PREC_FP32) launch_fwd_f32(a, c->stream);
+  else launch_fwd_f64(a, c->stream);
+}
+void launch_rev(mft_ctx* c, const RevArgs& a) {
+  if (c->precision == MFT_PREC_FP32) launch_rev_f32(a, c->stream);
+  else launch_rev_f64(a, c->stream);
+}
+
+void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_in) {
+  ensure_device_ops(c);
+  ensure_bcs(c);
+  refresh_dirichlet(c, t);
+  cudaStream_t s = c->stream;
+  const int64_t n = c->n;
+  const int V = c->nvars;
+  const bool f32 = c->precision == MFT_PREC_FP32;
+  MFT_REQUIRE(!f32 || us32, MFT_ERR_STATE, "FP32 apply needs the FP32 state shadow");
+
+  BcDev bc{c->d_tag.p, c->d_slot.p, c->d_normal.p, c->d_dvals.p};
+  Epilogue ep = ep_in;
+  ep.bc = bc;
+  ep.has_bc = c->nb > 0;
+  ep.u_s = us;
+
+  // 1. strong BCs, pass 1 (mutates u)
+  if (c->nb > 0) launch_bc_pass1(c->nb, c->d_bnode.p, V, c->eq, bc, us, us32, s);
+
+  // sources: at most one viscosity source and one hyperviscosity source
+  int iv = -1, ih = -1;
+  for (size_t k = 0; k < c->src_kind.size(); ++k) {
+    const int kind = c->src_kind[k];
+    if (kind == MFT_SRC_RV || kind == MFT_SRC_UPWIND) {
+      MFT_REQUIRE(iv < 0, MFT_ERR_UNSUPPORTED, "more than one viscosity source");
+      iv = (int)k;
+    } else {
+      MFT_REQUIRE(ih < 0, MFT_ERR_UNSUPPORTED, "more than one hyperviscosity source");
+      ih = (int)k;
+    }
+  }
+  const bool tominec = ih >= 0 && c->src_kind[ih] == MFT_SRC_HV_TOMINEC;
+  const bool flyer = ih >= 0 && c->src_kind[ih] == MFT_SRC_HV_FLYER;
+  const bool hv_first = ih >= 0 && iv >= 0 && ih < iv;
+  const double hv_gamma = ih >= 0 ? c->src_par[ih * 4] : 0.0;
+  if (tominec) MFT_REQUIRE(c->have_val[kSlotLap], MFT_ERR_STATE, "Tominec HV needs MFT_OP_LAP");
+  if (flyer) MFT_REQUIRE(c->have_val[kSlotHv], MFT_ERR_STATE, "Flyer HV needs MFT_OP_HV");
+
+  // 2. flux per node (FP64 Euler)
+  if (!f32) launch_flux_f64(n, c->eq, V, c->gamma, us, c->F.p, s);
+
+  // 3. forward gather
+  FwdArgs fa{};
+  fa.n = n;
+  fa.ell = c->fwd.view();
+  for (int d = 0; d < 3; ++d) {
+    fa.w[d] = d < c->dim ? c->fw[d].p : nullptr;
+    fa.w32[d] = d < c->dim ? c->fw32[d].p : nullptr;
+  }
+  const int wl_slot = tominec ? kSlotLap : (flyer ? kSlotHv : -1);
+  fa.wl = wl_slot >= 0 ? c->fw[wl_slot].p : nullptr;
+  fa.wl32 = wl_slot >= 0 ? c->fw32[wl_slot].p : nullptr;
+  fa.F = c->F.p;
+  fa.u = us;
+  fa.u32 = us32;
+  fa.eq = c->eq;
+  fa.V = V;
+  fa.gamma = c->gamma;
+  fa.ax = c->adv[0];
+  fa.ay = c->adv[1];
+  fa.hv_gamma = hv_gamma;
+  fa.want_t = iv >= 0;
+  fa.want_q = tominec;
+  fa.flyer = flyer ? ((iv < 0 || hv_first) ? 1 : 2) : 0;
+  fa.du_p = c->du_p.p;
+  fa.t = c->t.p;
+  fa.q = c->q.p;
+  fa.hvf = c->hvf.p;
+  fa.du_p32 = c->du_p32.p;
+  fa.t32 = c->t32.p;
+  fa.q32 = c->q32.p;
+  fa.final_epilogue = (iv < 0 && !tominec);
+  fa.ep = ep;
+  launch_fwd(c, fa);
+  if (fa.final_epilogue) return;
+
+  RevArgs ra{};
+  ra.n = n;
+  ra.ell = c->rev.view();
+  for (int d = 0; d < 3; ++d) {
+    ra.w[d] = d < c->dim ? c->rw[d].p : nullptr;
+    ra.w32[d] = d < c->dim ? c->rw32[d].p : nullptr;
+  }
+  ra.wl = tominec ? c->rw[kSlotLap].p : nullptr;
+  ra.wl32 = tominec ? c->rw32[kSlotLap].p : nullptr;
+  ra.V = V;
+  ra.hv_gamma = hv_gamma;
+  ra.q = c->q.p;
+  ra.q32 = c->q32.p;
+  ra.s = c->t.p;
+  ra.s32 = c->t32.p;
+
+  double* dp = c->du_p.p;
+  float* dp32 = c->du_p32.p;
+  if (tominec && hv_first) {
+    // lap' q must be part of the partial du that the residual viscosity reads.
+    RevArgs r1 = ra;
+    r1.rv = 0;
+    r1.lap = 1;
+    r1.du_p = dp;
+    r1.du_p32 = dp32;
+    r1.hvf = nullptr;
+    r1.final_epilogue = 0;
+    r1.du_p_out = c->du_p2.p;
+    r1.du_p_out32 = c->du_p2_32.p;
+    r1.ep = ep;
+    launch_rev(c, r1);
+    dp = c->du_p2.p;
+    dp32 = c->du_p2_32.p;
+  }
+
+  if (iv >= 0) {
+    const int kind = c->src_kind[iv];
+    const double* par = &c->src_par[iv * 4];
+    const int mode = kind == MFT_SRC_RV ? (int)par[3] : 0;
+    if (kind == MFT_SRC_RV) {
+      const double denom = mode == 0 ? (double)n * V : (double)n;
+      launch_mean(n, V, us, denom, c->red_partial.p, c->red_counter.p, c->mean.p,
+                  c->red_blocks, s);
+      launch_lexmax(n, V, us, c->mean.p, mode, c->red_partial.p, c->red_counter.p + 1,
+                    c->norms.p, c->red_blocks, s);
+    }
+    EpsArgs ea{};
+    ea.n = n;
+    ea.eq = c->eq;
+    ea.V = V;
+    ea.kind = kind;
+    ea.gamma = c->gamma;
+    ea.ax = c->adv[0];
+    ea.ay = c->adv[1];
+    ea.c_rv = kind == MFT_SRC_RV ? par[0] : 0.0;
+    ea.c_uw = kind == MFT_SRC_RV ? par[1] : par[0];
+    ea.h = kind == MFT_SRC_RV ? par[2] : par[1];
+    ea.success_iter = c->success_iter;
+    ea.u = us;
+    ea.du_p = f32 ? nullptr : dp;
+    ea.du_p32 = f32 ? dp32 : nullptr;
+    ea.hvf = nullptr;
+    ea.approx_du = c->approx_du.p;
+    ea.norms = c->norms.p;
+    ea.t = f32 ? nullptr : c->t.p;
+    ea.t32 = f32 ? c->t32.p : nullptr;
+    ea.eps = c->eps.p;
+    launch_eps(ea, s);
+  }
+
+  RevArgs r2 = ra;
+  r2.rv = iv >= 0;
+  r2.lap = tominec && !hv_first;
+  r2.du_p = dp;
+  r2.du_p32 = dp32;
+  r2.hvf = (flyer && fa.flyer == 2) ? c->hvf.p : nullptr;
+  r2.final_epilogue = 1;
+  r2.du_p_out = nullptr;
+  r2.ep = ep;
+  launch_rev(c, r2);
+}
+
+}  // namespace mft
+
+// ---------------------------------------------------------------- history helpers
+
+namespace {
+
+// time_deriv_weights! (src/callbacks_step/history.jl:131-152): w = scale*(A'\b),
+// A[i][k] = (t_i*scale)^k, b[k] = k*(t_0*scale)^(k-1), LU with partial pivoting.
+int time_deriv_weights(int m, const double* t, double* w) {
+  if (m < 1 || m > 16) return -1;
+  double a[16][16], b[16], tt[16];
+  double tmax = 0.0;
+  for (int i = 0; i < m; ++i) {
+    const double v = fabs(t[i]);
+    if (isnan(v) || v > tmax) tmax = isnan(tmax) ? tmax : v;
+  }
+  const double scale = 1.0 / tmax;
+  for (int i = 0; i < m; ++i) tt[i] = t[i] * scale;
+  const double te = tt[0];
+  auto pw = [](double x, int k) {
+    if (k < 0) {
+      double r = 1.0;
+      for (int i = 0; i < -k; ++i) r = r * x;
+      return 1.0 / r;
+    }
+    double r = 1.0;
+    for (int i = 0; i < k; ++i) r = r * x;
+    return r;
+  };
+  for (int i = 0; i < m; ++i)
+    for (int k = 0; k < m; ++k) a[k][i] = k == 0 ? 1.0 : pw(tt[i], k);
+  for (int k = 0; k < m; ++k) b[k] = (double)k * (k == 0 ? 1.0 / te : pw(te, k - 1));
+  for (int cc = 0; cc < m; ++cc) {
+    int p = cc;
+    double mx = fabs(a[cc][cc]);
+    for (int r = cc + 1; r < m; ++r)
+      if (fabs(a[r][cc]) > mx) { mx = fabs(a[r][cc]); p = r; }
+    if (p != cc) {
+      for (int k = 0; k < m; ++k) std::swap(a[cc][k], a[p][k]);
+      std::swap(b[cc], b[p]);
+    }
+    if (a[cc][cc] == 0.0) return -3;
+    const double rinv = 1.0 / a[cc][cc];
+    for (int r = cc + 1; r < m; ++r) {
+      const double l = a[r][cc] * rinv;
+      a[r][cc] = l;
+      for (int k = cc + 1; k < m; ++k) a[r][k] = a[r][k] - l * a[cc][k];
+    }
+  }
+  for (int cc = 0; cc < m; ++cc)
+    if (b[cc] != 0.0)
+      for (int r = cc + 1; r < m; ++r) b[r] = b[r] - b[cc] * a[r][cc];
+  for (int cc = m - 1; cc >= 0; --cc) {
+    if (b[cc] != 0.0) {
+      b[cc] = b[cc] / a[cc][cc];
+      for (int r = 0; r < cc; ++r) b[r] = b[r] - b[cc] * a[r][cc];
+    }
+  }
+  for (int i = 0; i < m; ++i) w[i] = scale * b[i];
+  return 0;
+}
+
+// modify_cache!(::SourceResidualViscosityTominec) (history.jl:91-103): push (t, u)
+// into the ring (newest first) and rebuild approx_du from min(success_iter+1, p+1)
+// points.
+void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
+  if (c->hist_order < 0) return;
+  const int slots = c->hist_order + 1;
+  const size_t nv = (size_t)c->n * c->nvars;
+  cudaStream_t s = c->stream;
+  c->success_iter = success_iter;
+  for (int k = slots - 1; k > 0; --k) c->hist_t[k] = c->hist_t[k - 1];
+  c->hist_t[0] = t;
+  c->hist_head = (c->hist_head + slots - 1) % slots;
+  MFT_CUDA(cudaMemcpyAsync(c->hist[c->hist_head].p, u_aos, nv * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+  const int m = std::min(success_iter + 1, slots);
+  if (success_iter <= 0) {
+    c->approx_du.zero(s);
+    return;
+  }
+  double w[16];
+  MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
+              "time_deriv_weights: singular Vandermonde system");
+  // Weights go through a small device buffer so that later launches may reuse it.
+  MFT_CUDA(cudaMemcpyAsync(c->hist_w.p, w, m * sizeof(double), cudaMemcpyHostToDevice, s));
+  MFT_CUDA(cudaStreamSynchronize(s));
+  const double* hs[8];
+  for (int k = 0; k < m; ++k) hs[k] = c->hist[(c->hist_head + k) % slots].p;
+  launch_history((int64_t)nv, m, c->hist_w.p, hs, c->approx_du.p, s);
+}
+
+void check_state_ready(mft_ctx* c) {
+  MFT_REQUIRE(c->n > 0, MFT_ERR_STATE, "no points set");
+  MFT_REQUIRE(c->eq >= 0, MFT_ERR_STATE, "equations not set");
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+mft_status mft_version(int* major, int* minor, int* patch) {
+  if (major) *major = MFT_VERSION_MAJOR;
+  if (minor) *minor = MFT_VERSION_MINOR;
+  if (patch) *patch = MFT_VERSION_PATCH;
+  return MFT_OK;
+}
+
+mft_status mft_ctx_create(mft_ctx** out, int device, int flags) {
+  if (!out) return MFT_ERR_ARG;
+  *out = nullptr;
+  (void)flags;
+  mft_ctx* c = nullptr;
+  try {
+    c = new mft_ctx();
+  } catch (...) {
+    return MFT_ERR_NOMEM;
+  }
+  c->device = device;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || device < 0 || device >= count) {
+    delete c;
+    return e != cudaSuccess ? MFT_ERR_CUDA : MFT_ERR_ARG;
+  }
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return MFT_ERR_CUDA;
+  }
+  *out = c;
+  return MFT_OK;
+}
+
+mft_status mft_ctx_destroy(mft_ctx* c) {
+  if (!c) return MFT_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  delete c;
+  return MFT_OK;
+}
+
+const char* mft_last_error(const mft_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+mft_status mft_sync(mft_ctx* c) {
+  return guarded(c, [&] {
+    set_device(c);
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+mft_status mft_set_points(mft_ctx* c, int dim, int64_t n, const double* xyz, const double* period) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(dim >= 1 && dim <= 3, MFT_ERR_ARG, "dim must be 1, 2 or 3");
+    MFT_REQUIRE(n >= 1 && n < (int64_t)INT32_MAX, MFT_ERR_ARG, "node count out of range");
+    MFT_REQUIRE(xyz, MFT_ERR_ARG, "xyz is NULL");
+    set_device(c);
+    c->dim = dim;
+    c->n = n;
+    c->xyz.assign(xyz, xyz + (size_t)n * dim);
+    c->periodic = period != nullptr;
+    for (int d = 0; d < 3; ++d) c->period[d] = (period && d < dim) ? period[d] : 0.0;
+    if (period)
+      for (int d = 0; d < dim; ++d)
+        MFT_REQUIRE(period[d] > 0.0, MFT_ERR_ARG, "period lengths must be positive");
+    c->d_xyz.upload(c->xyz, c->stream);
+    c->have_stencils = false;
+    c->have_pattern = false;
+    for (int k = 0; k < kSlots; ++k) c->have_val[k] = false;
+    c->dev_dirty = true;
+    c->bc_dirty = true;
+    c->state_valid = false;
+    c->fsal_valid = false;
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+mft_status mft_set_stencils(mft_ctx* c, const int64_t* rowptr, const int32_t* cols) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->n > 0, MFT_ERR_STATE, "call mft_set_points first");
+    MFT_REQUIRE(rowptr && cols, MFT_ERR_ARG, "NULL stencil arrays");
+    MFT_REQUIRE(rowptr[0] == 0, MFT_ERR_ARG, "rowptr[0] must be 0");
+    for (int64_t i = 0; i < c->n; ++i)
+      MFT_REQUIRE(rowptr[i + 1] > rowptr[i], MFT_ERR_ARG, "empty stencil");
+    const int64_t nnz = rowptr[c->n];
+    for (int64_t e = 0; e < nnz; ++e)
+      MFT_REQUIRE(cols[e] >= 0 && cols[e] < c->n, MFT_ERR_ARG, "stencil index out of range");
+    c->st_rp.assign(rowptr, rowptr + c->n + 1);
+    c->st_ci.assign(cols, cols + nnz);
+    c->have_stencils = true;
+    pattern_from_stencils(c);
+  });
+}
+
+mft_status mft_knn(mft_ctx* c, int k, int32_t* out_idx, double* out_dist, double* out_dx_min,
+                   double* out_dx_avg) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->n > 0, MFT_ERR_STATE, "call mft_set_points first");
+    MFT_REQUIRE(k >= 1 && k <= c->n && k <= 1024, MFT_ERR_ARG, "k out of range");
+    set_device(c);
+    std::vector<int32_t> idx;
+    std::vector<double> dist;
+    double dmin = 0, davg = 0;
+    knn_device(c, k, idx, out_dist ? &dist : nullptr, &dmin, &davg);
+    c->st_rp.resize(c->n + 1);
+    for (int64_t i = 0; i <= c->n; ++i) c->st_rp[i] = i * k;
+    c->st_ci = idx;
+    c->have_stencils = true;
+    pattern_from_stencils(c);
+    if (out_idx) memcpy(out_idx, idx.data(), idx.size() * sizeof(int32_t));
+    if (out_dist) memcpy(out_dist, dist.data(), dist.size() * sizeof(double));
+    if (out_dx_min) *out_dx_min = dmin;
+    if (out_dx_avg) *out_dx_avg = davg;
+  });
+}
+
+mft_status mft_weights(mft_ctx* c, int op, int rbf_pow, int polydeg, int deriv_order,
+                       double* out_w, double* out_max_resid) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->have_stencils, MFT_ERR_STATE, "no stencils: call mft_knn or mft_set_stencils");
+    MFT_REQUIRE(op >= MFT_OP_GRAD && op <= MFT_OP_HV, MFT_ERR_ARG, "bad operator slot");
+    MFT_REQUIRE(deriv_order >= 1 && deriv_order <= 8, MFT_ERR_ARG, "deriv_order out of range");
+    MFT_REQUIRE(polydeg >= 0 && polydeg <= 6, MFT_ERR_ARG, "polydeg out of range");
+    MFT_REQUIRE(rbf_pow >= 1 && rbf_pow <= 15, MFT_ERR_ARG, "rbf_pow out of range");
+    set_device(c);
+    std::vector<double> w;
+    weights_device(c, rbf_pow, polydeg, deriv_order, w, out_max_resid);
+    const int64_t nnz = (int64_t)c->st_ci.size();
+    const int D = c->dim;
+    if (out_w) memcpy(out_w, w.data(), (size_t)nnz * D * sizeof(double));
+    if (op == MFT_OP_GRAD) {
+      for (int d = 0; d < D; ++d) {
+        c->val[d].assign(nnz, 0.0);
+        for (int64_t e = 0; e < nnz; ++e) c->val[d][c->st2csr[e]] = w[e * D + d];
+        c->have_val[d] = true;
+      }
+    } else {
+      const int slot = op == MFT_OP_LAP ? kSlotLap : kSlotHv;
+      c->val[slot].assign(nnz, 0.0);
+      for (int64_t e = 0; e < nnz; ++e) {
+        double acc = w[e * D];
+        for (int d = 1; d < D; ++d) acc = acc + w[e * D + d];  // sum(operators)
+        c->val[slot][c->st2csr[e]] = acc;
+      }
+      c->have_val[slot] = true;
+    }
+    c->dev_dirty = true;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_load_csc(mft_ctx* c, int op, int comp, int64_t n, const int64_t* colptr,
+                        const int64_t* rowval, const double* nzval) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->n > 0 && n == c->n, MFT_ERR_ARG, "operator size differs from the point count");
+    MFT_REQUIRE(colptr && rowval && nzval, MFT_ERR_ARG, "NULL CSC arrays");
+    MFT_REQUIRE(op >= MFT_OP_GRAD && op <= MFT_OP_HV, MFT_ERR_ARG, "bad operator slot");
+    MFT_REQUIRE(op != MFT_OP_GRAD || (comp >= 0 && comp < c->dim), MFT_ERR_ARG, "bad component");
+    MFT_REQUIRE(colptr[0] == 1, MFT_ERR_ARG, "colptr must be 1-based (colptr[0] == 1)");
+    const int64_t nnz = colptr[n] - 1;
+    MFT_REQUIRE(nnz >= 0, MFT_ERR_ARG, "bad colptr");
+    for (int64_t j = 0; j < n; ++j)
+      MFT_REQUIRE(colptr[j + 1] >= colptr[j], MFT_ERR_ARG, "colptr not monotone");
+    for (int64_t p = 0; p < nnz; ++p) {
+      MFT_REQUIRE(rowval[p] >= 1 && rowval[p] <= n, MFT_ERR_ARG, "rowval out of range");
+    }
+    // The first load defines the pattern (CSR with ascending columns + CSC view);
+    // later loads must repeat it.
+    bool same = c->have_pattern && (int64_t)c->ri.size() == nnz;
+    if (same) {
+      for (int64_t j = 0; j <= n && same; ++j) same = c->cp[j] == colptr[j] - 1;
+      for (int64_t p = 0; p < nnz && same; ++p) same = c->ri[p] == rowval[p] - 1;
+    }
+    if (!same) {
+      bool any = false;
+      for (int k = 0; k < kSlots; ++k) any = any || (c->have_pattern && c->have_val[k]);
+      MFT_REQUIRE(!any, MFT_ERR_ARG, "operator sparsity pattern differs from the loaded operators");
+      c->rp.assign(n + 1, 0);
+      for (int64_t p = 0; p < nnz; ++p) c->rp[rowval[p]]++;
+      for (int64_t i = 0; i < n; ++i) c->rp[i + 1] += c->rp[i];
+      c->ci.assign(nnz, 0);
+      std::vector<int64_t> fill(c->rp.begin(), c->rp.end() - 1);
+      for (int64_t j = 0; j < n; ++j)
+        for (int64_t p = colptr[j] - 1; p < colptr[j + 1] - 1; ++p)
+          c->ci[fill[rowval[p] - 1]++] = (int32_t)j;
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t e = c->rp[i] + 1; e < c->rp[i + 1]; ++e)
+          MFT_REQUIRE(c->ci[e] > c->ci[e - 1], MFT_ERR_ARG, "duplicate entries in CSC");
+      finish_pattern(c);
+      c->st2csr.clear();
+      c->have_stencils = false;
+    }
+    const int slot = op == MFT_OP_GRAD ? comp : (op == MFT_OP_LAP ? kSlotLap : kSlotHv);
+    c->val[slot].assign(nnz, 0.0);
+    for (int64_t p = 0; p < nnz; ++p) c->val[slot][c->csc2csr[p]] = nzval[p];
+    c->have_val[slot] = true;
+    c->dev_dirty = true;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_set_equations(mft_ctx* c, int kind, const double* params) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(params, MFT_ERR_ARG, "params is NULL");
+    MFT_REQUIRE(c->dim == 2, MFT_ERR_UNSUPPORTED, "the rhs! engine covers 2D point clouds");
+    if (kind == MFT_EQ_EULER2D) {
+      c->eq = kind;
+      c->nvars = 4;
+      c->gamma = params[0];
+    } else if (kind == MFT_EQ_ADVECTION) {
+      c->eq = kind;
+      c->nvars = 1;
+      for (int d = 0; d < c->dim; ++d) c->adv[d] = params[d];
+    } else {
+      throw mft::Error(MFT_ERR_ARG, "unknown equation kind");
+    }
+    c->bc_dirty = true;
+    c->state_valid = false;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_set_bcs(mft_ctx* c, int n_bc, const int* kinds, const int64_t* ptr,
+                       const int32_t* idx, const double* normals) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(n_bc >= 0, MFT_ERR_ARG, "n_bc < 0");
+    MFT_REQUIRE(n_bc == 0 || (kinds && ptr), MFT_ERR_ARG, "NULL bc arrays");
+    c->n_bc = n_bc;
+    c->bc_kind.assign(kinds, kinds + n_bc);
+    c->bc_ptr.assign(ptr, ptr + n_bc + 1);
+    const int64_t total = n_bc ? ptr[n_bc] : 0;
+    MFT_REQUIRE(n_bc == 0 || ptr[0] == 0, MFT_ERR_ARG, "ptr[0] must be 0");
+    c->bc_idx.assign(idx, idx + total);
+    for (int64_t p = 0; p < total; ++p)
+      MFT_REQUIRE(idx[p] >= 0 && idx[p] < c->n, MFT_ERR_ARG, "boundary index out of range");
+    for (int b = 0; b < n_bc; ++b)
+      MFT_REQUIRE(kinds[b] >= MFT_BC_DIRICHLET && kinds[b] <= MFT_BC_DO_NOTHING, MFT_ERR_ARG,
+                  "unknown boundary-condition kind");
+    c->bc_normal.assign(normals ? normals : nullptr, normals ? normals + total * c->dim : nullptr);
+    c->dir_values.assign((size_t)total * std::max(c->nvars, 1), 0.0);
+    c->bc_dirty = true;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_set_dirichlet_values(mft_ctx* c, const double* values) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(values, MFT_ERR_ARG, "values is NULL");
+    MFT_REQUIRE(c->nvars > 0, MFT_ERR_STATE, "equations not set");
+    const int64_t total = c->n_bc ? c->bc_ptr[c->n_bc] : 0;
+    c->dir_values.assign(values, values + (size_t)total * c->nvars);
+    if (!c->bc_dirty && total > 0)
+      MFT_CUDA(cudaMemcpyAsync(c->d_dvals.p, c->dir_values.data(),
+                               c->dir_values.size() * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+mft_status mft_set_dirichlet_callback(mft_ctx* c, mft_dirichlet_fn fn, void* user) {
+  return guarded(c, [&] {
+    c->dir_fn = fn;
+    c->dir_user = user;
+  });
+}
+
+mft_status mft_set_sources(mft_ctx* c, int n_src, const int* kinds, const double* params) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(n_src >= 0 && n_src <= 8, MFT_ERR_ARG, "n_src out of range");
+    MFT_REQUIRE(n_src == 0 || (kinds && params), MFT_ERR_ARG, "NULL source arrays");
+    for (int k = 0; k < n_src; ++k)
+      MFT_REQUIRE(kinds[k] >= MFT_SRC_RV && kinds[k] <= MFT_SRC_HV_FLYER, MFT_ERR_ARG,
+                  "unknown source kind");
+    c->src_kind.assign(kinds, kinds + n_src);
+    c->src_par.assign(params, params + 4 * n_src);
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_set_precision(mft_ctx* c, int precision) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(precision == MFT_PREC_FP64 || precision == MFT_PREC_FP32, MFT_ERR_ARG,
+                "unknown precision");
+    c->precision = precision;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_rhs_device(mft_ctx* c, double* du, double* u, double t) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(du && u, MFT_ERR_ARG, "NULL device pointers");
+    set_device(c);
+    ensure_work(c);
+    const int64_t n = c->n;
+    const int V = c->nvars;
+    cudaStream_t s = c->stream;
+    launch_aos_from_soa(u, c->work_u.p, n, V, s);
+    float* u32 = nullptr;
+    if (c->precision == MFT_PREC_FP32) {
+      launch_aos_to_f32(c->work_u.p, c->work_u32.p, n * V, s);
+      u32 = c->work_u32.p;
+    }
+    Epilogue ep{};
+    ep.kind = kOutDu;
+    ep.out = c->work_du.p;
+    eval_rhs(c, c->work_u.p, u32, t, ep);
+    launch_soa_from_aos(c->work_du.p, du, n, V, s);
+    launch_soa_from_aos(c->work_u.p, u, n, V, s);
+    MFT_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+mft_status mft_rhs(mft_ctx* c, double* const* du, double* const* u, int nvars, double t) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(du && u && nvars == c->nvars, MFT_ERR_ARG, "bad state arrays or nvars");
+    set_device(c);
+    ensure_work(c);
+    const int64_t n = c->n;
+    const int V = c->nvars;
+    cudaStream_t s = c->stream;
+    for (int v = 0; v < V; ++v)
+      MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    launch_aos_from_soa(c->soa.p, c->work_u.p, n, V, s);
+    float* u32 = nullptr;
+    if (c->precision == MFT_PREC_FP32) {
+      launch_aos_to_f32(c->work_u.p, c->work_u32.p, n * V, s);
+      u32 = c->work_u32.p;
+    }
+    Epilogue ep{};
+    ep.kind = kOutDu;
+    ep.out = c->work_du.p;
+    eval_rhs(c, c->work_u.p, u32, t, ep);
+    launch_soa_from_aos(c->work_du.p, c->soa.p, n, V, s);
+    launch_soa_from_aos(c->work_u.p, c->soa2.p, n, V, s);
+    for (int v = 0; v < V; ++v) {
+      MFT_CUDA(cudaMemcpyAsync(du[v], c->soa.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+      MFT_CUDA(cudaMemcpyAsync(u[v], c->soa2.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    }
+    MFT_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+mft_status mft_set_state(mft_ctx* c, const double* const* u, int nvars, double t) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(u && nvars == c->nvars, MFT_ERR_ARG, "bad state arrays or nvars");
+    set_device(c);
+    ensure_work(c);
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    launch_aos_from_soa(c->soa.p, c->U[0].p, n, nvars, s);
+    MFT_CUDA(cudaStreamSynchronize(s));
+    c->t_state = t;
+    c->state_valid = true;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_get_state(mft_ctx* c, double* const* u, int nvars, double* t) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "no device state");
+    MFT_REQUIRE(u && nvars == c->nvars, MFT_ERR_ARG, "bad state arrays or nvars");
+    set_device(c);
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    launch_soa_from_aos(c->U[0].p, c->soa.p, n, nvars, s);
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    MFT_CUDA(cudaStreamSynchronize(s));
+    if (t) *t = c->t_state;
+  });
+}
+
+mft_status mft_history_init(mft_ctx* c, int approx_order) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(approx_order >= 0 && approx_order <= 7, MFT_ERR_ARG, "approx_order out of range");
+    set_device(c);
+    c->hist_order = approx_order;
+    c->hist_t.assign(approx_order + 1, 0.0);
+    const size_t nv = (size_t)c->n * c->nvars;
+    for (int k = 0; k < 8; ++k) {
+      if (k <= approx_order) {
+        c->hist[k].alloc(nv);
+        c->hist[k].zero(c->stream);
+      } else {
+        c->hist[k].release();
+      }
+    }
+    c->hist_w.alloc(16);
+    c->hist_head = 0;
+    c->success_iter = 0;
+    c->fsal_valid = false;
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+namespace {
+
+float* shadow(mft_ctx* c, int k) {
+  return c->precision == MFT_PREC_FP32 ? c->U32[k].p : nullptr;
+}
+
+void ssprk33_run(mft_ctx* c, double dt, int nsteps) {
+  ensure_work(c);
+  cudaStream_t s = c->stream;
+  const int64_t n = c->n;
+  const int V = c->nvars;
+  const bool f32 = c->precision == MFT_PREC_FP32;
+  if (!c->fsal_valid || c->fsal_dt != dt) {
+    // FSAL evaluation at the current state: k0 = f(u_n), stage 1 = u_n + dt*k0.
+    if (f32) launch_aos_to_f32(c->U[0].p, c->U32[0].p, n * V, s);
+    Epilogue ep{};
+    ep.kind = kStage1;
+    ep.dt = dt;
+    ep.out = c->U[1].p;
+    ep.out32 = shadow(c, 1);
+    eval_rhs(c, c->U[0].p, shadow(c, 0), c->t_state, ep);
+    if (c->hist_order >= 0 && c->success_iter == 0)
+      history_push(c, c->t_state, c->U[0].p, 0);
+    c->fsal_valid = true;
+    c->fsal_dt = dt;
+  }
+  const double t0 = c->t_state;
+  for (int k = 0; k < nsteps; ++k) {
+    const double t = t0 + k * dt;
+    Epilogue e2{};
+    e2.kind = kStage2;
+    e2.dt = dt;
+    e2.u_n = c->U[0].p;
+    e2.out = c->U[2].p;
+    e2.out32 = shadow(c, 2);
+    eval_rhs(c, c->U[1].p, shadow(c, 1), t + dt, e2);
+    Epilogue e3{};
+    e3.kind = kStage3;
+    e3.dt = dt;
+    e3.u_n = c->U[0].p;
+    e3.out = c->U[3].p;
+    e3.out32 = shadow(c, 3);
+    eval_rhs(c, c->U[2].p, shadow(c, 2), t + 0.5 * dt, e3);
+    const double tn = t0 + (k + 1) * dt;
+    Epilogue e1{};
+    e1.kind = kStage1;
+    e1.dt = dt;
+    e1.out = c->U[1].p;
+    e1.out32 = shadow(c, 1);
+    eval_rhs(c, c->U[3].p, shadow(c, 3), tn, e1);
+    std::swap(c->U[0].p, c->U[3].p);
+    std::swap(c->U32[0].p, c->U32[3].p);
+    c->t_state = tn;
+    if (c->hist_order >= 0) history_push(c, tn, c->U[0].p, c->success_iter + 1);
+  }
+}
+
+}  // namespace
+
+mft_status mft_ssprk33(mft_ctx* c, double dt, int nsteps, int use_graph) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "call mft_set_state first");
+    MFT_REQUIRE(nsteps >= 0, MFT_ERR_ARG, "nsteps < 0");
+    MFT_REQUIRE(dt > 0 && isfinite(dt), MFT_ERR_ARG, "dt must be positive and finite");
+    (void)use_graph;
+    set_device(c);
+    ssprk33_run(c, dt, nsteps);
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+mft_status mft_ssprk33_host(mft_ctx* c, double* const* u, int nvars, double* t, double dt,
+                            int nsteps) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(u && t && nvars == c->nvars, MFT_ERR_ARG, "bad state arrays");
+    MFT_REQUIRE(dt > 0 && isfinite(dt), MFT_ERR_ARG, "dt must be positive and finite");
+    set_device(c);
+    ensure_work(c);
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    // The pending first stage (FSAL) stays valid only if the caller hands back
+    // exactly the state this context holds at the same time.
+    bool keep = c->state_valid && c->fsal_valid && c->t_state == *t;
+    if (keep) {
+      launch_aos_from_soa(c->soa.p, c->work_u.p, n, nvars, s);
+      c->flag.alloc(1);
+      c->flag.zero(s);
+      launch_differs(c->work_u.p, c->U[0].p, n * nvars, c->flag.p, s);
+      int differs = 1;
+      MFT_CUDA(cudaMemcpyAsync(&differs, c->flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      MFT_CUDA(cudaStreamSynchronize(s));
+      if (differs) {
+        std::swap(c->work_u.p, c->U[0].p);
+        keep = false;
+      }
+    } else {
+      launch_aos_from_soa(c->soa.p, c->U[0].p, n, nvars, s);
+    }
+    c->t_state = *t;
+    c->state_valid = true;
+    if (!keep) c->fsal_valid = false;
+    ssprk33_run(c, dt, nsteps);
+    launch_soa_from_aos(c->U[0].p, c->soa.p, n, nvars, s);
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    MFT_CUDA(cudaStreamSynchronize(s));
+    *t = c->t_state;
+  });
+}
+
+mft_status mft_set_rv_state(mft_ctx* c, const double* const* approx_du, int nvars,
+                            int success_iter) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(nvars == c->nvars, MFT_ERR_ARG, "nvars differs from the equations");
+    MFT_REQUIRE(success_iter >= 0, MFT_ERR_ARG, "success_iter < 0");
+    set_device(c);
+    ensure_work(c);
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    if (approx_du) {
+      for (int v = 0; v < nvars; ++v)
+        MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, approx_du[v], n * sizeof(double),
+                                 cudaMemcpyHostToDevice, s));
+      launch_aos_from_soa(c->soa.p, c->approx_du.p, n, nvars, s);
+    }
+    c->success_iter = success_iter;
+    c->fsal_valid = false;
+    MFT_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+mft_status mft_get_viscosity(mft_ctx* c, double* eps) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(eps, MFT_ERR_ARG, "eps is NULL");
+    MFT_REQUIRE(c->eps.p, MFT_ERR_STATE, "no viscosity evaluated yet");
+    set_device(c);
+    MFT_CUDA(cudaMemcpyAsync(eps, c->eps.p, c->n * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,613 @@
+// Operator-apply kernels of the RBF-FD rhs! (FP64 form) for sm_103a.
+//
+// Pass structure of one rhs! evaluation (reference: Trixi.rhs!,
+// src/solvers/pointcloudsolver/rbfsolver.jl:397-428):
+//   bc_pass1   strong BCs on the boundary-node list (rbfsolver.jl:288-318)
+//   flux       F(u) per node (Euler flux in FP64 is issue-bound on this part,
+//              so it is evaluated once per node, not once per stencil entry)
+//   fwd        one sliced-ELL gather over the stencil: -sum_d D_d F_d, and, for the
+//              viscosity sources, t = D_d u and q = lap u (calc_fluxes!, :247-265)
+//   mean/lexmax  ode_mean / ode_maximum (src/auxiliary/mpi.jl:40-81)
+//   eps        update_upwind_visc! / update_residual_visc! / update_visc!
+//              (src/sources/hyperviscosity.jl:246-349), s = eps * t
+//   rev        transpose gather -sum_d D_d' s_d (and lap' q) over the reverse
+//              adjacency (hyperviscosity.jl:401-407, :121-134), BC pass 2 and the
+//              SSP-RK stage combination as epilogue.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mft_device.cuh"
+#include "mft_internal.cuh"
+
+namespace mft {
+
+namespace {
+
+using namespace dev;
+
+// ------------------------------------------------------------------ layout
+
+__global__ void k_aos_from_soa(const double* __restrict__ soa, double* __restrict__ aos,
+                               int64_t n, int V) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int v = 0; v < V; ++v) aos[i * V + v] = soa[(int64_t)v * n + i];
+}
+__global__ void k_soa_from_aos(const double* __restrict__ aos, double* __restrict__ soa,
+                               int64_t n, int V) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int v = 0; v < V; ++v) soa[(int64_t)v * n + i] = aos[i * V + v];
+}
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t count) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < count) b[i] = __double2float_rn(a[i]);
+}
+
+// ------------------------------------------------------------------ BC pass 1
+
+__global__ void k_bc_pass1(int64_t nb, const int32_t* __restrict__ bnode, int V, int eq, BcDev bc,
+                           double* __restrict__ u, float* __restrict__ u32) {
+  int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const int64_t i = bnode[b];
+  const int tag = bc.tag[i];
+  const int64_t slot = bc.slot[i];
+  if (tag == 1) {
+    for (int v = 0; v < V; ++v) u[i * V + v] = bc.dvalues[slot * V + v];
+  } else if (tag == 2 && eq == MFT_EQ_EULER2D) {
+    double uu[4] = {u[i * 4 + 0], u[i * 4 + 1], u[i * 4 + 2], u[i * 4 + 3]};
+    slip(bc.normal + 2 * slot, uu);
+    u[i * 4 + 1] = uu[1];
+    u[i * 4 + 2] = uu[2];
+  } else {
+    return;
+  }
+  if (u32)
+    for (int v = 0; v < V; ++v) u32[i * V + v] = __double2float_rn(u[i * V + v]);
+}
+
+// ------------------------------------------------------------------ flux
+
+__global__ void k_flux_euler(int64_t n, double g, const double* __restrict__ u,
+                             double* __restrict__ F) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2* ui = reinterpret_cast<const double2*>(u) + i * 2;
+  const double2 a = ui[0], b = ui[1];
+  double uu[4] = {a.x, a.y, b.x, b.y}, fx[4], fy[4];
+  euler_flux(g, uu, fx, fy);
+  double2* Fi = reinterpret_cast<double2*>(F) + i * 4;
+  Fi[0] = make_double2(fx[0], fx[1]);
+  Fi[1] = make_double2(fx[2], fx[3]);
+  Fi[2] = make_double2(fy[0], fy[1]);
+  Fi[3] = make_double2(fy[2], fy[3]);
+}
+
+// ------------------------------------------------------------------ forward gather
+
+// Euler (V = 4), FP64.  One node per thread; lane r of a warp owns row 32*s + r of
+// slice s and reads slot j at slice_off[s] + 32*j + r (coalesced weights/indices).
+// Per stencil entry: 64 B flux gather (+32 B state gather for t/q), 8 FP64 FMAs for
+// the flux divergence (6 when t is formed: d rho/dt reuses t).
+template <bool WT, bool WQ, int FLY>
+__global__ void __launch_bounds__(kBlock) k_fwd_euler_f64(FwdArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  const int32_t* __restrict__ col = a.ell.col;
+  const double* __restrict__ wxp = a.w[0];
+  const double* __restrict__ wyp = a.w[1];
+  const double* __restrict__ wlp = a.wl;
+  const double2* __restrict__ F2 = reinterpret_cast<const double2*>(a.F);
+  const double2* __restrict__ U2 = reinterpret_cast<const double2*>(a.u);
+  double f0 = 0, f1 = 0, f2 = 0, f3 = 0;                 // sum wx Fx + wy Fy
+  double tx0 = 0, tx1 = 0, tx2 = 0, tx3 = 0, ty0 = 0, ty1 = 0, ty2 = 0, ty3 = 0;
+  double q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+#pragma unroll 2
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(col + p);
+    const double wx = __ldg(wxp + p), wy = __ldg(wyp + p);
+    const double2 fa = __ldg(F2 + c * 4 + 0), fb = __ldg(F2 + c * 4 + 1);
+    const double2 fc = __ldg(F2 + c * 4 + 2), fd = __ldg(F2 + c * 4 + 3);
+    if (WT) {
+      // Fx[0] = rho v1 = u[1], Fy[0] = rho v2 = u[2]: the rho row of the flux
+      // divergence is tx1 + ty2, so it needs no FMAs of its own.
+      f1 = fma(wx, fa.y, f1); f1 = fma(wy, fc.y, f1);
+      f2 = fma(wx, fb.x, f2); f2 = fma(wy, fd.x, f2);
+      f3 = fma(wx, fb.y, f3); f3 = fma(wy, fd.y, f3);
+    } else {
+      f0 = fma(wx, fa.x, f0); f0 = fma(wy, fc.x, f0);
+      f1 = fma(wx, fa.y, f1); f1 = fma(wy, fc.y, f1);
+      f2 = fma(wx, fb.x, f2); f2 = fma(wy, fd.x, f2);
+      f3 = fma(wx, fb.y, f3); f3 = fma(wy, fd.y, f3);
+    }
+    if (WT || WQ || FLY) {
+      const double2 ua = __ldg(U2 + c * 2), ub = __ldg(U2 + c * 2 + 1);
+      if (WT) {
+        tx0 = fma(wx, ua.x, tx0); tx1 = fma(wx, ua.y, tx1); tx2 = fma(wx, ub.x, tx2); tx3 = fma(wx, ub.y, tx3);
+        ty0 = fma(wy, ua.x, ty0); ty1 = fma(wy, ua.y, ty1); ty2 = fma(wy, ub.x, ty2); ty3 = fma(wy, ub.y, ty3);
+      }
+      if (WQ || FLY) {
+        const double wl = __ldg(wlp + p);
+        q0 = fma(wl, ua.x, q0); q1 = fma(wl, ua.y, q1); q2 = fma(wl, ub.x, q2); q3 = fma(wl, ub.y, q3);
+      }
+    }
+  }
+  if (WT) f0 = tx1 + ty2;
+  double du[4] = {-f0, -f1, -f2, -f3};
+  if (FLY == 1) {
+    du[0] = fma(-a.hv_gamma, q0, du[0]); du[1] = fma(-a.hv_gamma, q1, du[1]);
+    du[2] = fma(-a.hv_gamma, q2, du[2]); du[3] = fma(-a.hv_gamma, q3, du[3]);
+  }
+  if (WT) {
+    double2* t2 = reinterpret_cast<double2*>(a.t) + i * 4;
+    t2[0] = make_double2(tx0, tx1); t2[1] = make_double2(tx2, tx3);
+    t2[2] = make_double2(ty0, ty1); t2[3] = make_double2(ty2, ty3);
+  }
+  if (WQ) {
+    double2* q2p = reinterpret_cast<double2*>(a.q) + i * 2;
+    q2p[0] = make_double2(q0, q1); q2p[1] = make_double2(q2, q3);
+  }
+  if (FLY == 2) {
+    double2* h2 = reinterpret_cast<double2*>(a.hvf) + i * 2;
+    h2[0] = make_double2(-a.hv_gamma * q0, -a.hv_gamma * q1);
+    h2[1] = make_double2(-a.hv_gamma * q2, -a.hv_gamma * q3);
+  }
+  if (a.final_epilogue) {
+    finish_node<4>(a.ep, i, du);
+  } else {
+    double2* d2 = reinterpret_cast<double2*>(a.du_p) + i * 2;
+    d2[0] = make_double2(du[0], du[1]);
+    d2[1] = make_double2(du[2], du[3]);
+  }
+}
+
+// Scalar advection (V = 1), FP64: flux a_d * u evaluated at the neighbour.
+template <bool WT, bool WQ, int FLY>
+__global__ void __launch_bounds__(kBlock) k_fwd_adv_f64(FwdArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  double f = 0, tx = 0, ty = 0, q = 0;
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(a.ell.col + p);
+    const double wx = __ldg(a.w[0] + p), wy = __ldg(a.w[1] + p);
+    const double uc = __ldg(a.u + c);
+    f = fma(wx, a.ax * uc, f);
+    f = fma(wy, a.ay * uc, f);
+    if (WT) { tx = fma(wx, uc, tx); ty = fma(wy, uc, ty); }
+    if (WQ || FLY) q = fma(__ldg(a.wl + p), uc, q);
+  }
+  double du[1] = {-f};
+  if (FLY == 1) du[0] = fma(-a.hv_gamma, q, du[0]);
+  if (WT) { a.t[i * 2] = tx; a.t[i * 2 + 1] = ty; }
+  if (WQ) a.q[i] = q;
+  if (FLY == 2) a.hvf[i] = -a.hv_gamma * q;
+  if (a.final_epilogue) finish_node<1>(a.ep, i, du);
+  else a.du_p[i] = du[0];
+}
+
+// ------------------------------------------------------------------ reductions
+
+template <int V>
+__device__ void block_sum(double* v) {
+  __shared__ double sh[V][kBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      double x = sh[k][0];
+      for (int w = 1; w < kBlock / 32; ++w) x += sh[k][w];
+      v[k] = x;
+    }
+  }
+}
+
+__device__ __forceinline__ int jl_isless(double a, double b) {
+  if (isnan(a)) return 0;
+  if (isnan(b)) return 1;
+  if (a < b) return 1;
+  if (a > b) return 0;
+  return signbit(a) && !signbit(b);
+}
+__device__ __forceinline__ int jl_isequal(double a, double b) {
+  if (isnan(a) || isnan(b)) return isnan(a) && isnan(b);
+  return a == b && signbit(a) == signbit(b);
+}
+template <int V>
+__device__ __forceinline__ int vec_isless(const double* a, const double* b) {
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    if (!jl_isequal(a[k], b[k])) return jl_isless(a[k], b[k]);
+  return 0;
+}
+// Base.max on vectors: max(a, b) = isless(b, a) ? a : b  (lexicographic).
+template <int V>
+__device__ __forceinline__ void vmax_into(double* a, const double* b) {
+  if (!vec_isless<V>(b, a)) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) a[k] = b[k];
+  }
+}
+__device__ __forceinline__ double jl_max(double a, double b) {
+  if (isnan(a) || isnan(b)) return a + b;
+  return jl_isless(a, b) ? b : a;
+}
+__device__ __forceinline__ double jl_min(double a, double b) {
+  if (isnan(a) || isnan(b)) return a + b;
+  return jl_isless(b, a) ? b : a;
+}
+
+// Sum of u per variable; the last block to finish sums the block partials in block
+// order (deterministic) and writes mean = sum / denom.
+template <int V>
+__global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __restrict__ u,
+                                                 double denom, double* partial,
+                                                 unsigned* counter, double* mean) {
+  double acc[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) acc[k] = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kBlock) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) acc[k] += u[i * V + k];
+  }
+  block_sum<V>(acc);
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = acc[k];
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x < V) {
+    __threadfence();
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(partial + b * V + threadIdx.x);
+    mean[threadIdx.x] = s / denom;
+  }
+  if (last && threadIdx.x == 0) *counter = 0u;
+}
+
+// ode_maximum(|u - mean|): lexicographic (max_mode 0) or per component (1); zero
+// entries become eps() (update_residual_visc!, hyperviscosity.jl:310-311).
+template <int V>
+__global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __restrict__ u,
+                                                   const double* __restrict__ mean, int max_mode,
+                                                   double* partial, unsigned* counter,
+                                                   double* norms) {
+  double m[V], best[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) { m[k] = mean[k]; best[k] = -1.0; }
+  bool have = false;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kBlock) {
+    double x[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) x[k] = fabs(dsub(u[i * V + k], m[k]));
+    if (!have) {
+#pragma unroll
+      for (int k = 0; k < V; ++k) best[k] = x[k];
+      have = true;
+    } else if (max_mode == 0) {
+      vmax_into<V>(best, x);
+    } else {
+#pragma unroll
+      for (int k = 0; k < V; ++k) best[k] = jl_max(best[k], x[k]);
+    }
+  }
+  // Entries of threads without nodes stay at -1 and never win (values are >= 0).
+  __shared__ double sh[kBlock][V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) sh[threadIdx.x][k] = best[k];
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      double* a = sh[threadIdx.x];
+      const double* b = sh[threadIdx.x + s];
+      if (max_mode == 0) vmax_into<V>(a, b);
+      else
+        for (int k = 0; k < V; ++k) a[k] = jl_max(a[k], b[k]);
+    }
+    __syncthreads();
+  }
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = sh[0][k];
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double b[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) b[k] = __ldcg(partial + k);
+    for (unsigned blk = 1; blk < gridDim.x; ++blk) {
+      double c[V];
+#pragma unroll
+      for (int k = 0; k < V; ++k) c[k] = __ldcg(partial + blk * V + k);
+      if (max_mode == 0) vmax_into<V>(b, c);
+      else
+        for (int k = 0; k < V; ++k) b[k] = jl_max(b[k], c[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < V; ++k) norms[k] = b[k] == 0.0 ? 2.220446049250313e-16 : b[k];
+    *counter = 0u;
+  }
+}
+
+// ------------------------------------------------------------------ viscosity
+
+template <int V>
+__global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  double eps_uw;
+  if (V == 4) {
+    const double rho = a.u[i * 4], m1 = a.u[i * 4 + 1], m2 = a.u[i * 4 + 2], en = a.u[i * 4 + 3];
+    const double v1 = ddiv(m1, rho), v2 = ddiv(m2, rho);
+    const double p = dmul(dsub(a.gamma, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
+    const double speed = sqrt(dadd(dmul(v1, v1), dmul(v2, v2)));
+    double c;
+    if (p < 0.0 || rho < 0.0) c = 0.0;
+    else c = sqrt(ddiv(dmul(a.gamma, p), rho));
+    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), dadd(speed, c));
+  } else {
+    const double an = sqrt(dadd(dmul(a.ax, a.ax), dmul(a.ay, a.ay)));
+    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), an);
+  }
+  double eps;
+  if (a.kind == MFT_SRC_RV) {
+    double mr = 0.0;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      double dp = a.du_p[i * V + v];
+      if (a.hvf) dp = dadd(dp, a.hvf[i * V + v]);
+      const double r = fabs(dsub(a.approx_du[i * V + v], dp));
+      const double qv = ddiv(r, a.norms[v]);
+      mr = v == 0 ? qv : jl_max(mr, qv);
+    }
+    const double eps_rv = dmul(dmul(dmul(0.5, a.c_rv), dmul(a.h, a.h)), mr);
+    if (isnan(eps_rv) || isinf(eps_rv) || a.success_iter == 0) {
+      eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16 : eps_uw;
+    } else {
+      eps = jl_min(eps_rv, eps_uw);
+    }
+  } else {
+    eps = eps_uw;
+  }
+  if (a.eps) a.eps[i] = eps;
+  if (a.t) {
+#pragma unroll
+    for (int k = 0; k < 2 * V; ++k) a.t[i * 2 * V + k] = dmul(eps, a.t[i * 2 * V + k]);
+  }
+  if (a.t32) {
+    const float e32 = __double2float_rn(eps);
+#pragma unroll
+    for (int k = 0; k < 2 * V; ++k) a.t32[i * 2 * V + k] = e32 * a.t32[i * 2 * V + k];
+  }
+}
+
+// ------------------------------------------------------------------ transpose gather
+
+// du_i = du_p_i - sum_{j: i in stencil(j)} (Dx[j,i] s_x[j] + Dy[j,i] s_y[j])
+//               - gamma * sum_j lap[j,i] q[j]
+// over the reverse adjacency (CSC column i), ascending j.
+template <int V, bool RV, bool LAP>
+__global__ void __launch_bounds__(kBlock) k_rev_f64(RevArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  double sx[V], sy[V], sl[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) { sx[v] = 0; sy[v] = 0; sl[v] = 0; }
+#pragma unroll 2
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(a.ell.col + p);
+    if (RV) {
+      const double wx = __ldg(a.w[0] + p), wy = __ldg(a.w[1] + p);
+      if (V == 4) {
+        const double2* S2 = reinterpret_cast<const double2*>(a.s) + c * 4;
+        const double2 xa = __ldg(S2), xb = __ldg(S2 + 1), ya = __ldg(S2 + 2), yb = __ldg(S2 + 3);
+        sx[0] = fma(wx, xa.x, sx[0]); sx[1] = fma(wx, xa.y, sx[1]);
+        sx[2] = fma(wx, xb.x, sx[2]); sx[3] = fma(wx, xb.y, sx[3]);
+        sy[0] = fma(wy, ya.x, sy[0]); sy[1] = fma(wy, ya.y, sy[1]);
+        sy[2] = fma(wy, yb.x, sy[2]); sy[3] = fma(wy, yb.y, sy[3]);
+      } else {
+        sx[0] = fma(wx, __ldg(a.s + c * 2), sx[0]);
+        sy[0] = fma(wy, __ldg(a.s + c * 2 + 1), sy[0]);
+      }
+    }
+    if (LAP) {
+      const double wl = __ldg(a.wl + p);
+#pragma unroll
+      for (int v = 0; v < V; ++v) sl[v] = fma(wl, __ldg(a.q + c * V + v), sl[v]);
+    }
+  }
+  double du[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    double d = a.du_p[i * V + v];
+    if (RV) d = (d - sx[v]) - sy[v];
+    if (LAP) d = fma(-a.hv_gamma, sl[v], d);
+    if (a.hvf) d = d + a.hvf[i * V + v];
+    du[v] = d;
+  }
+  if (a.final_epilogue) {
+    finish_node<V>(a.ep, i, du);
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v) a.du_p_out[i * V + v] = du[v];
+  }
+}
+
+// ------------------------------------------------------------------ history
+
+__global__ void k_history(int64_t count, int m, const double* __restrict__ w, const double* h0,
+                          const double* h1, const double* h2, const double* h3,
+                          const double* h4, const double* h5, const double* h6,
+                          const double* h7, double* __restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
+  // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
+  double acc = 0.0;
+  for (int k = 0; k < m; ++k) acc = dadd(acc, dmul(w[k], hs[k][i]));
+  out[i] = acc;
+}
+
+__global__ void k_differs(const double* __restrict__ a, const double* __restrict__ b,
+                          int64_t count, int* flag) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < count && __double_as_longlong(a[i]) != __double_as_longlong(b[i])) *flag = 1;
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+// ====================================================================== launchers
+
+void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s) {
+  if (n <= 0) return;
+  k_aos_from_soa<<<grid_for(n, 256), 256, 0, s>>>(soa, aos, n, V);
+  MFT_LAUNCH_CHECK();
+}
+void launch_soa_from_aos(const double* aos, double* soa, int64_t n, int V, cudaStream_t s) {
+  if (n <= 0) return;
+  k_soa_from_aos<<<grid_for(n, 256), 256, 0, s>>>(aos, soa, n, V);
+  MFT_LAUNCH_CHECK();
+}
+void launch_aos_to_f32(const double* aos, float* a32, int64_t count, cudaStream_t s) {
+  if (count <= 0) return;
+  k_to_f32<<<grid_for(count, 256), 256, 0, s>>>(aos, a32, count);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_bc_pass1(int64_t nb, const int32_t* bnode, int V, int eq, BcDev bc, double* u,
+                     float* u32, cudaStream_t s) {
+  if (nb <= 0) return;
+  k_bc_pass1<<<grid_for(nb, 128), 128, 0, s>>>(nb, bnode, V, eq, bc, u, u32);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_flux_f64(int64_t n, int eq, int V, double gamma, const double* u, double* F,
+                     cudaStream_t s) {
+  if (eq != MFT_EQ_EULER2D || n <= 0) return;
+  (void)V;
+  k_flux_euler<<<grid_for(n, 256), 256, 0, s>>>(n, gamma, u, F);
+  MFT_LAUNCH_CHECK();
+}
+
+template <int V>
+static void fwd_dispatch(const FwdArgs& a, cudaStream_t s) {
+  const unsigned g = grid_for(a.n, kBlock);
+  const bool wt = a.want_t != 0, wq = a.want_q != 0;
+#define MFT_FWD(WT, WQ, FLY)                                                       \
+  do {                                                                             \
+    if (V == 4) k_fwd_euler_f64<WT, WQ, FLY><<<g, kBlock, 0, s>>>(a);              \
+    else k_fwd_adv_f64<WT, WQ, FLY><<<g, kBlock, 0, s>>>(a);                       \
+  } while (0)
+  if (a.flyer == 0) {
+    if (wt && wq) MFT_FWD(true, true, 0);
+    else if (wt) MFT_FWD(true, false, 0);
+    else if (wq) MFT_FWD(false, true, 0);
+    else MFT_FWD(false, false, 0);
+  } else if (a.flyer == 1) {
+    if (wt) MFT_FWD(true, false, 1);
+    else MFT_FWD(false, false, 1);
+  } else {
+    if (wt) MFT_FWD(true, false, 2);
+    else MFT_FWD(false, false, 2);
+  }
+#undef MFT_FWD
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_fwd_f64(const FwdArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
+              "Flyer and Tominec hyperviscosity together are not supported");
+  if (a.V == 4) fwd_dispatch<4>(a, s);
+  else fwd_dispatch<1>(a, s);
+}
+
+void launch_mean(int64_t n, int V, const double* u, double denom, double* partial,
+                 unsigned* counter, double* mean, int nblocks, cudaStream_t s) {
+  if (V == 4) k_mean<4><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
+  else k_mean<1><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_lexmax(int64_t n, int V, const double* u, const double* mean, int max_mode,
+                   double* partial, unsigned* counter, double* norms, int nblocks,
+                   cudaStream_t s) {
+  if (V == 4)
+    k_lexmax<4><<<nblocks, kBlock, 0, s>>>(n, u, mean, max_mode, partial, counter, norms);
+  else
+    k_lexmax<1><<<nblocks, kBlock, 0, s>>>(n, u, mean, max_mode, partial, counter, norms);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_eps(const EpsArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  if (a.du_p32) {
+    launch_eps_f32(a, s);
+    return;
+  }
+  if (a.V == 4) k_eps<4><<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  else k_eps<1><<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_rev_f64(const RevArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const unsigned g = grid_for(a.n, kBlock);
+  if (a.V == 4) {
+    if (a.rv && a.lap) k_rev_f64<4, true, true><<<g, kBlock, 0, s>>>(a);
+    else if (a.rv) k_rev_f64<4, true, false><<<g, kBlock, 0, s>>>(a);
+    else if (a.lap) k_rev_f64<4, false, true><<<g, kBlock, 0, s>>>(a);
+    else k_rev_f64<4, false, false><<<g, kBlock, 0, s>>>(a);
+  } else {
+    if (a.rv && a.lap) k_rev_f64<1, true, true><<<g, kBlock, 0, s>>>(a);
+    else if (a.rv) k_rev_f64<1, true, false><<<g, kBlock, 0, s>>>(a);
+    else if (a.lap) k_rev_f64<1, false, true><<<g, kBlock, 0, s>>>(a);
+    else k_rev_f64<1, false, false><<<g, kBlock, 0, s>>>(a);
+  }
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s) {
+  if (count <= 0) return;
+  k_differs<<<grid_for(count, 256), 256, 0, s>>>(a, b, count, flag);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_history(int64_t count, int m, const double* w, const double* const* hist,
+                    double* approx_du, cudaStream_t s) {
+  if (count <= 0) return;
+  const double* h[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int k = 0; k < m && k < 8; ++k) h[k] = hist[k];
+  k_history<<<grid_for(count, 256), 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4],
+                                                  h[5], h[6], h[7], approx_du);
+  MFT_LAUNCH_CHECK();
+}
+
+}  // namespace mft

@@ -1,0 +1,283 @@
+// FP32-apply form of the rhs! gathers: FP32 weights (generated in FP64), FP32
+// states and FP32 accumulation in the operator apply; the SSP-RK stage combination
+// (finish_node) stays in FP64.  The Euler flux is cheap in FP32, so it is evaluated
+// at every stencil neighbour from the 16-byte FP32 state instead of being stored.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mft_device.cuh"
+#include "mft_internal.cuh"
+
+namespace mft {
+
+namespace {
+
+using namespace dev;
+
+__device__ __forceinline__ void euler_flux_f32(float gm1, float4 u, float* fx, float* fy) {
+  const float r = __frcp_rn(u.x);
+  const float v1 = u.y * r, v2 = u.z * r;
+  const float p = gm1 * (u.w - 0.5f * (u.y * v1 + u.z * v2));
+  const float ep = u.w + p;
+  fx[0] = u.y;
+  fx[1] = fmaf(u.y, v1, p);
+  fx[2] = u.y * v2;
+  fx[3] = ep * v1;
+  fy[0] = u.z;
+  fy[1] = u.z * v1;
+  fy[2] = fmaf(u.z, v2, p);
+  fy[3] = ep * v2;
+}
+
+template <bool WT, bool WQ, int FLY>
+__global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  const int32_t* __restrict__ col = a.ell.col;
+  const float* __restrict__ wxp = a.w32[0];
+  const float* __restrict__ wyp = a.w32[1];
+  const float* __restrict__ wlp = a.wl32;
+  const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
+  const float gm1 = (float)(a.gamma - 1.0);
+  float f[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+#pragma unroll 4
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int c = __ldg(col + p);
+    const float wx = __ldg(wxp + p), wy = __ldg(wyp + p);
+    const float4 uc = __ldg(U4 + c);
+    float fx[4], fy[4];
+    euler_flux_f32(gm1, uc, fx, fy);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v] = fmaf(wy, fy[v], fmaf(wx, fx[v], f[v]));
+    if (WT) {
+      tx[0] = fmaf(wx, uc.x, tx[0]); tx[1] = fmaf(wx, uc.y, tx[1]);
+      tx[2] = fmaf(wx, uc.z, tx[2]); tx[3] = fmaf(wx, uc.w, tx[3]);
+      ty[0] = fmaf(wy, uc.x, ty[0]); ty[1] = fmaf(wy, uc.y, ty[1]);
+      ty[2] = fmaf(wy, uc.z, ty[2]); ty[3] = fmaf(wy, uc.w, ty[3]);
+    }
+    if (WQ || FLY) {
+      const float wl = __ldg(wlp + p);
+      q[0] = fmaf(wl, uc.x, q[0]); q[1] = fmaf(wl, uc.y, q[1]);
+      q[2] = fmaf(wl, uc.z, q[2]); q[3] = fmaf(wl, uc.w, q[3]);
+    }
+  }
+  const float hg = (float)a.hv_gamma;
+  float du[4] = {-f[0], -f[1], -f[2], -f[3]};
+  if (FLY == 1)
+    for (int v = 0; v < 4; ++v) du[v] = fmaf(-hg, q[v], du[v]);
+  if (WT) {
+    float4* t4 = reinterpret_cast<float4*>(a.t32) + i * 2;
+    t4[0] = make_float4(tx[0], tx[1], tx[2], tx[3]);
+    t4[1] = make_float4(ty[0], ty[1], ty[2], ty[3]);
+  }
+  if (WQ) reinterpret_cast<float4*>(a.q32)[i] = make_float4(q[0], q[1], q[2], q[3]);
+  if (FLY == 2)
+    for (int v = 0; v < 4; ++v) a.hvf[i * 4 + v] = (double)(-hg * q[v]);
+  if (a.final_epilogue) {
+    double d[4] = {du[0], du[1], du[2], du[3]};
+    finish_node<4>(a.ep, i, d);
+  } else {
+    reinterpret_cast<float4*>(a.du_p32)[i] = make_float4(du[0], du[1], du[2], du[3]);
+  }
+}
+
+template <bool WT, bool WQ, int FLY>
+__global__ void __launch_bounds__(kBlock) k_fwd_adv_f32(FwdArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  const float ax = (float)a.ax, ay = (float)a.ay;
+  float f = 0, tx = 0, ty = 0, q = 0;
+#pragma unroll 4
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int c = __ldg(a.ell.col + p);
+    const float wx = __ldg(a.w32[0] + p), wy = __ldg(a.w32[1] + p);
+    const float uc = __ldg(a.u32 + c);
+    f = fmaf(wy, ay * uc, fmaf(wx, ax * uc, f));
+    if (WT) { tx = fmaf(wx, uc, tx); ty = fmaf(wy, uc, ty); }
+    if (WQ || FLY) q = fmaf(__ldg(a.wl32 + p), uc, q);
+  }
+  const float hg = (float)a.hv_gamma;
+  float du = -f;
+  if (FLY == 1) du = fmaf(-hg, q, du);
+  if (WT) { a.t32[i * 2] = tx; a.t32[i * 2 + 1] = ty; }
+  if (WQ) a.q32[i] = q;
+  if (FLY == 2) a.hvf[i] = (double)(-hg * q);
+  if (a.final_epilogue) {
+    double d[1] = {du};
+    finish_node<1>(a.ep, i, d);
+  } else {
+    a.du_p32[i] = du;
+  }
+}
+
+// update_upwind_visc! / update_residual_visc! / update_visc! in FP32
+// (src/sources/hyperviscosity.jl:246-349); approx_du and the norms come from the
+// FP64 history and reductions.
+template <int V>
+__global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float h = (float)a.h;
+  float eps_uw;
+  if (V == 4) {
+    const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
+    const double2 ub = reinterpret_cast<const double2*>(a.u)[i * 2 + 1];
+    const float rho = (float)ua.x, m1 = (float)ua.y, m2 = (float)ub.x, en = (float)ub.y;
+    const float r = __frcp_rn(rho);
+    const float v1 = m1 * r, v2 = m2 * r;
+    const float p = (float)(a.gamma - 1.0) * (en - 0.5f * (m1 * v1 + m2 * v2));
+    const float speed = sqrtf(v1 * v1 + v2 * v2);
+    const float c = (p < 0.0f || rho < 0.0f) ? 0.0f : sqrtf((float)a.gamma * p * r);
+    eps_uw = (float)a.c_uw * 0.5f * h * (speed + c);
+  } else {
+    eps_uw = (float)a.c_uw * 0.5f * h * (float)sqrt(a.ax * a.ax + a.ay * a.ay);
+  }
+  float eps;
+  if (a.kind == MFT_SRC_RV) {
+    float mr = 0.0f;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      float dp = a.du_p32[i * V + v];
+      if (a.hvf) dp += (float)a.hvf[i * V + v];
+      const float r = fabsf((float)a.approx_du[i * V + v] - dp);
+      const float qv = r / (float)a.norms[v];
+      mr = v == 0 ? qv : fmaxf(mr, qv);
+      if (isnan(qv)) mr = qv;
+    }
+    const float eps_rv = 0.5f * (float)a.c_rv * h * h * mr;
+    if (isnan(eps_rv) || isinf(eps_rv) || a.success_iter == 0)
+      eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16f : eps_uw;
+    else
+      eps = fminf(eps_rv, eps_uw);
+  } else {
+    eps = eps_uw;
+  }
+  if (a.eps) a.eps[i] = (double)eps;
+#pragma unroll
+  for (int k = 0; k < 2 * V; ++k) a.t32[i * 2 * V + k] *= eps;
+}
+
+template <int V, bool RV, bool LAP>
+__global__ void __launch_bounds__(kBlock) k_rev_f32(RevArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  float sx[V], sy[V], sl[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) { sx[v] = 0.f; sy[v] = 0.f; sl[v] = 0.f; }
+#pragma unroll 4
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int c = __ldg(a.ell.col + p);
+    if (RV) {
+      const float wx = __ldg(a.w32[0] + p), wy = __ldg(a.w32[1] + p);
+      if (V == 4) {
+        const float4* S4 = reinterpret_cast<const float4*>(a.s32) + (int64_t)c * 2;
+        const float4 xs = __ldg(S4), ys = __ldg(S4 + 1);
+        sx[0] = fmaf(wx, xs.x, sx[0]); sx[1] = fmaf(wx, xs.y, sx[1]);
+        sx[2] = fmaf(wx, xs.z, sx[2]); sx[3] = fmaf(wx, xs.w, sx[3]);
+        sy[0] = fmaf(wy, ys.x, sy[0]); sy[1] = fmaf(wy, ys.y, sy[1]);
+        sy[2] = fmaf(wy, ys.z, sy[2]); sy[3] = fmaf(wy, ys.w, sy[3]);
+      } else {
+        const float2 s2 = __ldg(reinterpret_cast<const float2*>(a.s32) + c);
+        sx[0] = fmaf(wx, s2.x, sx[0]);
+        sy[0] = fmaf(wy, s2.y, sy[0]);
+      }
+    }
+    if (LAP) {
+      const float wl = __ldg(a.wl32 + p);
+      if (V == 4) {
+        const float4 qq = __ldg(reinterpret_cast<const float4*>(a.q32) + c);
+        sl[0] = fmaf(wl, qq.x, sl[0]); sl[1] = fmaf(wl, qq.y, sl[1]);
+        sl[2] = fmaf(wl, qq.z, sl[2]); sl[3] = fmaf(wl, qq.w, sl[3]);
+      } else {
+        sl[0] = fmaf(wl, __ldg(a.q32 + c), sl[0]);
+      }
+    }
+  }
+  const float hg = (float)a.hv_gamma;
+  float du[V];
+  const float* dp32 = a.du_p32;
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    float d = dp32[i * V + v];
+    if (RV) d = (d - sx[v]) - sy[v];
+    if (LAP) d = fmaf(-hg, sl[v], d);
+    if (a.hvf) d += (float)a.hvf[i * V + v];
+    du[v] = d;
+  }
+  if (a.final_epilogue) {
+    double d[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) d[v] = du[v];
+    finish_node<V>(a.ep, i, d);
+  } else {
+    float* out = a.du_p_out32;
+#pragma unroll
+    for (int v = 0; v < V; ++v) out[i * V + v] = du[v];
+  }
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+void launch_fwd_f32(const FwdArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
+              "Flyer and Tominec hyperviscosity together are not supported");
+  const unsigned g = grid_for(a.n, kBlock);
+  const bool wt = a.want_t != 0, wq = a.want_q != 0;
+#define MFT_FWD32(WT, WQ, FLY)                                              \
+  do {                                                                      \
+    if (a.V == 4) k_fwd_euler_f32<WT, WQ, FLY><<<g, kBlock, 0, s>>>(a);     \
+    else k_fwd_adv_f32<WT, WQ, FLY><<<g, kBlock, 0, s>>>(a);                \
+  } while (0)
+  if (a.flyer == 0) {
+    if (wt && wq) MFT_FWD32(true, true, 0);
+    else if (wt) MFT_FWD32(true, false, 0);
+    else if (wq) MFT_FWD32(false, true, 0);
+    else MFT_FWD32(false, false, 0);
+  } else if (a.flyer == 1) {
+    if (wt) MFT_FWD32(true, false, 1);
+    else MFT_FWD32(false, false, 1);
+  } else {
+    if (wt) MFT_FWD32(true, false, 2);
+    else MFT_FWD32(false, false, 2);
+  }
+#undef MFT_FWD32
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_eps_f32(const EpsArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  if (a.V == 4) k_eps_f32<4><<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  else k_eps_f32<1><<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_rev_f32(const RevArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const unsigned g = grid_for(a.n, kBlock);
+  if (a.V == 4) {
+    if (a.rv && a.lap) k_rev_f32<4, true, true><<<g, kBlock, 0, s>>>(a);
+    else if (a.rv) k_rev_f32<4, true, false><<<g, kBlock, 0, s>>>(a);
+    else if (a.lap) k_rev_f32<4, false, true><<<g, kBlock, 0, s>>>(a);
+    else k_rev_f32<4, false, false><<<g, kBlock, 0, s>>>(a);
+  } else {
+    if (a.rv && a.lap) k_rev_f32<1, true, true><<<g, kBlock, 0, s>>>(a);
+    else if (a.rv) k_rev_f32<1, true, false><<<g, kBlock, 0, s>>>(a);
+    else if (a.lap) k_rev_f32<1, false, true><<<g, kBlock, 0, s>>>(a);
+    else k_rev_f32<1, false, false><<<g, kBlock, 0, s>>>(a);
+  }
+  MFT_LAUNCH_CHECK();
+}
+
+}  // namespace mft

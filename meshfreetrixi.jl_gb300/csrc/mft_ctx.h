@@ -1,0 +1,121 @@
+// Context object behind the opaque mft_ctx handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "mft_internal.cuh"
+
+// Operator value slots: 0..2 gradient components, 3 lap (sum of pure 2nd
+// derivatives), 4 ready hyperviscosity operator.
+constexpr int kSlotLap = 3;
+constexpr int kSlotHv = 4;
+constexpr int kSlots = 5;
+
+struct mft_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // geometry
+  int dim = 0;
+  int64_t n = 0;
+  std::vector<double> xyz;
+  bool periodic = false;
+  double period[3] = {0, 0, 0};
+  mft::DBuf<double> d_xyz;
+
+  // stencils in caller order (centre first)
+  std::vector<int64_t> st_rp;
+  std::vector<int32_t> st_ci;
+  bool have_stencils = false;
+
+  // operator pattern: CSR rows with ascending columns, its CSC view, and maps
+  bool have_pattern = false;
+  std::vector<int64_t> rp;
+  std::vector<int32_t> ci;
+  std::vector<int64_t> cp;
+  std::vector<int32_t> ri;
+  std::vector<int64_t> csc2csr;  // CSC entry -> CSR entry
+  std::vector<int64_t> st2csr;   // stencil entry -> CSR entry (when built from stencils)
+  std::vector<double> val[kSlots];
+  bool have_val[kSlots] = {false, false, false, false, false};
+  bool dev_dirty = true;
+  mft::EllBuf fwd, rev;
+  mft::DBuf<int64_t> fwd_pos, rev_pos;  // CSR entry -> ELL element
+  mft::DBuf<double> fw[kSlots], rw[kSlots];
+  mft::DBuf<float> fw32[kSlots], rw32[kSlots];
+
+  // physics
+  int eq = -1;
+  int nvars = 0;
+  double gamma = 1.4;
+  double adv[3] = {0, 0, 0};
+
+  // boundary conditions
+  int n_bc = 0;
+  std::vector<int> bc_kind;
+  std::vector<int64_t> bc_ptr;
+  std::vector<int32_t> bc_idx;
+  std::vector<double> bc_normal;
+  std::vector<double> dir_values;
+  int64_t nb = 0;  // boundary nodes with an active BC
+  mft::DBuf<int8_t> d_tag;
+  mft::DBuf<int32_t> d_slot;
+  mft::DBuf<double> d_normal;
+  mft::DBuf<double> d_dvals;
+  mft::DBuf<int32_t> d_bnode;
+  bool bc_dirty = true;
+  mft_dirichlet_fn dir_fn = nullptr;
+  void* dir_user = nullptr;
+  std::vector<double> dir_scratch;
+
+  // sources
+  std::vector<int> src_kind;
+  std::vector<double> src_par;
+  int precision = MFT_PREC_FP64;
+
+  // work buffers (AoS n x V unless noted)
+  mft::DBuf<double> U[4];  // u_n, stage 1, stage 2, stage 3
+  mft::DBuf<float> U32[4];
+  mft::DBuf<double> F, du_p, du_p2, t, q, hvf, eps, approx_du, soa, soa2, work_u, work_du;
+  mft::DBuf<float> du_p32, du_p2_32, t32, q32, work_u32;
+  mft::DBuf<double> red_partial, mean, norms;
+  mft::DBuf<unsigned> red_counter;
+  mft::DBuf<int> flag;
+  int red_blocks = 0;
+
+  // time integration state
+  double t_state = 0.0;
+  bool state_valid = false;
+  bool fsal_valid = false;
+  double fsal_dt = 0.0;
+
+  // history ring (HistoryCallback)
+  int hist_order = -1;
+  std::vector<double> hist_t;
+  mft::DBuf<double> hist[8];
+  int hist_head = 0;
+  int success_iter = 0;
+  mft::DBuf<double> hist_w;
+};
+
+namespace mft {
+// Builds (if needed) the device ELL layouts and operator values.
+void ensure_device_ops(mft_ctx* c);
+// One rhs! evaluation on the AoS state `us` (device), with the given epilogue.
+void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_in);
+// Work-buffer sizing for the current problem.
+void ensure_work(mft_ctx* c);
+// Pattern from stencils (caller order, centre first).
+void pattern_from_stencils(mft_ctx* c);
+// Reverse CSC view + ELL/maps rebuild flags after the CSR pattern is set.
+void finish_pattern(mft_ctx* c);
+// KNN and weights (mft_knn.cu, mft_weights.cu)
+void knn_device(mft_ctx* c, int k, std::vector<int32_t>& idx, std::vector<double>* dist,
+                double* dx_min, double* dx_avg);
+void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
+                    std::vector<double>& w_out, double* max_resid);
+}  // namespace mft

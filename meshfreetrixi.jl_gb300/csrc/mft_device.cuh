@@ -1,0 +1,101 @@
+// Device helpers shared by the FP64 and FP32 apply kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mft_internal.cuh"
+
+namespace mft {
+namespace dev {
+
+constexpr int kBlock = 128;
+
+static __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+static __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+static __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+static __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Textbook Euler flux (Trixi's `flux(u, orientation, ::CompressibleEulerEquations2D)`),
+// each operation rounded separately.
+static __device__ __forceinline__ void euler_flux(double g, const double* uu, double* fx, double* fy) {
+  const double rho = uu[0], m1 = uu[1], m2 = uu[2], en = uu[3];
+  const double v1 = ddiv(m1, rho), v2 = ddiv(m2, rho);
+  const double p = dmul(dsub(g, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
+  fx[0] = m1;
+  fx[1] = dadd(dmul(m1, v1), p);
+  fx[2] = dmul(m1, v2);
+  fx[3] = dmul(dadd(en, p), v1);
+  fy[0] = m2;
+  fy[1] = dmul(m2, v1);
+  fy[2] = dadd(dmul(m2, v2), p);
+  fy[3] = dmul(dadd(en, p), v2);
+}
+
+// apply_slip_velocity (src/equations/PointCloudBCs.jl:15-21) with the normal
+// normalised as boundary_condition_slip_wall does (:87-106).
+static __device__ __forceinline__ void slip(const double* nrm, double* uu) {
+  const double n1r = nrm[0], n2r = nrm[1];
+  const double nn = sqrt(dadd(dmul(n1r, n1r), dmul(n2r, n2r)));
+  const double n1 = ddiv(n1r, nn), n2 = ddiv(n2r, nn);
+  const double vn = dadd(dmul(uu[1], n1), dmul(uu[2], n2));
+  const double s1 = dsub(uu[1], dmul(vn, n1));
+  const double s2 = dsub(uu[2], dmul(vn, n2));
+  uu[1] = s1;
+  uu[2] = s2;
+}
+
+// BC pass 2 on du (and u at slip walls), then the stage epilogue.
+template <int V>
+static __device__ __forceinline__ void finish_node(const Epilogue& ep, int64_t i, double* du) {
+  double us[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) us[v] = ep.u_s[i * V + v];
+  if (ep.has_bc) {
+    const int tag = ep.bc.tag[i];
+    if (tag == 1) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) du[v] = 0.0;
+    } else if (tag == 2 && V == 4) {
+      du[1] = 0.0;
+      du[2] = 0.0;
+      slip(ep.bc.normal + 2 * (int64_t)ep.bc.slot[i], us);
+      ep.u_s[i * V + 1] = us[1];
+      ep.u_s[i * V + 2] = us[2];
+    }
+  }
+  double o[V];
+  switch (ep.kind) {
+    case kOutDu:
+#pragma unroll
+      for (int v = 0; v < V; ++v) o[v] = du[v];
+      break;
+    case kStage1:
+#pragma unroll
+      for (int v = 0; v < V; ++v) o[v] = dadd(us[v], dmul(ep.dt, du[v]));
+      break;
+    case kStage2:
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const double un = ep.u_n[i * V + v];
+        o[v] = ddiv(dadd(dadd(dmul(3.0, un), us[v]), dmul(ep.dt, du[v])), 4.0);
+      }
+      break;
+    default:
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const double un = ep.u_n[i * V + v];
+        o[v] = ddiv(dadd(dadd(un, dmul(2.0, us[v])), dmul(2.0 * ep.dt, du[v])), 3.0);
+      }
+      break;
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) ep.out[i * V + v] = o[v];
+  if (ep.out32) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) ep.out32[i * V + v] = __double2float_rn(o[v]);
+  }
+}
+
+}  // namespace dev
+}  // namespace mft

@@ -1,0 +1,220 @@
+// Internal declarations shared by the translation units of libmeshfree_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "meshfree_gb300.h"
+
+namespace mft {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define MFT_CUDA(call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      throw ::mft::Error(MFT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define MFT_REQUIRE(cond, code, msg)                \
+  do {                                              \
+    if (!(cond)) throw ::mft::Error((code), (msg)); \
+  } while (0)
+
+#define MFT_LAUNCH_CHECK() MFT_CUDA(cudaGetLastError())
+
+// Owning device buffer (cudaMalloc / cudaFree).
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (p && count == n) return;
+    release();
+    if (count) {
+      cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+      if (e != cudaSuccess) {
+        p = nullptr;
+        throw Error(MFT_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      }
+      n = count;
+    }
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) MFT_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+  void zero(cudaStream_t s) {
+    if (n) MFT_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+};
+
+// Sliced ELL of a square sparse operator pattern: rows grouped in slices of 32
+// (one warp), each slice padded to its longest row, slot-major inside a slice so
+// that lane r of a warp reads element slice_off + slot*32 + r (coalesced).
+constexpr int kSlice = 32;
+
+struct EllView {
+  int64_t n;
+  const int64_t* slice_off;
+  const int32_t* row_len;
+  const int32_t* col;
+};
+
+struct EllBuf {
+  int64_t n = 0, n_elems = 0;
+  int max_len = 0;
+  DBuf<int64_t> slice_off;
+  DBuf<int32_t> row_len;
+  DBuf<int32_t> col;
+  EllView view() const { return EllView{n, slice_off.p, row_len.p, col.p}; }
+};
+
+// Host description of the boundary conditions, flattened per node for kernels.
+struct BcDev {
+  const int8_t* tag;      // n: 0 none, 1 Dirichlet, 2 slip wall
+  const int32_t* slot;    // n: index into the per-boundary-node tables
+  const double* normal;   // n_bnodes x 2 (raw outward normal, normalised in-kernel)
+  const double* dvalues;  // n_bnodes x nvars (Dirichlet values of the current stage)
+};
+
+// Stage epilogue of the fused kernels (SSP-RK3 in Shu-Osher form, FSAL).
+enum StageKind : int {
+  kOutDu = 0,   // write du (rhs! output)
+  kStage1 = 1,  // u_out = u_s + dt*du
+  kStage2 = 2,  // u_out = ((3*u_n + u_s) + dt*du) / 4
+  kStage3 = 3   // u_out = ((u_n + 2*u_s) + (2*dt)*du) / 3
+};
+
+struct Epilogue {
+  int kind;
+  double dt;
+  const double* u_n;  // n x V (AoS) step-start state (stages 2, 3)
+  double* u_s;        // n x V (AoS) stage state, mutated at slip nodes by BC pass 2
+  double* out;        // n x V (AoS): du (kOutDu) or next stage state
+  float* out32;       // optional FP32 shadow of the next stage state
+  BcDev bc;
+  int has_bc;
+};
+
+// ------------------------------------------------------------------ launchers
+// (implemented in mft_apply.cu; all enqueue on `s` and return after launch)
+
+void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s);
+void launch_soa_from_aos(const double* aos, double* soa, int64_t n, int V, cudaStream_t s);
+void launch_aos_to_f32(const double* aos, float* a32, int64_t count, cudaStream_t s);
+
+// BC pass 1 over the boundary-node list: Dirichlet u = g, slip wall u = slip(u).
+void launch_bc_pass1(int64_t nb, const int32_t* bnode, int V, int eq, BcDev bc, double* u,
+                     float* u32, cudaStream_t s);
+
+// Flux precompute F(u) (Euler: n x 8) and optional block partial sums of u.
+void launch_flux_f64(int64_t n, int eq, int V, double gamma, const double* u, double* F,
+                     cudaStream_t s);
+
+struct FwdArgs {
+  int64_t n;
+  EllView ell;
+  const double* w[3];   // grad components (x, y)
+  const double* wl;     // lap (Tominec) or H (Flyer) weights, or null
+  const float* w32[3];
+  const float* wl32;
+  const double* F;      // n x 2V fluxes (Euler FP64)
+  const double* u;      // n x V state (FP64)
+  const float* u32;     // n x V state (FP32 path)
+  int eq, V;
+  double gamma, ax, ay;
+  double hv_gamma;      // Flyer: du += -gamma * H u
+  int want_t;           // write t = D u (n x 2V)
+  int want_q;           // write q = lap u (n x V) (Tominec)
+  int flyer;            // Flyer H in wl: 0 none, 1 add into du_p, 2 write hvf separately
+  double* du_p;         // n x V partial du (flux [+ Flyer])
+  double* t;            // n x 2V
+  double* q;            // n x V
+  double* hvf;          // n x V
+  float* t32;
+  float* q32;
+  float* du_p32;
+  int final_epilogue;   // 1: du is final here, apply BC2 + epilogue instead of writing du_p
+  Epilogue ep;
+};
+void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
+void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
+
+// Reductions for the residual viscosity normalisation (last-block-done pattern).
+void launch_mean(int64_t n, int V, const double* u, double denom, double* partial,
+                 unsigned* counter, double* mean, int nblocks, cudaStream_t s);
+void launch_lexmax(int64_t n, int V, const double* u, const double* mean, int max_mode,
+                   double* partial, unsigned* counter, double* norms, int nblocks,
+                   cudaStream_t s);
+
+struct EpsArgs {
+  int64_t n;
+  int eq, V, kind;  // kind: MFT_SRC_RV or MFT_SRC_UPWIND
+  double gamma, ax, ay, c_rv, c_uw, h;
+  int success_iter;
+  const double* u;
+  const double* du_p;
+  const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)
+  const double* hvf;       // added to du_p when the Flyer term precedes RV (else null)
+  const double* approx_du; // n x V
+  const double* norms;     // V
+  double* t;               // n x 2V, scaled in place to eps*t
+  double* eps;             // n (diagnostic copy)
+  float* t32;              // FP32 path: scaled in place
+};
+void launch_eps(const EpsArgs& a, cudaStream_t s);
+void launch_eps_f32(const EpsArgs& a, cudaStream_t s);
+
+struct RevArgs {
+  int64_t n;
+  EllView ell;
+  const double* w[3];
+  const double* wl;
+  const float* w32[3];
+  const float* wl32;
+  int V;
+  int rv;             // gather s = eps*D u over the reverse adjacency
+  int lap;            // gather q = lap u over the reverse adjacency (Tominec)
+  double hv_gamma;
+  const double* s;    // n x 2V
+  const double* q;    // n x V
+  const float* s32;
+  const float* q32;
+  const double* du_p; // n x V
+  const float* du_p32;
+  const double* hvf;  // n x V Flyer term added after RV (or null)
+  int final_epilogue; // 0: write du_p_out (intermediate), 1: BC2 + epilogue
+  double* du_p_out;
+  float* du_p_out32;
+  Epilogue ep;
+};
+void launch_rev_f64(const RevArgs& a, cudaStream_t s);
+void launch_rev_f32(const RevArgs& a, cudaStream_t s);
+
+// Sets *flag to 1 when a and b differ in any of `count` doubles (bitwise).
+void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s);
+
+// approx_du = sum_i w_i * hist_i (history ring, FP64) and push of the newest state.
+void launch_history(int64_t count, int m, const double* w, const double* const* hist,
+                    double* approx_du, cudaStream_t s);
+
+}  // namespace mft

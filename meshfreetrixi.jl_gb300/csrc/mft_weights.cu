@@ -1,0 +1,572 @@
+// K2: batched FP64 polyharmonic-spline + polynomial RBF-FD weights.
+//
+// Restates the per-node loop of compute_flux_operator
+// (src/solvers/pointcloudsolver/compute_operators.jl:409-453 and :549-594):
+//   shift_stencil (:225-246)  X^_j = (X_j - X_centre) * s,  s_d = 1/max_j |dX_jd|
+//   M = [R P; P' 0] upper (interpolation_block :265-267), R_ij = |X^_i - X^_j|^p,
+//   P_im = monomial_m(X^_i)
+//   RHS: d^k/dx_d^k of |x - X^_j|^p at the centre (mirror_stencil :248-263 with the
+//   centre entry at (eps,...,eps)), monomial derivatives at the origin
+//   w = M \ rhs by Bunch-Kaufman (LAPACK dsytf2 + dsytrs, upper), weights s_d^k w.
+//
+// One warp per system, the system in shared memory, one persistent launch over all
+// nodes with a work counter; systems are taken largest first so that uneven stencil
+// sizes (interior vs boundary, 2D vs 3D) balance across warps.  Every matrix element
+// sees the same sequence of separately rounded operations as in the CPU
+// restatement (updates are element-independent and the solve's dot products use a
+// fixed 32-way strided partial-sum order), so the weights are bit-identical to it.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "mft_ctx.h"
+
+namespace mft {
+
+namespace {
+
+constexpr int kWarpsPerBlock = 2;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct WArgs {
+  int dim, npoly, rbf_pow, order, nmax, kmax;
+  int periodic;
+  double period[3];
+  int64_t nsys;
+  const int64_t* order_list;  // node ids, largest stencil first
+  const int64_t* rowptr;
+  const int32_t* cols;
+  const double* xyz;
+  int mono[128][3];
+  double* w_out;  // nnz x dim (stencil order)
+  double* resid;  // optional per node
+  int* bad;       // smallest node index with a zero pivot, or INT_MAX
+  unsigned long long* next;
+};
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+__device__ double pow_int(double x, int k) {
+  if (k < 0) {
+    double r = 1.0;
+    for (int i = 0; i < -k; ++i) r = dmul(r, x);
+    return ddiv(1.0, r);
+  }
+  double r = 1.0;
+  for (int i = 0; i < k; ++i) r = dmul(r, x);
+  return r;
+}
+
+__device__ double fact(int k) {
+  double r = 1.0;
+  for (int i = 2; i <= k; ++i) r = dmul(r, (double)i);
+  return r;
+}
+
+// d^k/dx_d^k of r^p (Faa di Bruno on s^(p/2), s = |x|^2); same operation order as
+// the CPU restatement.
+__device__ double phs_deriv(int p, int k, double xd, double r) {
+  if (k == 0) return pow_int(r, p);
+  double sum = 0.0;
+  for (int j = 0; 2 * j <= k; ++j) {
+    const int m = k - j;
+    double cm = 1.0;
+    for (int i = 0; i < m; ++i) cm = dmul(cm, dsub(dmul(0.5, (double)p), (double)i));
+    if (cm == 0.0) continue;
+    const double cc = ddiv(fact(k), dmul(fact(j), fact(k - 2 * j)));
+    const double term =
+        dmul(dmul(dmul(cc, pow_int(dmul(2.0, xd), k - 2 * j)), cm), pow_int(r, p - 2 * m));
+    sum = dadd(sum, term);
+  }
+  return sum;
+}
+
+__device__ __forceinline__ double min_image(double d, double L) {
+  if (d > 0.5 * L) return dsub(d, L);
+  if (d < -0.5 * L) return dadd(d, L);
+  return d;
+}
+
+// first index of the largest |x| among lanes' candidates (value, index)
+__device__ __forceinline__ void warp_argmax(double& v, int& i) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(kFull, v, o);
+    const int i2 = __shfl_xor_sync(kFull, i, o);
+    if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+  }
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+// Triangular index t -> (i, j) with 0 <= i <= j: t = j(j+1)/2 + i.
+__device__ __forceinline__ void tri_ij(int t, int& i, int& j) {
+  int jj = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while ((jj + 1) * (jj + 2) / 2 <= t) ++jj;
+  while (jj * (jj + 1) / 2 > t) --jj;
+  j = jj;
+  i = t - jj * (jj + 1) / 2;
+}
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int nmax = a.nmax;
+  // per-warp shared layout: A[nmax*nmax], B[nmax*3], X[kmax*3], aux[nmax] (ints)
+  const size_t per = (size_t)nmax * nmax + (size_t)nmax * 3 + (size_t)a.kmax * 3 + nmax;
+  double* A = smem + per * wib;
+  double* B = A + (size_t)nmax * nmax;
+  double* X = B + (size_t)nmax * 3;
+  int* ipiv = reinterpret_cast<int*>(X + (size_t)a.kmax * 3);
+  double* tmpw = B;  // reuse is not possible (B live); use X tail for 2x2 temporaries
+  (void)tmpw;
+  const int dim = a.dim;
+
+  for (;;) {
+    unsigned long long job = 0;
+    if (lane == 0) job = atomicAdd(a.next, 1ull);
+    job = __shfl_sync(kFull, job, 0);
+    if (job >= (unsigned long long)a.nsys) break;
+    const int64_t e = a.order_list[job];
+    const int64_t rb = a.rowptr[e];
+    const int k = (int)(a.rowptr[e + 1] - rb);
+    const int n = k + a.npoly;
+#define AM(i, j) A[(size_t)((j)-1) * n + ((i)-1)]
+#define BM(i, c) B[(size_t)(c) * n + ((i)-1)]
+    const int32_t* st = a.cols + rb;
+    const int64_t ce = st[0];
+    // shift_stencil
+    for (int j = lane; j < k; j += 32)
+      for (int d = 0; d < dim; ++d) {
+        double t = dsub(a.xyz[(int64_t)st[j] * dim + d], a.xyz[ce * dim + d]);
+        if (a.periodic) t = min_image(t, a.period[d]);
+        X[j * 3 + d] = t;
+      }
+    __syncwarp();
+    double s[3] = {1.0, 1.0, 1.0};
+    for (int d = 0; d < dim; ++d) {
+      double m = 0.0;
+      for (int j = lane; j < k; j += 32) m = fmax(m, fabs(X[j * 3 + d]));
+      m = warp_max(m);
+      s[d] = ddiv(1.0, m);
+    }
+    for (int j = lane; j < k; j += 32)
+      for (int d = 0; d < dim; ++d) X[j * 3 + d] = dmul(X[j * 3 + d], s[d]);
+    __syncwarp();
+    // interpolation block (upper triangle, column-major)
+    const int T = n * (n + 1) / 2;
+    for (int t = lane; t < T; t += 32) {
+      int r, cidx;
+      tri_ij(t, r, cidx);
+      double v;
+      if (cidx < k) {
+        double d2 = 0.0;
+        for (int d = 0; d < dim; ++d) {
+          const double tt = dsub(X[r * 3 + d], X[cidx * 3 + d]);
+          d2 = dadd(d2, dmul(tt, tt));
+        }
+        v = pow_int(sqrt(d2), a.rbf_pow);
+      } else if (r < k) {
+        const int* ex = a.mono[cidx - k];
+        v = 1.0;
+        for (int d = 0; d < dim; ++d) v = dmul(v, pow_int(X[r * 3 + d], ex[d]));
+      } else {
+        v = 0.0;
+      }
+      A[(size_t)cidx * n + r] = v;
+    }
+    // right-hand sides
+    for (int t = lane; t < n * dim; t += 32) {
+      const int d = t / n, j = t % n;
+      double v;
+      if (j < k) {
+        double pt[3];
+        for (int dd = 0; dd < dim; ++dd)
+          pt[dd] = j == 0 ? 2.220446049250313e-16 : -X[j * 3 + dd];
+        double d2 = 0.0;
+        for (int dd = 0; dd < dim; ++dd) d2 = dadd(d2, dmul(pt[dd], pt[dd]));
+        v = phs_deriv(a.rbf_pow, a.order, pt[d], sqrt(d2));
+      } else {
+        const int* ex = a.mono[j - k];
+        bool ok = true;
+        for (int dd = 0; dd < dim; ++dd)
+          if (ex[dd] != (dd == d ? a.order : 0)) ok = false;
+        v = ok ? fact(a.order) : 0.0;
+      }
+      B[(size_t)d * n + j] = v;
+    }
+    __syncwarp();
+
+    // ---------------- Bunch-Kaufman factorisation (upper)
+    const double alpha = (1.0 + sqrt(17.0)) / 8.0;
+    int info = 0;
+    int kk = n;
+    while (kk >= 1) {
+      int kstep = 1, kp;
+      const double absakk = fabs(AM(kk, kk));
+      double colmax = 0.0;
+      int imax = 0;
+      if (kk > 1) {
+        double v = -1.0;
+        int iv = 1 << 30;
+        for (int i = 1 + lane; i < kk; i += 32) {
+          const double x = fabs(AM(i, kk));
+          if (x > v) { v = x; iv = i; }
+        }
+        warp_argmax(v, iv);
+        colmax = v;
+        imax = iv;
+      }
+      if (fmax(absakk, colmax) == 0.0 || isnan(absakk)) {
+        if (info == 0) info = kk;
+        kp = kk;
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = kk;
+        } else {
+          double v = -1.0;
+          int iv = 1 << 30;
+          for (int j = imax + 1 + lane; j <= kk; j += 32) {
+            const double x = fabs(AM(imax, j));
+            if (x > v) { v = x; iv = j; }
+          }
+          warp_argmax(v, iv);
+          double rowmax = v;
+          if (imax > 1) {
+            double v2 = -1.0;
+            int iv2 = 1 << 30;
+            for (int j = 1 + lane; j < imax; j += 32) {
+              const double x = fabs(AM(j, imax));
+              if (x > v2) { v2 = x; iv2 = j; }
+            }
+            warp_argmax(v2, iv2);
+            rowmax = fmax(rowmax, v2);
+          }
+          if (absakk >= alpha * colmax * (colmax / rowmax)) kp = kk;
+          else if (fabs(AM(imax, imax)) >= alpha * rowmax) kp = imax;
+          else { kp = imax; kstep = 2; }
+        }
+        const int kkk = kk - kstep + 1;
+        if (kp != kkk) {
+          for (int i = 1 + lane; i < kp; i += 32) {
+            const double t = AM(i, kkk); AM(i, kkk) = AM(i, kp); AM(i, kp) = t;
+          }
+          for (int j = kp + 1 + lane; j < kkk; j += 32) {
+            const double t = AM(j, kkk); AM(j, kkk) = AM(kp, j); AM(kp, j) = t;
+          }
+          if (lane == 0) {
+            double t = AM(kkk, kkk); AM(kkk, kkk) = AM(kp, kp); AM(kp, kp) = t;
+            if (kstep == 2) { t = AM(kk - 1, kk); AM(kk - 1, kk) = AM(kp, kk); AM(kp, kk) = t; }
+          }
+          __syncwarp();
+        }
+        if (kstep == 1) {
+          const double r1 = ddiv(1.0, AM(kk, kk));
+          const int Tu = (kk - 1) * kk / 2;
+          for (int t = lane; t < Tu; t += 32) {
+            int i0, j0;
+            tri_ij(t, i0, j0);
+            const double xj = AM(j0 + 1, kk);
+            if (xj != 0.0) {
+              const double temp = dmul(-r1, xj);
+              AM(i0 + 1, j0 + 1) = dadd(AM(i0 + 1, j0 + 1), dmul(AM(i0 + 1, kk), temp));
+            }
+          }
+          __syncwarp();
+          for (int i = 1 + lane; i < kk; i += 32) AM(i, kk) = dmul(r1, AM(i, kk));
+          __syncwarp();
+        } else if (kk > 2) {
+          const double d12o = AM(kk - 1, kk);
+          const double d22 = ddiv(AM(kk - 1, kk - 1), d12o);
+          const double d11 = ddiv(AM(kk, kk), d12o);
+          const double tt = ddiv(1.0, dsub(dmul(d11, d22), 1.0));
+          const double d12 = ddiv(tt, d12o);
+          // wk, wkm1 of every column j <= kk-2 from the original entries (kept in X's
+          // spare tail would alias; store them in B's unused columns is unsafe), so
+          // compute them on the fly per element: they depend only on column kk-1/kk.
+          const int Tu = (kk - 2) * (kk - 1) / 2;
+          for (int t = lane; t < Tu; t += 32) {
+            int i0, j0;
+            tri_ij(t, i0, j0);
+            const int j = j0 + 1, i = i0 + 1;
+            const double wkm1 = dmul(d12, dsub(dmul(d11, AM(j, kk - 1)), AM(j, kk)));
+            const double wk = dmul(d12, dsub(dmul(d22, AM(j, kk)), AM(j, kk - 1)));
+            AM(i, j) = dsub(dsub(AM(i, j), dmul(AM(i, kk), wk)), dmul(AM(i, kk - 1), wkm1));
+          }
+          __syncwarp();
+          // now overwrite columns kk-1, kk (rows 1..kk-2) with wkm1, wk
+          for (int j = 1 + lane; j <= kk - 2; j += 32) {
+            const double a1 = AM(j, kk - 1), a2 = AM(j, kk);
+            const double wkm1 = dmul(d12, dsub(dmul(d11, a1), a2));
+            const double wk = dmul(d12, dsub(dmul(d22, a2), a1));
+            AM(j, kk) = wk;
+            AM(j, kk - 1) = wkm1;
+          }
+          __syncwarp();
+        }
+      }
+      if (lane == 0) {
+        if (kstep == 1) ipiv[kk - 1] = kp;
+        else { ipiv[kk - 1] = -kp; ipiv[kk - 2] = -kp; }
+      }
+      __syncwarp();
+      kk -= kstep;
+    }
+
+    if (info != 0) {
+      if (lane == 0) atomicMin(a.bad, (int)e);
+      for (int t = lane; t < k * dim; t += 32) a.w_out[(rb + t / dim) * dim + t % dim] = NAN;
+      if (a.resid && lane == 0) a.resid[e] = NAN;
+      __syncwarp();
+      continue;
+    }
+
+    // ---------------- solve (dsytrs, upper), columns independent
+    const int nrhs = dim;
+    kk = n;
+    while (kk >= 1) {
+      if (ipiv[kk - 1] > 0) {
+        const int kp = ipiv[kk - 1];
+        if (kp != kk && lane < nrhs) {
+          const double t = BM(kk, lane); BM(kk, lane) = BM(kp, lane); BM(kp, lane) = t;
+        }
+        __syncwarp();
+        for (int c = 0; c < nrhs; ++c) {
+          const double bk = BM(kk, c);
+          if (bk != 0.0) {
+            const double temp = -bk;
+            for (int i = 1 + lane; i < kk; i += 32) BM(i, c) = dadd(BM(i, c), dmul(AM(i, kk), temp));
+          }
+        }
+        __syncwarp();
+        const double r = ddiv(1.0, AM(kk, kk));
+        if (lane < nrhs) BM(kk, lane) = dmul(r, BM(kk, lane));
+        __syncwarp();
+        kk -= 1;
+      } else {
+        const int kp = -ipiv[kk - 1];
+        if (kp != kk - 1 && lane < nrhs) {
+          const double t = BM(kk - 1, lane); BM(kk - 1, lane) = BM(kp, lane); BM(kp, lane) = t;
+        }
+        __syncwarp();
+        for (int c = 0; c < nrhs; ++c) {
+          const double bk = BM(kk, c);
+          const double bkm1 = BM(kk - 1, c);
+          for (int i = 1 + lane; i <= kk - 2; i += 32) {
+            double v = BM(i, c);
+            if (bk != 0.0) v = dadd(v, dmul(AM(i, kk), -bk));
+            if (bkm1 != 0.0) v = dadd(v, dmul(AM(i, kk - 1), -bkm1));
+            BM(i, c) = v;
+          }
+        }
+        __syncwarp();
+        if (lane < nrhs) {
+          const double akm1k = AM(kk - 1, kk);
+          const double akm1 = ddiv(AM(kk - 1, kk - 1), akm1k);
+          const double ak = ddiv(AM(kk, kk), akm1k);
+          const double denom = dsub(dmul(akm1, ak), 1.0);
+          const double bkm1 = ddiv(BM(kk - 1, lane), akm1k);
+          const double bk = ddiv(BM(kk, lane), akm1k);
+          BM(kk - 1, lane) = ddiv(dsub(dmul(ak, bkm1), bk), denom);
+          BM(kk, lane) = ddiv(dsub(dmul(akm1, bk), bkm1), denom);
+        }
+        __syncwarp();
+        kk -= 2;
+      }
+    }
+    kk = 1;
+    while (kk <= n) {
+      const bool one = ipiv[kk - 1] > 0;
+      const int ncol = one ? 1 : 2;
+      for (int c = 0; c < nrhs; ++c)
+        for (int q = 0; q < ncol; ++q) {
+          // dot product in a fixed 32-way strided order, then a pairwise tree
+          double part = 0.0;
+          for (int i = 1 + lane; i < kk; i += 32) part = dadd(part, dmul(BM(i, c), AM(i, kk + q)));
+          for (int o = 16; o > 0; o >>= 1) part = dadd(part, __shfl_down_sync(kFull, part, o));
+          if (lane == 0) BM(kk + q, c) = dadd(BM(kk + q, c), dmul(-1.0, part));
+          __syncwarp();
+        }
+      const int kp = one ? ipiv[kk - 1] : -ipiv[kk - 1];
+      if (kp != kk && lane < nrhs) {
+        const double t = BM(kk, lane); BM(kk, lane) = BM(kp, lane); BM(kp, lane) = t;
+      }
+      __syncwarp();
+      kk += ncol;
+    }
+
+    // weights: s_d^order * w[1:k, d]
+    for (int t = lane; t < k * dim; t += 32) {
+      const int j = t / dim, d = t % dim;
+      a.w_out[(rb + j) * dim + d] = dmul(pow_int(s[d], a.order), BM(j + 1, d));
+    }
+    if (a.resid) {
+      // ||M w - b||_inf / ||b||_inf per column, M and b re-evaluated from X^
+      double worst = 0.0;
+      for (int d = 0; d < dim; ++d) {
+        double rn = 0.0, bn = 0.0;
+        for (int r = lane; r < n; r += 32) {
+          double acc = 0.0;
+          for (int cidx = 0; cidx < n; ++cidx) {
+            const int lo = min(r, cidx), hi = max(r, cidx);
+            double v;
+            if (hi < k) {
+              double d2 = 0.0;
+              for (int dd = 0; dd < dim; ++dd) {
+                const double tt = dsub(X[lo * 3 + dd], X[hi * 3 + dd]);
+                d2 = dadd(d2, dmul(tt, tt));
+              }
+              v = pow_int(sqrt(d2), a.rbf_pow);
+            } else if (lo < k) {
+              const int* ex = a.mono[hi - k];
+              v = 1.0;
+              for (int dd = 0; dd < dim; ++dd) v = dmul(v, pow_int(X[lo * 3 + dd], ex[dd]));
+            } else {
+              v = 0.0;
+            }
+            acc += v * BM(cidx + 1, d);
+          }
+          double bv;
+          if (r < k) {
+            double pt[3];
+            for (int dd = 0; dd < dim; ++dd) pt[dd] = r == 0 ? 2.220446049250313e-16 : -X[r * 3 + dd];
+            double d2 = 0.0;
+            for (int dd = 0; dd < dim; ++dd) d2 = dadd(d2, dmul(pt[dd], pt[dd]));
+            bv = phs_deriv(a.rbf_pow, a.order, pt[d], sqrt(d2));
+          } else {
+            const int* ex = a.mono[r - k];
+            bool ok = true;
+            for (int dd = 0; dd < dim; ++dd)
+              if (ex[dd] != (dd == d ? a.order : 0)) ok = false;
+            bv = ok ? fact(a.order) : 0.0;
+          }
+          rn = fmax(rn, fabs(acc - bv));
+          bn = fmax(bn, fabs(bv));
+        }
+        rn = warp_max(rn);
+        bn = warp_max(bn);
+        worst = fmax(worst, bn > 0 ? rn / bn : rn);
+      }
+      if (lane == 0) a.resid[e] = worst;
+    }
+    __syncwarp();
+#undef AM
+#undef BM
+  }
+}
+
+int make_monomials(int dim, int deg, int (*ex)[3], int cap) {
+  int m = 0;
+  for (int q = 0; q <= deg; ++q) {
+    if (dim == 1) {
+      if (m < cap) { ex[m][0] = q; ex[m][1] = 0; ex[m][2] = 0; }
+      m++;
+      continue;
+    }
+    for (int a = q; a >= 0; --a) {
+      if (dim == 2) {
+        if (m < cap) { ex[m][0] = a; ex[m][1] = q - a; ex[m][2] = 0; }
+        m++;
+        continue;
+      }
+      for (int b = q - a; b >= 0; --b) {
+        if (m < cap) { ex[m][0] = a; ex[m][1] = b; ex[m][2] = q - a - b; }
+        m++;
+      }
+    }
+  }
+  return m;
+}
+
+}  // namespace
+
+void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
+                    std::vector<double>& w_out, double* max_resid) {
+  const int dim = c->dim;
+  const int64_t n = c->n;
+  WArgs a{};
+  a.dim = dim;
+  a.npoly = make_monomials(dim, polydeg, a.mono, 128);
+  MFT_REQUIRE(a.npoly <= 128, MFT_ERR_ARG, "polynomial degree too high");
+  a.rbf_pow = rbf_pow;
+  a.order = deriv_order;
+  a.periodic = c->periodic ? 1 : 0;
+  for (int d = 0; d < 3; ++d) a.period[d] = c->period[d];
+  std::vector<int64_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
+    return (c->st_rp[x + 1] - c->st_rp[x]) > (c->st_rp[y + 1] - c->st_rp[y]);
+  });
+  int kmax = 0;
+  for (int64_t i = 0; i < n; ++i) kmax = std::max<int>(kmax, (int)(c->st_rp[i + 1] - c->st_rp[i]));
+  a.kmax = kmax;
+  a.nmax = kmax + a.npoly;
+  const size_t per = (size_t)a.nmax * a.nmax + (size_t)a.nmax * 3 + (size_t)kmax * 3 + a.nmax;
+  const size_t shmem = per * sizeof(double) * kWarpsPerBlock;
+  MFT_REQUIRE(shmem <= 227 * 1024, MFT_ERR_ARG, "stencil too large for the weight kernel");
+  cudaStream_t s = c->stream;
+  DBuf<int64_t> d_order, d_rp;
+  DBuf<int32_t> d_ci;
+  DBuf<double> d_w, d_res;
+  DBuf<int> d_bad;
+  DBuf<unsigned long long> d_next;
+  d_order.upload(order, s);
+  d_rp.upload(c->st_rp, s);
+  d_ci.upload(c->st_ci, s);
+  const int64_t nnz = (int64_t)c->st_ci.size();
+  d_w.alloc((size_t)nnz * dim);
+  if (max_resid) d_res.alloc(n);
+  d_bad.alloc(1);
+  const int big = 0x7fffffff;
+  MFT_CUDA(cudaMemcpyAsync(d_bad.p, &big, sizeof(int), cudaMemcpyHostToDevice, s));
+  d_next.alloc(1);
+  d_next.zero(s);
+  a.nsys = n;
+  a.order_list = d_order.p;
+  a.rowptr = d_rp.p;
+  a.cols = d_ci.p;
+  a.xyz = c->d_xyz.p;
+  a.w_out = d_w.p;
+  a.resid = max_resid ? d_res.p : nullptr;
+  a.bad = d_bad.p;
+  a.next = d_next.p;
+  MFT_CUDA(cudaFuncSetAttribute(k_weights, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
+  int dev = 0, sms = 0, per_sm = 0;
+  MFT_CUDA(cudaGetDevice(&dev));
+  MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights, 32 * kWarpsPerBlock, shmem));
+  per_sm = std::max(per_sm, 1);
+  const int64_t want = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
+  k_weights<<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
+  MFT_LAUNCH_CHECK();
+  w_out.resize((size_t)nnz * dim);
+  int bad = big;
+  MFT_CUDA(cudaMemcpyAsync(w_out.data(), d_w.p, w_out.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  MFT_CUDA(cudaMemcpyAsync(&bad, d_bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  std::vector<double> res;
+  if (max_resid) {
+    res.resize(n);
+    MFT_CUDA(cudaMemcpyAsync(res.data(), d_res.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  MFT_CUDA(cudaStreamSynchronize(s));
+  MFT_REQUIRE(bad == big, MFT_ERR_SINGULAR,
+              "saddle-point system of node " + std::to_string(bad) + " has an exactly zero pivot");
+  if (max_resid) {
+    double m = 0.0;
+    for (double r : res) m = std::max(m, r);
+    *max_resid = m;
+  }
+}
+
+}  // namespace mft

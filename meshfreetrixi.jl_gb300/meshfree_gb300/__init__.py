@@ -1,0 +1,12 @@
+"""meshfree_gb300: GB300 (sm_103a) engine for the RBF-FD semidiscretization of
+MeshfreeTrixi.jl, with a host API that mirrors the reference's point-cloud API."""
+from ._lib import Context, MFTError, load  # noqa: F401
+from .api import (  # noqa: F401
+    RBF, BoundaryConditionDirichlet, BoundaryConditionDoNothing, BoundaryData,
+    CompressibleEulerEquations2D, HistoryCallback, LinearScalarAdvectionEquation2D, ODEProblem,
+    Point1D, Point2D, Point3D, PointCloudBasis, PointCloudDomain, PointCloudDomain_from_medusa,
+    PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
+    SemidiscretizationHyperbolic, SourceHyperviscosityFlyer, SourceHyperviscosityTominec,
+    SourceResidualViscosityTominec, SourceTerms, SourceUpwindViscosityTominec, SSPRK33,
+    boundary_condition_slip_wall, rhs_, semidiscretize, solve)
+from .medusa import read_medusa_file  # noqa: F401

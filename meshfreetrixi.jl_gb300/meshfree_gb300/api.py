@@ -1,0 +1,409 @@
+"""Host-side mirror of the reference's point-cloud API over libmeshfree_gb300.so.
+
+Names, arguments and behaviour follow MeshfreeTrixi.jl and the Trixi.jl calls it
+is used with (PointCloudBasis, PointCloudSolver, PointCloudDomain,
+SemidiscretizationHyperbolic, semidiscretize, rhs!, the source types, the
+HistoryCallback and an SSPRK33 integrator).  Arrays follow the StructArray
+layout: a state is an (nvars, n) float64 array, one row per conserved variable.
+Node indices are 0-based.  Every numerical step runs in the CUDA library.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable
+
+import numpy as np
+
+from . import _lib as L
+from .medusa import read_medusa_file
+
+# ------------------------------------------------------------------ basis
+# src/domains/PointCloudDomain/geometry_primatives.jl:1-209
+
+
+class Point1D:
+    ndims = 1
+
+
+class Point2D:
+    ndims = 2
+
+
+class Point3D:
+    ndims = 3
+
+
+@dataclass(frozen=True)
+class PolyharmonicSpline:
+    """phi(r) = r^Nrbf (geometry_primatives.jl:110-114, 212-237)."""
+    Nrbf: int = 3
+
+
+@dataclass(frozen=True)
+class RBF:
+    rbf_type: PolyharmonicSpline = field(default_factory=PolyharmonicSpline)
+
+    @property
+    def Nrbf(self):
+        return self.rbf_type.Nrbf
+
+
+@dataclass(frozen=True)
+class RefPointData:
+    """element_type, approximation_type, N (polynomial degree), nv (stencil size)
+    (geometry_primatives.jl:27-35)."""
+    element_type: object
+    approximation_type: RBF
+    N: int
+    nv: int
+
+    @property
+    def ndims(self):
+        return self.element_type.ndims
+
+
+def PointCloudBasis(element_type, polydeg, approximation_type=None, nv=None):
+    """types.jl:83-86; nv defaults to max(2*binomial(N+d, d), (10,15,20)[d])
+    (geometry_primatives.jl:183-184)."""
+    at = approximation_type if approximation_type is not None else RBF()
+    d = element_type.ndims
+    if nv is None:
+        nv = max(2 * math.comb(polydeg + d, d), (10, 15, 20)[d - 1])
+    return RefPointData(element_type, at, int(polydeg), int(nv))
+
+
+# ------------------------------------------------------------------ solver
+# src/solvers/rbfsolver.jl:8-71, src/solvers/pointcloudsolver/types.jl:49-74
+
+
+@dataclass
+class RBFFDEngineGB300:
+    """The GB300 engine (the reference's RBFFDEngineCUDA slot).  precision is
+    "fp64" (FP64 weights, states and sums) or "fp32" (FP32 apply, FP64 RK)."""
+    device: int = 0
+    precision: str = "fp64"
+
+
+@dataclass
+class RBFSolver:
+    basis: RefPointData
+    engine: RBFFDEngineGB300
+
+
+def PointCloudSolver(basis, engine=None):
+    return RBFSolver(basis, engine if engine is not None else RBFFDEngineGB300())
+
+
+# ------------------------------------------------------------------ domain
+# src/domains/PointCloudDomain/*.jl
+
+
+@dataclass
+class PointData:
+    """geometry_primatives.jl:300-339: neighbours (n, nv) sorted by distance, self
+    first; dx_min / dx_avg: min and mean nearest-neighbour distance."""
+    points: np.ndarray
+    neighbors: np.ndarray
+    num_points: int
+    num_neighbors: int
+    dx_min: float
+    dx_avg: float
+
+
+@dataclass
+class BoundaryData:
+    idx: np.ndarray
+    normals: np.ndarray
+
+
+class PointCloudDomain:
+    """Point cloud with GPU-built stencils and boundary tags.  Holds the engine
+    context that the semidiscretization on this domain uses."""
+
+    def __init__(self, solver, points, boundary_tags=None, period=None):
+        basis = solver.basis
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        assert pts.ndim == 2 and pts.shape[1] == basis.ndims
+        self.solver = solver
+        self.period = None if period is None else tuple(float(p) for p in period)
+        self.ctx = L.Context(solver.engine.device)
+        self.ctx.set_points(pts, self.period)
+        idx, _dist, dmin, davg = self.ctx.knn(basis.nv)
+        self.pd = PointData(pts, idx, pts.shape[0], basis.nv, dmin, davg)
+        self.boundary_tags = dict(boundary_tags or {})
+        self.loaded = {}
+
+    @property
+    def ndims(self):
+        return self.pd.points.shape[1]
+
+    def operator(self, op, rbf_pow, polydeg, deriv_order):
+        """Computes (once) the weights of operator slot `op` on the GPU."""
+        key = (op, rbf_pow, polydeg, deriv_order)
+        if self.loaded.get(op) != key:
+            self.ctx.weights(op, rbf_pow, polydeg, deriv_order)
+            self.loaded[op] = key
+
+
+def PointCloudDomain_from_medusa(solver, casename, boundary_names):
+    """PointCloudDomain(solver, casename, Dict(:inlet => 1, ...)) (types.jl:133-145,
+    SerialPointCloud.jl:45-54)."""
+    pos, _interior, b_idx, b_nrm, _normals, _types = read_medusa_file(casename)
+    tags = {name: BoundaryData(b_idx[i - 1], b_nrm[i - 1]) for name, i in boundary_names.items()}
+    return PointCloudDomain(solver, pos, tags)
+
+
+# ------------------------------------------------------------------ equations
+
+
+@dataclass
+class CompressibleEulerEquations2D:
+    gamma: float = 1.4
+    nvariables = 4
+    kind = L.EQ_EULER2D
+
+    def params(self):
+        return [self.gamma]
+
+    def cons2prim(self, u):
+        rho, m1, m2, e = u
+        v1, v2 = m1 / rho, m2 / rho
+        p = (self.gamma - 1.0) * (e - 0.5 * (m1 * v1 + m2 * v2))
+        return np.stack([rho, v1, v2, p])
+
+    def prim2cons(self, w):
+        rho, v1, v2, p = w
+        return np.stack([rho, rho * v1, rho * v2, p / (self.gamma - 1.0) + 0.5 * rho * (v1 * v1 + v2 * v2)])
+
+
+@dataclass
+class LinearScalarAdvectionEquation2D:
+    advection_velocity: tuple = (1.0, 0.5)
+    nvariables = 1
+    kind = L.EQ_ADVECTION
+
+    def params(self):
+        return list(self.advection_velocity)
+
+
+# ------------------------------------------------------------------ boundary conditions
+# src/equations/PointCloudBCs.jl
+
+
+@dataclass
+class BoundaryConditionDirichlet:
+    """boundary_value_function(x (m, d), t, equations) -> (m, nvars) array."""
+    boundary_value_function: Callable
+    kind = L.BC_DIRICHLET
+
+
+class BoundaryConditionSlipWall:
+    kind = L.BC_SLIP_WALL
+
+
+class BoundaryConditionDoNothing:
+    kind = L.BC_DO_NOTHING
+
+
+boundary_condition_slip_wall = BoundaryConditionSlipWall()
+
+
+# ------------------------------------------------------------------ sources
+# src/sources/generic_sources.jl, src/sources/hyperviscosity.jl
+
+
+class SourceTerms(dict):
+    """SourceTerms(; kwargs...): an ordered name -> source mapping."""
+
+    def __init__(self, **kw):
+        super().__init__(kw)
+
+
+@dataclass
+class SourceResidualViscosityTominec:
+    solver: RBFSolver
+    equations: object
+    domain: PointCloudDomain
+    c_rv: float = 1.0
+    c_uw: float = 1.0
+    polydeg: int = 4
+    norm_mode: int = 0  # 0: reference ode_mean/ode_maximum; 1: per-component
+
+    def spec(self):
+        return L.SRC_RV, [self.c_rv, self.c_uw, self.domain.pd.dx_avg, self.norm_mode]
+
+
+@dataclass
+class SourceUpwindViscosityTominec:
+    solver: RBFSolver
+    equations: object
+    domain: PointCloudDomain
+    c: float = 1.0
+    c_uw: float = 1.0
+    polydeg: int = 4
+
+    def spec(self):
+        return L.SRC_UPWIND, [self.c_uw, self.domain.pd.dx_avg, 0.0, 0.0]
+
+
+@dataclass
+class SourceHyperviscosityTominec:
+    """gamma = c * dx_min^4.5; operator lap' * lap, lap = Dxx + Dyy (:101-119)."""
+    solver: RBFSolver
+    equations: object
+    domain: PointCloudDomain
+    c: float = 1.0
+
+    @property
+    def gamma(self):
+        return self.c * self.domain.pd.dx_min ** 4.5
+
+    def prepare(self):
+        b = self.solver.basis
+        self.domain.operator(L.OP_LAP, b.approximation_type.Nrbf, b.N, 2)
+
+    def spec(self):
+        return L.SRC_HV_TOMINEC, [self.gamma, 0.0, 0.0, 0.0]
+
+
+@dataclass
+class SourceHyperviscosityFlyer:
+    """gamma = c * dx_min^(2k); operator sum_d D_d^(2k) (:34-50)."""
+    solver: RBFSolver
+    equations: object
+    domain: PointCloudDomain
+    k: int = 2
+    c: float = 1.0
+
+    @property
+    def gamma(self):
+        return self.c * self.domain.pd.dx_min ** (2 * self.k)
+
+    def prepare(self):
+        b = self.solver.basis
+        self.domain.operator(L.OP_HV, b.approximation_type.Nrbf, b.N, 2 * self.k)
+
+    def spec(self):
+        return L.SRC_HV_FLYER, [self.gamma, 0.0, 0.0, 0.0]
+
+
+# ------------------------------------------------------------------ semidiscretization
+
+
+class SemidiscretizationHyperbolic:
+    """Trixi's SemidiscretizationHyperbolic specialised to point clouds: the cache
+    (Trixi.create_cache, rbfsolver.jl:130-165) lives in the engine context."""
+
+    def __init__(self, domain, equations, initial_condition, solver, boundary_conditions=None,
+                 source_terms=None):
+        self.domain, self.equations, self.solver = domain, equations, solver
+        self.initial_condition = initial_condition
+        self.boundary_conditions = dict(boundary_conditions or {})
+        self.source_terms = source_terms if source_terms is not None else SourceTerms()
+        b = solver.basis
+        ctx = domain.ctx
+        domain.operator(L.OP_GRAD, b.approximation_type.Nrbf, b.N, 1)
+        ctx.set_equations(equations.kind, equations.params())
+        ctx.set_precision(L.PREC_FP32 if solver.engine.precision == "fp32" else L.PREC_FP64)
+        kinds, ptr, idx, nrm = [], [0], [], []
+        self._dirichlet = []
+        for name, bc in self.boundary_conditions.items():
+            tag = domain.boundary_tags[name]
+            ii = np.asarray(tag.idx, dtype=np.int32)
+            kinds.append(bc.kind)
+            idx.append(ii)
+            nrm.append(np.asarray(tag.normals, dtype=np.float64).reshape(ii.size, -1))
+            if bc.kind == L.BC_DIRICHLET:
+                self._dirichlet.append((slice(ptr[-1], ptr[-1] + ii.size), ii, bc))
+            ptr.append(ptr[-1] + ii.size)
+        self._nb = ptr[-1]
+        if kinds:
+            ctx.set_bcs(kinds, ptr, np.concatenate(idx), np.concatenate(nrm))
+        else:
+            ctx.set_bcs([], [0], np.zeros(0, np.int32), None)
+        if self._dirichlet:
+            ctx.set_dirichlet_callback(self.dirichlet_values)
+        else:
+            ctx.set_dirichlet_callback(None)
+        skinds, spars = [], []
+        for src in self.source_terms.values():
+            if hasattr(src, "prepare"):
+                src.prepare()
+            k, p = src.spec()
+            skinds.append(k)
+            spars.append(p)
+        ctx.set_sources(skinds, spars)
+
+    def dirichlet_values(self, t):
+        V = self.equations.nvariables
+        out = np.zeros((self._nb, V))
+        for sl, ii, bc in self._dirichlet:
+            x = self.domain.pd.points[ii]
+            out[sl] = np.asarray(bc.boundary_value_function(x, t, self.equations)).reshape(-1, V)
+        return out
+
+    def compute_coefficients(self, t):
+        """u = initial_condition(x, t, equations) at every node (rbfsolver.jl:174-185)."""
+        u = self.initial_condition(self.domain.pd.points, t, self.equations)
+        return np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(self.equations.nvariables, -1))
+
+
+@dataclass
+class ODEProblem:
+    u0: np.ndarray
+    tspan: tuple
+    p: SemidiscretizationHyperbolic
+
+
+def semidiscretize(semi, tspan):
+    return ODEProblem(semi.compute_coefficients(tspan[0]), tuple(tspan), semi)
+
+
+def rhs_(du, u, semi, t):
+    """Trixi's rhs!(du_ode, u_ode, semi, t) (rbfsolver.jl:397-428) on the GPU.
+    du, u: (nvars, n) float64 C-contiguous; u is mutated at boundary nodes."""
+    semi.domain.ctx.rhs(du, u, t)
+    return None
+
+
+# ------------------------------------------------------------------ time integration
+
+
+@dataclass
+class HistoryCallback:
+    """HistoryCallback(; approx_order) (src/callbacks_step/history.jl:43-49)."""
+    approx_order: int
+
+
+class SSPRK33:
+    """Shu-Osher SSP-RK3 with first-same-as-last stage reuse."""
+
+
+@dataclass
+class ODESolution:
+    u: np.ndarray
+    t: float
+    nsteps: int
+
+
+def solve(ode, alg=None, dt=None, callback=None, save_everystep=False):
+    """Fixed-step SSPRK33 on the device from tspan[0] to tspan[1]."""
+    assert dt is not None and dt > 0
+    semi = ode.p
+    ctx = semi.domain.ctx
+    t0, t1 = ode.tspan
+    cbs = callback if isinstance(callback, (list, tuple)) else ([callback] if callback else [])
+    ctx.set_state(ode.u0, t0)
+    for cb in cbs:
+        if isinstance(cb, HistoryCallback):
+            ctx.history_init(cb.approx_order)
+    nfull = int(math.floor((t1 - t0) / dt + 1e-9))
+    ctx.ssprk33(dt, nfull)
+    steps = nfull
+    rest = (t1 - t0) - nfull * dt
+    if rest > 1e-12 * dt:
+        ctx.ssprk33(rest, 1)
+        steps += 1
+    u, t = ctx.get_state()
+    return ODESolution(u, t, steps)

@@ -1,0 +1,97 @@
+"""Shared set-up for parity tests: the same inputs for the CPU oracle and the GPU."""
+from __future__ import annotations
+
+import numpy as np
+
+GAMMA = 1.4
+
+
+def ic_gradient(x, t=0.0):
+    """initial_condition_gradient of test/divergence_test.jl:28-38 (conserved vars)."""
+    s = 0.1 * x[:, 0] + 0.1 * x[:, 1]
+    return np.ascontiguousarray(np.stack([1.4 + s, 4.1 + s, 0.0 + s, 8.8 + s]))
+
+
+def ic_bumpy(x, seed=3):
+    """Smooth non-trivial Euler state (positive density / pressure)."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    a = g.uniform(0.5, 1.5, 6)
+    rho = 1.0 + 0.2 * np.sin(a[0] * 3 * x[:, 0]) * np.cos(a[1] * 2 * x[:, 1])
+    u = 0.5 + 0.3 * np.cos(a[2] * 2 * x[:, 0] + x[:, 1])
+    v = -0.2 + 0.3 * np.sin(a[3] * 2 * x[:, 1] - x[:, 0])
+    p = 1.0 + 0.1 * np.cos(a[4] * x[:, 0] * x[:, 1])
+    e = p / (GAMMA - 1.0) + 0.5 * rho * (u * u + v * v)
+    return np.ascontiguousarray(np.stack([rho, rho * u, rho * v, e]))
+
+
+def cyl_bcs(cyl, dirichlet_fn):
+    """Reference test BCs (divergence_test.jl:40-44) in NamedTuple order:
+    inlet Dirichlet, outlet DoNothing, top / bottom / cyl slip walls.
+    Boundary groups: inlet 1, outlet 2, bottom 3, top 4, cyl 5."""
+    from oracle.oracle import BC_DIRICHLET, BC_DO_NOTHING, BC_SLIP_WALL
+    return [
+        (BC_DIRICHLET, cyl["bidx_1"], cyl["bnrm_1"], dirichlet_fn),
+        (BC_DO_NOTHING, cyl["bidx_2"], cyl["bnrm_2"], None),
+        (BC_SLIP_WALL, cyl["bidx_4"], cyl["bnrm_4"], None),
+        (BC_SLIP_WALL, cyl["bidx_3"], cyl["bnrm_3"], None),
+        (BC_SLIP_WALL, cyl["bidx_5"], cyl["bnrm_5"], None),
+    ]
+
+
+def stencil_ops(oracle, points, idx, rbf_pow=3, polydeg=3, order=1, period=None):
+    n, k = idx.shape
+    rowptr = np.arange(n + 1, dtype=np.int64) * k
+    w = oracle.weights(points, rowptr, idx.ravel(), rbf_pow=rbf_pow, polydeg=polydeg,
+                       deriv_order=order, period=period)
+    return oracle.operators_from_stencils(n, rowptr, idx.ravel(), w), w
+
+
+def load_ops_into(ctx, ops, lap=None, hv=None):
+    """Loads oracle CSR/CSC operators into a GPU context through the 1-based CSC
+    entry point, as a Julia caller would pass SparseMatrixCSC arrays."""
+    from meshfree_gb300 import _lib as L
+    for d, o in enumerate(ops):
+        ctx.load_csc(L.OP_GRAD, d, o.cp + 1, o.ri.astype(np.int64) + 1, o.valt)
+    if lap is not None:
+        ctx.load_csc(L.OP_LAP, 0, lap.cp + 1, lap.ri.astype(np.int64) + 1, lap.valt)
+    if hv is not None:
+        ctx.load_csc(L.OP_HV, 0, hv.cp + 1, hv.ri.astype(np.int64) + 1, hv.valt)
+
+
+def isapprox(a, b, rtol=np.sqrt(np.finfo(float).eps)):
+    """Julia's isapprox for arrays: norm(a-b) <= rtol * max(norm(a), norm(b))."""
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    return np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(a), np.linalg.norm(b))
+
+
+def flux_np(u, d, gamma=GAMMA):
+    rho, m1, m2, e = u
+    v1, v2 = m1 / rho, m2 / rho
+    p = (gamma - 1.0) * (e - 0.5 * (m1 * v1 + m2 * v2))
+    if d == 0:
+        return np.stack([m1, m1 * v1 + p, m1 * v2, (e + p) * v1])
+    return np.stack([m2, m2 * v1, m2 * v2 + p, (e + p) * v2])
+
+
+def cond_scale(ops, u, fluxes=None, eps=None, lap=None, hv_gamma=0.0, hvop=None):
+    """Per-variable condition scale  |D||F| + sum_d |D_d|'(|eps| |D_d||u|)
+    + gamma |lap|'|lap||u| (+ gamma |H||u|), max over nodes."""
+    A = [abs(o.to_scipy()) for o in ops]
+    V = u.shape[0]
+    out = np.zeros(V)
+    for v in range(V):
+        s = np.zeros(u.shape[1])
+        if fluxes is not None:
+            for d, a in enumerate(A):
+                s += a @ np.abs(fluxes[d][v])
+        if eps is not None:
+            for a in A:
+                s += a.T @ (np.abs(eps) * (a @ np.abs(u[v])))
+        if lap is not None:
+            la = abs(lap.to_scipy())
+            s += hv_gamma * (la.T @ (la @ np.abs(u[v])))
+        if hvop is not None:
+            s += hv_gamma * (abs(hvop.to_scipy()) @ np.abs(u[v]))
+        out[v] = s.max()
+    return out

@@ -1,0 +1,122 @@
+"""SSP-RK3 + HistoryCallback trajectories on the GPU against the CPU oracle, the
+FP32-apply form against the FP64 form, and the host-buffer entry point."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _advection_problem(n_side, prec="fp64"):
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, tags, h = W.advection_cloud(n_side)
+    eq = M.LinearScalarAdvectionEquation2D((1.0, 0.5))
+    basis = M.PointCloudBasis(M.Point2D(), 3, approximation_type=M.RBF(M.PolyharmonicSpline(3)),
+                              nv=35)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision=prec))
+    domain = M.PointCloudDomain(solver, pts, {k: M.BoundaryData(*v) for k, v in tags.items()})
+    ic = lambda x, t, e: W.gaussian_bump(x, t)
+    bcs = {"inflow": M.BoundaryConditionDirichlet(lambda x, t, e: W.gaussian_bump(x, t).T),
+           "outflow": M.BoundaryConditionDoNothing()}
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, domain, c_rv=1.0, c_uw=1.0))
+    semi = M.SemidiscretizationHyperbolic(domain, eq, ic, solver, boundary_conditions=bcs,
+                                          source_terms=src)
+    return semi, domain, pts, tags, h
+
+
+def _oracle_advection(oracle, pts, tags, domain, nv=35):
+    from meshfree_gb300 import workloads as W
+    n = pts.shape[0]
+    idx, _, dmin, davg = oracle.knn(pts, nv)
+    assert np.array_equal(idx, domain.pd.neighbors)
+    rowptr = np.arange(n + 1, dtype=np.int64) * nv
+    w = oracle.weights(pts, rowptr, idx.ravel())
+    ops = oracle.operators_from_stencils(n, rowptr, idx.ravel(), w)
+    bcs = [(oracle.BC_DIRICHLET, tags["inflow"][0], tags["inflow"][1],
+            lambda x, t: W.gaussian_bump(x, t).T),
+           (oracle.BC_DO_NOTHING, tags["outflow"][0], tags["outflow"][1], None)]
+    return oracle.Semi(pts, ops, eq="advection", adv=(1.0, 0.5), bcs=bcs,
+                       sources=(oracle.SRC_RV,), c_rv=1.0, c_uw=1.0, h=davg)
+
+
+def test_advection_rv_trajectory_matches_oracle(oracle, gpu_lib):
+    import meshfree_gb300 as M
+    semi, domain, pts, tags, h = _advection_problem(32)
+    dt, nsteps = 0.2 * h, 30
+    ode = M.semidiscretize(semi, (0.0, nsteps * dt))
+    sol = M.solve(ode, M.SSPRK33(), dt=dt, callback=M.HistoryCallback(approx_order=3))
+    osemi = _oracle_advection(oracle, pts, tags, domain)
+    hist = oracle.History(osemi, 3)
+    u_ref, t_ref = oracle.ssprk33(osemi, ode.u0, 0.0, dt, nsteps, history=hist)
+    assert sol.nsteps == nsteps
+    assert abs(sol.t - t_ref) <= 1e-14
+    err = np.abs(sol.u - u_ref).max() / np.abs(u_ref).max()
+    assert err < 1e-10, err
+
+
+def test_vortex_rv_trajectory_matches_oracle(oracle, gpu_lib):
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(32)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver = M.PointCloudSolver(basis)
+    domain = M.PointCloudDomain(solver, pts, period=per)
+    ic = lambda x, t, e: W.isentropic_vortex(x, t)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, domain))
+    semi = M.SemidiscretizationHyperbolic(domain, eq, ic, solver, source_terms=src)
+    dt, nsteps = 0.1 * h, 12
+    ode = M.semidiscretize(semi, (0.0, nsteps * dt))
+    sol = M.solve(ode, M.SSPRK33(), dt=dt, callback=M.HistoryCallback(approx_order=3))
+    n = pts.shape[0]
+    idx, _, _, davg = oracle.knn(pts, 35, period=per)
+    rowptr = np.arange(n + 1, dtype=np.int64) * 35
+    w = oracle.weights(pts, rowptr, idx.ravel(), period=per)
+    ops = oracle.operators_from_stencils(n, rowptr, idx.ravel(), w)
+    osemi = oracle.Semi(pts, ops, eq="euler", gamma=1.4, sources=(oracle.SRC_RV,), h=davg)
+    u_ref, _ = oracle.ssprk33(osemi, ode.u0, 0.0, dt, nsteps, history=oracle.History(osemi, 3))
+    err = np.abs(sol.u - u_ref).max(axis=1) / np.abs(u_ref).max(axis=1)
+    assert np.all(err < 1e-10), err
+
+
+def test_fp32_apply_error_vs_fp64(gpu_lib):
+    """FP32 weights/states/sums in the apply; error of density vs the FP64 form."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(64)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        eq = M.CompressibleEulerEquations2D(1.4)
+        basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+        solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision=prec))
+        domain = M.PointCloudDomain(solver, pts, period=per)
+        src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, domain))
+        semi = M.SemidiscretizationHyperbolic(domain, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                              solver, source_terms=src)
+        ode = M.semidiscretize(semi, (0.0, 20 * 0.1 * h))
+        res[prec] = M.solve(ode, M.SSPRK33(), dt=0.1 * h, callback=M.HistoryCallback(3)).u
+    r64, r32 = res["fp64"][0], res["fp32"][0]
+    l2 = np.linalg.norm(r32 - r64) / np.linalg.norm(r64)
+    assert l2 < 1e-5, l2
+
+
+def test_host_entry_point_equals_device_steps(gpu_lib):
+    """mft_ssprk33_host step by step (state handed back each time) equals device
+    stepping, and reuses the pending first stage when handed its own state back."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    semi, domain, pts, tags, h = _advection_problem(24)
+    ctx = domain.ctx
+    u0 = semi.compute_coefficients(0.0)
+    dt = 0.2 * h
+    ctx.history_init(3)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, 3)
+    u_dev, t_dev = ctx.get_state()
+    ctx.history_init(3)
+    u = u0.copy()
+    t = 0.0
+    for _ in range(3):
+        t = ctx.ssprk33_host(u, t, dt, 1)
+    assert t == t_dev
+    assert np.array_equal(u, u_dev)
