@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark of the RBF-FD rhs! hot path on one GB300 (replicas for --gpus N > 1).
+
+Workload: 2D compressible Euler isentropic vortex on the periodic square [-5,5]^2,
+N = 262,144 seeded jittered nodes, PHS r^3 + degree-3 polynomials, 35-node stencils,
+FP64 weights and states, residual-viscosity source with the HistoryCallback
+(approx_order 3), SSP-RK3.  One step = one SSP-RK3 step = 3 rhs! evaluations.
+Metric: node-RHS updates/s = nodes * rhs! evaluations / device seconds.
+
+--impl reference runs the CPU restatement of the reference's rhs! (the oracle: the
+reference is Julia and no Julia toolchain exists on the box) on all host cores,
+same workload and metric.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for p in (str(ROOT), str(ROOT / "meshfreetrixi.jl_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "node-RHS updates/s"
+UNIT = "node-rhs/s"
+N_SIDE = 512
+K_STENCIL = 35
+DT_FACTOR = 0.2          # dt = 0.2 h
+RHS_PER_STEP = 3
+DFMA_PEAK_GFMA = 505.1   # measured FP64 FMA rate of this GB300 (probe in profiles/)
+
+# Algorithmic bytes per node and launch (FP64 form, V=4, D=2, k=35, int32 indices):
+#   fwd_gather: idx 4k + weights 2*8k + state read 32 + du_p write 32 + t=Du write 64
+#   rev_gather: idx 4k + weights 2*8k + s read 64 + du_p 32 + u_s 32 + u_n 32 + out 32
+BYTES = {
+    "fp64": {"fwd_gather": 4 * 35 + 16 * 35 + 32 + 32 + 64,
+             "rev_gather": 4 * 35 + 16 * 35 + 64 + 32 + 32 + 32 + 32},
+    "fp32": {"fwd_gather": 4 * 35 + 8 * 35 + 16 + 16 + 32,
+             "rev_gather": 4 * 35 + 8 * 35 + 32 + 16 + 32 + 32 + 32 + 16},
+}
+# FP64 FMAs per node and launch: fwd 14 per stencil entry (t: 8, du rows 2-4: 6),
+# rev 8 per reverse-adjacency entry (mean in-degree = k).
+DFMA = {"fwd_gather": 14 * 35, "rev_gather": 8 * 35}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-side", type=int, default=N_SIDE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=ws)
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def build_problem(n_side, prec, device):
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(n_side)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    basis = M.PointCloudBasis(M.Point2D(), 3, approximation_type=M.RBF(M.PolyharmonicSpline(3)),
+                              nv=K_STENCIL)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=device, precision=prec))
+    domain = M.PointCloudDomain(solver, pts, period=per)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, domain, c_rv=1.0, c_uw=1.0))
+    semi = M.SemidiscretizationHyperbolic(domain, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                          solver, source_terms=src)
+    return semi, domain, semi.compute_coefficients(0.0), DT_FACTOR * h
+
+
+def timed_steps(ctx, u0, dt, warmup, steps, pg, clocks=None, profile=True):
+    ctx.history_init(3)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, warmup)
+    ctx.sync()
+    barrier(pg)
+    if profile:
+        ctx.profile(True)
+    if clocks:
+        clocks.start()
+    ctx.region_begin()
+    ctx.ssprk33(dt, steps)
+    ms = ctx.region_end()
+    clk = clocks.stop() if clocks else None
+    prof = ctx.profile_report() if profile else {}
+    ctx.profile(False)
+    return ms, prof, clk
+
+
+def roofline(prof, n, prec, peaks):
+    name = max(prof, key=lambda k: prof[k][0])
+    ms, launches = prof[name]
+    per_launch = ms / launches
+    bpn = BYTES[prec].get(name)
+    out = {"kernel": name, "avg_launch_ms": per_launch, "launches": launches}
+    if bpn is not None:
+        achieved = bpn * n / (per_launch * 1e-3) / 1e9
+        out.update({"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                    "algorithmic_bytes_per_node": bpn, "peak_source": peaks["source"]})
+    traffic = ncu_traffic(name, prec)
+    out["traffic"] = None if traffic is None else traffic * n
+    out["traffic_source"] = None if traffic is None else "profiles/ ncu dram bytes per node x N"
+    if prec == "fp64" and name in DFMA:
+        g = DFMA[name] * n / (per_launch * 1e-3) / 1e9
+        out["fp64_issue"] = {"achieved_gfma_s": g, "peak_gfma_s": DFMA_PEAK_GFMA,
+                             "frac": g / DFMA_PEAK_GFMA, "dfma_per_node": DFMA[name]}
+    return out
+
+
+def ncu_traffic(kernel, prec):
+    """DRAM bytes per node of one launch from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / ("ncu_%s_%s.md" % (kernel, prec))
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_node:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def cpu_baseline_oracle(n_side, steps, nthreads):
+    """The oracle's rhs! + SSP-RK3 on the host cores over a bounded number of steps."""
+    from oracle import oracle as O
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(n_side)
+    n = pts.shape[0]
+    idx, _, _, davg = O.knn(pts, K_STENCIL, period=per, nthreads=nthreads)
+    rowptr = np.arange(n + 1, dtype=np.int64) * K_STENCIL
+    w = O.weights(pts, rowptr, idx.ravel(), period=per, nthreads=nthreads)
+    ops = O.operators_from_stencils(n, rowptr, idx.ravel(), w)
+    semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=(O.SRC_RV,), h=davg)
+    u0 = W.isentropic_vortex(pts, 0.0)
+    hist = O.History(semi, 3)
+    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, 1, history=hist, nthreads=nthreads)  # warm-up
+    t0 = time.perf_counter()
+    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, steps, history=hist, nthreads=nthreads)
+    sec = time.perf_counter() - t0
+    return n * RHS_PER_STEP * steps / sec, sec
+
+
+def run_reference(args):
+    ws, rank, local, pg = dist_setup()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    n = args.n_side ** 2
+    from oracle import oracle as O
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(args.n_side)
+    idx, _, _, davg = O.knn(pts, K_STENCIL, period=per, nthreads=nthreads)
+    rowptr = np.arange(n + 1, dtype=np.int64) * K_STENCIL
+    w = O.weights(pts, rowptr, idx.ravel(), period=per, nthreads=nthreads)
+    ops = O.operators_from_stencils(n, rowptr, idx.ravel(), w)
+    semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=(O.SRC_RV,), h=davg)
+    u0 = W.isentropic_vortex(pts, 0.0)
+    hist = O.History(semi, 3)
+    dt = DT_FACTOR * h
+    u, t = O.ssprk33(semi, u0, 0.0, dt, args.warmup, history=hist, nthreads=nthreads)
+    t0 = time.perf_counter()
+    O.ssprk33(semi, u, t, dt, args.steps, history=hist, nthreads=nthreads)
+    sec = time.perf_counter() - t0
+    value = n * RHS_PER_STEP * args.steps / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3 / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(n, "fp64"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "full workload, %d SSP-RK3 steps after %d warm-up"
+                                   % (args.steps, args.warmup)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C restatement of the reference rhs! (Julia is not installed); OpenMP over rows",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(n, prec):
+    return {"workload": "2D Euler isentropic vortex, periodic [-5,5]^2, N=%d jittered nodes, "
+                        "PHS r^3 + degree-3 polynomials, k=%d, residual viscosity + history "
+                        "(order 3), SSP-RK3 dt=0.2h; one step = 3 rhs! evaluations" % (n, K_STENCIL),
+            "nodes": n, "stencil": K_STENCIL, "precision": prec,
+            "l2": "inputs larger than L2 (operator arrays ~%d MB)" % (n * K_STENCIL * 40 // 2 ** 20),
+            "parallelism": "replicas"}
+
+
+def run_ours(args):
+    ws, rank, local, pg = dist_setup()
+    peaks = load_peaks()
+    n = args.n_side ** 2
+    semi, domain, u0, dt = build_problem(args.n_side, "fp64", local)
+    ctx = domain.ctx
+    clocks = Clocks(local) if rank == 0 else None
+    ms, prof, clk = timed_steps(ctx, u0, dt, args.warmup, args.steps, pg, clocks)
+    ms_max = max_over_ranks(pg, ms)
+    value = n * RHS_PER_STEP * args.steps * ws / (ms_max * 1e-3)
+    launches = sum(v[1] for v in prof.values())
+    roof = roofline(prof, n, "fp64", peaks)
+    u64, _ = ctx.get_state()
+
+    # FP32-apply form on the same workload and steps
+    semi32, dom32, _, _ = build_problem(args.n_side, "fp32", local)
+    ms32, prof32, _ = timed_steps(dom32.ctx, u0, dt, args.warmup, args.steps, pg)
+    u32, _ = dom32.ctx.get_state()
+    ms32_max = max_over_ranks(pg, ms32)
+    # same number of steps from u0 in both forms: L2 density error of FP32 vs FP64
+    l2 = float(np.linalg.norm(u32[0] - u64[0]) / np.linalg.norm(u64[0]))
+    linf = float(np.abs(u32[0] - u64[0]).max() / np.abs(u64[0]).max())
+    value32 = n * RHS_PER_STEP * args.steps * ws / (ms32_max * 1e-3)
+    roof32 = roofline(prof32, n, "fp32", peaks)
+    dom32.ctx.close()
+
+    # end to end through the host entry point: every step uploads u from pinned host
+    # memory and downloads the new state
+    import torch
+    pinned = torch.empty((4, n), dtype=torch.float64, pin_memory=True)
+    uh = pinned.numpy()
+    uh[:] = u0
+    ctx.history_init(3)
+    t = ctx.ssprk33_host(uh, 0.0, dt, 1)
+    barrier(pg)
+    ctx.region_begin()
+    for _ in range(args.steps):
+        t = ctx.ssprk33_host(uh, t, dt, 1)
+    ms_e2e = max_over_ranks(pg, ctx.region_end())
+    e2e = n * RHS_PER_STEP * args.steps * ws / (ms_e2e * 1e-3)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        cpu_steps = 2
+        v, sec = cpu_baseline_oracle(args.n_side, cpu_steps, nthreads)
+        cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": "full N=%d, %d SSP-RK3 steps (%.1f s), oracle rhs! with OpenMP"
+                         % (n, cpu_steps, sec)}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(n, "fp64"),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * n * 8,
+                "d2h_bytes_per_step": 4 * n * 8, "entry_point": "mft_ssprk33_host"},
+        "gpu_launches": launches,
+        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
+        "clocks": clk,
+        "fp32_apply": {"value": value32, "unit": UNIT, "speedup_vs_fp64": value32 / value,
+                       "l2_density_err_vs_fp64": l2, "linf_density_err_vs_fp64": linf,
+                       "steps": args.steps, "roofline": roof32,
+                       "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

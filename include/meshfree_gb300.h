@@ -189,6 +189,28 @@ mft_status mft_set_rv_state(mft_ctx* ctx, const double* const* approx_du, int nv
 /* Viscosity of the last RV/upwind source evaluation (host, n values). */
 mft_status mft_get_viscosity(mft_ctx* ctx, double* eps);
 
+/* ---------------------------------------------------------------- timing
+ * Device timing with CUDA events on the context stream (the reference wraps the
+ * same phases in @trixi_timeit timers, rbfsolver.jl:400-425). */
+
+/* Kernel kinds reported by mft_profile_get. */
+enum {
+  MFT_K_BC = 0, MFT_K_FLUX, MFT_K_FWD, MFT_K_MEAN, MFT_K_LEXMAX, MFT_K_EPS, MFT_K_REV,
+  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_COUNT
+};
+
+/* enable != 0 starts recording an event pair around every kernel launch (and clears
+ * the accumulated totals); 0 stops recording. */
+mft_status mft_profile(mft_ctx* ctx, int enable);
+/* Totals since mft_profile(ctx, 1) for one kernel kind: summed device milliseconds,
+ * launch count and a static name. */
+mft_status mft_profile_get(mft_ctx* ctx, int kind, double* total_ms, int64_t* launches,
+                           const char** name);
+/* begin != 0: records the start event of a timed region on the context stream;
+ * begin == 0: records the stop event, waits for it and returns the region's device
+ * time in *ms. */
+mft_status mft_region(mft_ctx* ctx, int begin, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

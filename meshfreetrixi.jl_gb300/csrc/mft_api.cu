@@ -90,6 +90,51 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
 
 namespace mft {
 
+static cudaEvent_t pool_event(mft_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  MFT_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+ProfScope::ProfScope(mft_ctx* ctx, int k) : c(ctx), kind(k) {
+  if (!c->prof_on) return;
+  e1 = pool_event(c);
+  MFT_CUDA(cudaEventRecord(e1, c->stream));
+}
+
+ProfScope::~ProfScope() {
+  if (!c->prof_on || !e1) return;
+  cudaEvent_t e2 = nullptr;
+  if (!c->ev_pool.empty()) {
+    e2 = c->ev_pool.back();
+    c->ev_pool.pop_back();
+  } else if (cudaEventCreate(&e2) != cudaSuccess) {
+    c->ev_pool.push_back(e1);
+    return;
+  }
+  cudaEventRecord(e2, c->stream);
+  c->prof_pending.push_back({kind, {e1, e2}});
+}
+
+static void prof_drain(mft_ctx* c) {
+  if (c->prof_pending.empty()) return;
+  MFT_CUDA(cudaStreamSynchronize(c->stream));
+  for (auto& p : c->prof_pending) {
+    float ms = 0.f;
+    MFT_CUDA(cudaEventElapsedTime(&ms, p.second.first, p.second.second));
+    c->prof_ms[p.first] += ms;
+    c->prof_n[p.first] += 1;
+    c->ev_pool.push_back(p.second.first);
+    c->ev_pool.push_back(p.second.second);
+  }
+  c->prof_pending.clear();
+}
+
 void finish_pattern(mft_ctx* c) {
   const int64_t n = c->n;
   const int64_t nnz = c->rp[n];
@@ -293,7 +338,10 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   ep.u_s = us;
 
   // 1. strong BCs, pass 1 (mutates u)
-  if (c->nb > 0) launch_bc_pass1(c->nb, c->d_bnode.p, V, c->eq, bc, us, us32, s);
+  if (c->nb > 0) {
+    ProfScope ps(c, MFT_K_BC);
+    launch_bc_pass1(c->nb, c->d_bnode.p, V, c->eq, bc, us, us32, s);
+  }
 
   // sources: at most one viscosity source and one hyperviscosity source
   int iv = -1, ih = -1;
@@ -315,7 +363,10 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   if (flyer) MFT_REQUIRE(c->have_val[kSlotHv], MFT_ERR_STATE, "Flyer HV needs MFT_OP_HV");
 
   // 2. flux per node (FP64 Euler)
-  if (!f32) launch_flux_f64(n, c->eq, V, c->gamma, us, c->F.p, s);
+  if (!f32 && c->eq == MFT_EQ_EULER2D) {
+    ProfScope ps(c, MFT_K_FLUX);
+    launch_flux_f64(n, c->eq, V, c->gamma, us, c->F.p, s);
+  }
 
   // 3. forward gather
   FwdArgs fa{};
@@ -349,7 +400,10 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   fa.q32 = c->q32.p;
   fa.final_epilogue = (iv < 0 && !tominec);
   fa.ep = ep;
-  launch_fwd(c, fa);
+  {
+    ProfScope ps(c, MFT_K_FWD);
+    launch_fwd(c, fa);
+  }
   if (fa.final_epilogue) return;
 
   RevArgs ra{};
@@ -382,6 +436,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     r1.du_p_out = c->du_p2.p;
     r1.du_p_out32 = c->du_p2_32.p;
     r1.ep = ep;
+    ProfScope ps(c, MFT_K_REV_LAP);
     launch_rev(c, r1);
     dp = c->du_p2.p;
     dp32 = c->du_p2_32.p;
@@ -393,8 +448,12 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     const int mode = kind == MFT_SRC_RV ? (int)par[3] : 0;
     if (kind == MFT_SRC_RV) {
       const double denom = mode == 0 ? (double)n * V : (double)n;
-      launch_mean(n, V, us, denom, c->red_partial.p, c->red_counter.p, c->mean.p,
-                  c->red_blocks, s);
+      {
+        ProfScope ps(c, MFT_K_MEAN);
+        launch_mean(n, V, us, denom, c->red_partial.p, c->red_counter.p, c->mean.p,
+                    c->red_blocks, s);
+      }
+      ProfScope ps(c, MFT_K_LEXMAX);
       launch_lexmax(n, V, us, c->mean.p, mode, c->red_partial.p, c->red_counter.p + 1,
                     c->norms.p, c->red_blocks, s);
     }
@@ -419,6 +478,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ea.t = f32 ? nullptr : c->t.p;
     ea.t32 = f32 ? c->t32.p : nullptr;
     ea.eps = c->eps.p;
+    ProfScope ps(c, MFT_K_EPS);
     launch_eps(ea, s);
   }
 
@@ -431,6 +491,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   r2.final_epilogue = 1;
   r2.du_p_out = nullptr;
   r2.ep = ep;
+  ProfScope ps(c, MFT_K_REV);
   launch_rev(c, r2);
 }
 
@@ -508,6 +569,7 @@ void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
   for (int k = slots - 1; k > 0; --k) c->hist_t[k] = c->hist_t[k - 1];
   c->hist_t[0] = t;
   c->hist_head = (c->hist_head + slots - 1) % slots;
+  ProfScope ps(c, MFT_K_HISTORY);
   MFT_CUDA(cudaMemcpyAsync(c->hist[c->hist_head].p, u_aos, nv * sizeof(double),
                            cudaMemcpyDeviceToDevice, s));
   const int m = std::min(success_iter + 1, slots);
@@ -577,6 +639,13 @@ mft_status mft_ctx_destroy(mft_ctx* c) {
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
   }
+  for (auto& p : c->prof_pending) {
+    cudaEventDestroy(p.second.first);
+    cudaEventDestroy(p.second.second);
+  }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  for (auto e : c->region_ev)
+    if (e) cudaEventDestroy(e);
   delete c;
   return MFT_OK;
 }
@@ -1079,6 +1148,50 @@ mft_status mft_set_rv_state(mft_ctx* c, const double* const* approx_du, int nvar
     c->success_iter = success_iter;
     c->fsal_valid = false;
     MFT_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+mft_status mft_profile(mft_ctx* c, int enable) {
+  return guarded(c, [&] {
+    set_device(c);
+    prof_drain(c);
+    for (int k = 0; k < MFT_K_COUNT; ++k) {
+      c->prof_ms[k] = 0.0;
+      c->prof_n[k] = 0;
+    }
+    c->prof_on = enable != 0;
+  });
+}
+
+mft_status mft_profile_get(mft_ctx* c, int kind, double* total_ms, int64_t* launches,
+                           const char** name) {
+  static const char* names[MFT_K_COUNT] = {"bc_pass1", "flux", "fwd_gather", "mean",
+                                           "lexmax", "eps", "rev_gather", "rev_lap",
+                                           "history", "layout"};
+  return guarded(c, [&] {
+    MFT_REQUIRE(kind >= 0 && kind < MFT_K_COUNT, MFT_ERR_ARG, "bad kernel kind");
+    set_device(c);
+    prof_drain(c);
+    if (total_ms) *total_ms = c->prof_ms[kind];
+    if (launches) *launches = c->prof_n[kind];
+    if (name) *name = names[kind];
+  });
+}
+
+mft_status mft_region(mft_ctx* c, int begin, double* ms) {
+  return guarded(c, [&] {
+    set_device(c);
+    for (auto& e : c->region_ev)
+      if (!e) MFT_CUDA(cudaEventCreate(&e));
+    if (begin) {
+      MFT_CUDA(cudaEventRecord(c->region_ev[0], c->stream));
+    } else {
+      MFT_CUDA(cudaEventRecord(c->region_ev[1], c->stream));
+      MFT_CUDA(cudaEventSynchronize(c->region_ev[1]));
+      float t = 0.f;
+      MFT_CUDA(cudaEventElapsedTime(&t, c->region_ev[0], c->region_ev[1]));
+      if (ms) *ms = t;
+    }
   });
 }
 

@@ -100,7 +100,26 @@ struct mft_ctx {
   int hist_head = 0;
   int success_iter = 0;
   mft::DBuf<double> hist_w;
+
+  // timing
+  bool prof_on = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  double prof_ms[MFT_K_COUNT] = {};
+  int64_t prof_n[MFT_K_COUNT] = {};
+  cudaEvent_t region_ev[2] = {nullptr, nullptr};
 };
+
+namespace mft {
+// Event pair around one kernel launch when profiling is on.
+struct ProfScope {
+  mft_ctx* c;
+  int kind;
+  cudaEvent_t e1 = nullptr;
+  ProfScope(mft_ctx* ctx, int k);
+  ~ProfScope();
+};
+}  // namespace mft
 
 namespace mft {
 // Builds (if needed) the device ELL layouts and operator values.

@@ -93,13 +93,16 @@ __device__ __forceinline__ double min_image(double d, double L) {
   return d;
 }
 
-// first index of the largest |x| among lanes' candidates (value, index)
-__device__ __forceinline__ void warp_argmax(double& v, int& i) {
+// first index of the largest |x| among lanes' candidates (value, index).  Lanes
+// start from (-1, sentinel); if no candidate compares (all NaN) the result falls
+// back to index `lo` so that every later access stays inside the system.
+__device__ __forceinline__ void warp_argmax(double& v, int& i, int lo) {
   for (int o = 16; o > 0; o >>= 1) {
     const double v2 = __shfl_xor_sync(kFull, v, o);
     const int i2 = __shfl_xor_sync(kFull, i, o);
     if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
   }
+  if (i == (1 << 30)) { i = lo; v = NAN; }
 }
 
 __device__ __forceinline__ double warp_max(double v) {
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           const double x = fabs(AM(i, kk));
           if (x > v) { v = x; iv = i; }
         }
-        warp_argmax(v, iv);
+        warp_argmax(v, iv, 1);
         colmax = v;
         imax = iv;
       }
@@ -239,7 +242,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
             const double x = fabs(AM(imax, j));
             if (x > v) { v = x; iv = j; }
           }
-          warp_argmax(v, iv);
+          warp_argmax(v, iv, 1);
           double rowmax = v;
           if (imax > 1) {
             double v2 = -1.0;
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
               const double x = fabs(AM(j, imax));
               if (x > v2) { v2 = x; iv2 = j; }
             }
-            warp_argmax(v2, iv2);
+            warp_argmax(v2, iv2, 1);
             rowmax = fmax(rowmax, v2);
           }
           if (absakk >= alpha * colmax * (colmax / rowmax)) kp = kk;

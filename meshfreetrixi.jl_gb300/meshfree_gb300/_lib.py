@@ -52,7 +52,12 @@ SIGNATURES = {
     "mft_ssprk33_host": (I32, [VP, VP, I32, C.POINTER(DBL), DBL, I32]),
     "mft_set_rv_state": (I32, [VP, VP, I32, I32]),
     "mft_get_viscosity": (I32, [VP, VP]),
+    "mft_profile": (I32, [VP, I32]),
+    "mft_profile_get": (I32, [VP, I32, C.POINTER(DBL), C.POINTER(I64), C.POINTER(C.c_char_p)]),
+    "mft_region": (I32, [VP, I32, C.POINTER(DBL)]),
 }
+K_NAMES = ["bc_pass1", "flux", "fwd_gather", "mean", "lexmax", "eps", "rev_gather", "rev_lap",
+           "history", "layout"]
 
 _lib = None
 
@@ -231,3 +236,25 @@ class Context:
 
     def sync(self):
         self.check(self.lib.mft_sync(self.h))
+
+    # timing ---------------------------------------------------------------
+    def profile(self, enable=True):
+        self.check(self.lib.mft_profile(self.h, 1 if enable else 0))
+
+    def profile_report(self):
+        """{kernel name: (total device ms, launches)} since profile(True)."""
+        out = {}
+        for k in range(len(K_NAMES)):
+            ms, n, name = C.c_double(), C.c_int64(), C.c_char_p()
+            self.check(self.lib.mft_profile_get(self.h, k, C.byref(ms), C.byref(n), C.byref(name)))
+            if n.value:
+                out[name.value.decode()] = (ms.value, n.value)
+        return out
+
+    def region_begin(self):
+        self.check(self.lib.mft_region(self.h, 1, None))
+
+    def region_end(self):
+        ms = C.c_double()
+        self.check(self.lib.mft_region(self.h, 0, C.byref(ms)))
+        return ms.value
