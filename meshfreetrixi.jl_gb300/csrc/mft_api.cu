@@ -580,12 +580,11 @@ void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
   double w[16];
   MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
               "time_deriv_weights: singular Vandermonde system");
-  // Weights go through a small device buffer so that later launches may reuse it.
-  MFT_CUDA(cudaMemcpyAsync(c->hist_w.p, w, m * sizeof(double), cudaMemcpyHostToDevice, s));
-  MFT_CUDA(cudaStreamSynchronize(s));
+  HistW hw{};
+  for (int k = 0; k < m; ++k) hw.w[k] = w[k];
   const double* hs[8];
   for (int k = 0; k < m; ++k) hs[k] = c->hist[(c->hist_head + k) % slots].p;
-  launch_history((int64_t)nv, m, c->hist_w.p, hs, c->approx_du.p, s);
+  launch_history((int64_t)nv, m, hw, hs, c->approx_du.p, s);
 }
 
 void check_state_ready(mft_ctx* c) {

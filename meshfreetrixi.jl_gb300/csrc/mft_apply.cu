@@ -222,25 +222,6 @@ __device__ __forceinline__ int jl_isless(double a, double b) {
   if (a > b) return 0;
   return signbit(a) && !signbit(b);
 }
-__device__ __forceinline__ int jl_isequal(double a, double b) {
-  if (isnan(a) || isnan(b)) return isnan(a) && isnan(b);
-  return a == b && signbit(a) == signbit(b);
-}
-template <int V>
-__device__ __forceinline__ int vec_isless(const double* a, const double* b) {
-#pragma unroll
-  for (int k = 0; k < V; ++k)
-    if (!jl_isequal(a[k], b[k])) return jl_isless(a[k], b[k]);
-  return 0;
-}
-// Base.max on vectors: max(a, b) = isless(b, a) ? a : b  (lexicographic).
-template <int V>
-__device__ __forceinline__ void vmax_into(double* a, const double* b) {
-  if (!vec_isless<V>(b, a)) {
-#pragma unroll
-    for (int k = 0; k < V; ++k) a[k] = b[k];
-  }
-}
 __device__ __forceinline__ double jl_max(double a, double b) {
   if (isnan(a) || isnan(b)) return a + b;
   return jl_isless(a, b) ? b : a;
@@ -250,8 +231,8 @@ __device__ __forceinline__ double jl_min(double a, double b) {
   return jl_isless(b, a) ? b : a;
 }
 
-// Sum of u per variable; the last block to finish sums the block partials in block
-// order (deterministic) and writes mean = sum / denom.
+// Sum of u per variable; the last block to finish reduces the block partials with a
+// fixed strided-then-tree order (deterministic) and writes mean = sum / denom.
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __restrict__ u,
                                                  double denom, double* partial,
@@ -273,80 +254,109 @@ __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __rest
     last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x < V) {
-    __threadfence();
-    double s = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(partial + b * V + threadIdx.x);
-    mean[threadIdx.x] = s / denom;
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < V; ++k) acc[k] = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock)
+#pragma unroll
+    for (int k = 0; k < V; ++k) acc[k] += __ldcg(partial + b * V + k);
+  block_sum<V>(acc);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) mean[k] = acc[k] / denom;
+    *counter = 0u;
   }
-  if (last && threadIdx.x == 0) *counter = 0u;
 }
 
-// ode_maximum(|u - mean|): lexicographic (max_mode 0) or per component (1); zero
-// entries become eps() (update_residual_visc!, hyperviscosity.jl:310-311).
+// ode_maximum(|u - mean|) (mpi.jl:61-81): lexicographic Base.isless order on vectors
+// (max_mode 0) or per component (1); zero entries become eps() (update_residual_visc!,
+// hyperviscosity.jl:310-311).  |u - mean| >= 0, so the IEEE bit pattern of every
+// component orders like its value (NaN above +Inf, as Base.isless does): the maximum
+// is taken on 64-bit integer keys.
+typedef unsigned long long u64;
+
+template <int V>
+__device__ __forceinline__ bool key_less(const u64* a, const u64* b) {
+#pragma unroll
+  for (int k = 0; k < V; ++k)
+    if (a[k] != b[k]) return a[k] < b[k];
+  return false;
+}
+
+// max(a, b) = isless(b, a) ? a : b, written into a.
+template <int V>
+__device__ __forceinline__ void key_max_into(u64* a, const u64* b, int max_mode) {
+  if (max_mode == 0) {
+    if (!key_less<V>(b, a)) {
+#pragma unroll
+      for (int k = 0; k < V; ++k) a[k] = b[k];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < V; ++k) a[k] = a[k] < b[k] ? b[k] : a[k];
+  }
+}
+
+template <int V>
+__device__ void block_keymax(u64* best, int max_mode) {
+  __shared__ u64 sh[kBlock][V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) sh[threadIdx.x][k] = best[k];
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) key_max_into<V>(sh[threadIdx.x], sh[threadIdx.x + s], max_mode);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < V; ++k) best[k] = sh[0][k];
+  __syncthreads();
+}
+
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __restrict__ u,
                                                    const double* __restrict__ mean, int max_mode,
                                                    double* partial, unsigned* counter,
                                                    double* norms) {
-  double m[V], best[V];
+  double m[V];
+  u64 best[V];
 #pragma unroll
-  for (int k = 0; k < V; ++k) { m[k] = mean[k]; best[k] = -1.0; }
-  bool have = false;
+  for (int k = 0; k < V; ++k) { m[k] = mean[k]; best[k] = 0ull; }
+  // Threads without nodes keep the all-zero key, the smallest possible: it can only
+  // tie with a real all-zero vector, which has the same value.
   for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kBlock) {
-    double x[V];
+    u64 x[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) x[k] = fabs(dsub(u[i * V + k], m[k]));
-    if (!have) {
-#pragma unroll
-      for (int k = 0; k < V; ++k) best[k] = x[k];
-      have = true;
-    } else if (max_mode == 0) {
-      vmax_into<V>(best, x);
-    } else {
-#pragma unroll
-      for (int k = 0; k < V; ++k) best[k] = jl_max(best[k], x[k]);
-    }
+    for (int k = 0; k < V; ++k) x[k] = (u64)__double_as_longlong(fabs(dsub(u[i * V + k], m[k])));
+    key_max_into<V>(best, x, max_mode);
   }
-  // Entries of threads without nodes stay at -1 and never win (values are >= 0).
-  __shared__ double sh[kBlock][V];
-#pragma unroll
-  for (int k = 0; k < V; ++k) sh[threadIdx.x][k] = best[k];
-  __syncthreads();
-  for (int s = kBlock / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      double* a = sh[threadIdx.x];
-      const double* b = sh[threadIdx.x + s];
-      if (max_mode == 0) vmax_into<V>(a, b);
-      else
-        for (int k = 0; k < V; ++k) a[k] = jl_max(a[k], b[k]);
-    }
-    __syncthreads();
-  }
+  block_keymax<V>(best, max_mode);
   __shared__ int last;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = sh[0][k];
+    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = __longlong_as_double((long long)best[k]);
     __threadfence();
     last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double b[V];
+  if (!last) return;
+  __threadfence();
 #pragma unroll
-    for (int k = 0; k < V; ++k) b[k] = __ldcg(partial + k);
-    for (unsigned blk = 1; blk < gridDim.x; ++blk) {
-      double c[V];
+  for (int k = 0; k < V; ++k) best[k] = 0ull;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock) {
+    u64 c[V];
 #pragma unroll
-      for (int k = 0; k < V; ++k) c[k] = __ldcg(partial + blk * V + k);
-      if (max_mode == 0) vmax_into<V>(b, c);
-      else
-        for (int k = 0; k < V; ++k) b[k] = jl_max(b[k], c[k]);
+    for (int k = 0; k < V; ++k) c[k] = (u64)__double_as_longlong(__ldcg(partial + b * V + k));
+    key_max_into<V>(best, c, max_mode);
+  }
+  block_keymax<V>(best, max_mode);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const double v = __longlong_as_double((long long)best[k]);
+      norms[k] = v == 0.0 ? 2.220446049250313e-16 : v;
     }
-#pragma unroll
-    for (int k = 0; k < V; ++k) norms[k] = b[k] == 0.0 ? 2.220446049250313e-16 : b[k];
     *counter = 0u;
   }
 }
@@ -460,7 +470,7 @@ __global__ void __launch_bounds__(kBlock) k_rev_f64(RevArgs a) {
 
 // ------------------------------------------------------------------ history
 
-__global__ void k_history(int64_t count, int m, const double* __restrict__ w, const double* h0,
+__global__ void k_history(int64_t count, int m, HistW w, const double* h0,
                           const double* h1, const double* h2, const double* h3,
                           const double* h4, const double* h5, const double* h6,
                           const double* h7, double* __restrict__ out) {
@@ -469,7 +479,7 @@ __global__ void k_history(int64_t count, int m, const double* __restrict__ w, co
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
   // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
   double acc = 0.0;
-  for (int k = 0; k < m; ++k) acc = dadd(acc, dmul(w[k], hs[k][i]));
+  for (int k = 0; k < m; ++k) acc = dadd(acc, dmul(w.w[k], hs[k][i]));
   out[i] = acc;
 }
 
@@ -600,7 +610,7 @@ void launch_differs(const double* a, const double* b, int64_t count, int* flag, 
   MFT_LAUNCH_CHECK();
 }
 
-void launch_history(int64_t count, int m, const double* w, const double* const* hist,
+void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
                     double* approx_du, cudaStream_t s) {
   if (count <= 0) return;
   const double* h[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

@@ -214,7 +214,10 @@ void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s);
 
 // approx_du = sum_i w_i * hist_i (history ring, FP64) and push of the newest state.
-void launch_history(int64_t count, int m, const double* w, const double* const* hist,
+struct HistW {
+  double w[8];
+};
+void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
                     double* approx_du, cudaStream_t s);
 
 }  // namespace mft
