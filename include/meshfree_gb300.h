@@ -108,6 +108,26 @@ mft_status mft_set_stencils(mft_ctx* ctx, const int64_t* rowptr, const int32_t* 
 mft_status mft_weights(mft_ctx* ctx, int op, int rbf_pow, int polydeg, int deriv_order,
                        double* out_w, double* out_max_resid);
 
+/* Allocation-free weights (no counterpart in the reference).  For callers that cannot
+ * allocate device memory during the solve -- code running inside a stream-ordered pool
+ * it does not own, or a host whose allocator must not be bypassed by cudaMalloc (which
+ * also synchronises the device).  Same numbers as mft_weights(MFT_OP_GRAD ...) on the
+ * same stencils, without a context: every input and output is caller-owned device
+ * memory (xyz n*dim, rowptr n+1, cols rowptr[n] with centre first, w rowptr[n]*dim in
+ * stencil order [slot][axis]); period is a host array of dim lengths or NULL; stream
+ * may be 0.  kmax: the caller's bound on the stencil size; kmax + number of monomials
+ * must be <= 118 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  A
+ * stencil longer than kmax is skipped and reported as MFT_ERR_ARG.  The only global
+ * scratch is a 32-byte static device array per GPU; its address is looked up on the
+ * first call on each device (make that call before any stream capture), and it is
+ * reset at the start of every call.  Calls that overlap on the GPU (other streams,
+ * other host threads) share that array and race.  Blocks until the solve finished.
+ * err (may be NULL) receives a message of at most err_len bytes. */
+mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz, const double* period,
+                               const int64_t* rowptr, const int32_t* cols, int kmax,
+                               int rbf_pow, int polydeg, int deriv_order, double* w,
+                               void* stream, char* err, int err_len);
+
 /* Loads one component of an operator from the reference's SparseMatrixCSC arrays
  * (1-based colptr[n+1], rowval[nnz], nzval[nnz]), e.g.
  * semi.cache.rbf_differentiation_matrices[comp+1] (rbfsolver.jl:139).  All loaded

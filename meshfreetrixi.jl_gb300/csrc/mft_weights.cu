@@ -18,8 +18,12 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <string.h>
+
 #include <algorithm>
+#include <mutex>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "mft_ctx.h"
@@ -119,6 +123,9 @@ __device__ __forceinline__ void tri_ij(int t, int& i, int& j) {
   i = t - jj * (jj + 1) / 2;
 }
 
+// kOrdered: systems are taken in the order of a.order_list (largest first); otherwise
+// in node order.
+template <bool kOrdered>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
@@ -139,12 +146,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
     if (lane == 0) job = atomicAdd(a.next, 1ull);
     job = __shfl_sync(kFull, job, 0);
     if (job >= (unsigned long long)a.nsys) break;
-    const int64_t e = a.order_list[job];
+    const int64_t e = kOrdered ? a.order_list[job] : (int64_t)job;
     const int64_t rb = a.rowptr[e];
     const int k = (int)(a.rowptr[e + 1] - rb);
     const int n = k + a.npoly;
 #define AM(i, j) A[(size_t)((j)-1) * n + ((i)-1)]
 #define BM(i, c) B[(size_t)(c) * n + ((i)-1)]
+    if (!kOrdered && k > a.kmax) {
+      // caller-declared maximum stencil size exceeded: flag it and skip the system
+      if (lane == 0) atomicExch(reinterpret_cast<int*>(a.next + 2), 1);
+      continue;
+    }
     const int32_t* st = a.cols + rb;
     const int64_t ce = st[0];
     // shift_stencil
@@ -542,15 +554,15 @@ void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
   a.resid = max_resid ? d_res.p : nullptr;
   a.bad = d_bad.p;
   a.next = d_next.p;
-  MFT_CUDA(cudaFuncSetAttribute(k_weights, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
+  MFT_CUDA(cudaFuncSetAttribute(k_weights<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
   int dev = 0, sms = 0, per_sm = 0;
   MFT_CUDA(cudaGetDevice(&dev));
   MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights, 32 * kWarpsPerBlock, shmem));
+  MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<true>, 32 * kWarpsPerBlock, shmem));
   per_sm = std::max(per_sm, 1);
   const int64_t want = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
-  k_weights<<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
+  k_weights<true><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
   MFT_LAUNCH_CHECK();
   w_out.resize((size_t)nnz * dim);
   int bad = big;
@@ -573,3 +585,141 @@ void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
 }
 
 }  // namespace mft
+
+// ---------------------------------------------------------------- allocation-free variant
+//
+// mft_weights_noalloc is for callers that cannot allocate device memory while they
+// compute weights: a solver running inside a stream-ordered memory pool it does not own,
+// a host that has handed all device memory to its own allocator, or code that must not
+// call cudaMalloc/cudaFree because those calls synchronise the device.  The caller passes
+// every input and output as device memory; the only global scratch the solve needs (the
+// work counter and two status words) lives in the file-scope array below.
+
+namespace {
+
+// [0] work counter, [1] first node with a zero pivot (low 32 bits, 0x7F7F7F7F = none),
+// [2] oversize-stencil flag, [3] unused.  32 bytes on every GPU that loads the library,
+// held until the process exits.
+constexpr int kNoAllocWords = 4;
+static __device__ __align__(256) unsigned long long g_weights_scratch[kNoAllocWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_scratch_mu;
+unsigned long long* g_scratch_addr[kNoAllocMaxDevices] = {};
+
+void put_err(char* err, int len, const std::string& msg) {
+  if (err && len > 0) {
+    const size_t m = std::min<size_t>((size_t)len - 1, msg.size());
+    memcpy(err, msg.data(), m);
+    err[m] = '\0';
+  }
+}
+
+}  // namespace
+
+extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
+                                          const double* period, const int64_t* rowptr,
+                                          const int32_t* cols, int kmax, int rbf_pow,
+                                          int polydeg, int deriv_order, double* w,
+                                          void* stream, char* err, int err_len) {
+  using namespace mft;
+  put_err(err, err_len, "");
+  if (dim < 1 || dim > 3 || n < 1 || n > (int64_t)INT32_MAX || !xyz || !rowptr || !cols || !w ||
+      kmax < 1 || rbf_pow < 1 || rbf_pow > 15 || polydeg < 0 || polydeg > 6 || deriv_order < 1 ||
+      deriv_order > 8) {
+    put_err(err, err_len, "mft_weights_noalloc: invalid argument");
+    return MFT_ERR_ARG;
+  }
+  WArgs a{};
+  a.dim = dim;
+  a.npoly = make_monomials(dim, polydeg, a.mono, 128);
+  a.rbf_pow = rbf_pow;
+  a.order = deriv_order;
+  a.periodic = period ? 1 : 0;
+  for (int d = 0; d < 3; ++d) a.period[d] = (period && d < dim) ? period[d] : 0.0;
+  a.kmax = kmax;
+  a.nmax = kmax + a.npoly;
+  const size_t per = (size_t)a.nmax * a.nmax + (size_t)a.nmax * 3 + (size_t)kmax * 3 + a.nmax;
+  const size_t shmem = per * sizeof(double) * kWarpsPerBlock;
+  const size_t kMaxShmem = 227 * 1024;
+  if (a.npoly > 128 || shmem > kMaxShmem) {
+    put_err(err, err_len,
+            "mft_weights_noalloc: stencil size " + std::to_string(kmax) + " plus " +
+                std::to_string(a.npoly) + " monomials needs " + std::to_string(shmem) +
+                " bytes of shared memory; the maximum is " + std::to_string(kMaxShmem) +
+                " (kmax + monomials <= 118)");
+    return MFT_ERR_ARG;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    put_err(err, err_len, "mft_weights_noalloc: no current CUDA device");
+    return MFT_ERR_CUDA;
+  }
+  unsigned long long* scratch = nullptr;
+  {
+    // First call on this device (with it current): resolve the device address of the
+    // scratch array.  Later calls reuse it.  Make the first call before any capture.
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+      void* ptr = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&ptr, g_weights_scratch);
+      if (e != cudaSuccess || !ptr) {
+        put_err(err, err_len, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        return MFT_ERR_CUDA;
+      }
+      g_scratch_addr[dev] = reinterpret_cast<unsigned long long*>(ptr);
+    }
+    scratch = g_scratch_addr[dev];
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  // the counter and the status words must start from their initial values
+  if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(scratch + 1, 0x7F, sizeof(int), s) != cudaSuccess ||
+      cudaMemsetAsync(scratch + 2, 0, sizeof(unsigned long long), s) != cudaSuccess) {
+    put_err(err, err_len, "mft_weights_noalloc: cudaMemsetAsync failed");
+    return MFT_ERR_CUDA;
+  }
+  a.nsys = n;
+  a.order_list = nullptr;
+  a.rowptr = rowptr;
+  a.cols = cols;
+  a.xyz = xyz;
+  a.w_out = w;
+  a.resid = nullptr;
+  a.bad = reinterpret_cast<int*>(scratch + 1);
+  a.next = scratch;
+  int sms = 0, per_sm = 0;
+  if (cudaFuncSetAttribute(k_weights<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)shmem) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<false>,
+                                                    32 * kWarpsPerBlock, shmem) != cudaSuccess) {
+    put_err(err, err_len, "mft_weights_noalloc: kernel configuration failed");
+    return MFT_ERR_CUDA;
+  }
+  per_sm = std::max(per_sm, 1);
+  const int64_t want = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const unsigned grid =
+      (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
+  k_weights<false><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  int status[3] = {0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status[0], scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status[1], scratch + 2, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    put_err(err, err_len, std::string("mft_weights_noalloc: ") + cudaGetErrorString(e));
+    return MFT_ERR_CUDA;
+  }
+  if (status[1] != 0) {
+    put_err(err, err_len, "mft_weights_noalloc: a stencil is longer than kmax = " +
+                              std::to_string(kmax) + "; its weights were not computed");
+    return MFT_ERR_ARG;
+  }
+  if (status[0] != 0x7F7F7F7F) {
+    put_err(err, err_len, "mft_weights_noalloc: node " + std::to_string(status[0]) +
+                              " has an exactly zero pivot");
+    return MFT_ERR_SINGULAR;
+  }
+  return MFT_OK;
+}

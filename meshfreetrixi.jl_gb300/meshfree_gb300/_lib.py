@@ -37,6 +37,8 @@ SIGNATURES = {
     "mft_set_stencils": (I32, [VP, VP, VP]),
     "mft_weights": (I32, [VP, I32, I32, I32, I32, VP, C.POINTER(DBL)]),
     "mft_load_csc": (I32, [VP, I32, I32, I64, VP, VP, VP]),
+    "mft_weights_noalloc": (I32, [I32, I64, VP, VP, VP, VP, I32, I32, I32, I32, VP, VP,
+                                  C.c_char_p, I32]),
     "mft_set_equations": (I32, [VP, I32, VP]),
     "mft_set_bcs": (I32, [VP, I32, VP, VP, VP, VP]),
     "mft_set_dirichlet_values": (I32, [VP, VP]),
