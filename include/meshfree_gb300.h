@@ -170,6 +170,14 @@ mft_status mft_set_sources(mft_ctx* ctx, int n_src, const int* kinds, const doub
 
 mft_status mft_set_precision(mft_ctx* ctx, int precision);
 
+/* Engine options.  MFT_OPT_GATHER selects the mapping of the FP32 operator gathers:
+ * MFT_GATHER_THREAD (one node per thread, direct loads), MFT_GATHER_STAGED (one warp
+ * per 32-node slice with the slice's indices and weights streamed into shared memory by
+ * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
+enum { MFT_OPT_GATHER = 0 };
+enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2 };
+mft_status mft_set_option(mft_ctx* ctx, int option, int value);
+
 /* ---------------------------------------------------------------- rhs! */
 
 /* du = rhs!(u, t) with host StructArray-style arrays (nvars pointers of length n).

@@ -204,6 +204,10 @@ void ensure_work(mft_ctx* c) {
   c->soa2.alloc(nv);
   c->work_u.alloc(nv);
   c->work_du.alloc(nv);
+  if (!c->kerr.p) {
+    c->kerr.alloc(1);
+    c->kerr.zero(c->stream);
+  }
   if (c->red_blocks == 0) {
     c->red_blocks = 512;
     c->red_partial.alloc((size_t)c->red_blocks * 8);
@@ -312,13 +316,39 @@ static void refresh_dirichlet(mft_ctx* c, double t) {
   MFT_CUDA(cudaStreamSynchronize(c->stream));
 }
 
+static bool staged_gathers(mft_ctx* c) {
+  return c->gather_mode == MFT_GATHER_STAGED ||
+         (c->gather_mode == MFT_GATHER_AUTO && c->precision == MFT_PREC_FP32);
+}
+
 void launch_fwd(mft_ctx* c, const FwdArgs& a) {
-  if (c->precision == MFT_PREC_FP32) launch_fwd_f32(a, c->stream);
-  else launch_fwd_f64(a, c->stream);
+  if (c->precision == MFT_PREC_FP32) {
+    if (staged_gathers(c) && launch_fwd_f32_tma(a, c->kerr.p, c->stream)) return;
+    launch_fwd_f32(a, c->stream);
+  } else {
+    launch_fwd_f64(a, c->stream);
+  }
 }
 void launch_rev(mft_ctx* c, const RevArgs& a) {
-  if (c->precision == MFT_PREC_FP32) launch_rev_f32(a, c->stream);
-  else launch_rev_f64(a, c->stream);
+  if (c->precision == MFT_PREC_FP32) {
+    if (staged_gathers(c) && launch_rev_f32_tma(a, c->kerr.p, c->stream)) return;
+    launch_rev_f32(a, c->stream);
+  } else {
+    launch_rev_f64(a, c->stream);
+  }
+}
+
+// Device error word set by kernels with bounded waits; read at synchronisation points.
+static void check_kernel_errors(mft_ctx* c) {
+  if (!c->kerr.p) return;
+  int e = 0;
+  MFT_CUDA(cudaMemcpyAsync(&e, c->kerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MFT_CUDA(cudaStreamSynchronize(c->stream));
+  if (e != 0) {
+    c->kerr.zero(c->stream);
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+    throw mft::Error(e, "a device wait gave up (bulk-copy completion not observed)");
+  }
 }
 
 void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_in) {
@@ -886,6 +916,18 @@ mft_status mft_set_sources(mft_ctx* c, int n_src, const int* kinds, const double
   });
 }
 
+mft_status mft_set_option(mft_ctx* c, int option, int value) {
+  return guarded(c, [&] {
+    if (option == MFT_OPT_GATHER) {
+      MFT_REQUIRE(value >= MFT_GATHER_AUTO && value <= MFT_GATHER_STAGED, MFT_ERR_ARG,
+                  "unknown gather mapping");
+      c->gather_mode = value;
+    } else {
+      throw mft::Error(MFT_ERR_ARG, "unknown option");
+    }
+  });
+}
+
 mft_status mft_set_precision(mft_ctx* c, int precision) {
   return guarded(c, [&] {
     MFT_REQUIRE(precision == MFT_PREC_FP64 || precision == MFT_PREC_FP32, MFT_ERR_ARG,
@@ -917,6 +959,7 @@ mft_status mft_rhs_device(mft_ctx* c, double* du, double* u, double t) {
     launch_soa_from_aos(c->work_du.p, du, n, V, s);
     launch_soa_from_aos(c->work_u.p, u, n, V, s);
     MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
   });
 }
 
@@ -951,6 +994,7 @@ mft_status mft_rhs(mft_ctx* c, double* const* du, double* const* u, int nvars, d
                                cudaMemcpyDeviceToHost, s));
     }
     MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
   });
 }
 
@@ -1081,6 +1125,7 @@ mft_status mft_ssprk33(mft_ctx* c, double dt, int nsteps, int use_graph) {
     set_device(c);
     ssprk33_run(c, dt, nsteps);
     MFT_CUDA(cudaStreamSynchronize(c->stream));
+    check_kernel_errors(c);
   });
 }
 
@@ -1124,6 +1169,7 @@ mft_status mft_ssprk33_host(mft_ctx* c, double* const* u, int nvars, double* t, 
       MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
     MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
     *t = c->t_state;
   });
 }

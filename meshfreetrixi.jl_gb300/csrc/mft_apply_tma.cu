@@ -1,0 +1,357 @@
+// FP32-apply gathers with bulk-copy staging (Euler, V = 4).
+//
+// The plain FP32 gathers are latency-bound: every stencil entry needs its column index
+// before the neighbour state can be loaded.  Here each warp owns one 32-row slice at a
+// time (persistent grid) and streams the slice's index and weight arrays into shared
+// memory in chunks of kCh slots with cp.async.bulk, two chunks ahead of use and
+// completed on an mbarrier.  The warp then issues the kCh neighbour-state gathers of a
+// chunk back to back, so only those (L1/L2-resident) loads remain on the critical path.
+// Waits are bounded: on a timeout the warp records MFT_ERR_TIMEOUT in *err, waits
+// (bounded) for its copies in flight and stops.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mft_device.cuh"
+#include "mft_internal.cuh"
+#include "mft_tma.cuh"
+
+namespace mft {
+
+namespace {
+
+using namespace dev;
+
+constexpr int kCh = 8;          // slots per staged chunk
+constexpr int kTmaWarps = 4;    // warps per block
+constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr int kChunkBytes = kCh * 32 * 4;  // one array, one chunk (int32 / float)
+
+__device__ __forceinline__ void euler_flux_f32(float gm1, float4 u, float* fx, float* fy) {
+  const float r = __frcp_rn(u.x);
+  const float v1 = u.y * r, v2 = u.z * r;
+  const float p = gm1 * (u.w - 0.5f * (u.y * v1 + u.z * v2));
+  const float ep = u.w + p;
+  fx[0] = u.y;
+  fx[1] = fmaf(u.y, v1, p);
+  fx[2] = u.y * v2;
+  fx[3] = ep * v1;
+  fy[0] = u.z;
+  fy[1] = u.z * v1;
+  fy[2] = fmaf(u.z, v2, p);
+  fy[3] = ep * v2;
+}
+
+// Warp-uniform cursor over (slice, chunk) pairs of this warp's slices.
+struct Cursor {
+  int64_t s;
+  int c;
+};
+
+__device__ __forceinline__ int slice_slots(const EllView& e, int64_t s) {
+  return (int)((e.slice_off[s + 1] - e.slice_off[s]) >> 5);
+}
+
+template <int NARR>
+__device__ __forceinline__ void issue_chunk(unsigned char (*buf)[kChunkBytes], uint64_t* bar,
+                                            const EllView& e, const void* const* arrs,
+                                            Cursor cur) {
+  const int slots = slice_slots(e, cur.s);
+  const int n = min(kCh, slots - cur.c * kCh);
+  const uint32_t bytes = (uint32_t)n * 32u * 4u;
+  const int64_t base = e.slice_off[cur.s] + (int64_t)cur.c * kCh * 32;
+  tma::fence_proxy_async();
+  tma::arrive_expect_tx(bar, bytes * NARR);
+#pragma unroll
+  for (int k = 0; k < NARR; ++k)
+    tma::bulk_g2s(buf[k], static_cast<const unsigned char*>(arrs[k]) + base * 4, bytes, bar);
+}
+
+__device__ __forceinline__ void advance(const EllView& e, Cursor& cur, int64_t stride) {
+  const int nch = (slice_slots(e, cur.s) + kCh - 1) / kCh;
+  if (++cur.c >= nch) {
+    cur.c = 0;
+    cur.s += stride;
+  }
+}
+
+template <bool WT, bool WQ, int FLY>
+__global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a, int* err) {
+  constexpr int NARR = (WQ || FLY) ? 4 : 3;
+  __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][kChunkBytes];
+  __shared__ __align__(8) uint64_t bars[kTmaWarps][2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nslices = (a.n + 31) >> 5;
+  const int64_t stride = (int64_t)gridDim.x * kTmaWarps;
+  const int64_t first = (int64_t)blockIdx.x * kTmaWarps + w;
+  const void* arrs[4] = {a.ell.col, a.w32[0], a.w32[1], a.wl32};
+  if (lane == 0) {
+    tma::bar_init(&bars[w][0], 1);
+    tma::bar_init(&bars[w][1], 1);
+    tma::fence_init();
+  }
+  __syncwarp();
+  const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
+  const float gm1 = (float)(a.gamma - 1.0);
+  const float hg = (float)a.hv_gamma;
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  Cursor iss{first, 0};
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    if (iss.s < nslices) {
+      if (lane == 0) issue_chunk<NARR>(sbuf[w][b], &bars[w][b], a.ell, arrs, iss);
+      pending[b] = true;
+      advance(a.ell, iss, stride);
+    }
+  }
+  int buf = 0;
+  for (int64_t s = first; s < nslices; s += stride) {
+    const int64_t i = (s << 5) + lane;
+    const bool valid = i < a.n;
+    const int len = valid ? a.ell.row_len[i] : 0;
+    const int slots = slice_slots(a.ell, s);
+    const int nch = (slots + kCh - 1) / kCh;
+    float f[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+    for (int c = 0; c < nch; ++c) {
+      if (!tma::wait_bounded(&bars[w][buf], phase[buf], kWaitLimit)) {
+        if (lane == 0) atomicExch(err, MFT_ERR_TIMEOUT);
+        for (int b = 0; b < 2; ++b)
+          if (pending[b]) tma::wait_bounded(&bars[w][b], phase[b], kWaitLimit);
+        return;
+      }
+      phase[buf] ^= 1u;
+      pending[buf] = false;
+      const int* scol = reinterpret_cast<const int*>(sbuf[w][buf][0]);
+      const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][1]);
+      const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][2]);
+      const float* swl = reinterpret_cast<const float*>(sbuf[w][buf][NARR - 1]);
+      const int j0 = c * kCh;
+      float4 uc[kCh];
+#pragma unroll
+      for (int k = 0; k < kCh; ++k)
+        if (j0 + k < len) uc[k] = __ldg(U4 + scol[k * 32 + lane]);
+#pragma unroll
+      for (int k = 0; k < kCh; ++k) {
+        if (j0 + k < len) {
+          const float wx = swx[k * 32 + lane], wy = swy[k * 32 + lane];
+          float fx[4], fy[4];
+          euler_flux_f32(gm1, uc[k], fx, fy);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) f[v] = fmaf(wy, fy[v], fmaf(wx, fx[v], f[v]));
+          if (WT) {
+            tx[0] = fmaf(wx, uc[k].x, tx[0]); tx[1] = fmaf(wx, uc[k].y, tx[1]);
+            tx[2] = fmaf(wx, uc[k].z, tx[2]); tx[3] = fmaf(wx, uc[k].w, tx[3]);
+            ty[0] = fmaf(wy, uc[k].x, ty[0]); ty[1] = fmaf(wy, uc[k].y, ty[1]);
+            ty[2] = fmaf(wy, uc[k].z, ty[2]); ty[3] = fmaf(wy, uc[k].w, ty[3]);
+          }
+          if (WQ || FLY) {
+            const float wl = swl[k * 32 + lane];
+            q[0] = fmaf(wl, uc[k].x, q[0]); q[1] = fmaf(wl, uc[k].y, q[1]);
+            q[2] = fmaf(wl, uc[k].z, q[2]); q[3] = fmaf(wl, uc[k].w, q[3]);
+          }
+        }
+      }
+      __syncwarp();
+      if (iss.s < nslices) {
+        if (lane == 0) issue_chunk<NARR>(sbuf[w][buf], &bars[w][buf], a.ell, arrs, iss);
+        pending[buf] = true;
+        advance(a.ell, iss, stride);
+      }
+      buf ^= 1;
+    }
+    if (!valid) continue;
+    float du[4] = {-f[0], -f[1], -f[2], -f[3]};
+    if (FLY == 1)
+      for (int v = 0; v < 4; ++v) du[v] = fmaf(-hg, q[v], du[v]);
+    if (WT) {
+      float4* t4 = reinterpret_cast<float4*>(a.t32) + i * 2;
+      t4[0] = make_float4(tx[0], tx[1], tx[2], tx[3]);
+      t4[1] = make_float4(ty[0], ty[1], ty[2], ty[3]);
+    }
+    if (WQ) reinterpret_cast<float4*>(a.q32)[i] = make_float4(q[0], q[1], q[2], q[3]);
+    if (FLY == 2)
+      for (int v = 0; v < 4; ++v) a.hvf[i * 4 + v] = (double)(-hg * q[v]);
+    if (a.final_epilogue) {
+      double d[4] = {du[0], du[1], du[2], du[3]};
+      finish_node<4>(a.ep, i, d);
+    } else {
+      reinterpret_cast<float4*>(a.du_p32)[i] = make_float4(du[0], du[1], du[2], du[3]);
+    }
+  }
+}
+
+template <bool RV, bool LAP>
+__global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* err) {
+  constexpr int NARR = 1 + (RV ? 2 : 0) + (LAP ? 1 : 0);
+  __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][kChunkBytes];
+  __shared__ __align__(8) uint64_t bars[kTmaWarps][2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t nslices = (a.n + 31) >> 5;
+  const int64_t stride = (int64_t)gridDim.x * kTmaWarps;
+  const int64_t first = (int64_t)blockIdx.x * kTmaWarps + w;
+  const void* arrs[4];
+  {
+    int k = 0;
+    arrs[k++] = a.ell.col;
+    if (RV) { arrs[k++] = a.w32[0]; arrs[k++] = a.w32[1]; }
+    if (LAP) arrs[k++] = a.wl32;
+    for (; k < 4; ++k) arrs[k] = nullptr;
+  }
+  if (lane == 0) {
+    tma::bar_init(&bars[w][0], 1);
+    tma::bar_init(&bars[w][1], 1);
+    tma::fence_init();
+  }
+  __syncwarp();
+  const float4* __restrict__ S4 = reinterpret_cast<const float4*>(a.s32);
+  const float4* __restrict__ Q4 = reinterpret_cast<const float4*>(a.q32);
+  const float hg = (float)a.hv_gamma;
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  Cursor iss{first, 0};
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    if (iss.s < nslices) {
+      if (lane == 0) issue_chunk<NARR>(sbuf[w][b], &bars[w][b], a.ell, arrs, iss);
+      pending[b] = true;
+      advance(a.ell, iss, stride);
+    }
+  }
+  int buf = 0;
+  for (int64_t s = first; s < nslices; s += stride) {
+    const int64_t i = (s << 5) + lane;
+    const bool valid = i < a.n;
+    const int len = valid ? a.ell.row_len[i] : 0;
+    const int slots = slice_slots(a.ell, s);
+    const int nch = (slots + kCh - 1) / kCh;
+    float sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sl[4] = {0, 0, 0, 0};
+    for (int c = 0; c < nch; ++c) {
+      if (!tma::wait_bounded(&bars[w][buf], phase[buf], kWaitLimit)) {
+        if (lane == 0) atomicExch(err, MFT_ERR_TIMEOUT);
+        for (int b = 0; b < 2; ++b)
+          if (pending[b]) tma::wait_bounded(&bars[w][b], phase[b], kWaitLimit);
+        return;
+      }
+      phase[buf] ^= 1u;
+      pending[buf] = false;
+      const int* scol = reinterpret_cast<const int*>(sbuf[w][buf][0]);
+      const int j0 = c * kCh;
+      if (RV) {
+        const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][1]);
+        const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][2]);
+        float4 xs[kCh], ys[kCh];
+#pragma unroll
+        for (int k = 0; k < kCh; ++k)
+          if (j0 + k < len) {
+            const int64_t cc = scol[k * 32 + lane];
+            xs[k] = __ldg(S4 + cc * 2);
+            ys[k] = __ldg(S4 + cc * 2 + 1);
+          }
+#pragma unroll
+        for (int k = 0; k < kCh; ++k)
+          if (j0 + k < len) {
+            const float wx = swx[k * 32 + lane], wy = swy[k * 32 + lane];
+            sx[0] = fmaf(wx, xs[k].x, sx[0]); sx[1] = fmaf(wx, xs[k].y, sx[1]);
+            sx[2] = fmaf(wx, xs[k].z, sx[2]); sx[3] = fmaf(wx, xs[k].w, sx[3]);
+            sy[0] = fmaf(wy, ys[k].x, sy[0]); sy[1] = fmaf(wy, ys[k].y, sy[1]);
+            sy[2] = fmaf(wy, ys[k].z, sy[2]); sy[3] = fmaf(wy, ys[k].w, sy[3]);
+          }
+      }
+      if (LAP) {
+        const float* swl = reinterpret_cast<const float*>(sbuf[w][buf][NARR - 1]);
+        float4 qs[kCh];
+#pragma unroll
+        for (int k = 0; k < kCh; ++k)
+          if (j0 + k < len) qs[k] = __ldg(Q4 + scol[k * 32 + lane]);
+#pragma unroll
+        for (int k = 0; k < kCh; ++k)
+          if (j0 + k < len) {
+            const float wl = swl[k * 32 + lane];
+            sl[0] = fmaf(wl, qs[k].x, sl[0]); sl[1] = fmaf(wl, qs[k].y, sl[1]);
+            sl[2] = fmaf(wl, qs[k].z, sl[2]); sl[3] = fmaf(wl, qs[k].w, sl[3]);
+          }
+      }
+      __syncwarp();
+      if (iss.s < nslices) {
+        if (lane == 0) issue_chunk<NARR>(sbuf[w][buf], &bars[w][buf], a.ell, arrs, iss);
+        pending[buf] = true;
+        advance(a.ell, iss, stride);
+      }
+      buf ^= 1;
+    }
+    if (!valid) continue;
+    float du[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      float d = a.du_p32[i * 4 + v];
+      if (RV) d = (d - sx[v]) - sy[v];
+      if (LAP) d = fmaf(-hg, sl[v], d);
+      if (a.hvf) d += (float)a.hvf[i * 4 + v];
+      du[v] = d;
+    }
+    if (a.final_epilogue) {
+      double d[4] = {du[0], du[1], du[2], du[3]};
+      finish_node<4>(a.ep, i, d);
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) a.du_p_out32[i * 4 + v] = du[v];
+    }
+  }
+}
+
+template <class K>
+unsigned persistent_grid(K kernel, int64_t n) {
+  static int cached = 0;
+  if (cached == 0) {
+    int dev = 0, sms = 0, per = 0;
+    MFT_CUDA(cudaGetDevice(&dev));
+    MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 32 * kTmaWarps, 0));
+    cached = sms * (per > 0 ? per : 1);
+  }
+  const int64_t slices = (n + 31) / 32;
+  const int64_t need = (slices + kTmaWarps - 1) / kTmaWarps;
+  return (unsigned)(need < cached ? need : cached);
+}
+
+}  // namespace
+
+bool launch_fwd_f32_tma(const FwdArgs& a, int* err, cudaStream_t s) {
+  if (a.V != 4 || a.n <= 0) return false;
+  const bool wt = a.want_t != 0, wq = a.want_q != 0;
+#define MFT_T(WT, WQ, FLY)                                                              \
+  do {                                                                                  \
+    const unsigned g = persistent_grid(k_fwd_euler_f32_tma<WT, WQ, FLY>, a.n);          \
+    k_fwd_euler_f32_tma<WT, WQ, FLY><<<g, 32 * kTmaWarps, 0, s>>>(a, err);              \
+  } while (0)
+  if (a.flyer == 0) {
+    if (wt && wq) MFT_T(true, true, 0);
+    else if (wt) MFT_T(true, false, 0);
+    else if (wq) MFT_T(false, true, 0);
+    else MFT_T(false, false, 0);
+  } else if (a.flyer == 1) {
+    if (wt) MFT_T(true, false, 1);
+    else MFT_T(false, false, 1);
+  } else {
+    if (wt) MFT_T(true, false, 2);
+    else MFT_T(false, false, 2);
+  }
+#undef MFT_T
+  MFT_LAUNCH_CHECK();
+  return true;
+}
+
+bool launch_rev_f32_tma(const RevArgs& a, int* err, cudaStream_t s) {
+  if (a.V != 4 || a.n <= 0 || (!a.rv && !a.lap)) return false;
+  if (a.rv && a.lap) {
+    k_rev_f32_tma<true, true><<<persistent_grid(k_rev_f32_tma<true, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+  } else if (a.rv) {
+    k_rev_f32_tma<true, false><<<persistent_grid(k_rev_f32_tma<true, false>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+  } else {
+    k_rev_f32_tma<false, true><<<persistent_grid(k_rev_f32_tma<false, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+  }
+  MFT_LAUNCH_CHECK();
+  return true;
+}
+
+}  // namespace mft

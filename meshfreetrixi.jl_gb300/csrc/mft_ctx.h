@@ -76,6 +76,7 @@ struct mft_ctx {
   std::vector<int> src_kind;
   std::vector<double> src_par;
   int precision = MFT_PREC_FP64;
+  int gather_mode = MFT_GATHER_AUTO;
 
   // work buffers (AoS n x V unless noted)
   mft::DBuf<double> U[4];  // u_n, stage 1, stage 2, stage 3
@@ -85,6 +86,7 @@ struct mft_ctx {
   mft::DBuf<double> red_partial, mean, norms;
   mft::DBuf<unsigned> red_counter;
   mft::DBuf<int> flag;
+  mft::DBuf<int> kerr;  // device error word of kernels with bounded waits
   int red_blocks = 0;
 
   // time integration state
