@@ -290,6 +290,9 @@ def run_ours(args):
     semi32, dom32, _, _ = build_problem(args.n_side, "fp32", local)
     ms32, prof32, _ = timed_steps(dom32.ctx, u0, dt, args.warmup, args.steps, pg)
     u32, _ = dom32.ctx.get_state()
+    from meshfree_gb300 import _lib as L
+    mapping = {"fwd_gather": dom32.ctx.get_option(L.OPT_TUNED_FWD),
+               "rev_gather": dom32.ctx.get_option(L.OPT_TUNED_REV)}
     ms32_max = max_over_ranks(pg, ms32)
     # same number of steps from u0 in both forms: L2 density error of FP32 vs FP64
     l2 = float(np.linalg.norm(u32[0] - u64[0]) / np.linalg.norm(u64[0]))
@@ -338,6 +341,7 @@ def run_ours(args):
         "fp32_apply": {"value": value32, "unit": UNIT, "speedup_vs_fp64": value32 / value,
                        "l2_density_err_vs_fp64": l2, "linf_density_err_vs_fp64": linf,
                        "steps": args.steps, "roofline": roof32,
+                       "autotuned_mapping": mapping,
                        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
     }
     print(json.dumps(line), flush=True)

@@ -174,9 +174,14 @@ mft_status mft_set_precision(mft_ctx* ctx, int precision);
  * MFT_GATHER_THREAD (one node per thread, direct loads), MFT_GATHER_STAGED (one warp
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
  * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
-enum { MFT_OPT_GATHER = 0 };
+enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2 };
 enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2 };
 mft_status mft_set_option(mft_ctx* ctx, int option, int value);
+/* Reads an option; MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV return the mapping the
+ * autotuner chose for the most recent forward / transpose gather configuration
+ * (0 = one node per thread, 4 or 8 = staged with that many slots per bulk copy,
+ * -1 = not tuned yet). */
+mft_status mft_get_option(mft_ctx* ctx, int option, int* value);
 
 /* ---------------------------------------------------------------- rhs! */
 

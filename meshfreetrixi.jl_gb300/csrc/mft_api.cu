@@ -223,6 +223,7 @@ void ensure_work(mft_ctx* c) {
     c->t32.alloc((size_t)n * 2 * V);
     c->q32.alloc(nv);
     c->work_u32.alloc(nv);
+    c->work_du32.alloc(nv);
   }
 }
 
@@ -263,6 +264,8 @@ void ensure_device_ops(mft_ctx* c) {
   }
   MFT_CUDA(cudaStreamSynchronize(s));
   c->dev_dirty = false;
+  for (int &k : c->tuned_fwd) k = -1;
+  for (int &k : c->tuned_rev) k = -1;
 }
 
 static void ensure_bcs(mft_ctx* c) {
@@ -316,14 +319,84 @@ static void refresh_dirichlet(mft_ctx* c, double t) {
   MFT_CUDA(cudaStreamSynchronize(c->stream));
 }
 
-static bool staged_gathers(mft_ctx* c) {
-  return c->gather_mode == MFT_GATHER_STAGED ||
-         (c->gather_mode == MFT_GATHER_AUTO && c->precision == MFT_PREC_FP32);
+// ---------------------------------------------------------------- gather autotuner
+//
+// The FP32 Euler gathers have three mappings: one node per thread with direct loads
+// (choice 0) and one warp per 32-row slice with the slice's indices/weights staged in
+// shared memory by bulk copies, 4 or 8 slots per copy (choices 4, 8).  With
+// MFT_GATHER_AUTO the first launch of each kernel configuration times every mapping on
+// the live inputs (CUDA events, best of 3 after a warm-up) and keeps the fastest for this
+// context until the operators change.
+
+static const int kGatherChoices[3] = {0, 4, 8};
+
+template <class Launch>
+static int tune_gather(mft_ctx* c, Launch&& launch) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  MFT_CUDA(cudaEventCreate(&e0));
+  MFT_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int choice : kGatherChoices) {
+    launch(choice);
+    float t = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      MFT_CUDA(cudaEventRecord(e0, c->stream));
+      launch(choice);
+      MFT_CUDA(cudaEventRecord(e1, c->stream));
+      MFT_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      MFT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      t = std::min(t, ms);
+    }
+    if (t < best_ms) {
+      best_ms = t;
+      best = choice;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+static int fwd_choice(mft_ctx* c, const FwdArgs& a) {
+  if (a.V != 4) return 0;
+  if (c->gather_mode == MFT_GATHER_THREAD) return 0;
+  if (c->gather_mode == MFT_GATHER_STAGED) return 8;
+  const int key = (a.want_t ? 1 : 0) + (a.want_q ? 2 : 0) + 4 * a.flyer;
+  if (c->tuned_fwd[key] < 0) {
+    FwdArgs probe = a;
+    probe.final_epilogue = 0;  // timing launches write only scratch outputs
+    c->tuned_fwd[key] = tune_gather(c, [&](int ch) {
+      if (ch == 0 || !launch_fwd_f32_tma(probe, ch, c->kerr.p, c->stream))
+        launch_fwd_f32(probe, c->stream);
+    });
+  }
+  return c->tuned_fwd[key];
+}
+
+static int rev_choice(mft_ctx* c, const RevArgs& a) {
+  if (a.V != 4) return 0;
+  if (c->gather_mode == MFT_GATHER_THREAD) return 0;
+  if (c->gather_mode == MFT_GATHER_STAGED) return 8;
+  const int key = (a.rv ? 1 : 0) + (a.lap ? 2 : 0);
+  if (c->tuned_rev[key] < 0) {
+    RevArgs probe = a;
+    probe.final_epilogue = 0;
+    probe.du_p_out32 = c->du_p2_32.p == a.du_p32 ? c->work_du32.p : c->du_p2_32.p;
+    c->tuned_rev[key] = tune_gather(c, [&](int ch) {
+      if (ch == 0 || !launch_rev_f32_tma(probe, ch, c->kerr.p, c->stream))
+        launch_rev_f32(probe, c->stream);
+    });
+  }
+  return c->tuned_rev[key];
 }
 
 void launch_fwd(mft_ctx* c, const FwdArgs& a) {
   if (c->precision == MFT_PREC_FP32) {
-    if (staged_gathers(c) && launch_fwd_f32_tma(a, c->kerr.p, c->stream)) return;
+    const int ch = fwd_choice(c, a);
+    c->last_fwd_choice = ch;
+    if (ch > 0 && launch_fwd_f32_tma(a, ch, c->kerr.p, c->stream)) return;
     launch_fwd_f32(a, c->stream);
   } else {
     launch_fwd_f64(a, c->stream);
@@ -331,7 +404,9 @@ void launch_fwd(mft_ctx* c, const FwdArgs& a) {
 }
 void launch_rev(mft_ctx* c, const RevArgs& a) {
   if (c->precision == MFT_PREC_FP32) {
-    if (staged_gathers(c) && launch_rev_f32_tma(a, c->kerr.p, c->stream)) return;
+    const int ch = rev_choice(c, a);
+    c->last_rev_choice = ch;
+    if (ch > 0 && launch_rev_f32_tma(a, ch, c->kerr.p, c->stream)) return;
     launch_rev_f32(a, c->stream);
   } else {
     launch_rev_f64(a, c->stream);
@@ -922,9 +997,21 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
       MFT_REQUIRE(value >= MFT_GATHER_AUTO && value <= MFT_GATHER_STAGED, MFT_ERR_ARG,
                   "unknown gather mapping");
       c->gather_mode = value;
+      for (int& k : c->tuned_fwd) k = -1;
+      for (int& k : c->tuned_rev) k = -1;
     } else {
       throw mft::Error(MFT_ERR_ARG, "unknown option");
     }
+  });
+}
+
+mft_status mft_get_option(mft_ctx* c, int option, int* value) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(value, MFT_ERR_ARG, "value is NULL");
+    if (option == MFT_OPT_GATHER) *value = c->gather_mode;
+    else if (option == MFT_OPT_TUNED_FWD) *value = c->last_fwd_choice;
+    else if (option == MFT_OPT_TUNED_REV) *value = c->last_rev_choice;
+    else throw mft::Error(MFT_ERR_ARG, "unknown option");
   });
 }
 

@@ -356,6 +356,7 @@ __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __re
     for (int k = 0; k < V; ++k) {
       const double v = __longlong_as_double((long long)best[k]);
       norms[k] = v == 0.0 ? 2.220446049250313e-16 : v;
+      norms[V + k] = 1.0 / norms[k];
     }
     *counter = 0u;
   }
@@ -369,35 +370,42 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   if (i >= a.n) return;
   double eps_uw;
   if (V == 4) {
+    // one reciprocal instead of three divisions (FP64 division is a long sequence on
+    // this part); results differ from the divisions by at most an ulp
     const double rho = a.u[i * 4], m1 = a.u[i * 4 + 1], m2 = a.u[i * 4 + 2], en = a.u[i * 4 + 3];
-    const double v1 = ddiv(m1, rho), v2 = ddiv(m2, rho);
+    const double rinv = ddiv(1.0, rho);
+    const double v1 = dmul(m1, rinv), v2 = dmul(m2, rinv);
     const double p = dmul(dsub(a.gamma, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
     const double speed = sqrt(dadd(dmul(v1, v1), dmul(v2, v2)));
     double c;
     if (p < 0.0 || rho < 0.0) c = 0.0;
-    else c = sqrt(ddiv(dmul(a.gamma, p), rho));
+    else c = sqrt(dmul(dmul(a.gamma, p), rinv));
     eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), dadd(speed, c));
   } else {
     const double an = sqrt(dadd(dmul(a.ax, a.ax), dmul(a.ay, a.ay)));
     eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), an);
   }
   double eps;
-  if (a.kind == MFT_SRC_RV) {
+  if (a.kind == MFT_SRC_RV && a.success_iter != 0) {
+    // residual / norm with the norms' reciprocals (written by k_lexmax after the norms)
     double mr = 0.0;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       double dp = a.du_p[i * V + v];
       if (a.hvf) dp = dadd(dp, a.hvf[i * V + v]);
       const double r = fabs(dsub(a.approx_du[i * V + v], dp));
-      const double qv = ddiv(r, a.norms[v]);
+      const double qv = dmul(r, a.norms[V + v]);
       mr = v == 0 ? qv : jl_max(mr, qv);
     }
     const double eps_rv = dmul(dmul(dmul(0.5, a.c_rv), dmul(a.h, a.h)), mr);
-    if (isnan(eps_rv) || isinf(eps_rv) || a.success_iter == 0) {
+    if (isnan(eps_rv) || isinf(eps_rv)) {
       eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16 : eps_uw;
     } else {
       eps = jl_min(eps_rv, eps_uw);
     }
+  } else if (a.kind == MFT_SRC_RV) {
+    // success_iter == 0: update_visc! takes eps_uw (or eps() when it is not finite)
+    eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16 : eps_uw;
   } else {
     eps = eps_uw;
   }

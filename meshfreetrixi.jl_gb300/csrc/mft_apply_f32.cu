@@ -14,21 +14,6 @@ namespace {
 
 using namespace dev;
 
-__device__ __forceinline__ void euler_flux_f32(float gm1, float4 u, float* fx, float* fy) {
-  const float r = __frcp_rn(u.x);
-  const float v1 = u.y * r, v2 = u.z * r;
-  const float p = gm1 * (u.w - 0.5f * (u.y * v1 + u.z * v2));
-  const float ep = u.w + p;
-  fx[0] = u.y;
-  fx[1] = fmaf(u.y, v1, p);
-  fx[2] = u.y * v2;
-  fx[3] = ep * v1;
-  fy[0] = u.z;
-  fy[1] = u.z * v1;
-  fy[2] = fmaf(u.z, v2, p);
-  fy[3] = ep * v2;
-}
-
 template <bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
@@ -48,16 +33,7 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
     const int c = __ldg(col + p);
     const float wx = __ldg(wxp + p), wy = __ldg(wyp + p);
     const float4 uc = __ldg(U4 + c);
-    float fx[4], fy[4];
-    euler_flux_f32(gm1, uc, fx, fy);
-#pragma unroll
-    for (int v = 0; v < 4; ++v) f[v] = fmaf(wy, fy[v], fmaf(wx, fx[v], f[v]));
-    if (WT) {
-      tx[0] = fmaf(wx, uc.x, tx[0]); tx[1] = fmaf(wx, uc.y, tx[1]);
-      tx[2] = fmaf(wx, uc.z, tx[2]); tx[3] = fmaf(wx, uc.w, tx[3]);
-      ty[0] = fmaf(wy, uc.x, ty[0]); ty[1] = fmaf(wy, uc.y, ty[1]);
-      ty[2] = fmaf(wy, uc.z, ty[2]); ty[3] = fmaf(wy, uc.w, ty[3]);
-    }
+    euler_accum_f32<WT>(gm1, uc, wx, wy, f, tx, ty);
     if (WQ || FLY) {
       const float wl = __ldg(wlp + p);
       q[0] = fmaf(wl, uc.x, q[0]); q[1] = fmaf(wl, uc.y, q[1]);
@@ -65,6 +41,7 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
     }
   }
   const float hg = (float)a.hv_gamma;
+  if (WT) f[0] = tx[1] + ty[2];
   float du[4] = {-f[0], -f[1], -f[2], -f[3]};
   if (FLY == 1)
     for (int v = 0; v < 4; ++v) du[v] = fmaf(-hg, q[v], du[v]);

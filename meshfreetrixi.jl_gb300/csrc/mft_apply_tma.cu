@@ -21,25 +21,8 @@ namespace {
 
 using namespace dev;
 
-constexpr int kCh = 8;          // slots per staged chunk
 constexpr int kTmaWarps = 4;    // warps per block
 constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr int kChunkBytes = kCh * 32 * 4;  // one array, one chunk (int32 / float)
-
-__device__ __forceinline__ void euler_flux_f32(float gm1, float4 u, float* fx, float* fy) {
-  const float r = __frcp_rn(u.x);
-  const float v1 = u.y * r, v2 = u.z * r;
-  const float p = gm1 * (u.w - 0.5f * (u.y * v1 + u.z * v2));
-  const float ep = u.w + p;
-  fx[0] = u.y;
-  fx[1] = fmaf(u.y, v1, p);
-  fx[2] = u.y * v2;
-  fx[3] = ep * v1;
-  fy[0] = u.z;
-  fy[1] = u.z * v1;
-  fy[2] = fmaf(u.z, v2, p);
-  fy[3] = ep * v2;
-}
 
 // Warp-uniform cursor over (slice, chunk) pairs of this warp's slices.
 struct Cursor {
@@ -51,14 +34,14 @@ __device__ __forceinline__ int slice_slots(const EllView& e, int64_t s) {
   return (int)((e.slice_off[s + 1] - e.slice_off[s]) >> 5);
 }
 
-template <int NARR>
-__device__ __forceinline__ void issue_chunk(unsigned char (*buf)[kChunkBytes], uint64_t* bar,
+template <int NARR, int CH>
+__device__ __forceinline__ void issue_chunk(unsigned char (*buf)[CH * 128], uint64_t* bar,
                                             const EllView& e, const void* const* arrs,
                                             Cursor cur) {
   const int slots = slice_slots(e, cur.s);
-  const int n = min(kCh, slots - cur.c * kCh);
+  const int n = min(CH, slots - cur.c * CH);
   const uint32_t bytes = (uint32_t)n * 32u * 4u;
-  const int64_t base = e.slice_off[cur.s] + (int64_t)cur.c * kCh * 32;
+  const int64_t base = e.slice_off[cur.s] + (int64_t)cur.c * CH * 32;
   tma::fence_proxy_async();
   tma::arrive_expect_tx(bar, bytes * NARR);
 #pragma unroll
@@ -66,18 +49,19 @@ __device__ __forceinline__ void issue_chunk(unsigned char (*buf)[kChunkBytes], u
     tma::bulk_g2s(buf[k], static_cast<const unsigned char*>(arrs[k]) + base * 4, bytes, bar);
 }
 
+template <int CH>
 __device__ __forceinline__ void advance(const EllView& e, Cursor& cur, int64_t stride) {
-  const int nch = (slice_slots(e, cur.s) + kCh - 1) / kCh;
+  const int nch = (slice_slots(e, cur.s) + CH - 1) / CH;
   if (++cur.c >= nch) {
     cur.c = 0;
     cur.s += stride;
   }
 }
 
-template <bool WT, bool WQ, int FLY>
+template <int CH, bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a, int* err) {
   constexpr int NARR = (WQ || FLY) ? 4 : 3;
-  __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][kChunkBytes];
+  __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][CH * 128];
   __shared__ __align__(8) uint64_t bars[kTmaWarps][2];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t nslices = (a.n + 31) >> 5;
@@ -99,9 +83,9 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
 #pragma unroll
   for (int b = 0; b < 2; ++b) {
     if (iss.s < nslices) {
-      if (lane == 0) issue_chunk<NARR>(sbuf[w][b], &bars[w][b], a.ell, arrs, iss);
+      if (lane == 0) issue_chunk<NARR, CH>(sbuf[w][b], &bars[w][b], a.ell, arrs, iss);
       pending[b] = true;
-      advance(a.ell, iss, stride);
+      advance<CH>(a.ell, iss, stride);
     }
   }
   int buf = 0;
@@ -110,7 +94,7 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
     const bool valid = i < a.n;
     const int len = valid ? a.ell.row_len[i] : 0;
     const int slots = slice_slots(a.ell, s);
-    const int nch = (slots + kCh - 1) / kCh;
+    const int nch = (slots + CH - 1) / CH;
     float f[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
     for (int c = 0; c < nch; ++c) {
       if (!tma::wait_bounded(&bars[w][buf], phase[buf], kWaitLimit)) {
@@ -125,25 +109,16 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
       const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][1]);
       const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][2]);
       const float* swl = reinterpret_cast<const float*>(sbuf[w][buf][NARR - 1]);
-      const int j0 = c * kCh;
-      float4 uc[kCh];
+      const int j0 = c * CH;
+      float4 uc[CH];
 #pragma unroll
-      for (int k = 0; k < kCh; ++k)
+      for (int k = 0; k < CH; ++k)
         if (j0 + k < len) uc[k] = __ldg(U4 + scol[k * 32 + lane]);
 #pragma unroll
-      for (int k = 0; k < kCh; ++k) {
+      for (int k = 0; k < CH; ++k) {
         if (j0 + k < len) {
           const float wx = swx[k * 32 + lane], wy = swy[k * 32 + lane];
-          float fx[4], fy[4];
-          euler_flux_f32(gm1, uc[k], fx, fy);
-#pragma unroll
-          for (int v = 0; v < 4; ++v) f[v] = fmaf(wy, fy[v], fmaf(wx, fx[v], f[v]));
-          if (WT) {
-            tx[0] = fmaf(wx, uc[k].x, tx[0]); tx[1] = fmaf(wx, uc[k].y, tx[1]);
-            tx[2] = fmaf(wx, uc[k].z, tx[2]); tx[3] = fmaf(wx, uc[k].w, tx[3]);
-            ty[0] = fmaf(wy, uc[k].x, ty[0]); ty[1] = fmaf(wy, uc[k].y, ty[1]);
-            ty[2] = fmaf(wy, uc[k].z, ty[2]); ty[3] = fmaf(wy, uc[k].w, ty[3]);
-          }
+          euler_accum_f32<WT>(gm1, uc[k], wx, wy, f, tx, ty);
           if (WQ || FLY) {
             const float wl = swl[k * 32 + lane];
             q[0] = fmaf(wl, uc[k].x, q[0]); q[1] = fmaf(wl, uc[k].y, q[1]);
@@ -153,13 +128,14 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
       }
       __syncwarp();
       if (iss.s < nslices) {
-        if (lane == 0) issue_chunk<NARR>(sbuf[w][buf], &bars[w][buf], a.ell, arrs, iss);
+        if (lane == 0) issue_chunk<NARR, CH>(sbuf[w][buf], &bars[w][buf], a.ell, arrs, iss);
         pending[buf] = true;
-        advance(a.ell, iss, stride);
+        advance<CH>(a.ell, iss, stride);
       }
       buf ^= 1;
     }
     if (!valid) continue;
+    if (WT) f[0] = tx[1] + ty[2];
     float du[4] = {-f[0], -f[1], -f[2], -f[3]};
     if (FLY == 1)
       for (int v = 0; v < 4; ++v) du[v] = fmaf(-hg, q[v], du[v]);
@@ -180,10 +156,10 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
   }
 }
 
-template <bool RV, bool LAP>
+template <int CH, bool RV, bool LAP>
 __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* err) {
   constexpr int NARR = 1 + (RV ? 2 : 0) + (LAP ? 1 : 0);
-  __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][kChunkBytes];
+  __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][CH * 128];
   __shared__ __align__(8) uint64_t bars[kTmaWarps][2];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t nslices = (a.n + 31) >> 5;
@@ -212,9 +188,9 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
 #pragma unroll
   for (int b = 0; b < 2; ++b) {
     if (iss.s < nslices) {
-      if (lane == 0) issue_chunk<NARR>(sbuf[w][b], &bars[w][b], a.ell, arrs, iss);
+      if (lane == 0) issue_chunk<NARR, CH>(sbuf[w][b], &bars[w][b], a.ell, arrs, iss);
       pending[b] = true;
-      advance(a.ell, iss, stride);
+      advance<CH>(a.ell, iss, stride);
     }
   }
   int buf = 0;
@@ -223,7 +199,7 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
     const bool valid = i < a.n;
     const int len = valid ? a.ell.row_len[i] : 0;
     const int slots = slice_slots(a.ell, s);
-    const int nch = (slots + kCh - 1) / kCh;
+    const int nch = (slots + CH - 1) / CH;
     float sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sl[4] = {0, 0, 0, 0};
     for (int c = 0; c < nch; ++c) {
       if (!tma::wait_bounded(&bars[w][buf], phase[buf], kWaitLimit)) {
@@ -235,20 +211,20 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
       phase[buf] ^= 1u;
       pending[buf] = false;
       const int* scol = reinterpret_cast<const int*>(sbuf[w][buf][0]);
-      const int j0 = c * kCh;
+      const int j0 = c * CH;
       if (RV) {
         const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][1]);
         const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][2]);
-        float4 xs[kCh], ys[kCh];
+        float4 xs[CH], ys[CH];
 #pragma unroll
-        for (int k = 0; k < kCh; ++k)
+        for (int k = 0; k < CH; ++k)
           if (j0 + k < len) {
             const int64_t cc = scol[k * 32 + lane];
             xs[k] = __ldg(S4 + cc * 2);
             ys[k] = __ldg(S4 + cc * 2 + 1);
           }
 #pragma unroll
-        for (int k = 0; k < kCh; ++k)
+        for (int k = 0; k < CH; ++k)
           if (j0 + k < len) {
             const float wx = swx[k * 32 + lane], wy = swy[k * 32 + lane];
             sx[0] = fmaf(wx, xs[k].x, sx[0]); sx[1] = fmaf(wx, xs[k].y, sx[1]);
@@ -259,12 +235,12 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
       }
       if (LAP) {
         const float* swl = reinterpret_cast<const float*>(sbuf[w][buf][NARR - 1]);
-        float4 qs[kCh];
+        float4 qs[CH];
 #pragma unroll
-        for (int k = 0; k < kCh; ++k)
+        for (int k = 0; k < CH; ++k)
           if (j0 + k < len) qs[k] = __ldg(Q4 + scol[k * 32 + lane]);
 #pragma unroll
-        for (int k = 0; k < kCh; ++k)
+        for (int k = 0; k < CH; ++k)
           if (j0 + k < len) {
             const float wl = swl[k * 32 + lane];
             sl[0] = fmaf(wl, qs[k].x, sl[0]); sl[1] = fmaf(wl, qs[k].y, sl[1]);
@@ -273,9 +249,9 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
       }
       __syncwarp();
       if (iss.s < nslices) {
-        if (lane == 0) issue_chunk<NARR>(sbuf[w][buf], &bars[w][buf], a.ell, arrs, iss);
+        if (lane == 0) issue_chunk<NARR, CH>(sbuf[w][buf], &bars[w][buf], a.ell, arrs, iss);
         pending[buf] = true;
-        advance(a.ell, iss, stride);
+        advance<CH>(a.ell, iss, stride);
       }
       buf ^= 1;
     }
@@ -316,13 +292,13 @@ unsigned persistent_grid(K kernel, int64_t n) {
 
 }  // namespace
 
-bool launch_fwd_f32_tma(const FwdArgs& a, int* err, cudaStream_t s) {
-  if (a.V != 4 || a.n <= 0) return false;
+template <int CH>
+static void fwd_tma(const FwdArgs& a, int* err, cudaStream_t s) {
   const bool wt = a.want_t != 0, wq = a.want_q != 0;
 #define MFT_T(WT, WQ, FLY)                                                              \
   do {                                                                                  \
-    const unsigned g = persistent_grid(k_fwd_euler_f32_tma<WT, WQ, FLY>, a.n);          \
-    k_fwd_euler_f32_tma<WT, WQ, FLY><<<g, 32 * kTmaWarps, 0, s>>>(a, err);              \
+    const unsigned g = persistent_grid(k_fwd_euler_f32_tma<CH, WT, WQ, FLY>, a.n);      \
+    k_fwd_euler_f32_tma<CH, WT, WQ, FLY><<<g, 32 * kTmaWarps, 0, s>>>(a, err);          \
   } while (0)
   if (a.flyer == 0) {
     if (wt && wq) MFT_T(true, true, 0);
@@ -337,19 +313,30 @@ bool launch_fwd_f32_tma(const FwdArgs& a, int* err, cudaStream_t s) {
     else MFT_T(false, false, 2);
   }
 #undef MFT_T
+}
+
+template <int CH>
+static void rev_tma(const RevArgs& a, int* err, cudaStream_t s) {
+  if (a.rv && a.lap)
+    k_rev_f32_tma<CH, true, true><<<persistent_grid(k_rev_f32_tma<CH, true, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+  else if (a.rv)
+    k_rev_f32_tma<CH, true, false><<<persistent_grid(k_rev_f32_tma<CH, true, false>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+  else
+    k_rev_f32_tma<CH, false, true><<<persistent_grid(k_rev_f32_tma<CH, false, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+}
+
+bool launch_fwd_f32_tma(const FwdArgs& a, int chunk, int* err, cudaStream_t s) {
+  if (a.V != 4 || a.n <= 0) return false;
+  if (chunk <= 4) fwd_tma<4>(a, err, s);
+  else fwd_tma<8>(a, err, s);
   MFT_LAUNCH_CHECK();
   return true;
 }
 
-bool launch_rev_f32_tma(const RevArgs& a, int* err, cudaStream_t s) {
+bool launch_rev_f32_tma(const RevArgs& a, int chunk, int* err, cudaStream_t s) {
   if (a.V != 4 || a.n <= 0 || (!a.rv && !a.lap)) return false;
-  if (a.rv && a.lap) {
-    k_rev_f32_tma<true, true><<<persistent_grid(k_rev_f32_tma<true, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
-  } else if (a.rv) {
-    k_rev_f32_tma<true, false><<<persistent_grid(k_rev_f32_tma<true, false>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
-  } else {
-    k_rev_f32_tma<false, true><<<persistent_grid(k_rev_f32_tma<false, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
-  }
+  if (chunk <= 4) rev_tma<4>(a, err, s);
+  else rev_tma<8>(a, err, s);
   MFT_LAUNCH_CHECK();
   return true;
 }

@@ -77,12 +77,15 @@ struct mft_ctx {
   std::vector<double> src_par;
   int precision = MFT_PREC_FP64;
   int gather_mode = MFT_GATHER_AUTO;
+  int tuned_fwd[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  int tuned_rev[4] = {-1, -1, -1, -1};
+  int last_fwd_choice = -1, last_rev_choice = -1;
 
   // work buffers (AoS n x V unless noted)
   mft::DBuf<double> U[4];  // u_n, stage 1, stage 2, stage 3
   mft::DBuf<float> U32[4];
   mft::DBuf<double> F, du_p, du_p2, t, q, hvf, eps, approx_du, soa, soa2, work_u, work_du;
-  mft::DBuf<float> du_p32, du_p2_32, t32, q32, work_u32;
+  mft::DBuf<float> du_p32, du_p2_32, t32, q32, work_u32, work_du32;
   mft::DBuf<double> red_partial, mean, norms;
   mft::DBuf<unsigned> red_counter;
   mft::DBuf<int> flag;

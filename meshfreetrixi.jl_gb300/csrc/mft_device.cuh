@@ -97,5 +97,32 @@ static __device__ __forceinline__ void finish_node(const Epilogue& ep, int64_t i
   }
 }
 
+
+// FP32 Euler flux divergence contribution of one neighbour state u with weights
+// (wx, wy), in the form that needs no flux vector: with a = wx v1 + wy v2,
+//   sum wx Fx + wy Fy = (rho a, m1 a + wx p, m2 a + wy p, (E + p) a).
+// With WT the rho row is left to the caller (it equals tx[1] + ty[2]) and
+// t = (wx u, wy u) is accumulated.  Shared by every FP32 gather variant so that they
+// round identically.
+template <bool WT>
+static __device__ __forceinline__ void euler_accum_f32(float gm1, float4 u, float wx, float wy,
+                                                       float* f, float* tx, float* ty) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(u.x));
+  const float v1 = u.y * r, v2 = u.z * r;
+  const float p = gm1 * fmaf(-0.5f, fmaf(u.z, v2, u.y * v1), u.w);
+  const float a = fmaf(wx, v1, wy * v2);
+  if (!WT) f[0] = fmaf(u.x, a, f[0]);
+  f[1] = fmaf(u.y, a, fmaf(wx, p, f[1]));
+  f[2] = fmaf(u.z, a, fmaf(wy, p, f[2]));
+  f[3] = fmaf(u.w + p, a, f[3]);
+  if (WT) {
+    tx[0] = fmaf(wx, u.x, tx[0]); tx[1] = fmaf(wx, u.y, tx[1]);
+    tx[2] = fmaf(wx, u.z, tx[2]); tx[3] = fmaf(wx, u.w, tx[3]);
+    ty[0] = fmaf(wy, u.x, ty[0]); ty[1] = fmaf(wy, u.y, ty[1]);
+    ty[2] = fmaf(wy, u.z, ty[2]); ty[3] = fmaf(wy, u.w, ty[3]);
+  }
+}
+
 }  // namespace dev
 }  // namespace mft

@@ -210,8 +210,9 @@ struct RevArgs {
 void launch_rev_f64(const RevArgs& a, cudaStream_t s);
 void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 // Bulk-copy-staged FP32 gathers (Euler); return false when the case is not covered.
-bool launch_fwd_f32_tma(const FwdArgs& a, int* err, cudaStream_t s);
-bool launch_rev_f32_tma(const RevArgs& a, int* err, cudaStream_t s);
+// chunk: slots staged per bulk copy (4 or 8).
+bool launch_fwd_f32_tma(const FwdArgs& a, int chunk, int* err, cudaStream_t s);
+bool launch_rev_f32_tma(const RevArgs& a, int chunk, int* err, cudaStream_t s);
 
 // Sets *flag to 1 when a and b differ in any of `count` doubles (bitwise).
 void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s);

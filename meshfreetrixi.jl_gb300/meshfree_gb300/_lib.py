@@ -21,7 +21,7 @@ BC_DIRICHLET, BC_SLIP_WALL, BC_DO_NOTHING = 0, 1, 2
 SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER = 0, 1, 2, 3
 OP_GRAD, OP_LAP, OP_HV = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
-OPT_GATHER = 0
+OPT_GATHER, OPT_TUNED_FWD, OPT_TUNED_REV = 0, 1, 2
 GATHER_AUTO, GATHER_THREAD, GATHER_STAGED = 0, 1, 2
 
 # Every entry point of include/meshfree_gb300.h with (restype, argtypes).
@@ -48,6 +48,7 @@ SIGNATURES = {
     "mft_set_sources": (I32, [VP, I32, VP, VP]),
     "mft_set_precision": (I32, [VP, I32]),
     "mft_set_option": (I32, [VP, I32, I32]),
+    "mft_get_option": (I32, [VP, I32, C.POINTER(I32)]),
     "mft_rhs": (I32, [VP, VP, VP, I32, DBL]),
     "mft_rhs_device": (I32, [VP, VP, VP, DBL]),
     "mft_set_state": (I32, [VP, VP, I32, DBL]),
@@ -198,6 +199,11 @@ class Context:
 
     def set_option(self, option, value):
         self.check(self.lib.mft_set_option(self.h, option, value))
+
+    def get_option(self, option):
+        v = C.c_int()
+        self.check(self.lib.mft_get_option(self.h, option, C.byref(v)))
+        return v.value
 
     # rhs! / stepping ----------------------------------------------------
     def rhs(self, du, u, t):

@@ -19,14 +19,16 @@ def test_fp32_staged_equals_thread_and_tracks_fp64(oracle, gpu_lib, cyl, cyl_ops
     semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, case)
     ctx.set_precision(L.PREC_FP32)
     out = {}
-    for mode in (L.GATHER_THREAD, L.GATHER_STAGED):
+    for mode in (L.GATHER_THREAD, L.GATHER_STAGED, L.GATHER_AUTO):
         ctx.set_option(L.OPT_GATHER, mode)
         du = np.empty_like(u0)
         u = u0.copy()
         ctx.rhs(du, u, 0.0)
         out[mode] = (du, u)
-    assert np.array_equal(out[L.GATHER_THREAD][0], out[L.GATHER_STAGED][0])
-    assert np.array_equal(out[L.GATHER_THREAD][1], out[L.GATHER_STAGED][1])
+    assert ctx.get_option(L.OPT_TUNED_FWD) in (0, 4, 8)
+    for mode in (L.GATHER_STAGED, L.GATHER_AUTO):
+        assert np.array_equal(out[L.GATHER_THREAD][0], out[mode][0])
+        assert np.array_equal(out[L.GATHER_THREAD][1], out[mode][1])
     u_ref = u0.copy()
     du_ref, eps_ref = semi.rhs(u_ref, 0.0, want_eps=True)
     srcs = CASES[case]
@@ -55,10 +57,11 @@ def test_fp32_staged_equals_thread_large(gpu_lib):
     ctx = domain.ctx
     u0 = semi.compute_coefficients(0.0)
     res = {}
-    for mode in (L.GATHER_THREAD, L.GATHER_STAGED):
+    for mode in (L.GATHER_THREAD, L.GATHER_STAGED, L.GATHER_AUTO):
         ctx.set_option(L.OPT_GATHER, mode)
         ctx.history_init(3)
         ctx.set_state(u0, 0.0)
         ctx.ssprk33(0.2 * h, 4)
         res[mode] = ctx.get_state()[0]
     assert np.array_equal(res[L.GATHER_THREAD], res[L.GATHER_STAGED])
+    assert np.array_equal(res[L.GATHER_THREAD], res[L.GATHER_AUTO])
