@@ -233,6 +233,7 @@ void ensure_device_ops(mft_ctx* c) {
     MFT_REQUIRE(c->have_val[d], MFT_ERR_STATE,
                 "gradient operator component " + std::to_string(d) + " not set");
   if (!c->dev_dirty) return;
+  c->graph_valid = false;
   cudaStream_t s = c->stream;
   std::vector<int64_t> pos;
   build_ell(c->n, c->rp, c->ci, c->fwd, pos, s);
@@ -270,6 +271,7 @@ void ensure_device_ops(mft_ctx* c) {
 
 static void ensure_bcs(mft_ctx* c) {
   if (!c->bc_dirty) return;
+  c->graph_valid = false;
   cudaStream_t s = c->stream;
   const int64_t n = c->n;
   std::vector<int8_t> tag(n, 0);
@@ -583,6 +585,8 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ea.t = f32 ? nullptr : c->t.p;
     ea.t32 = f32 ? c->t32.p : nullptr;
     ea.eps = c->eps.p;
+    ea.tab = c->capturing ? c->d_tab.p : nullptr;
+    ea.ctr = c->d_ctr.p;
     ProfScope ps(c, MFT_K_EPS);
     launch_eps(ea, s);
   }
@@ -748,6 +752,8 @@ mft_status mft_ctx_destroy(mft_ctx* c) {
     cudaEventDestroy(p.second.second);
   }
   for (auto e : c->ev_pool) cudaEventDestroy(e);
+  for (auto g : c->gexec)
+    if (g) cudaGraphExecDestroy(g);
   for (auto e : c->region_ev)
     if (e) cudaEventDestroy(e);
   delete c;
@@ -765,6 +771,7 @@ mft_status mft_sync(mft_ctx* c) {
 
 mft_status mft_set_points(mft_ctx* c, int dim, int64_t n, const double* xyz, const double* period) {
   return guarded(c, [&] {
+    c->graph_valid = false;
     MFT_REQUIRE(dim >= 1 && dim <= 3, MFT_ERR_ARG, "dim must be 1, 2 or 3");
     MFT_REQUIRE(n >= 1 && n < (int64_t)INT32_MAX, MFT_ERR_ARG, "node count out of range");
     MFT_REQUIRE(xyz, MFT_ERR_ARG, "xyz is NULL");
@@ -915,6 +922,7 @@ mft_status mft_load_csc(mft_ctx* c, int op, int comp, int64_t n, const int64_t* 
 
 mft_status mft_set_equations(mft_ctx* c, int kind, const double* params) {
   return guarded(c, [&] {
+    c->graph_valid = false;
     MFT_REQUIRE(params, MFT_ERR_ARG, "params is NULL");
     MFT_REQUIRE(c->dim == 2, MFT_ERR_UNSUPPORTED, "the rhs! engine covers 2D point clouds");
     if (kind == MFT_EQ_EULER2D) {
@@ -980,6 +988,7 @@ mft_status mft_set_dirichlet_callback(mft_ctx* c, mft_dirichlet_fn fn, void* use
 
 mft_status mft_set_sources(mft_ctx* c, int n_src, const int* kinds, const double* params) {
   return guarded(c, [&] {
+    c->graph_valid = false;
     MFT_REQUIRE(n_src >= 0 && n_src <= 8, MFT_ERR_ARG, "n_src out of range");
     MFT_REQUIRE(n_src == 0 || (kinds && params), MFT_ERR_ARG, "NULL source arrays");
     for (int k = 0; k < n_src; ++k)
@@ -993,10 +1002,12 @@ mft_status mft_set_sources(mft_ctx* c, int n_src, const int* kinds, const double
 
 mft_status mft_set_option(mft_ctx* c, int option, int value) {
   return guarded(c, [&] {
+    c->graph_valid = false;
     if (option == MFT_OPT_GATHER) {
       MFT_REQUIRE(value >= MFT_GATHER_AUTO && value <= MFT_GATHER_STAGED, MFT_ERR_ARG,
                   "unknown gather mapping");
       c->gather_mode = value;
+      c->fsal_valid = false;
       for (int& k : c->tuned_fwd) k = -1;
       for (int& k : c->tuned_rev) k = -1;
     } else {
@@ -1017,6 +1028,7 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
 
 mft_status mft_set_precision(mft_ctx* c, int precision) {
   return guarded(c, [&] {
+    c->graph_valid = false;
     MFT_REQUIRE(precision == MFT_PREC_FP64 || precision == MFT_PREC_FP32, MFT_ERR_ARG,
                 "unknown precision");
     c->precision = precision;
@@ -1122,6 +1134,7 @@ mft_status mft_get_state(mft_ctx* c, double* const* u, int nvars, double* t) {
 
 mft_status mft_history_init(mft_ctx* c, int approx_order) {
   return guarded(c, [&] {
+    c->graph_valid = false;
     check_state_ready(c);
     MFT_REQUIRE(approx_order >= 0 && approx_order <= 7, MFT_ERR_ARG, "approx_order out of range");
     set_device(c);
@@ -1150,55 +1163,154 @@ float* shadow(mft_ctx* c, int k) {
   return c->precision == MFT_PREC_FP32 ? c->U32[k].p : nullptr;
 }
 
-void ssprk33_run(mft_ctx* c, double dt, int nsteps) {
-  ensure_work(c);
-  cudaStream_t s = c->stream;
+// FSAL evaluation at the current state: k0 = f(u_n), stage 1 = u_n + dt*k0.
+void fsal_eval(mft_ctx* c, double dt) {
+  if (c->fsal_valid && c->fsal_dt == dt) return;
   const int64_t n = c->n;
   const int V = c->nvars;
-  const bool f32 = c->precision == MFT_PREC_FP32;
-  if (!c->fsal_valid || c->fsal_dt != dt) {
-    // FSAL evaluation at the current state: k0 = f(u_n), stage 1 = u_n + dt*k0.
-    if (f32) launch_aos_to_f32(c->U[0].p, c->U32[0].p, n * V, s);
-    Epilogue ep{};
-    ep.kind = kStage1;
-    ep.dt = dt;
-    ep.out = c->U[1].p;
-    ep.out32 = shadow(c, 1);
-    eval_rhs(c, c->U[0].p, shadow(c, 0), c->t_state, ep);
-    if (c->hist_order >= 0 && c->success_iter == 0)
-      history_push(c, c->t_state, c->U[0].p, 0);
-    c->fsal_valid = true;
-    c->fsal_dt = dt;
-  }
+  if (c->precision == MFT_PREC_FP32) launch_aos_to_f32(c->U[0].p, c->U32[0].p, n * V, c->stream);
+  Epilogue ep{};
+  ep.kind = kStage1;
+  ep.dt = dt;
+  ep.out = c->U[1].p;
+  ep.out32 = shadow(c, 1);
+  eval_rhs(c, c->U[0].p, shadow(c, 0), c->t_state, ep);
+  if (c->hist_order >= 0 && c->success_iter == 0) history_push(c, c->t_state, c->U[0].p, 0);
+  c->fsal_valid = true;
+  c->fsal_dt = dt;
+}
+
+// Stages 2, 3 and the next step's first stage from u_n in buffer `un` (stage-3 state
+// into `u3`); `t` is the step start time.
+void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3) {
+  Epilogue e2{};
+  e2.kind = kStage2;
+  e2.dt = dt;
+  e2.u_n = c->U[iu_n].p;
+  e2.out = c->U[2].p;
+  e2.out32 = shadow(c, 2);
+  eval_rhs(c, c->U[1].p, shadow(c, 1), t + dt, e2);
+  Epilogue e3{};
+  e3.kind = kStage3;
+  e3.dt = dt;
+  e3.u_n = c->U[iu_n].p;
+  e3.out = c->U[iu_3].p;
+  e3.out32 = shadow(c, iu_3);
+  eval_rhs(c, c->U[2].p, shadow(c, 2), t + 0.5 * dt, e3);
+  Epilogue e1{};
+  e1.kind = kStage1;
+  e1.dt = dt;
+  e1.out = c->U[1].p;
+  e1.out32 = shadow(c, 1);
+  eval_rhs(c, c->U[iu_3].p, shadow(c, iu_3), t + dt, e1);
+}
+
+void ssprk33_direct(mft_ctx* c, double dt, int nsteps) {
   const double t0 = c->t_state;
   for (int k = 0; k < nsteps; ++k) {
-    const double t = t0 + k * dt;
-    Epilogue e2{};
-    e2.kind = kStage2;
-    e2.dt = dt;
-    e2.u_n = c->U[0].p;
-    e2.out = c->U[2].p;
-    e2.out32 = shadow(c, 2);
-    eval_rhs(c, c->U[1].p, shadow(c, 1), t + dt, e2);
-    Epilogue e3{};
-    e3.kind = kStage3;
-    e3.dt = dt;
-    e3.u_n = c->U[0].p;
-    e3.out = c->U[3].p;
-    e3.out32 = shadow(c, 3);
-    eval_rhs(c, c->U[2].p, shadow(c, 2), t + 0.5 * dt, e3);
+    enqueue_step(c, dt, t0 + k * dt, 0, 3);
     const double tn = t0 + (k + 1) * dt;
-    Epilogue e1{};
-    e1.kind = kStage1;
-    e1.dt = dt;
-    e1.out = c->U[1].p;
-    e1.out32 = shadow(c, 1);
-    eval_rhs(c, c->U[3].p, shadow(c, 3), tn, e1);
     std::swap(c->U[0].p, c->U[3].p);
     std::swap(c->U32[0].p, c->U32[3].p);
     c->t_state = tn;
     if (c->hist_order >= 0) history_push(c, tn, c->U[0].p, c->success_iter + 1);
   }
+}
+
+// One SSP-RK3 step captured as a CUDA graph, once with u_n in U0 and once with u_n in
+// U3 (the buffers swap roles every step).  Per-step values (history weights, the ring
+// slot, success_iter) come from the step table at the device step counter.
+void capture_step_graphs(mft_ctx* c, double dt) {
+  for (int g = 0; g < 2; ++g) {
+    if (c->gexec[g]) cudaGraphExecDestroy(c->gexec[g]);
+    c->gexec[g] = nullptr;
+  }
+  c->graph_valid = false;
+  const int slots = c->hist_order + 1;
+  for (int g = 0; g < 2; ++g) {
+    const int iu_n = g == 0 ? 0 : 3, iu_3 = g == 0 ? 3 : 0;
+    MFT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    try {
+      enqueue_step(c, dt, 0.0, iu_n, iu_3);
+      if (c->hist_order >= 0) {
+        const double* ring[8];
+        for (int k = 0; k < slots; ++k) ring[k] = c->hist[k].p;
+        launch_history_dev((int64_t)c->n * c->nvars, c->U[iu_3].p, ring, slots, c->d_tab.p,
+                           c->d_ctr.p, c->approx_du.p, c->stream);
+      }
+      launch_step_advance(c->d_ctr.p, c->stream);
+    } catch (...) {
+      c->capturing = false;
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(c->stream, &junk);
+      if (junk) cudaGraphDestroy(junk);
+      throw;
+    }
+    c->capturing = false;
+    cudaGraph_t graph = nullptr;
+    MFT_CUDA(cudaStreamEndCapture(c->stream, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&c->gexec[g], graph, 0);
+    cudaGraphDestroy(graph);
+    MFT_CUDA(e);
+    c->graph_un[g] = c->U[iu_n].p;
+  }
+  c->graph_dt = dt;
+  c->graph_valid = true;
+}
+
+void ssprk33_graph(mft_ctx* c, double dt, int nsteps) {
+  const int slots = c->hist_order + 1;
+  // host-side bookkeeping of the HistoryCallback for the whole batch
+  std::vector<StepParams> tab(nsteps);
+  const double t0 = c->t_state;
+  for (int k = 0; k < nsteps; ++k) {
+    StepParams& sp = tab[k];
+    memset(&sp, 0, sizeof(sp));
+    sp.si_eps = c->success_iter;
+    if (c->hist_order >= 0) {
+      const double tn = t0 + (k + 1) * dt;
+      for (int q = slots - 1; q > 0; --q) c->hist_t[q] = c->hist_t[q - 1];
+      c->hist_t[0] = tn;
+      c->hist_head = (c->hist_head + slots - 1) % slots;
+      sp.head = c->hist_head;
+      const int push_si = c->success_iter + 1;
+      const int m = std::min(push_si + 1, slots);
+      double w[16];
+      MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
+                  "time_deriv_weights: singular Vandermonde system");
+      for (int q = 0; q < m; ++q) sp.w[q] = w[q];
+      sp.m = m;
+      c->success_iter = push_si;
+    }
+  }
+  if (c->d_tab.n < (size_t)nsteps) {
+    c->d_tab.alloc(std::max<size_t>(nsteps, 64));
+    c->graph_valid = false;
+  }
+  if (!c->d_ctr.p) c->d_ctr.alloc(1);
+  MFT_CUDA(cudaMemcpyAsync(c->d_tab.p, tab.data(), nsteps * sizeof(StepParams),
+                           cudaMemcpyHostToDevice, c->stream));
+  c->d_ctr.zero(c->stream);
+  if (!c->graph_valid || c->graph_dt != dt ||
+      (c->U[0].p != c->graph_un[0] && c->U[0].p != c->graph_un[1]))
+    capture_step_graphs(c, dt);
+  const int first = c->U[0].p == c->graph_un[0] ? 0 : 1;
+  for (int k = 0; k < nsteps; ++k) MFT_CUDA(cudaGraphLaunch(c->gexec[(first + k) & 1], c->stream));
+  if (nsteps & 1) {
+    std::swap(c->U[0].p, c->U[3].p);
+    std::swap(c->U32[0].p, c->U32[3].p);
+  }
+  c->t_state = t0 + nsteps * dt;
+  // the table must stay alive until the copy has been staged; it has (pageable source)
+  MFT_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void ssprk33_run(mft_ctx* c, double dt, int nsteps, bool use_graph = false) {
+  ensure_work(c);
+  fsal_eval(c, dt);
+  if (use_graph && nsteps > 0 && !c->dir_fn && !c->prof_on) ssprk33_graph(c, dt, nsteps);
+  else ssprk33_direct(c, dt, nsteps);
 }
 
 }  // namespace
@@ -1208,9 +1320,8 @@ mft_status mft_ssprk33(mft_ctx* c, double dt, int nsteps, int use_graph) {
     MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "call mft_set_state first");
     MFT_REQUIRE(nsteps >= 0, MFT_ERR_ARG, "nsteps < 0");
     MFT_REQUIRE(dt > 0 && isfinite(dt), MFT_ERR_ARG, "dt must be positive and finite");
-    (void)use_graph;
     set_device(c);
-    ssprk33_run(c, dt, nsteps);
+    ssprk33_run(c, dt, nsteps, use_graph != 0);
     MFT_CUDA(cudaStreamSynchronize(c->stream));
     check_kernel_errors(c);
   });

@@ -386,7 +386,8 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
     eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), an);
   }
   double eps;
-  if (a.kind == MFT_SRC_RV && a.success_iter != 0) {
+  const int si = a.tab ? a.tab[*a.ctr].si_eps : a.success_iter;
+  if (a.kind == MFT_SRC_RV && si != 0) {
     // residual / norm with the norms' reciprocals (written by k_lexmax after the norms)
     double mr = 0.0;
 #pragma unroll
@@ -609,6 +610,53 @@ void launch_rev_f64(const RevArgs& a, cudaStream_t s) {
     else if (a.lap) k_rev_f64<1, false, true><<<g, kBlock, 0, s>>>(a);
     else k_rev_f64<1, false, false><<<g, kBlock, 0, s>>>(a);
   }
+  MFT_LAUNCH_CHECK();
+}
+
+namespace {
+
+struct RingPtrs {
+  double* p[8];
+};
+
+// HistoryCallback push inside a captured step: the step's parameters come from the
+// step table at the device step counter.  ring[head] = u_new, then
+// approx_du = sum_{k<m} w_k ring[(head + k) % slots] (k = 0 is u_new itself).
+__global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, RingPtrs ring,
+                              int slots, const StepParams* __restrict__ tab,
+                              const int* __restrict__ ctr, double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const StepParams& sp = tab[*ctr];
+  const double un = u_new[i];
+  ring.p[sp.head][i] = un;
+  double acc = 0.0;
+  for (int k = 0; k < sp.m; ++k) {
+    const double hk = k == 0 ? un : ring.p[(sp.head + k) % slots][i];
+    acc = dadd(acc, dmul(sp.w[k], hk));
+  }
+  out[i] = acc;
+}
+
+__global__ void k_step_advance(int* ctr) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *ctr += 1;
+}
+
+}  // namespace
+
+void launch_history_dev(int64_t count, const double* u_new, const double* const* ring,
+                        int slots, const StepParams* tab, const int* ctr, double* approx_du,
+                        cudaStream_t s) {
+  if (count <= 0) return;
+  RingPtrs rp{};
+  for (int k = 0; k < slots && k < 8; ++k) rp.p[k] = const_cast<double*>(ring[k]);
+  k_history_dev<<<grid_for(count, 256), 256, 0, s>>>(count, u_new, rp, slots, tab, ctr,
+                                                      approx_du);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_step_advance(int* ctr, cudaStream_t s) {
+  k_step_advance<<<1, 32, 0, s>>>(ctr);
   MFT_LAUNCH_CHECK();
 }
 

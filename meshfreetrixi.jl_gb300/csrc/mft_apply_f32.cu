@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
       if (isnan(qv)) mr = qv;
     }
     const float eps_rv = 0.5f * (float)a.c_rv * h * h * mr;
-    if (isnan(eps_rv) || isinf(eps_rv) || a.success_iter == 0)
+    const int si = a.tab ? a.tab[*a.ctr].si_eps : a.success_iter;
+    if (isnan(eps_rv) || isinf(eps_rv) || si == 0)
       eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16f : eps_uw;
     else
       eps = fminf(eps_rv, eps_uw);

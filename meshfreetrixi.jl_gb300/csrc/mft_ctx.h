@@ -106,6 +106,15 @@ struct mft_ctx {
   int success_iter = 0;
   mft::DBuf<double> hist_w;
 
+  // one SSP-RK3 step as a CUDA graph (u_n in U0 / in U3) and its step table
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  const double* graph_un[2] = {nullptr, nullptr};
+  double graph_dt = 0.0;
+  bool graph_valid = false;
+  bool capturing = false;
+  mft::DBuf<mft::StepParams> d_tab;
+  mft::DBuf<int> d_ctr;
+
   // timing
   bool prof_on = false;
   std::vector<cudaEvent_t> ev_pool;

@@ -171,6 +171,8 @@ struct EpsArgs {
   int eq, V, kind;  // kind: MFT_SRC_RV or MFT_SRC_UPWIND
   double gamma, ax, ay, c_rv, c_uw, h;
   int success_iter;
+  const struct StepParams* tab;  // graph mode: success_iter = tab[*ctr].si_eps
+  const int* ctr;
   const double* u;
   const double* du_p;
   const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)
@@ -223,5 +225,20 @@ struct HistW {
 };
 void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
                     double* approx_du, cudaStream_t s);
+
+// Per-step parameters of a captured SSP-RK3 step, read on the device through a step
+// counter so that one graph serves every step of a batch.
+struct StepParams {
+  double w[8];       // time-derivative weights of the history push after the step
+  int m;             // number of history points used (0: approx_du = 0)
+  int si_eps;        // success_iter seen by the viscosity kernels during the step
+  int head;          // ring slot that receives the new state
+  int pad;
+};
+// Graph-mode history push: ring[tab.head] = u_new; approx_du = sum_k w_k ring_k.
+void launch_history_dev(int64_t count, const double* u_new, const double* const* ring,
+                        int slots, const StepParams* tab, const int* ctr, double* approx_du,
+                        cudaStream_t s);
+void launch_step_advance(int* ctr, cudaStream_t s);
 
 }  // namespace mft

@@ -120,3 +120,29 @@ def test_host_entry_point_equals_device_steps(gpu_lib):
         t = ctx.ssprk33_host(u, t, dt, 1)
     assert t == t_dev
     assert np.array_equal(u, u_dev)
+
+
+def test_graph_steps_equal_direct_steps(gpu_lib):
+    """Steps replayed from the captured per-step CUDA graphs (device step table for the
+    history weights) equal directly launched steps bit for bit, across odd batch sizes
+    that swap the state buffers and a change of dt."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(40)
+    res = []
+    for use_graph in (False, True):
+        eq = M.CompressibleEulerEquations2D(1.4)
+        basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+        solver = M.PointCloudSolver(basis)
+        domain = M.PointCloudDomain(solver, pts, period=per)
+        src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, domain))
+        semi = M.SemidiscretizationHyperbolic(domain, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                              solver, source_terms=src)
+        ctx = domain.ctx
+        ctx.history_init(3)
+        ctx.set_state(semi.compute_coefficients(0.0), 0.0)
+        for nsteps, dt in ((3, 0.1 * h), (2, 0.1 * h), (5, 0.1 * h), (1, 0.05 * h), (4, 0.05 * h)):
+            ctx.ssprk33(dt, nsteps, use_graph=use_graph)
+        res.append(ctx.get_state())
+    assert res[0][1] == res[1][1]
+    assert np.array_equal(res[0][0], res[1][0])
