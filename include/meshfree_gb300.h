@@ -170,6 +170,13 @@ mft_status mft_set_sources(mft_ctx* ctx, int n_src, const int* kinds, const doub
 
 mft_status mft_set_precision(mft_ctx* ctx, int precision);
 
+/* Ensembles: the context holds nseg independent point clouds back to back; member m owns
+ * nodes [offsets[m], offsets[m+1]) (offsets[0] = 0, offsets[nseg] = n) and its stencils
+ * must stay inside the member.  The residual-viscosity normalisation (ode_mean /
+ * ode_maximum, src/auxiliary/mpi.jl:40-81) is then taken per member, and h[m] is the
+ * member's dx_avg (replacing the source's h).  nseg = 0 returns to one problem. */
+mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, const double* h);
+
 /* Engine options.  MFT_OPT_GATHER selects the mapping of the FP32 operator gathers:
  * MFT_GATHER_THREAD (one node per thread, direct loads), MFT_GATHER_STAGED (one warp
  * per 32-node slice with the slice's indices and weights streamed into shared memory by

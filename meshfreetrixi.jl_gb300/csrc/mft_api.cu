@@ -553,7 +553,16 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     const int kind = c->src_kind[iv];
     const double* par = &c->src_par[iv * 4];
     const int mode = kind == MFT_SRC_RV ? (int)par[3] : 0;
-    if (kind == MFT_SRC_RV) {
+    if (kind == MFT_SRC_RV && c->nseg > 0) {
+      {
+        ProfScope ps(c, MFT_K_MEAN);
+        launch_mean_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, mode, c->seg_partial.p,
+                        c->seg_counter.p, c->seg_mean.p, s);
+      }
+      ProfScope ps(c, MFT_K_LEXMAX);
+      launch_lexmax_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, c->seg_mean.p, mode,
+                        c->seg_partial.p, c->seg_counter.p + c->nseg, c->seg_norms.p, s);
+    } else if (kind == MFT_SRC_RV) {
       const double denom = mode == 0 ? (double)n * V : (double)n;
       {
         ProfScope ps(c, MFT_K_MEAN);
@@ -581,7 +590,9 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ea.du_p32 = f32 ? dp32 : nullptr;
     ea.hvf = nullptr;
     ea.approx_du = c->approx_du.p;
-    ea.norms = c->norms.p;
+    ea.norms = c->nseg > 0 ? c->seg_norms.p : c->norms.p;
+    ea.seg_id = c->nseg > 0 ? c->d_seg_id.p : nullptr;
+    ea.seg_h = c->nseg > 0 ? c->d_seg_h.p : nullptr;
     ea.t = f32 ? nullptr : c->t.p;
     ea.t32 = f32 ? c->t32.p : nullptr;
     ea.eps = c->eps.p;
@@ -1023,6 +1034,45 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_TUNED_FWD) *value = c->last_fwd_choice;
     else if (option == MFT_OPT_TUNED_REV) *value = c->last_rev_choice;
     else throw mft::Error(MFT_ERR_ARG, "unknown option");
+  });
+}
+
+mft_status mft_set_segments(mft_ctx* c, int nseg, const int64_t* offsets, const double* h) {
+  return guarded(c, [&] {
+    c->graph_valid = false;
+    MFT_REQUIRE(c->n > 0, MFT_ERR_STATE, "call mft_set_points first");
+    MFT_REQUIRE(nseg >= 0 && nseg <= 1 << 20, MFT_ERR_ARG, "nseg out of range");
+    set_device(c);
+    c->fsal_valid = false;
+    if (nseg == 0) {
+      c->nseg = 0;
+      return;
+    }
+    MFT_REQUIRE(offsets && h, MFT_ERR_ARG, "NULL segment arrays");
+    MFT_REQUIRE(offsets[0] == 0 && offsets[nseg] == c->n, MFT_ERR_ARG,
+                "segment offsets must start at 0 and end at n");
+    for (int m = 0; m < nseg; ++m)
+      MFT_REQUIRE(offsets[m + 1] > offsets[m], MFT_ERR_ARG, "empty or unordered segment");
+    std::vector<int> sid(c->n);
+    for (int m = 0; m < nseg; ++m)
+      for (int64_t i = offsets[m]; i < offsets[m + 1]; ++i) sid[i] = m;
+    if (c->have_pattern)
+      for (int64_t i = 0; i < c->n; ++i)
+        for (int64_t e = c->rp[i]; e < c->rp[i + 1]; ++e)
+          MFT_REQUIRE(sid[c->ci[e]] == sid[i], MFT_ERR_ARG,
+                      "the stencil of node " + std::to_string(i) + " leaves its segment");
+    c->nseg = nseg;
+    c->seg_off.assign(offsets, offsets + nseg + 1);
+    cudaStream_t s = c->stream;
+    c->d_seg_off.upload(c->seg_off, s);
+    c->d_seg_id.upload(sid, s);
+    c->d_seg_h.upload(h, nseg, s);
+    c->seg_partial.alloc((size_t)nseg * kSegBlocks * 8);
+    c->seg_counter.alloc((size_t)2 * nseg);
+    c->seg_counter.zero(s);
+    c->seg_mean.alloc((size_t)nseg * 8);
+    c->seg_norms.alloc((size_t)nseg * 8);
+    MFT_CUDA(cudaStreamSynchronize(s));
   });
 }
 

@@ -362,12 +362,108 @@ __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __re
   }
 }
 
+// Segmented versions for ensembles: segment s owns nodes [off[s], off[s+1]) and is
+// reduced by `per` blocks (blockIdx.x = s * per + part); the last block of a segment
+// finishes it with the same strided-then-tree order as above.
+template <int V>
+__global__ void __launch_bounds__(kBlock) k_mean_seg(const int64_t* __restrict__ off, int per,
+                                                     const double* __restrict__ u, int mode,
+                                                     double* partial, unsigned* counter,
+                                                     double* mean) {
+  const int sg = blockIdx.x / per, part = blockIdx.x % per;
+  const int64_t lo = off[sg], hi = off[sg + 1];
+  double acc[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) acc[k] = 0.0;
+  for (int64_t i = lo + (int64_t)part * kBlock + threadIdx.x; i < hi; i += (int64_t)per * kBlock) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) acc[k] += u[i * V + k];
+  }
+  block_sum<V>(acc);
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = acc[k];
+    __threadfence();
+    last = (atomicAdd(counter + sg, 1u) == (unsigned)per - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < V; ++k) acc[k] = 0.0;
+  for (int b = threadIdx.x; b < per; b += kBlock)
+#pragma unroll
+    for (int k = 0; k < V; ++k) acc[k] += __ldcg(partial + (sg * per + b) * V + k);
+  block_sum<V>(acc);
+  if (threadIdx.x == 0) {
+    const double denom = mode == 0 ? (double)(hi - lo) * V : (double)(hi - lo);
+#pragma unroll
+    for (int k = 0; k < V; ++k) mean[sg * V + k] = acc[k] / denom;
+    counter[sg] = 0u;
+  }
+}
+
+template <int V>
+__global__ void __launch_bounds__(kBlock) k_lexmax_seg(const int64_t* __restrict__ off, int per,
+                                                       const double* __restrict__ u,
+                                                       const double* __restrict__ mean,
+                                                       int max_mode, double* partial,
+                                                       unsigned* counter, double* norms) {
+  const int sg = blockIdx.x / per, part = blockIdx.x % per;
+  const int64_t lo = off[sg], hi = off[sg + 1];
+  double m[V];
+  u64 best[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) { m[k] = mean[sg * V + k]; best[k] = 0ull; }
+  for (int64_t i = lo + (int64_t)part * kBlock + threadIdx.x; i < hi; i += (int64_t)per * kBlock) {
+    u64 x[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) x[k] = (u64)__double_as_longlong(fabs(dsub(u[i * V + k], m[k])));
+    key_max_into<V>(best, x, max_mode);
+  }
+  block_keymax<V>(best, max_mode);
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = __longlong_as_double((long long)best[k]);
+    __threadfence();
+    last = (atomicAdd(counter + sg, 1u) == (unsigned)per - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < V; ++k) best[k] = 0ull;
+  for (int b = threadIdx.x; b < per; b += kBlock) {
+    u64 c[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k)
+      c[k] = (u64)__double_as_longlong(__ldcg(partial + (sg * per + b) * V + k));
+    key_max_into<V>(best, c, max_mode);
+  }
+  block_keymax<V>(best, max_mode);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const double v = __longlong_as_double((long long)best[k]);
+      const double nv = v == 0.0 ? 2.220446049250313e-16 : v;
+      norms[sg * 2 * V + k] = nv;
+      norms[sg * 2 * V + V + k] = 1.0 / nv;
+    }
+    counter[sg] = 0u;
+  }
+}
+
 // ------------------------------------------------------------------ viscosity
 
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= a.n) return;
+  const int sg = a.seg_id ? a.seg_id[i] : 0;
+  const double h = a.seg_h ? a.seg_h[sg] : a.h;
+  const double* __restrict__ norms = a.norms + (a.seg_id ? sg * 2 * V : 0);
   double eps_uw;
   if (V == 4) {
     // one reciprocal instead of three divisions (FP64 division is a long sequence on
@@ -380,10 +476,10 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
     double c;
     if (p < 0.0 || rho < 0.0) c = 0.0;
     else c = sqrt(dmul(dmul(a.gamma, p), rinv));
-    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), dadd(speed, c));
+    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), h), dadd(speed, c));
   } else {
     const double an = sqrt(dadd(dmul(a.ax, a.ax), dmul(a.ay, a.ay)));
-    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), a.h), an);
+    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), h), an);
   }
   double eps;
   const int si = a.tab ? a.tab[*a.ctr].si_eps : a.success_iter;
@@ -395,10 +491,10 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
       double dp = a.du_p[i * V + v];
       if (a.hvf) dp = dadd(dp, a.hvf[i * V + v]);
       const double r = fabs(dsub(a.approx_du[i * V + v], dp));
-      const double qv = dmul(r, a.norms[V + v]);
+      const double qv = dmul(r, norms[V + v]);
       mr = v == 0 ? qv : jl_max(mr, qv);
     }
-    const double eps_rv = dmul(dmul(dmul(0.5, a.c_rv), dmul(a.h, a.h)), mr);
+    const double eps_rv = dmul(dmul(dmul(0.5, a.c_rv), dmul(h, h)), mr);
     if (isnan(eps_rv) || isinf(eps_rv)) {
       eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16 : eps_uw;
     } else {
@@ -582,6 +678,25 @@ void launch_lexmax(int64_t n, int V, const double* u, const double* mean, int ma
     k_lexmax<4><<<nblocks, kBlock, 0, s>>>(n, u, mean, max_mode, partial, counter, norms);
   else
     k_lexmax<1><<<nblocks, kBlock, 0, s>>>(n, u, mean, max_mode, partial, counter, norms);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double* u, int mode,
+                     double* partial, unsigned* counter, double* mean, cudaStream_t s) {
+  if (nseg <= 0) return;
+  if (V == 4) k_mean_seg<4><<<nseg * per, kBlock, 0, s>>>(off, per, u, mode, partial, counter, mean);
+  else k_mean_seg<1><<<nseg * per, kBlock, 0, s>>>(off, per, u, mode, partial, counter, mean);
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_lexmax_seg(int nseg, const int64_t* off, int per, int V, const double* u,
+                       const double* mean, int max_mode, double* partial, unsigned* counter,
+                       double* norms, cudaStream_t s) {
+  if (nseg <= 0) return;
+  if (V == 4)
+    k_lexmax_seg<4><<<nseg * per, kBlock, 0, s>>>(off, per, u, mean, max_mode, partial, counter, norms);
+  else
+    k_lexmax_seg<1><<<nseg * per, kBlock, 0, s>>>(off, per, u, mean, max_mode, partial, counter, norms);
   MFT_LAUNCH_CHECK();
 }
 

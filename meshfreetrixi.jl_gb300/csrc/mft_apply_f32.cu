@@ -100,7 +100,9 @@ template <int V>
 __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= a.n) return;
-  const float h = (float)a.h;
+  const int sg = a.seg_id ? a.seg_id[i] : 0;
+  const float h = (float)(a.seg_h ? a.seg_h[sg] : a.h);
+  const double* __restrict__ norms = a.norms + (a.seg_id ? sg * 2 * V : 0);
   float eps_uw;
   if (V == 4) {
     const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
       float dp = a.du_p32[i * V + v];
       if (a.hvf) dp += (float)a.hvf[i * V + v];
       const float r = fabsf((float)a.approx_du[i * V + v] - dp);
-      const float qv = r / (float)a.norms[v];
+      const float qv = r * (float)norms[V + v];
       mr = v == 0 ? qv : fmaxf(mr, qv);
       if (isnan(qv)) mr = qv;
     }

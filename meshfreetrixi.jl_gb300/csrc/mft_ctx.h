@@ -13,6 +13,8 @@
 constexpr int kSlotLap = 3;
 constexpr int kSlotHv = 4;
 constexpr int kSlots = 5;
+// Blocks per ensemble member in the segmented reductions.
+constexpr int kSegBlocks = 8;
 
 struct mft_ctx {
   int device = 0;
@@ -105,6 +107,14 @@ struct mft_ctx {
   int hist_head = 0;
   int success_iter = 0;
   mft::DBuf<double> hist_w;
+
+  // ensemble members (segments)
+  int nseg = 0;
+  std::vector<int64_t> seg_off;
+  mft::DBuf<int64_t> d_seg_off;
+  mft::DBuf<int> d_seg_id;
+  mft::DBuf<double> d_seg_h, seg_partial, seg_mean, seg_norms;
+  mft::DBuf<unsigned> seg_counter;
 
   // one SSP-RK3 step as a CUDA graph (u_n in U0 / in U3) and its step table
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};

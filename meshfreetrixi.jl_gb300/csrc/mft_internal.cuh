@@ -173,6 +173,8 @@ struct EpsArgs {
   int success_iter;
   const struct StepParams* tab;  // graph mode: success_iter = tab[*ctr].si_eps
   const int* ctr;
+  const int* seg_id;       // ensembles: segment of each node (null: one problem)
+  const double* seg_h;     // ensembles: dx_avg per segment; norms hold 2V per segment
   const double* u;
   const double* du_p;
   const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)
@@ -184,6 +186,11 @@ struct EpsArgs {
   float* t32;              // FP32 path: scaled in place
 };
 void launch_eps(const EpsArgs& a, cudaStream_t s);
+void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double* u, int mode,
+                     double* partial, unsigned* counter, double* mean, cudaStream_t s);
+void launch_lexmax_seg(int nseg, const int64_t* off, int per, int V, const double* u,
+                       const double* mean, int max_mode, double* partial, unsigned* counter,
+                       double* norms, cudaStream_t s);
 void launch_eps_f32(const EpsArgs& a, cudaStream_t s);
 
 struct RevArgs {

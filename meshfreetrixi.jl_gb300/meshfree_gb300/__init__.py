@@ -5,7 +5,7 @@ from .api import (  # noqa: F401
     RBF, BoundaryConditionDirichlet, BoundaryConditionDoNothing, BoundaryData,
     CompressibleEulerEquations2D, HistoryCallback, LinearScalarAdvectionEquation2D, ODEProblem,
     Point1D, Point2D, Point3D, PointCloudBasis, PointCloudDomain, PointCloudDomain_from_medusa,
-    PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
+    PointCloudEnsemble, PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
     SemidiscretizationHyperbolic, SourceHyperviscosityFlyer, SourceHyperviscosityTominec,
     SourceResidualViscosityTominec, SourceTerms, SourceUpwindViscosityTominec, SSPRK33,
     boundary_condition_slip_wall, rhs_, semidiscretize, solve)

@@ -48,6 +48,7 @@ SIGNATURES = {
     "mft_set_sources": (I32, [VP, I32, VP, VP]),
     "mft_set_precision": (I32, [VP, I32]),
     "mft_set_option": (I32, [VP, I32, I32]),
+    "mft_set_segments": (I32, [VP, I32, VP, VP]),
     "mft_get_option": (I32, [VP, I32, C.POINTER(I32)]),
     "mft_rhs": (I32, [VP, VP, VP, I32, DBL]),
     "mft_rhs_device": (I32, [VP, VP, VP, DBL]),
@@ -196,6 +197,14 @@ class Context:
 
     def set_precision(self, prec):
         self.check(self.lib.mft_set_precision(self.h, prec))
+
+    def set_segments(self, offsets, h):
+        """Ensemble members: offsets (nseg+1) and per-member dx_avg (nseg)."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        hh = np.ascontiguousarray(h, dtype=np.float64)
+        nseg = off.size - 1
+        self.check(self.lib.mft_set_segments(self.h, nseg, _p(off) if nseg else None,
+                                             _p(hh) if nseg else None))
 
     def set_option(self, option, value):
         self.check(self.lib.mft_set_option(self.h, option, value))

@@ -146,6 +146,53 @@ class PointCloudDomain:
             self.loaded[op] = key
 
 
+class PointCloudEnsemble(PointCloudDomain):
+    """Independent point clouds advanced together in one engine context (one set of
+    kernels and one graph per step for all members).  Member m owns nodes
+    offsets[m]:offsets[m+1]; stencils are built per member (GPU KNN) and never cross
+    members; the residual-viscosity normalisation and dx_avg are per member."""
+
+    def __init__(self, solver, member_points, period=None):
+        basis = solver.basis
+        self.solver = solver
+        self.period = None if period is None else tuple(float(p) for p in period)
+        k = basis.nv
+        idx_all, pts_all, dmins, davgs, offs = [], [], [], [0], []
+        tmp = L.Context(solver.engine.device)
+        for pts in member_points:
+            pts = np.ascontiguousarray(pts, dtype=np.float64)
+            tmp.set_points(pts, self.period)
+            idx, _d, dmin, davg = tmp.knn(k)
+            idx_all.append(idx.astype(np.int64) + offs[-1])
+            pts_all.append(pts)
+            dmins.append(dmin)
+            davgs.append(davg)
+            offs.append(offs[-1] + pts.shape[0])
+        tmp.close()
+        points = np.ascontiguousarray(np.concatenate(pts_all))
+        neighbors = np.ascontiguousarray(np.concatenate(idx_all).astype(np.int32))
+        self.offsets = np.asarray(offs, dtype=np.int64)
+        self.dx_min = np.asarray(dmins)
+        self.dx_avg = np.asarray(davgs)
+        self.ctx = L.Context(solver.engine.device)
+        self.ctx.set_points(points, self.period)
+        n = points.shape[0]
+        self.ctx.set_stencils(np.arange(n + 1, dtype=np.int64) * k, neighbors.ravel())
+        self.ctx.set_segments(self.offsets, self.dx_avg)
+        self.pd = PointData(points, neighbors, n, k, float(self.dx_min.min()),
+                            float(self.dx_avg.mean()))
+        self.boundary_tags = {}
+        self.loaded = {}
+
+    @property
+    def members(self):
+        return len(self.offsets) - 1
+
+    def member(self, u, m):
+        """Member m's slice of an (nvars, n) ensemble state."""
+        return u[:, self.offsets[m]:self.offsets[m + 1]]
+
+
 def PointCloudDomain_from_medusa(solver, casename, boundary_names):
     """PointCloudDomain(solver, casename, Dict(:inlet => 1, ...)) (types.jl:133-145,
     SerialPointCloud.jl:45-54)."""
