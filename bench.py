@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-side", type=int, default=N_SIDE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ens-members", type=int, default=64,
+                    help="members of the ensemble measurement (0 skips it)")
     return ap.parse_args()
 
 
@@ -175,6 +177,64 @@ def timed_steps(ctx, u0, dt, warmup, steps, pg, clocks=None):
     return ms, prof, clk, u_end, ms_prof
 
 
+def ensemble_sizes(members, lo, hi, seed=5):
+    """Member node counts drawn uniformly from [lo, hi], rounded to square grids."""
+    rng = np.random.default_rng(seed)
+    return [int(round(math.sqrt(v))) for v in rng.uniform(lo, hi, members)]
+
+
+def run_ensemble(args, local, pg):
+    """64 independent vortex problems (N uniform in 4,096-131,072) advanced together:
+    one context, one CUDA graph per SSP-RK3 step for all members.  The same members
+    stepped one context after another (each its own per-step graph) are timed beside it."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    sides = ensemble_sizes(args.ens_members, 4096, 131072)
+    clouds = [W.vortex_cloud(s, seed=1000 + i) for i, s in enumerate(sides)]
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64"))
+    eq = M.CompressibleEulerEquations2D(1.4)
+
+    def semi_of(dom):
+        src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom))
+        return M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                              solver, source_terms=src)
+
+    dt = DT_FACTOR * min(c[2] for c in clouds)
+    ens = M.PointCloudEnsemble(solver, [c[0] for c in clouds], period=(10.0, 10.0))
+    semi = semi_of(ens)
+    u0 = semi.compute_coefficients(0.0)
+    ntot = int(ens.offsets[-1])
+    ms, prof, _, _, _ = timed_steps(ens.ctx, u0, dt, args.warmup, args.steps, pg)
+    ms = max_over_ranks(pg, ms)
+    ens.ctx.close()
+    # the same members, one context each, stepped one after another
+    ms_seq = 0.0
+    for pts, per, _h in clouds:
+        dom = M.PointCloudDomain(solver, pts, period=per)
+        s1 = semi_of(dom)
+        ctx = dom.ctx
+        ctx.history_init(3)
+        ctx.set_state(s1.compute_coefficients(0.0), 0.0)
+        ctx.ssprk33(dt, args.warmup, use_graph=True)
+        ctx.sync()
+        ctx.region_begin()
+        ctx.ssprk33(dt, args.steps, use_graph=True)
+        ms_seq += ctx.region_end()
+        ctx.close()
+    ms_seq = max_over_ranks(pg, ms_seq)
+    launches = sum(v[1] for v in prof.values())
+    return {"members": len(sides), "total_nodes": ntot,
+            "member_nodes": {"min": min(s * s for s in sides), "max": max(s * s for s in sides)},
+            "value": ntot * RHS_PER_STEP * args.steps / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms / args.steps, "steps": args.steps,
+            "kernel_launches_per_step": launches / args.steps,
+            "members_one_at_a_time": {"value": ntot * RHS_PER_STEP * args.steps / (ms_seq * 1e-3),
+                                      "ms_per_step": ms_seq / args.steps},
+            "workload": "isentropic vortex members on [-5,5]^2, k=%d, RV + history (order 3), "
+                        "FP64, dt=0.2 min(h), one CUDA graph per SSP-RK3 step" % K_STENCIL}
+
+
 def roofline(prof, n, prec, peaks):
     name = max(prof, key=lambda k: prof[k][0])
     ms, launches = prof[name]
@@ -215,7 +275,7 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def cpu_baseline_oracle(n_side, steps, nthreads):
+def cpu_baseline_oracle(n_side, max_steps, nthreads, min_seconds=10.0):
     """The oracle's rhs! + SSP-RK3 on the host cores over a bounded number of steps."""
     from oracle import oracle as O
     from meshfree_gb300 import workloads as W
@@ -228,11 +288,15 @@ def cpu_baseline_oracle(n_side, steps, nthreads):
     semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=(O.SRC_RV,), h=davg)
     u0 = W.isentropic_vortex(pts, 0.0)
     hist = O.History(semi, 3)
-    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, 1, history=hist, nthreads=nthreads)  # warm-up
     t0 = time.perf_counter()
-    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, steps, history=hist, nthreads=nthreads)
+    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, 1, history=hist, nthreads=nthreads)  # warm-up
+    per_step = (time.perf_counter() - t0) / 1.33    # 4 rhs! evaluations in a 1-step call
+    done = int(min(max_steps, max(2, min_seconds / per_step)))   # a sample of ~min_seconds
+    hist = O.History(semi, 3)
+    t0 = time.perf_counter()
+    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, done, history=hist, nthreads=nthreads)
     sec = time.perf_counter() - t0
-    return n * RHS_PER_STEP * steps / sec, sec
+    return n * RHS_PER_STEP * done / sec, sec, done
 
 
 def run_reference(args):
@@ -322,12 +386,14 @@ def run_ours(args):
         t = ctx.ssprk33_host(uh, t, dt, 1)
     ms_e2e = max_over_ranks(pg, ctx.region_end())
     e2e = n * RHS_PER_STEP * args.steps * ws / (ms_e2e * 1e-3)
+    ctx.close()
+
+    ens = run_ensemble(args, local, pg) if args.ens_members > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        cpu_steps = 2
-        v, sec = cpu_baseline_oracle(args.n_side, cpu_steps, nthreads)
+        v, sec, cpu_steps = cpu_baseline_oracle(args.n_side, 400, nthreads)
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": "full N=%d, %d SSP-RK3 steps (%.1f s), oracle rhs! with OpenMP"
                          % (n, cpu_steps, sec)}
@@ -352,6 +418,7 @@ def run_ours(args):
                        "steps": args.steps, "roofline": roof32,
                        "autotuned_mapping": mapping,
                        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
+        "ensemble": ens,
     }
     print(json.dumps(line), flush=True)
 

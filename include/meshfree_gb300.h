@@ -229,6 +229,37 @@ mft_status mft_set_rv_state(mft_ctx* ctx, const double* const* approx_du, int nv
 /* Viscosity of the last RV/upwind source evaluation (host, n values). */
 mft_status mft_get_viscosity(mft_ctx* ctx, double* eps);
 
+/* ---------------------------------------------------------------- adjoint
+ * Reverse-mode derivatives of rhs! and of the SSP-RK3 trajectory.  No function of
+ * the reference corresponds: MeshfreeTrixi.jl differentiates rhs! only through
+ * ForwardDiff.jl duals; these entry points are what a ChainRulesCore rrule for
+ * rhs! and for solve() would call.  Covered: 2D Euler and linear advection, the
+ * strong BCs (Dirichlet, slip wall, do-nothing), the hyperviscosity sources, FP64.
+ * A residual-viscosity or upwind-viscosity source gives MFT_ERR_UNSUPPORTED (its
+ * viscosity is a maximum over the field). */
+
+/* out = (d rhs!(u, t) / du)^T lam with host StructArray-style arrays (nvars pointers
+ * of length n).  u is not mutated. */
+mft_status mft_rhs_adjoint(mft_ctx* ctx, double* const* out, const double* const* lam,
+                           const double* const* u, int nvars, double t);
+
+/* Same on caller-owned device memory: out, lam, u are nvars x n (SoA) FP64. */
+mft_status mft_rhs_adjoint_device(mft_ctx* ctx, double* out, const double* lam, const double* u,
+                                  double t);
+
+/* Advances the device state nsteps SSP-RK3 steps of size dt (the same arithmetic as
+ * mft_ssprk33) and records the trajectory for mft_ssprk33_adjoint: the state every
+ * `every` steps (the stage states are recomputed from these checkpoints during the
+ * reverse sweep), or every stage state of every step when every == 0. */
+mft_status mft_ssprk33_record(mft_ctx* ctx, double dt, int nsteps, int every);
+
+/* Reverse sweep over the recorded trajectory.  On entry lam (host StructArray-style)
+ * holds dJ/du at the final state; on return it holds dJ/du at the initial state. */
+mft_status mft_ssprk33_adjoint(mft_ctx* ctx, double* const* lam, int nvars);
+
+/* Same on caller-owned device memory (nvars x n SoA FP64), in place. */
+mft_status mft_ssprk33_adjoint_device(mft_ctx* ctx, double* lam);
+
 /* ---------------------------------------------------------------- timing
  * Device timing with CUDA events on the context stream (the reference wraps the
  * same phases in @trixi_timeit timers, rbfsolver.jl:400-425). */
@@ -236,7 +267,7 @@ mft_status mft_get_viscosity(mft_ctx* ctx, double* eps);
 /* Kernel kinds reported by mft_profile_get. */
 enum {
   MFT_K_BC = 0, MFT_K_FLUX, MFT_K_FWD, MFT_K_MEAN, MFT_K_LEXMAX, MFT_K_EPS, MFT_K_REV,
-  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_COUNT
+  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_ADJ, MFT_K_COUNT
 };
 
 /* enable != 0 starts recording an event pair around every kernel launch (and clears

@@ -1,0 +1,222 @@
+// Adjoint of rhs! on the device.
+//
+// rhs!(u) = M2 [ -sum_d D_d F_d(P u) - gamma H P u ] with P the strong-BC pass
+// (Dirichlet values, slip-wall momentum projection; derivative Pi) and M2 the rows
+// the second BC pass zeroes.  Its transpose product
+//   r = Pi [ -sum_d J_Fd(P u)^T D_d^T (M2 lam) - gamma H^T (M2 lam) ]
+// is one transpose-stencil gather over the reverse adjacency (the CSC view of the
+// operator stored as a sliced ELL), fused with the flux-Jacobian-transpose product
+// at the gathering node and with the SSP-RK3 adjoint stage combination.
+#include "mft_device.cuh"
+
+namespace mft {
+namespace {
+
+using namespace dev;
+
+// M2 at node c: Dirichlet rows carry no cotangent, slip walls none in momentum.
+template <int V>
+static __device__ __forceinline__ void mask_rows(const BcDev& bc, int64_t c, double* l) {
+  const int tag = bc.tag[c];
+  if (tag == 1) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) l[v] = 0.0;
+  } else if (tag == 2) {
+    if constexpr (V == 4) {
+      l[1] = 0.0;
+      l[2] = 0.0;
+    }
+  }
+}
+
+template <int V>
+static __device__ __forceinline__ void load_row(const double* a, int64_t c, double* l) {
+  if constexpr (V == 4) {
+    const double2* p = reinterpret_cast<const double2*>(a) + c * 2;
+    const double2 x = __ldg(p), y = __ldg(p + 1);
+    l[0] = x.x; l[1] = x.y; l[2] = y.x; l[3] = y.y;
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v) l[v] = __ldg(a + c * V + v);
+  }
+}
+
+// Pi at node i on a cotangent row.
+template <int V>
+static __device__ __forceinline__ void project_row(const BcDev& bc, int64_t i, double* o) {
+  const int tag = bc.tag[i];
+  if (tag == 1) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) o[v] = 0.0;
+  } else if (tag == 2) {
+    if constexpr (V == 4) slip(bc.normal + 2 * (int64_t)bc.slot[i], o);
+  }
+}
+
+template <int V, bool EULER, bool BC, int HV>
+__global__ void __launch_bounds__(kBlock) k_adj_f64(AdjArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
+  const int len = a.ell.row_len[i];
+  double gx[V], gy[V], gh[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) { gx[v] = 0; gy[v] = 0; gh[v] = 0; }
+#pragma unroll 2
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(a.ell.col + p);
+    const double wx = __ldg(a.w[0] + p), wy = __ldg(a.w[1] + p);
+    double l[V];
+    load_row<V>(a.lam, c, l);
+    if (BC) mask_rows<V>(a.bc, c, l);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      gx[v] = fma(wx, l[v], gx[v]);
+      gy[v] = fma(wy, l[v], gy[v]);
+    }
+    if constexpr (HV == 2) {
+      const double wh = __ldg(a.wh + p);
+#pragma unroll
+      for (int v = 0; v < V; ++v) gh[v] = fma(wh, l[v], gh[v]);
+    } else if constexpr (HV == 1) {
+      const double wh = __ldg(a.wh + p);
+      double qq[V];
+      load_row<V>(a.q, c, qq);
+#pragma unroll
+      for (int v = 0; v < V; ++v) gh[v] = fma(wh, qq[v], gh[v]);
+    }
+  }
+  double r[V];
+  if constexpr (EULER) {
+    double uu[4];
+    load_row<4>(a.u, i, uu);
+    if (BC && a.bc.tag[i] == 2) slip(a.bc.normal + 2 * (int64_t)a.bc.slot[i], uu);
+    double ub[4];
+    euler_flux_vjp(a.gamma, uu, gx, gy, ub);
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = -ub[v];
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = -(a.ax * gx[v] + a.ay * gy[v]);
+  }
+  if constexpr (HV != 0) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = fma(-a.hv_gamma, gh[v], r[v]);
+  }
+  double o[V];
+  if (a.kind == kAdjPlain) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) o[v] = r[v];
+  } else {
+    double li[V];
+    load_row<V>(a.lam, i, li);
+    if (a.kind == kAdjStage3) {
+      const double c3 = 2.0 / 3.0, cr = 2.0 * a.dt / 3.0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        o[v] = c3 * li[v] + cr * r[v];
+        a.acc[i * V + v] = li[v] / 3.0;
+      }
+    } else if (a.kind == kAdjStage2) {
+      const double cr = 0.25 * a.dt;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        o[v] = 0.25 * li[v] + cr * r[v];
+        a.acc[i * V + v] = a.acc[i * V + v] + 0.75 * li[v];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) o[v] = (a.acc[i * V + v] + li[v]) + a.dt * r[v];
+    }
+  }
+  if (BC) project_row<V>(a.bc, i, o);
+#pragma unroll
+  for (int v = 0; v < V; ++v) a.out[i * V + v] = o[v];
+}
+
+// q_i = sum_j lap[i,j] (M2 lam)_j over the forward sliced ELL.
+template <int V, bool BC>
+__global__ void __launch_bounds__(kBlock) k_lap_masked(int64_t n, EllView ell, const double* wl,
+                                                       const double* lam, BcDev bc, double* q) {
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= n) return;
+  const int64_t base = ell.slice_off[i >> 5] + (i & 31);
+  const int len = ell.row_len[i];
+  double acc[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) acc[v] = 0;
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(ell.col + p);
+    const double w = __ldg(wl + p);
+    double l[V];
+    load_row<V>(lam, c, l);
+    if (BC) mask_rows<V>(bc, c, l);
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = fma(w, l[v], acc[v]);
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) q[i * V + v] = acc[v];
+}
+
+template <int V>
+__global__ void k_bc_project(int64_t nb, const int32_t* bnode, BcDev bc, double* lam) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  const int64_t i = bnode[k];
+  double o[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) o[v] = lam[i * V + v];
+  project_row<V>(bc, i, o);
+#pragma unroll
+  for (int v = 0; v < V; ++v) lam[i * V + v] = o[v];
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+template <int V, bool EULER, bool BC>
+void adj_hv(const AdjArgs& a, cudaStream_t s) {
+  const unsigned g = grid_for(a.n, kBlock);
+  if (a.hv == 1) k_adj_f64<V, EULER, BC, 1><<<g, kBlock, 0, s>>>(a);
+  else if (a.hv == 2) k_adj_f64<V, EULER, BC, 2><<<g, kBlock, 0, s>>>(a);
+  else k_adj_f64<V, EULER, BC, 0><<<g, kBlock, 0, s>>>(a);
+}
+
+}  // namespace
+
+void launch_adj_f64(const AdjArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  if (a.V == 4) {
+    if (a.has_bc) adj_hv<4, true, true>(a, s);
+    else adj_hv<4, true, false>(a, s);
+  } else {
+    if (a.has_bc) adj_hv<1, false, true>(a, s);
+    else adj_hv<1, false, false>(a, s);
+  }
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_lap_masked(int64_t n, EllView fwd, const double* wl, const double* lam, int V,
+                       BcDev bc, int has_bc, double* q, cudaStream_t s) {
+  if (n <= 0) return;
+  const unsigned g = grid_for(n, kBlock);
+  if (V == 4) {
+    if (has_bc) k_lap_masked<4, true><<<g, kBlock, 0, s>>>(n, fwd, wl, lam, bc, q);
+    else k_lap_masked<4, false><<<g, kBlock, 0, s>>>(n, fwd, wl, lam, bc, q);
+  } else {
+    if (has_bc) k_lap_masked<1, true><<<g, kBlock, 0, s>>>(n, fwd, wl, lam, bc, q);
+    else k_lap_masked<1, false><<<g, kBlock, 0, s>>>(n, fwd, wl, lam, bc, q);
+  }
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_bc_project(int64_t nb, const int32_t* bnode, int V, BcDev bc, double* lam,
+                       cudaStream_t s) {
+  if (nb <= 0) return;
+  if (V == 4) k_bc_project<4><<<grid_for(nb, 256), 256, 0, s>>>(nb, bnode, bc, lam);
+  else k_bc_project<1><<<grid_for(nb, 256), 256, 0, s>>>(nb, bnode, bc, lam);
+  MFT_LAUNCH_CHECK();
+}
+
+}  // namespace mft

@@ -1460,7 +1460,7 @@ mft_status mft_profile_get(mft_ctx* c, int kind, double* total_ms, int64_t* laun
                            const char** name) {
   static const char* names[MFT_K_COUNT] = {"bc_pass1", "flux", "fwd_gather", "mean",
                                            "lexmax", "eps", "rev_gather", "rev_lap",
-                                           "history", "layout"};
+                                           "history", "layout", "adjoint"};
   return guarded(c, [&] {
     MFT_REQUIRE(kind >= 0 && kind < MFT_K_COUNT, MFT_ERR_ARG, "bad kernel kind");
     set_device(c);
@@ -1496,6 +1496,308 @@ mft_status mft_get_viscosity(mft_ctx* c, double* eps) {
     MFT_CUDA(cudaMemcpyAsync(eps, c->eps.p, c->n * sizeof(double), cudaMemcpyDeviceToHost,
                              c->stream));
     MFT_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+// ---------------------------------------------------------------- adjoint
+
+namespace {
+
+// Hyperviscosity mode of the adjoint (0 none, 1 Tominec, 2 Flyer) and its gamma;
+// viscosity sources have no adjoint.
+int adj_hv_mode(mft_ctx* c, double* gamma) {
+  int mode = 0;
+  *gamma = 0.0;
+  for (size_t k = 0; k < c->src_kind.size(); ++k) {
+    const int kind = c->src_kind[k];
+    MFT_REQUIRE(kind != MFT_SRC_RV && kind != MFT_SRC_UPWIND, MFT_ERR_UNSUPPORTED,
+                "adjoint: residual/upwind viscosity has no adjoint (its viscosity is a "
+                "maximum over the field)");
+    MFT_REQUIRE(mode == 0, MFT_ERR_UNSUPPORTED, "more than one hyperviscosity source");
+    mode = kind == MFT_SRC_HV_TOMINEC ? 1 : 2;
+    *gamma = c->src_par[k * 4];
+  }
+  return mode;
+}
+
+void check_adjoint_ready(mft_ctx* c) {
+  check_state_ready(c);
+  MFT_REQUIRE(c->dim == 2, MFT_ERR_UNSUPPORTED, "adjoint: 2D problems only");
+  MFT_REQUIRE(c->precision == MFT_PREC_FP64, MFT_ERR_UNSUPPORTED, "adjoint: FP64 form only");
+  double g;
+  adj_hv_mode(c, &g);
+}
+
+void ensure_adj_work(mft_ctx* c) {
+  const size_t nv = (size_t)c->n * c->nvars;
+  for (auto& b : c->adj_lam) b.alloc(nv);
+  c->adj_acc.alloc(nv);
+  c->adj_q.alloc(nv);
+}
+
+// out = stage combination `kind` of (d rhs!/du)^T lam at state u (n x V AoS, device).
+void eval_rhs_adjoint(mft_ctx* c, const double* u, const double* lam, int kind, double dt,
+                      double* acc, double* out) {
+  ensure_device_ops(c);
+  ensure_bcs(c);
+  double hv_gamma = 0.0;
+  const int hv = adj_hv_mode(c, &hv_gamma);
+  if (hv == 1) MFT_REQUIRE(c->have_val[kSlotLap], MFT_ERR_STATE, "Tominec HV needs MFT_OP_LAP");
+  if (hv == 2) MFT_REQUIRE(c->have_val[kSlotHv], MFT_ERR_STATE, "Flyer HV needs MFT_OP_HV");
+  MFT_REQUIRE(out != lam, MFT_ERR_ARG, "adjoint output aliases its input");
+  cudaStream_t s = c->stream;
+  BcDev bc{c->d_tag.p, c->d_slot.p, c->d_normal.p, c->d_dvals.p};
+  const int has_bc = c->nb > 0;
+  if (hv == 1) {
+    ProfScope ps(c, MFT_K_ADJ);
+    launch_lap_masked(c->n, c->fwd.view(), c->fw[kSlotLap].p, lam, c->nvars, bc, has_bc,
+                      c->adj_q.p, s);
+  }
+  AdjArgs a{};
+  a.n = c->n;
+  a.ell = c->rev.view();
+  a.w[0] = c->rw[0].p;
+  a.w[1] = c->rw[1].p;
+  a.wh = hv == 1 ? c->rw[kSlotLap].p : (hv == 2 ? c->rw[kSlotHv].p : nullptr);
+  a.hv = hv;
+  a.hv_gamma = hv_gamma;
+  a.lam = lam;
+  a.q = c->adj_q.p;
+  a.u = u;
+  a.eq = c->eq;
+  a.V = c->nvars;
+  a.gamma = c->gamma;
+  a.ax = c->adv[0];
+  a.ay = c->adv[1];
+  a.bc = bc;
+  a.has_bc = has_bc;
+  a.kind = kind;
+  a.dt = dt;
+  a.acc = acc;
+  a.out = out;
+  ProfScope ps(c, MFT_K_ADJ);
+  launch_adj_f64(a, s);
+}
+
+// Time of the first stage of step k as the FSAL integrator evaluates it.
+double stage1_time(double t0, double dt, int k) { return k == 0 ? t0 : (t0 + (k - 1) * dt) + dt; }
+
+// One SSP-RK3 step from x: stage states into s1, s2, the next state into y.  Same
+// kernels and epilogues as the FSAL integrator (the first stage fused here).
+void record_step(mft_ctx* c, double dt, int k, double* x, double* s1, double* s2, double* y) {
+  const double t0 = c->adj_t0;
+  const double t = t0 + k * dt;
+  Epilogue e1{};
+  e1.kind = kStage1;
+  e1.dt = dt;
+  e1.out = s1;
+  eval_rhs(c, x, nullptr, stage1_time(t0, dt, k), e1);
+  Epilogue e2{};
+  e2.kind = kStage2;
+  e2.dt = dt;
+  e2.u_n = x;
+  e2.out = s2;
+  eval_rhs(c, s1, nullptr, t + dt, e2);
+  Epilogue e3{};
+  e3.kind = kStage3;
+  e3.dt = dt;
+  e3.u_n = x;
+  e3.out = y;
+  eval_rhs(c, s2, nullptr, t + 0.5 * dt, e3);
+}
+
+void d2d(mft_ctx* c, double* dst, const double* src, size_t count) {
+  MFT_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+}
+
+void ssprk33_record(mft_ctx* c, double dt, int nsteps, int every) {
+  ensure_work(c);
+  ensure_adj_work(c);
+  const size_t nv = (size_t)c->n * c->nvars;
+  c->adj_valid = false;
+  c->adj_t0 = c->t_state;
+  c->adj_dt = dt;
+  c->adj_nsteps = nsteps;
+  c->adj_every = every;
+  if (every == 0) {
+    c->adj_ckpt.release();
+    c->adj_store.alloc((size_t)3 * nsteps * nv);
+    double* st = c->adj_store.p;
+    d2d(c, st, c->U[0].p, nv);
+    for (int k = 0; k < nsteps; ++k) {
+      double* x = st + (size_t)3 * k * nv;
+      double* y = k + 1 < nsteps ? x + 3 * nv : c->U[0].p;
+      record_step(c, dt, k, x, x + nv, x + 2 * nv, y);
+    }
+  } else {
+    const int nck = (nsteps + every - 1) / every;
+    c->adj_ckpt.alloc((size_t)nck * nv);
+    c->adj_store.alloc((size_t)3 * every * nv);
+    for (int k = 0; k < nsteps; ++k) {
+      if (k % every == 0) d2d(c, c->adj_ckpt.p + (size_t)(k / every) * nv, c->U[0].p, nv);
+      record_step(c, dt, k, c->U[0].p, c->U[1].p, c->U[2].p, c->U[3].p);
+      std::swap(c->U[0].p, c->U[3].p);
+    }
+  }
+  c->t_state = c->adj_t0 + nsteps * dt;
+  // the pending first stage of the next step, as the FSAL integrator leaves it
+  Epilogue e1{};
+  e1.kind = kStage1;
+  e1.dt = dt;
+  e1.out = c->U[1].p;
+  eval_rhs(c, c->U[0].p, nullptr, stage1_time(c->adj_t0, dt, nsteps), e1);
+  c->fsal_valid = true;
+  c->fsal_dt = dt;
+  c->adj_valid = true;
+}
+
+// Reverse sweep; L holds Pi lam_T on entry (n x V AoS) and dJ/du0 on return.
+void ssprk33_adjoint_sweep(mft_ctx* c, double* L) {
+  const size_t nv = (size_t)c->n * c->nvars;
+  const int N = c->adj_nsteps, E = c->adj_every;
+  const double dt = c->adj_dt;
+  double* A = c->adj_lam[1].p;
+  double* B = c->adj_lam[2].p;
+  double* acc = c->adj_acc.p;
+  auto back = [&](const double* x, const double* s1, const double* s2) {
+    eval_rhs_adjoint(c, s2, L, kAdjStage3, dt, acc, A);
+    eval_rhs_adjoint(c, s1, A, kAdjStage2, dt, acc, B);
+    eval_rhs_adjoint(c, x, B, kAdjStage1, dt, acc, L);
+  };
+  double* st = c->adj_store.p;
+  if (E == 0) {
+    for (int k = N - 1; k >= 0; --k) {
+      const double* x = st + (size_t)3 * k * nv;
+      back(x, x + nv, x + 2 * nv);
+    }
+    return;
+  }
+  const int nck = (N + E - 1) / E;
+  for (int seg = nck - 1; seg >= 0; --seg) {
+    const int a = seg * E, b = std::min(N, a + E);
+    d2d(c, st, c->adj_ckpt.p + (size_t)seg * nv, nv);
+    for (int k = a; k < b; ++k) {
+      double* x = st + (size_t)3 * (k - a) * nv;
+      double* y = k + 1 < b ? x + 3 * nv : c->U[3].p;
+      record_step(c, dt, k, x, x + nv, x + 2 * nv, y);
+    }
+    for (int k = b - 1; k >= a; --k) {
+      const double* x = st + (size_t)3 * (k - a) * nv;
+      back(x, x + nv, x + 2 * nv);
+    }
+  }
+}
+
+void ssprk33_adjoint_soa(mft_ctx* c, double* lam_soa) {
+  MFT_REQUIRE(c->adj_valid, MFT_ERR_STATE, "call mft_ssprk33_record first");
+  check_adjoint_ready(c);
+  ensure_work(c);
+  ensure_adj_work(c);
+  ensure_bcs(c);
+  cudaStream_t s = c->stream;
+  const int64_t n = c->n;
+  const int V = c->nvars;
+  double* L = c->adj_lam[0].p;
+  launch_aos_from_soa(lam_soa, L, n, V, s);
+  BcDev bc{c->d_tag.p, c->d_slot.p, c->d_normal.p, c->d_dvals.p};
+  if (c->nb > 0) launch_bc_project(c->nb, c->d_bnode.p, V, bc, L, s);
+  ssprk33_adjoint_sweep(c, L);
+  launch_soa_from_aos(L, lam_soa, n, V, s);
+}
+
+}  // namespace
+
+mft_status mft_rhs_adjoint(mft_ctx* c, double* const* out, const double* const* lam,
+                           const double* const* u, int nvars, double t) {
+  (void)t;
+  return guarded(c, [&] {
+    check_adjoint_ready(c);
+    MFT_REQUIRE(out && lam && u && nvars == c->nvars, MFT_ERR_ARG, "bad arrays or nvars");
+    set_device(c);
+    ensure_work(c);
+    ensure_adj_work(c);
+    const int64_t n = c->n;
+    const int V = c->nvars;
+    cudaStream_t s = c->stream;
+    for (int v = 0; v < V; ++v) {
+      MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+      MFT_CUDA(cudaMemcpyAsync(c->soa2.p + (size_t)v * n, lam[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    }
+    launch_aos_from_soa(c->soa.p, c->work_u.p, n, V, s);
+    launch_aos_from_soa(c->soa2.p, c->adj_lam[0].p, n, V, s);
+    eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p);
+    launch_soa_from_aos(c->adj_lam[1].p, c->soa.p, n, V, s);
+    for (int v = 0; v < V; ++v)
+      MFT_CUDA(cudaMemcpyAsync(out[v], c->soa.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
+  });
+}
+
+mft_status mft_rhs_adjoint_device(mft_ctx* c, double* out, const double* lam, const double* u,
+                                  double t) {
+  (void)t;
+  return guarded(c, [&] {
+    check_adjoint_ready(c);
+    MFT_REQUIRE(out && lam && u, MFT_ERR_ARG, "NULL device array");
+    set_device(c);
+    ensure_work(c);
+    ensure_adj_work(c);
+    const int64_t n = c->n;
+    const int V = c->nvars;
+    cudaStream_t s = c->stream;
+    launch_aos_from_soa(u, c->work_u.p, n, V, s);
+    launch_aos_from_soa(lam, c->adj_lam[0].p, n, V, s);
+    eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p);
+    launch_soa_from_aos(c->adj_lam[1].p, out, n, V, s);
+    MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
+  });
+}
+
+mft_status mft_ssprk33_record(mft_ctx* c, double dt, int nsteps, int every) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "call mft_set_state first");
+    MFT_REQUIRE(nsteps >= 1, MFT_ERR_ARG, "nsteps < 1");
+    MFT_REQUIRE(every >= 0, MFT_ERR_ARG, "every < 0");
+    MFT_REQUIRE(dt > 0 && isfinite(dt), MFT_ERR_ARG, "dt must be positive and finite");
+    check_adjoint_ready(c);
+    set_device(c);
+    ssprk33_record(c, dt, nsteps, every);
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+    check_kernel_errors(c);
+  });
+}
+
+mft_status mft_ssprk33_adjoint(mft_ctx* c, double* const* lam, int nvars) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(lam && nvars == c->nvars, MFT_ERR_ARG, "bad arrays or nvars");
+    set_device(c);
+    ensure_work(c);
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(c->soa2.p + (size_t)v * n, lam[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    ssprk33_adjoint_soa(c, c->soa2.p);
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(lam[v], c->soa2.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
+  });
+}
+
+mft_status mft_ssprk33_adjoint_device(mft_ctx* c, double* lam) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(lam, MFT_ERR_ARG, "NULL device array");
+    set_device(c);
+    ssprk33_adjoint_soa(c, lam);
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+    check_kernel_errors(c);
   });
 }
 

@@ -116,6 +116,12 @@ struct mft_ctx {
   mft::DBuf<double> d_seg_h, seg_partial, seg_mean, seg_norms;
   mft::DBuf<unsigned> seg_counter;
 
+  // adjoint: recorded trajectory (checkpoints, or every stage state) and cotangents
+  mft::DBuf<double> adj_lam[3], adj_acc, adj_q, adj_store, adj_ckpt;
+  bool adj_valid = false;
+  double adj_t0 = 0.0, adj_dt = 0.0;
+  int adj_nsteps = 0, adj_every = 0;
+
   // one SSP-RK3 step as a CUDA graph (u_n in U0 / in U3) and its step table
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   const double* graph_un[2] = {nullptr, nullptr};

@@ -32,6 +32,28 @@ static __device__ __forceinline__ void euler_flux(double g, const double* uu, do
   fy[3] = dmul(dadd(en, p), v2);
 }
 
+// Reverse-mode product of the Euler flux pair at state uu:
+// ub = (dF/du)^T gx + (dG/du)^T gy for F = (m1, m1 v1 + p, m1 v2, (E + p) v1),
+// G = (m2, m2 v1, m2 v2 + p, (E + p) v2), v = m / rho,
+// p = (gamma - 1)(E - (m1 v1 + m2 v2) / 2).
+static __device__ __forceinline__ void euler_flux_vjp(double g, const double* uu, const double* gx,
+                                                      const double* gy, double* ub) {
+  const double rho = uu[0], m1 = uu[1], m2 = uu[2], en = uu[3];
+  const double ri = 1.0 / rho;
+  const double v1 = m1 * ri, v2 = m2 * ri;
+  const double gm1 = g - 1.0;
+  const double p = gm1 * (en - 0.5 * (m1 * v1 + m2 * v2));
+  const double ep = en + p;
+  const double pb = gx[1] + gx[3] * v1 + gy[2] + gy[3] * v2;
+  const double hp = 0.5 * gm1 * pb;
+  const double v1b = gx[1] * m1 + gx[3] * ep + gy[1] * m2 - hp * m1;
+  const double v2b = gx[2] * m1 + gy[2] * m2 + gy[3] * ep - hp * m2;
+  ub[0] = -(v1b * v1 + v2b * v2) * ri;
+  ub[1] = gx[0] + gx[1] * v1 + gx[2] * v2 - hp * v1 + v1b * ri;
+  ub[2] = gy[0] + gy[1] * v1 + gy[2] * v2 - hp * v2 + v2b * ri;
+  ub[3] = gx[3] * v1 + gy[3] * v2 + gm1 * pb;
+}
+
 // apply_slip_velocity (src/equations/PointCloudBCs.jl:15-21) with the normal
 // normalised as boundary_condition_slip_wall does (:87-106).
 static __device__ __forceinline__ void slip(const double* nrm, double* uu) {

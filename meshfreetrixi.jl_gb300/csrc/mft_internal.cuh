@@ -223,6 +223,40 @@ void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 bool launch_fwd_f32_tma(const FwdArgs& a, int chunk, int* err, cudaStream_t s);
 bool launch_rev_f32_tma(const RevArgs& a, int chunk, int* err, cudaStream_t s);
 
+// Adjoint of rhs! (reverse mode) and the SSP-RK3 adjoint stage combinations.
+// With r = (d rhs!/du)^T lam at state u and Pi the strong-BC projection:
+//   kAdjPlain:  out = r
+//   kAdjStage3: out = Pi(2/3 lam) + 2dt/3 r,  acc = lam / 3
+//   kAdjStage2: out = Pi(lam / 4) + dt/4 r,   acc += 3/4 lam
+//   kAdjStage1: out = Pi(acc + lam) + dt r
+enum AdjKind : int { kAdjPlain = 0, kAdjStage1 = 1, kAdjStage2 = 2, kAdjStage3 = 3 };
+struct AdjArgs {
+  int64_t n;
+  EllView ell;         // reverse adjacency (column j of D as row j)
+  const double* w[2];  // D_x, D_y on the reverse layout
+  const double* wh;    // lap (Tominec) or H (Flyer) on the reverse layout, or null
+  int hv;              // 0 none, 1 Tominec (gathers q = lap M2 lam), 2 Flyer (gathers M2 lam)
+  double hv_gamma;
+  const double* lam;   // n x V cotangent
+  const double* q;     // n x V lap M2 lam (Tominec)
+  const double* u;     // n x V state the product linearises about
+  int eq, V;
+  double gamma, ax, ay;
+  BcDev bc;
+  int has_bc;
+  int kind;
+  double dt;
+  double* acc;         // n x V stage accumulator (stage kinds)
+  double* out;         // n x V
+};
+void launch_adj_f64(const AdjArgs& a, cudaStream_t s);
+// q_i = sum_j lap[i,j] (M2 lam)_j over the forward layout (Tominec adjoint).
+void launch_lap_masked(int64_t n, EllView fwd, const double* wl, const double* lam, int V,
+                       BcDev bc, int has_bc, double* q, cudaStream_t s);
+// lam = Pi lam at the listed boundary nodes (Dirichlet zero, slip-wall projection).
+void launch_bc_project(int64_t nb, const int32_t* bnode, int V, BcDev bc, double* lam,
+                       cudaStream_t s);
+
 // Sets *flag to 1 when a and b differ in any of `count` doubles (bitwise).
 void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s);
 

@@ -8,5 +8,5 @@ from .api import (  # noqa: F401
     PointCloudEnsemble, PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
     SemidiscretizationHyperbolic, SourceHyperviscosityFlyer, SourceHyperviscosityTominec,
     SourceResidualViscosityTominec, SourceTerms, SourceUpwindViscosityTominec, SSPRK33,
-    boundary_condition_slip_wall, rhs_, semidiscretize, solve)
+    boundary_condition_slip_wall, rhs_, rhs_adjoint_, semidiscretize, solve, solve_adjoint)
 from .medusa import read_medusa_file  # noqa: F401

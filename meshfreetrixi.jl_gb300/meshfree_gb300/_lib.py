@@ -58,13 +58,18 @@ SIGNATURES = {
     "mft_ssprk33": (I32, [VP, DBL, I32, I32]),
     "mft_ssprk33_host": (I32, [VP, VP, I32, C.POINTER(DBL), DBL, I32]),
     "mft_set_rv_state": (I32, [VP, VP, I32, I32]),
+    "mft_rhs_adjoint": (I32, [VP, VP, VP, VP, I32, DBL]),
+    "mft_rhs_adjoint_device": (I32, [VP, VP, VP, VP, DBL]),
+    "mft_ssprk33_record": (I32, [VP, DBL, I32, I32]),
+    "mft_ssprk33_adjoint": (I32, [VP, VP, I32]),
+    "mft_ssprk33_adjoint_device": (I32, [VP, VP]),
     "mft_get_viscosity": (I32, [VP, VP]),
     "mft_profile": (I32, [VP, I32]),
     "mft_profile_get": (I32, [VP, I32, C.POINTER(DBL), C.POINTER(I64), C.POINTER(C.c_char_p)]),
     "mft_region": (I32, [VP, I32, C.POINTER(DBL)]),
 }
 K_NAMES = ["bc_pass1", "flux", "fwd_gather", "mean", "lexmax", "eps", "rev_gather", "rev_lap",
-           "history", "layout"]
+           "history", "layout", "adjoint"]
 
 _lib = None
 
@@ -243,6 +248,32 @@ class Context:
         self.check(self.lib.mft_ssprk33_host(self.h, _ptrs(list(u)), u.shape[0], C.byref(tt),
                                              dt, nsteps))
         return tt.value
+
+    # adjoint --------------------------------------------------------------
+    def rhs_adjoint(self, lam, u, t=0.0):
+        """(d rhs!(u)/du)^T lam for (nvars, n) host arrays; u is not mutated."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        out = np.empty_like(u)
+        self.check(self.lib.mft_rhs_adjoint(self.h, _ptrs(list(out)), _ptrs(list(lam)),
+                                            _ptrs(list(u)), u.shape[0], t))
+        return out
+
+    def rhs_adjoint_device(self, out_ptr, lam_ptr, u_ptr, t=0.0):
+        self.check(self.lib.mft_rhs_adjoint_device(self.h, C.c_void_p(out_ptr), C.c_void_p(lam_ptr),
+                                                   C.c_void_p(u_ptr), t))
+
+    def ssprk33_record(self, dt, nsteps, every=0):
+        self.check(self.lib.mft_ssprk33_record(self.h, dt, nsteps, every))
+
+    def ssprk33_adjoint(self, lam_T):
+        """dJ/du(t0) from dJ/du(T) over the recorded trajectory (host arrays)."""
+        lam = np.array(lam_T, dtype=np.float64, order="C", copy=True)
+        self.check(self.lib.mft_ssprk33_adjoint(self.h, _ptrs(list(lam)), lam.shape[0]))
+        return lam
+
+    def ssprk33_adjoint_device(self, lam_ptr):
+        self.check(self.lib.mft_ssprk33_adjoint_device(self.h, C.c_void_p(lam_ptr)))
 
     def set_rv_state(self, approx_du, success_iter):
         ptrs = None

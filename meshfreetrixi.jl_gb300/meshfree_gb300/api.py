@@ -157,7 +157,7 @@ class PointCloudEnsemble(PointCloudDomain):
         self.solver = solver
         self.period = None if period is None else tuple(float(p) for p in period)
         k = basis.nv
-        idx_all, pts_all, dmins, davgs, offs = [], [], [], [0], []
+        idx_all, pts_all, dmins, davgs, offs = [], [], [], [], [0]
         tmp = L.Context(solver.engine.device)
         for pts in member_points:
             pts = np.ascontiguousarray(pts, dtype=np.float64)
@@ -414,6 +414,14 @@ def rhs_(du, u, semi, t):
     return None
 
 
+def rhs_adjoint_(out, lam, u, semi, t):
+    """Pullback of rhs!: out = (d rhs!(u, t)/du)^T lam on the GPU (mft_rhs_adjoint);
+    the reference has no counterpart (it differentiates rhs! with ForwardDiff duals).
+    u is not mutated."""
+    out[...] = semi.domain.ctx.rhs_adjoint(lam, u, t)
+    return None
+
+
 # ------------------------------------------------------------------ time integration
 
 
@@ -454,3 +462,21 @@ def solve(ode, alg=None, dt=None, callback=None, save_everystep=False):
         steps += 1
     u, t = ctx.get_state()
     return ODESolution(u, t, steps)
+
+
+def solve_adjoint(ode, dt, dJdu, checkpoint_every=0):
+    """Gradient of an objective of the final state w.r.t. the initial state: SSP-RK3
+    from tspan[0] to tspan[1] in steps of dt (which must divide the span), recorded
+    with a checkpoint every `checkpoint_every` steps (0 keeps every stage state), then
+    the reverse sweep from dJdu(u(T)).  Returns (ODESolution, dJ/du0)."""
+    semi = ode.p
+    ctx = semi.domain.ctx
+    t0, t1 = ode.tspan
+    nsteps = int(round((t1 - t0) / dt))
+    if nsteps < 1 or abs(nsteps * dt - (t1 - t0)) > 1e-9 * max(abs(t1 - t0), dt):
+        raise ValueError("dt must divide tspan into a whole number of steps")
+    ctx.set_state(ode.u0, t0)
+    ctx.ssprk33_record(dt, nsteps, checkpoint_every)
+    u, t = ctx.get_state()
+    lam = np.ascontiguousarray(dJdu(u), dtype=np.float64)
+    return ODESolution(u, t, nsteps), ctx.ssprk33_adjoint(lam)

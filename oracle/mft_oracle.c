@@ -995,6 +995,127 @@ int mfto_rhs(const mfto_semi* s, double t, const double* dirichlet, double* cons
 }
 
 /* ------------------------------------------------------------------------ */
+/* Adjoint of rhs! (extension)                                               */
+/* ------------------------------------------------------------------------ */
+
+/* Reverse-mode product of the Euler flux pair (flux_point d = 0, 1) at state uu:
+ * ub = (dF/du)^T gx + (dG/du)^T gy, derived from the flux definition
+ * F = (m1, m1 v1 + p, m1 v2, (E + p) v1), G = (m2, m2 v1, m2 v2 + p, (E + p) v2),
+ * v = m / rho, p = (gamma - 1)(E - (m1 v1 + m2 v2) / 2). */
+static void euler_flux_vjp(double gamma, const double* uu, const double* gx, const double* gy,
+                           double* ub) {
+  double rho = uu[0], m1 = uu[1], m2 = uu[2], en = uu[3];
+  double v1 = m1 / rho, v2 = m2 / rho;
+  double gm1 = gamma - 1.0;
+  double p = gm1 * (en - 0.5 * (m1 * v1 + m2 * v2));
+  double ep = en + p;
+  double pb = gx[1] + gx[3] * v1 + gy[2] + gy[3] * v2;
+  double eb = gx[3] * v1 + gy[3] * v2 + gm1 * pb;
+  double v1b = gx[1] * m1 + gx[3] * ep + gy[1] * m2 - 0.5 * gm1 * m1 * pb;
+  double v2b = gx[2] * m1 + gy[2] * m2 + gy[3] * ep - 0.5 * gm1 * m2 * pb;
+  double m1b = gx[0] + gx[1] * v1 + gx[2] * v2 - 0.5 * gm1 * v1 * pb + v1b / rho;
+  double m2b = gy[0] + gy[1] * v1 + gy[2] * v2 - 0.5 * gm1 * v2 * pb + v2b / rho;
+  double rhob = -(v1b * v1 + v2b * v2) / rho;
+  ub[0] = rhob;
+  ub[1] = m1b;
+  ub[2] = m2b;
+  ub[3] = eb;
+}
+
+/* Unit normal of boundary-list entry p. */
+static void unit_normal(const mfto_semi* s, int64_t p, double* n1, double* n2) {
+  double a = s->bc_normal[p * s->dim + 0], b = s->bc_normal[p * s->dim + 1];
+  double nrm = sqrt(a * a + b * b);
+  *n1 = a / nrm;
+  *n2 = b / nrm;
+}
+
+int mfto_rhs_adjoint(const mfto_semi* s, const double* const* u, const double* const* lam,
+                     double* const* out, int nthreads) {
+  int64_t n = s->n;
+  int V = s->nvars, D = s->dim;
+  for (int q = 0; q < s->n_src; ++q)
+    if (s->src_kind[q] == MFTO_SRC_RV || s->src_kind[q] == MFTO_SRC_UPWIND) return -1;
+  /* per-node BC tag (last listing wins, as bc_pass applies them in order) */
+  signed char* tag = (signed char*)calloc((size_t)n, 1);
+  int64_t* slot = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+  double* lt = (double*)malloc((size_t)n * V * sizeof(double));
+  double* g = (double*)calloc((size_t)n * V * D, sizeof(double));
+  if (!tag || !slot || !lt || !g) { free(tag); free(slot); free(lt); free(g); return -2; }
+  for (int b = 0; b < s->n_bc; ++b) {
+    for (int64_t p = s->bc_ptr[b]; p < s->bc_ptr[b + 1]; ++p) {
+      int32_t i = s->bc_idx[p];
+      if (s->bc_kind[b] == MFTO_BC_DIRICHLET) { tag[i] = 1; slot[i] = p; }
+      else if (s->bc_kind[b] == MFTO_BC_SLIP_WALL && s->eq == MFTO_EQ_EULER2D) { tag[i] = 2; slot[i] = p; }
+    }
+  }
+  /* lam~ = M2 lam: the rows that bc_pass zeroes in du carry no cotangent */
+  for (int v = 0; v < V; ++v)
+    for (int64_t i = 0; i < n; ++i) {
+      double x = lam[v][i];
+      if (tag[i] == 1 || (tag[i] == 2 && (v == 1 || v == 2))) x = 0.0;
+      lt[(size_t)v * n + i] = x;
+    }
+  /* g_d = D_d^T lam~ */
+  for (int d = 0; d < D; ++d)
+    for (int v = 0; v < V; ++v)
+      mfto_spmv_t_accum(&s->dop[d], 1.0, lt + (size_t)v * n, g + ((size_t)d * V + v) * n, nthreads);
+  /* flux-Jacobian-transpose products at each node, on the state bc_pass leaves */
+#pragma omp parallel for num_threads(nthreads_or_default(nthreads)) schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    double uu[8], gx[8], gy[8], ub[8];
+    for (int v = 0; v < V; ++v) {
+      uu[v] = u[v][i];
+      gx[v] = g[(size_t)v * n + i];
+      gy[v] = g[((size_t)V + v) * n + i];
+    }
+    if (s->eq == MFTO_EQ_EULER2D) {
+      if (tag[i] == 2) {
+        double n1, n2;
+        unit_normal(s, slot[i], &n1, &n2);
+        double vn = uu[1] * n1 + uu[2] * n2;
+        double s1 = uu[1] - vn * n1, s2 = uu[2] - vn * n2;
+        uu[1] = s1;
+        uu[2] = s2;
+      }
+      euler_flux_vjp(s->gamma, uu, gx, gy, ub);
+    } else {
+      for (int v = 0; v < V; ++v) {
+        double acc = 0.0;
+        for (int d = 0; d < D; ++d) acc = acc + s->adv[d] * g[((size_t)d * V + v) * n + i];
+        ub[v] = acc;
+      }
+    }
+    for (int v = 0; v < V; ++v) out[v][i] = -ub[v];
+  }
+  /* hyperviscosity du -= gamma H u  ->  out -= gamma H^T lam~ */
+  for (int q = 0; q < s->n_src; ++q) {
+    if (s->src_kind[q] != MFTO_SRC_HV_TOMINEC && s->src_kind[q] != MFTO_SRC_HV_FLYER) continue;
+    for (int v = 0; v < V; ++v)
+      for (int64_t r = 0; r < n; ++r) {
+        double x = lt[(size_t)v * n + r];
+        for (int64_t p = s->hv.rp[r]; p < s->hv.rp[r + 1]; ++p)
+          out[v][s->hv.ci[p]] -= s->hv_gamma * s->hv.val[p] * x;
+      }
+  }
+  /* Pi: Dirichlet values do not depend on u; slip walls project the momentum */
+  for (int64_t i = 0; i < n; ++i) {
+    if (tag[i] == 1) {
+      for (int v = 0; v < V; ++v) out[v][i] = 0.0;
+    } else if (tag[i] == 2) {
+      double n1, n2;
+      unit_normal(s, slot[i], &n1, &n2);
+      double vn = out[1][i] * n1 + out[2][i] * n2;
+      double s1 = out[1][i] - vn * n1, s2 = out[2][i] - vn * n2;
+      out[1][i] = s1;
+      out[2][i] = s2;
+    }
+  }
+  free(tag); free(slot); free(lt); free(g);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* A16  time_deriv_weights!  history.jl:131-152                              */
 /* ------------------------------------------------------------------------ */
 

@@ -121,6 +121,15 @@ typedef struct {
 int mfto_rhs(const mfto_semi* s, double t, const double* dirichlet, double* const* du,
              double* const* u, double* eps_out, mfto_rv_diag* diag, int nthreads);
 
+/* Adjoint of rhs! at state u (extension: the reference differentiates rhs! with
+ * ForwardDiff duals).  out = (d rhs!(u)/du)^T lam for the flux divergence
+ * (calc_fluxes!, rbfsolver.jl:247-265), the strong BCs (bc_pass above: Dirichlet
+ * rows/values constant, slip-wall momentum projection) and the hyperviscosity
+ * sources (du -= gamma*H*u).  u and lam are nvars pointers of length n; u is not
+ * mutated.  Returns -1 when a residual/upwind viscosity source is present (its
+ * viscosity is a maximum over the field and has no adjoint here). */
+int mfto_rhs_adjoint(const mfto_semi* s, const double* const* u, const double* const* lam,
+                     double* const* out, int nthreads);
 /* Pieces of rhs! exposed for the reference's own identity tests. */
 int mfto_calc_fluxes(const mfto_semi* s, double* const* du, double* const* u, int nthreads);
 /* y += alpha * A x (SparseArrays 5-arg mul!, CSC column scatter == ascending CSR rows) */

@@ -69,6 +69,8 @@ def lib():
         L.mfto_rhs.restype = C.c_int
         L.mfto_rhs.argtypes = [C.POINTER(_Semi), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.POINTER(_Diag), C.c_int]
+        L.mfto_rhs_adjoint.restype = C.c_int
+        L.mfto_rhs_adjoint.argtypes = [C.POINTER(_Semi), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.mfto_calc_fluxes.restype = C.c_int
         L.mfto_calc_fluxes.argtypes = [C.POINTER(_Semi), C.c_void_p, C.c_void_p, C.c_int]
         for name in ("mfto_spmv_accum", "mfto_spmv_t_accum"):
@@ -359,6 +361,39 @@ class Semi:
             out.append((np.array(dg.mean[:self.nvars]), np.array(dg.norms[:self.nvars])))
         return out[0] if len(out) == 1 else tuple(out)
 
+    def rhs_adjoint(self, u, lam, nthreads=8):
+        """(d rhs!(u)/du)^T lam (flux divergence, strong BCs, hyperviscosity); u is
+        not mutated."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        assert u.shape == (self.nvars, self.n) and lam.shape == u.shape
+        out = np.empty_like(u)
+        ptrs = [(C.c_void_p * self.nvars)(*[a[v].ctypes.data for v in range(self.nvars)])
+                for a in (u, lam, out)]
+        rc = lib().mfto_rhs_adjoint(C.byref(self.s), C.cast(ptrs[0], C.c_void_p),
+                                    C.cast(ptrs[1], C.c_void_p), C.cast(ptrs[2], C.c_void_p),
+                                    nthreads)
+        if rc:
+            raise RuntimeError("mfto_rhs_adjoint failed: %d" % rc)
+        return out
+
+    def bc_project(self, lam):
+        """Pi lam: the derivative of the strong-BC pass (Dirichlet entries zero,
+        slip-wall momentum projected on the wall)."""
+        out = np.array(lam, dtype=np.float64, copy=True)
+        for kind, ii, normals, _fn in self.bcs:
+            ii = np.asarray(ii, dtype=np.int64)
+            if kind == BC_DIRICHLET:
+                out[:, ii] = 0.0
+            elif kind == BC_SLIP_WALL and self.nvars == 4:
+                nr = np.asarray(normals, dtype=np.float64).reshape(ii.size, self.dim)
+                nn = np.sqrt(nr[:, 0] * nr[:, 0] + nr[:, 1] * nr[:, 1])
+                n1, n2 = nr[:, 0] / nn, nr[:, 1] / nn
+                vn = out[1, ii] * n1 + out[2, ii] * n2
+                out[1, ii] = out[1, ii] - vn * n1
+                out[2, ii] = out[2, ii] - vn * n2
+        return out
+
 
 class History:
     """HistoryCallback (history.jl:15-152): ring of (t, u), newest first."""
@@ -412,3 +447,42 @@ def ssprk33(semi: Semi, u0, t0, dt, nsteps, history: History | None = None, nthr
         if callback is not None:
             callback(step + 1, t, u)
     return u, t
+
+
+def ssprk33_record(semi: Semi, u0, t0, dt, nsteps, nthreads=8):
+    """ssprk33 without callbacks, keeping per step the stage states the adjoint
+    sweep linearises about: (u_n, u_1, u_2), each as rhs! left it (strong BCs
+    applied).  Returns (u_T, t_T, record); u_T is projected by the BC pass like the
+    FSAL evaluation at the end of ssprk33 leaves it."""
+    u = np.array(u0, dtype=np.float64, copy=True)
+    t = t0
+    rec = []
+    for step in range(nsteps):
+        k = semi.rhs(u, t, nthreads)
+        un = u.copy()
+        u1 = un + dt * k
+        k1 = semi.rhs(u1, t + dt, nthreads)
+        u2 = (3.0 * un + u1 + dt * k1) / 4.0
+        k2 = semi.rhs(u2, t + 0.5 * dt, nthreads)
+        u3 = (un + 2.0 * u2 + 2.0 * dt * k2) / 3.0
+        rec.append((un, u1, u2))
+        t = t0 + (step + 1) * dt
+        u = u3
+    semi.rhs(u, t, nthreads)
+    return u, t, rec
+
+
+def ssprk33_adjoint(semi: Semi, rec, dt, lam_T, nthreads=8):
+    """Reverse sweep of ssprk33: given lam_T = dJ/du(T), returns dJ/du(t0).
+    Per step (Shu-Osher stages with the BC projection Pi):
+      a   = Pi(2/3 lam) + 2dt/3 J(u_2)^T lam
+      b   = Pi(a/4)     + dt/4  J(u_1)^T a
+      lam = Pi(lam/3 + 3a/4 + b) + dt J(u_n)^T b."""
+    lam = semi.bc_project(lam_T)
+    for un, u1, u2 in reversed(rec):
+        a = semi.bc_project((2.0 / 3.0) * lam) + (2.0 * dt / 3.0) * semi.rhs_adjoint(u2, lam, nthreads)
+        acc = lam / 3.0
+        b = semi.bc_project(0.25 * a) + (0.25 * dt) * semi.rhs_adjoint(u1, a, nthreads)
+        acc = acc + 0.75 * a
+        lam = semi.bc_project(acc + b) + dt * semi.rhs_adjoint(un, b, nthreads)
+    return lam
