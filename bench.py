@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
+    ap.add_argument("--only", default="all", choices=["all", "adjoint"],
+                    help="'adjoint' runs the adjoint measurement alone")
+    ap.add_argument("--adj-side", type=int, default=256,
+                    help="nodes per side of the adjoint measurement (0 skips it)")
     return ap.parse_args()
 
 
@@ -235,6 +239,91 @@ def run_ensemble(args, local, pg):
                         "FP64, dt=0.2 min(h), one CUDA graph per SSP-RK3 step" % K_STENCIL}
 
 
+def run_adjoint(args, local, peaks):
+    """Gradient of J = 0.5 |rho(T) - rho*|^2 w.r.t. u0 for the isentropic vortex at
+    N = 65,536 (T = 0.5, 500 SSP-RK3 steps, checkpoint every 20 steps; rho* the exact
+    density at T with seeded 1% noise), against the forward solve's cost."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    side, T, nsteps, every = args.adj_side, 0.5, 500, 20
+    dt = T / nsteps
+    pts, per, _h = W.vortex_cloud(side)
+    n = pts.shape[0]
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    semi = M.SemidiscretizationHyperbolic(dom, M.CompressibleEulerEquations2D(1.4),
+                                          lambda x, t, e: W.isentropic_vortex(x, t), solver)
+    ctx = dom.ctx
+    u0 = semi.compute_coefficients(0.0)
+    rng = np.random.default_rng(20)
+    target = W.isentropic_vortex(pts, T)[0] * (1.0 + 0.01 * rng.standard_normal(n))
+
+    def J(u):
+        d = u[0] - target
+        return 0.5 * float(d @ d)
+
+    def forward(u):
+        ctx.set_state(u, 0.0)
+        ctx.region_begin()
+        ctx.ssprk33(dt, nsteps, use_graph=True)
+        ms = ctx.region_end()
+        return ctx.get_state()[0], ms
+
+    def gradient(k):
+        ctx.set_state(u0, 0.0)
+        ctx.region_begin()
+        ctx.ssprk33_record(dt, nsteps, k)
+        ms_rec = ctx.region_end()
+        uT = ctx.get_state()[0]
+        lam = np.zeros_like(uT)
+        lam[0] = uT[0] - target
+        ctx.region_begin()
+        g = ctx.ssprk33_adjoint(lam)
+        return g, ms_rec, ctx.region_end()
+
+    forward(u0)                     # warm-up (graph capture)
+    uT, ms_fwd = forward(u0)
+    gradient(every)                 # warm-up
+    grad, ms_rec, ms_adj = gradient(every)
+    grad0, ms_rec0, ms_adj0 = gradient(0)
+    ctx.profile(True)
+    gradient(every)
+    prof = ctx.profile_report()
+    ctx.profile(False)
+    # centred difference of J along a seeded direction, through two forward solves
+    v = rng.standard_normal(u0.shape) * np.abs(u0).max(axis=1, keepdims=True)
+    e = 1e-6
+    fd = (J(forward(np.ascontiguousarray(u0 + e * v))[0])
+          - J(forward(np.ascontiguousarray(u0 - e * v))[0])) / (2 * e)
+    ad = float(np.sum(grad * v))
+    ms_k, launches = prof.get("adjoint", (0.0, 0))
+    per_launch = ms_k / max(launches, 1)
+    # adjoint kernel, per node: idx 4k + D_x, D_y 16k + lam row 32 + u 32 + lam_i 32
+    # + acc read/write 64 + out 32 (cached neighbour rows); FP64 FMAs 8 per entry
+    bytes_node = 4 * K_STENCIL + 16 * K_STENCIL + 32 * 6
+    ctx.close()
+    return {"workload": "isentropic vortex N=%d, T=%.1f, %d SSP-RK3 steps, k=%d, no viscosity "
+                        "source; J = 0.5|rho(T) - rho*|^2, rho* exact density with 1%% seeded "
+                        "noise" % (n, T, nsteps, K_STENCIL),
+            "nodes": n, "steps": nsteps, "checkpoint_every": every,
+            "forward_ms": ms_fwd, "record_ms": ms_rec, "adjoint_sweep_ms": ms_adj,
+            "gradient_over_forward": (ms_rec + ms_adj) / ms_fwd,
+            "adjoint_sweep_over_forward": ms_adj / ms_fwd,
+            "store_all_stages": {"record_ms": ms_rec0, "adjoint_sweep_ms": ms_adj0,
+                                 "adjoint_sweep_over_forward": ms_adj0 / ms_fwd,
+                                 "stored_bytes": 3 * nsteps * 4 * n * 8,
+                                 "max_abs_diff_vs_checkpointed": float(np.abs(grad0 - grad).max())},
+            "fd_check": {"directional_fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(ad),
+                         "fd_step": e},
+            "kernel": {"name": "adjoint", "avg_launch_ms": per_launch, "launches": launches,
+                       "algorithmic_bytes_per_node": bytes_node,
+                       "achieved_gbs": bytes_node * n / (per_launch * 1e-3) / 1e9 if launches else None,
+                       "hbm_frac": (bytes_node * n / (per_launch * 1e-3) / 1e9) / peaks["hbm_gbs"]
+                       if launches else None,
+                       "fp64_gfma_s": 8 * K_STENCIL * n / (per_launch * 1e-3) / 1e9 if launches else None}}
+
+
 def roofline(prof, n, prec, peaks):
     name = max(prof, key=lambda k: prof[k][0])
     ms, launches = prof[name]
@@ -348,6 +437,10 @@ def config_dict(n, prec):
 def run_ours(args):
     ws, rank, local, pg = dist_setup()
     peaks = load_peaks()
+    if args.only == "adjoint":       # the adjoint measurement alone (profiling runs)
+        if rank == 0:
+            print(json.dumps({"adjoint": run_adjoint(args, local, peaks)}), flush=True)
+        return
     n = args.n_side ** 2
     semi, domain, u0, dt = build_problem(args.n_side, "fp64", local)
     ctx = domain.ctx
@@ -389,6 +482,7 @@ def run_ours(args):
     ctx.close()
 
     ens = run_ensemble(args, local, pg) if args.ens_members > 0 else None
+    adj = run_adjoint(args, local, peaks) if args.adj_side > 0 and rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -419,6 +513,7 @@ def run_ours(args):
                        "autotuned_mapping": mapping,
                        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
         "ensemble": ens,
+        "adjoint": adj,
     }
     print(json.dumps(line), flush=True)
 
