@@ -63,6 +63,8 @@ def parse():
                     help="members of the ensemble measurement (0 skips it)")
     ap.add_argument("--only", default="all", choices=["all", "adjoint"],
                     help="'adjoint' runs the adjoint measurement alone")
+    ap.add_argument("--adj-steps", type=int, default=500,
+                    help="SSP-RK3 steps of the adjoint measurement (to t = 0.5)")
     ap.add_argument("--adj-side", type=int, default=256,
                     help="nodes per side of the adjoint measurement (0 skips it)")
     return ap.parse_args()
@@ -245,7 +247,7 @@ def run_adjoint(args, local, peaks):
     density at T with seeded 1% noise), against the forward solve's cost."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
-    side, T, nsteps, every = args.adj_side, 0.5, 500, 20
+    side, T, nsteps, every = args.adj_side, 0.5, args.adj_steps, 20
     dt = T / nsteps
     pts, per, _h = W.vortex_cloud(side)
     n = pts.shape[0]
