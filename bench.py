@@ -61,10 +61,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
-    ap.add_argument("--only", default="all", choices=["all", "adjoint"],
-                    help="'adjoint' runs the adjoint measurement alone")
+    ap.add_argument("--only", default="all", choices=["all", "adjoint", "riemann"],
+                    help="run one auxiliary measurement alone")
+    ap.add_argument("--riemann-side", type=int, default=1024,
+                    help="nodes per side of the Riemann FP32/FP64 measurement (0 skips it)")
     ap.add_argument("--adj-steps", type=int, default=500,
-                    help="SSP-RK3 steps of the adjoint measurement (to t = 0.5)")
+                    help="SSP-RK3 steps of the adjoint measurement")
+    ap.add_argument("--adj-tend", type=float, default=0.5,
+                    help="end time of the adjoint measurement")
     ap.add_argument("--adj-side", type=int, default=256,
                     help="nodes per side of the adjoint measurement (0 skips it)")
     return ap.parse_args()
@@ -241,13 +245,67 @@ def run_ensemble(args, local, pg):
                         "FP64, dt=0.2 min(h), one CUDA graph per SSP-RK3 step" % K_STENCIL}
 
 
+def run_riemann(args, local):
+    """Four-quadrant Riemann problem on the unit square (N = side^2 jittered nodes, no
+    boundary condition: one-sided stencils at the edges), residual viscosity + Tominec
+    hyperviscosity (c = 1), SSP-RK3 with dt = 0.1 h to t = 0.2, in the FP64 form and the
+    FP32-apply form: throughput of both and the FP32 density error at t = 0.2."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    side = args.riemann_side
+    pts, h = W.riemann_cloud(side)
+    n = pts.shape[0]
+    dt = 0.1 * h
+    nsteps = int(round(0.2 / dt))
+    eq = M.CompressibleEulerEquations2D(1.4)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
+        solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision=prec))
+        dom = M.PointCloudDomain(solver, pts)
+        src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom),
+                            hv=M.SourceHyperviscosityTominec(solver, eq, dom))
+        semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.riemann_ic(x), solver,
+                                              source_terms=src)
+        ctx = dom.ctx
+        u0 = semi.compute_coefficients(0.0)
+        ctx.history_init(3)
+        ctx.set_state(u0, 0.0)
+        ctx.ssprk33(dt, 3, use_graph=True)          # warm-up (autotune, graph capture)
+        ctx.history_init(3)
+        ctx.set_state(u0, 0.0)
+        ctx.region_begin()
+        ctx.ssprk33(dt, nsteps, use_graph=True)
+        ms = ctx.region_end()
+        u, t = ctx.get_state()
+        ctx.close()
+        out[prec] = (ms, u, t)
+    ms64, u64, t64 = out["fp64"]
+    ms32, u32, _ = out["fp32"]
+    v64 = n * RHS_PER_STEP * nsteps / (ms64 * 1e-3)
+    v32 = n * RHS_PER_STEP * nsteps / (ms32 * 1e-3)
+    return {"workload": "four-quadrant Riemann problem, unit square, N=%d jittered nodes, k=%d, "
+                        "RV + Tominec HV, SSP-RK3 dt=0.1h to t=%.3f (%d steps), open edges"
+                        % (n, K_STENCIL, t64, nsteps),
+            "nodes": n, "steps": nsteps,
+            "fp64": {"value": v64, "unit": UNIT, "ms_per_step": ms64 / nsteps,
+                     "finite": bool(np.isfinite(u64).all())},
+            "fp32_apply": {"value": v32, "unit": UNIT, "ms_per_step": ms32 / nsteps,
+                           "speedup_vs_fp64": v32 / v64,
+                           "l2_density_err_vs_fp64": float(np.linalg.norm(u32[0] - u64[0])
+                                                           / np.linalg.norm(u64[0])),
+                           "linf_density_err_vs_fp64": float(np.abs(u32[0] - u64[0]).max()
+                                                             / np.abs(u64[0]).max())},
+            "density_range_fp64": [float(u64[0].min()), float(u64[0].max())]}
+
+
 def run_adjoint(args, local, peaks):
     """Gradient of J = 0.5 |rho(T) - rho*|^2 w.r.t. u0 for the isentropic vortex at
     N = 65,536 (T = 0.5, 500 SSP-RK3 steps, checkpoint every 20 steps; rho* the exact
-    density at T with seeded 1% noise), against the forward solve's cost."""
+    density at T plus seeded 1e-3 N(0,1) noise), against the forward solve's cost."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
-    side, T, nsteps, every = args.adj_side, 0.5, args.adj_steps, 20
+    side, T, nsteps, every = args.adj_side, args.adj_tend, args.adj_steps, 20
     dt = T / nsteps
     pts, per, _h = W.vortex_cloud(side)
     n = pts.shape[0]
@@ -259,7 +317,7 @@ def run_adjoint(args, local, peaks):
     ctx = dom.ctx
     u0 = semi.compute_coefficients(0.0)
     rng = np.random.default_rng(20)
-    target = W.isentropic_vortex(pts, T)[0] * (1.0 + 0.01 * rng.standard_normal(n))
+    target = W.isentropic_vortex(pts, T)[0] + 1e-3 * rng.standard_normal(n)
 
     def J(u):
         d = u[0] - target
@@ -306,8 +364,8 @@ def run_adjoint(args, local, peaks):
     bytes_node = 4 * K_STENCIL + 16 * K_STENCIL + 32 * 6
     ctx.close()
     return {"workload": "isentropic vortex N=%d, T=%.1f, %d SSP-RK3 steps, k=%d, no viscosity "
-                        "source; J = 0.5|rho(T) - rho*|^2, rho* exact density with 1%% seeded "
-                        "noise" % (n, T, nsteps, K_STENCIL),
+                        "source; J = 0.5|rho(T) - rho*|^2, rho* = exact density + 1e-3 N(0,1) "
+                        "(seeded)" % (n, T, nsteps, K_STENCIL),
             "nodes": n, "steps": nsteps, "checkpoint_every": every,
             "forward_ms": ms_fwd, "record_ms": ms_rec, "adjoint_sweep_ms": ms_adj,
             "gradient_over_forward": (ms_rec + ms_adj) / ms_fwd,
@@ -439,9 +497,10 @@ def config_dict(n, prec):
 def run_ours(args):
     ws, rank, local, pg = dist_setup()
     peaks = load_peaks()
-    if args.only == "adjoint":       # the adjoint measurement alone (profiling runs)
+    if args.only != "all":           # one auxiliary measurement alone (profiling runs)
         if rank == 0:
-            print(json.dumps({"adjoint": run_adjoint(args, local, peaks)}), flush=True)
+            leg = run_adjoint(args, local, peaks) if args.only == "adjoint" else run_riemann(args, local)
+            print(json.dumps({args.only: leg}), flush=True)
         return
     n = args.n_side ** 2
     semi, domain, u0, dt = build_problem(args.n_side, "fp64", local)
@@ -485,6 +544,7 @@ def run_ours(args):
 
     ens = run_ensemble(args, local, pg) if args.ens_members > 0 else None
     adj = run_adjoint(args, local, peaks) if args.adj_side > 0 and rank == 0 else None
+    rie = run_riemann(args, local) if args.riemann_side > 0 and rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -516,6 +576,7 @@ def run_ours(args):
                        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
         "ensemble": ens,
         "adjoint": adj,
+        "riemann": rie,
     }
     print(json.dumps(line), flush=True)
 
