@@ -116,7 +116,7 @@ mft_status mft_weights(mft_ctx* ctx, int op, int rbf_pow, int polydeg, int deriv
  * memory (xyz n*dim, rowptr n+1, cols rowptr[n] with centre first, w rowptr[n]*dim in
  * stencil order [slot][axis]); period is a host array of dim lengths or NULL; stream
  * may be 0.  kmax: the caller's bound on the stencil size; kmax + number of monomials
- * must be <= 118 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  A
+ * must be <= 116 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  A
  * stencil longer than kmax is skipped and reported as MFT_ERR_ARG.  The only global
  * scratch is a 32-byte static device array per GPU; its address is looked up on the
  * first call on each device (make that call before any stream capture), and it is
@@ -229,6 +229,25 @@ mft_status mft_set_rv_state(mft_ctx* ctx, const double* const* approx_du, int nv
 /* Viscosity of the last RV/upwind source evaluation (host, n values). */
 mft_status mft_get_viscosity(mft_ctx* ctx, double* eps);
 
+/* ---------------------------------------------------------------- positivity limiter
+ * PositivityPreservingLimiterZhangShu(; thresholds, variables)
+ * (src/callbacks_stage/positivity_zhang_shu.jl:22-66 with the point-cloud kernel
+ * limiter_zhang_shu!, positivity_zhang_shu_point2d.jl:22-82), used as the stage limiter
+ * of SSP-RK3: after every stage of mft_ssprk33 / mft_ssprk33_host, one pass per
+ * variable in the given order.  2D Euler only.  A node's stencil is its operator row;
+ * the stencil mean divides by that node's stencil size (the reference divides by the
+ * global neighbour count, the same number for its uniform stencils). */
+enum { MFT_LIM_DENSITY = 0, MFT_LIM_PRESSURE = 1 };
+
+/* nvar (<= 4) variables with their thresholds; nvar = 0 turns the limiter off. */
+mft_status mft_set_limiter(mft_ctx* ctx, int nvar, const int* variables,
+                           const double* thresholds);
+
+/* One application of the configured limiter to host StructArray-style arrays u (nvars
+ * pointers of length n), in place: Trixi.limiter_zhang_shu!(u, thresholds, variables,
+ * ...) (positivity_zhang_shu.jl:44-66). */
+mft_status mft_limit(mft_ctx* ctx, double* const* u, int nvars);
+
 /* ---------------------------------------------------------------- adjoint
  * Reverse-mode derivatives of rhs! and of the SSP-RK3 trajectory.  No function of
  * the reference corresponds: MeshfreeTrixi.jl differentiates rhs! only through
@@ -267,7 +286,7 @@ mft_status mft_ssprk33_adjoint_device(mft_ctx* ctx, double* lam);
 /* Kernel kinds reported by mft_profile_get. */
 enum {
   MFT_K_BC = 0, MFT_K_FLUX, MFT_K_FWD, MFT_K_MEAN, MFT_K_LEXMAX, MFT_K_EPS, MFT_K_REV,
-  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_ADJ, MFT_K_COUNT
+  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_ADJ, MFT_K_LIMITER, MFT_K_COUNT
 };
 
 /* enable != 0 starts recording an event pair around every kernel launch (and clears

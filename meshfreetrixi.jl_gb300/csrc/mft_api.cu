@@ -1213,6 +1213,17 @@ float* shadow(mft_ctx* c, int k) {
   return c->precision == MFT_PREC_FP32 ? c->U32[k].p : nullptr;
 }
 
+// Stage limiter: one Zhang-Shu pass per configured variable on stage state u.
+void apply_limiter(mft_ctx* c, double* u, float* u32) {
+  if (c->lim_n == 0) return;
+  c->lim_buf.alloc((size_t)c->n * 4);
+  for (int q = 0; q < c->lim_n; ++q) {
+    ProfScope ps(c, MFT_K_LIMITER);
+    launch_zs_limiter(c->n, c->fwd.view(), c->lim_var[q], c->lim_thr[q], c->gamma, u, u32,
+                      c->lim_buf.p, c->stream);
+  }
+}
+
 // FSAL evaluation at the current state: k0 = f(u_n), stage 1 = u_n + dt*k0.
 void fsal_eval(mft_ctx* c, double dt) {
   if (c->fsal_valid && c->fsal_dt == dt) return;
@@ -1225,6 +1236,7 @@ void fsal_eval(mft_ctx* c, double dt) {
   ep.out = c->U[1].p;
   ep.out32 = shadow(c, 1);
   eval_rhs(c, c->U[0].p, shadow(c, 0), c->t_state, ep);
+  apply_limiter(c, c->U[1].p, shadow(c, 1));
   if (c->hist_order >= 0 && c->success_iter == 0) history_push(c, c->t_state, c->U[0].p, 0);
   c->fsal_valid = true;
   c->fsal_dt = dt;
@@ -1240,6 +1252,7 @@ void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3) {
   e2.out = c->U[2].p;
   e2.out32 = shadow(c, 2);
   eval_rhs(c, c->U[1].p, shadow(c, 1), t + dt, e2);
+  apply_limiter(c, c->U[2].p, shadow(c, 2));
   Epilogue e3{};
   e3.kind = kStage3;
   e3.dt = dt;
@@ -1247,12 +1260,14 @@ void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3) {
   e3.out = c->U[iu_3].p;
   e3.out32 = shadow(c, iu_3);
   eval_rhs(c, c->U[2].p, shadow(c, 2), t + 0.5 * dt, e3);
+  apply_limiter(c, c->U[iu_3].p, shadow(c, iu_3));
   Epilogue e1{};
   e1.kind = kStage1;
   e1.dt = dt;
   e1.out = c->U[1].p;
   e1.out32 = shadow(c, 1);
   eval_rhs(c, c->U[iu_3].p, shadow(c, iu_3), t + dt, e1);
+  apply_limiter(c, c->U[1].p, shadow(c, 1));
 }
 
 void ssprk33_direct(mft_ctx* c, double dt, int nsteps) {
@@ -1460,7 +1475,7 @@ mft_status mft_profile_get(mft_ctx* c, int kind, double* total_ms, int64_t* laun
                            const char** name) {
   static const char* names[MFT_K_COUNT] = {"bc_pass1", "flux", "fwd_gather", "mean",
                                            "lexmax", "eps", "rev_gather", "rev_lap",
-                                           "history", "layout", "adjoint"};
+                                           "history", "layout", "adjoint", "limiter"};
   return guarded(c, [&] {
     MFT_REQUIRE(kind >= 0 && kind < MFT_K_COUNT, MFT_ERR_ARG, "bad kernel kind");
     set_device(c);
@@ -1499,6 +1514,53 @@ mft_status mft_get_viscosity(mft_ctx* c, double* eps) {
   });
 }
 
+// ---------------------------------------------------------------- positivity limiter
+
+mft_status mft_set_limiter(mft_ctx* c, int nvar, const int* variables, const double* thresholds) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(nvar >= 0 && nvar <= 4, MFT_ERR_ARG, "between 0 and 4 limiter variables");
+    MFT_REQUIRE(nvar == 0 || (variables && thresholds), MFT_ERR_ARG, "NULL variables/thresholds");
+    if (nvar > 0) MFT_REQUIRE(c->eq == MFT_EQ_EULER2D, MFT_ERR_UNSUPPORTED,
+                              "the positivity limiter needs the 2D Euler equations");
+    for (int q = 0; q < nvar; ++q) {
+      MFT_REQUIRE(variables[q] == MFT_LIM_DENSITY || variables[q] == MFT_LIM_PRESSURE,
+                  MFT_ERR_ARG, "limiter variable must be MFT_LIM_DENSITY or MFT_LIM_PRESSURE");
+      MFT_REQUIRE(isfinite(thresholds[q]), MFT_ERR_ARG, "limiter threshold must be finite");
+    }
+    c->lim_n = nvar;
+    for (int q = 0; q < nvar; ++q) {
+      c->lim_var[q] = variables[q];
+      c->lim_thr[q] = thresholds[q];
+    }
+    c->graph_valid = false;
+    c->fsal_valid = false;
+  });
+}
+
+mft_status mft_limit(mft_ctx* c, double* const* u, int nvars) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(u && nvars == c->nvars, MFT_ERR_ARG, "bad state arrays or nvars");
+    MFT_REQUIRE(c->lim_n > 0, MFT_ERR_STATE, "no limiter configured (mft_set_limiter)");
+    set_device(c);
+    ensure_work(c);
+    ensure_device_ops(c);
+    const int64_t n = c->n;
+    cudaStream_t s = c->stream;
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+    launch_aos_from_soa(c->soa.p, c->work_u.p, n, nvars, s);
+    apply_limiter(c, c->work_u.p, nullptr);
+    launch_soa_from_aos(c->work_u.p, c->soa.p, n, nvars, s);
+    for (int v = 0; v < nvars; ++v)
+      MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    MFT_CUDA(cudaStreamSynchronize(s));
+    check_kernel_errors(c);
+  });
+}
+
 // ---------------------------------------------------------------- adjoint
 
 namespace {
@@ -1522,6 +1584,8 @@ int adj_hv_mode(mft_ctx* c, double* gamma) {
 
 void check_adjoint_ready(mft_ctx* c) {
   check_state_ready(c);
+  MFT_REQUIRE(c->lim_n == 0, MFT_ERR_UNSUPPORTED,
+              "adjoint: the positivity limiter is not differentiable (turn it off)");
   MFT_REQUIRE(c->dim == 2, MFT_ERR_UNSUPPORTED, "adjoint: 2D problems only");
   MFT_REQUIRE(c->precision == MFT_PREC_FP64, MFT_ERR_UNSUPPORTED, "adjoint: FP64 form only");
   double g;

@@ -116,6 +116,12 @@ struct mft_ctx {
   mft::DBuf<double> d_seg_h, seg_partial, seg_mean, seg_norms;
   mft::DBuf<unsigned> seg_counter;
 
+  // Zhang-Shu positivity limiter after every SSP-RK3 stage (variables in order)
+  int lim_n = 0;
+  int lim_var[4] = {0, 0, 0, 0};
+  double lim_thr[4] = {0, 0, 0, 0};
+  mft::DBuf<double> lim_buf;
+
   // adjoint: recorded trajectory (checkpoints, or every stage state) and cotangents
   mft::DBuf<double> adj_lam[3], adj_acc, adj_q, adj_store, adj_ckpt;
   bool adj_valid = false;

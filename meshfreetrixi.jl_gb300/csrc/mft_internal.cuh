@@ -257,6 +257,12 @@ void launch_lap_masked(int64_t n, EllView fwd, const double* wl, const double* l
 void launch_bc_project(int64_t nb, const int32_t* bnode, int V, BcDev bc, double* lam,
                        cudaStream_t s);
 
+// One Zhang-Shu positivity-limiter pass (variable 0 density, 1 pressure) on the Euler
+// state u (n x 4 AoS, FP32 shadow u32 optional) over the stencils of the forward layout;
+// loc is n x 4 scratch.
+void launch_zs_limiter(int64_t n, EllView ell, int variable, double threshold, double gamma,
+                       double* u, float* u32, double* loc, cudaStream_t s);
+
 // Sets *flag to 1 when a and b differ in any of `count` doubles (bitwise).
 void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s);
 

@@ -114,13 +114,17 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
-// Triangular index t -> (i, j) with 0 <= i <= j: t = j(j+1)/2 + i.
-__device__ __forceinline__ void tri_ij(int t, int& i, int& j) {
-  int jj = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-  while ((jj + 1) * (jj + 2) / 2 <= t) ++jj;
-  while (jj * (jj + 1) / 2 > t) --jj;
-  j = jj;
-  i = t - jj * (jj + 1) / 2;
+// Advances (i, j), 0 <= i <= j, to the next element a warp stride further along the
+// column-major upper triangle (t = j(j+1)/2 + i).
+__device__ __forceinline__ void tri_next(int& i, int& j, int step) {
+  i += step;
+  while (i > j) { i -= j + 1; ++j; }
+}
+
+// Doubles of shared memory one warp of k_weights uses: A (nmax^2), B (3 nmax),
+// X (3 kmax), two column-multiplier arrays (2 nmax) and the pivot ints (nmax).
+__host__ __device__ __forceinline__ size_t weights_smem_doubles(int nmax, int kmax) {
+  return (size_t)nmax * nmax + (size_t)nmax * 3 + (size_t)kmax * 3 + (size_t)nmax * 2 + nmax;
 }
 
 // kOrdered: systems are taken in the order of a.order_list (largest first); otherwise
@@ -131,14 +135,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int nmax = a.nmax;
-  // per-warp shared layout: A[nmax*nmax], B[nmax*3], X[kmax*3], aux[nmax] (ints)
-  const size_t per = (size_t)nmax * nmax + (size_t)nmax * 3 + (size_t)a.kmax * 3 + nmax;
+  // per-warp shared layout: A[nmax*nmax], B[nmax*3], X[kmax*3], TC[nmax], TC2[nmax],
+  // ipiv[nmax] (ints)
+  const size_t per = weights_smem_doubles(nmax, a.kmax);
   double* A = smem + per * wib;
   double* B = A + (size_t)nmax * nmax;
   double* X = B + (size_t)nmax * 3;
-  int* ipiv = reinterpret_cast<int*>(X + (size_t)a.kmax * 3);
-  double* tmpw = B;  // reuse is not possible (B live); use X tail for 2x2 temporaries
-  (void)tmpw;
+  double* TC = X + (size_t)a.kmax * 3;
+  double* TC2 = TC + nmax;
+  int* ipiv = reinterpret_cast<int*>(TC2 + nmax);
   const int dim = a.dim;
 
   for (;;) {
@@ -179,9 +184,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
     __syncwarp();
     // interpolation block (upper triangle, column-major)
     const int T = n * (n + 1) / 2;
-    for (int t = lane; t < T; t += 32) {
-      int r, cidx;
-      tri_ij(t, r, cidx);
+    int r = 0, cidx = 0;
+    tri_next(r, cidx, lane);
+    for (int t = lane; t < T; t += 32, tri_next(r, cidx, 32)) {
       double v;
       if (cidx < k) {
         double d2 = 0.0;
@@ -286,15 +291,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
         }
         if (kstep == 1) {
           const double r1 = ddiv(1.0, AM(kk, kk));
+          // column multipliers temp_j = -r1 x_j (dsyr), then A(i,j) += A(i,kk) temp_j
+          // for x_j != 0, one fused multiply-add per element
+          for (int j = lane; j < kk - 1; j += 32) TC[j] = dmul(-r1, AM(j + 1, kk));
+          __syncwarp();
           const int Tu = (kk - 1) * kk / 2;
-          for (int t = lane; t < Tu; t += 32) {
-            int i0, j0;
-            tri_ij(t, i0, j0);
-            const double xj = AM(j0 + 1, kk);
-            if (xj != 0.0) {
-              const double temp = dmul(-r1, xj);
-              AM(i0 + 1, j0 + 1) = dadd(AM(i0 + 1, j0 + 1), dmul(AM(i0 + 1, kk), temp));
-            }
+          int i0 = 0, j0 = 0;
+          tri_next(i0, j0, lane);
+          for (int t = lane; t < Tu; t += 32, tri_next(i0, j0, 32)) {
+            if (AM(j0 + 1, kk) != 0.0)
+              AM(i0 + 1, j0 + 1) = fma(AM(i0 + 1, kk), TC[j0], AM(i0 + 1, j0 + 1));
           }
           __syncwarp();
           for (int i = 1 + lane; i < kk; i += 32) AM(i, kk) = dmul(r1, AM(i, kk));
@@ -305,26 +311,27 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           const double d11 = ddiv(AM(kk, kk), d12o);
           const double tt = ddiv(1.0, dsub(dmul(d11, d22), 1.0));
           const double d12 = ddiv(tt, d12o);
-          // wk, wkm1 of every column j <= kk-2 from the original entries (kept in X's
-          // spare tail would alias; store them in B's unused columns is unsafe), so
-          // compute them on the fly per element: they depend only on column kk-1/kk.
-          const int Tu = (kk - 2) * (kk - 1) / 2;
-          for (int t = lane; t < Tu; t += 32) {
-            int i0, j0;
-            tri_ij(t, i0, j0);
-            const int j = j0 + 1, i = i0 + 1;
-            const double wkm1 = dmul(d12, dsub(dmul(d11, AM(j, kk - 1)), AM(j, kk)));
-            const double wk = dmul(d12, dsub(dmul(d22, AM(j, kk)), AM(j, kk - 1)));
-            AM(i, j) = dsub(dsub(AM(i, j), dmul(AM(i, kk), wk)), dmul(AM(i, kk - 1), wkm1));
+          // wkm1, wk of every column j <= kk-2 from the original entries, then
+          // A(i,j) -= A(i,kk) wk + A(i,kk-1) wkm1 as two fused multiply-adds, then
+          // columns kk-1, kk take wkm1, wk (dsytf2 order: each update reads only
+          // rows i <= j, which the column overwrite has not reached)
+          for (int j = lane; j < kk - 2; j += 32) {
+            const double a1 = AM(j + 1, kk - 1), a2 = AM(j + 1, kk);
+            TC[j] = dmul(d12, dsub(dmul(d11, a1), a2));
+            TC2[j] = dmul(d12, dsub(dmul(d22, a2), a1));
           }
           __syncwarp();
-          // now overwrite columns kk-1, kk (rows 1..kk-2) with wkm1, wk
-          for (int j = 1 + lane; j <= kk - 2; j += 32) {
-            const double a1 = AM(j, kk - 1), a2 = AM(j, kk);
-            const double wkm1 = dmul(d12, dsub(dmul(d11, a1), a2));
-            const double wk = dmul(d12, dsub(dmul(d22, a2), a1));
-            AM(j, kk) = wk;
-            AM(j, kk - 1) = wkm1;
+          const int Tu = (kk - 2) * (kk - 1) / 2;
+          int i0 = 0, j0 = 0;
+          tri_next(i0, j0, lane);
+          for (int t = lane; t < Tu; t += 32, tri_next(i0, j0, 32)) {
+            const int j = j0 + 1, i = i0 + 1;
+            AM(i, j) = fma(-AM(i, kk - 1), TC[j0], fma(-AM(i, kk), TC2[j0], AM(i, j)));
+          }
+          __syncwarp();
+          for (int j = lane; j < kk - 2; j += 32) {
+            AM(j + 1, kk) = TC2[j];
+            AM(j + 1, kk - 1) = TC[j];
           }
           __syncwarp();
         }
@@ -359,7 +366,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           const double bk = BM(kk, c);
           if (bk != 0.0) {
             const double temp = -bk;
-            for (int i = 1 + lane; i < kk; i += 32) BM(i, c) = dadd(BM(i, c), dmul(AM(i, kk), temp));
+            for (int i = 1 + lane; i < kk; i += 32) BM(i, c) = fma(AM(i, kk), temp, BM(i, c));
           }
         }
         __syncwarp();
@@ -378,8 +385,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           const double bkm1 = BM(kk - 1, c);
           for (int i = 1 + lane; i <= kk - 2; i += 32) {
             double v = BM(i, c);
-            if (bk != 0.0) v = dadd(v, dmul(AM(i, kk), -bk));
-            if (bkm1 != 0.0) v = dadd(v, dmul(AM(i, kk - 1), -bkm1));
+            if (bk != 0.0) v = fma(AM(i, kk), -bk, v);
+            if (bkm1 != 0.0) v = fma(AM(i, kk - 1), -bkm1, v);
             BM(i, c) = v;
           }
         }
@@ -406,7 +413,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
         for (int q = 0; q < ncol; ++q) {
           // dot product in a fixed 32-way strided order, then a pairwise tree
           double part = 0.0;
-          for (int i = 1 + lane; i < kk; i += 32) part = dadd(part, dmul(BM(i, c), AM(i, kk + q)));
+          for (int i = 1 + lane; i < kk; i += 32) part = fma(BM(i, c), AM(i, kk + q), part);
           for (int o = 16; o > 0; o >>= 1) part = dadd(part, __shfl_down_sync(kFull, part, o));
           if (lane == 0) BM(kk + q, c) = dadd(BM(kk + q, c), dmul(-1.0, part));
           __syncwarp();
@@ -525,8 +532,7 @@ void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
   for (int64_t i = 0; i < n; ++i) kmax = std::max<int>(kmax, (int)(c->st_rp[i + 1] - c->st_rp[i]));
   a.kmax = kmax;
   a.nmax = kmax + a.npoly;
-  const size_t per = (size_t)a.nmax * a.nmax + (size_t)a.nmax * 3 + (size_t)kmax * 3 + a.nmax;
-  const size_t shmem = per * sizeof(double) * kWarpsPerBlock;
+  const size_t shmem = weights_smem_doubles(a.nmax, kmax) * sizeof(double) * kWarpsPerBlock;
   MFT_REQUIRE(shmem <= 227 * 1024, MFT_ERR_ARG, "stencil too large for the weight kernel");
   cudaStream_t s = c->stream;
   DBuf<int64_t> d_order, d_rp;
@@ -639,15 +645,14 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   for (int d = 0; d < 3; ++d) a.period[d] = (period && d < dim) ? period[d] : 0.0;
   a.kmax = kmax;
   a.nmax = kmax + a.npoly;
-  const size_t per = (size_t)a.nmax * a.nmax + (size_t)a.nmax * 3 + (size_t)kmax * 3 + a.nmax;
-  const size_t shmem = per * sizeof(double) * kWarpsPerBlock;
+  const size_t shmem = weights_smem_doubles(a.nmax, kmax) * sizeof(double) * kWarpsPerBlock;
   const size_t kMaxShmem = 227 * 1024;
   if (a.npoly > 128 || shmem > kMaxShmem) {
     put_err(err, err_len,
             "mft_weights_noalloc: stencil size " + std::to_string(kmax) + " plus " +
                 std::to_string(a.npoly) + " monomials needs " + std::to_string(shmem) +
                 " bytes of shared memory; the maximum is " + std::to_string(kMaxShmem) +
-                " (kmax + monomials <= 118)");
+                " (kmax + monomials <= 116)");
     return MFT_ERR_ARG;
   }
   int dev = 0;

@@ -4,7 +4,7 @@ from ._lib import Context, MFTError, load  # noqa: F401
 from .api import (  # noqa: F401
     RBF, BoundaryConditionDirichlet, BoundaryConditionDoNothing, BoundaryData,
     CompressibleEulerEquations2D, HistoryCallback, LinearScalarAdvectionEquation2D, ODEProblem,
-    Point1D, Point2D, Point3D, PointCloudBasis, PointCloudDomain, PointCloudDomain_from_medusa,
+    Point1D, Point2D, Point3D, PointCloudBasis, PositivityPreservingLimiterZhangShu, density, pressure, PointCloudDomain, PointCloudDomain_from_medusa,
     PointCloudEnsemble, PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
     SemidiscretizationHyperbolic, SourceHyperviscosityFlyer, SourceHyperviscosityTominec,
     SourceResidualViscosityTominec, SourceTerms, SourceUpwindViscosityTominec, SSPRK33,

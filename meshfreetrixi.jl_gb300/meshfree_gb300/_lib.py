@@ -21,6 +21,7 @@ BC_DIRICHLET, BC_SLIP_WALL, BC_DO_NOTHING = 0, 1, 2
 SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER = 0, 1, 2, 3
 OP_GRAD, OP_LAP, OP_HV = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
+LIM_DENSITY, LIM_PRESSURE = 0, 1
 OPT_GATHER, OPT_TUNED_FWD, OPT_TUNED_REV = 0, 1, 2
 GATHER_AUTO, GATHER_THREAD, GATHER_STAGED = 0, 1, 2
 
@@ -58,6 +59,8 @@ SIGNATURES = {
     "mft_ssprk33": (I32, [VP, DBL, I32, I32]),
     "mft_ssprk33_host": (I32, [VP, VP, I32, C.POINTER(DBL), DBL, I32]),
     "mft_set_rv_state": (I32, [VP, VP, I32, I32]),
+    "mft_set_limiter": (I32, [VP, I32, VP, VP]),
+    "mft_limit": (I32, [VP, VP, I32]),
     "mft_rhs_adjoint": (I32, [VP, VP, VP, VP, I32, DBL]),
     "mft_rhs_adjoint_device": (I32, [VP, VP, VP, VP, DBL]),
     "mft_ssprk33_record": (I32, [VP, DBL, I32, I32]),
@@ -69,7 +72,7 @@ SIGNATURES = {
     "mft_region": (I32, [VP, I32, C.POINTER(DBL)]),
 }
 K_NAMES = ["bc_pass1", "flux", "fwd_gather", "mean", "lexmax", "eps", "rev_gather", "rev_lap",
-           "history", "layout", "adjoint"]
+           "history", "layout", "adjoint", "limiter"]
 
 _lib = None
 
@@ -248,6 +251,18 @@ class Context:
         self.check(self.lib.mft_ssprk33_host(self.h, _ptrs(list(u)), u.shape[0], C.byref(tt),
                                              dt, nsteps))
         return tt.value
+
+    # positivity limiter ------------------------------------------------------
+    def set_limiter(self, kinds, thresholds):
+        k = np.ascontiguousarray(kinds, dtype=np.int32)
+        th = np.ascontiguousarray(thresholds, dtype=np.float64)
+        self.check(self.lib.mft_set_limiter(self.h, k.size, _p(k) if k.size else None,
+                                            _p(th) if k.size else None))
+
+    def limit(self, u):
+        """Applies the configured limiter to the (nvars, n) host array u in place."""
+        assert u.flags.c_contiguous and u.dtype == np.float64
+        self.check(self.lib.mft_limit(self.h, _ptrs(list(u)), u.shape[0]))
 
     # adjoint --------------------------------------------------------------
     def rhs_adjoint(self, lam, u, t=0.0):

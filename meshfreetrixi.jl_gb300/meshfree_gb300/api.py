@@ -432,7 +432,46 @@ class HistoryCallback:
 
 
 class SSPRK33:
-    """Shu-Osher SSP-RK3 with first-same-as-last stage reuse."""
+    """Shu-Osher SSP-RK3 with first-same-as-last stage reuse; SSPRK33(stage_limiter!)
+    applies the limiter after every stage, as OrdinaryDiffEq does."""
+
+    def __init__(self, stage_limiter=None):
+        self.stage_limiter = stage_limiter
+
+
+def density(u, equations=None):
+    """Trixi.density (the first conserved variable)."""
+    return u[0]
+
+
+def pressure(u, equations):
+    """Trixi.pressure for CompressibleEulerEquations2D."""
+    return (equations.gamma - 1.0) * (u[3] - 0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0])
+
+
+class PositivityPreservingLimiterZhangShu:
+    """PositivityPreservingLimiterZhangShu(; thresholds, variables)
+    (src/callbacks_stage/positivity_zhang_shu.jl:22-31); variables are `density` and
+    `pressure`, applied in the given order.  Calling it on (u, semi) limits u in place
+    (limiter_zhang_shu!, positivity_zhang_shu_point2d.jl:22-82) on the GPU."""
+
+    def __init__(self, thresholds, variables):
+        if len(thresholds) != len(variables):
+            raise ValueError("one threshold per variable")
+        kinds = {density: L.LIM_DENSITY, pressure: L.LIM_PRESSURE}
+        self.thresholds = tuple(float(x) for x in thresholds)
+        self.variables = tuple(variables)
+        self.kinds = [kinds[v] for v in self.variables]
+
+    def configure(self, ctx):
+        ctx.set_limiter(self.kinds, self.thresholds)
+
+    def __call__(self, u, semi):
+        ctx = semi.domain.ctx
+        self.configure(ctx)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        ctx.limit(u)
+        return u
 
 
 @dataclass
@@ -450,6 +489,11 @@ def solve(ode, alg=None, dt=None, callback=None, save_everystep=False):
     t0, t1 = ode.tspan
     cbs = callback if isinstance(callback, (list, tuple)) else ([callback] if callback else [])
     ctx.set_state(ode.u0, t0)
+    lim = getattr(alg, "stage_limiter", None)
+    if lim is not None:
+        lim.configure(ctx)
+    else:
+        ctx.set_limiter([], [])
     for cb in cbs:
         if isinstance(cb, HistoryCallback):
             ctx.history_init(cb.approx_order)

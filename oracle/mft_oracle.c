@@ -279,6 +279,9 @@ int mfto_knn(int dim, int64_t n, const double* x, const double* period, int k, i
 /* Bunch-Kaufman LDL^T, upper storage (restating LAPACK dsytf2 + dsytrs,     */
 /* the factorisation behind `Symmetric \` at compute_operators.jl:435)       */
 /* ------------------------------------------------------------------------ */
+/* The rank-1 / rank-2 updates and the solve's axpy and dot products use explicit
+ * fused multiply-adds (one rounding per update, as optimised BLAS kernels do); the
+ * device solver performs the same operations in the same order. */
 
 #define AM(i, j) a[(size_t)((j)-1) * (size_t)n + (size_t)((i)-1)]
 #define BM(i, c) b[(size_t)(c) * (size_t)n + (size_t)((i)-1)]
@@ -332,7 +335,7 @@ static int bk_factor(int n, double* a, int* ipiv) {
           double xj = AM(j, k);
           if (xj != 0.0) {
             double temp = -r1 * xj;
-            for (int i = 1; i <= j; ++i) AM(i, j) = AM(i, j) + AM(i, k) * temp;
+            for (int i = 1; i <= j; ++i) AM(i, j) = fma(AM(i, k), temp, AM(i, j));
           }
         }
         for (int i = 1; i < k; ++i) AM(i, k) = r1 * AM(i, k);
@@ -345,7 +348,7 @@ static int bk_factor(int n, double* a, int* ipiv) {
         for (int j = k - 2; j >= 1; --j) {
           double wkm1 = d12 * (d11 * AM(j, k - 1) - AM(j, k));
           double wk = d12 * (d22 * AM(j, k) - AM(j, k - 1));
-          for (int i = j; i >= 1; --i) AM(i, j) = AM(i, j) - AM(i, k) * wk - AM(i, k - 1) * wkm1;
+          for (int i = j; i >= 1; --i) AM(i, j) = fma(-AM(i, k - 1), wkm1, fma(-AM(i, k), wk, AM(i, j)));
           AM(j, k) = wk;
           AM(j, k - 1) = wkm1;
         }
@@ -359,13 +362,14 @@ static int bk_factor(int n, double* a, int* ipiv) {
 }
 
 /* The dot products of dsytrs (DGEMV 'T') are summed in a fixed order: 32 strided
- * partial sums (term i goes to partial (i-1) mod 32, ascending i), then combined
+ * fused multiply-add partial sums (term i goes to partial (i-1) mod 32, ascending i),
+ * then combined
  * pairwise (p[L] += p[L+16], then +8, +4, +2, +1).  LAPACK leaves this order to the
  * BLAS build; fixing it here lets the device solve be checked bit for bit. */
 static double dot_strided(int m, const double* x, const double* y) {
   double p[32];
   for (int l = 0; l < 32; ++l) p[l] = 0.0;
-  for (int i = 0; i < m; ++i) p[i & 31] = p[i & 31] + x[i] * y[i];
+  for (int i = 0; i < m; ++i) p[i & 31] = fma(x[i], y[i], p[i & 31]);
   for (int o = 16; o > 0; o >>= 1)
     for (int l = 0; l < o; ++l) p[l] = p[l] + p[l + o];
   return p[0];
@@ -382,7 +386,7 @@ static void bk_solve_factored(int n, const double* a, const int* ipiv, int nrhs,
         double bk = BM(k, c);
         if (bk != 0.0) {
           double temp = -bk;
-          for (int i = 1; i < k; ++i) BM(i, c) = BM(i, c) + AM(i, k) * temp;
+          for (int i = 1; i < k; ++i) BM(i, c) = fma(AM(i, k), temp, BM(i, c));
         }
       }
       double r = 1.0 / AM(k, k);
@@ -396,14 +400,14 @@ static void bk_solve_factored(int n, const double* a, const int* ipiv, int nrhs,
         double bk = BM(k, c);
         if (bk != 0.0) {
           double temp = -bk;
-          for (int i = 1; i <= k - 2; ++i) BM(i, c) = BM(i, c) + AM(i, k) * temp;
+          for (int i = 1; i <= k - 2; ++i) BM(i, c) = fma(AM(i, k), temp, BM(i, c));
         }
       }
       for (int c = 0; c < nrhs; ++c) {
         double bk = BM(k - 1, c);
         if (bk != 0.0) {
           double temp = -bk;
-          for (int i = 1; i <= k - 2; ++i) BM(i, c) = BM(i, c) + AM(i, k - 1) * temp;
+          for (int i = 1; i <= k - 2; ++i) BM(i, c) = fma(AM(i, k - 1), temp, BM(i, c));
         }
       }
       double akm1k = AM(k - 1, k);
@@ -1113,6 +1117,51 @@ int mfto_rhs_adjoint(const mfto_semi* s, const double* const* u, const double* c
   }
   free(tag); free(slot); free(lt); free(g);
   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Zhang-Shu positivity limiter  positivity_zhang_shu_point2d.jl:22-82       */
+/* ------------------------------------------------------------------------ */
+
+/* Trixi's density(u) and pressure(u) for CompressibleEulerEquations2D. */
+static double zs_variable(int variable, double gamma, const double* uu) {
+  if (variable == 0) return uu[0];
+  return (gamma - 1.0) * (uu[3] - 0.5 * (uu[1] * uu[1] + uu[2] * uu[2]) / uu[0]);
+}
+
+int64_t mfto_limiter_zhang_shu(int64_t n, int nvars, double gamma, const int64_t* rowptr,
+                               const int32_t* cols, int variable, double threshold,
+                               double* const* u) {
+  double* loc = (double*)calloc((size_t)n * nvars, sizeof(double));
+  if (!loc) return -2;
+  int64_t limited = 0;
+  for (int64_t e = 0; e < n; ++e) {
+    double uu[8], mean[8];
+    double vmin = INFINITY;
+    for (int64_t p = rowptr[e]; p < rowptr[e + 1]; ++p) {
+      for (int v = 0; v < nvars; ++v) uu[v] = u[v][cols[p]];
+      vmin = jl_min(vmin, zs_variable(variable, gamma, uu));
+    }
+    if (!(vmin < threshold)) continue;
+    for (int v = 0; v < nvars; ++v) mean[v] = 0.0;
+    for (int64_t p = rowptr[e]; p < rowptr[e + 1]; ++p)
+      for (int v = 0; v < nvars; ++v) mean[v] = mean[v] + u[v][cols[p]];
+    const double cnt = (double)(rowptr[e + 1] - rowptr[e]);
+    for (int v = 0; v < nvars; ++v) mean[v] = mean[v] / cnt;
+    const double vmean = zs_variable(variable, gamma, mean);
+    const double theta = (vmean - threshold) / (vmean - vmin);
+    for (int v = 0; v < nvars; ++v)
+      loc[(size_t)e * nvars + v] = fma(theta, u[v][e], (1.0 - theta) * mean[v]);
+  }
+  for (int64_t e = 0; e < n; ++e) {
+    int nz = 0;
+    for (int v = 0; v < nvars; ++v) nz |= loc[(size_t)e * nvars + v] != 0.0;
+    if (!nz) continue;
+    for (int v = 0; v < nvars; ++v) u[v][e] = loc[(size_t)e * nvars + v];
+    limited++;
+  }
+  free(loc);
+  return limited;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -16,7 +16,9 @@
  *     parity unpinned (no Julia toolchain exists to run the reference).
  *
  * Arithmetic conventions: this file is compiled with -ffp-contract=off so every
- * a*b+c rounds twice, like Julia code outside @muladd (SparseArrays, Distances).
+ * a*b+c rounds twice, like Julia code outside @muladd (SparseArrays, Distances);
+ * explicit fma() calls restate fused operations (the Bunch-Kaufman updates, as
+ * optimised BLAS kernels perform them, and @muladd expressions of the limiter).
  */
 #ifndef MFT_ORACLE_H
 #define MFT_ORACLE_H
@@ -130,6 +132,20 @@ int mfto_rhs(const mfto_semi* s, double t, const double* dirichlet, double* cons
  * viscosity is a maximum over the field and has no adjoint here). */
 int mfto_rhs_adjoint(const mfto_semi* s, const double* const* u, const double* const* lam,
                      double* const* out, int nthreads);
+/* Zhang-Shu positivity limiter on a point cloud, one variable pass of
+ * limiter_zhang_shu! (src/callbacks_stage/positivity_zhang_shu_point2d.jl:22-82):
+ * per node e, value_min = min over e's stencil of variable(u); where
+ * value_min < threshold, u_mean = (sum over the stencil of u) / stencil size,
+ * theta = (variable(u_mean) - threshold) / (variable(u_mean) - value_min) and the new
+ * state is muladd(theta, u[e], (1 - theta) u_mean), applied after all nodes are
+ * computed (a zero result leaves the node unchanged, as the reference's test does).
+ * variable: 0 density, 1 pressure (Euler, gamma).  Stencils in the given order
+ * (rowptr, cols).  u: nvars pointers, mutated.  Returns the number of limited nodes.
+ * The reference divides by the global neighbour count; it equals the stencil size
+ * for the uniform stencils it supports. */
+int64_t mfto_limiter_zhang_shu(int64_t n, int nvars, double gamma, const int64_t* rowptr,
+                               const int32_t* cols, int variable, double threshold,
+                               double* const* u);
 /* Pieces of rhs! exposed for the reference's own identity tests. */
 int mfto_calc_fluxes(const mfto_semi* s, double* const* du, double* const* u, int nthreads);
 /* y += alpha * A x (SparseArrays 5-arg mul!, CSC column scatter == ascending CSR rows) */

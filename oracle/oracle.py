@@ -71,6 +71,9 @@ def lib():
                                C.c_void_p, C.POINTER(_Diag), C.c_int]
         L.mfto_rhs_adjoint.restype = C.c_int
         L.mfto_rhs_adjoint.argtypes = [C.POINTER(_Semi), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.mfto_limiter_zhang_shu.restype = C.c_int64
+        L.mfto_limiter_zhang_shu.argtypes = [C.c_int64, C.c_int, C.c_double, I64P, I32P, C.c_int,
+                                             C.c_double, C.c_void_p]
         L.mfto_calc_fluxes.restype = C.c_int
         L.mfto_calc_fluxes.argtypes = [C.POINTER(_Semi), C.c_void_p, C.c_void_p, C.c_int]
         for name in ("mfto_spmv_accum", "mfto_spmv_t_accum"):
@@ -423,10 +426,35 @@ class History:
         return ad
 
 
+LIM_DENSITY, LIM_PRESSURE = 0, 1
+
+
+def limiter_zhang_shu(u, rowptr, cols, variable, threshold, gamma=1.4):
+    """One variable pass of limiter_zhang_shu! (positivity_zhang_shu_point2d.jl:22-82)
+    on the (4, n) Euler state u, in place; stencils (rowptr, cols) in the order given.
+    Returns the number of limited nodes."""
+    assert u.flags.c_contiguous and u.dtype == np.float64 and u.shape[0] == 4
+    rp = np.ascontiguousarray(rowptr, dtype=np.int64)
+    ci = np.ascontiguousarray(cols, dtype=np.int32)
+    ptrs = (C.c_void_p * 4)(*[u[v].ctypes.data for v in range(4)])
+    return int(lib().mfto_limiter_zhang_shu(u.shape[1], 4, gamma, rp, ci, variable, threshold,
+                                            C.cast(ptrs, C.c_void_p)))
+
+
+def stage_limiter(rowptr, cols, variables, thresholds, gamma=1.4):
+    """PositivityPreservingLimiterZhangShu(; thresholds, variables) as a callable on u."""
+    def lim(u):
+        for var, thr in zip(variables, thresholds):
+            limiter_zhang_shu(u, rowptr, cols, var, thr, gamma)
+    return lim
+
+
 def ssprk33(semi: Semi, u0, t0, dt, nsteps, history: History | None = None, nthreads=8,
-            callback=None):
+            callback=None, stage_limiter=None):
     """OrdinaryDiffEq SSPRK33 (Shu-Osher form, FSAL) with the HistoryCallback
-    applied after every accepted step and once at initialisation."""
+    applied after every accepted step and once at initialisation; stage_limiter(u)
+    (in place) after every stage, as SSPRK33(stage_limiter!) applies it."""
+    lim = stage_limiter if stage_limiter is not None else (lambda u: None)
     u = np.array(u0, dtype=np.float64, copy=True)
     t = t0
     k = semi.rhs(u, t, nthreads)
@@ -435,10 +463,13 @@ def ssprk33(semi: Semi, u0, t0, dt, nsteps, history: History | None = None, nthr
     for step in range(nsteps):
         un = u.copy()
         u1 = un + dt * k
+        lim(u1)
         k1 = semi.rhs(u1, t + dt, nthreads)
         u2 = (3.0 * un + u1 + dt * k1) / 4.0
+        lim(u2)
         k2 = semi.rhs(u2, t + 0.5 * dt, nthreads)
         u3 = (un + 2.0 * u2 + 2.0 * dt * k2) / 3.0
+        lim(u3)
         t = t0 + (step + 1) * dt
         k = semi.rhs(u3, t, nthreads)
         u = u3

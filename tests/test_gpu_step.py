@@ -54,6 +54,26 @@ def test_advection_rv_trajectory_matches_oracle(oracle, gpu_lib):
     assert err < 1e-10, err
 
 
+def test_advection_64_200_steps_matches_oracle(oracle, gpu_lib):
+    """The reference's CPU-runnable case: 64x64 jittered nodes + exact inflow, PHS r^3,
+    degree 3, k=35, residual viscosity, SSP-RK3 dt=0.2h for 200 steps."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    semi, domain, pts, tags, h = _advection_problem(64)
+    dt, nsteps = 0.2 * h, 200
+    ode = M.semidiscretize(semi, (0.0, nsteps * dt))
+    sol = M.solve(ode, M.SSPRK33(), dt=dt, callback=M.HistoryCallback(approx_order=3))
+    osemi = _oracle_advection(oracle, pts, tags, domain)
+    hist = oracle.History(osemi, 3)
+    u_ref, t_ref = oracle.ssprk33(osemi, ode.u0, 0.0, dt, nsteps, history=hist)
+    assert sol.nsteps == nsteps
+    err = np.abs(sol.u - u_ref).max() / np.abs(u_ref).max()
+    assert err < 1e-10, err
+    exact = W.gaussian_bump(pts, t_ref)
+    # bump width 0.05 = 3.2 h: residual viscosity smears it to ~11 % L2 error at t = 0.625
+    assert np.linalg.norm(sol.u - exact) / np.linalg.norm(exact) < 0.2
+
+
 def test_vortex_rv_trajectory_matches_oracle(oracle, gpu_lib):
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
