@@ -61,8 +61,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
-    ap.add_argument("--only", default="all", choices=["all", "adjoint", "riemann"],
+    ap.add_argument("--only", default="all", choices=["all", "adjoint", "riemann", "weights"],
                     help="run one auxiliary measurement alone")
+    ap.add_argument("--weights-n", type=int, default=1048576,
+                    help="stencils of the batched-weights measurement (0 skips it)")
     ap.add_argument("--riemann-side", type=int, default=1024,
                     help="nodes per side of the Riemann FP32/FP64 measurement (0 skips it)")
     ap.add_argument("--adj-steps", type=int, default=500,
@@ -243,6 +245,79 @@ def run_ensemble(args, local, pg):
                                       "ms_per_step": ms_seq / args.steps},
             "workload": "isentropic vortex members on [-5,5]^2, k=%d, RV + history (order 3), "
                         "FP64, dt=0.2 min(h), one CUDA graph per SSP-RK3 step" % K_STENCIL}
+
+
+def _ragged_stencils(ctx, pts, ks):
+    """GPU KNN with the largest k, each node truncated to its own k (nearest first)."""
+    ctx.set_points(pts)
+    idx, _, _, _ = ctx.knn(int(ks.max()))
+    rp = np.zeros(pts.shape[0] + 1, dtype=np.int64)
+    rp[1:] = np.cumsum(ks)
+    cols = idx[np.arange(idx.shape[1])[None, :] < ks[:, None]].astype(np.int32)
+    return rp, cols
+
+
+def run_weights(args, local):
+    """Batched weight generation: 1,048,576 stencils, 90 % 2D seeded-Halton centres
+    (interior k = 35, boundary band k uniform in 40..60, degree 3) and 10 % 3D Halton
+    (k uniform in 60..90, degree 2), PHS r^3, first derivatives, in one batch
+    (size-bucketed persistent launches).  A seeded sample of nodes is checked against
+    the oracle's per-node solves; the oracle's time on that sample is the CPU figure."""
+    from meshfree_gb300 import _lib as L
+    from meshfree_gb300 import workloads as W
+    from oracle import oracle as O
+    total = args.weights_n
+    n3 = total // 10
+    n2 = total - n3
+    p2 = W.halton_points(n2, 2, seed=31)
+    k2 = W.halton_stencil_sizes(p2, seed=31)
+    p3 = W.halton_points(n3, 3, seed=32)
+    k3 = np.random.default_rng(32).integers(60, 91, n3)
+    ctx2, ctx3 = L.Context(local), L.Context(local)
+    rp2, c2 = _ragged_stencils(ctx2, p2, k2)
+    rp3, c3 = _ragged_stencils(ctx3, p3, k3)
+    pw = W.halton_points(4096, 2, seed=34)                  # warm-up batch
+    rpw, cw = _ragged_stencils(ctx3, pw, np.full(4096, K_STENCIL))
+    ctx3.close()
+    groups = [(p2, rp2, c2, 3, 3, 1), (p3, rp3, c3, 3, 2, 1)]
+    ctx2.weights_batch([(pw, rpw, cw, 3, 3, 1)])
+    ctx2.region_begin()
+    t0 = time.perf_counter()
+    (w2, w3), _ = ctx2.weights_batch(groups)
+    wall = time.perf_counter() - t0
+    dev_ms = ctx2.region_end()
+    ctx2.close()
+    rng = np.random.default_rng(33)
+    s2 = np.sort(rng.choice(n2, 2000, replace=False))
+    s3 = np.sort(rng.choice(n3, 300, replace=False))
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r2 = O.weights_rows(p2, rp2, c2, s2, rbf_pow=3, polydeg=3, nthreads=nthreads)
+    r3 = O.weights_rows(p3, rp3, c3, s3, rbf_pow=3, polydeg=2, nthreads=nthreads)
+    cpu_s = time.perf_counter() - t0
+    m2 = np.zeros(n2, bool)
+    m2[s2] = True
+    m3 = np.zeros(n3, bool)
+    m3[s3] = True
+    e2 = np.repeat(m2, k2)
+    e3 = np.repeat(m3, k3)
+    same = bool(np.array_equal(w2[e2], r2[e2]) and np.array_equal(w3[e3], r3[e3]))
+    rel = max(float(np.abs(w2[e2] - r2[e2]).max() / np.abs(r2[e2]).max()),
+              float(np.abs(w3[e3] - r3[e3]).max() / np.abs(r3[e3]).max()))
+    return {"workload": "%d stencils: %d 2D Halton (k 35 interior, 40-60 boundary band, degree 3) "
+                        "+ %d 3D Halton (k 60-90, degree 2), PHS r^3, first derivatives"
+                        % (total, n2, n3),
+            "systems": total, "max_system": int(max(k2.max() + 10, k3.max() + 10)),
+            "value": total / (dev_ms * 1e-3), "unit": "systems/s",
+            "device_ms": dev_ms, "wall_s": wall,
+            "timing": "device time of the whole batch call on the stream (stencil upload, "
+                      "size-bucketed solves, weight download)",
+            "parity_sample": {"nodes_2d": int(s2.size), "nodes_3d": int(s3.size),
+                              "bit_identical": same, "max_rel_diff": rel},
+            "cpu_sample": {"value": (s2.size + s3.size) / cpu_s, "unit": "systems/s",
+                           "cores": nthreads, "kind": "port",
+                           "sample": "the same %d sampled systems, oracle per-node solves"
+                                     % (s2.size + s3.size)}}
 
 
 def run_riemann(args, local):
@@ -499,7 +574,10 @@ def run_ours(args):
     peaks = load_peaks()
     if args.only != "all":           # one auxiliary measurement alone (profiling runs)
         if rank == 0:
-            leg = run_adjoint(args, local, peaks) if args.only == "adjoint" else run_riemann(args, local)
+            legs = {"adjoint": lambda: run_adjoint(args, local, peaks),
+                    "riemann": lambda: run_riemann(args, local),
+                    "weights": lambda: run_weights(args, local)}
+            leg = legs[args.only]()
             print(json.dumps({args.only: leg}), flush=True)
         return
     n = args.n_side ** 2
@@ -545,6 +623,7 @@ def run_ours(args):
     ens = run_ensemble(args, local, pg) if args.ens_members > 0 else None
     adj = run_adjoint(args, local, peaks) if args.adj_side > 0 and rank == 0 else None
     rie = run_riemann(args, local) if args.riemann_side > 0 and rank == 0 else None
+    wts = run_weights(args, local) if args.weights_n > 0 and rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -577,6 +656,7 @@ def run_ours(args):
         "ensemble": ens,
         "adjoint": adj,
         "riemann": rie,
+        "weights_batch": wts,
     }
     print(json.dumps(line), flush=True)
 

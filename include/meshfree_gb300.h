@@ -108,6 +108,28 @@ mft_status mft_set_stencils(mft_ctx* ctx, const int64_t* rowptr, const int32_t* 
 mft_status mft_weights(mft_ctx* ctx, int op, int rbf_pow, int polydeg, int deriv_order,
                        double* out_w, double* out_max_resid);
 
+/* One group of a weight batch: `n` stencils over the group's own point cloud (host
+ * arrays: xyz n*dim, rowptr n+1 starting at 0, cols rowptr[n] with the centre first,
+ * w rowptr[n]*dim out in stencil order [slot][axis]); PHS r^rbf_pow with polynomials of
+ * degree polydeg, derivatives of order deriv_order along each axis. */
+typedef struct {
+  int dim;
+  int64_t n;
+  const double* xyz;
+  const int64_t* rowptr;
+  const int32_t* cols;
+  int rbf_pow, polydeg, deriv_order;
+  double* w;
+} mft_weight_group;
+
+/* Weights of up to two groups (e.g. a 2D and a 3D cloud, uneven stencil sizes) solved
+ * together in one persistent launch, largest systems first; per-node solves as
+ * compute_flux_operator (compute_operators.jl:409-453, :549-594) performs them, with
+ * the same arithmetic as mft_weights.  max_resid (optional): max over nodes of
+ * ||M w - b||_inf / ||b||_inf.  The context only provides the stream and device. */
+mft_status mft_weights_batch(mft_ctx* ctx, int ngroups, const mft_weight_group* groups,
+                             double* max_resid);
+
 /* Allocation-free weights (no counterpart in the reference).  For callers that cannot
  * allocate device memory during the solve -- code running inside a stream-ordered pool
  * it does not own, or a host whose allocator must not be bypassed by cudaMalloc (which

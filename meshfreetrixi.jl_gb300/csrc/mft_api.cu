@@ -846,6 +846,14 @@ mft_status mft_knn(mft_ctx* c, int k, int32_t* out_idx, double* out_dist, double
   });
 }
 
+mft_status mft_weights_batch(mft_ctx* c, int ngroups, const mft_weight_group* groups,
+                             double* max_resid) {
+  return guarded(c, [&] {
+    set_device(c);
+    weights_batch(c, ngroups, groups, max_resid);
+  });
+}
+
 mft_status mft_weights(mft_ctx* c, int op, int rbf_pow, int polydeg, int deriv_order,
                        double* out_w, double* out_max_resid) {
   return guarded(c, [&] {

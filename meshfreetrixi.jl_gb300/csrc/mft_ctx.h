@@ -173,4 +173,5 @@ void knn_device(mft_ctx* c, int k, std::vector<int32_t>& idx, std::vector<double
                 double* dx_min, double* dx_avg);
 void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
                     std::vector<double>& w_out, double* max_resid);
+void weights_batch(mft_ctx* c, int ngroups, const mft_weight_group* groups, double* max_resid);
 }  // namespace mft

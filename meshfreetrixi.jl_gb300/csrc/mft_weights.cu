@@ -35,20 +35,31 @@ namespace {
 constexpr int kWarpsPerBlock = 2;
 constexpr unsigned kFull = 0xffffffffu;
 
-struct WArgs {
-  int dim, npoly, rbf_pow, order, nmax, kmax;
+// One batch of stencils sharing dimension, basis and derivative order.
+constexpr int kMaxMono = 84;  // monomials of total degree <= 6 in 3D
+struct WGroup {
+  int dim, npoly, rbf_pow, order;
   int periodic;
   double period[3];
-  int64_t nsys;
-  const int64_t* order_list;  // node ids, largest stencil first
   const int64_t* rowptr;
   const int32_t* cols;
   const double* xyz;
-  int mono[128][3];
   double* w_out;  // nnz x dim (stencil order)
   double* resid;  // optional per node
-  int* bad;       // smallest node index with a zero pivot, or INT_MAX
+  int mono[kMaxMono][3];
+};
+
+constexpr int kMaxGroups = 2;
+// Work item codes: group << kGroupShift | node.
+constexpr int kGroupShift = 48;
+
+struct WArgs {
+  int nmax, kmax;
+  int64_t nsys;
+  const int64_t* order_list;  // work item codes, largest stencil first
+  int* bad;                   // smallest node index with a zero pivot, or INT_MAX
   unsigned long long* next;
+  WGroup g[kMaxGroups];
 };
 
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
@@ -144,17 +155,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
   double* TC = X + (size_t)a.kmax * 3;
   double* TC2 = TC + nmax;
   int* ipiv = reinterpret_cast<int*>(TC2 + nmax);
-  const int dim = a.dim;
-
   for (;;) {
     unsigned long long job = 0;
     if (lane == 0) job = atomicAdd(a.next, 1ull);
     job = __shfl_sync(kFull, job, 0);
     if (job >= (unsigned long long)a.nsys) break;
-    const int64_t e = kOrdered ? a.order_list[job] : (int64_t)job;
-    const int64_t rb = a.rowptr[e];
-    const int k = (int)(a.rowptr[e + 1] - rb);
-    const int n = k + a.npoly;
+    const int64_t code = kOrdered ? a.order_list[job] : (int64_t)job;
+    const int grp = (int)(code >> kGroupShift);
+    const int64_t e = code & ((1ll << kGroupShift) - 1);
+    const int dim = a.g[grp].dim, npoly = a.g[grp].npoly;
+    const int rbf_pow = a.g[grp].rbf_pow, order = a.g[grp].order, periodic = a.g[grp].periodic;
+    const int64_t* rowptr = a.g[grp].rowptr;
+    const int32_t* cols = a.g[grp].cols;
+    const double* xyz = a.g[grp].xyz;
+    double* w_out = a.g[grp].w_out;
+    double* resid = a.g[grp].resid;
+    const int64_t rb = rowptr[e];
+    const int k = (int)(rowptr[e + 1] - rb);
+    const int n = k + npoly;
 #define AM(i, j) A[(size_t)((j)-1) * n + ((i)-1)]
 #define BM(i, c) B[(size_t)(c) * n + ((i)-1)]
     if (!kOrdered && k > a.kmax) {
@@ -162,13 +180,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
       if (lane == 0) atomicExch(reinterpret_cast<int*>(a.next + 2), 1);
       continue;
     }
-    const int32_t* st = a.cols + rb;
+    const int32_t* st = cols + rb;
     const int64_t ce = st[0];
     // shift_stencil
     for (int j = lane; j < k; j += 32)
       for (int d = 0; d < dim; ++d) {
-        double t = dsub(a.xyz[(int64_t)st[j] * dim + d], a.xyz[ce * dim + d]);
-        if (a.periodic) t = min_image(t, a.period[d]);
+        double t = dsub(xyz[(int64_t)st[j] * dim + d], xyz[ce * dim + d]);
+        if (periodic) t = min_image(t, a.g[grp].period[d]);
         X[j * 3 + d] = t;
       }
     __syncwarp();
@@ -194,9 +212,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           const double tt = dsub(X[r * 3 + d], X[cidx * 3 + d]);
           d2 = dadd(d2, dmul(tt, tt));
         }
-        v = pow_int(sqrt(d2), a.rbf_pow);
+        v = pow_int(sqrt(d2), rbf_pow);
       } else if (r < k) {
-        const int* ex = a.mono[cidx - k];
+        const int* ex = a.g[grp].mono[cidx - k];
         v = 1.0;
         for (int d = 0; d < dim; ++d) v = dmul(v, pow_int(X[r * 3 + d], ex[d]));
       } else {
@@ -214,13 +232,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           pt[dd] = j == 0 ? 2.220446049250313e-16 : -X[j * 3 + dd];
         double d2 = 0.0;
         for (int dd = 0; dd < dim; ++dd) d2 = dadd(d2, dmul(pt[dd], pt[dd]));
-        v = phs_deriv(a.rbf_pow, a.order, pt[d], sqrt(d2));
+        v = phs_deriv(rbf_pow, order, pt[d], sqrt(d2));
       } else {
-        const int* ex = a.mono[j - k];
+        const int* ex = a.g[grp].mono[j - k];
         bool ok = true;
         for (int dd = 0; dd < dim; ++dd)
-          if (ex[dd] != (dd == d ? a.order : 0)) ok = false;
-        v = ok ? fact(a.order) : 0.0;
+          if (ex[dd] != (dd == d ? order : 0)) ok = false;
+        v = ok ? fact(order) : 0.0;
       }
       B[(size_t)d * n + j] = v;
     }
@@ -346,8 +364,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
 
     if (info != 0) {
       if (lane == 0) atomicMin(a.bad, (int)e);
-      for (int t = lane; t < k * dim; t += 32) a.w_out[(rb + t / dim) * dim + t % dim] = NAN;
-      if (a.resid && lane == 0) a.resid[e] = NAN;
+      for (int t = lane; t < k * dim; t += 32) w_out[(rb + t / dim) * dim + t % dim] = NAN;
+      if (resid && lane == 0) resid[e] = NAN;
       __syncwarp();
       continue;
     }
@@ -429,9 +447,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
     // weights: s_d^order * w[1:k, d]
     for (int t = lane; t < k * dim; t += 32) {
       const int j = t / dim, d = t % dim;
-      a.w_out[(rb + j) * dim + d] = dmul(pow_int(s[d], a.order), BM(j + 1, d));
+      w_out[(rb + j) * dim + d] = dmul(pow_int(s[d], order), BM(j + 1, d));
     }
-    if (a.resid) {
+    if (resid) {
       // ||M w - b||_inf / ||b||_inf per column, M and b re-evaluated from X^
       double worst = 0.0;
       for (int d = 0; d < dim; ++d) {
@@ -447,9 +465,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
                 const double tt = dsub(X[lo * 3 + dd], X[hi * 3 + dd]);
                 d2 = dadd(d2, dmul(tt, tt));
               }
-              v = pow_int(sqrt(d2), a.rbf_pow);
+              v = pow_int(sqrt(d2), rbf_pow);
             } else if (lo < k) {
-              const int* ex = a.mono[hi - k];
+              const int* ex = a.g[grp].mono[hi - k];
               v = 1.0;
               for (int dd = 0; dd < dim; ++dd) v = dmul(v, pow_int(X[lo * 3 + dd], ex[dd]));
             } else {
@@ -463,13 +481,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
             for (int dd = 0; dd < dim; ++dd) pt[dd] = r == 0 ? 2.220446049250313e-16 : -X[r * 3 + dd];
             double d2 = 0.0;
             for (int dd = 0; dd < dim; ++dd) d2 = dadd(d2, dmul(pt[dd], pt[dd]));
-            bv = phs_deriv(a.rbf_pow, a.order, pt[d], sqrt(d2));
+            bv = phs_deriv(rbf_pow, order, pt[d], sqrt(d2));
           } else {
-            const int* ex = a.mono[r - k];
+            const int* ex = a.g[grp].mono[r - k];
             bool ok = true;
             for (int dd = 0; dd < dim; ++dd)
-              if (ex[dd] != (dd == d ? a.order : 0)) ok = false;
-            bv = ok ? fact(a.order) : 0.0;
+              if (ex[dd] != (dd == d ? order : 0)) ok = false;
+            bv = ok ? fact(order) : 0.0;
           }
           rn = fmax(rn, fabs(acc - bv));
           bn = fmax(bn, fabs(bv));
@@ -478,7 +496,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
         bn = warp_max(bn);
         worst = fmax(worst, bn > 0 ? rn / bn : rn);
       }
-      if (lane == 0) a.resid[e] = worst;
+      if (lane == 0) resid[e] = worst;
     }
     __syncwarp();
 #undef AM
@@ -511,83 +529,198 @@ int make_monomials(int dim, int deg, int (*ex)[3], int cap) {
 
 }  // namespace
 
-void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
-                    std::vector<double>& w_out, double* max_resid) {
-  const int dim = c->dim;
-  const int64_t n = c->n;
+// Host description of one group of a weight batch (host arrays).
+struct HostGroup {
+  int dim, rbf_pow, polydeg, order;
+  const double* period;  // dim lengths or null
+  int64_t n;
+  const double* d_xyz;   // device coordinates (n x dim)
+  const int64_t* rowptr; // host, n + 1
+  const int32_t* cols;   // host, rowptr[n]
+  double* w_out;         // host, rowptr[n] x dim
+};
+
+// All groups' systems, largest first, in persistent launches over size buckets of the
+// system order n = k + monomials (one launch per non-empty bucket, each with the shared
+// memory and occupancy its largest system allows).
+constexpr int kBucketEdges[] = {48, 64, 80, 104};
+
+static void weights_run(cudaStream_t s, const std::vector<HostGroup>& gs, double* max_resid) {
+  MFT_REQUIRE(!gs.empty() && gs.size() <= (size_t)kMaxGroups, MFT_ERR_ARG,
+              "between 1 and 2 weight groups");
   WArgs a{};
-  a.dim = dim;
-  a.npoly = make_monomials(dim, polydeg, a.mono, 128);
-  MFT_REQUIRE(a.npoly <= 128, MFT_ERR_ARG, "polynomial degree too high");
-  a.rbf_pow = rbf_pow;
-  a.order = deriv_order;
-  a.periodic = c->periodic ? 1 : 0;
-  for (int d = 0; d < 3; ++d) a.period[d] = c->period[d];
-  std::vector<int64_t> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
-    return (c->st_rp[x + 1] - c->st_rp[x]) > (c->st_rp[y + 1] - c->st_rp[y]);
-  });
-  int kmax = 0;
-  for (int64_t i = 0; i < n; ++i) kmax = std::max<int>(kmax, (int)(c->st_rp[i + 1] - c->st_rp[i]));
-  a.kmax = kmax;
-  a.nmax = kmax + a.npoly;
-  const size_t shmem = weights_smem_doubles(a.nmax, kmax) * sizeof(double) * kWarpsPerBlock;
-  MFT_REQUIRE(shmem <= 227 * 1024, MFT_ERR_ARG, "stencil too large for the weight kernel");
-  cudaStream_t s = c->stream;
-  DBuf<int64_t> d_order, d_rp;
-  DBuf<int32_t> d_ci;
-  DBuf<double> d_w, d_res;
+  int kmax = 0, nmax = 0;
+  int64_t nsys = 0;
+  std::vector<int64_t> order;
+  std::vector<int> ks, ns;
+  for (size_t g = 0; g < gs.size(); ++g) {
+    const HostGroup& h = gs[g];
+    WGroup& G = a.g[g];
+    G.dim = h.dim;
+    G.npoly = make_monomials(h.dim, h.polydeg, G.mono, kMaxMono);
+    MFT_REQUIRE(G.npoly <= kMaxMono, MFT_ERR_ARG, "polynomial degree too high");
+    G.rbf_pow = h.rbf_pow;
+    G.order = h.order;
+    G.periodic = h.period ? 1 : 0;
+    for (int d = 0; d < 3; ++d) G.period[d] = (h.period && d < h.dim) ? h.period[d] : 0.0;
+    int km = 0;
+    for (int64_t i = 0; i < h.n; ++i) {
+      const int k = (int)(h.rowptr[i + 1] - h.rowptr[i]);
+      MFT_REQUIRE(k >= 1, MFT_ERR_ARG, "empty stencil");
+      km = std::max(km, k);
+      order.push_back(((int64_t)g << kGroupShift) | i);
+      ks.push_back(k);
+      ns.push_back(k + G.npoly);
+    }
+    kmax = std::max(kmax, km);
+    nmax = std::max(nmax, km + G.npoly);
+    nsys += h.n;
+  }
+  std::vector<int64_t> perm(order.size());
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](int64_t x, int64_t y) { return ns[x] > ns[y]; });
+  std::vector<int64_t> order_sorted(order.size());
+  for (size_t q = 0; q < perm.size(); ++q) order_sorted[q] = order[perm[q]];
+  (void)kmax;
+  MFT_REQUIRE(weights_smem_doubles(nmax, nmax) * sizeof(double) * kWarpsPerBlock <= 227 * 1024,
+              MFT_ERR_ARG, "stencil too large for the weight kernel");
+  // buckets: [begin, end) ranges of the sorted list with their largest n and k
+  struct Bucket { int64_t begin, end; int nmax, kmax; };
+  std::vector<Bucket> buckets;
+  auto bucket_of = [](int n) {
+    int b = 0;
+    for (int edge : kBucketEdges) { if (n <= edge) return b; ++b; }
+    return b;
+  };
+  for (size_t q = 0; q < perm.size(); ++q) {
+    const int n = ns[perm[q]], k = ks[perm[q]];
+    if (buckets.empty() || bucket_of(n) != bucket_of(buckets.back().nmax))
+      buckets.push_back({(int64_t)q, (int64_t)q, n, k});
+    Bucket& b = buckets.back();
+    b.end = (int64_t)q + 1;
+    b.kmax = std::max(b.kmax, k);
+  }
+  DBuf<int64_t> d_order, d_rp[kMaxGroups];
+  DBuf<int32_t> d_ci[kMaxGroups];
+  DBuf<double> d_w[kMaxGroups], d_res[kMaxGroups];
   DBuf<int> d_bad;
   DBuf<unsigned long long> d_next;
-  d_order.upload(order, s);
-  d_rp.upload(c->st_rp, s);
-  d_ci.upload(c->st_ci, s);
-  const int64_t nnz = (int64_t)c->st_ci.size();
-  d_w.alloc((size_t)nnz * dim);
-  if (max_resid) d_res.alloc(n);
+  d_order.upload(order_sorted, s);
+  for (size_t g = 0; g < gs.size(); ++g) {
+    const HostGroup& h = gs[g];
+    const int64_t nnz = h.rowptr[h.n];
+    d_rp[g].upload(h.rowptr, h.n + 1, s);
+    d_ci[g].upload(h.cols, nnz, s);
+    d_w[g].alloc((size_t)nnz * h.dim);
+    if (max_resid) d_res[g].alloc(h.n);
+    a.g[g].rowptr = d_rp[g].p;
+    a.g[g].cols = d_ci[g].p;
+    a.g[g].xyz = h.d_xyz;
+    a.g[g].w_out = d_w[g].p;
+    a.g[g].resid = max_resid ? d_res[g].p : nullptr;
+  }
   d_bad.alloc(1);
   const int big = 0x7fffffff;
   MFT_CUDA(cudaMemcpyAsync(d_bad.p, &big, sizeof(int), cudaMemcpyHostToDevice, s));
-  d_next.alloc(1);
+  d_next.alloc(buckets.size());
   d_next.zero(s);
-  a.nsys = n;
-  a.order_list = d_order.p;
-  a.rowptr = d_rp.p;
-  a.cols = d_ci.p;
-  a.xyz = c->d_xyz.p;
-  a.w_out = d_w.p;
-  a.resid = max_resid ? d_res.p : nullptr;
   a.bad = d_bad.p;
-  a.next = d_next.p;
-  MFT_CUDA(cudaFuncSetAttribute(k_weights<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0;
   MFT_CUDA(cudaGetDevice(&dev));
   MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<true>, 32 * kWarpsPerBlock, shmem));
-  per_sm = std::max(per_sm, 1);
-  const int64_t want = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
-  k_weights<true><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
-  MFT_LAUNCH_CHECK();
-  w_out.resize((size_t)nnz * dim);
-  int bad = big;
-  MFT_CUDA(cudaMemcpyAsync(w_out.data(), d_w.p, w_out.size() * sizeof(double),
-                           cudaMemcpyDeviceToHost, s));
-  MFT_CUDA(cudaMemcpyAsync(&bad, d_bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  std::vector<double> res;
-  if (max_resid) {
-    res.resize(n);
-    MFT_CUDA(cudaMemcpyAsync(res.data(), d_res.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MFT_CUDA(cudaFuncSetAttribute(k_weights<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                227 * 1024));
+  for (size_t b = 0; b < buckets.size(); ++b) {
+    const Bucket& bk = buckets[b];
+    WArgs ab = a;
+    ab.nmax = bk.nmax;
+    ab.kmax = bk.kmax;
+    ab.nsys = bk.end - bk.begin;
+    ab.order_list = d_order.p + bk.begin;
+    ab.next = d_next.p + b;
+    const size_t shmem = weights_smem_doubles(bk.nmax, bk.kmax) * sizeof(double) * kWarpsPerBlock;
+    int per_sm = 0;
+    MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<true>,
+                                                           32 * kWarpsPerBlock, shmem));
+    per_sm = std::max(per_sm, 1);
+    const int64_t want = (ab.nsys + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const unsigned grid =
+        (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
+    k_weights<true><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(ab);
+    MFT_LAUNCH_CHECK();
   }
+  int bad = big;
+  std::vector<std::vector<double>> res(gs.size());
+  for (size_t g = 0; g < gs.size(); ++g) {
+    const HostGroup& h = gs[g];
+    MFT_CUDA(cudaMemcpyAsync(h.w_out, d_w[g].p, (size_t)h.rowptr[h.n] * h.dim * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+    if (max_resid) {
+      res[g].resize(h.n);
+      MFT_CUDA(cudaMemcpyAsync(res[g].data(), d_res[g].p, h.n * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    }
+  }
+  MFT_CUDA(cudaMemcpyAsync(&bad, d_bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   MFT_CUDA(cudaStreamSynchronize(s));
   MFT_REQUIRE(bad == big, MFT_ERR_SINGULAR,
               "saddle-point system of node " + std::to_string(bad) + " has an exactly zero pivot");
   if (max_resid) {
     double m = 0.0;
-    for (double r : res) m = std::max(m, r);
+    for (auto& r : res)
+      for (double x : r) m = std::max(m, x);
     *max_resid = m;
   }
+}
+
+void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
+                    std::vector<double>& w_out, double* max_resid) {
+  HostGroup h{};
+  h.dim = c->dim;
+  h.rbf_pow = rbf_pow;
+  h.polydeg = polydeg;
+  h.order = deriv_order;
+  h.period = c->periodic ? c->period : nullptr;
+  h.n = c->n;
+  h.d_xyz = c->d_xyz.p;
+  h.rowptr = c->st_rp.data();
+  h.cols = c->st_ci.data();
+  w_out.resize((size_t)c->st_ci.size() * c->dim);
+  h.w_out = w_out.data();
+  weights_run(c->stream, {h}, max_resid);
+}
+
+void weights_batch(mft_ctx* c, int ngroups, const mft_weight_group* groups, double* max_resid) {
+  MFT_REQUIRE(ngroups >= 1 && ngroups <= kMaxGroups && groups, MFT_ERR_ARG,
+              "between 1 and 2 weight groups");
+  std::vector<HostGroup> hs(ngroups);
+  std::vector<DBuf<double>> xyz(ngroups);
+  for (int g = 0; g < ngroups; ++g) {
+    const mft_weight_group& q = groups[g];
+    MFT_REQUIRE(q.dim >= 1 && q.dim <= 3 && q.n >= 1 && q.xyz && q.rowptr && q.cols && q.w,
+                MFT_ERR_ARG, "bad weight group");
+    MFT_REQUIRE(q.rbf_pow >= 1 && q.polydeg >= 0 && q.polydeg <= 6 && q.deriv_order >= 1 &&
+                    q.deriv_order <= 8, MFT_ERR_ARG, "bad basis or derivative order");
+    MFT_REQUIRE(q.rowptr[0] == 0, MFT_ERR_ARG, "rowptr[0] must be 0");
+    for (int64_t i = 0; i < q.n; ++i) {
+      MFT_REQUIRE(q.rowptr[i + 1] > q.rowptr[i], MFT_ERR_ARG, "empty stencil");
+      for (int64_t p = q.rowptr[i]; p < q.rowptr[i + 1]; ++p)
+        MFT_REQUIRE(q.cols[p] >= 0 && q.cols[p] < q.n, MFT_ERR_ARG, "stencil index out of range");
+    }
+    xyz[g].upload(q.xyz, (size_t)q.n * q.dim, c->stream);
+    HostGroup& h = hs[g];
+    h.dim = q.dim;
+    h.rbf_pow = q.rbf_pow;
+    h.polydeg = q.polydeg;
+    h.order = q.deriv_order;
+    h.period = nullptr;
+    h.n = q.n;
+    h.d_xyz = xyz[g].p;
+    h.rowptr = q.rowptr;
+    h.cols = q.cols;
+    h.w_out = q.w;
+  }
+  weights_run(c->stream, hs, max_resid);
 }
 
 }  // namespace mft
@@ -637,20 +770,21 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
     return MFT_ERR_ARG;
   }
   WArgs a{};
-  a.dim = dim;
-  a.npoly = make_monomials(dim, polydeg, a.mono, 128);
-  a.rbf_pow = rbf_pow;
-  a.order = deriv_order;
-  a.periodic = period ? 1 : 0;
-  for (int d = 0; d < 3; ++d) a.period[d] = (period && d < dim) ? period[d] : 0.0;
+  WGroup& G = a.g[0];
+  G.dim = dim;
+  G.npoly = make_monomials(dim, polydeg, G.mono, kMaxMono);
+  G.rbf_pow = rbf_pow;
+  G.order = deriv_order;
+  G.periodic = period ? 1 : 0;
+  for (int d = 0; d < 3; ++d) G.period[d] = (period && d < dim) ? period[d] : 0.0;
   a.kmax = kmax;
-  a.nmax = kmax + a.npoly;
+  a.nmax = kmax + G.npoly;
   const size_t shmem = weights_smem_doubles(a.nmax, kmax) * sizeof(double) * kWarpsPerBlock;
   const size_t kMaxShmem = 227 * 1024;
-  if (a.npoly > 128 || shmem > kMaxShmem) {
+  if (G.npoly > kMaxMono || shmem > kMaxShmem) {
     put_err(err, err_len,
             "mft_weights_noalloc: stencil size " + std::to_string(kmax) + " plus " +
-                std::to_string(a.npoly) + " monomials needs " + std::to_string(shmem) +
+                std::to_string(G.npoly) + " monomials needs " + std::to_string(shmem) +
                 " bytes of shared memory; the maximum is " + std::to_string(kMaxShmem) +
                 " (kmax + monomials <= 116)");
     return MFT_ERR_ARG;
@@ -686,11 +820,11 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   }
   a.nsys = n;
   a.order_list = nullptr;
-  a.rowptr = rowptr;
-  a.cols = cols;
-  a.xyz = xyz;
-  a.w_out = w;
-  a.resid = nullptr;
+  G.rowptr = rowptr;
+  G.cols = cols;
+  G.xyz = xyz;
+  G.w_out = w;
+  G.resid = nullptr;
   a.bad = reinterpret_cast<int*>(scratch + 1);
   a.next = scratch;
   int sms = 0, per_sm = 0;

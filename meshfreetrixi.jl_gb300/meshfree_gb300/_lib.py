@@ -59,6 +59,7 @@ SIGNATURES = {
     "mft_ssprk33": (I32, [VP, DBL, I32, I32]),
     "mft_ssprk33_host": (I32, [VP, VP, I32, C.POINTER(DBL), DBL, I32]),
     "mft_set_rv_state": (I32, [VP, VP, I32, I32]),
+    "mft_weights_batch": (I32, [VP, I32, VP, VP]),
     "mft_set_limiter": (I32, [VP, I32, VP, VP]),
     "mft_limit": (I32, [VP, VP, I32]),
     "mft_rhs_adjoint": (I32, [VP, VP, VP, VP, I32, DBL]),
@@ -105,6 +106,13 @@ def _p(a):
 
 def _ptrs(arrs):
     return (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+class WeightGroup(C.Structure):
+    """mft_weight_group (include/meshfree_gb300.h)."""
+    _fields_ = [("dim", C.c_int), ("n", C.c_int64), ("xyz", C.c_void_p), ("rowptr", C.c_void_p),
+                ("cols", C.c_void_p), ("rbf_pow", C.c_int), ("polydeg", C.c_int),
+                ("deriv_order", C.c_int), ("w", C.c_void_p)]
 
 
 class Context:
@@ -251,6 +259,25 @@ class Context:
         self.check(self.lib.mft_ssprk33_host(self.h, _ptrs(list(u)), u.shape[0], C.byref(tt),
                                              dt, nsteps))
         return tt.value
+
+    def weights_batch(self, groups, want_resid=False):
+        """groups: [(xyz (n, dim), rowptr (n+1), cols, rbf_pow, polydeg, deriv_order)], at most
+        two, solved in one batch.  Returns ([w (nnz, dim) per group], max_resid or None)."""
+        keep, outs = [], []
+        arr = (WeightGroup * len(groups))()
+        for g, (xyz, rp, ci, p, deg, order) in enumerate(groups):
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+            rp = np.ascontiguousarray(rp, dtype=np.int64)
+            ci = np.ascontiguousarray(ci, dtype=np.int32)
+            w = np.empty((int(rp[-1]), xyz.shape[1]))
+            keep += [xyz, rp, ci]
+            outs.append(w)
+            arr[g] = WeightGroup(xyz.shape[1], xyz.shape[0], xyz.ctypes.data, rp.ctypes.data,
+                                 ci.ctypes.data, p, deg, order, w.ctypes.data)
+        res = C.c_double()
+        self.check(self.lib.mft_weights_batch(self.h, len(groups), arr,
+                                              C.byref(res) if want_resid else None))
+        return outs, (res.value if want_resid else None)
 
     # positivity limiter ------------------------------------------------------
     def set_limiter(self, kinds, thresholds):

@@ -576,15 +576,37 @@ int mfto_saddle_system(int dim, const double* x, const double* period, const int
   return nn_;
 }
 
+static int weights_impl(int dim, int64_t n, const double* x, const double* period,
+                        const int64_t* rowptr, const int32_t* stencil, int rbf_pow, int polydeg,
+                        int deriv_order, double* w, double* resid, int nthreads,
+                        int64_t nrows, const int64_t* rows);
+
 int mfto_weights(int dim, int64_t n, const double* x, const double* period, const int64_t* rowptr,
                  const int32_t* stencil, int rbf_pow, int polydeg, int deriv_order, double* w,
                  double* resid, int nthreads) {
+  return weights_impl(dim, n, x, period, rowptr, stencil, rbf_pow, polydeg, deriv_order, w,
+                      resid, nthreads, n, NULL);
+}
+
+int mfto_weights_rows(int dim, int64_t n, const double* x, const double* period,
+                      const int64_t* rowptr, const int32_t* stencil, int rbf_pow, int polydeg,
+                      int deriv_order, double* w, int nthreads, int64_t nrows,
+                      const int64_t* rows) {
+  return weights_impl(dim, n, x, period, rowptr, stencil, rbf_pow, polydeg, deriv_order, w,
+                      NULL, nthreads, nrows, rows);
+}
+
+static int weights_impl(int dim, int64_t n, const double* x, const double* period,
+                        const int64_t* rowptr, const int32_t* stencil, int rbf_pow, int polydeg,
+                        int deriv_order, double* w, double* resid, int nthreads,
+                        int64_t nrows, const int64_t* rows) {
   if (dim < 1 || dim > 3 || deriv_order < 1) return -1;
   int ex[256][3];
   int npoly = make_monomials(dim, polydeg, ex);
   if (npoly != binom(polydeg + dim, dim)) return -1;
   int kmax = 0;
-  for (int64_t e = 0; e < n; ++e) {
+  for (int64_t q = 0; q < nrows; ++q) {
+    int64_t e = rows ? rows[q] : q;
     int k = (int)(rowptr[e + 1] - rowptr[e]);
     if (k > kmax) kmax = k;
   }
@@ -599,7 +621,8 @@ int mfto_weights(int dim, int64_t n, const double* x, const double* period, cons
     double* xh = (double*)malloc((size_t)kmax * 3 * sizeof(double));
     int* ipiv = (int*)malloc((size_t)nmax * sizeof(int));
 #pragma omp for schedule(dynamic, 64)
-    for (int64_t e = 0; e < n; ++e) {
+    for (int64_t q = 0; q < nrows; ++q) {
+      const int64_t e = rows ? rows[q] : q;
       int k = (int)(rowptr[e + 1] - rowptr[e]);
       const int32_t* st = stencil + rowptr[e];
       int nn_ = k + npoly;
@@ -975,6 +998,89 @@ static int visc_source(const mfto_semi* s, int kind, double* const* du, double* 
 }
 
 /* Trixi.rhs!  rbfsolver.jl:397-428 */
+/* SourceIGR  src/sources/IGR.jl:17-239 (Cao & Schafer 2023): solve
+ *   (rho^-1 - alpha (Dx rho^-1 Dx + Dy rho^-1 Dy)) sigma = alpha (tr(Du)^2 + tr(Du^2))
+ * by unpreconditioned conjugate gradients from sigma = 0 with at most igr_maxiter
+ * iterations and relative tolerance sqrt(eps) (the reference names IterativeSolvers'
+ * cg; its call cg(sigma, A, b; maxiter = 20) matches no method of that package, so the
+ * in-place cg!(sigma, A, b; maxiter = 20) it intends is restated: Hestenes-Stiefel CG
+ * in IterativeSolvers' CGIterable order), then du[rho v1] -= Dx sigma,
+ * du[rho v2] -= Dy sigma.  tr(Du) is formed as the reference writes it,
+ * Dx(rho) + Dy(v1) (update_igr_rhs!, :143-145), and tr(Du^2) =
+ * (Dx v1)^2 + 2 (Dy v1)(Dx v2) + (Dy v2)^2 (:151-153). */
+static double dot_seq(int64_t n, const double* a, const double* b) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s = s + a[i] * b[i];
+  return s;
+}
+
+/* y = (rho^-1 - alpha (Dx rho^-1 Dx + Dy rho^-1 Dy)) v  (IGRCompositeMatrix mul!, :59-73) */
+static void igr_apply(const mfto_semi* s, const double* rinv, const double* v, double* y,
+                      double* t1, double* t2, double* t3, int nthreads) {
+  int64_t n = s->n;
+  mfto_spmv(&s->dop[0], v, t1, nthreads);
+  mfto_spmv(&s->dop[1], v, t2, nthreads);
+  for (int64_t i = 0; i < n; ++i) { t1[i] = rinv[i] * t1[i]; t2[i] = rinv[i] * t2[i]; }
+  mfto_spmv(&s->dop[0], t1, t3, nthreads);
+  mfto_spmv(&s->dop[1], t2, t1, nthreads);
+  for (int64_t i = 0; i < n; ++i) {
+    y[i] = rinv[i] * v[i];
+    y[i] = y[i] - s->igr_alpha * (t3[i] + t1[i]);
+  }
+}
+
+static int igr_source(const mfto_semi* s, double* const* du, double* const* u, int nthreads) {
+  if (s->eq != MFTO_EQ_EULER2D || s->dim != 2) return -1;
+  int64_t n = s->n;
+  double* w = (double*)calloc((size_t)n * 16, sizeof(double));
+  if (!w) return -2;
+  double *rho = w, *v1 = w + n, *v2 = w + 2 * n, *rinv = w + 3 * n, *b = w + 4 * n;
+  double *dxr = w + 5 * n, *dxv1 = w + 6 * n, *dxv2 = w + 7 * n, *dyv1 = w + 8 * n,
+         *dyv2 = w + 9 * n;
+  double *x = w + 10 * n, *r = w + 11 * n, *cu = w + 12 * n, *cc = w + 13 * n;
+  double *t1 = dxr, *t2 = dxv1, *t3 = dxv2; /* reused once b is formed */
+  for (int64_t i = 0; i < n; ++i) {
+    rho[i] = u[0][i];
+    v1[i] = u[1][i] / u[0][i];
+    v2[i] = u[2][i] / u[0][i];
+  }
+  mfto_spmv(&s->dop[0], rho, dxr, nthreads);
+  mfto_spmv(&s->dop[0], v1, dxv1, nthreads);
+  mfto_spmv(&s->dop[0], v2, dxv2, nthreads);
+  mfto_spmv(&s->dop[1], v1, dyv1, nthreads);
+  mfto_spmv(&s->dop[1], v2, dyv2, nthreads);
+  for (int64_t i = 0; i < n; ++i) {
+    double tr = 0.0;
+    tr = tr + dxr[i];
+    tr = tr + dyv1[i];
+    double tsq = dxv1[i] * dxv1[i] + 2.0 * dyv1[i] * dxv2[i] + dyv2[i] * dyv2[i];
+    b[i] = s->igr_alpha * (tr * tr + tsq);
+    rinv[i] = 1.0 / u[0][i];
+  }
+  /* cg!: x = 0, r = b - A x = b, u = 0 */
+  for (int64_t i = 0; i < n; ++i) { x[i] = 0.0; r[i] = b[i]; cu[i] = 0.0; }
+  double res = sqrt(dot_seq(n, r, r));
+  double prev = 1.0;
+  const double tol = res * sqrt(JL_EPS);
+  for (int it = 0; it < s->igr_maxiter && !(res <= tol); ++it) {
+    double beta = (res * res) / (prev * prev);
+    for (int64_t i = 0; i < n; ++i) cu[i] = r[i] + beta * cu[i];
+    igr_apply(s, rinv, cu, cc, t1, t2, t3, nthreads);
+    double alpha = (res * res) / dot_seq(n, cu, cc);
+    for (int64_t i = 0; i < n; ++i) {
+      x[i] = x[i] + alpha * cu[i];
+      r[i] = r[i] - alpha * cc[i];
+    }
+    prev = res;
+    res = sqrt(dot_seq(n, r, r));
+  }
+  if (s->igr_sigma) memcpy(s->igr_sigma, x, (size_t)n * sizeof(double));
+  mfto_spmv_accum(&s->dop[0], -1.0, x, du[1], nthreads);
+  mfto_spmv_accum(&s->dop[1], -1.0, x, du[2], nthreads);
+  free(w);
+  return 0;
+}
+
 int mfto_rhs(const mfto_semi* s, double t, const double* dirichlet, double* const* du,
              double* const* u, double* eps_out, mfto_rv_diag* diag, int nthreads) {
   (void)t;
@@ -990,6 +1096,9 @@ int mfto_rhs(const mfto_semi* s, double t, const double* dirichlet, double* cons
       if (rc) return rc;
     } else if (kind == MFTO_SRC_HV_TOMINEC || kind == MFTO_SRC_HV_FLYER) {
       for (int v = 0; v < V; ++v) mfto_spmv_accum(&s->hv, -s->hv_gamma, u[v], du[v], nthreads);
+    } else if (kind == MFTO_SRC_IGR) {
+      rc = igr_source(s, du, u, nthreads);
+      if (rc) return rc;
     } else {
       return -1;
     }

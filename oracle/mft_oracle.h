@@ -53,6 +53,13 @@ int mfto_weights(int dim, int64_t n, const double* x, const double* period,
                  const int64_t* rowptr, const int32_t* stencil, int rbf_pow, int polydeg,
                  int deriv_order, double* w, double* resid, int nthreads);
 
+/* mfto_weights restricted to the listed rows (nrows node indices in rows); only
+ * those rows' entries of w are written. */
+int mfto_weights_rows(int dim, int64_t n, const double* x, const double* period,
+                      const int64_t* rowptr, const int32_t* stencil, int rbf_pow, int polydeg,
+                      int deriv_order, double* w, int nthreads, int64_t nrows,
+                      const int64_t* rows);
+
 /* Node e's saddle-point system as mfto_weights builds it: full symmetric M
  * (n x n), rhs b (n x dim), both column-major, and the axis scales s (dim).
  * Returns n = k + number of monomials. */
@@ -69,7 +76,8 @@ int mfto_bk_solve(int n, double* a, int nrhs, double* b);
 /* Equation kinds and boundary-condition kinds. */
 enum { MFTO_EQ_EULER2D = 0, MFTO_EQ_ADVECTION = 1 };
 enum { MFTO_BC_DIRICHLET = 0, MFTO_BC_SLIP_WALL = 1, MFTO_BC_DO_NOTHING = 2 };
-enum { MFTO_SRC_RV = 0, MFTO_SRC_UPWIND = 1, MFTO_SRC_HV_TOMINEC = 2, MFTO_SRC_HV_FLYER = 3 };
+enum { MFTO_SRC_RV = 0, MFTO_SRC_UPWIND = 1, MFTO_SRC_HV_TOMINEC = 2, MFTO_SRC_HV_FLYER = 3,
+       MFTO_SRC_IGR = 4 };
 
 /* Compressed sparse rows with ascending columns (CSR), plus the same operator
  * stored by columns (CSC) for transposed products. */
@@ -107,6 +115,10 @@ typedef struct {
   /* hyperviscosity: materialised operator H (CSR only) and its scale */
   mfto_csr hv;
   double hv_gamma;
+  /* information geometric regularisation (SourceIGR): alpha and CG iteration cap */
+  double igr_alpha;
+  int igr_maxiter;
+  double* igr_sigma; /* optional n output: sigma of the last evaluation */
 } mfto_semi;
 
 /* Diagnostics of the last residual-viscosity evaluation (optional output). */

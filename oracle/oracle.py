@@ -24,7 +24,7 @@ F64P = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 EQ_EULER2D, EQ_ADVECTION = 0, 1
 BC_DIRICHLET, BC_SLIP_WALL, BC_DO_NOTHING = 0, 1, 2
-SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER = 0, 1, 2, 3
+SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER, SRC_IGR = 0, 1, 2, 3, 4
 
 
 class _Csr(C.Structure):
@@ -41,7 +41,8 @@ class _Semi(C.Structure):
                 ("c_rv", C.c_double), ("c_uw", C.c_double), ("h", C.c_double),
                 ("success_iter", C.c_int), ("approx_du", C.c_void_p),
                 ("mean_mode", C.c_int), ("max_mode", C.c_int),
-                ("hv", _Csr), ("hv_gamma", C.c_double)]
+                ("hv", _Csr), ("hv_gamma", C.c_double),
+                ("igr_alpha", C.c_double), ("igr_maxiter", C.c_int), ("igr_sigma", C.c_void_p)]
 
 
 class _Diag(C.Structure):
@@ -61,6 +62,9 @@ def lib():
         L.mfto_weights.restype = C.c_int
         L.mfto_weights.argtypes = [C.c_int, C.c_int64, F64P, C.c_void_p, I64P, I32P, C.c_int,
                                    C.c_int, C.c_int, F64P, C.c_void_p, C.c_int]
+        L.mfto_weights_rows.restype = C.c_int
+        L.mfto_weights_rows.argtypes = [C.c_int, C.c_int64, F64P, C.c_void_p, I64P, I32P, C.c_int,
+                                        C.c_int, C.c_int, F64P, C.c_int, C.c_int64, I64P]
         L.mfto_saddle_system.restype = C.c_int
         L.mfto_saddle_system.argtypes = [C.c_int, F64P, C.c_void_p, I64P, I32P, C.c_int, C.c_int,
                                          C.c_int, C.c_int64, F64P, F64P, F64P]
@@ -136,6 +140,23 @@ def weights(points, rowptr, stencil, rbf_pow=3, polydeg=3, deriv_order=1, period
     if rc:
         raise RuntimeError("mfto_weights: singular system at node %d" % (-rc - 1))
     return (w, resid) if want_resid else w
+
+
+def weights_rows(points, rowptr, stencil, rows, rbf_pow=3, polydeg=3, deriv_order=1,
+                 period=None, nthreads=8):
+    """weights() for the listed rows only; other rows' entries are NaN."""
+    x = np.ascontiguousarray(points, dtype=np.float64)
+    n, dim = x.shape
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    stencil = np.ascontiguousarray(stencil, dtype=np.int32)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    w = np.full((int(rowptr[-1]), dim), np.nan)
+    per = None if period is None else np.ascontiguousarray(period, dtype=np.float64)
+    rc = lib().mfto_weights_rows(dim, n, x, _ptr(per), rowptr, stencil, rbf_pow, polydeg,
+                                 deriv_order, w, nthreads, rows.size, rows)
+    if rc:
+        raise RuntimeError("mfto_weights_rows: singular system at node %d" % (-rc - 1))
+    return w
 
 
 def saddle_system(points, rowptr, stencil, e, rbf_pow=3, polydeg=3, deriv_order=1, period=None):
@@ -290,7 +311,8 @@ class Semi:
     value_fn) in NamedTuple order; value_fn(x (m,dim), t) -> (m, nvars)."""
 
     def __init__(self, points, ops, eq="euler", gamma=1.4, adv=(1.0, 0.5), bcs=(), sources=(),
-                 c_rv=1.0, c_uw=1.0, h=1.0, hv=None, hv_gamma=0.0, mean_mode=0, max_mode=0):
+                 c_rv=1.0, c_uw=1.0, h=1.0, hv=None, hv_gamma=0.0, mean_mode=0, max_mode=0,
+                 igr_alpha=1.0, igr_maxiter=20):
         self.points = np.ascontiguousarray(points, dtype=np.float64)
         self.n, self.dim = self.points.shape
         self.ops = list(ops)
@@ -331,6 +353,10 @@ class Semi:
         if hv is not None:
             s.hv = hv.cstruct()
         s.hv_gamma = hv_gamma
+        s.igr_alpha = igr_alpha
+        s.igr_maxiter = igr_maxiter
+        self.igr_sigma = np.zeros(self.n)
+        s.igr_sigma = self.igr_sigma.ctypes.data
         self.s = s
 
     def dirichlet_values(self, t):
