@@ -50,7 +50,8 @@ enum { MFT_EQ_EULER2D = 0, MFT_EQ_ADVECTION = 1 };
 enum { MFT_BC_DIRICHLET = 0, MFT_BC_SLIP_WALL = 1, MFT_BC_DO_NOTHING = 2 };
 
 /* Source kinds (src/sources/hyperviscosity.jl). */
-enum { MFT_SRC_RV = 0, MFT_SRC_UPWIND = 1, MFT_SRC_HV_TOMINEC = 2, MFT_SRC_HV_FLYER = 3 };
+enum { MFT_SRC_RV = 0, MFT_SRC_UPWIND = 1, MFT_SRC_HV_TOMINEC = 2, MFT_SRC_HV_FLYER = 3,
+       MFT_SRC_IGR = 4 };
 
 /* Operator slots. MFT_OP_GRAD holds D_1..D_dim (compute_flux_operator(solver, domain));
  * MFT_OP_LAP holds sum_d D_d^(2) (Tominec HV builds lap'*lap from it);
@@ -187,6 +188,10 @@ mft_status mft_set_dirichlet_callback(mft_ctx* ctx, mft_dirichlet_fn fn, void* u
  *   MFT_SRC_UPWIND  {c_uw, h = dx_avg, 0, 0}             SourceUpwindViscosityTominec
  *   MFT_SRC_HV_TOMINEC {gamma = c*dx_min^4.5, 0, 0, 0}   SourceHyperviscosityTominec
  *   MFT_SRC_HV_FLYER   {gamma = c*dx_min^(2k), 0, 0, 0}  SourceHyperviscosityFlyer
+ *   MFT_SRC_IGR     {alpha, max CG iterations (20), 0, 0}  SourceIGR (src/sources/IGR.jl):
+ *                   (rho^-1 - alpha (Dx rho^-1 Dx + Dy rho^-1 Dy)) sigma =
+ *                   alpha (tr(Du)^2 + tr(Du^2)) by conjugate gradients from 0 (relative
+ *                   tolerance sqrt(eps)), then du[rho v] -= (Dx sigma, Dy sigma); 2D Euler
  * mean_mode 0: ode_mean divides by n*nvars (Trixi recursive_length); 1: by n. */
 mft_status mft_set_sources(mft_ctx* ctx, int n_src, const int* kinds, const double* params);
 
@@ -308,7 +313,8 @@ mft_status mft_ssprk33_adjoint_device(mft_ctx* ctx, double* lam);
 /* Kernel kinds reported by mft_profile_get. */
 enum {
   MFT_K_BC = 0, MFT_K_FLUX, MFT_K_FWD, MFT_K_MEAN, MFT_K_LEXMAX, MFT_K_EPS, MFT_K_REV,
-  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_ADJ, MFT_K_LIMITER, MFT_K_COUNT
+  MFT_K_REV_LAP, MFT_K_HISTORY, MFT_K_LAYOUT, MFT_K_ADJ, MFT_K_LIMITER, MFT_K_IGR,
+  MFT_K_COUNT
 };
 
 /* enable != 0 starts recording an event pair around every kernel launch (and clears

@@ -428,6 +428,22 @@ static void check_kernel_errors(mft_ctx* c) {
   }
 }
 
+// Work buffers of the IGR source.
+static void ensure_igr(mft_ctx* c) {
+  const size_t n = (size_t)c->n;
+  c->igr_prim.alloc(n * 3);
+  for (auto* b : {&c->igr_rinv, &c->igr_x, &c->igr_r, &c->igr_u0, &c->igr_u1, &c->igr_c})
+    b->alloc(n);
+  c->igr_t.alloc(n * 2);
+  c->igr_add.alloc(n * 2);
+  c->igr_partial.alloc((n + kBlockHost - 1) / kBlockHost + 1);
+  if (!c->igr_counter.p) {
+    c->igr_counter.alloc(1);
+    c->igr_counter.zero(c->stream);
+  }
+  c->igr_sc.alloc(1);
+}
+
 void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_in) {
   ensure_device_ops(c);
   ensure_bcs(c);
@@ -450,13 +466,16 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     launch_bc_pass1(c->nb, c->d_bnode.p, V, c->eq, bc, us, us32, s);
   }
 
-  // sources: at most one viscosity source and one hyperviscosity source
-  int iv = -1, ih = -1;
+  // sources: at most one viscosity source, one hyperviscosity source and one IGR source
+  int iv = -1, ih = -1, ig = -1;
   for (size_t k = 0; k < c->src_kind.size(); ++k) {
     const int kind = c->src_kind[k];
     if (kind == MFT_SRC_RV || kind == MFT_SRC_UPWIND) {
       MFT_REQUIRE(iv < 0, MFT_ERR_UNSUPPORTED, "more than one viscosity source");
       iv = (int)k;
+    } else if (kind == MFT_SRC_IGR) {
+      MFT_REQUIRE(ig < 0, MFT_ERR_UNSUPPORTED, "more than one IGR source");
+      ig = (int)k;
     } else {
       MFT_REQUIRE(ih < 0, MFT_ERR_UNSUPPORTED, "more than one hyperviscosity source");
       ih = (int)k;
@@ -468,6 +487,37 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   const double hv_gamma = ih >= 0 ? c->src_par[ih * 4] : 0.0;
   if (tominec) MFT_REQUIRE(c->have_val[kSlotLap], MFT_ERR_STATE, "Tominec HV needs MFT_OP_LAP");
   if (flyer) MFT_REQUIRE(c->have_val[kSlotHv], MFT_ERR_STATE, "Flyer HV needs MFT_OP_HV");
+
+  // IGR: sigma from the BC-corrected state, added to the momentum rows in the epilogue
+  if (ig >= 0) {
+    MFT_REQUIRE(c->eq == MFT_EQ_EULER2D && c->dim == 2, MFT_ERR_UNSUPPORTED,
+                "the IGR source needs the 2D Euler equations");
+    ensure_igr(c);
+    IgrArgs ia{};
+    ia.n = n;
+    ia.ell = c->fwd.view();
+    ia.wx = c->fw[0].p;
+    ia.wy = c->fw[1].p;
+    ia.alpha = c->src_par[ig * 4];
+    ia.maxiter = (int)c->src_par[ig * 4 + 1];
+    ia.prim = c->igr_prim.p;
+    ia.rinv = c->igr_rinv.p;
+    ia.x = c->igr_x.p;
+    ia.r = c->igr_r.p;
+    ia.u0 = c->igr_u0.p;
+    ia.u1 = c->igr_u1.p;
+    ia.c = c->igr_c.p;
+    ia.t = c->igr_t.p;
+    ia.add = c->igr_add.p;
+    ia.partial = c->igr_partial.p;
+    ia.counter = c->igr_counter.p;
+    ia.sc = c->igr_sc.p;
+    {
+      ProfScope ps(c, MFT_K_IGR);
+      launch_igr(ia, us, s);
+    }
+    ep.xadd = c->igr_add.p;
+  }
 
   // 2. flux per node (FP64 Euler)
   if (!f32 && c->eq == MFT_EQ_EULER2D) {
@@ -1010,9 +1060,14 @@ mft_status mft_set_sources(mft_ctx* c, int n_src, const int* kinds, const double
     c->graph_valid = false;
     MFT_REQUIRE(n_src >= 0 && n_src <= 8, MFT_ERR_ARG, "n_src out of range");
     MFT_REQUIRE(n_src == 0 || (kinds && params), MFT_ERR_ARG, "NULL source arrays");
-    for (int k = 0; k < n_src; ++k)
-      MFT_REQUIRE(kinds[k] >= MFT_SRC_RV && kinds[k] <= MFT_SRC_HV_FLYER, MFT_ERR_ARG,
+    for (int k = 0; k < n_src; ++k) {
+      MFT_REQUIRE(kinds[k] >= MFT_SRC_RV && kinds[k] <= MFT_SRC_IGR, MFT_ERR_ARG,
                   "unknown source kind");
+      if (kinds[k] == MFT_SRC_IGR)
+        MFT_REQUIRE(params[4 * k + 1] >= 0 && params[4 * k + 1] <= 1000 &&
+                        isfinite(params[4 * k]), MFT_ERR_ARG,
+                    "IGR parameters: finite alpha and 0..1000 CG iterations");
+    }
     c->src_kind.assign(kinds, kinds + n_src);
     c->src_par.assign(params, params + 4 * n_src);
     c->fsal_valid = false;
@@ -1483,7 +1538,7 @@ mft_status mft_profile_get(mft_ctx* c, int kind, double* total_ms, int64_t* laun
                            const char** name) {
   static const char* names[MFT_K_COUNT] = {"bc_pass1", "flux", "fwd_gather", "mean",
                                            "lexmax", "eps", "rev_gather", "rev_lap",
-                                           "history", "layout", "adjoint", "limiter"};
+                                           "history", "layout", "adjoint", "limiter", "igr"};
   return guarded(c, [&] {
     MFT_REQUIRE(kind >= 0 && kind < MFT_K_COUNT, MFT_ERR_ARG, "bad kernel kind");
     set_device(c);
@@ -1583,6 +1638,8 @@ int adj_hv_mode(mft_ctx* c, double* gamma) {
     MFT_REQUIRE(kind != MFT_SRC_RV && kind != MFT_SRC_UPWIND, MFT_ERR_UNSUPPORTED,
                 "adjoint: residual/upwind viscosity has no adjoint (its viscosity is a "
                 "maximum over the field)");
+    MFT_REQUIRE(kind != MFT_SRC_IGR, MFT_ERR_UNSUPPORTED,
+                "adjoint: the IGR source (an iterative solve) has no adjoint");
     MFT_REQUIRE(mode == 0, MFT_ERR_UNSUPPORTED, "more than one hyperviscosity source");
     mode = kind == MFT_SRC_HV_TOMINEC ? 1 : 2;
     *gamma = c->src_par[k * 4];

@@ -13,6 +13,8 @@
 constexpr int kSlotLap = 3;
 constexpr int kSlotHv = 4;
 constexpr int kSlots = 5;
+// Threads per block of the node-parallel kernels (sizes the per-block reduction partials).
+constexpr int kBlockHost = 128;
 // Blocks per ensemble member in the segmented reductions.
 constexpr int kSegBlocks = 8;
 
@@ -115,6 +117,12 @@ struct mft_ctx {
   mft::DBuf<int> d_seg_id;
   mft::DBuf<double> d_seg_h, seg_partial, seg_mean, seg_norms;
   mft::DBuf<unsigned> seg_counter;
+
+  // IGR source work buffers and CG scalars
+  mft::DBuf<double> igr_prim, igr_rinv, igr_x, igr_r, igr_u0, igr_u1, igr_c, igr_t, igr_add,
+      igr_partial;
+  mft::DBuf<unsigned> igr_counter;
+  mft::DBuf<mft::IgrScalars> igr_sc;
 
   // Zhang-Shu positivity limiter after every SSP-RK3 stage (variables in order)
   int lim_n = 0;

@@ -70,6 +70,12 @@ static __device__ __forceinline__ void slip(const double* nrm, double* uu) {
 // BC pass 2 on du (and u at slip walls), then the stage epilogue.
 template <int V>
 static __device__ __forceinline__ void finish_node(const Epilogue& ep, int64_t i, double* du) {
+  if constexpr (V == 4) {
+    if (ep.xadd) {
+      du[1] = dadd(du[1], ep.xadd[i * 2]);
+      du[2] = dadd(du[2], ep.xadd[i * 2 + 1]);
+    }
+  }
   double us[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) us[v] = ep.u_s[i * V + v];

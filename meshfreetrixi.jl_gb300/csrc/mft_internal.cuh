@@ -113,6 +113,7 @@ struct Epilogue {
   float* out32;       // optional FP32 shadow of the next stage state
   BcDev bc;
   int has_bc;
+  const double* xadd; // n x 2 additions to the momentum rows (IGR source) or null
 };
 
 // ------------------------------------------------------------------ launchers
@@ -262,6 +263,34 @@ void launch_bc_project(int64_t nb, const int32_t* bnode, int V, BcDev bc, double
 // loc is n x 4 scratch.
 void launch_zs_limiter(int64_t n, EllView ell, int variable, double threshold, double gamma,
                        double* u, float* u32, double* loc, cudaStream_t s);
+
+// IGR source (mft_igr.cu): conjugate-gradient scalars kept in device memory.
+struct IgrScalars {
+  double res, prev, tol, alpha_cg, beta;
+  int iter, done;
+};
+struct IgrArgs {
+  int64_t n;
+  EllView ell;          // forward layout
+  const double* wx;     // D_x, D_y on the forward layout
+  const double* wy;
+  double alpha;
+  int maxiter;
+  double* prim;         // n x 3 (rho, v1, v2)
+  double* rinv;         // n
+  double* x;            // n: sigma
+  double* r;            // n
+  double* u0;           // n: CG directions, alternating
+  double* u1;
+  double* c;            // n
+  double* t;            // n x 2
+  double* add;          // n x 2 output: -(Dx sigma), -(Dy sigma)
+  double* partial;      // one double per block
+  unsigned* counter;
+  IgrScalars* sc;
+};
+// Full IGR pipeline on the Euler state u (n x 4 AoS): prim, right-hand side, CG, flux.
+void launch_igr(const IgrArgs& a, const double* u, cudaStream_t s);
 
 // Sets *flag to 1 when a and b differ in any of `count` doubles (bitwise).
 void launch_differs(const double* a, const double* b, int64_t count, int* flag, cudaStream_t s);

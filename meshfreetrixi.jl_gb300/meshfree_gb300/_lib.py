@@ -18,7 +18,7 @@ MFT_OK, MFT_ERR_ARG, MFT_ERR_CUDA, MFT_ERR_STATE, MFT_ERR_SINGULAR = 0, 1, 2, 3,
 MFT_ERR_NONFINITE, MFT_ERR_TIMEOUT, MFT_ERR_UNSUPPORTED, MFT_ERR_NOMEM = 5, 6, 7, 8
 EQ_EULER2D, EQ_ADVECTION = 0, 1
 BC_DIRICHLET, BC_SLIP_WALL, BC_DO_NOTHING = 0, 1, 2
-SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER = 0, 1, 2, 3
+SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER, SRC_IGR = 0, 1, 2, 3, 4
 OP_GRAD, OP_LAP, OP_HV = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 LIM_DENSITY, LIM_PRESSURE = 0, 1
@@ -73,7 +73,7 @@ SIGNATURES = {
     "mft_region": (I32, [VP, I32, C.POINTER(DBL)]),
 }
 K_NAMES = ["bc_pass1", "flux", "fwd_gather", "mean", "lexmax", "eps", "rev_gather", "rev_lap",
-           "history", "layout", "adjoint", "limiter"]
+           "history", "layout", "adjoint", "limiter", "igr"]
 
 _lib = None
 

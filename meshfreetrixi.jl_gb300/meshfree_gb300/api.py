@@ -315,6 +315,22 @@ class SourceHyperviscosityTominec:
 
 
 @dataclass
+class SourceIGR:
+    """SourceIGR(solver, equations, domain; alpha) (src/sources/IGR.jl:17-32): information
+    geometric regularisation; sigma from a conjugate-gradient solve (at most `maxiter`
+    iterations) of (rho^-1 - alpha (Dx rho^-1 Dx + Dy rho^-1 Dy)) sigma =
+    alpha (tr(Du)^2 + tr(Du^2)), then du[rho v] -= (Dx sigma, Dy sigma)."""
+    solver: RBFSolver
+    equations: object
+    domain: PointCloudDomain
+    alpha: float = 1.0
+    maxiter: int = 20
+
+    def spec(self):
+        return L.SRC_IGR, [self.alpha, float(self.maxiter), 0.0, 0.0]
+
+
+@dataclass
 class SourceHyperviscosityFlyer:
     """gamma = c * dx_min^(2k); operator sum_d D_d^(2k) (:34-50)."""
     solver: RBFSolver
