@@ -1279,6 +1279,8 @@ float* shadow(mft_ctx* c, int k) {
 // Stage limiter: one Zhang-Shu pass per configured variable on stage state u.
 void apply_limiter(mft_ctx* c, double* u, float* u32) {
   if (c->lim_n == 0) return;
+  MFT_REQUIRE(c->eq == MFT_EQ_EULER2D && c->nvars == 4, MFT_ERR_UNSUPPORTED,
+              "the positivity limiter needs the 2D Euler equations");
   c->lim_buf.alloc((size_t)c->n * 4);
   for (int q = 0; q < c->lim_n; ++q) {
     ProfScope ps(c, MFT_K_LIMITER);
@@ -1489,7 +1491,7 @@ mft_status mft_ssprk33_host(mft_ctx* c, double* const* u, int nvars, double* t, 
     c->t_state = *t;
     c->state_valid = true;
     if (!keep) c->fsal_valid = false;
-    ssprk33_run(c, dt, nsteps);
+    ssprk33_run(c, dt, nsteps, true);
     launch_soa_from_aos(c->U[0].p, c->soa.p, n, nvars, s);
     for (int v = 0; v < nvars; ++v)
       MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
