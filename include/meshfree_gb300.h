@@ -139,7 +139,7 @@ mft_status mft_weights_batch(mft_ctx* ctx, int ngroups, const mft_weight_group* 
  * memory (xyz n*dim, rowptr n+1, cols rowptr[n] with centre first, w rowptr[n]*dim in
  * stencil order [slot][axis]); period is a host array of dim lengths or NULL; stream
  * may be 0.  kmax: the caller's bound on the stencil size; kmax + number of monomials
- * must be <= 116 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  A
+ * must be <= 161 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  A
  * stencil longer than kmax is skipped and reported as MFT_ERR_ARG.  The only global
  * scratch is a 32-byte static device array per GPU; its address is looked up on the
  * first call on each device (make that call before any stream capture), and it is

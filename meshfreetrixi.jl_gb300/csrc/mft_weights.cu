@@ -132,10 +132,13 @@ __device__ __forceinline__ void tri_next(int& i, int& j, int step) {
   while (i > j) { i -= j + 1; ++j; }
 }
 
-// Doubles of shared memory one warp of k_weights uses: A (nmax^2), B (3 nmax),
-// X (3 kmax), two column-multiplier arrays (2 nmax) and the pivot ints (nmax).
+// Doubles of shared memory one warp of k_weights uses: the upper triangle of A packed by
+// columns (nmax (nmax + 1) / 2; Bunch-Kaufman in upper storage reads and writes only
+// i <= j), B (3 nmax), X (3 kmax), two column-multiplier arrays (2 nmax) and the pivot
+// ints (nmax).
 __host__ __device__ __forceinline__ size_t weights_smem_doubles(int nmax, int kmax) {
-  return (size_t)nmax * nmax + (size_t)nmax * 3 + (size_t)kmax * 3 + (size_t)nmax * 2 + nmax;
+  return (size_t)nmax * (nmax + 1) / 2 + (size_t)nmax * 3 + (size_t)kmax * 3 +
+         (size_t)nmax * 2 + nmax;
 }
 
 // kOrdered: systems are taken in the order of a.order_list (largest first); otherwise
@@ -146,11 +149,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int nmax = a.nmax;
-  // per-warp shared layout: A[nmax*nmax], B[nmax*3], X[kmax*3], TC[nmax], TC2[nmax],
+  // per-warp shared layout: A[nmax(nmax+1)/2] (upper, packed), B[nmax*3], X[kmax*3],
+  // TC[nmax], TC2[nmax],
   // ipiv[nmax] (ints)
   const size_t per = weights_smem_doubles(nmax, a.kmax);
   double* A = smem + per * wib;
-  double* B = A + (size_t)nmax * nmax;
+  double* B = A + (size_t)nmax * (nmax + 1) / 2;
   double* X = B + (size_t)nmax * 3;
   double* TC = X + (size_t)a.kmax * 3;
   double* TC2 = TC + nmax;
@@ -173,7 +177,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
     const int64_t rb = rowptr[e];
     const int k = (int)(rowptr[e + 1] - rb);
     const int n = k + npoly;
-#define AM(i, j) A[(size_t)((j)-1) * n + ((i)-1)]
+// upper-packed element (i, j), 1 <= i <= j: column j starts at j (j - 1) / 2
+#define AM(i, j) A[(((j) * ((j)-1)) >> 1) + ((i)-1)]
 #define BM(i, c) B[(size_t)(c) * n + ((i)-1)]
     if (!kOrdered && k > a.kmax) {
       // caller-declared maximum stencil size exceeded: flag it and skip the system
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
       } else {
         v = 0.0;
       }
-      A[(size_t)cidx * n + r] = v;
+      A[((cidx * (cidx + 1)) >> 1) + r] = v;
     }
     // right-hand sides
     for (int t = lane; t < n * dim; t += 32) {
@@ -786,7 +791,7 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
             "mft_weights_noalloc: stencil size " + std::to_string(kmax) + " plus " +
                 std::to_string(G.npoly) + " monomials needs " + std::to_string(shmem) +
                 " bytes of shared memory; the maximum is " + std::to_string(kMaxShmem) +
-                " (kmax + monomials <= 116)");
+                " (kmax + monomials <= 161)");
     return MFT_ERR_ARG;
   }
   int dev = 0;
