@@ -32,7 +32,7 @@ namespace mft {
 
 namespace {
 
-constexpr int kWarpsPerBlock = 1;
+constexpr int kWarpsPerBlock = 2;
 constexpr unsigned kFull = 0xffffffffu;
 
 // One batch of stencils sharing dimension, basis and derivative order.
@@ -144,7 +144,7 @@ __host__ __device__ __forceinline__ size_t weights_smem_doubles(int nmax, int km
 // kOrdered: systems are taken in the order of a.order_list (largest first); otherwise
 // in node order.
 template <bool kOrdered>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 16) k_weights(WArgs a) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -318,36 +318,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 16) k_weights(WArgs a) {
           // for x_j != 0, one fused multiply-add per element
           for (int j = lane; j < kk - 1; j += 32) TC[j] = dmul(-r1, AM(j + 1, kk));
           __syncwarp();
-          // element t of the leading (kk-1) triangle is A[t] (packed); four elements per
-          // lane and pass for independent loads in flight
           const int Tu = (kk - 1) * kk / 2;
-          const double* colk = &AM(1, kk);
-          int iq[4], jq[4];
-          iq[0] = 0;
-          jq[0] = 0;
-          tri_next(iq[0], jq[0], lane);
-#pragma unroll
-          for (int q = 1; q < 4; ++q) {
-            iq[q] = iq[q - 1];
-            jq[q] = jq[q - 1];
-            tri_next(iq[q], jq[q], 32);
-          }
-          for (int t = lane; t < Tu; t += 128) {
-            double av[4], xv[4], cv[4], sv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              if (t + 32 * q < Tu) {
-                av[q] = A[t + 32 * q];
-                xv[q] = colk[iq[q]];
-                cv[q] = TC[jq[q]];
-                sv[q] = colk[jq[q]];
-              }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (t + 32 * q < Tu && sv[q] != 0.0) A[t + 32 * q] = fma(xv[q], cv[q], av[q]);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) tri_next(iq[q], jq[q], 128);
+          int i0 = 0, j0 = 0;
+          tri_next(i0, j0, lane);
+          for (int t = lane; t < Tu; t += 32, tri_next(i0, j0, 32)) {
+            if (AM(j0 + 1, kk) != 0.0)
+              AM(i0 + 1, j0 + 1) = fma(AM(i0 + 1, kk), TC[j0], AM(i0 + 1, j0 + 1));
           }
           __syncwarp();
           for (int i = 1 + lane; i < kk; i += 32) AM(i, kk) = dmul(r1, AM(i, kk));
@@ -369,35 +345,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 16) k_weights(WArgs a) {
           }
           __syncwarp();
           const int Tu = (kk - 2) * (kk - 1) / 2;
-          const double* colk = &AM(1, kk);
-          const double* colk1 = &AM(1, kk - 1);
-          int iq[4], jq[4];
-          iq[0] = 0;
-          jq[0] = 0;
-          tri_next(iq[0], jq[0], lane);
-#pragma unroll
-          for (int q = 1; q < 4; ++q) {
-            iq[q] = iq[q - 1];
-            jq[q] = jq[q - 1];
-            tri_next(iq[q], jq[q], 32);
-          }
-          for (int t = lane; t < Tu; t += 128) {
-            double av[4], x1[4], x2[4], c1[4], c2[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              if (t + 32 * q < Tu) {
-                av[q] = A[t + 32 * q];
-                x1[q] = colk1[iq[q]];
-                x2[q] = colk[iq[q]];
-                c1[q] = TC[jq[q]];
-                c2[q] = TC2[jq[q]];
-              }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (t + 32 * q < Tu) A[t + 32 * q] = fma(-x1[q], c1[q], fma(-x2[q], c2[q], av[q]));
-#pragma unroll
-            for (int q = 0; q < 4; ++q) tri_next(iq[q], jq[q], 128);
+          int i0 = 0, j0 = 0;
+          tri_next(i0, j0, lane);
+          for (int t = lane; t < Tu; t += 32, tri_next(i0, j0, 32)) {
+            const int j = j0 + 1, i = i0 + 1;
+            AM(i, j) = fma(-AM(i, kk - 1), TC[j0], fma(-AM(i, kk), TC2[j0], AM(i, j)));
           }
           __syncwarp();
           for (int j = lane; j < kk - 2; j += 32) {

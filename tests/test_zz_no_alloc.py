@@ -58,7 +58,7 @@ def test_noalloc_rejects_oversized_stencils(gpu_lib):
     ci = torch.zeros(1000, dtype=torch.int32, device=dev)
     w = torch.empty(2000, dtype=torch.float64, device=dev)
     err = C.create_string_buffer(512)
-    rc = f(2, 200, pts.data_ptr(), None, rp.data_ptr(), ci.data_ptr(), 200, 3, 3, 1, w.data_ptr(),
+    rc = f(2, 200, pts.data_ptr(), None, rp.data_ptr(), ci.data_ptr(), 400, 3, 3, 1, w.data_ptr(),
            None, err, len(err))
     assert rc == L.MFT_ERR_ARG
     assert b"maximum" in err.value
