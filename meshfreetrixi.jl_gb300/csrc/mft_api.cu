@@ -488,6 +488,42 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   if (tominec) MFT_REQUIRE(c->have_val[kSlotLap], MFT_ERR_STATE, "Tominec HV needs MFT_OP_LAP");
   if (flyer) MFT_REQUIRE(c->have_val[kSlotHv], MFT_ERR_STATE, "Flyer HV needs MFT_OP_HV");
 
+  // Residual-viscosity normalisation (ode_mean, ode_maximum of u): it only reads the
+  // BC-corrected state, so outside profiling it runs on a side stream while the flux and
+  // forward gather kernels (FP64-bound, they leave memory and issue slots free) run here;
+  // the viscosity kernel waits for it.
+  auto rv_norms = [&](cudaStream_t st) {
+    const int mode = (int)c->src_par[iv * 4 + 3];
+    if (c->nseg > 0) {
+      {
+        ProfScope ps(c, MFT_K_MEAN);
+        launch_mean_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, mode, c->seg_partial.p,
+                        c->seg_counter.p, c->seg_mean.p, st);
+      }
+      ProfScope ps(c, MFT_K_LEXMAX);
+      launch_lexmax_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, c->seg_mean.p, mode,
+                        c->seg_partial.p, c->seg_counter.p + c->nseg, c->seg_norms.p, st);
+    } else {
+      const double denom = mode == 0 ? (double)n * V : (double)n;
+      {
+        ProfScope ps(c, MFT_K_MEAN);
+        launch_mean(n, V, us, denom, c->red_partial.p, c->red_counter.p, c->mean.p,
+                    c->red_blocks, st);
+      }
+      ProfScope ps(c, MFT_K_LEXMAX);
+      launch_lexmax(n, V, us, c->mean.p, mode, c->red_partial.p, c->red_counter.p + 1,
+                    c->norms.p, c->red_blocks, st);
+    }
+  };
+  bool forked = false;
+  if (iv >= 0 && c->src_kind[iv] == MFT_SRC_RV && !c->prof_on) {
+    MFT_CUDA(cudaEventRecord(c->ev_fork, s));
+    MFT_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+    rv_norms(c->stream2);
+    MFT_CUDA(cudaEventRecord(c->ev_join, c->stream2));
+    forked = true;
+  }
+
   // IGR: sigma from the BC-corrected state, added to the momentum rows in the epilogue
   if (ig >= 0) {
     MFT_REQUIRE(c->eq == MFT_EQ_EULER2D && c->dim == 2, MFT_ERR_UNSUPPORTED,
@@ -602,27 +638,8 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   if (iv >= 0) {
     const int kind = c->src_kind[iv];
     const double* par = &c->src_par[iv * 4];
-    const int mode = kind == MFT_SRC_RV ? (int)par[3] : 0;
-    if (kind == MFT_SRC_RV && c->nseg > 0) {
-      {
-        ProfScope ps(c, MFT_K_MEAN);
-        launch_mean_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, mode, c->seg_partial.p,
-                        c->seg_counter.p, c->seg_mean.p, s);
-      }
-      ProfScope ps(c, MFT_K_LEXMAX);
-      launch_lexmax_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, c->seg_mean.p, mode,
-                        c->seg_partial.p, c->seg_counter.p + c->nseg, c->seg_norms.p, s);
-    } else if (kind == MFT_SRC_RV) {
-      const double denom = mode == 0 ? (double)n * V : (double)n;
-      {
-        ProfScope ps(c, MFT_K_MEAN);
-        launch_mean(n, V, us, denom, c->red_partial.p, c->red_counter.p, c->mean.p,
-                    c->red_blocks, s);
-      }
-      ProfScope ps(c, MFT_K_LEXMAX);
-      launch_lexmax(n, V, us, c->mean.p, mode, c->red_partial.p, c->red_counter.p + 1,
-                    c->norms.p, c->red_blocks, s);
-    }
+    if (forked) MFT_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+    else if (kind == MFT_SRC_RV) rv_norms(s);
     EpsArgs ea{};
     ea.n = n;
     ea.eq = c->eq;
@@ -793,7 +810,13 @@ mft_status mft_ctx_create(mft_ctx** out, int device, int flags) {
     return e != cudaSuccess ? MFT_ERR_CUDA : MFT_ERR_ARG;
   }
   if (cudaSetDevice(device) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     delete c;
     return MFT_ERR_CUDA;
   }
@@ -808,6 +831,12 @@ mft_status mft_ctx_destroy(mft_ctx* c) {
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
   }
+  if (c->stream2) {
+    cudaStreamSynchronize(c->stream2);
+    cudaStreamDestroy(c->stream2);
+  }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   for (auto& p : c->prof_pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);

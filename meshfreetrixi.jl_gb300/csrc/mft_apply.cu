@@ -734,23 +734,62 @@ struct RingPtrs {
   double* p[8];
 };
 
+// Ring slot k of the history (constant-offset parameter loads, no local copy).
+__device__ __forceinline__ double* ring_slot(const RingPtrs& r, int k) {
+  switch (k) {
+    case 0: return r.p[0];
+    case 1: return r.p[1];
+    case 2: return r.p[2];
+    case 3: return r.p[3];
+    case 4: return r.p[4];
+    case 5: return r.p[5];
+    case 6: return r.p[6];
+    default: return r.p[7];
+  }
+}
+
 // HistoryCallback push inside a captured step: the step's parameters come from the
 // step table at the device step counter.  ring[head] = u_new, then
 // approx_du = sum_{k<m} w_k ring[(head + k) % slots] (k = 0 is u_new itself).
+// Two values per thread (16-byte loads and stores); count is even or the last thread
+// takes the single remaining value.
 __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, RingPtrs ring,
                               int slots, const StepParams* __restrict__ tab,
                               const int* __restrict__ ctr, double* __restrict__ out) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = 2 * j;
   if (i >= count) return;
-  const StepParams& sp = tab[*ctr];
-  const double un = u_new[i];
-  ring.p[sp.head][i] = un;
-  double acc = 0.0;
-  for (int k = 0; k < sp.m; ++k) {
-    const double hk = k == 0 ? un : ring.p[(sp.head + k) % slots][i];
-    acc = dadd(acc, dmul(sp.w[k], hk));
+  const StepParams* sp = tab + *ctr;
+  const int m = sp->m, head = sp->head;
+  double* dst = ring_slot(ring, head);
+  if (i + 1 < count) {
+    const double2 un = reinterpret_cast<const double2*>(u_new)[j];
+    reinterpret_cast<double2*>(dst)[j] = un;
+    double ax = 0.0, ay = 0.0;
+    for (int k = 0; k < m; ++k) {
+      double2 hk = un;
+      if (k > 0) {
+        int q = head + k;
+        if (q >= slots) q -= slots;
+        hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
+      }
+      const double wk = sp->w[k];
+      ax = dadd(ax, dmul(wk, hk.x));
+      ay = dadd(ay, dmul(wk, hk.y));
+    }
+    reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
+  } else {
+    const double un = u_new[i];
+    dst[i] = un;
+    double acc = 0.0;
+    for (int k = 0; k < m; ++k) {
+      int q = head + k;
+      if (q >= slots) q -= slots;
+      const double hk = k == 0 ? un : ring_slot(ring, q)[i];
+      acc = dadd(acc, dmul(sp->w[k], hk));
+    }
+    out[i] = acc;
   }
-  out[i] = acc;
 }
 
 __global__ void k_step_advance(int* ctr) {
@@ -765,8 +804,8 @@ void launch_history_dev(int64_t count, const double* u_new, const double* const*
   if (count <= 0) return;
   RingPtrs rp{};
   for (int k = 0; k < slots && k < 8; ++k) rp.p[k] = const_cast<double*>(ring[k]);
-  k_history_dev<<<grid_for(count, 256), 256, 0, s>>>(count, u_new, rp, slots, tab, ctr,
-                                                      approx_du);
+  k_history_dev<<<grid_for((count + 1) / 2, 256), 256, 0, s>>>(count, u_new, rp, slots, tab,
+                                                                ctr, approx_du);
   MFT_LAUNCH_CHECK();
 }
 

@@ -145,6 +145,10 @@ struct mft_ctx {
   mft::DBuf<mft::StepParams> d_tab;
   mft::DBuf<int> d_ctr;
 
+  // side stream for the residual-viscosity reductions (overlap with the gathers)
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+
   // timing
   bool prof_on = false;
   std::vector<cudaEvent_t> ev_pool;
