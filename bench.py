@@ -472,6 +472,27 @@ def run_adjoint(args, local, peaks):
                        "fp64_gfma_s": 8 * K_STENCIL * n / (per_launch * 1e-3) / 1e9 if launches else None}}
 
 
+# Whole-rhs! algorithmic bytes per node (2D Euler, V=4, k=35, int32 indices), the
+# formula of the scope table: plain fused rhs! (u read, D_x/D_y weights, indices, du
+# write) + the fused SSP-RK stage combination (u_n read) + the residual-viscosity
+# passes (D^T weights and indices, t = D u written and read, approx_du, eps).
+PATH_BYTES = {
+    "fp64": {"formula": "764 plain + 32 stage + 876 RV", "bytes": 764 + 32 + 876},
+    "fp32": {"formula": "452 plain + 32 stage (FP64 u_n) + 532 RV (FP32 weights/t)",
+             "bytes": 452 + 32 + (280 + 140 + 64 + 32 + 16)},
+}
+SPEC_HBM_GBS = 8000.0    # the nominal HBM figure the scope table quotes beside the measured one
+
+
+def path_roofline(node_rhs_per_s, prec, peaks):
+    """HBM roofline of the whole rhs! from the end-to-end node-RHS rate."""
+    b = PATH_BYTES[prec]
+    achieved = b["bytes"] * node_rhs_per_s / 1e9
+    return {"bytes_per_node_rhs": b["bytes"], "formula": b["formula"], "achieved_gbs": achieved,
+            "frac_of_measured": achieved / peaks["hbm_gbs"],
+            "frac_of_8tbs": achieved / SPEC_HBM_GBS}
+
+
 def roofline(prof, n, prec, peaks):
     name = max(prof, key=lambda k: prof[k][0])
     ms, launches = prof[name]
@@ -653,6 +674,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_dict(n, "fp64"),
         "roofline": roof,
+        "path_roofline": path_roofline(value, "fp64", peaks),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * n * 8,
                 "d2h_bytes_per_step": 4 * n * 8, "entry_point": "mft_ssprk33_host"},
@@ -664,6 +686,7 @@ def run_ours(args):
         "fp32_apply": {"value": value32, "unit": UNIT, "speedup_vs_fp64": value32 / value,
                        "l2_density_err_vs_fp64": l2, "linf_density_err_vs_fp64": linf,
                        "steps": args.steps, "roofline": roof32,
+                       "path_roofline": path_roofline(value32, "fp32", peaks),
                        "autotuned_mapping": mapping,
                        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
         "ensemble": ens,
