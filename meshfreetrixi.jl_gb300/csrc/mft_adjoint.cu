@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_f64(AdjArgs a) {
 #pragma unroll
       for (int v = 0; v < V; ++v) {
         o[v] = c3 * li[v] + cr * r[v];
-        a.acc[i * V + v] = li[v] / 3.0;
+        a.acc[i * V + v] = div3(li[v]);
       }
     } else if (a.kind == kAdjStage2) {
       const double cr = 0.25 * a.dt;
