@@ -1,0 +1,102 @@
+"""Size-independent properties at the benchmark's full size (N = 262,144 nodes, k = 35,
+GPU KNN and weights), where the oracle would take minutes:
+  * polynomial reproduction: a constant Euler state is steady (|du| <= 1e-9 max|F|/h);
+  * linearity of the advection rhs! (no viscosity source): f(a u + b v) = a f(u) + b f(v);
+  * the adjoint identity <lam, J v> = <J^T lam, v> against a centred difference of the
+    GPU's own rhs!;
+  * FP32-apply vs FP64 rhs! on the vortex: relative L2 difference <= 1e-5;
+  * graph-replayed and directly launched SSP-RK3 steps agree bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SIDE = 512
+
+
+@pytest.fixture(scope="module")
+def vortex_domain():
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(SIDE)
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    return M, W, solver, dom, pts, h
+
+
+def test_constant_state_is_steady(vortex_domain):
+    M, W, solver, dom, pts, h = vortex_domain
+    eq = M.CompressibleEulerEquations2D(1.4)
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t), solver)
+    u = np.ascontiguousarray(np.tile(np.array([[1.2], [0.3], [-0.4], [2.9]]), (1, pts.shape[0])))
+    du = np.empty_like(u)
+    M.rhs_(du, u.copy(), semi, 0.0)
+    assert np.abs(du).max() <= 1e-9 * 3.0 / h
+
+
+def test_advection_rhs_is_linear(vortex_domain):
+    M, W, solver, dom, pts, h = vortex_domain
+    eq = M.LinearScalarAdvectionEquation2D((1.0, 0.5))
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.gaussian_bump(x, t), solver)
+    g = np.random.default_rng(1)
+    u = np.ascontiguousarray(np.sin(pts[:, 0])[None, :] + 0.1 * g.standard_normal((1, pts.shape[0])))
+    v = np.ascontiguousarray(np.cos(pts[:, 1])[None, :])
+    a, b = 0.7, -1.3
+    fu, fv, fw = np.empty_like(u), np.empty_like(u), np.empty_like(u)
+    M.rhs_(fu, u.copy(), semi, 0.0)
+    M.rhs_(fv, v.copy(), semi, 0.0)
+    M.rhs_(fw, np.ascontiguousarray(a * u + b * v), semi, 0.0)
+    scale = np.abs(fu).max() + np.abs(fv).max()
+    assert np.abs(fw - (a * fu + b * fv)).max() <= 1e-12 * scale
+
+
+def test_adjoint_identity_full_size(vortex_domain):
+    M, W, solver, dom, pts, h = vortex_domain
+    eq = M.CompressibleEulerEquations2D(1.4)
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t), solver)
+    ctx = dom.ctx
+    u = W.isentropic_vortex(pts, 0.0)
+    g = np.random.default_rng(2)
+    lam = g.standard_normal(u.shape)
+    v = g.standard_normal(u.shape) * np.abs(u).max(axis=1, keepdims=True)
+    e = 1e-6
+    dp, dm = np.empty_like(u), np.empty_like(u)
+    ctx.rhs(dp, np.ascontiguousarray(u + e * v), 0.0)
+    ctx.rhs(dm, np.ascontiguousarray(u - e * v), 0.0)
+    lhs = float(np.sum(lam * (dp - dm))) / (2 * e)
+    rhs = float(np.sum(ctx.rhs_adjoint(lam, u) * v))
+    assert abs(lhs - rhs) / abs(rhs) < 1e-7, (lhs, rhs)
+
+
+def test_fp32_apply_close_to_fp64_full_size(vortex_domain):
+    M, W, solver, dom, pts, h = vortex_domain
+    eq = M.CompressibleEulerEquations2D(1.4)
+    basis32 = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver32 = M.PointCloudSolver(basis32, M.RBFFDEngineGB300(precision="fp32"))
+    dom32 = M.PointCloudDomain(solver32, pts, period=(10.0, 10.0))
+    ic = lambda x, t, e: W.isentropic_vortex(x, t)
+    s64 = M.SemidiscretizationHyperbolic(dom, eq, ic, solver)
+    s32 = M.SemidiscretizationHyperbolic(dom32, eq, ic, solver32)
+    u = W.isentropic_vortex(pts, 0.0)
+    d64, d32 = np.empty_like(u), np.empty_like(u)
+    M.rhs_(d64, u.copy(), s64, 0.0)
+    M.rhs_(d32, u.copy(), s32, 0.0)
+    assert np.linalg.norm(d32 - d64) / np.linalg.norm(d64) <= 1e-5
+
+
+def test_graph_and_direct_steps_agree_full_size(vortex_domain):
+    M, W, solver, dom, pts, h = vortex_domain
+    eq = M.CompressibleEulerEquations2D(1.4)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom))
+    M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t), solver,
+                                   source_terms=src)
+    ctx = dom.ctx
+    u0 = W.isentropic_vortex(pts, 0.0)
+    out = []
+    for graph in (True, False):
+        ctx.history_init(3)
+        ctx.set_state(u0, 0.0)
+        ctx.ssprk33(0.2 * h, 6, use_graph=graph)
+        out.append(ctx.get_state()[0])
+    assert np.array_equal(out[0], out[1])
