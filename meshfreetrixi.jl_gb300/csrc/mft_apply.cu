@@ -586,13 +586,16 @@ __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
   if (i >= count) return;
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
   if (i + 1 < count) {
+    double2 hk[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)   // all loads in flight before the sum
+      if (k < m) hk[k] = reinterpret_cast<const double2*>(hs[k])[j];
     double ax = 0.0, ay = 0.0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       if (k < m) {
-        const double2 hk = reinterpret_cast<const double2*>(hs[k])[j];
-        ax = dadd(ax, dmul(w.w[k], hk.x));
-        ay = dadd(ay, dmul(w.w[k], hk.y));
+        ax = dadd(ax, dmul(w.w[k], hk[k].x));
+        ay = dadd(ay, dmul(w.w[k], hk[k].y));
       }
     }
     reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
@@ -781,18 +784,25 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
   double* dst = ring_slot(ring, head);
   if (i + 1 < count) {
     const double2 un = reinterpret_cast<const double2*>(u_new)[j];
-    reinterpret_cast<double2*>(dst)[j] = un;
-    double ax = 0.0, ay = 0.0;
-    for (int k = 0; k < m; ++k) {
-      double2 hk = un;
-      if (k > 0) {
+    double2 hk[8];
+    hk[0] = un;
+#pragma unroll
+    for (int k = 1; k < 8; ++k) {   // all loads in flight before the sum
+      if (k < m) {
         int q = head + k;
         if (q >= slots) q -= slots;
-        hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
+        hk[k] = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
       }
-      const double wk = sp->w[k];
-      ax = dadd(ax, dmul(wk, hk.x));
-      ay = dadd(ay, dmul(wk, hk.y));
+    }
+    reinterpret_cast<double2*>(dst)[j] = un;
+    double ax = 0.0, ay = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < m) {
+        const double wk = sp->w[k];
+        ax = dadd(ax, dmul(wk, hk[k].x));
+        ay = dadd(ay, dmul(wk, hk[k].y));
+      }
     }
     reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
   } else {
