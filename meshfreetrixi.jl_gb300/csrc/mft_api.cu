@@ -756,17 +756,19 @@ void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
   for (int k = slots - 1; k > 0; --k) c->hist_t[k] = c->hist_t[k - 1];
   c->hist_t[0] = t;
   c->hist_head = (c->hist_head + slots - 1) % slots;
+  const int m = std::min(success_iter + 1, slots);
+  // host weights first, so that the timed region holds only the device work
+  double w[16];
+  if (success_iter > 0)
+    MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
+                "time_deriv_weights: singular Vandermonde system");
   ProfScope ps(c, MFT_K_HISTORY);
   MFT_CUDA(cudaMemcpyAsync(c->hist[c->hist_head].p, u_aos, nv * sizeof(double),
                            cudaMemcpyDeviceToDevice, s));
-  const int m = std::min(success_iter + 1, slots);
   if (success_iter <= 0) {
     c->approx_du.zero(s);
     return;
   }
-  double w[16];
-  MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
-              "time_deriv_weights: singular Vandermonde system");
   HistW hw{};
   for (int k = 0; k < m; ++k) hw.w[k] = w[k];
   const double* hs[8];
