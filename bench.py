@@ -61,8 +61,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
-    ap.add_argument("--only", default="all", choices=["all", "adjoint", "riemann", "weights"],
+    ap.add_argument("--only", default="all", choices=["all", "adjoint", "riemann", "weights", "igr"],
                     help="run one auxiliary measurement alone")
+    ap.add_argument("--igr", type=int, default=1, help="1 runs the IGR-source measurement")
     ap.add_argument("--weights-n", type=int, default=1048576,
                     help="stencils of the batched-weights measurement (0 skips it)")
     ap.add_argument("--riemann-side", type=int, default=1024,
@@ -387,6 +388,37 @@ def run_riemann(args, local):
             "density_range_fp64": [float(u64[0].min()), float(u64[0].max())]}
 
 
+def run_igr(args, local):
+    """IGR source on the vortex (N = 262,144, alpha = h^2, at most 20 CG iterations per
+    rhs! evaluation): SSP-RK3 steps with graphs, against the same steps without it."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(args.n_side)
+    n = pts.shape[0]
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    ic = lambda x, t, e: W.isentropic_vortex(x, t)
+    out = {}
+    for name, src in (("plain", M.SourceTerms()),
+                      ("igr", M.SourceTerms(igr=M.SourceIGR(solver, eq, dom, alpha=h * h)))):
+        semi = M.SemidiscretizationHyperbolic(dom, eq, ic, solver, source_terms=src)
+        u0 = semi.compute_coefficients(0.0)
+        ctx = dom.ctx
+        ctx.set_state(u0, 0.0)
+        ctx.ssprk33(DT_FACTOR * h, 2, use_graph=True)
+        ctx.set_state(u0, 0.0)
+        ctx.region_begin()
+        ctx.ssprk33(DT_FACTOR * h, args.steps, use_graph=True)
+        out[name] = ctx.region_end() / args.steps
+    ctx.close()
+    return {"workload": "isentropic vortex N=%d, k=%d, SourceIGR alpha=h^2, <= 20 CG iterations "
+                        "per rhs!, SSP-RK3 graphs" % (n, K_STENCIL),
+            "ms_per_step": out["igr"], "ms_per_step_without_igr": out["plain"],
+            "igr_ms_per_rhs": (out["igr"] - out["plain"]) / RHS_PER_STEP}
+
+
 def run_adjoint(args, local, peaks):
     """Gradient of J = 0.5 |rho(T) - rho*|^2 w.r.t. u0 for the isentropic vortex at
     N = 65,536 (T = 0.5, 500 SSP-RK3 steps, checkpoint every 20 steps; rho* the exact
@@ -610,7 +642,8 @@ def run_ours(args):
         if rank == 0:
             legs = {"adjoint": lambda: run_adjoint(args, local, peaks),
                     "riemann": lambda: run_riemann(args, local),
-                    "weights": lambda: run_weights(args, local)}
+                    "weights": lambda: run_weights(args, local),
+                    "igr": lambda: run_igr(args, local)}
             leg = legs[args.only]()
             print(json.dumps({args.only: leg}), flush=True)
         return
@@ -658,6 +691,7 @@ def run_ours(args):
     adj = run_adjoint(args, local, peaks) if args.adj_side > 0 and rank == 0 else None
     rie = run_riemann(args, local) if args.riemann_side > 0 and rank == 0 else None
     wts = run_weights(args, local) if args.weights_n > 0 and rank == 0 else None
+    igr = run_igr(args, local) if args.igr and rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -693,6 +727,7 @@ def run_ours(args):
         "adjoint": adj,
         "riemann": rie,
         "weights_batch": wts,
+        "igr": igr,
     }
     print(json.dumps(line), flush=True)
 
