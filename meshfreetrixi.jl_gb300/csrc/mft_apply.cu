@@ -579,33 +579,13 @@ __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
                           const double* h1, const double* h2, const double* h3,
                           const double* h4, const double* h5, const double* h6,
                           const double* h7, double* __restrict__ out) {
-  // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126); two values per
-  // thread, the ring unrolled so that every slot pointer stays in a register
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t i = 2 * j;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= count) return;
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
-  if (i + 1 < count) {
-    double2 hk[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k)   // all loads in flight before the sum
-      if (k < m) hk[k] = reinterpret_cast<const double2*>(hs[k])[j];
-    double ax = 0.0, ay = 0.0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (k < m) {
-        ax = dadd(ax, dmul(w.w[k], hk[k].x));
-        ay = dadd(ay, dmul(w.w[k], hk[k].y));
-      }
-    }
-    reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
-  } else {
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if (k < m) acc = dadd(acc, dmul(w.w[k], hs[k][i]));
-    out[i] = acc;
-  }
+  // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
+  double acc = 0.0;
+  for (int k = 0; k < m; ++k) acc = dadd(acc, dmul(w.w[k], hs[k][i]));
+  out[i] = acc;
 }
 
 __global__ void k_differs(const double* __restrict__ a, const double* __restrict__ b,
@@ -784,25 +764,18 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
   double* dst = ring_slot(ring, head);
   if (i + 1 < count) {
     const double2 un = reinterpret_cast<const double2*>(u_new)[j];
-    double2 hk[8];
-    hk[0] = un;
-#pragma unroll
-    for (int k = 1; k < 8; ++k) {   // all loads in flight before the sum
-      if (k < m) {
-        int q = head + k;
-        if (q >= slots) q -= slots;
-        hk[k] = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
-      }
-    }
     reinterpret_cast<double2*>(dst)[j] = un;
     double ax = 0.0, ay = 0.0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (k < m) {
-        const double wk = sp->w[k];
-        ax = dadd(ax, dmul(wk, hk[k].x));
-        ay = dadd(ay, dmul(wk, hk[k].y));
+    for (int k = 0; k < m; ++k) {
+      double2 hk = un;
+      if (k > 0) {
+        int q = head + k;
+        if (q >= slots) q -= slots;
+        hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
       }
+      const double wk = sp->w[k];
+      ax = dadd(ax, dmul(wk, hk.x));
+      ay = dadd(ay, dmul(wk, hk.y));
     }
     reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
   } else {
@@ -852,8 +825,8 @@ void launch_history(int64_t count, int m, const HistW& w, const double* const* h
   if (count <= 0) return;
   const double* h[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   for (int k = 0; k < m && k < 8; ++k) h[k] = hist[k];
-  k_history<<<grid_for((count + 1) / 2, 256), 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3],
-                                                            h[4], h[5], h[6], h[7], approx_du);
+  k_history<<<grid_for(count, 256), 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4],
+                                                  h[5], h[6], h[7], approx_du);
   MFT_LAUNCH_CHECK();
 }
 
