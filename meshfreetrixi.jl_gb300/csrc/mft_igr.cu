@@ -7,7 +7,7 @@
 //       conjugate gradients from sigma = 0, at most maxiter iterations, relative
 //       tolerance sqrt(eps) (the in-place cg! the reference intends at :189);
 //   du[rho v1] -= Dx sigma, du[rho v2] -= Dy sigma (:214-237).
-// The CG runs as a fixed sequence of kernels (three per iteration) whose scalars live in
+// The CG runs as a fixed sequence of kernels (four per iteration) whose scalars live in
 // device memory; once converged, the remaining kernels return at entry, so one rhs!
 // evaluation is a fixed launch sequence that a CUDA graph can hold.  Reductions are
 // block partials finished by the last block in a fixed order (deterministic).
@@ -116,23 +116,29 @@ __global__ void __launch_bounds__(kBlock) k_igr_rhs(IgrArgs a) {
   }
 }
 
-// u_new = r + beta u_old; t1 = rinv (Dx u_new), t2 = rinv (Dy u_new)
-__global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* uo, double* un) {
+// u_new = r + beta u_old (elementwise; the gathers below then read u_new directly)
+__global__ void k_igr_newdir(IgrArgs a, const double* uo, double* un) {
   if (a.sc->done) return;
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= a.n) return;
-  const double beta = a.sc->beta;
+  un[i] = dadd(a.r[i], dmul(a.sc->beta, uo[i]));
+}
+
+// t1 = rinv (Dx u_new), t2 = rinv (Dy u_new)
+__global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un) {
+  if (a.sc->done) return;
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  if (i >= a.n) return;
   const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
   const int len = a.ell.row_len[i];
   double sx = 0.0, sy = 0.0;
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
     const int64_t c = __ldg(a.ell.col + p);
-    const double uc = dadd(a.r[c], dmul(beta, uo[c]));
+    const double uc = un[c];
     sx = fma(__ldg(a.wx + p), uc, sx);
     sy = fma(__ldg(a.wy + p), uc, sy);
   }
-  un[i] = dadd(a.r[i], dmul(beta, uo[i]));
   a.t[i * 2] = dmul(a.rinv[i], sx);
   a.t[i * 2 + 1] = dmul(a.rinv[i], sy);
 }
@@ -215,7 +221,9 @@ void launch_igr(const IgrArgs& a, const double* u, cudaStream_t s) {
   for (int it = 0; it < a.maxiter; ++it) {
     const double* uo = (it & 1) ? a.u1 : a.u0;
     double* un = (it & 1) ? a.u0 : a.u1;
-    k_igr_dir<<<g, kBlock, 0, s>>>(a, uo, un);
+    k_igr_newdir<<<g, kBlock, 0, s>>>(a, uo, un);
+    MFT_LAUNCH_CHECK();
+    k_igr_dir<<<g, kBlock, 0, s>>>(a, un);
     MFT_LAUNCH_CHECK();
     k_igr_op<<<g, kBlock, 0, s>>>(a, un);
     MFT_LAUNCH_CHECK();
