@@ -815,10 +815,12 @@ mft_status mft_ctx_create(mft_ctx** out, int device, int flags) {
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_tab, cudaEventDisableTiming) != cudaSuccess) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return MFT_ERR_CUDA;
   }
@@ -839,6 +841,8 @@ mft_status mft_ctx_destroy(mft_ctx* c) {
   }
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_tab) cudaEventDestroy(c->ev_tab);
+  if (c->h_tab) cudaFreeHost(c->h_tab);
   for (auto& p : c->prof_pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
@@ -1450,8 +1454,24 @@ void ssprk33_graph(mft_ctx* c, double dt, int nsteps) {
     c->graph_valid = false;
   }
   if (!c->d_ctr.p) c->d_ctr.alloc(1);
-  MFT_CUDA(cudaMemcpyAsync(c->d_tab.p, tab.data(), nsteps * sizeof(StepParams),
+  // stage the table in pinned memory; the previous batch's copy must have left it
+  if (c->h_tab_n < (size_t)nsteps) {
+    if (c->h_tab) {
+      MFT_CUDA(cudaEventSynchronize(c->ev_tab));
+      cudaFreeHost(c->h_tab);
+      c->h_tab = nullptr;
+      c->h_tab_n = 0;
+    }
+    const size_t cap = std::max<size_t>(nsteps, 64);
+    MFT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&c->h_tab), cap * sizeof(StepParams)));
+    c->h_tab_n = cap;
+  } else {
+    MFT_CUDA(cudaEventSynchronize(c->ev_tab));
+  }
+  memcpy(c->h_tab, tab.data(), nsteps * sizeof(StepParams));
+  MFT_CUDA(cudaMemcpyAsync(c->d_tab.p, c->h_tab, nsteps * sizeof(StepParams),
                            cudaMemcpyHostToDevice, c->stream));
+  MFT_CUDA(cudaEventRecord(c->ev_tab, c->stream));
   c->d_ctr.zero(c->stream);
   if (!c->graph_valid || c->graph_dt != dt ||
       (c->U[0].p != c->graph_un[0] && c->U[0].p != c->graph_un[1]))
@@ -1463,8 +1483,6 @@ void ssprk33_graph(mft_ctx* c, double dt, int nsteps) {
     std::swap(c->U32[0].p, c->U32[3].p);
   }
   c->t_state = t0 + nsteps * dt;
-  // the table must stay alive until the copy has been staged; it has (pageable source)
-  MFT_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 void ssprk33_run(mft_ctx* c, double dt, int nsteps, bool use_graph = false) {
@@ -1498,14 +1516,34 @@ mft_status mft_ssprk33_host(mft_ctx* c, double* const* u, int nvars, double* t, 
     ensure_work(c);
     const int64_t n = c->n;
     cudaStream_t s = c->stream;
-    for (int v = 0; v < nvars; ++v)
-      MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
-                               cudaMemcpyHostToDevice, s));
+    // Pinned caller arrays mapped for the device are read and written in place by the
+    // layout kernels (one pass over C2C); other host memory goes through staging copies.
+    VarPtrs vp{};
+    bool direct = nvars <= 8;
+    for (int v = 0; v < nvars && direct; ++v) {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, u[v]) != cudaSuccess) {
+        cudaGetLastError();
+        direct = false;
+      } else if (at.type != cudaMemoryTypeHost || !at.devicePointer) {
+        direct = false;
+      } else {
+        vp.p[v] = static_cast<double*>(at.devicePointer);
+      }
+    }
+    if (!direct)
+      for (int v = 0; v < nvars; ++v)
+        MFT_CUDA(cudaMemcpyAsync(c->soa.p + (size_t)v * n, u[v], n * sizeof(double),
+                                 cudaMemcpyHostToDevice, s));
+    auto upload_to = [&](double* aos) {
+      if (direct) launch_aos_from_vars(vp, aos, n, nvars, s);
+      else launch_aos_from_soa(c->soa.p, aos, n, nvars, s);
+    };
     // The pending first stage (FSAL) stays valid only if the caller hands back
     // exactly the state this context holds at the same time.
     bool keep = c->state_valid && c->fsal_valid && c->t_state == *t;
     if (keep) {
-      launch_aos_from_soa(c->soa.p, c->work_u.p, n, nvars, s);
+      upload_to(c->work_u.p);
       c->flag.alloc(1);
       c->flag.zero(s);
       launch_differs(c->work_u.p, c->U[0].p, n * nvars, c->flag.p, s);
@@ -1517,16 +1555,20 @@ mft_status mft_ssprk33_host(mft_ctx* c, double* const* u, int nvars, double* t, 
         keep = false;
       }
     } else {
-      launch_aos_from_soa(c->soa.p, c->U[0].p, n, nvars, s);
+      upload_to(c->U[0].p);
     }
     c->t_state = *t;
     c->state_valid = true;
     if (!keep) c->fsal_valid = false;
     ssprk33_run(c, dt, nsteps, true);
-    launch_soa_from_aos(c->U[0].p, c->soa.p, n, nvars, s);
-    for (int v = 0; v < nvars; ++v)
-      MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
-                               cudaMemcpyDeviceToHost, s));
+    if (direct) {
+      launch_vars_from_aos(c->U[0].p, vp, n, nvars, s);
+    } else {
+      launch_soa_from_aos(c->U[0].p, c->soa.p, n, nvars, s);
+      for (int v = 0; v < nvars; ++v)
+        MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+    }
     MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
     *t = c->t_state;

@@ -39,6 +39,22 @@ __global__ void k_soa_from_aos(const double* __restrict__ aos, double* __restric
   if (i >= n) return;
   for (int v = 0; v < V; ++v) soa[(int64_t)v * n + i] = aos[i * V + v];
 }
+// SoA <-> AoS between the engine state and caller arrays addressed one pointer per
+// variable (pinned, device-mapped host memory or device memory).
+template <int V>
+__global__ void k_aos_from_vars(VarPtrs src, double* __restrict__ aos, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int v = 0; v < V; ++v) aos[i * V + v] = src.p[v][i];
+}
+template <int V>
+__global__ void k_vars_from_aos(const double* __restrict__ aos, VarPtrs dst, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int v = 0; v < V; ++v) dst.p[v][i] = aos[i * V + v];
+}
 __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t count) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < count) b[i] = __double2float_rn(a[i]);
@@ -603,6 +619,21 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s) {
   if (n <= 0) return;
   k_aos_from_soa<<<grid_for(n, 256), 256, 0, s>>>(soa, aos, n, V);
+  MFT_LAUNCH_CHECK();
+}
+void launch_aos_from_vars(const VarPtrs& src, double* aos, int64_t n, int V, cudaStream_t s) {
+  if (n <= 0) return;
+  MFT_REQUIRE(V == 1 || V == 4, MFT_ERR_UNSUPPORTED, "1 or 4 variables");
+  if (V == 4) k_aos_from_vars<4><<<grid_for(n, 256), 256, 0, s>>>(src, aos, n);
+  else k_aos_from_vars<1><<<grid_for(n, 256), 256, 0, s>>>(src, aos, n);
+  MFT_LAUNCH_CHECK();
+}
+void launch_vars_from_aos(const double* aos, const VarPtrs& dst, int64_t n, int V,
+                          cudaStream_t s) {
+  if (n <= 0) return;
+  MFT_REQUIRE(V == 1 || V == 4, MFT_ERR_UNSUPPORTED, "1 or 4 variables");
+  if (V == 4) k_vars_from_aos<4><<<grid_for(n, 256), 256, 0, s>>>(aos, dst, n);
+  else k_vars_from_aos<1><<<grid_for(n, 256), 256, 0, s>>>(aos, dst, n);
   MFT_LAUNCH_CHECK();
 }
 void launch_soa_from_aos(const double* aos, double* soa, int64_t n, int V, cudaStream_t s) {

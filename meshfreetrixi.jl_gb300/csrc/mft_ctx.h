@@ -143,6 +143,9 @@ struct mft_ctx {
   bool graph_valid = false;
   bool capturing = false;
   mft::DBuf<mft::StepParams> d_tab;
+  mft::StepParams* h_tab = nullptr;  // pinned staging of the step table
+  size_t h_tab_n = 0;
+  cudaEvent_t ev_tab = nullptr;      // the last table copy
   mft::DBuf<int> d_ctr;
 
   // side stream for the residual-viscosity reductions (overlap with the gathers)

@@ -122,6 +122,13 @@ struct Epilogue {
 void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s);
 void launch_soa_from_aos(const double* aos, double* soa, int64_t n, int V, cudaStream_t s);
 void launch_aos_to_f32(const double* aos, float* a32, int64_t count, cudaStream_t s);
+// One pointer per variable (pinned host memory mapped for the device, or device memory).
+struct VarPtrs {
+  double* p[8];
+};
+void launch_aos_from_vars(const VarPtrs& src, double* aos, int64_t n, int V, cudaStream_t s);
+void launch_vars_from_aos(const double* aos, const VarPtrs& dst, int64_t n, int V,
+                          cudaStream_t s);
 
 // BC pass 1 over the boundary-node list: Dirichlet u = g, slip wall u = slip(u).
 void launch_bc_pass1(int64_t nb, const int32_t* bnode, int V, int eq, BcDev bc, double* u,

@@ -142,6 +142,45 @@ def test_host_entry_point_equals_device_steps(gpu_lib):
     assert np.array_equal(u, u_dev)
 
 
+def test_host_entry_point_pinned_and_pageable_agree(gpu_lib):
+    """Pinned caller arrays (read and written in place by the layout kernels) and pageable
+    ones (staged copies) give the same states as device stepping, bit for bit (vortex with
+    residual viscosity: graph-replayed steps)."""
+    torch = pytest.importorskip("torch")
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(40)
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom))
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                          solver, source_terms=src)
+    ctx = dom.ctx
+    u0 = semi.compute_coefficients(0.0)
+    dt = 0.2 * h
+    ctx.history_init(3)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, 4)
+    u_dev, _ = ctx.get_state()
+    results = []
+    for pinned in (True, False):
+        if pinned:
+            buf = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
+            u = buf.numpy()
+            u[:] = u0
+        else:
+            u = u0.copy()
+        ctx.history_init(3)
+        t = 0.0
+        for _ in range(4):
+            t = ctx.ssprk33_host(u, t, dt, 1)
+        results.append(np.array(u, copy=True))
+    assert np.array_equal(results[0], u_dev)
+    assert np.array_equal(results[1], u_dev)
+
+
 def test_graph_steps_equal_direct_steps(gpu_lib):
     """Steps replayed from the captured per-step CUDA graphs (device step table for the
     history weights) equal directly launched steps bit for bit, across odd batch sizes
