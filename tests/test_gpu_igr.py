@@ -57,3 +57,26 @@ def test_igr_trajectory_matches_oracle(oracle, gpu_lib):
     got, _ = ctx.get_state()
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err < 1e-9, err
+
+
+def test_igr_in_fp32_form_close_to_fp64(gpu_lib):
+    """The IGR term is computed in FP64 and added in the FP64 stage epilogue of the
+    FP32-apply kernels: the FP32 form's rhs! stays within FP32 rounding of the FP64 one."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(64, seed=5)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+        solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision=prec))
+        dom = M.PointCloudDomain(solver, pts, period=per)
+        eq = M.CompressibleEulerEquations2D(1.4)
+        src = M.SourceTerms(igr=M.SourceIGR(solver, eq, dom, alpha=h * h))
+        semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                              solver, source_terms=src)
+        u = W.isentropic_vortex(pts, 0.0)
+        du = np.empty_like(u)
+        M.rhs_(du, u.copy(), semi, 0.0)
+        out[prec] = du
+    err = np.linalg.norm(out["fp32"] - out["fp64"]) / np.linalg.norm(out["fp64"])
+    assert err < 2e-4, err

@@ -75,3 +75,24 @@ def test_adjoint_refuses_limiter(gpu_lib):
     u0 = dip_state(pts)
     with pytest.raises(MFTError):
         dom.ctx.rhs_adjoint(u0, u0)
+
+
+def test_limited_trajectory_fp32_form_close_to_fp64(gpu_lib):
+    """The limiter runs on the FP64 stage state and refreshes the FP32 shadow the FP32
+    gathers read: the FP32 form's limited trajectory stays within 1e-5 of the FP64 one."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, (h, _) = W.jittered_grid(32, 32, jitter=0.25)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+        solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision=prec))
+        dom = M.PointCloudDomain(solver, pts)
+        eq = M.CompressibleEulerEquations2D(GAMMA)
+        semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: dip_state(x), solver)
+        lim = M.PositivityPreservingLimiterZhangShu(thresholds=(0.05, 0.05),
+                                                    variables=(M.density, M.pressure))
+        ode = M.semidiscretize(semi, (0.0, 10 * 0.05 * h))
+        res[prec] = M.solve(ode, M.SSPRK33(stage_limiter=lim), dt=0.05 * h).u
+    err = np.linalg.norm(res["fp32"][0] - res["fp64"][0]) / np.linalg.norm(res["fp64"][0])
+    assert err < 1e-5, err
