@@ -61,8 +61,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
-    ap.add_argument("--only", default="all", choices=["all", "adjoint", "riemann", "weights", "igr"],
+    ap.add_argument("--only", default="all",
+                    choices=["all", "adjoint", "riemann", "weights", "igr", "fp32"],
                     help="run one auxiliary measurement alone")
+    ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged"],
+                    help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
     ap.add_argument("--igr", type=int, default=1, help="1 runs the IGR-source measurement")
     ap.add_argument("--weights-n", type=int, default=1048576,
                     help="stencils of the batched-weights measurement (0 skips it)")
@@ -565,8 +568,11 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def cpu_baseline_oracle(n_side, max_steps, nthreads, min_seconds=10.0):
-    """The oracle's rhs! + SSP-RK3 on the host cores over a bounded number of steps."""
+def cpu_baseline_oracle(n_side, max_steps, nthreads, min_seconds=10.0, single_seconds=4.0):
+    """The oracle's rhs! + SSP-RK3 on the host cores over a bounded number of steps, with
+    all `nthreads` cores and with one (the reference's own SpMV and flux loops are
+    serial).  The operators are built once, with all cores, outside the timed regions.
+    Returns {threads: (node-rhs/s, seconds, steps)}."""
     from oracle import oracle as O
     from meshfree_gb300 import workloads as W
     pts, per, h = W.vortex_cloud(n_side)
@@ -577,16 +583,19 @@ def cpu_baseline_oracle(n_side, max_steps, nthreads, min_seconds=10.0):
     ops = O.operators_from_stencils(n, rowptr, idx.ravel(), w)
     semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=(O.SRC_RV,), h=davg)
     u0 = W.isentropic_vortex(pts, 0.0)
-    hist = O.History(semi, 3)
-    t0 = time.perf_counter()
-    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, 1, history=hist, nthreads=nthreads)  # warm-up
-    per_step = (time.perf_counter() - t0) / 1.33    # 4 rhs! evaluations in a 1-step call
-    done = int(min(max_steps, max(2, min_seconds / per_step)))   # a sample of ~min_seconds
-    hist = O.History(semi, 3)
-    t0 = time.perf_counter()
-    O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, done, history=hist, nthreads=nthreads)
-    sec = time.perf_counter() - t0
-    return n * RHS_PER_STEP * done / sec, sec, done
+    out = {}
+    for nt, budget in ((nthreads, min_seconds), (1, single_seconds)):
+        hist = O.History(semi, 3)
+        t0 = time.perf_counter()
+        O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, 1, history=hist, nthreads=nt)  # warm-up
+        per_step = (time.perf_counter() - t0) / 1.33    # 4 rhs! evaluations in a 1-step call
+        done = int(min(max_steps, max(2, budget / per_step)))   # a sample of ~budget s
+        hist = O.History(semi, 3)
+        t0 = time.perf_counter()
+        O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, done, history=hist, nthreads=nt)
+        sec = time.perf_counter() - t0
+        out[nt] = (n * RHS_PER_STEP * done / sec, sec, done)
+    return out
 
 
 def run_reference(args):
@@ -635,6 +644,26 @@ def config_dict(n, prec):
             "parallelism": "replicas"}
 
 
+def run_fp32(args, local, peaks):
+    """The FP32-apply form alone on the headline workload, with the gather mapping chosen
+    by --gather (profiling runs of the FP32 kernels)."""
+    from meshfree_gb300 import _lib as L
+    n = args.n_side ** 2
+    _, dom, u0, dt = build_problem(args.n_side, "fp32", local)
+    ctx = dom.ctx
+    ctx.set_option(L.OPT_GATHER, {"auto": L.GATHER_AUTO, "thread": L.GATHER_THREAD,
+                                  "staged": L.GATHER_STAGED}[args.gather])
+    ms, prof, _, _, ms_prof = timed_steps(ctx, u0, dt, args.warmup, args.steps, None)
+    out = {"value": n * RHS_PER_STEP * args.steps / (ms * 1e-3), "unit": UNIT,
+           "ms_per_step": ms / args.steps, "gather": args.gather,
+           "mapping": {"fwd_gather": ctx.get_option(L.OPT_TUNED_FWD),
+                       "rev_gather": ctx.get_option(L.OPT_TUNED_REV)},
+           "kernels_us": {k: v[0] / v[1] * 1e3 for k, v in prof.items()},
+           "roofline": roofline(prof, n, "fp32", peaks)}
+    ctx.close()
+    return out
+
+
 def run_ours(args):
     ws, rank, local, pg = dist_setup()
     peaks = load_peaks()
@@ -643,7 +672,8 @@ def run_ours(args):
             legs = {"adjoint": lambda: run_adjoint(args, local, peaks),
                     "riemann": lambda: run_riemann(args, local),
                     "weights": lambda: run_weights(args, local),
-                    "igr": lambda: run_igr(args, local)}
+                    "igr": lambda: run_igr(args, local),
+                    "fp32": lambda: run_fp32(args, local, peaks)}
             leg = legs[args.only]()
             print(json.dumps({args.only: leg}), flush=True)
         return
@@ -696,10 +726,15 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        v, sec, cpu_steps = cpu_baseline_oracle(args.n_side, 400, nthreads)
+        res = cpu_baseline_oracle(args.n_side, 400, nthreads)
+        v, sec, cpu_steps = res[nthreads]
+        v1, sec1, steps1 = res[1]
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": "full N=%d, %d SSP-RK3 steps (%.1f s), oracle rhs! with OpenMP"
-                         % (n, cpu_steps, sec)}
+                         % (n, cpu_steps, sec),
+               "single_thread": {"value": v1, "unit": UNIT, "cores": 1,
+                                 "sample": "full N=%d, %d SSP-RK3 steps (%.1f s)"
+                                           % (n, steps1, sec1)}}
     if rank != 0:
         return
     line = {

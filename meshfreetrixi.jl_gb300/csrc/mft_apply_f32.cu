@@ -119,12 +119,25 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
   }
   float eps;
   if (a.kind == MFT_SRC_RV) {
+    // node records as 16-byte vectors (V = 4): du_p32 one float4, approx_du two double2
+    float dpv[V], adv[V];
+    if (V == 4) {
+      const float4 d4 = reinterpret_cast<const float4*>(a.du_p32)[i];
+      const double2 a0 = reinterpret_cast<const double2*>(a.approx_du)[i * 2];
+      const double2 a1 = reinterpret_cast<const double2*>(a.approx_du)[i * 2 + 1];
+      dpv[0] = d4.x; dpv[1 % V] = d4.y; dpv[2 % V] = d4.z; dpv[3 % V] = d4.w;
+      adv[0] = (float)a0.x; adv[1 % V] = (float)a0.y; adv[2 % V] = (float)a1.x;
+      adv[3 % V] = (float)a1.y;
+    } else {
+      dpv[0] = a.du_p32[i];
+      adv[0] = (float)a.approx_du[i];
+    }
     float mr = 0.0f;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      float dp = a.du_p32[i * V + v];
+      float dp = dpv[v];
       if (a.hvf) dp += (float)a.hvf[i * V + v];
-      const float r = fabsf((float)a.approx_du[i * V + v] - dp);
+      const float r = fabsf(adv[v] - dp);
       const float qv = r * (float)norms[V + v];
       mr = v == 0 ? qv : fmaxf(mr, qv);
       if (isnan(qv)) mr = qv;
@@ -139,8 +152,17 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
     eps = eps_uw;
   }
   if (a.eps) a.eps[i] = (double)eps;
+  if (V == 4) {
+    float4* t4 = reinterpret_cast<float4*>(a.t32) + i * 2;
+    float4 x = t4[0], y = t4[1];
+    x.x *= eps; x.y *= eps; x.z *= eps; x.w *= eps;
+    y.x *= eps; y.y *= eps; y.z *= eps; y.w *= eps;
+    t4[0] = x;
+    t4[1] = y;
+  } else {
 #pragma unroll
-  for (int k = 0; k < 2 * V; ++k) a.t32[i * 2 * V + k] *= eps;
+    for (int k = 0; k < 2 * V; ++k) a.t32[i * 2 * V + k] *= eps;
+  }
 }
 
 template <int V, bool RV, bool LAP>
@@ -159,8 +181,8 @@ __global__ void __launch_bounds__(kBlock) k_rev_f32(RevArgs a) {
     if (RV) {
       const float wx = __ldg(a.w32[0] + p), wy = __ldg(a.w32[1] + p);
       if (V == 4) {
-        const float4* S4 = reinterpret_cast<const float4*>(a.s32) + (int64_t)c * 2;
-        const float4 xs = __ldg(S4), ys = __ldg(S4 + 1);
+        const F8 st = ldg_f8(a.s32 + (int64_t)c * 8);
+        const float4 xs = st.lo, ys = st.hi;
         sx[0] = fmaf(wx, xs.x, sx[0]); sx[1] = fmaf(wx, xs.y, sx[1]);
         sx[2] = fmaf(wx, xs.z, sx[2]); sx[3] = fmaf(wx, xs.w, sx[3]);
         sy[0] = fmaf(wy, ys.x, sy[0]); sy[1] = fmaf(wy, ys.y, sy[1]);

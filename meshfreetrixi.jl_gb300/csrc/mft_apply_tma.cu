@@ -11,6 +11,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
+#include <vector>
+
 #include "mft_device.cuh"
 #include "mft_internal.cuh"
 #include "mft_tma.cuh"
@@ -34,6 +37,20 @@ __device__ __forceinline__ int slice_slots(const EllView& e, int64_t s) {
   return (int)((e.slice_off[s + 1] - e.slice_off[s]) >> 5);
 }
 
+// Row length of this lane's row in slice s (0 past the end); loaded one slice ahead.
+__device__ __forceinline__ int row_len_at(const EllView& e, int64_t n, int64_t s, int lane,
+                                          int64_t nslices) {
+  const int64_t i = (s << 5) + lane;
+  return (s < nslices && i < n) ? e.row_len[i] : 0;
+}
+
+// The stage epilogue's node records (stage state, step-start state) requested into L2 at
+// the start of a slice, so that they arrive while the slice's gathers run.
+__device__ __forceinline__ void prefetch_epilogue(const Epilogue& ep, int64_t i) {
+  tma::prefetch_l2(ep.u_s + i * 4);
+  if (ep.kind == kStage2 || ep.kind == kStage3) tma::prefetch_l2(ep.u_n + i * 4);
+}
+
 template <int NARR, int CH>
 __device__ __forceinline__ void issue_chunk(unsigned char (*buf)[CH * 128], uint64_t* bar,
                                             const EllView& e, const void* const* arrs,
@@ -42,11 +59,13 @@ __device__ __forceinline__ void issue_chunk(unsigned char (*buf)[CH * 128], uint
   const int n = min(CH, slots - cur.c * CH);
   const uint32_t bytes = (uint32_t)n * 32u * 4u;
   const int64_t base = e.slice_off[cur.s] + (int64_t)cur.c * CH * 32;
+  const uint64_t pol = tma::policy_evict_first();
   tma::fence_proxy_async();
   tma::arrive_expect_tx(bar, bytes * NARR);
 #pragma unroll
   for (int k = 0; k < NARR; ++k)
-    tma::bulk_g2s(buf[k], static_cast<const unsigned char*>(arrs[k]) + base * 4, bytes, bar);
+    tma::bulk_g2s_hint(buf[k], static_cast<const unsigned char*>(arrs[k]) + base * 4, bytes,
+                       bar, pol);
 }
 
 template <int CH>
@@ -89,10 +108,13 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
     }
   }
   int buf = 0;
+  int len_next = row_len_at(a.ell, a.n, first, lane, nslices);
   for (int64_t s = first; s < nslices; s += stride) {
     const int64_t i = (s << 5) + lane;
     const bool valid = i < a.n;
-    const int len = valid ? a.ell.row_len[i] : 0;
+    const int len = len_next;
+    len_next = row_len_at(a.ell, a.n, s + stride, lane, nslices);
+    if (valid && a.final_epilogue) prefetch_epilogue(a.ep, i);
     const int slots = slice_slots(a.ell, s);
     const int nch = (slots + CH - 1) / CH;
     float f[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
@@ -179,7 +201,6 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
     tma::fence_init();
   }
   __syncwarp();
-  const float4* __restrict__ S4 = reinterpret_cast<const float4*>(a.s32);
   const float4* __restrict__ Q4 = reinterpret_cast<const float4*>(a.q32);
   const float hg = (float)a.hv_gamma;
   uint32_t phase[2] = {0u, 0u};
@@ -194,10 +215,16 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
     }
   }
   int buf = 0;
+  int len_next = row_len_at(a.ell, a.n, first, lane, nslices);
   for (int64_t s = first; s < nslices; s += stride) {
     const int64_t i = (s << 5) + lane;
     const bool valid = i < a.n;
-    const int len = valid ? a.ell.row_len[i] : 0;
+    const int len = len_next;
+    len_next = row_len_at(a.ell, a.n, s + stride, lane, nslices);
+    if (valid) {
+      tma::prefetch_l2(a.du_p32 + i * 4);
+      if (a.final_epilogue) prefetch_epilogue(a.ep, i);
+    }
     const int slots = slice_slots(a.ell, s);
     const int nch = (slots + CH - 1) / CH;
     float sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0}, sl[4] = {0, 0, 0, 0};
@@ -215,22 +242,19 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
       if (RV) {
         const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][1]);
         const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][2]);
-        float4 xs[CH], ys[CH];
+        F8 st[CH];
 #pragma unroll
         for (int k = 0; k < CH; ++k)
-          if (j0 + k < len) {
-            const int64_t cc = scol[k * 32 + lane];
-            xs[k] = __ldg(S4 + cc * 2);
-            ys[k] = __ldg(S4 + cc * 2 + 1);
-          }
+          if (j0 + k < len) st[k] = ldg_f8(a.s32 + (int64_t)scol[k * 32 + lane] * 8);
 #pragma unroll
         for (int k = 0; k < CH; ++k)
           if (j0 + k < len) {
             const float wx = swx[k * 32 + lane], wy = swy[k * 32 + lane];
-            sx[0] = fmaf(wx, xs[k].x, sx[0]); sx[1] = fmaf(wx, xs[k].y, sx[1]);
-            sx[2] = fmaf(wx, xs[k].z, sx[2]); sx[3] = fmaf(wx, xs[k].w, sx[3]);
-            sy[0] = fmaf(wy, ys[k].x, sy[0]); sy[1] = fmaf(wy, ys[k].y, sy[1]);
-            sy[2] = fmaf(wy, ys[k].z, sy[2]); sy[3] = fmaf(wy, ys[k].w, sy[3]);
+            const float4 xs = st[k].lo, ys = st[k].hi;
+            sx[0] = fmaf(wx, xs.x, sx[0]); sx[1] = fmaf(wx, xs.y, sx[1]);
+            sx[2] = fmaf(wx, xs.z, sx[2]); sx[3] = fmaf(wx, xs.w, sx[3]);
+            sy[0] = fmaf(wy, ys.x, sy[0]); sy[1] = fmaf(wy, ys.y, sy[1]);
+            sy[2] = fmaf(wy, ys.z, sy[2]); sy[3] = fmaf(wy, ys.w, sy[3]);
           }
       }
       if (LAP) {
@@ -275,19 +299,43 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
   }
 }
 
+// Resident blocks of one kernel on the current device (SMs x blocks per SM).  The
+// instantiations share a function type but not their register or shared-memory use, so
+// the figure is cached per (kernel, device): a grid sized for another instantiation
+// would run its last blocks as a second partial wave.
+int resident_blocks(const void* kernel) {
+  struct Entry {
+    const void* k;
+    int dev, blocks;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> cache;
+  int dev = 0;
+  MFT_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  for (const Entry& e : cache)
+    if (e.k == kernel && e.dev == dev) return e.blocks;
+  int sms = 0, per = 0;
+  MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 32 * kTmaWarps, 0));
+  cache.push_back({kernel, dev, sms * (per > 0 ? per : 1)});
+  return cache.back().blocks;
+}
+
+// Persistent grid: at most one wave of resident blocks, and no more warps than slices.
+// The slices are then spread evenly: with s slices and w warps a warp takes ceil(s / w)
+// of them, so w is lowered to the smallest count with the same ceiling.
 template <class K>
 unsigned persistent_grid(K kernel, int64_t n) {
-  static int cached = 0;
-  if (cached == 0) {
-    int dev = 0, sms = 0, per = 0;
-    MFT_CUDA(cudaGetDevice(&dev));
-    MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 32 * kTmaWarps, 0));
-    cached = sms * (per > 0 ? per : 1);
-  }
+  const int64_t cap = resident_blocks(reinterpret_cast<const void*>(kernel));
   const int64_t slices = (n + 31) / 32;
-  const int64_t need = (slices + kTmaWarps - 1) / kTmaWarps;
-  return (unsigned)(need < cached ? need : cached);
+  int64_t blocks = (slices + kTmaWarps - 1) / kTmaWarps;
+  if (blocks > cap) {
+    const int64_t per_warp = (slices + cap * kTmaWarps - 1) / (cap * kTmaWarps);
+    const int64_t warps = (slices + per_warp - 1) / per_warp;
+    blocks = (warps + kTmaWarps - 1) / kTmaWarps;
+  }
+  return (unsigned)blocks;
 }
 
 }  // namespace

@@ -16,6 +16,22 @@ static __device__ __forceinline__ double dsub(double a, double b) { return __dsu
 static __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 static __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// One 32-byte read-only global load (the 256-bit vector load of sm_100 and later): both
+// halves of a node's 8-float record in one request, so each cache line it touches is
+// looked up once instead of once per 16-byte half.  p must be 32-byte aligned and the
+// data must not change during the kernel.
+struct F8 {
+  float4 lo, hi;
+};
+static __device__ __forceinline__ F8 ldg_f8(const float* p) {
+  F8 r;
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(r.lo.x), "=f"(r.lo.y), "=f"(r.lo.z), "=f"(r.lo.w), "=f"(r.hi.x), "=f"(r.hi.y),
+        "=f"(r.hi.z), "=f"(r.hi.w)
+      : "l"(p));
+  return r;
+}
+
 // Textbook Euler flux (Trixi's `flux(u, orientation, ::CompressibleEulerEquations2D)`),
 // each operation rounded separately.
 static __device__ __forceinline__ void euler_flux(double g, const double* uu, double* fx, double* fy) {
