@@ -773,7 +773,7 @@ void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
   for (int k = 0; k < m; ++k) hw.w[k] = w[k];
   const double* hs[8];
   for (int k = 0; k < m; ++k) hs[k] = c->hist[(c->hist_head + k) % slots].p;
-  launch_history((int64_t)nv, m, hw, hs, c->approx_du.p, s);
+  launch_history((int64_t)nv, m, hw, hs, c->approx_du.p, c->precision == MFT_PREC_FP32, s);
 }
 
 void check_state_ready(mft_ctx* c) {
@@ -1402,7 +1402,8 @@ void capture_step_graphs(mft_ctx* c, double dt) {
         const double* ring[8];
         for (int k = 0; k < slots; ++k) ring[k] = c->hist[k].p;
         launch_history_dev((int64_t)c->n * c->nvars, c->U[iu_3].p, ring, slots, c->d_tab.p,
-                           c->d_ctr.p, c->approx_du.p, c->stream);
+                           c->d_ctr.p, c->approx_du.p, c->precision == MFT_PREC_FP32,
+                           c->stream);
       }
       launch_step_advance(c->d_ctr.p, c->stream);
     } catch (...) {

@@ -591,6 +591,14 @@ __global__ void __launch_bounds__(kBlock) k_rev_f64(RevArgs a) {
 
 // ------------------------------------------------------------------ history
 
+// FUSED (FP32-apply form): fused multiply-adds, half the FP64 operations; the FP64 form
+// keeps the separately rounded products and sums of the reference's broadcasts.
+template <bool FUSED>
+__device__ __forceinline__ double hist_acc(double acc, double w, double h) {
+  return FUSED ? fma(w, h, acc) : dadd(acc, dmul(w, h));
+}
+
+template <bool FUSED>
 __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
                           const double* h1, const double* h2, const double* h3,
                           const double* h4, const double* h5, const double* h6,
@@ -600,7 +608,7 @@ __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
   // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
   double acc = 0.0;
-  for (int k = 0; k < m; ++k) acc = dadd(acc, dmul(w.w[k], hs[k][i]));
+  for (int k = 0; k < m; ++k) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
   out[i] = acc;
 }
 
@@ -784,6 +792,7 @@ __device__ __forceinline__ double* ring_slot(const RingPtrs& r, int k) {
 // approx_du = sum_{k<m} w_k ring[(head + k) % slots] (k = 0 is u_new itself).
 // Two values per thread (16-byte loads and stores); count is even or the last thread
 // takes the single remaining value.
+template <bool FUSED>
 __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, RingPtrs ring,
                               int slots, const StepParams* __restrict__ tab,
                               const int* __restrict__ ctr, double* __restrict__ out) {
@@ -805,8 +814,8 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
         hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
       }
       const double wk = sp->w[k];
-      ax = dadd(ax, dmul(wk, hk.x));
-      ay = dadd(ay, dmul(wk, hk.y));
+      ax = hist_acc<FUSED>(ax, wk, hk.x);
+      ay = hist_acc<FUSED>(ay, wk, hk.y);
     }
     reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
   } else {
@@ -817,7 +826,7 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
       int q = head + k;
       if (q >= slots) q -= slots;
       const double hk = k == 0 ? un : ring_slot(ring, q)[i];
-      acc = dadd(acc, dmul(sp->w[k], hk));
+      acc = hist_acc<FUSED>(acc, sp->w[k], hk);
     }
     out[i] = acc;
   }
@@ -831,12 +840,13 @@ __global__ void k_step_advance(int* ctr) {
 
 void launch_history_dev(int64_t count, const double* u_new, const double* const* ring,
                         int slots, const StepParams* tab, const int* ctr, double* approx_du,
-                        cudaStream_t s) {
+                        bool fused, cudaStream_t s) {
   if (count <= 0) return;
   RingPtrs rp{};
   for (int k = 0; k < slots && k < 8; ++k) rp.p[k] = const_cast<double*>(ring[k]);
-  k_history_dev<<<grid_for((count + 1) / 2, 256), 256, 0, s>>>(count, u_new, rp, slots, tab,
-                                                                ctr, approx_du);
+  const unsigned g = grid_for((count + 1) / 2, 256);
+  if (fused) k_history_dev<true><<<g, 256, 0, s>>>(count, u_new, rp, slots, tab, ctr, approx_du);
+  else k_history_dev<false><<<g, 256, 0, s>>>(count, u_new, rp, slots, tab, ctr, approx_du);
   MFT_LAUNCH_CHECK();
 }
 
@@ -852,12 +862,17 @@ void launch_differs(const double* a, const double* b, int64_t count, int* flag, 
 }
 
 void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
-                    double* approx_du, cudaStream_t s) {
+                    double* approx_du, bool fused, cudaStream_t s) {
   if (count <= 0) return;
   const double* h[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   for (int k = 0; k < m && k < 8; ++k) h[k] = hist[k];
-  k_history<<<grid_for(count, 256), 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4],
-                                                  h[5], h[6], h[7], approx_du);
+  const unsigned g = grid_for(count, 256);
+  if (fused)
+    k_history<true><<<g, 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4], h[5], h[6],
+                                      h[7], approx_du);
+  else
+    k_history<false><<<g, 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4], h[5], h[6],
+                                       h[7], approx_du);
   MFT_LAUNCH_CHECK();
 }
 

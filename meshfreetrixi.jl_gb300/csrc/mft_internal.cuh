@@ -306,8 +306,9 @@ void launch_differs(const double* a, const double* b, int64_t count, int* flag, 
 struct HistW {
   double w[8];
 };
+// fused: multiply-adds (FP32-apply form) instead of separately rounded products and sums.
 void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
-                    double* approx_du, cudaStream_t s);
+                    double* approx_du, bool fused, cudaStream_t s);
 
 // Per-step parameters of a captured SSP-RK3 step, read on the device through a step
 // counter so that one graph serves every step of a batch.
@@ -321,7 +322,7 @@ struct StepParams {
 // Graph-mode history push: ring[tab.head] = u_new; approx_du = sum_k w_k ring_k.
 void launch_history_dev(int64_t count, const double* u_new, const double* const* ring,
                         int slots, const StepParams* tab, const int* ctr, double* approx_du,
-                        cudaStream_t s);
+                        bool fused, cudaStream_t s);
 void launch_step_advance(int* ctr, cudaStream_t s);
 
 }  // namespace mft

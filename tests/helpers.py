@@ -95,3 +95,102 @@ def cond_scale(ops, u, fluxes=None, eps=None, lap=None, hv_gamma=0.0, hvop=None)
             s += hv_gamma * (abs(hvop.to_scipy()) @ np.abs(u[v]))
         out[v] = s.max()
     return out
+
+
+# --------------------------------------------------------------------------------------
+# Forward-mode derivative of rhs! by the complex step: the counterpart of ForwardDiff
+# through the reference rhs!.  rhs_complex restates the oracle's rhs! (mfto_rhs in
+# oracle/mft_oracle.c: strong BC pass, flux divergence, hyperviscosity, second BC pass;
+# rbfsolver.jl:397-428, PointCloudBCs.jl:49-115) in numpy so that it runs on complex
+# states; for the real-analytic map u -> du,  J v = Im rhs(u + i h v) / h  with h = 1e-30
+# has no truncation and no cancellation error.
+
+CS_STEP = 1e-30
+
+
+def _bc_pass_complex(semi, dirichlet, du, u):
+    from oracle.oracle import BC_DIRICHLET, BC_SLIP_WALL
+    for b, (kind, ii, normals, _fn) in enumerate(semi.bcs):
+        ii = np.asarray(ii, dtype=np.int64)
+        if kind == BC_DIRICHLET:
+            du[:, ii] = 0.0
+            u[:, ii] = dirichlet[semi.bc_ptr[b]:semi.bc_ptr[b + 1]].T
+        elif kind == BC_SLIP_WALL and semi.nvars == 4:
+            nr = np.asarray(normals, dtype=np.float64).reshape(ii.size, semi.dim)
+            nn = np.sqrt(nr[:, 0] ** 2 + nr[:, 1] ** 2)
+            n1, n2 = nr[:, 0] / nn, nr[:, 1] / nn
+            vn = u[1, ii] * n1 + u[2, ii] * n2
+            s1, s2 = u[1, ii] - vn * n1, u[2, ii] - vn * n2
+            du[1, ii] = 0.0
+            du[2, ii] = 0.0
+            u[1, ii] = s1
+            u[2, ii] = s2
+
+
+def rhs_complex(semi, u, t=0.0, return_state=False):
+    """rhs!(u, t) of an oracle Semi without viscosity or IGR sources, for real or
+    complex u (nvars, n); u is not mutated.  With return_state, also the state as the
+    BC pass leaves it (rhs! mutates u at boundary nodes)."""
+    from oracle.oracle import SRC_HV_FLYER, SRC_HV_TOMINEC
+    u = np.array(u, dtype=np.complex128)
+    du = np.zeros_like(u)
+    dv = semi.dirichlet_values(t)
+    _bc_pass_complex(semi, dv, du, u)
+    for d, op in enumerate(semi.ops):
+        A = op.to_scipy()
+        if semi.nvars == 4:
+            f = flux_np(u, d, semi.s.gamma)
+        else:
+            f = semi.s.adv[d] * u
+        for v in range(semi.nvars):
+            du[v] -= A @ f[v]
+    srcs = [int(k) for k in semi.src[:semi.s.n_src]]
+    for k in srcs:
+        assert k in (SRC_HV_TOMINEC, SRC_HV_FLYER), "viscosity / IGR sources: no derivative"
+        H = semi.hv.to_scipy()
+        for v in range(semi.nvars):
+            du[v] -= semi.s.hv_gamma * (H @ u[v])
+    _bc_pass_complex(semi, dv, du, u)
+    return (du, u) if return_state else du
+
+
+def ssprk33_complex(semi, u0, t0, dt, nsteps):
+    """The oracle's ssprk33_record trajectory (Shu-Osher SSP-RK3; every rhs! projects its
+    argument by the BC pass; the final FSAL evaluation projects u_T) on complex states."""
+    u = np.array(u0, dtype=np.complex128)
+    t = t0
+    for step in range(nsteps):
+        k, u = rhs_complex(semi, u, t, return_state=True)
+        un = u
+        u1 = un + dt * k
+        k1, u1 = rhs_complex(semi, u1, t + dt, return_state=True)
+        u2 = (3.0 * un + u1 + dt * k1) / 4.0
+        k2, u2 = rhs_complex(semi, u2, t + 0.5 * dt, return_state=True)
+        u = (un + 2.0 * u2 + 2.0 * dt * k2) / 3.0
+        t = t0 + (step + 1) * dt
+    _, u = rhs_complex(semi, u, t, return_state=True)
+    return u
+
+
+def trajectory_jvp_complex(semi, u0, v, dt, nsteps, t0=0.0):
+    """d u_T / d u0 applied to v by the complex step."""
+    uc = np.asarray(u0) + 1j * CS_STEP * np.asarray(v)
+    return ssprk33_complex(semi, uc, t0, dt, nsteps).imag / CS_STEP
+
+
+def jvp_complex(semi, u, v, t=0.0):
+    """J(u) v by the complex step."""
+    return rhs_complex(semi, np.asarray(u) + 1j * CS_STEP * np.asarray(v), t).imag / CS_STEP
+
+
+def jacobian_complex(semi, u, t=0.0):
+    """Dense Jacobian d vec(du) / d vec(u) (row-major (nvars, n) vectorisation), one
+    complex-step column per unknown; small problems only."""
+    V, n = u.shape
+    J = np.empty((V * n, V * n))
+    e = np.zeros((V, n))
+    for q in range(V * n):
+        e.flat[q] = 1.0
+        J[:, q] = jvp_complex(semi, u, e, t).ravel()
+        e.flat[q] = 0.0
+    return J

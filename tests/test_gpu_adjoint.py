@@ -5,7 +5,8 @@ per variable max |gpu - ref| <= 1e-12 * s with the rounding scale
 s = max_i [ sum_d (|D_d|^T sum_v |lam_v|)_i * Jmax_i + gamma (|H|^T |lam_v|)_i ]
 (Jmax_i = largest flux-Jacobian entry at node i); (2) centred finite differences of
 the GPU's own forward rhs! and trajectory (1e-7 for rhs!, 1e-6 for the trajectory
-gradient); (3) checkpointed sweeps (recomputation between checkpoints) equal the
+gradient), and forward-mode (complex-step) derivatives of the numpy restatement of rhs!
+(1e-12: dot products on the reference fixture, the full Jacobian at N = 64); (3) checkpointed sweeps (recomputation between checkpoints) equal the
 sweep over stored stage states bit for bit; (4) the torch.autograd mirror.
 """
 import types
@@ -13,7 +14,8 @@ import types
 import numpy as np
 import pytest
 
-from helpers import GAMMA, flux_np, ic_bumpy, load_ops_into, stencil_ops
+from helpers import (GAMMA, flux_np, ic_bumpy, jacobian_complex, jvp_complex,
+                     load_ops_into, stencil_ops, trajectory_jvp_complex)
 from test_gpu_rhs import _setup
 
 pytestmark = pytest.mark.gpu
@@ -116,6 +118,36 @@ def test_rhs_adjoint_vortex_matches_oracle(oracle, gpu_lib, vortex):
     assert np.all(err <= TOL), err
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_rhs_adjoint_dot_product_with_forward_mode(oracle, gpu_lib, cyl, cyl_ops, case):
+    """<lam, J v> by the complex step through the numpy restatement of rhs! (forward
+    mode, exact to rounding) against <J^T lam, v> from the GPU adjoint: 1e-12 relative."""
+    semi, ctx, _hv, _g = _setup(oracle, gpu_lib, cyl, cyl_ops, case)
+    u = ic_bumpy(cyl["positions"])
+    rng = np.random.default_rng(6)
+    lam = rng.standard_normal(u.shape)
+    v = rng.standard_normal(u.shape) * np.abs(u).max(axis=1, keepdims=True)
+    lhs = float(np.sum(lam * jvp_complex(semi, u, v)))
+    rhs = float(np.sum(ctx.rhs_adjoint(lam, u) * v))
+    assert abs(lhs - rhs) / abs(rhs) < TOL, (lhs, rhs)
+
+
+def test_rhs_adjoint_equals_forward_mode_jacobian_small(oracle, gpu_lib):
+    """N = 64 vortex cloud (256 unknowns): the GPU adjoint equals J^T lam of the dense
+    complex-step Jacobian entry by entry (1e-12 of the product's scale)."""
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(8, seed=11)
+    idx, _, _, _ = oracle.knn(pts, 20, period=per)
+    ops, _ = stencil_ops(oracle, pts, idx, period=per)
+    semi, ctx = vortex_ctx(oracle, (pts, ops, h))
+    u = W.isentropic_vortex(pts, 0.0)
+    J = jacobian_complex(semi, u)
+    lam = np.random.default_rng(7).standard_normal(u.shape)
+    ref = (J.T @ lam.ravel()).reshape(u.shape)
+    got = ctx.rhs_adjoint(lam, u)
+    assert np.abs(got - ref).max() <= TOL * (np.abs(J).T @ np.abs(lam).ravel()).max()
+
+
 @pytest.mark.parametrize("case", ["plain", "flyer"])
 def test_rhs_adjoint_dot_product_with_gpu_fd(oracle, gpu_lib, cyl, cyl_ops, case):
     _semi, ctx, _hv, _g = _setup(oracle, gpu_lib, cyl, cyl_ops, case)
@@ -180,6 +212,26 @@ def test_trajectory_adjoint_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, vortex
     assert np.abs(states[0] - uT_o).max() <= 1e-10 * np.abs(uT_o).max()
     err = np.linalg.norm(grads[0] - ref) / np.linalg.norm(ref)
     assert err < 1e-10, err
+
+
+@pytest.mark.parametrize("case", ["vortex", "cyl"])
+def test_trajectory_adjoint_matches_forward_mode(oracle, gpu_lib, cyl, cyl_ops, vortex, case):
+    """Checkpointed GPU reverse sweep (every 2 steps) against the forward-mode derivative
+    of the whole 6-step trajectory (complex step through the numpy restatement):
+    <lam_T, (du_T/du_0) v> = <lam_0, v>.  The GPU linearises about its own stage states
+    (within 1e-14 of the restatement's), hence 1e-11 rather than the 1e-12 of a single
+    rhs!."""
+    semi, ctx, u0, dt = _trajectory(oracle, gpu_lib, cyl, cyl_ops, vortex, case)
+    nsteps = 6
+    rng = np.random.default_rng(9)
+    lamT = rng.standard_normal(u0.shape)
+    v = rng.standard_normal(u0.shape) * np.abs(u0).max(axis=1, keepdims=True)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33_record(dt, nsteps, 2)
+    lam0 = ctx.ssprk33_adjoint(lamT)
+    lhs = float(np.sum(lamT * trajectory_jvp_complex(semi, u0, v, dt, nsteps)))
+    rhs = float(np.sum(lam0 * v))
+    assert abs(lhs - rhs) / abs(rhs) < 1e-11, (lhs, rhs)
 
 
 def test_solve_adjoint_vortex_matches_gpu_fd():
