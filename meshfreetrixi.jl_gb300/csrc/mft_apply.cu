@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <cmath>
+
 #include "mft_device.cuh"
 #include "mft_internal.cuh"
 
@@ -91,8 +93,15 @@ __global__ void k_flux_euler(int64_t n, double g, const double* __restrict__ u,
   if (i >= n) return;
   const double2* ui = reinterpret_cast<const double2*>(u) + i * 2;
   const double2 a = ui[0], b = ui[1];
-  double uu[4] = {a.x, a.y, b.x, b.y}, fx[4], fy[4];
-  euler_flux(g, uu, fx, fy);
+  // The textbook flux with one reciprocal for both velocities (an FP64 division is a
+  // long sequence on this part): v = m * (1 / rho) is within an ulp of m / rho.
+  const double rho = a.x, m1 = a.y, m2 = b.x, en = b.y;
+  const double rinv = ddiv(1.0, rho);
+  const double v1 = dmul(m1, rinv), v2 = dmul(m2, rinv);
+  const double p = dmul(dsub(g, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
+  const double ep = dadd(en, p);
+  const double fx[4] = {m1, dadd(dmul(m1, v1), p), dmul(m1, v2), dmul(ep, v1)};
+  const double fy[4] = {m2, dmul(m2, v1), dadd(dmul(m2, v2), p), dmul(ep, v2)};
   double2* Fi = reinterpret_cast<double2*>(F) + i * 4;
   Fi[0] = make_double2(fx[0], fx[1]);
   Fi[1] = make_double2(fx[2], fx[3]);
@@ -473,6 +482,21 @@ __global__ void __launch_bounds__(kBlock) k_lexmax_seg(const int64_t* __restrict
 
 // ------------------------------------------------------------------ viscosity
 
+// Julia's max for arguments that are +0 or larger, or NaN (NaN propagates as a + b):
+// without NaN the larger value is the larger IEEE bit pattern, so no FP64 comparison
+// is issued.
+__device__ __forceinline__ double jl_max_nonneg(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  const long long inf = 0x7FF0000000000000LL;
+  if ((ia & 0x7FFFFFFFFFFFFFFFLL) > inf || (ib & 0x7FFFFFFFFFFFFFFFLL) > inf) return a + b;
+  return ib > ia ? b : a;
+}
+
+// isnan(x) || isinf(x) on the exponent bits
+__device__ __forceinline__ bool not_finite(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7FF) == 0x7FF;
+}
+
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
@@ -480,27 +504,13 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   const int sg = a.seg_id ? a.seg_id[i] : 0;
   const double h = a.seg_h ? a.seg_h[sg] : a.h;
   const double* __restrict__ norms = a.norms + (a.seg_id ? sg * 2 * V : 0);
-  double eps_uw;
-  if (V == 4) {
-    // one reciprocal instead of three divisions (FP64 division is a long sequence on
-    // this part); results differ from the divisions by at most an ulp
-    const double rho = a.u[i * 4], m1 = a.u[i * 4 + 1], m2 = a.u[i * 4 + 2], en = a.u[i * 4 + 3];
-    const double rinv = ddiv(1.0, rho);
-    const double v1 = dmul(m1, rinv), v2 = dmul(m2, rinv);
-    const double p = dmul(dsub(a.gamma, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
-    const double speed = sqrt(dadd(dmul(v1, v1), dmul(v2, v2)));
-    double c;
-    if (p < 0.0 || rho < 0.0) c = 0.0;
-    else c = sqrt(dmul(dmul(a.gamma, p), rinv));
-    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), h), dadd(speed, c));
-  } else {
-    const double an = sqrt(dadd(dmul(a.ax, a.ax), dmul(a.ay, a.ay)));
-    eps_uw = dmul(dmul(dmul(a.c_uw, 0.5), h), an);
-  }
-  double eps;
   const int si = a.tab ? a.tab[*a.ctr].si_eps : a.success_iter;
-  if (a.kind == MFT_SRC_RV && si != 0) {
-    // residual / norm with the norms' reciprocals (written by k_lexmax after the norms)
+  const bool rv = a.kind == MFT_SRC_RV && si != 0;
+  double eps_rv = 0.0;
+  bool rv_finite = false;
+  if (rv) {
+    // residual / norm with the norms' reciprocals (written by k_lexmax after the norms);
+    // r >= 0 and the reciprocals are positive, so every qv is +0 or larger, or NaN
     double mr = 0.0;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
@@ -508,19 +518,66 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
       if (a.hvf) dp = dadd(dp, a.hvf[i * V + v]);
       const double r = fabs(dsub(a.approx_du[i * V + v], dp));
       const double qv = dmul(r, norms[V + v]);
-      mr = v == 0 ? qv : jl_max(mr, qv);
+      mr = v == 0 ? qv : jl_max_nonneg(mr, qv);
     }
-    const double eps_rv = dmul(dmul(dmul(0.5, a.c_rv), dmul(h, h)), mr);
-    if (isnan(eps_rv) || isinf(eps_rv)) {
-      eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16 : eps_uw;
+    const double rvc = a.seg_h ? dmul(dmul(0.5, a.c_rv), dmul(h, h)) : a.rv_coef;
+    eps_rv = dmul(rvc, mr);
+    rv_finite = !not_finite(eps_rv);
+  }
+  double eps;
+  double rho = 0.0, m1 = 0.0, m2 = 0.0, en = 0.0;
+  if (V == 4) {
+    const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
+    const double2 ub = reinterpret_cast<const double2*>(a.u)[i * 2 + 1];
+    rho = ua.x; m1 = ua.y; m2 = ub.x; en = ub.y;
+  }
+  const double uwc = a.seg_h ? dmul(dmul(a.c_uw, 0.5), h) : a.uw_coef;
+  // Decided without forming eps_uw: the computed eps_uw = uwc (speed + c) is at least
+  // uwc |m| / rho (1 - 5 u) (c >= 0, no cancellation in speed; u = 2^-53), so
+  // (eps_rv rho)^2 (1 + 1e-12) < uwc^2 (1 - 1e-12) |m|^2, evaluated in FP64 with a normal,
+  // finite right side, proves eps_rv < eps_uw and update_visc!'s min is eps_rv.  This
+  // skips the division and the two square roots wherever the residual viscosity is the
+  // smaller one (smooth flow).  A NaN energy, or a density so small that 1 / rho
+  // overflows (0 * inf in a velocity), would make eps_uw NaN: no shortcut then.
+  bool done = false;
+  if (V == 4 && rv_finite && rho >= 1e-300 && uwc > 0.0 && en == en) {
+    const double er = dmul(eps_rv, rho);
+    const double lhs = dmul(dmul(er, er), 1.0 + 1e-12);
+    const double rhs = dmul(dmul(dmul(uwc, uwc), 1.0 - 1e-12), dadd(dmul(m1, m1), dmul(m2, m2)));
+    if (rhs >= 1e-290 && rhs <= 1.7e308 && lhs < rhs) {
+      eps = eps_rv;
+      done = true;
+    }
+  }
+  if (!done) {
+    double eps_uw;
+    if (V == 4) {
+      // one reciprocal instead of three divisions (FP64 division is a long sequence on
+      // this part); results differ from the divisions by at most an ulp
+      const double rinv = ddiv(1.0, rho);
+      const double v1 = dmul(m1, rinv), v2 = dmul(m2, rinv);
+      const double p =
+          dmul(dsub(a.gamma, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
+      const double speed = sqrt(dadd(dmul(v1, v1), dmul(v2, v2)));
+      double c;
+      if (p < 0.0 || rho < 0.0) c = 0.0;
+      else c = sqrt(dmul(dmul(a.gamma, p), rinv));
+      eps_uw = dmul(uwc, dadd(speed, c));
+    } else if (a.seg_h) {
+      const double an = sqrt(dadd(dmul(a.ax, a.ax), dmul(a.ay, a.ay)));
+      eps_uw = dmul(uwc, an);
     } else {
-      eps = jl_min(eps_rv, eps_uw);
+      eps_uw = a.uw_adv;
     }
-  } else if (a.kind == MFT_SRC_RV) {
-    // success_iter == 0: update_visc! takes eps_uw (or eps() when it is not finite)
-    eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16 : eps_uw;
-  } else {
-    eps = eps_uw;
+    if (rv) {
+      if (!rv_finite) eps = not_finite(eps_uw) ? 2.220446049250313e-16 : eps_uw;
+      else eps = jl_min(eps_rv, eps_uw);
+    } else if (a.kind == MFT_SRC_RV) {
+      // success_iter == 0: update_visc! takes eps_uw (or eps() when it is not finite)
+      eps = not_finite(eps_uw) ? 2.220446049250313e-16 : eps_uw;
+    } else {
+      eps = eps_uw;
+    }
   }
   if (a.eps) a.eps[i] = eps;
   if (a.t) {
@@ -739,8 +796,14 @@ void launch_lexmax_seg(int nseg, const int64_t* off, int per, int V, const doubl
   MFT_LAUNCH_CHECK();
 }
 
-void launch_eps(const EpsArgs& a, cudaStream_t s) {
-  if (a.n <= 0) return;
+void launch_eps(const EpsArgs& args, cudaStream_t s) {
+  if (args.n <= 0) return;
+  EpsArgs a = args;
+  // host IEEE double arithmetic without contraction: the same values the per-node
+  // products give
+  a.uw_coef = (a.c_uw * 0.5) * a.h;
+  a.uw_adv = a.uw_coef * std::sqrt(a.ax * a.ax + a.ay * a.ay);
+  a.rv_coef = (0.5 * a.c_rv) * (a.h * a.h);
   if (a.du_p32) {
     launch_eps_f32(a, s);
     return;

@@ -183,6 +183,11 @@ struct EpsArgs {
   const int* ctr;
   const int* seg_id;       // ensembles: segment of each node (null: one problem)
   const double* seg_h;     // ensembles: dx_avg per segment; norms hold 2V per segment
+  // Node-independent factors, formed by launch_eps in the kernel's operation order
+  // (one problem only; with seg_h the kernel forms them per node):
+  double uw_coef;          // (c_uw * 0.5) * h
+  double uw_adv;           // advection: uw_coef * sqrt(ax^2 + ay^2)
+  double rv_coef;          // (0.5 * c_rv) * (h * h)
   const double* u;
   const double* du_p;
   const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)

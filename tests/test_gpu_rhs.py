@@ -139,6 +139,43 @@ def test_rhs_residual_viscosity_active(oracle, gpu_lib, cyl, cyl_ops, case):
     _check(semi, ctx, u0, cyl_ops["ops"], CASES[case], hv, g, lap_op=cyl_ops["lap"])
 
 
+@pytest.mark.parametrize("scale", [1e-4, 1e-2, 0.05, 0.5, 5.0])
+def test_viscosity_selection_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, scale):
+    """eps = min(eps_rv, eps_uw) node by node: residual estimates from far below to far
+    above the upwind viscosity, and resting nodes (zero momentum, where the bound on
+    eps_uw from the speed alone is zero).  The kernel decides eps_rv < eps_uw without
+    forming eps_uw where that bound proves it.  Where the oracle takes eps_uw the GPU
+    must too (1e-14: same formula up to an ulp); where it takes eps_rv the GPU value must
+    be the smaller one and match to 1e-11 / scale (the residual |approx_du - du| is
+    ~scale * max|du|, so the rhs! rounding, ~1e-13 of max|du|, cancels into it);
+    near-ties (1e-6) are skipped."""
+    pts = cyl["positions"]
+    n = pts.shape[0]
+    u0 = ic_bumpy(pts)
+    rng = np.random.default_rng(12)
+    rest = rng.choice(n, 40, replace=False)
+    u0[1:3, rest] = 0.0
+    semi0, _ctx0, _, _ = _setup(oracle, gpu_lib, cyl, cyl_ops, "plain")
+    du_plain = semi0.rhs(u0.copy(), 0.0)
+    approx = np.ascontiguousarray(du_plain + scale * np.abs(du_plain).max(axis=1, keepdims=True)
+                                  * rng.standard_normal(du_plain.shape))
+    semi, ctx, _hv, _g = _setup(oracle, gpu_lib, cyl, cyl_ops, "rv", success_iter=2,
+                                approx_du=approx)
+    semi_uw, _c, _, _ = _setup(oracle, gpu_lib, cyl, cyl_ops, "upwind")
+    _du_ref, eps_ref = semi.rhs(u0.copy(), 0.0, want_eps=True)
+    _du_uw, eps_uw = semi_uw.rhs(u0.copy(), 0.0, want_eps=True)
+    du = np.empty_like(u0)
+    ctx.rhs(du, u0.copy(), 0.0)
+    eps_gpu = ctx.viscosity()
+    took_uw = eps_ref == eps_uw
+    tie = np.abs(eps_ref - eps_uw) <= 1e-6 * eps_uw
+    a, b = took_uw & ~tie, ~took_uw & ~tie
+    assert np.allclose(eps_gpu[a], eps_uw[a], rtol=1e-14, atol=0)
+    assert np.all(eps_gpu[b] < eps_uw[b])
+    assert np.allclose(eps_gpu[b], eps_ref[b], rtol=1e-11 / scale, atol=0)
+    assert b.sum() > 0 or scale >= 5.0
+
+
 @pytest.mark.parametrize("case", ["plain", "rv", "upwind", "tominec", "rv_tominec"])
 def test_rhs_advection_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, case):
     pts = cyl["positions"]
