@@ -32,7 +32,15 @@ namespace mft {
 
 namespace {
 
-constexpr int kWarpsPerBlock = 2;
+constexpr int kWarpsPerBlock = 2;  // systems per block with one warp per system
+// Buckets of systems larger than kMultiWarpMinN share kSystemWarps warps per system: their
+// packed matrices limit an SM to a few systems, and one warp each leaves the FP64 pipe
+// idle behind shared-memory and reduction latencies.  Measured on the 1M-stencil batch
+// (2D k 35/40-60, 3D k 60-90): one warp everywhere 498 ms; two warps above n = 64
+// 482 ms; four warps above n = 64 512 ms (the block barriers of every column step cost
+// more than the added warps recover); several warps for the 2D buckets 611-879 ms.
+constexpr int kSystemWarps = 2;
+constexpr int kMultiWarpMinN = 64;
 constexpr unsigned kFull = 0xffffffffu;
 
 // One batch of stencils sharing dimension, basis and derivative order.
@@ -125,6 +133,54 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// Synchronisation of the threads that share one system: the warp (W == 1) or the block.
+template <int W>
+__device__ __forceinline__ void gsync() {
+  if (W == 1) __syncwarp();
+  else __syncthreads();
+}
+
+// warp_argmax over the W warps of a block (red_v, red_i: W-entry shared scratch); every
+// thread of the block must call it.  The warps' candidates combine with the same rule
+// (larger value, then smaller index), so the result is the single-warp one.
+template <int W>
+__device__ __forceinline__ void group_argmax(double& v, int& i, int lo, double* red_v,
+                                             int* red_i) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_xor_sync(kFull, v, o);
+    const int i2 = __shfl_xor_sync(kFull, i, o);
+    if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+  }
+  if (W > 1) {
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { red_v[w] = v; red_i[w] = i; }
+    __syncthreads();
+    v = red_v[0];
+    i = red_i[0];
+    for (int q = 1; q < W; ++q) {
+      const double v2 = red_v[q];
+      const int i2 = red_i[q];
+      if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+    }
+    __syncthreads();
+  }
+  if (i == (1 << 30)) { i = lo; v = NAN; }
+}
+
+template <int W>
+__device__ __forceinline__ double group_max(double v, double* red_v) {
+  v = warp_max(v);
+  if (W > 1) {
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red_v[w] = v;
+    __syncthreads();
+    v = red_v[0];
+    for (int q = 1; q < W; ++q) v = fmax(v, red_v[q]);
+    __syncthreads();
+  }
+  return v;
+}
+
 // Advances (i, j), 0 <= i <= j, to the next element a warp stride further along the
 // column-major upper triangle (t = j(j+1)/2 + i).
 __device__ __forceinline__ void tri_next(int& i, int& j, int step) {
@@ -143,17 +199,26 @@ __host__ __device__ __forceinline__ size_t weights_smem_doubles(int nmax, int km
 
 // kOrdered: systems are taken in the order of a.order_list (largest first); otherwise
 // in node order.
-template <bool kOrdered>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
+template <bool kOrdered, int W>
+__global__ void __launch_bounds__(W == 1 ? 32 * kWarpsPerBlock : 32 * W) k_weights(WArgs a) {
   extern __shared__ double smem[];
+  // W == 1: one warp per system, kWarpsPerBlock systems per block.  W > 1: the W warps
+  // of a block share one system (large systems: more warps per SM than the per-system
+  // shared memory would otherwise allow); the factorisation's element loops and
+  // reductions span the block, the triangular solves run in warp 0.
+  constexpr int G = 32 * W;  // threads per system
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
+  const int gt = W == 1 ? lane : (int)threadIdx.x;
   const int nmax = a.nmax;
-  // per-warp shared layout: A[nmax(nmax+1)/2] (upper, packed), B[nmax*3], X[kmax*3],
+  __shared__ double red_v[W];
+  __shared__ int red_i[W];
+  __shared__ unsigned long long s_job;
+  // per-system shared layout: A[nmax(nmax+1)/2] (upper, packed), B[nmax*3], X[kmax*3],
   // TC[nmax], TC2[nmax],
   // ipiv[nmax] (ints)
   const size_t per = weights_smem_doubles(nmax, a.kmax);
-  double* A = smem + per * wib;
+  double* A = smem + per * (W == 1 ? wib : 0);
   double* B = A + (size_t)nmax * (nmax + 1) / 2;
   double* X = B + (size_t)nmax * 3;
   double* TC = X + (size_t)a.kmax * 3;
@@ -161,8 +226,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
   int* ipiv = reinterpret_cast<int*>(TC2 + nmax);
   for (;;) {
     unsigned long long job = 0;
-    if (lane == 0) job = atomicAdd(a.next, 1ull);
-    job = __shfl_sync(kFull, job, 0);
+    if (W == 1) {
+      if (lane == 0) job = atomicAdd(a.next, 1ull);
+      job = __shfl_sync(kFull, job, 0);
+    } else {
+      __syncthreads();  // every thread is done with the previous system
+      if (gt == 0) s_job = atomicAdd(a.next, 1ull);
+      __syncthreads();
+      job = s_job;
+    }
     if (job >= (unsigned long long)a.nsys) break;
     const int64_t code = kOrdered ? a.order_list[job] : (int64_t)job;
     const int grp = (int)(code >> kGroupShift);
@@ -182,34 +254,34 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
 #define BM(i, c) B[(size_t)(c) * n + ((i)-1)]
     if (!kOrdered && k > a.kmax) {
       // caller-declared maximum stencil size exceeded: flag it and skip the system
-      if (lane == 0) atomicExch(reinterpret_cast<int*>(a.next + 2), 1);
+      if (gt == 0) atomicExch(reinterpret_cast<int*>(a.next + 2), 1);
       continue;
     }
     const int32_t* st = cols + rb;
     const int64_t ce = st[0];
     // shift_stencil
-    for (int j = lane; j < k; j += 32)
+    for (int j = gt; j < k; j += G)
       for (int d = 0; d < dim; ++d) {
         double t = dsub(xyz[(int64_t)st[j] * dim + d], xyz[ce * dim + d]);
         if (periodic) t = min_image(t, a.g[grp].period[d]);
         X[j * 3 + d] = t;
       }
-    __syncwarp();
+    gsync<W>();
     double s[3] = {1.0, 1.0, 1.0};
     for (int d = 0; d < dim; ++d) {
       double m = 0.0;
-      for (int j = lane; j < k; j += 32) m = fmax(m, fabs(X[j * 3 + d]));
-      m = warp_max(m);
+      for (int j = gt; j < k; j += G) m = fmax(m, fabs(X[j * 3 + d]));
+      m = group_max<W>(m, red_v);
       s[d] = ddiv(1.0, m);
     }
-    for (int j = lane; j < k; j += 32)
+    for (int j = gt; j < k; j += G)
       for (int d = 0; d < dim; ++d) X[j * 3 + d] = dmul(X[j * 3 + d], s[d]);
-    __syncwarp();
+    gsync<W>();
     // interpolation block (upper triangle, column-major)
     const int T = n * (n + 1) / 2;
     int r = 0, cidx = 0;
-    tri_next(r, cidx, lane);
-    for (int t = lane; t < T; t += 32, tri_next(r, cidx, 32)) {
+    tri_next(r, cidx, gt);
+    for (int t = gt; t < T; t += G, tri_next(r, cidx, G)) {
       double v;
       if (cidx < k) {
         double d2 = 0.0;
@@ -228,7 +300,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
       A[((cidx * (cidx + 1)) >> 1) + r] = v;
     }
     // right-hand sides
-    for (int t = lane; t < n * dim; t += 32) {
+    for (int t = gt; t < n * dim; t += G) {
       const int d = t / n, j = t % n;
       double v;
       if (j < k) {
@@ -247,7 +319,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
       }
       B[(size_t)d * n + j] = v;
     }
-    __syncwarp();
+    gsync<W>();
 
     // ---------------- Bunch-Kaufman factorisation (upper)
     const double alpha = (1.0 + sqrt(17.0)) / 8.0;
@@ -261,11 +333,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
       if (kk > 1) {
         double v = -1.0;
         int iv = 1 << 30;
-        for (int i = 1 + lane; i < kk; i += 32) {
+        for (int i = 1 + gt; i < kk; i += G) {
           const double x = fabs(AM(i, kk));
           if (x > v) { v = x; iv = i; }
         }
-        warp_argmax(v, iv, 1);
+        group_argmax<W>(v, iv, 1, red_v, red_i);
         colmax = v;
         imax = iv;
       }
@@ -278,56 +350,59 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
         } else {
           double v = -1.0;
           int iv = 1 << 30;
-          for (int j = imax + 1 + lane; j <= kk; j += 32) {
+          for (int j = imax + 1 + gt; j <= kk; j += G) {
             const double x = fabs(AM(imax, j));
             if (x > v) { v = x; iv = j; }
           }
-          warp_argmax(v, iv, 1);
+          group_argmax<W>(v, iv, 1, red_v, red_i);
           double rowmax = v;
           if (imax > 1) {
             double v2 = -1.0;
             int iv2 = 1 << 30;
-            for (int j = 1 + lane; j < imax; j += 32) {
+            for (int j = 1 + gt; j < imax; j += G) {
               const double x = fabs(AM(j, imax));
               if (x > v2) { v2 = x; iv2 = j; }
             }
-            warp_argmax(v2, iv2, 1);
+            group_argmax<W>(v2, iv2, 1, red_v, red_i);
             rowmax = fmax(rowmax, v2);
           }
           if (absakk >= alpha * colmax * (colmax / rowmax)) kp = kk;
           else if (fabs(AM(imax, imax)) >= alpha * rowmax) kp = imax;
           else { kp = imax; kstep = 2; }
         }
+        // every thread has read the pivot candidates (A(imax, imax) above) before the
+        // interchange below overwrites them
+        gsync<W>();
         const int kkk = kk - kstep + 1;
         if (kp != kkk) {
-          for (int i = 1 + lane; i < kp; i += 32) {
+          for (int i = 1 + gt; i < kp; i += G) {
             const double t = AM(i, kkk); AM(i, kkk) = AM(i, kp); AM(i, kp) = t;
           }
-          for (int j = kp + 1 + lane; j < kkk; j += 32) {
+          for (int j = kp + 1 + gt; j < kkk; j += G) {
             const double t = AM(j, kkk); AM(j, kkk) = AM(kp, j); AM(kp, j) = t;
           }
-          if (lane == 0) {
+          if (gt == 0) {
             double t = AM(kkk, kkk); AM(kkk, kkk) = AM(kp, kp); AM(kp, kp) = t;
             if (kstep == 2) { t = AM(kk - 1, kk); AM(kk - 1, kk) = AM(kp, kk); AM(kp, kk) = t; }
           }
-          __syncwarp();
+          gsync<W>();
         }
         if (kstep == 1) {
           const double r1 = ddiv(1.0, AM(kk, kk));
           // column multipliers temp_j = -r1 x_j (dsyr), then A(i,j) += A(i,kk) temp_j
           // for x_j != 0, one fused multiply-add per element
-          for (int j = lane; j < kk - 1; j += 32) TC[j] = dmul(-r1, AM(j + 1, kk));
-          __syncwarp();
+          for (int j = gt; j < kk - 1; j += G) TC[j] = dmul(-r1, AM(j + 1, kk));
+          gsync<W>();
           const int Tu = (kk - 1) * kk / 2;
           int i0 = 0, j0 = 0;
-          tri_next(i0, j0, lane);
-          for (int t = lane; t < Tu; t += 32, tri_next(i0, j0, 32)) {
+          tri_next(i0, j0, gt);
+          for (int t = gt; t < Tu; t += G, tri_next(i0, j0, G)) {
             if (AM(j0 + 1, kk) != 0.0)
               AM(i0 + 1, j0 + 1) = fma(AM(i0 + 1, kk), TC[j0], AM(i0 + 1, j0 + 1));
           }
-          __syncwarp();
-          for (int i = 1 + lane; i < kk; i += 32) AM(i, kk) = dmul(r1, AM(i, kk));
-          __syncwarp();
+          gsync<W>();
+          for (int i = 1 + gt; i < kk; i += G) AM(i, kk) = dmul(r1, AM(i, kk));
+          gsync<W>();
         } else if (kk > 2) {
           const double d12o = AM(kk - 1, kk);
           const double d22 = ddiv(AM(kk - 1, kk - 1), d12o);
@@ -338,43 +413,45 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
           // A(i,j) -= A(i,kk) wk + A(i,kk-1) wkm1 as two fused multiply-adds, then
           // columns kk-1, kk take wkm1, wk (dsytf2 order: each update reads only
           // rows i <= j, which the column overwrite has not reached)
-          for (int j = lane; j < kk - 2; j += 32) {
+          for (int j = gt; j < kk - 2; j += G) {
             const double a1 = AM(j + 1, kk - 1), a2 = AM(j + 1, kk);
             TC[j] = dmul(d12, dsub(dmul(d11, a1), a2));
             TC2[j] = dmul(d12, dsub(dmul(d22, a2), a1));
           }
-          __syncwarp();
+          gsync<W>();
           const int Tu = (kk - 2) * (kk - 1) / 2;
           int i0 = 0, j0 = 0;
-          tri_next(i0, j0, lane);
-          for (int t = lane; t < Tu; t += 32, tri_next(i0, j0, 32)) {
+          tri_next(i0, j0, gt);
+          for (int t = gt; t < Tu; t += G, tri_next(i0, j0, G)) {
             const int j = j0 + 1, i = i0 + 1;
             AM(i, j) = fma(-AM(i, kk - 1), TC[j0], fma(-AM(i, kk), TC2[j0], AM(i, j)));
           }
-          __syncwarp();
-          for (int j = lane; j < kk - 2; j += 32) {
+          gsync<W>();
+          for (int j = gt; j < kk - 2; j += G) {
             AM(j + 1, kk) = TC2[j];
             AM(j + 1, kk - 1) = TC[j];
           }
-          __syncwarp();
+          gsync<W>();
         }
       }
-      if (lane == 0) {
+      if (gt == 0) {
         if (kstep == 1) ipiv[kk - 1] = kp;
         else { ipiv[kk - 1] = -kp; ipiv[kk - 2] = -kp; }
       }
-      __syncwarp();
+      gsync<W>();
       kk -= kstep;
     }
 
     if (info != 0) {
-      if (lane == 0) atomicMin(a.bad, (int)e);
-      for (int t = lane; t < k * dim; t += 32) w_out[(rb + t / dim) * dim + t % dim] = NAN;
-      if (resid && lane == 0) resid[e] = NAN;
-      __syncwarp();
+      if (gt == 0) atomicMin(a.bad, (int)e);
+      for (int t = gt; t < k * dim; t += G) w_out[(rb + t / dim) * dim + t % dim] = NAN;
+      if (resid && gt == 0) resid[e] = NAN;
+      gsync<W>();
       continue;
     }
 
+    gsync<W>();  // factorisation complete and visible to the solving warp
+    if (W == 1 || wib == 0) {
     // ---------------- solve (dsytrs, upper), columns independent
     const int nrhs = dim;
     kk = n;
@@ -504,6 +581,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_weights(WArgs a) {
       if (lane == 0) resid[e] = worst;
     }
     __syncwarp();
+    }
 #undef AM
 #undef BM
   }
@@ -587,7 +665,8 @@ static void weights_run(cudaStream_t s, const std::vector<HostGroup>& gs, double
   std::vector<int64_t> order_sorted(order.size());
   for (size_t q = 0; q < perm.size(); ++q) order_sorted[q] = order[perm[q]];
   (void)kmax;
-  MFT_REQUIRE(weights_smem_doubles(nmax, nmax) * sizeof(double) * kWarpsPerBlock <= 227 * 1024,
+  MFT_REQUIRE(weights_smem_doubles(nmax, nmax) * sizeof(double) * kWarpsPerBlock <=
+                  227 * 1024 - 256,
               MFT_ERR_ARG, "stencil too large for the weight kernel");
   // buckets: [begin, end) ranges of the sorted list with their largest n and k
   struct Bucket { int64_t begin, end; int nmax, kmax; };
@@ -633,8 +712,6 @@ static void weights_run(cudaStream_t s, const std::vector<HostGroup>& gs, double
   int dev = 0, sms = 0;
   MFT_CUDA(cudaGetDevice(&dev));
   MFT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  MFT_CUDA(cudaFuncSetAttribute(k_weights<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                227 * 1024));
   for (size_t b = 0; b < buckets.size(); ++b) {
     const Bucket& bk = buckets[b];
     WArgs ab = a;
@@ -643,15 +720,29 @@ static void weights_run(cudaStream_t s, const std::vector<HostGroup>& gs, double
     ab.nsys = bk.end - bk.begin;
     ab.order_list = d_order.p + bk.begin;
     ab.next = d_next.p + b;
-    const size_t shmem = weights_smem_doubles(bk.nmax, bk.kmax) * sizeof(double) * kWarpsPerBlock;
+    const bool multi = bk.nmax > kMultiWarpMinN;
+    const int spb = multi ? 1 : kWarpsPerBlock;  // systems per block
+    const int threads = multi ? 32 * kSystemWarps : 32 * kWarpsPerBlock;
+    const size_t shmem = weights_smem_doubles(bk.nmax, bk.kmax) * sizeof(double) * spb;
+    // the opt-in dynamic shared memory this bucket needs (the static part is small)
     int per_sm = 0;
-    MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<true>,
-                                                           32 * kWarpsPerBlock, shmem));
+    if (multi) {
+      MFT_CUDA(cudaFuncSetAttribute(k_weights<true, kSystemWarps>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
+      MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, k_weights<true, kSystemWarps>, threads, shmem));
+    } else {
+      MFT_CUDA(cudaFuncSetAttribute(k_weights<true, 1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
+      MFT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<true, 1>,
+                                                             threads, shmem));
+    }
     per_sm = std::max(per_sm, 1);
-    const int64_t want = (ab.nsys + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const int64_t want = (ab.nsys + spb - 1) / spb;
     const unsigned grid =
         (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
-    k_weights<true><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(ab);
+    if (multi) k_weights<true, kSystemWarps><<<grid, threads, shmem, s>>>(ab);
+    else k_weights<true, 1><<<grid, threads, shmem, s>>>(ab);
     MFT_LAUNCH_CHECK();
   }
   int bad = big;
@@ -833,10 +924,10 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   a.bad = reinterpret_cast<int*>(scratch + 1);
   a.next = scratch;
   int sms = 0, per_sm = 0;
-  if (cudaFuncSetAttribute(k_weights<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(k_weights<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)shmem) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<false>,
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_weights<false, 1>,
                                                     32 * kWarpsPerBlock, shmem) != cudaSuccess) {
     put_err(err, err_len, "mft_weights_noalloc: kernel configuration failed");
     return MFT_ERR_CUDA;
@@ -845,7 +936,7 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   const int64_t want = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
   const unsigned grid =
       (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, want));
-  k_weights<false><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
+  k_weights<false, 1><<<grid, 32 * kWarpsPerBlock, shmem, s>>>(a);
   cudaError_t e = cudaGetLastError();
   int status[3] = {0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status[0], scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
