@@ -265,6 +265,9 @@ __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __rest
   double acc[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) acc[k] = 0.0;
+  // unrolled so that four nodes' loads are in flight together; the additions keep the
+  // node order of the plain grid-stride loop
+#pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kBlock) {
 #pragma unroll
@@ -283,6 +286,7 @@ __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __rest
   __threadfence();
 #pragma unroll
   for (int k = 0; k < V; ++k) acc[k] = 0.0;
+#pragma unroll 4
   for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock)
 #pragma unroll
     for (int k = 0; k < V; ++k) acc[k] += __ldcg(partial + b * V + k);
@@ -349,6 +353,7 @@ __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __re
   for (int k = 0; k < V; ++k) { m[k] = mean[k]; best[k] = 0ull; }
   // Threads without nodes keep the all-zero key, the smallest possible: it can only
   // tie with a real all-zero vector, which has the same value.
+#pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kBlock) {
     u64 x[V];
@@ -369,6 +374,7 @@ __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __re
   __threadfence();
 #pragma unroll
   for (int k = 0; k < V; ++k) best[k] = 0ull;
+#pragma unroll 4
   for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock) {
     u64 c[V];
 #pragma unroll
