@@ -35,7 +35,7 @@ N_SIDE = 512
 K_STENCIL = 35
 DT_FACTOR = 0.2          # dt = 0.2 h
 RHS_PER_STEP = 3
-DFMA_PEAK_GFMA = 505.1   # measured FP64 FMA rate of this GB300 (probe in profiles/)
+DFMA_PEAK_GFMA = 528.3   # measured FP64 FMA rate of this GB300 (probe in profiles/)
 
 # Algorithmic bytes per node and launch (FP64 form, V=4, D=2, k=35, int32 indices):
 #   fwd_gather: idx 4k + weights 2*8k + state read 32 + du_p write 32 + t=Du write 64

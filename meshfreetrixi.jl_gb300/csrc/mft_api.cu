@@ -459,6 +459,8 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   ep.bc = bc;
   ep.has_bc = c->nb > 0;
   ep.u_s = us;
+  ep.fused = f32 ? 1 : 0;
+  ep.cdt = ep.kind == kStage2 ? 0.25 * ep.dt : ep.kind == kStage3 ? (2.0 / 3.0) * ep.dt : ep.dt;
 
   // 1. strong BCs, pass 1 (mutates u)
   if (c->nb > 0) {
@@ -653,6 +655,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ea.h = kind == MFT_SRC_RV ? par[2] : par[1];
     ea.success_iter = c->success_iter;
     ea.u = us;
+    ea.u32 = f32 ? us32 : nullptr;
     ea.du_p = f32 ? nullptr : dp;
     ea.du_p32 = f32 ? dp32 : nullptr;
     ea.hvf = nullptr;

@@ -810,6 +810,11 @@ void launch_eps(const EpsArgs& args, cudaStream_t s) {
   a.uw_coef = (a.c_uw * 0.5) * a.h;
   a.uw_adv = a.uw_coef * std::sqrt(a.ax * a.ax + a.ay * a.ay);
   a.rv_coef = (0.5 * a.c_rv) * (a.h * a.h);
+  const float h32 = (float)a.h;
+  a.gamma32 = (float)a.gamma;
+  a.gm1_32 = (float)(a.gamma - 1.0);
+  a.uw_coef32 = ((float)a.c_uw * 0.5f) * h32;
+  a.rv_coef32 = ((0.5f * (float)a.c_rv) * h32) * h32;
   if (a.du_p32) {
     launch_eps_f32(a, s);
     return;

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
   const float* __restrict__ wyp = a.w32[1];
   const float* __restrict__ wlp = a.wl32;
   const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
-  const float gm1 = (float)(a.gamma - 1.0);
+  const float gm1 = a.gm1_32;
   float f[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
 #pragma unroll 4
   for (int j = 0; j < len; ++j) {
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
       q[2] = fmaf(wl, uc.z, q[2]); q[3] = fmaf(wl, uc.w, q[3]);
     }
   }
-  const float hg = (float)a.hv_gamma;
+  const float hg = a.hg32;
   if (WT) f[0] = tx[1] + ty[2];
   float du[4] = {-f[0], -f[1], -f[2], -f[3]};
   if (FLY == 1)
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kBlock) k_fwd_adv_f32(FwdArgs a) {
     if (WT) { tx = fmaf(wx, uc, tx); ty = fmaf(wy, uc, ty); }
     if (WQ || FLY) q = fmaf(__ldg(a.wl32 + p), uc, q);
   }
-  const float hg = (float)a.hv_gamma;
+  const float hg = a.hg32;
   float du = -f;
   if (FLY == 1) du = fmaf(-hg, q, du);
   if (WT) { a.t32[i * 2] = tx; a.t32[i * 2 + 1] = ty; }
@@ -98,22 +98,34 @@ __global__ void __launch_bounds__(kBlock) k_fwd_adv_f32(FwdArgs a) {
 // FP64 history and reductions.
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
+  // FP64 -> FP32 conversions run on the FP64 pipe of this part: the state comes from its
+  // FP32 shadow (the same rounded values), the node-independent factors from the launch
+  // and, for one problem, the norms' reciprocals are converted once per block.
+  __shared__ float s_rnorm[V];
+  if (!a.seg_id && threadIdx.x < V) s_rnorm[threadIdx.x] = (float)a.norms[V + threadIdx.x];
+  __syncthreads();
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= a.n) return;
   const int sg = a.seg_id ? a.seg_id[i] : 0;
-  const float h = (float)(a.seg_h ? a.seg_h[sg] : a.h);
-  const double* __restrict__ norms = a.norms + (a.seg_id ? sg * 2 * V : 0);
+  const float h = a.seg_h ? (float)a.seg_h[sg] : (float)a.h;
   float eps_uw;
   if (V == 4) {
-    const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
-    const double2 ub = reinterpret_cast<const double2*>(a.u)[i * 2 + 1];
-    const float rho = (float)ua.x, m1 = (float)ua.y, m2 = (float)ub.x, en = (float)ub.y;
+    float rho, m1, m2, en;
+    if (a.u32) {
+      const float4 q = reinterpret_cast<const float4*>(a.u32)[i];
+      rho = q.x; m1 = q.y; m2 = q.z; en = q.w;
+    } else {
+      const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
+      const double2 ub = reinterpret_cast<const double2*>(a.u)[i * 2 + 1];
+      rho = (float)ua.x; m1 = (float)ua.y; m2 = (float)ub.x; en = (float)ub.y;
+    }
     const float r = __frcp_rn(rho);
     const float v1 = m1 * r, v2 = m2 * r;
-    const float p = (float)(a.gamma - 1.0) * (en - 0.5f * (m1 * v1 + m2 * v2));
+    const float p = a.gm1_32 * (en - 0.5f * (m1 * v1 + m2 * v2));
     const float speed = sqrtf(v1 * v1 + v2 * v2);
-    const float c = (p < 0.0f || rho < 0.0f) ? 0.0f : sqrtf((float)a.gamma * p * r);
-    eps_uw = (float)a.c_uw * 0.5f * h * (speed + c);
+    const float c = (p < 0.0f || rho < 0.0f) ? 0.0f : sqrtf(a.gamma32 * p * r);
+    const float uwc = a.seg_h ? (float)a.c_uw * 0.5f * h : a.uw_coef32;
+    eps_uw = uwc * (speed + c);
   } else {
     eps_uw = (float)a.c_uw * 0.5f * h * (float)sqrt(a.ax * a.ax + a.ay * a.ay);
   }
@@ -138,11 +150,13 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
       float dp = dpv[v];
       if (a.hvf) dp += (float)a.hvf[i * V + v];
       const float r = fabsf(adv[v] - dp);
-      const float qv = r * (float)norms[V + v];
+      const float rn = a.seg_id ? (float)a.norms[sg * 2 * V + V + v] : s_rnorm[v];
+      const float qv = r * rn;
       mr = v == 0 ? qv : fmaxf(mr, qv);
       if (isnan(qv)) mr = qv;
     }
-    const float eps_rv = 0.5f * (float)a.c_rv * h * h * mr;
+    const float rvc = a.seg_h ? 0.5f * (float)a.c_rv * h * h : a.rv_coef32;
+    const float eps_rv = rvc * mr;
     const int si = a.tab ? a.tab[*a.ctr].si_eps : a.success_iter;
     if (isnan(eps_rv) || isinf(eps_rv) || si == 0)
       eps = (isnan(eps_uw) || isinf(eps_uw)) ? 2.220446049250313e-16f : eps_uw;
@@ -204,7 +218,7 @@ __global__ void __launch_bounds__(kBlock) k_rev_f32(RevArgs a) {
       }
     }
   }
-  const float hg = (float)a.hv_gamma;
+  const float hg = a.hg32;
   float du[V];
   const float* dp32 = a.du_p32;
 #pragma unroll
@@ -231,8 +245,11 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 
 }  // namespace
 
-void launch_fwd_f32(const FwdArgs& a, cudaStream_t s) {
-  if (a.n <= 0) return;
+void launch_fwd_f32(const FwdArgs& args, cudaStream_t s) {
+  if (args.n <= 0) return;
+  FwdArgs a = args;
+  a.gm1_32 = (float)(a.gamma - 1.0);
+  a.hg32 = (float)a.hv_gamma;
   MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
               "Flyer and Tominec hyperviscosity together are not supported");
   const unsigned g = grid_for(a.n, kBlock);
@@ -265,8 +282,10 @@ void launch_eps_f32(const EpsArgs& a, cudaStream_t s) {
   MFT_LAUNCH_CHECK();
 }
 
-void launch_rev_f32(const RevArgs& a, cudaStream_t s) {
-  if (a.n <= 0) return;
+void launch_rev_f32(const RevArgs& args, cudaStream_t s) {
+  if (args.n <= 0) return;
+  RevArgs a = args;
+  a.hg32 = (float)a.hv_gamma;
   const unsigned g = grid_for(a.n, kBlock);
   if (a.V == 4) {
     if (a.rv && a.lap) k_rev_f32<4, true, true><<<g, kBlock, 0, s>>>(a);

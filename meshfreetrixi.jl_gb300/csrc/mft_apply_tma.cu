@@ -94,8 +94,8 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
   }
   __syncwarp();
   const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
-  const float gm1 = (float)(a.gamma - 1.0);
-  const float hg = (float)a.hv_gamma;
+  const float gm1 = a.gm1_32;
+  const float hg = a.hg32;
   uint32_t phase[2] = {0u, 0u};
   bool pending[2] = {false, false};
   Cursor iss{first, 0};
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
   }
   __syncwarp();
   const float4* __restrict__ Q4 = reinterpret_cast<const float4*>(a.q32);
-  const float hg = (float)a.hv_gamma;
+  const float hg = a.hg32;
   uint32_t phase[2] = {0u, 0u};
   bool pending[2] = {false, false};
   Cursor iss{first, 0};
@@ -373,16 +373,21 @@ static void rev_tma(const RevArgs& a, int* err, cudaStream_t s) {
     k_rev_f32_tma<CH, false, true><<<persistent_grid(k_rev_f32_tma<CH, false, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
 }
 
-bool launch_fwd_f32_tma(const FwdArgs& a, int chunk, int* err, cudaStream_t s) {
-  if (a.V != 4 || a.n <= 0) return false;
+bool launch_fwd_f32_tma(const FwdArgs& args, int chunk, int* err, cudaStream_t s) {
+  if (args.V != 4 || args.n <= 0) return false;
+  FwdArgs a = args;
+  a.gm1_32 = (float)(a.gamma - 1.0);
+  a.hg32 = (float)a.hv_gamma;
   if (chunk <= 4) fwd_tma<4>(a, err, s);
   else fwd_tma<8>(a, err, s);
   MFT_LAUNCH_CHECK();
   return true;
 }
 
-bool launch_rev_f32_tma(const RevArgs& a, int chunk, int* err, cudaStream_t s) {
-  if (a.V != 4 || a.n <= 0 || (!a.rv && !a.lap)) return false;
+bool launch_rev_f32_tma(const RevArgs& args, int chunk, int* err, cudaStream_t s) {
+  if (args.V != 4 || args.n <= 0 || (!args.rv && !args.lap)) return false;
+  RevArgs a = args;
+  a.hg32 = (float)a.hv_gamma;
   if (chunk <= 4) rev_tma<4>(a, err, s);
   else rev_tma<8>(a, err, s);
   MFT_LAUNCH_CHECK();

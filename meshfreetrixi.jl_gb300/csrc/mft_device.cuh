@@ -121,7 +121,20 @@ static __device__ __forceinline__ void finish_node(const Epilogue& ep, int64_t i
     }
   }
   double o[V];
-  switch (ep.kind) {
+  if (ep.fused && ep.kind != kOutDu) {
+    // FP32-apply form: u1 = us + dt du; u2 = (3 un + us)/4 + (dt/4) du;
+    // u3 = un/3 + (2/3) us + (2dt/3) du as fused multiply-adds
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      if (ep.kind == kStage1) {
+        o[v] = fma(ep.dt, du[v], us[v]);
+      } else if (ep.kind == kStage2) {
+        o[v] = fma(ep.cdt, du[v], fma(0.75, ep.u_n[i * V + v], 0.25 * us[v]));
+      } else {
+        o[v] = fma(ep.cdt, du[v], fma(2.0 / 3.0, us[v], ep.u_n[i * V + v] * (1.0 / 3.0)));
+      }
+    }
+  } else switch (ep.kind) {
     case kOutDu:
 #pragma unroll
       for (int v = 0; v < V; ++v) o[v] = du[v];

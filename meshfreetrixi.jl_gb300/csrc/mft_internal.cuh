@@ -114,6 +114,11 @@ struct Epilogue {
   BcDev bc;
   int has_bc;
   const double* xadd; // n x 2 additions to the momentum rows (IGR source) or null
+  // FP32-apply form: the stage combination as fused multiply-adds (within an ulp of the
+  // FP64 form's separately rounded formulas, half the FP64 operations); cdt is dt / 4
+  // (stage 2) or 2 dt / 3 (stage 3)
+  int fused;
+  double cdt;
 };
 
 // ------------------------------------------------------------------ launchers
@@ -151,6 +156,7 @@ struct FwdArgs {
   int eq, V;
   double gamma, ax, ay;
   double hv_gamma;      // Flyer: du += -gamma * H u
+  float gm1_32, hg32;   // (float)(gamma - 1), (float) hv_gamma (FP32 kernels; set by the launchers)
   int want_t;           // write t = D u (n x 2V)
   int want_q;           // write q = lap u (n x V) (Tominec)
   int flyer;            // Flyer H in wl: 0 none, 1 add into du_p, 2 write hvf separately
@@ -188,6 +194,12 @@ struct EpsArgs {
   double uw_coef;          // (c_uw * 0.5) * h
   double uw_adv;           // advection: uw_coef * sqrt(ax^2 + ay^2)
   double rv_coef;          // (0.5 * c_rv) * (h * h)
+  // FP32 form: the FP32 shadow of u and the FP32 factors, formed by launch_eps in the
+  // FP32 kernel's operation order
+  const float* u32;
+  float gamma32, gm1_32;   // (float) gamma, (float)(gamma - 1)
+  float uw_coef32;         // ((float) c_uw * 0.5f) * (float) h
+  float rv_coef32;         // ((0.5f * (float) c_rv) * (float) h) * (float) h
   const double* u;
   const double* du_p;
   const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)
@@ -217,6 +229,7 @@ struct RevArgs {
   int rv;             // gather s = eps*D u over the reverse adjacency
   int lap;            // gather q = lap u over the reverse adjacency (Tominec)
   double hv_gamma;
+  float hg32;           // (float) hv_gamma (FP32 kernels; set by the launchers)
   const double* s;    // n x 2V
   const double* q;    // n x V
   const float* s32;

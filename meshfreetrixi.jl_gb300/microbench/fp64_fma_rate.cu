@@ -24,14 +24,18 @@ __global__ void ffma_k(float* out, float a, float b, int iters) {
   float s = 0; for (int i = 0; i < ILP; ++i) s += x[i];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+// F2F.F32.F64: every iteration converts a different value (the last mantissa bit of each
+// chain flips by an integer XOR, which no FP64 operation or hoisting can replace).
 template <int ILP>
 __global__ void cvt_k(float* out, double a, int iters) {
   double x[ILP]; float y[ILP];
-  for (int i = 0; i < ILP; ++i) { x[i] = threadIdx.x * 1e-3 + i; y[i] = 0.f; }
+  for (int i = 0; i < ILP; ++i) { x[i] = threadIdx.x * 1e-3 + i + a; y[i] = 0.f; }
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
-    for (int i = 0; i < ILP; ++i) { y[i] += __double2float_rn(x[i]); }
-    x[0] += a;
+    for (int i = 0; i < ILP; ++i) {
+      y[i] += __double2float_rn(x[i]);
+      x[i] = __longlong_as_double(__double_as_longlong(x[i]) ^ 1ll);
+    }
   }
   float s = 0; for (int i = 0; i < ILP; ++i) s += y[i];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
@@ -60,7 +64,7 @@ int main() {
     cudaEventRecord(e0); cvt_k<8><<<blocks, threads>>>(fout, 1e-9, iters); cudaEventRecord(e1);
     cudaEventSynchronize(e1); cudaEventElapsedTime(&ms, e0, e1);
     ops = double(blocks) * threads * iters * 8;
-    printf("F2F.F32.F64 (+FADD): %.3f ms  %.1f Gcvt/s per-SM-per-clk %.2f\n", ms, ops / ms / 1e6,
+    printf("F2F.F32.F64 (+FADD, LOP): %.3f ms  %.1f Gcvt/s per-SM-per-clk %.2f\n", ms, ops / ms / 1e6,
            ops / (ms * 1e-3) / p.multiProcessorCount / (clk * 1e3));
   }
   cudaError_t err = cudaDeviceSynchronize();
