@@ -217,6 +217,13 @@ mft_status mft_set_option(mft_ctx* ctx, int option, int value);
  * -1 = not tuned yet). */
 mft_status mft_get_option(mft_ctx* ctx, int option, int* value);
 
+/* Self-test of the bounded-wait error path (no fault involved): one warp waits on a
+ * shared-memory mbarrier that nothing completes, gives up after `polls` polls (1 ..
+ * 1,000,000), records MFT_ERR_TIMEOUT in the device error word and returns; the host
+ * reads the word as every staged gather's caller does.  Returns MFT_ERR_TIMEOUT (the
+ * expected outcome) with the context still usable. */
+mft_status mft_selftest_bounded_wait(mft_ctx* ctx, int polls);
+
 /* ---------------------------------------------------------------- rhs! */
 
 /* du = rhs!(u, t) with host StructArray-style arrays (nvars pointers of length n).

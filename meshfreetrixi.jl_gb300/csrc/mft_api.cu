@@ -1128,6 +1128,19 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
   });
 }
 
+mft_status mft_selftest_bounded_wait(mft_ctx* c, int polls) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(polls >= 1 && polls <= 1000000, MFT_ERR_ARG, "polls must be 1 .. 1000000");
+    set_device(c);
+    if (!c->kerr.p) {
+      c->kerr.alloc(1);
+      c->kerr.zero(c->stream);
+    }
+    launch_wait_selftest(c->kerr.p, (unsigned)polls, c->stream);
+    check_kernel_errors(c);
+  });
+}
+
 mft_status mft_get_option(mft_ctx* c, int option, int* value) {
   return guarded(c, [&] {
     MFT_REQUIRE(value, MFT_ERR_ARG, "value is NULL");

@@ -325,6 +325,19 @@ int resident_blocks(const void* kernel) {
 // Persistent grid: at most one wave of resident blocks, and no more warps than slices.
 // The slices are then spread evenly: with s slices and w warps a warp takes ceil(s / w)
 // of them, so w is lowered to the smallest count with the same ceiling.
+// Error-path self-test: the barrier is initialised and never arrived on, and no bulk copy
+// is issued, so nothing is in flight when the warp gives up.
+__global__ void k_wait_selftest(int* err, uint32_t polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tma::bar_init(&bar, 1);
+    tma::fence_init();
+  }
+  __syncwarp();
+  const bool done = tma::wait_bounded(&bar, 0u, polls);
+  if (!done && threadIdx.x == 0) atomicExch(err, MFT_ERR_TIMEOUT);
+}
+
 template <class K>
 unsigned persistent_grid(K kernel, int64_t n) {
   const int64_t cap = resident_blocks(reinterpret_cast<const void*>(kernel));
@@ -371,6 +384,11 @@ static void rev_tma(const RevArgs& a, int* err, cudaStream_t s) {
     k_rev_f32_tma<CH, true, false><<<persistent_grid(k_rev_f32_tma<CH, true, false>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
   else
     k_rev_f32_tma<CH, false, true><<<persistent_grid(k_rev_f32_tma<CH, false, true>, a.n), 32 * kTmaWarps, 0, s>>>(a, err);
+}
+
+void launch_wait_selftest(int* err, unsigned polls, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(err, polls);
+  MFT_LAUNCH_CHECK();
 }
 
 bool launch_fwd_f32_tma(const FwdArgs& args, int chunk, int* err, cudaStream_t s) {

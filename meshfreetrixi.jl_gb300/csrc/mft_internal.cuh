@@ -248,6 +248,8 @@ void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 // chunk: slots staged per bulk copy (4 or 8).
 bool launch_fwd_f32_tma(const FwdArgs& a, int chunk, int* err, cudaStream_t s);
 bool launch_rev_f32_tma(const RevArgs& a, int chunk, int* err, cudaStream_t s);
+// One warp's bounded wait on an mbarrier that nothing completes (error-path self-test).
+void launch_wait_selftest(int* err, unsigned polls, cudaStream_t s);
 
 // Adjoint of rhs! (reverse mode) and the SSP-RK3 adjoint stage combinations.
 // With r = (d rhs!/du)^T lam at state u and Pi the strong-BC projection:

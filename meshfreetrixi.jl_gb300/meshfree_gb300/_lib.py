@@ -51,6 +51,7 @@ SIGNATURES = {
     "mft_set_option": (I32, [VP, I32, I32]),
     "mft_set_segments": (I32, [VP, I32, VP, VP]),
     "mft_get_option": (I32, [VP, I32, C.POINTER(I32)]),
+    "mft_selftest_bounded_wait": (I32, [VP, I32]),
     "mft_rhs": (I32, [VP, VP, VP, I32, DBL]),
     "mft_rhs_device": (I32, [VP, VP, VP, DBL]),
     "mft_set_state": (I32, [VP, VP, I32, DBL]),
@@ -229,6 +230,11 @@ class Context:
         v = C.c_int()
         self.check(self.lib.mft_get_option(self.h, option, C.byref(v)))
         return v.value
+
+    def selftest_bounded_wait(self, polls=1000):
+        """Runs the bounded-wait self-test; returns its status code (MFT_ERR_TIMEOUT is
+        the expected outcome) without raising."""
+        return int(self.lib.mft_selftest_bounded_wait(self.h, polls))
 
     # rhs! / stepping ----------------------------------------------------
     def rhs(self, du, u, t):

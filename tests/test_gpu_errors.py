@@ -54,3 +54,19 @@ def test_unsupported_combinations(gpu_lib):
     ctx.set_equations(L.EQ_ADVECTION, [1.0, 0.5])
     assert _code(lambda: ctx.set_limiter([0], [0.1])) == L.MFT_ERR_UNSUPPORTED
     ctx.close()
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(gpu_lib):
+    """The error path of the staged gathers' bounded mbarrier waits, without a fault: a
+    warp waits on a barrier that nothing completes, gives up after 1000 polls and the
+    host reads MFT_ERR_TIMEOUT from the device error word; the error word is cleared and
+    the context keeps working."""
+    L, W, ctx, pts = _ctx()
+    assert ctx.selftest_bounded_wait(1000) == L.MFT_ERR_TIMEOUT
+    assert ctx.selftest_bounded_wait(1) == L.MFT_ERR_TIMEOUT
+    assert _code(lambda: ctx.check(ctx.lib.mft_selftest_bounded_wait(ctx.h, 0))) == L.MFT_ERR_ARG
+    u = W.isentropic_vortex(pts, 0.0)
+    du = np.empty_like(u)
+    ctx.rhs(du, u.copy(), 0.0)
+    assert np.isfinite(du).all()
+    ctx.close()
