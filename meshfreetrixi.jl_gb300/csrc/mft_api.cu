@@ -416,11 +416,17 @@ void launch_rev(mft_ctx* c, const RevArgs& a) {
 }
 
 // Device error word set by kernels with bounded waits; read at synchronisation points.
+// Synchronises the stream and reads the word: the word's copy into pinned memory is
+// queued behind the work, so one synchronisation covers both.
 static void check_kernel_errors(mft_ctx* c) {
-  if (!c->kerr.p) return;
-  int e = 0;
-  MFT_CUDA(cudaMemcpyAsync(&e, c->kerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (!c->kerr.p) {
+    MFT_CUDA(cudaStreamSynchronize(c->stream));
+    return;
+  }
+  if (!c->h_kerr) MFT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&c->h_kerr), sizeof(int)));
+  MFT_CUDA(cudaMemcpyAsync(c->h_kerr, c->kerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MFT_CUDA(cudaStreamSynchronize(c->stream));
+  const int e = *c->h_kerr;
   if (e != 0) {
     c->kerr.zero(c->stream);
     MFT_CUDA(cudaStreamSynchronize(c->stream));
@@ -846,6 +852,7 @@ mft_status mft_ctx_destroy(mft_ctx* c) {
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_tab) cudaEventDestroy(c->ev_tab);
   if (c->h_tab) cudaFreeHost(c->h_tab);
+  if (c->h_kerr) cudaFreeHost(c->h_kerr);
   for (auto& p : c->prof_pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
@@ -1221,7 +1228,6 @@ mft_status mft_rhs_device(mft_ctx* c, double* du, double* u, double t) {
     eval_rhs(c, c->work_u.p, u32, t, ep);
     launch_soa_from_aos(c->work_du.p, du, n, V, s);
     launch_soa_from_aos(c->work_u.p, u, n, V, s);
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
   });
 }
@@ -1256,7 +1262,6 @@ mft_status mft_rhs(mft_ctx* c, double* const* du, double* const* u, int nvars, d
       MFT_CUDA(cudaMemcpyAsync(u[v], c->soa2.p + (size_t)v * n, n * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
     }
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
   });
 }
@@ -1518,7 +1523,6 @@ mft_status mft_ssprk33(mft_ctx* c, double dt, int nsteps, int use_graph) {
     MFT_REQUIRE(dt > 0 && isfinite(dt), MFT_ERR_ARG, "dt must be positive and finite");
     set_device(c);
     ssprk33_run(c, dt, nsteps, use_graph != 0);
-    MFT_CUDA(cudaStreamSynchronize(c->stream));
     check_kernel_errors(c);
   });
 }
@@ -1586,7 +1590,6 @@ mft_status mft_ssprk33_host(mft_ctx* c, double* const* u, int nvars, double* t, 
         MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
     }
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
     *t = c->t_state;
   });
@@ -1711,7 +1714,6 @@ mft_status mft_limit(mft_ctx* c, double* const* u, int nvars) {
     for (int v = 0; v < nvars; ++v)
       MFT_CUDA(cudaMemcpyAsync(u[v], c->soa.p + (size_t)v * n, n * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
   });
 }
@@ -1953,7 +1955,6 @@ mft_status mft_rhs_adjoint(mft_ctx* c, double* const* out, const double* const* 
     for (int v = 0; v < V; ++v)
       MFT_CUDA(cudaMemcpyAsync(out[v], c->soa.p + (size_t)v * n, n * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
   });
 }
@@ -1974,7 +1975,6 @@ mft_status mft_rhs_adjoint_device(mft_ctx* c, double* out, const double* lam, co
     launch_aos_from_soa(lam, c->adj_lam[0].p, n, V, s);
     eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p);
     launch_soa_from_aos(c->adj_lam[1].p, out, n, V, s);
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
   });
 }
@@ -1988,7 +1988,6 @@ mft_status mft_ssprk33_record(mft_ctx* c, double dt, int nsteps, int every) {
     check_adjoint_ready(c);
     set_device(c);
     ssprk33_record(c, dt, nsteps, every);
-    MFT_CUDA(cudaStreamSynchronize(c->stream));
     check_kernel_errors(c);
   });
 }
@@ -2007,7 +2006,6 @@ mft_status mft_ssprk33_adjoint(mft_ctx* c, double* const* lam, int nvars) {
     for (int v = 0; v < nvars; ++v)
       MFT_CUDA(cudaMemcpyAsync(lam[v], c->soa2.p + (size_t)v * n, n * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
-    MFT_CUDA(cudaStreamSynchronize(s));
     check_kernel_errors(c);
   });
 }
@@ -2017,7 +2015,6 @@ mft_status mft_ssprk33_adjoint_device(mft_ctx* c, double* lam) {
     MFT_REQUIRE(lam, MFT_ERR_ARG, "NULL device array");
     set_device(c);
     ssprk33_adjoint_soa(c, lam);
-    MFT_CUDA(cudaStreamSynchronize(c->stream));
     check_kernel_errors(c);
   });
 }

@@ -146,6 +146,7 @@ struct mft_ctx {
   mft::StepParams* h_tab = nullptr;  // pinned staging of the step table
   size_t h_tab_n = 0;
   cudaEvent_t ev_tab = nullptr;      // the last table copy
+  int* h_kerr = nullptr;             // pinned copy of the device error word
   mft::DBuf<int> d_ctr;
 
   // side stream for the residual-viscosity reductions (overlap with the gathers)

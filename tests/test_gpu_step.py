@@ -181,6 +181,58 @@ def test_host_entry_point_pinned_and_pageable_agree(gpu_lib):
     assert np.array_equal(results[1], u_dev)
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_entry_point_reruns_when_caller_changed_state(gpu_lib, pinned):
+    """The caller edits its state between host calls (same time): the steps that ran
+    speculatively on the held state are discarded and rerun from the caller's state,
+    with the HistoryCallback bookkeeping and approx_du restored; the result equals
+    device stepping from the edited state bit for bit (vortex, residual viscosity,
+    history of order 3)."""
+    torch = pytest.importorskip("torch")
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(40)
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom))
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                          solver, source_terms=src)
+    ctx = dom.ctx
+    u0 = semi.compute_coefficients(0.0)
+    dt = 0.2 * h
+    # reference: device stepping, the state replaced after three steps
+    ctx.history_init(3)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, 3)
+    u3, t3 = ctx.get_state()
+    u_edit = u3.copy()
+    u_edit[0, 17] *= 1.001
+    u_edit[3, 301] *= 0.999
+    ctx.set_state(u_edit, t3)
+    ctx.ssprk33(dt, 2)
+    u_ref, t_ref = ctx.get_state()
+    # host stepping with the same edit between calls
+    if pinned:
+        u = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+        u[:] = u0
+    else:
+        u = u0.copy()
+    ctx.history_init(3)
+    t = 0.0
+    for _ in range(3):
+        t = ctx.ssprk33_host(u, t, dt, 1)
+    assert np.array_equal(u, u3) and t == t3
+    u[0, 17] *= 1.001
+    u[3, 301] *= 0.999
+    assert np.array_equal(u, u_edit)
+    for _ in range(2):
+        t = ctx.ssprk33_host(u, t, dt, 1)
+    assert t == t_ref
+    assert np.array_equal(u, u_ref)
+
+
 def test_graph_steps_equal_direct_steps(gpu_lib):
     """Steps replayed from the captured per-step CUDA graphs (device step table for the
     history weights) equal directly launched steps bit for bit, across odd batch sizes
