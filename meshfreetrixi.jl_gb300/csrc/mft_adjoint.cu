@@ -55,10 +55,11 @@ static __device__ __forceinline__ void project_row(const BcDev& bc, int64_t i, d
 
 template <int V, bool EULER, bool BC, int HV>
 __global__ void __launch_bounds__(kBlock) k_adj_f64(AdjArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t row = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (row >= a.n) return;
+  const int64_t i = ell_node(a.ell, row);
+  const int64_t base = a.ell.slice_off[row >> 5] + (row & 31);
+  const int len = a.ell.row_len[row];
   double gx[V], gy[V], gh[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) { gx[v] = 0; gy[v] = 0; gh[v] = 0; }

@@ -181,10 +181,11 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
 
 template <int V, bool RV, bool LAP>
 __global__ void __launch_bounds__(kBlock) k_rev_f32(RevArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   float sx[V], sy[V], sl[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) { sx[v] = 0.f; sy[v] = 0.f; sl[v] = 0.f; }

@@ -72,21 +72,32 @@ struct DBuf {
 // that lane r of a warp reads element slice_off + slot*32 + r (coalesced).
 constexpr int kSlice = 32;
 
+// Row r of the layout holds node perm[r]'s row (perm null: node r).  slice_off and
+// row_len are indexed by layout row; everything per node by perm[r].
 struct EllView {
   int64_t n;
   const int64_t* slice_off;
   const int32_t* row_len;
   const int32_t* col;
+  const int32_t* perm;
 };
 
 struct EllBuf {
   int64_t n = 0, n_elems = 0;
   int max_len = 0;
+  int window = 0;  // rows sorted by length inside windows of this many rows (0: none)
   DBuf<int64_t> slice_off;
   DBuf<int32_t> row_len;
   DBuf<int32_t> col;
-  EllView view() const { return EllView{n, slice_off.p, row_len.p, col.p}; }
+  DBuf<int32_t> perm;
+  EllView view() const {
+    return EllView{n, slice_off.p, row_len.p, col.p, window > 0 ? perm.p : nullptr};
+  }
 };
+
+__host__ __device__ __forceinline__ int64_t ell_node(const EllView& e, int64_t r) {
+  return e.perm ? (int64_t)e.perm[r] : r;
+}
 
 // Host description of the boundary conditions, flattened per node for kernels.
 struct BcDev {
