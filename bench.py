@@ -62,11 +62,13 @@ def parse():
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
     ap.add_argument("--only", default="all",
-                    choices=["all", "adjoint", "riemann", "weights", "igr", "fp32"],
+                    choices=["all", "adjoint", "riemann", "weights", "igr", "fp32", "setup"],
                     help="run one auxiliary measurement alone")
     ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
     ap.add_argument("--igr", type=int, default=1, help="1 runs the IGR-source measurement")
+    ap.add_argument("--setup", type=int, default=1,
+                    help="1 runs the set-up measurement (KNN and weights of the headline cloud)")
     ap.add_argument("--weights-n", type=int, default=1048576,
                     help="stencils of the batched-weights measurement (0 skips it)")
     ap.add_argument("--riemann-side", type=int, default=1024,
@@ -259,6 +261,61 @@ def _ragged_stencils(ctx, pts, ks):
     rp[1:] = np.cumsum(ks)
     cols = idx[np.arange(idx.shape[1])[None, :] < ks[:, None]].astype(np.int32)
     return rp, cols
+
+
+def run_setup(args, local):
+    """Set-up of the headline workload: KNN stencils (k = 35, periodic minimum image) and
+    the gradient operator's weights for every node, each timed as the call a user makes
+    (host binning and the engine's host copies included), beside the oracle's KNN and
+    per-node Bunch-Kaufman solves on the host cores (the reference's dominant set-up
+    cost: one LAPACK factorisation per node)."""
+    from meshfree_gb300 import _lib as L
+    from meshfree_gb300 import workloads as W
+    from oracle import oracle as O
+    pts, per, h = W.vortex_cloud(args.n_side)
+    n = pts.shape[0]
+    ctx = L.Context(local)
+    ctx.set_points(pts, per)
+    ctx.knn(K_STENCIL)
+    ctx.weights(L.OP_GRAD, 3, 3, 1)            # warm-up (module load, allocations)
+    ctx.set_points(pts, per)
+    t0 = time.perf_counter()
+    ctx.knn(K_STENCIL)
+    knn_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.weights(L.OP_GRAD, 3, 3, 1)
+    w_s = time.perf_counter() - t0
+    # the first rhs! call lays the operators out on the device (sliced ELL, both
+    # directions, FP64 and FP32 values); a second call is the plain evaluation
+    ctx.set_equations(L.EQ_EULER2D, [1.4])
+    ctx.set_bcs([], [0], np.zeros(0, np.int32), None)
+    ctx.set_sources([], [])
+    u = W.isentropic_vortex(pts, 0.0)
+    du = np.empty_like(u)
+    t0 = time.perf_counter()
+    ctx.rhs(du, u.copy(), 0.0)
+    first_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.rhs(du, u.copy(), 0.0)
+    rhs_s = time.perf_counter() - t0
+    ctx.close()
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    idx, _, _, _ = O.knn(pts, K_STENCIL, period=per, nthreads=nthreads)
+    oknn_s = time.perf_counter() - t0
+    rowptr = np.arange(n + 1, dtype=np.int64) * K_STENCIL
+    t0 = time.perf_counter()
+    O.weights(pts, rowptr, idx.ravel(), period=per, nthreads=nthreads)
+    ow_s = time.perf_counter() - t0
+    return {"workload": "isentropic vortex cloud N=%d, k=%d, periodic; PHS r^3 + degree 3, "
+                        "first derivatives" % (n, K_STENCIL),
+            "knn_ms": knn_s * 1e3, "weights_ms": w_s * 1e3,
+            "layout_ms": (first_s - rhs_s) * 1e3,
+            "timing": "wall time of mft_knn and mft_weights (host binning, device search "
+                      "and solves, stencil and weight copies the engine keeps); layout: "
+                      "first host rhs! call minus a second one",
+            "oracle": {"knn_ms": oknn_s * 1e3, "weights_ms": ow_s * 1e3, "cores": nthreads,
+                       "kind": "port"}}
 
 
 def run_weights(args, local):
@@ -673,7 +730,8 @@ def run_ours(args):
                     "riemann": lambda: run_riemann(args, local),
                     "weights": lambda: run_weights(args, local),
                     "igr": lambda: run_igr(args, local),
-                    "fp32": lambda: run_fp32(args, local, peaks)}
+                    "fp32": lambda: run_fp32(args, local, peaks),
+                    "setup": lambda: run_setup(args, local)}
             leg = legs[args.only]()
             print(json.dumps({args.only: leg}), flush=True)
         return
@@ -722,6 +780,7 @@ def run_ours(args):
     rie = run_riemann(args, local) if args.riemann_side > 0 and rank == 0 else None
     wts = run_weights(args, local) if args.weights_n > 0 and rank == 0 else None
     igr = run_igr(args, local) if args.igr and rank == 0 else None
+    setup = run_setup(args, local) if args.setup and rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -763,6 +822,7 @@ def run_ours(args):
         "riemann": rie,
         "weights_batch": wts,
         "igr": igr,
+        "setup": setup,
     }
     print(json.dumps(line), flush=True)
 

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -52,6 +53,7 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   std::vector<int32_t> order(n);
   std::iota(order.begin(), order.end(), 0);
   if (window > 0) {
+#pragma omp parallel for schedule(static)
     for (int64_t w0 = 0; w0 < n; w0 += window) {
       const int64_t w1 = std::min<int64_t>(n, w0 + window);
       std::stable_sort(order.begin() + w0, order.begin() + w1, [&](int32_t x, int32_t y) {
@@ -62,7 +64,7 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   const int64_t nsl = (n + kSlice - 1) / kSlice;
   std::vector<int64_t> soff(nsl + 1, 0);
   std::vector<int32_t> rlen(n);
-  int maxlen = 0;
+#pragma omp parallel for schedule(static)
   for (int64_t sl = 0; sl < nsl; ++sl) {
     int m = 0;
     for (int64_t r = sl * kSlice; r < std::min<int64_t>(n, (sl + 1) * kSlice); ++r) {
@@ -71,12 +73,17 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
       rlen[r] = len;
       m = std::max(m, len);
     }
-    maxlen = std::max(maxlen, m);
-    soff[sl + 1] = soff[sl] + (int64_t)m * kSlice;
+    soff[sl + 1] = (int64_t)m * kSlice;
+  }
+  int maxlen = 0;
+  for (int64_t sl = 0; sl < nsl; ++sl) {
+    maxlen = std::max<int>(maxlen, (int)(soff[sl + 1] / kSlice));
+    soff[sl + 1] += soff[sl];
   }
   const int64_t ne = soff[nsl];
   std::vector<int32_t> col(ne);
   pos.assign(rowptr[n], 0);
+#pragma omp parallel for schedule(static)
   for (int64_t sl = 0; sl < nsl; ++sl) {
     const int m = (int)((soff[sl + 1] - soff[sl]) / kSlice);
     for (int64_t lane = 0; lane < kSlice; ++lane) {
@@ -156,19 +163,43 @@ static void prof_drain(mft_ctx* c) {
 void finish_pattern(mft_ctx* c) {
   const int64_t n = c->n;
   const int64_t nnz = c->rp[n];
-  // CSC view (rows ascending inside each column) with the map to CSR entries.
+  // CSC view (rows ascending inside each column) with the map to CSR entries: column
+  // counts, a prefix sum, entries placed through per-column cursors by all host
+  // threads, then every column put back in ascending row order.
   c->cp.assign(n + 1, 0);
-  for (int64_t e = 0; e < nnz; ++e) c->cp[c->ci[e] + 1]++;
-  for (int64_t j = 0; j < n; ++j) c->cp[j + 1] += c->cp[j];
+  int64_t* cp = c->cp.data();
+  const int32_t* ci = c->ci.data();
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < nnz; ++e) __atomic_fetch_add(&cp[ci[e] + 1], (int64_t)1, __ATOMIC_RELAXED);
+  for (int64_t j = 0; j < n; ++j) cp[j + 1] += cp[j];
   c->ri.assign(nnz, 0);
   c->csc2csr.assign(nnz, 0);
   std::vector<int64_t> fill(c->cp.begin(), c->cp.end() - 1);
+  int32_t* ri = c->ri.data();
+  int64_t* c2r = c->csc2csr.data();
+  const int64_t* rp = c->rp.data();
+#pragma omp parallel for schedule(static)
   for (int64_t r = 0; r < n; ++r)
-    for (int64_t e = c->rp[r]; e < c->rp[r + 1]; ++e) {
-      const int64_t p = fill[c->ci[e]]++;
-      c->ri[p] = (int32_t)r;
-      c->csc2csr[p] = e;
+    for (int64_t e = rp[r]; e < rp[r + 1]; ++e) {
+      const int64_t p = __atomic_fetch_add(&fill[ci[e]], (int64_t)1, __ATOMIC_RELAXED);
+      ri[p] = (int32_t)r;
+      c2r[p] = e;
     }
+#pragma omp parallel
+  {
+    std::vector<std::pair<int32_t, int64_t>> col;
+#pragma omp for schedule(static)
+    for (int64_t j = 0; j < n; ++j) {
+      const int64_t b = cp[j], e = cp[j + 1];
+      col.resize(e - b);
+      for (int64_t q = b; q < e; ++q) col[q - b] = {ri[q], c2r[q]};
+      std::sort(col.begin(), col.end());
+      for (int64_t q = b; q < e; ++q) {
+        ri[q] = col[q - b].first;
+        c2r[q] = col[q - b].second;
+      }
+    }
+  }
   for (int k = 0; k < kSlots; ++k) {
     c->val[k].clear();
     c->have_val[k] = false;
@@ -183,21 +214,32 @@ void pattern_from_stencils(mft_ctx* c) {
   c->rp.assign(n + 1, 0);
   c->ci.assign(c->st_ci.size(), 0);
   c->st2csr.assign(c->st_ci.size(), 0);
-  std::vector<int64_t> ord;
-  for (int64_t r = 0; r < n; ++r) {
-    const int64_t b = c->st_rp[r], e = c->st_rp[r + 1];
-    ord.resize(e - b);
-    std::iota(ord.begin(), ord.end(), b);
-    std::stable_sort(ord.begin(), ord.end(),
-                     [&](int64_t x, int64_t y) { return c->st_ci[x] < c->st_ci[y]; });
-    for (int64_t k = 0; k < e - b; ++k) {
-      MFT_REQUIRE(k == 0 || c->st_ci[ord[k]] != c->st_ci[ord[k - 1]], MFT_ERR_ARG,
-                  "stencil of node " + std::to_string(r) + " lists a node twice");
-      c->ci[b + k] = c->st_ci[ord[k]];
-      c->st2csr[ord[k]] = b + k;
+  // rows sorted by column on all host threads; (column, position) packed in one integer
+  // gives one plain sort per row with equal columns in position order (rejected)
+  int64_t dup = INT64_MAX;  // smallest row that lists a node twice
+#pragma omp parallel
+  {
+    std::vector<int64_t> key;
+    int64_t my_dup = INT64_MAX;
+#pragma omp for schedule(static)
+    for (int64_t r = 0; r < n; ++r) {
+      const int64_t b = c->st_rp[r], e = c->st_rp[r + 1];
+      key.resize(e - b);
+      for (int64_t q = 0; q < e - b; ++q) key[q] = ((int64_t)c->st_ci[b + q] << 32) | q;
+      std::sort(key.begin(), key.end());
+      for (int64_t k = 0; k < e - b; ++k) {
+        const int64_t src = b + (key[k] & 0xffffffffll);
+        if (k > 0 && (key[k] >> 32) == (key[k - 1] >> 32)) my_dup = std::min(my_dup, r);
+        c->ci[b + k] = c->st_ci[src];
+        c->st2csr[src] = b + k;
+      }
+      c->rp[r + 1] = e;
     }
-    c->rp[r + 1] = e;
+#pragma omp critical(mft_pattern_dup)
+    dup = std::min(dup, my_dup);
   }
+  MFT_REQUIRE(dup == INT64_MAX, MFT_ERR_ARG,
+              "stencil of node " + std::to_string(dup) + " lists a node twice");
   finish_pattern(c);
 }
 
@@ -267,27 +309,27 @@ void ensure_device_ops(mft_ctx* c) {
   std::vector<int64_t> rpos_csc;
   build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window);
   std::vector<int64_t> rpos(rpos_csc.size());
-  for (size_t p = 0; p < rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < (int64_t)rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
   c->rev_pos.upload(rpos, s);
-  const std::vector<int64_t>& fpos = pos;
+  // values: uploaded once in structure order, placed into both layouts (FP64 and FP32)
+  // on the device; padding elements stay zero
+  DBuf<double> d_v;
   for (int k = 0; k < kSlots; ++k) {
     if (!c->have_val[k]) {
       c->fw[k].release(); c->rw[k].release(); c->fw32[k].release(); c->rw32[k].release();
       continue;
     }
-    std::vector<double> f(c->fwd.n_elems, 0.0), r(c->rev.n_elems, 0.0);
-    std::vector<float> f32(c->fwd.n_elems, 0.0f), r32(c->rev.n_elems, 0.0f);
     const std::vector<double>& v = c->val[k];
-    for (size_t e = 0; e < v.size(); ++e) {
-      f[fpos[e]] = v[e];
-      r[rpos[e]] = v[e];
-      f32[fpos[e]] = (float)v[e];
-      r32[rpos[e]] = (float)v[e];
-    }
-    c->fw[k].upload(f, s);
-    c->rw[k].upload(r, s);
-    c->fw32[k].upload(f32, s);
-    c->rw32[k].upload(r32, s);
+    d_v.upload(v, s);
+    c->fw[k].alloc(c->fwd.n_elems);
+    c->rw[k].alloc(c->rev.n_elems);
+    c->fw32[k].alloc(c->fwd.n_elems);
+    c->rw32[k].alloc(c->rev.n_elems);
+    for (auto* b : {&c->fw[k], &c->rw[k]}) b->zero(s);
+    for (auto* b : {&c->fw32[k], &c->rw32[k]}) b->zero(s);
+    launch_scatter_values((int64_t)v.size(), c->fwd_pos.p, d_v.p, c->fw[k].p, c->fw32[k].p, s);
+    launch_scatter_values((int64_t)v.size(), c->rev_pos.p, d_v.p, c->rw[k].p, c->rw32[k].p, s);
   }
   MFT_CUDA(cudaStreamSynchronize(s));
   c->dev_dirty = false;
@@ -992,7 +1034,9 @@ mft_status mft_weights(mft_ctx* c, int op, int rbf_pow, int polydeg, int deriv_o
     if (op == MFT_OP_GRAD) {
       for (int d = 0; d < D; ++d) {
         c->val[d].assign(nnz, 0.0);
-        for (int64_t e = 0; e < nnz; ++e) c->val[d][c->st2csr[e]] = w[e * D + d];
+        double* vd = c->val[d].data();
+#pragma omp parallel for schedule(static)
+        for (int64_t e = 0; e < nnz; ++e) vd[c->st2csr[e]] = w[e * D + d];
         c->have_val[d] = true;
       }
     } else {

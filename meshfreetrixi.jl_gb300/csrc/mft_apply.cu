@@ -682,11 +682,28 @@ __global__ void k_differs(const double* __restrict__ a, const double* __restrict
   if (i < count && __double_as_longlong(a[i]) != __double_as_longlong(b[i])) *flag = 1;
 }
 
+__global__ void k_scatter_values(int64_t nnz, const int64_t* __restrict__ pos,
+                                 const double* __restrict__ v, double* __restrict__ out,
+                                 float* __restrict__ out32) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  const int64_t p = pos[e];
+  out[p] = v[e];
+  if (out32) out32[p] = __double2float_rn(v[e]);
+}
+
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 }  // namespace
 
 // ====================================================================== launchers
+
+void launch_scatter_values(int64_t nnz, const int64_t* pos, const double* v, double* out,
+                           float* out32, cudaStream_t s) {
+  if (nnz <= 0) return;
+  k_scatter_values<<<grid_for(nnz, 256), 256, 0, s>>>(nnz, pos, v, out, out32);
+  MFT_LAUNCH_CHECK();
+}
 
 void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s) {
   if (n <= 0) return;

@@ -138,6 +138,11 @@ struct Epilogue {
 void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s);
 void launch_soa_from_aos(const double* aos, double* soa, int64_t n, int V, cudaStream_t s);
 void launch_aos_to_f32(const double* aos, float* a32, int64_t count, cudaStream_t s);
+// out[pos[e]] = v[e] (and out32[pos[e]] = (float) v[e] when out32 is not null): the
+// operator values of structure entry e placed at their sliced-ELL element.
+void launch_scatter_values(int64_t nnz, const int64_t* pos, const double* v, double* out,
+                           float* out32, cudaStream_t s);
+
 // One pointer per variable (pinned host memory mapped for the device, or device memory).
 struct VarPtrs {
   double* p[8];

@@ -306,24 +306,32 @@ void knn_device(mft_ctx* c, int k, std::vector<int32_t>& idx, std::vector<double
   MFT_LAUNCH_CHECK();
   int err = 0;
   idx.resize((size_t)n * k);
-  std::vector<double> d2((size_t)n * k);
   MFT_CUDA(cudaMemcpyAsync(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   MFT_CUDA(cudaMemcpyAsync(idx.data(), d_idx.p, idx.size() * sizeof(int32_t),
                            cudaMemcpyDeviceToHost, s));
-  MFT_CUDA(cudaMemcpyAsync(d2.data(), d_d2.p, d2.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                           s));
+  // the squared distances: all of them when asked for, else only the nearest other
+  // node's (column 1, for dx_min / dx_avg)
+  std::vector<double> d2(dist ? (size_t)n * k : (size_t)n);
+  if (dist) {
+    MFT_CUDA(cudaMemcpyAsync(d2.data(), d_d2.p, d2.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  } else if (k >= 2) {
+    MFT_CUDA(cudaMemcpy2DAsync(d2.data(), sizeof(double), d_d2.p + 1, (size_t)k * sizeof(double),
+                               sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, s));
+  }
   MFT_CUDA(cudaStreamSynchronize(s));
   MFT_REQUIRE(err == 0, MFT_ERR_ARG, "KNN search could not collect k neighbours");
   if (dist) {
     dist->resize(d2.size());
     for (size_t e = 0; e < d2.size(); ++e) (*dist)[e] = sqrt(d2[e]);
   }
+  const int64_t d2_stride = dist ? k : 1, d2_col = dist ? 1 : 0;
   // dx_min = minimum(dists)[2], dx_avg = mean(dists)[2] over the 2-NN query.
   if (k >= 2) {
     std::vector<double> nn(n);
     double m = INFINITY;
     for (int64_t i = 0; i < n; ++i) {
-      nn[i] = sqrt(d2[(size_t)i * k + 1]);
+      nn[i] = sqrt(d2[(size_t)i * d2_stride + d2_col]);
       if (nn[i] < m || isnan(nn[i])) m = nn[i];
     }
     if (dx_min) *dx_min = m;
