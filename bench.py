@@ -349,8 +349,10 @@ def run_weights(args, local):
     dev_ms = ctx2.region_end()
     ctx2.close()
     rng = np.random.default_rng(33)
-    s2 = np.sort(rng.choice(n2, 2000, replace=False))
-    s3 = np.sort(rng.choice(n3, 300, replace=False))
+    # a sample large enough to keep the host cores busy (the CPU figure) and to check
+    # bit-identity on tens of thousands of systems
+    s2 = np.sort(rng.choice(n2, min(n2, 40000), replace=False))
+    s3 = np.sort(rng.choice(n3, min(n3, 4000), replace=False))
     nthreads = os.cpu_count() or 1
     t0 = time.perf_counter()
     r2 = O.weights_rows(p2, rp2, c2, s2, rbf_pow=3, polydeg=3, nthreads=nthreads)

@@ -636,6 +636,11 @@ static void weights_run(cudaStream_t s, const std::vector<HostGroup>& gs, double
   int64_t nsys = 0;
   std::vector<int64_t> order;
   std::vector<int> ks, ns;
+  int64_t total = 0;
+  for (const HostGroup& h : gs) total += h.n;
+  order.reserve(total);
+  ks.reserve(total);
+  ns.reserve(total);
   for (size_t g = 0; g < gs.size(); ++g) {
     const HostGroup& h = gs[g];
     WGroup& G = a.g[g];
@@ -659,9 +664,14 @@ static void weights_run(cudaStream_t s, const std::vector<HostGroup>& gs, double
     nmax = std::max(nmax, km + G.npoly);
     nsys += h.n;
   }
+  // systems by size, largest first, ties in input order: a counting sort on n
   std::vector<int64_t> perm(order.size());
-  std::iota(perm.begin(), perm.end(), 0);
-  std::stable_sort(perm.begin(), perm.end(), [&](int64_t x, int64_t y) { return ns[x] > ns[y]; });
+  {
+    std::vector<int64_t> start((size_t)nmax + 2, 0);
+    for (int v : ns) start[(size_t)(nmax - v) + 1]++;
+    for (size_t q = 1; q < start.size(); ++q) start[q] += start[q - 1];
+    for (size_t q = 0; q < ns.size(); ++q) perm[start[(size_t)(nmax - ns[q])]++] = (int64_t)q;
+  }
   std::vector<int64_t> order_sorted(order.size());
   for (size_t q = 0; q < perm.size(); ++q) order_sorted[q] = order[perm[q]];
   (void)kmax;
