@@ -517,12 +517,24 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   if (rv) {
     // residual / norm with the norms' reciprocals (written by k_lexmax after the norms);
     // r >= 0 and the reciprocals are positive, so every qv is +0 or larger, or NaN
+    // node records as 16-byte vectors (V = 4)
+    double dpv[V], adv[V];
+    if (V == 4) {
+      const double2* dp2 = reinterpret_cast<const double2*>(a.du_p) + i * 2;
+      const double2* ad2 = reinterpret_cast<const double2*>(a.approx_du) + i * 2;
+      const double2 d0 = dp2[0], d1 = dp2[1], a0 = ad2[0], a1 = ad2[1];
+      dpv[0] = d0.x; dpv[1 % V] = d0.y; dpv[2 % V] = d1.x; dpv[3 % V] = d1.y;
+      adv[0] = a0.x; adv[1 % V] = a0.y; adv[2 % V] = a1.x; adv[3 % V] = a1.y;
+    } else {
+      dpv[0] = a.du_p[i];
+      adv[0] = a.approx_du[i];
+    }
     double mr = 0.0;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-      double dp = a.du_p[i * V + v];
+      double dp = dpv[v];
       if (a.hvf) dp = dadd(dp, a.hvf[i * V + v]);
-      const double r = fabs(dsub(a.approx_du[i * V + v], dp));
+      const double r = fabs(dsub(adv[v], dp));
       const double qv = dmul(r, norms[V + v]);
       mr = v == 0 ? qv : jl_max_nonneg(mr, qv);
     }
@@ -587,8 +599,15 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   }
   if (a.eps) a.eps[i] = eps;
   if (a.t) {
+    if (V == 4) {
+      double2* t2 = reinterpret_cast<double2*>(a.t) + i * 4;
+      double2 x[4] = {t2[0], t2[1], t2[2], t2[3]};
 #pragma unroll
-    for (int k = 0; k < 2 * V; ++k) a.t[i * 2 * V + k] = dmul(eps, a.t[i * 2 * V + k]);
+      for (int q = 0; q < 4; ++q) t2[q] = make_double2(dmul(eps, x[q].x), dmul(eps, x[q].y));
+    } else {
+#pragma unroll
+      for (int k = 0; k < 2 * V; ++k) a.t[i * 2 * V + k] = dmul(eps, a.t[i * 2 * V + k]);
+    }
   }
   if (a.t32) {
     const float e32 = __double2float_rn(eps);
@@ -662,6 +681,12 @@ __device__ __forceinline__ double hist_acc(double acc, double w, double h) {
   return FUSED ? fma(w, h, acc) : dadd(acc, dmul(w, h));
 }
 
+// The first term: 0 + w h is w h itself (it can differ only in the sign of a zero, which
+// |approx_du - du| in the viscosity does not see), so the addition is skipped.
+__device__ __forceinline__ double hist_first(int m, double w, double h) {
+  return m > 0 ? dmul(w, h) : 0.0;
+}
+
 template <bool FUSED>
 __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
                           const double* h1, const double* h2, const double* h3,
@@ -671,8 +696,8 @@ __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
   if (i >= count) return;
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
   // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
-  double acc = 0.0;
-  for (int k = 0; k < m; ++k) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
+  double acc = hist_first(m, w.w[0], m > 0 ? hs[0][i] : 0.0);
+  for (int k = 1; k < m; ++k) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
   out[i] = acc;
 }
 
@@ -897,14 +922,11 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
   if (i + 1 < count) {
     const double2 un = reinterpret_cast<const double2*>(u_new)[j];
     reinterpret_cast<double2*>(dst)[j] = un;
-    double ax = 0.0, ay = 0.0;
-    for (int k = 0; k < m; ++k) {
-      double2 hk = un;
-      if (k > 0) {
-        int q = head + k;
-        if (q >= slots) q -= slots;
-        hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
-      }
+    double ax = hist_first(m, sp->w[0], un.x), ay = hist_first(m, sp->w[0], un.y);
+    for (int k = 1; k < m; ++k) {
+      int q = head + k;
+      if (q >= slots) q -= slots;
+      const double2 hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
       const double wk = sp->w[k];
       ax = hist_acc<FUSED>(ax, wk, hk.x);
       ay = hist_acc<FUSED>(ay, wk, hk.y);
@@ -913,12 +935,11 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
   } else {
     const double un = u_new[i];
     dst[i] = un;
-    double acc = 0.0;
-    for (int k = 0; k < m; ++k) {
+    double acc = hist_first(m, sp->w[0], un);
+    for (int k = 1; k < m; ++k) {
       int q = head + k;
       if (q >= slots) q -= slots;
-      const double hk = k == 0 ? un : ring_slot(ring, q)[i];
-      acc = hist_acc<FUSED>(acc, sp->w[k], hk);
+      acc = hist_acc<FUSED>(acc, sp->w[k], ring_slot(ring, q)[i]);
     }
     out[i] = acc;
   }
