@@ -552,17 +552,25 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   const double uwc = a.seg_h ? dmul(dmul(a.c_uw, 0.5), h) : a.uw_coef;
   // Decided without forming eps_uw: the computed eps_uw = uwc (speed + c) is at least
   // uwc |m| / rho (1 - 5 u) (c >= 0, no cancellation in speed; u = 2^-53), so
-  // (eps_rv rho)^2 (1 + 1e-12) < uwc^2 (1 - 1e-12) |m|^2, evaluated in FP64 with a normal,
-  // finite right side, proves eps_rv < eps_uw and update_visc!'s min is eps_rv.  This
-  // skips the division and the two square roots wherever the residual viscosity is the
-  // smaller one (smooth flow).  A NaN energy, or a density so small that 1 / rho
-  // overflows (0 * inf in a velocity), would make eps_uw NaN: no shortcut then.
+  // (eps_rv rho)^2 < uwc^2 (1 - 1e-12) / (1 + 1e-12) |m|^2, evaluated in FP64 with a
+  // normal, finite right side, proves eps_rv < eps_uw and update_visc!'s min is eps_rv.
+  // This skips the division and the two square roots wherever the residual viscosity is
+  // the smaller one (smooth flow).  A NaN energy, or a density so small that 1 / rho
+  // overflows (0 * inf in a velocity), would make eps_uw NaN: no shortcut then.  Every
+  // comparison is on bit patterns of values >= 0 (or NaN, which fails them), so the
+  // test issues only five products and one sum on the FP64 pipe.
   bool done = false;
-  if (V == 4 && rv_finite && rho >= 1e-300 && uwc > 0.0 && en == en) {
+  const double kb = a.seg_h ? dmul(dmul(uwc, uwc), (1.0 - 1e-12) / (1.0 + 1e-12)) : a.uw_bound;
+  const long long bits_rho = __double_as_longlong(rho);
+  const long long bits_en = __double_as_longlong(en) & 0x7FFFFFFFFFFFFFFFLL;
+  if (V == 4 && rv_finite && bits_rho >= 0x01A56E1FC2F8F359LL /* 1e-300 */ &&
+      __double_as_longlong(uwc) > 0 && bits_en <= 0x7FF0000000000000LL) {
     const double er = dmul(eps_rv, rho);
-    const double lhs = dmul(dmul(er, er), 1.0 + 1e-12);
-    const double rhs = dmul(dmul(dmul(uwc, uwc), 1.0 - 1e-12), dadd(dmul(m1, m1), dmul(m2, m2)));
-    if (rhs >= 1e-290 && rhs <= 1.7e308 && lhs < rhs) {
+    const double lhs = dmul(er, er);
+    const double rhs = dmul(kb, dadd(dmul(m1, m1), dmul(m2, m2)));
+    const long long bl = __double_as_longlong(lhs), br = __double_as_longlong(rhs);
+    if (br >= 0x03B8F2B061AEA072LL /* 1e-290 */ && br <= 0x7FE0000000000000LL /* 2^1023 */ &&
+        bl < br) {
       eps = eps_rv;
       done = true;
     }
@@ -696,8 +704,8 @@ __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
   if (i >= count) return;
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
   // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
-  double acc = hist_first(m, w.w[0], m > 0 ? hs[0][i] : 0.0);
-  for (int k = 1; k < m; ++k) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
+  double acc = 0.0;
+  for (int k = 0; k < m; ++k) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
   out[i] = acc;
 }
 
@@ -853,6 +861,7 @@ void launch_eps(const EpsArgs& args, cudaStream_t s) {
   a.uw_coef = (a.c_uw * 0.5) * a.h;
   a.uw_adv = a.uw_coef * std::sqrt(a.ax * a.ax + a.ay * a.ay);
   a.rv_coef = (0.5 * a.c_rv) * (a.h * a.h);
+  a.uw_bound = a.uw_coef * a.uw_coef * ((1.0 - 1e-12) / (1.0 + 1e-12));
   const float h32 = (float)a.h;
   a.gamma32 = (float)a.gamma;
   a.gm1_32 = (float)(a.gamma - 1.0);

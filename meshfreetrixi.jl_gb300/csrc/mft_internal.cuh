@@ -210,6 +210,7 @@ struct EpsArgs {
   double uw_coef;          // (c_uw * 0.5) * h
   double uw_adv;           // advection: uw_coef * sqrt(ax^2 + ay^2)
   double rv_coef;          // (0.5 * c_rv) * (h * h)
+  double uw_bound;         // uw_coef^2 (1 - 1e-12) / (1 + 1e-12): the eps_uw bound's factor
   // FP32 form: the FP32 shadow of u and the FP32 factors, formed by launch_eps in the
   // FP32 kernel's operation order
   const float* u32;
