@@ -161,6 +161,11 @@ class Context:
     def set_stencils(self, rowptr, cols):
         rp = np.ascontiguousarray(rowptr, dtype=np.int64)
         ci = np.ascontiguousarray(cols, dtype=np.int32)
+        # the C entry point reads n + 1 row offsets and rowptr[n] columns: check the
+        # lengths here, where they are known
+        if rp.ndim != 1 or rp.size != self.n + 1 or ci.ndim != 1 or rp[-1] != ci.size:
+            raise MFTError(MFT_ERR_ARG, "rowptr must hold n + 1 offsets and cols rowptr[n] "
+                                        "indices")
         self.check(self.lib.mft_set_stencils(self.h, _p(rp), _p(ci)))
         self.nnz = int(rp[-1])
 
@@ -177,6 +182,9 @@ class Context:
         cp = np.ascontiguousarray(colptr, dtype=np.int64)
         rv = np.ascontiguousarray(rowval, dtype=np.int64)
         nz = np.ascontiguousarray(nzval, dtype=np.float64)
+        if cp.ndim != 1 or cp.size < 2 or rv.size < cp[-1] - cp[0] or nz.size < cp[-1] - cp[0]:
+            raise MFTError(MFT_ERR_ARG, "colptr must hold n + 1 offsets and rowval / nzval "
+                                        "colptr[n] - colptr[0] entries")
         self.check(self.lib.mft_load_csc(self.h, op, comp, cp.size - 1, _p(cp), _p(rv), _p(nz)))
 
     # physics ------------------------------------------------------------
@@ -190,6 +198,11 @@ class Context:
         pt = np.ascontiguousarray(ptr, dtype=np.int64)
         ii = np.ascontiguousarray(idx if len(idx) else np.zeros(1), dtype=np.int32)
         nm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64)
+        total = int(pt[-1]) if pt.size else 0
+        if pt.size != k.size + 1 or (total and ii.size < total) or (
+                nm is not None and total and nm.size < total * max(1, getattr(self, "dim", 2))):
+            raise MFTError(MFT_ERR_ARG, "ptr must hold len(kinds) + 1 offsets, idx ptr[-1] "
+                                        "nodes and normals dim values per node")
         self.check(self.lib.mft_set_bcs(self.h, k.size, _p(k), _p(pt), _p(ii), _p(nm)))
 
     def set_dirichlet_values(self, values):
