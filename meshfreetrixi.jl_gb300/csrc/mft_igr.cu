@@ -152,11 +152,13 @@ __global__ void __launch_bounds__(kBlock) k_igr_op(IgrArgs a, const double* un) 
     const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
     const int len = a.ell.row_len[i];
     double sx = 0.0, sy = 0.0;
+    const double2* __restrict__ t2 = reinterpret_cast<const double2*>(a.t);
     for (int j = 0; j < len; ++j) {
       const int64_t p = base + ((int64_t)j << 5);
       const int64_t c = __ldg(a.ell.col + p);
-      sx = fma(__ldg(a.wx + p), a.t[c * 2], sx);
-      sy = fma(__ldg(a.wy + p), a.t[c * 2 + 1], sy);
+      const double2 tc = t2[c];  // (t1, t2) of the neighbour in one 16-byte load
+      sx = fma(__ldg(a.wx + p), tc.x, sx);
+      sy = fma(__ldg(a.wy + p), tc.y, sy);
     }
     const double ci = dsub(dmul(a.rinv[i], un[i]), dmul(a.alpha, dadd(sx, sy)));
     a.c[i] = ci;
