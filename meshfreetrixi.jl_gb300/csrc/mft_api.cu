@@ -840,17 +840,20 @@ void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
     MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
                 "time_deriv_weights: singular Vandermonde system");
   ProfScope ps(c, MFT_K_HISTORY);
-  MFT_CUDA(cudaMemcpyAsync(c->hist[c->hist_head].p, u_aos, nv * sizeof(double),
-                           cudaMemcpyDeviceToDevice, s));
   if (success_iter <= 0) {
+    MFT_CUDA(cudaMemcpyAsync(c->hist[c->hist_head].p, u_aos, nv * sizeof(double),
+                             cudaMemcpyDeviceToDevice, s));
     c->approx_du.zero(s);
     return;
   }
   HistW hw{};
   for (int k = 0; k < m; ++k) hw.w[k] = w[k];
+  // the kernel reads the new state from u_aos and writes its copy into the ring
   const double* hs[8];
-  for (int k = 0; k < m; ++k) hs[k] = c->hist[(c->hist_head + k) % slots].p;
-  launch_history((int64_t)nv, m, hw, hs, c->approx_du.p, c->precision == MFT_PREC_FP32, s);
+  hs[0] = u_aos;
+  for (int k = 1; k < m; ++k) hs[k] = c->hist[(c->hist_head + k) % slots].p;
+  launch_history((int64_t)nv, m, hw, hs, c->hist[c->hist_head].p, c->approx_du.p,
+                 c->precision == MFT_PREC_FP32, s);
 }
 
 void check_state_ready(mft_ctx* c) {

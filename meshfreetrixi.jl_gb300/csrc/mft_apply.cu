@@ -695,17 +695,59 @@ __device__ __forceinline__ double hist_first(int m, double w, double h) {
   return m > 0 ? dmul(w, h) : 0.0;
 }
 
+// approx_du = sum_{k<M} w_k h_k for two values per thread, M known at compile time so
+// that the M 16-byte loads of a thread are in flight together (h_0 is the new state).
+template <bool FUSED, int M>
+__device__ __forceinline__ double2 history_pair(const double2 (&h)[M > 0 ? M : 1],
+                                                const double* w) {
+  double ax = hist_first(M, w[0], h[0].x), ay = hist_first(M, w[0], h[0].y);
+#pragma unroll
+  for (int k = 1; k < M; ++k) {
+    ax = hist_acc<FUSED>(ax, w[k], h[k].x);
+    ay = hist_acc<FUSED>(ay, w[k], h[k].y);
+  }
+  return make_double2(ax, ay);
+}
+
+// approx_du .= 0; approx_du .+= w_k .* sol_k (history.jl:115-126) outside a captured
+// step, two values per thread: h0 is the new state, also copied into its ring slot dst
+// (never one of h1..h7).
+template <bool FUSED, int M>
+__device__ __forceinline__ void history_host_pair(int64_t j, const double* const (&hs)[8],
+                                                  const HistW& w, double* dst, double* out) {
+  double2 h[M > 0 ? M : 1];
+#pragma unroll
+  for (int k = 0; k < (M > 0 ? M : 1); ++k) h[k] = reinterpret_cast<const double2*>(hs[k])[j];
+  reinterpret_cast<double2*>(dst)[j] = h[0];
+  reinterpret_cast<double2*>(out)[j] = history_pair<FUSED, M>(h, w.w);
+}
+
 template <bool FUSED>
 __global__ void k_history(int64_t count, int m, HistW w, const double* h0,
                           const double* h1, const double* h2, const double* h3,
                           const double* h4, const double* h5, const double* h6,
-                          const double* h7, double* __restrict__ out) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+                          const double* h7, double* __restrict__ dst,
+                          double* __restrict__ out) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = 2 * j;
   if (i >= count) return;
   const double* hs[8] = {h0, h1, h2, h3, h4, h5, h6, h7};
-  // approx_du .= 0; approx_du .+= w_k .* sol_k  (history.jl:115-126)
-  double acc = 0.0;
-  for (int k = 0; k < m; ++k) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
+  if (i + 1 < count) {
+    switch (m) {
+#define MFT_HIST_CASE(M) \
+  case M: history_host_pair<FUSED, M>(j, hs, w, dst, out); return;
+      MFT_HIST_CASE(0) MFT_HIST_CASE(1) MFT_HIST_CASE(2) MFT_HIST_CASE(3)
+      MFT_HIST_CASE(4) MFT_HIST_CASE(5) MFT_HIST_CASE(6) MFT_HIST_CASE(7)
+      default: history_host_pair<FUSED, 8>(j, hs, w, dst, out); return;
+#undef MFT_HIST_CASE
+    }
+  }
+  const double un = h0[i];
+  dst[i] = un;
+  double acc = hist_first(m, w.w[0], un);
+#pragma unroll
+  for (int k = 1; k < 8; ++k)  // constant indices: hs and w stay in registers
+    if (k < m) acc = hist_acc<FUSED>(acc, w.w[k], hs[k][i]);
   out[i] = acc;
 }
 
@@ -913,11 +955,28 @@ __device__ __forceinline__ double* ring_slot(const RingPtrs& r, int k) {
   }
 }
 
+template <bool FUSED, int M>
+__device__ __forceinline__ void history_dev_pair(int64_t j, const double* u_new,
+                                                 const RingPtrs& ring, int slots, int head,
+                                                 const double* w, double* out) {
+  double2 h[M > 0 ? M : 1];
+  h[0] = reinterpret_cast<const double2*>(u_new)[j];
+#pragma unroll
+  for (int k = 1; k < M; ++k) {
+    int q = head + k;
+    if (q >= slots) q -= slots;
+    h[k] = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
+  }
+  reinterpret_cast<double2*>(ring_slot(ring, head))[j] = h[0];
+  reinterpret_cast<double2*>(out)[j] = history_pair<FUSED, M>(h, w);
+}
+
 // HistoryCallback push inside a captured step: the step's parameters come from the
 // step table at the device step counter.  ring[head] = u_new, then
 // approx_du = sum_{k<m} w_k ring[(head + k) % slots] (k = 0 is u_new itself).
 // Two values per thread (16-byte loads and stores); count is even or the last thread
-// takes the single remaining value.
+// takes the single remaining value.  The ring slots read are never ring[head], the one
+// written.
 template <bool FUSED>
 __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, RingPtrs ring,
                               int slots, const StepParams* __restrict__ tab,
@@ -927,31 +986,26 @@ __global__ void k_history_dev(int64_t count, const double* __restrict__ u_new, R
   if (i >= count) return;
   const StepParams* sp = tab + *ctr;
   const int m = sp->m, head = sp->head;
-  double* dst = ring_slot(ring, head);
   if (i + 1 < count) {
-    const double2 un = reinterpret_cast<const double2*>(u_new)[j];
-    reinterpret_cast<double2*>(dst)[j] = un;
-    double ax = hist_first(m, sp->w[0], un.x), ay = hist_first(m, sp->w[0], un.y);
-    for (int k = 1; k < m; ++k) {
-      int q = head + k;
-      if (q >= slots) q -= slots;
-      const double2 hk = reinterpret_cast<const double2*>(ring_slot(ring, q))[j];
-      const double wk = sp->w[k];
-      ax = hist_acc<FUSED>(ax, wk, hk.x);
-      ay = hist_acc<FUSED>(ay, wk, hk.y);
+    switch (m) {
+#define MFT_HIST_CASE(M) \
+  case M: history_dev_pair<FUSED, M>(j, u_new, ring, slots, head, sp->w, out); return;
+      MFT_HIST_CASE(0) MFT_HIST_CASE(1) MFT_HIST_CASE(2) MFT_HIST_CASE(3)
+      MFT_HIST_CASE(4) MFT_HIST_CASE(5) MFT_HIST_CASE(6) MFT_HIST_CASE(7)
+      default: history_dev_pair<FUSED, 8>(j, u_new, ring, slots, head, sp->w, out); return;
+#undef MFT_HIST_CASE
     }
-    reinterpret_cast<double2*>(out)[j] = make_double2(ax, ay);
-  } else {
-    const double un = u_new[i];
-    dst[i] = un;
-    double acc = hist_first(m, sp->w[0], un);
-    for (int k = 1; k < m; ++k) {
-      int q = head + k;
-      if (q >= slots) q -= slots;
-      acc = hist_acc<FUSED>(acc, sp->w[k], ring_slot(ring, q)[i]);
-    }
-    out[i] = acc;
   }
+  double* dst = ring_slot(ring, head);
+  const double un = u_new[i];
+  dst[i] = un;
+  double acc = hist_first(m, sp->w[0], un);
+  for (int k = 1; k < m; ++k) {
+    int q = head + k;
+    if (q >= slots) q -= slots;
+    acc = hist_acc<FUSED>(acc, sp->w[k], ring_slot(ring, q)[i]);
+  }
+  out[i] = acc;
 }
 
 __global__ void k_step_advance(int* ctr) {
@@ -984,17 +1038,17 @@ void launch_differs(const double* a, const double* b, int64_t count, int* flag, 
 }
 
 void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
-                    double* approx_du, bool fused, cudaStream_t s) {
+                    double* ring_dst, double* approx_du, bool fused, cudaStream_t s) {
   if (count <= 0) return;
   const double* h[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   for (int k = 0; k < m && k < 8; ++k) h[k] = hist[k];
-  const unsigned g = grid_for(count, 256);
+  const unsigned g = grid_for((count + 1) / 2, 256);
   if (fused)
     k_history<true><<<g, 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4], h[5], h[6],
-                                      h[7], approx_du);
+                                      h[7], ring_dst, approx_du);
   else
     k_history<false><<<g, 256, 0, s>>>(count, m, w, h[0], h[1], h[2], h[3], h[4], h[5], h[6],
-                                       h[7], approx_du);
+                                       h[7], ring_dst, approx_du);
   MFT_LAUNCH_CHECK();
 }
 

@@ -343,9 +343,10 @@ void launch_differs(const double* a, const double* b, int64_t count, int* flag, 
 struct HistW {
   double w[8];
 };
+// approx_du = sum_k w_k hist[k]; hist[0] (the new state) is also copied to ring_dst.
 // fused: multiply-adds (FP32-apply form) instead of separately rounded products and sums.
 void launch_history(int64_t count, int m, const HistW& w, const double* const* hist,
-                    double* approx_du, bool fused, cudaStream_t s);
+                    double* ring_dst, double* approx_du, bool fused, cudaStream_t s);
 
 // Per-step parameters of a captured SSP-RK3 step, read on the device through a step
 // counter so that one graph serves every step of a batch.

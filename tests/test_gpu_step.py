@@ -39,9 +39,12 @@ def _oracle_advection(oracle, pts, tags, domain, nv=35):
                        sources=(oracle.SRC_RV,), c_rv=1.0, c_uw=1.0, h=davg)
 
 
-def test_advection_rv_trajectory_matches_oracle(oracle, gpu_lib):
+@pytest.mark.parametrize("n_side", [32, 31])
+def test_advection_rv_trajectory_matches_oracle(oracle, gpu_lib, n_side):
+    """n_side 31 gives 1085 nodes: an odd number of history values, whose last one the
+    history kernels take singly."""
     import meshfree_gb300 as M
-    semi, domain, pts, tags, h = _advection_problem(32)
+    semi, domain, pts, tags, h = _advection_problem(n_side)
     dt, nsteps = 0.2 * h, 30
     ode = M.semidiscretize(semi, (0.0, nsteps * dt))
     sol = M.solve(ode, M.SSPRK33(), dt=dt, callback=M.HistoryCallback(approx_order=3))
@@ -120,12 +123,13 @@ def test_fp32_apply_error_vs_fp64(gpu_lib):
     assert l2 < 1e-5, l2
 
 
-def test_host_entry_point_equals_device_steps(gpu_lib):
+@pytest.mark.parametrize("n_side", [24, 31])
+def test_host_entry_point_equals_device_steps(gpu_lib, n_side):
     """mft_ssprk33_host step by step (state handed back each time) equals device
     stepping, and reuses the pending first stage when handed its own state back."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
-    semi, domain, pts, tags, h = _advection_problem(24)
+    semi, domain, pts, tags, h = _advection_problem(n_side)
     ctx = domain.ctx
     u0 = semi.compute_coefficients(0.0)
     dt = 0.2 * h
@@ -254,6 +258,23 @@ def test_graph_steps_equal_direct_steps(gpu_lib):
         ctx.set_state(semi.compute_coefficients(0.0), 0.0)
         for nsteps, dt in ((3, 0.1 * h), (2, 0.1 * h), (5, 0.1 * h), (1, 0.05 * h), (4, 0.05 * h)):
             ctx.ssprk33(dt, nsteps, use_graph=use_graph)
+        res.append(ctx.get_state())
+    assert res[0][1] == res[1][1]
+    assert np.array_equal(res[0][0], res[1][0])
+
+
+def test_graph_steps_equal_direct_steps_odd_count(gpu_lib):
+    """Scalar advection on 1085 nodes (an odd number of history values): graph-replayed
+    and directly launched steps agree bit for bit, the history ring filling up over the
+    first steps (1 to 4 history points)."""
+    res = []
+    for use_graph in (False, True):
+        semi, domain, pts, tags, h = _advection_problem(31)
+        ctx = domain.ctx
+        ctx.history_init(3)
+        ctx.set_state(semi.compute_coefficients(0.0), 0.0)
+        for nsteps in (1, 1, 1, 3, 2):
+            ctx.ssprk33(0.2 * h, nsteps, use_graph=use_graph)
         res.append(ctx.get_state())
     assert res[0][1] == res[1][1]
     assert np.array_equal(res[0][0], res[1][0])
