@@ -139,13 +139,17 @@ mft_status mft_weights_batch(mft_ctx* ctx, int ngroups, const mft_weight_group* 
  * memory (xyz n*dim, rowptr n+1, cols rowptr[n] with centre first, w rowptr[n]*dim in
  * stencil order [slot][axis]); period is a host array of dim lengths or NULL; stream
  * may be 0.  kmax: the caller's bound on the stencil size; kmax + number of monomials
- * must be <= 161 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  A
- * stencil longer than kmax is skipped and reported as MFT_ERR_ARG.  The only global
+ * must be <= 161 (shared-memory limit), else MFT_ERR_ARG with the reason in err.  The
+ * device arrays are checked on the device before any coordinate is read: a stencil
+ * longer than kmax, an empty stencil, a row outside [0, rowptr[n]) or a column outside
+ * 0..n-1 is skipped, its weights (where its row lies inside cols) are set to NaN, and
+ * the call returns MFT_ERR_ARG; the other stencils are solved.  The only global
  * scratch is a 32-byte static device array per GPU; its address is looked up on the
- * first call on each device (make that call before any stream capture), and it is
- * reset at the start of every call.  Calls that overlap on the GPU (other streams,
- * other host threads) share that array and race.  Blocks until the solve finished.
- * err (may be NULL) receives a message of at most err_len bytes. */
+ * first call on each device (make that call before any stream capture; a
+ * cudaDeviceReset after it is not supported), and it is reset at the start of every
+ * call.  Calls that overlap on the GPU (other streams, other host threads) share that
+ * array and race.  Blocks until the solve finished.  err (may be NULL) receives a
+ * message of at most err_len bytes. */
 mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz, const double* period,
                                const int64_t* rowptr, const int32_t* cols, int kmax,
                                int rbf_pow, int polydeg, int deriv_order, double* w,

@@ -247,16 +247,39 @@ __global__ void __launch_bounds__(W == 1 ? 32 * kWarpsPerBlock : 32 * W) k_weigh
     double* w_out = a.g[grp].w_out;
     double* resid = a.g[grp].resid;
     const int64_t rb = rowptr[e];
+    if (!kOrdered) {
+      // Unordered work comes from caller-owned device arrays that no host code checked
+      // (mft_weights_noalloc; one warp per system).  Before any coordinate is read, a
+      // stencil is skipped, its weights set to NaN where its row lies inside cols, and a
+      // status word set, when its size is outside 1..kmax (word 2 for > kmax, word 3
+      // otherwise), its extent leaves [0, rowptr[n]) or a column is not a node (word 3).
+      static_assert(kOrdered || W == 1, "unordered systems run one warp per system");
+      const int64_t re = rowptr[e + 1], nnz = rowptr[a.nsys];
+      const int64_t k64 = re - rb;
+      const bool in_cols = rb >= 0 && re <= nnz && k64 >= 0;
+      int why = 0;
+      if (!in_cols || k64 < 1) why = 3;
+      else if (k64 > a.kmax) why = 2;
+      if (why == 0) {
+        bool badc = false;
+        for (int64_t j = gt; j < k64; j += G) {
+          const int32_t cj = cols[rb + j];
+          badc |= cj < 0 || (int64_t)cj >= a.nsys;
+        }
+        if (__any_sync(kFull, badc)) why = 3;
+      }
+      if (why != 0) {
+        if (gt == 0) atomicExch(reinterpret_cast<int*>(a.next + why), 1);
+        if (in_cols)
+          for (int64_t t = rb * dim + gt; t < re * dim; t += G) w_out[t] = __longlong_as_double(0x7FF8000000000000LL);
+        continue;
+      }
+    }
     const int k = (int)(rowptr[e + 1] - rb);
     const int n = k + npoly;
 // upper-packed element (i, j), 1 <= i <= j: column j starts at j (j - 1) / 2
 #define AM(i, j) A[(((j) * ((j)-1)) >> 1) + ((i)-1)]
 #define BM(i, c) B[(size_t)(c) * n + ((i)-1)]
-    if (!kOrdered && k > a.kmax) {
-      // caller-declared maximum stencil size exceeded: flag it and skip the system
-      if (gt == 0) atomicExch(reinterpret_cast<int*>(a.next + 2), 1);
-      continue;
-    }
     const int32_t* st = cols + rb;
     const int64_t ce = st[0];
     // shift_stencil
@@ -843,8 +866,9 @@ void weights_batch(mft_ctx* c, int ngroups, const mft_weight_group* groups, doub
 namespace {
 
 // [0] work counter, [1] first node with a zero pivot (low 32 bits, 0x7F7F7F7F = none),
-// [2] oversize-stencil flag, [3] unused.  32 bytes on every GPU that loads the library,
-// held until the process exits.
+// [2] oversize-stencil flag, [3] invalid-stencil flag (empty or decreasing rowptr, a row
+// outside cols, a column that is not a node).  32 bytes on every GPU that loads the
+// library, held until the process exits.
 constexpr int kNoAllocWords = 4;
 static __device__ __align__(256) unsigned long long g_weights_scratch[kNoAllocWords];
 
@@ -903,7 +927,9 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   unsigned long long* scratch = nullptr;
   {
     // First call on this device (with it current): resolve the device address of the
-    // scratch array.  Later calls reuse it.  Make the first call before any capture.
+    // scratch array.  Later calls reuse it.  Make the first call before any capture.  The
+    // address is kept for the life of the process: a cudaDeviceReset after the first call
+    // on a device is not supported (the kept address would be stale).
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (!g_scratch_addr[dev]) {
       void* ptr = nullptr;
@@ -920,7 +946,7 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   // the counter and the status words must start from their initial values
   if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), s) != cudaSuccess ||
       cudaMemsetAsync(scratch + 1, 0x7F, sizeof(int), s) != cudaSuccess ||
-      cudaMemsetAsync(scratch + 2, 0, sizeof(unsigned long long), s) != cudaSuccess) {
+      cudaMemsetAsync(scratch + 2, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess) {
     put_err(err, err_len, "mft_weights_noalloc: cudaMemsetAsync failed");
     return MFT_ERR_CUDA;
   }
@@ -951,14 +977,21 @@ extern "C" mft_status mft_weights_noalloc(int dim, int64_t n, const double* xyz,
   int status[3] = {0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status[0], scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&status[1], scratch + 2, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status[2], scratch + 3, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     put_err(err, err_len, std::string("mft_weights_noalloc: ") + cudaGetErrorString(e));
     return MFT_ERR_CUDA;
   }
+  if (status[2] != 0) {
+    put_err(err, err_len,
+            "mft_weights_noalloc: a stencil is empty, leaves cols (rowptr not increasing "
+            "up to rowptr[n]) or lists a column outside 0..n-1; its weights are NaN");
+    return MFT_ERR_ARG;
+  }
   if (status[1] != 0) {
     put_err(err, err_len, "mft_weights_noalloc: a stencil is longer than kmax = " +
-                              std::to_string(kmax) + "; its weights were not computed");
+                              std::to_string(kmax) + "; its weights were not computed (NaN)");
     return MFT_ERR_ARG;
   }
   if (status[0] != 0x7F7F7F7F) {

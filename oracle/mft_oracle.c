@@ -849,7 +849,7 @@ int mfto_calc_fluxes(const mfto_semi* s, double* const* du, double* const* u, in
   for (int d = 0; d < s->dim; ++d) {
 #pragma omp parallel for num_threads(nthreads_or_default(nthreads)) schedule(static)
     for (int64_t e = 0; e < n; ++e) {
-      double uu[8], ff[8];
+      double uu[8], ff[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (int v = 0; v < V; ++v) uu[v] = u[v][e];
       flux_point(s, uu, d, ff);
       for (int v = 0; v < V; ++v) f[(size_t)v * n + e] = ff[v];

@@ -49,10 +49,23 @@ class _Diag(C.Structure):
     _fields_ = [("mean", C.c_double * 8), ("norms", C.c_double * 8)]
 
 
+_variant = "parity"
+
+
+def select_build(variant: str) -> None:
+    """"parity" (default, no FMA contraction: the checker) or "speed" (-O3 with
+    contraction: only for timing the CPU baseline).  Takes effect at the next lib()."""
+    global _lib, _variant
+    assert variant in ("parity", "speed")
+    if variant != _variant:
+        _variant = variant
+        _lib = None
+
+
 def lib():
     global _lib
     if _lib is None:
-        path = _build.build()
+        path = _build.build(variant=_variant)
         L = C.CDLL(str(path))
         L.mfto_pairwise_sum.restype = C.c_double
         L.mfto_pairwise_sum.argtypes = [F64P, C.c_int64, C.c_int64]

@@ -9,7 +9,8 @@ reference checkout can use the same inputs:
   knn (nv = 20, the reference default for 2D degree 3) and dx_min / dx_avg
   weights Dx, Dy for PHS r^3 with degree-3 polynomials
 
-Usage: python tests/golden/make_golden.py [path/to/reference/test/data/cyl_0_05]
+Usage: python tests/golden/make_golden.py <reference checkout>/test/data/cyl_0_05
+(the case prefix of the Medusa files; required).
 """
 import sys
 from pathlib import Path
@@ -43,4 +44,6 @@ def main(casename):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test/data/cyl_0_05")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout>/test/data/cyl_0_05")
+    main(sys.argv[1])
