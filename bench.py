@@ -1,14 +1,19 @@
 #!/usr/bin/env python
 """Benchmark of the RBF-FD rhs! hot path on one GB300 (replicas for --gpus N > 1).
 
-Workload: 2D compressible Euler isentropic vortex on the periodic square [-5,5]^2,
-N = 262,144 seeded jittered nodes, PHS r^3 + degree-3 polynomials, 35-node stencils,
-FP64 weights and states, residual-viscosity source with the HistoryCallback
-(approx_order 3), SSP-RK3.  One step = one SSP-RK3 step = 3 rhs! evaluations.
-Metric: node-RHS updates/s = nodes * rhs! evaluations / device seconds.
+Headline workload (--workload riemann, the default): 2D compressible Euler four-quadrant
+Riemann problem on the periodic unit square, N = 1,048,576 seeded jittered nodes, PHS r^3 +
+degree-3 polynomials, 35-node stencils, FP64 weights and states, residual viscosity with
+the HistoryCallback (approx_order 3) plus Tominec hyperviscosity (c = 1), SSP-RK3 with
+dt = 0.1 h.  One step = one SSP-RK3 step = 3 rhs! evaluations.  Metric: node-RHS
+updates/s = nodes * rhs! evaluations / device seconds.  The FP64 form's gathers run in
+double-word FP32 arithmetic (the engine default); the same workload with FP64 fused
+multiply-adds and with the FP32-apply form are reported beside it, and the isentropic
+vortex at N = 262,144 (with its L2 error against the exact solution at t = 1) as a
+second workload.
 
---impl reference runs the CPU restatement of the reference's rhs! (the oracle: the
-reference is Julia and no Julia toolchain exists on the box) on all host cores,
+--impl reference runs the CPU restatement of the reference's rhs! (the oracle, -O3 build:
+the reference is Julia and no Julia toolchain exists on the box) on all host cores,
 same workload and metric.
 """
 import argparse
@@ -31,24 +36,31 @@ import numpy as np  # noqa: E402
 
 METRIC = "node-RHS updates/s"
 UNIT = "node-rhs/s"
-N_SIDE = 512
 K_STENCIL = 35
-DT_FACTOR = 0.2          # dt = 0.2 h
 RHS_PER_STEP = 3
-DFMA_PEAK_GFMA = 528.3   # measured FP64 FMA rate of this GB300 (probe in profiles/)
+SIDES = {"riemann": 1024, "vortex": 512}
+DT_FACTOR = {"riemann": 0.1, "vortex": 0.2}     # dt = factor * h
+HV = {"riemann": True, "vortex": False}          # Tominec hyperviscosity on
 
-# Algorithmic bytes per node and launch (FP64 form, V=4, D=2, k=35, int32 indices):
-#   fwd_gather: idx 4k + weights 2*8k + state read 32 + du_p write 32 + t=Du write 64
-#   rev_gather: idx 4k + weights 2*8k + s read 64 + du_p 32 + u_s 32 + u_n 32 + out 32
-BYTES = {
-    "fp64": {"fwd_gather": 4 * 35 + 16 * 35 + 32 + 32 + 64,
-             "rev_gather": 4 * 35 + 16 * 35 + 64 + 32 + 32 + 32 + 32},
-    "fp32": {"fwd_gather": 4 * 35 + 8 * 35 + 16 + 16 + 32,
-             "rev_gather": 4 * 35 + 8 * 35 + 32 + 16 + 32 + 32 + 32 + 16},
-}
-# FP64 FMAs per node and launch: fwd 14 per stencil entry (t: 8, du rows 2-4: 6),
-# rev 8 per reverse-adjacency entry (mean in-degree = k).
-DFMA = {"fwd_gather": 14 * 35, "rev_gather": 8 * 35}
+
+def _kernel_bytes(prec, hv):
+    """Algorithmic bytes per node and launch (V = 4, D = 2, k = 35, int32 indices; a
+    neighbour's record counted once, as the scope formula does).
+    fwd_gather: idx 4k + weights (2 [+1 lap]) * s k + u V s + du_p V s + t 2V s [+ q V s]
+    rev_gather: idx 4k + weights (2 [+1 lap]) * s k + s 2V s [+ q V s] + du_p V s
+                + u_s 32 + u_n 32 + out 32 (FP64 state) [+ FP32 shadow 16]"""
+    s = 8 if prec == "fp64" else 4
+    k = K_STENCIL
+    nw = 3 if hv else 2
+    fwd = 4 * k + nw * s * k + 4 * s + 4 * s + 8 * s + (4 * s if hv else 0)
+    rev = 4 * k + nw * s * k + 8 * s + (4 * s if hv else 0) + 4 * s + 96 + (16 if prec == "fp32" else 0)
+    return {"fwd_gather": fwd, "rev_gather": rev}
+
+
+# Products (one multiply-add each) per node and launch: fwd 14 per stencil entry (t: 8,
+# du rows 2-4: 6) [+ 4 for q = lap u]; rev 8 per reverse-adjacency entry [+ 4 lap'].
+def _kernel_fmas(hv):
+    return {"fwd_gather": (18 if hv else 14) * K_STENCIL, "rev_gather": (12 if hv else 8) * K_STENCIL}
 
 
 def parse():
@@ -57,29 +69,36 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n-side", type=int, default=N_SIDE)
+    ap.add_argument("--workload", default="riemann", choices=["riemann", "vortex"])
+    ap.add_argument("--side", type=int, default=0, help="nodes per side (0: the workload's)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ens-members", type=int, default=64,
                     help="members of the ensemble measurement (0 skips it)")
     ap.add_argument("--only", default="all",
-                    choices=["all", "adjoint", "riemann", "weights", "igr", "fp32", "setup"],
+                    choices=["all", "adjoint", "riemann", "weights", "igr", "fp32", "setup",
+                             "rates", "dfma", "vortex"],
                     help="run one auxiliary measurement alone")
     ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
     ap.add_argument("--igr", type=int, default=1, help="1 runs the IGR-source measurement")
     ap.add_argument("--setup", type=int, default=1,
-                    help="1 runs the set-up measurement (KNN and weights of the headline cloud)")
+                    help="1 runs the set-up measurement (KNN and weights of the vortex cloud)")
     ap.add_argument("--weights-n", type=int, default=1048576,
                     help="stencils of the batched-weights measurement (0 skips it)")
     ap.add_argument("--riemann-side", type=int, default=1024,
-                    help="nodes per side of the Riemann FP32/FP64 measurement (0 skips it)")
+                    help="nodes per side of the Riemann FP32/FP64 run to t = 0.2 (0 skips it)")
+    ap.add_argument("--vortex-side", type=int, default=512,
+                    help="nodes per side of the vortex measurement (0 skips it)")
     ap.add_argument("--adj-steps", type=int, default=500,
                     help="SSP-RK3 steps of the adjoint measurement")
     ap.add_argument("--adj-tend", type=float, default=0.5,
                     help="end time of the adjoint measurement")
     ap.add_argument("--adj-side", type=int, default=256,
                     help="nodes per side of the adjoint measurement (0 skips it)")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.side <= 0:
+        a.side = SIDES[a.workload]
+    return a
 
 
 def dist_setup():
@@ -152,19 +171,30 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def build_problem(n_side, prec, device):
+def build_problem(workload, side, prec, device, arith="auto"):
+    """The workload through the package's Julia-mirroring API (GPU KNN, weights, layout).
+    Returns (semi, domain, u0, dt, n)."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
-    pts, per, h = W.vortex_cloud(n_side)
     eq = M.CompressibleEulerEquations2D(1.4)
     basis = M.PointCloudBasis(M.Point2D(), 3, approximation_type=M.RBF(M.PolyharmonicSpline(3)),
                               nv=K_STENCIL)
-    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=device, precision=prec))
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=device, precision=prec,
+                                                           fp64_arith=arith))
+    if workload == "vortex":
+        pts, per, h = W.vortex_cloud(side)
+        ic = lambda x, t, e: W.isentropic_vortex(x, t)
+    else:
+        pts, h = W.riemann_cloud(side)
+        per = (1.0, 1.0)
+        ic = lambda x, t, e: W.riemann_ic(x)
     domain = M.PointCloudDomain(solver, pts, period=per)
-    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, domain, c_rv=1.0, c_uw=1.0))
-    semi = M.SemidiscretizationHyperbolic(domain, eq, lambda x, t, e: W.isentropic_vortex(x, t),
-                                          solver, source_terms=src)
-    return semi, domain, semi.compute_coefficients(0.0), DT_FACTOR * h
+    terms = {"rv": M.SourceResidualViscosityTominec(solver, eq, domain, c_rv=1.0, c_uw=1.0)}
+    if HV[workload]:
+        terms["hv"] = M.SourceHyperviscosityTominec(solver, eq, domain, c=1.0)
+    semi = M.SemidiscretizationHyperbolic(domain, eq, ic, solver,
+                                          source_terms=M.SourceTerms(**terms))
+    return semi, domain, semi.compute_coefficients(0.0), DT_FACTOR[workload] * h, pts.shape[0]
 
 
 def timed_steps(ctx, u0, dt, warmup, steps, pg, clocks=None):
@@ -218,7 +248,7 @@ def run_ensemble(args, local, pg):
         return M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
                                               solver, source_terms=src)
 
-    dt = DT_FACTOR * min(c[2] for c in clouds)
+    dt = DT_FACTOR["vortex"] * min(c[2] for c in clouds)
     ens = M.PointCloudEnsemble(solver, [c[0] for c in clouds], period=(10.0, 10.0))
     semi = semi_of(ens)
     u0 = semi.compute_coefficients(0.0)
@@ -272,7 +302,7 @@ def run_setup(args, local):
     from meshfree_gb300 import _lib as L
     from meshfree_gb300 import workloads as W
     from oracle import oracle as O
-    pts, per, h = W.vortex_cloud(args.n_side)
+    pts, per, h = W.vortex_cloud(args.vortex_side or SIDES["vortex"])
     n = pts.shape[0]
     ctx = L.Context(local)
     ctx.set_points(pts, per)
@@ -455,7 +485,7 @@ def run_igr(args, local):
     rhs! evaluation): SSP-RK3 steps with graphs, against the same steps without it."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
-    pts, per, h = W.vortex_cloud(args.n_side)
+    pts, per, h = W.vortex_cloud(args.vortex_side or SIDES["vortex"])
     n = pts.shape[0]
     basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
     solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64"))
@@ -469,10 +499,10 @@ def run_igr(args, local):
         u0 = semi.compute_coefficients(0.0)
         ctx = dom.ctx
         ctx.set_state(u0, 0.0)
-        ctx.ssprk33(DT_FACTOR * h, 2, use_graph=True)
+        ctx.ssprk33(DT_FACTOR["vortex"] * h, 2, use_graph=True)
         ctx.set_state(u0, 0.0)
         ctx.region_begin()
-        ctx.ssprk33(DT_FACTOR * h, args.steps, use_graph=True)
+        ctx.ssprk33(DT_FACTOR["vortex"] * h, args.steps, use_graph=True)
         out[name] = ctx.region_end() / args.steps
     ctx.close()
     return {"workload": "isentropic vortex N=%d, k=%d, SourceIGR alpha=h^2, <= 20 CG iterations "
@@ -566,51 +596,79 @@ def run_adjoint(args, local, peaks):
                        "fp64_gfma_s": 8 * K_STENCIL * n / (per_launch * 1e-3) / 1e9 if launches else None}}
 
 
-# Whole-rhs! algorithmic bytes per node (2D Euler, V=4, k=35, int32 indices), the
+# Whole-rhs! algorithmic bytes per node and rhs! (2D Euler, V=4, k=35, int32 indices), the
 # formula of the scope table: plain fused rhs! (u read, D_x/D_y weights, indices, du
-# write) + the fused SSP-RK stage combination (u_n read) + the residual-viscosity
-# passes (D^T weights and indices, t = D u written and read, approx_du, eps).
-PATH_BYTES = {
-    "fp64": {"formula": "764 plain + 32 stage + 876 RV", "bytes": 764 + 32 + 876},
-    "fp32": {"formula": "452 plain + 32 stage (FP64 u_n) + 532 RV (FP32 weights/t)",
-             "bytes": 452 + 32 + (280 + 140 + 64 + 32 + 16)},
-}
+# write) + the fused SSP-RK stage combination (u_n read) + the residual-viscosity passes
+# (D^T weights and indices, t = D u written and read, approx_du, eps) [+ Tominec
+# hyperviscosity lap'(lap u): two gathers of lap weights and indices, q written and read].
+def path_bytes(prec, hv):
+    k = K_STENCIL
+    if prec == "fp64":
+        parts = [("plain", 764), ("stage", 32), ("RV", 876)]
+        if hv:
+            parts.append(("Tominec HV", 2 * (8 * k + 4 * k) + 2 * 4 * 8))
+    else:
+        parts = [("plain", 452), ("stage (FP64 u_n)", 32), ("RV (FP32 weights/t)", 532)]
+        if hv:
+            parts.append(("Tominec HV", 2 * (4 * k + 4 * k) + 2 * 4 * 4))
+    return {"formula": " + ".join("%d %s" % (b, nm) for nm, b in parts),
+            "bytes": sum(b for _, b in parts)}
+
+
 SPEC_HBM_GBS = 8000.0    # the nominal HBM figure the scope table quotes beside the measured one
 
 
-def path_roofline(node_rhs_per_s, prec, peaks):
+def path_roofline(node_rhs_per_s, prec, hv, peaks):
     """HBM roofline of the whole rhs! from the end-to-end node-RHS rate."""
-    b = PATH_BYTES[prec]
+    b = path_bytes(prec, hv)
     achieved = b["bytes"] * node_rhs_per_s / 1e9
     return {"bytes_per_node_rhs": b["bytes"], "formula": b["formula"], "achieved_gbs": achieved,
             "frac_of_measured": achieved / peaks["hbm_gbs"],
             "frac_of_8tbs": achieved / SPEC_HBM_GBS}
 
 
-def roofline(prof, n, prec, peaks):
+def roofline(prof, n, prec, hv, peaks, arith=None, tag=None):
+    """Roofline of the kernel with the largest share of the profiled steps: algorithmic
+    bytes per launch / its average CUDA-event duration, against the measured HBM copy
+    bandwidth; for the FP64 form also its multiply-adds per second against the measured
+    FP64 (DFMA arithmetic) or FP32 (double-word arithmetic, 12 FP32 operations per
+    product) rate."""
     name = max(prof, key=lambda k: prof[k][0])
     ms, launches = prof[name]
     per_launch = ms / launches
-    bpn = BYTES[prec].get(name)
-    out = {"kernel": name, "avg_launch_ms": per_launch, "launches": launches}
+    bpn = _kernel_bytes(prec, hv).get(name)
+    out = {"kernel": name, "avg_launch_ms": per_launch, "launches": launches,
+           "share_of_profiled_step": ms / sum(v[0] for v in prof.values())}
     if bpn is not None:
         achieved = bpn * n / (per_launch * 1e-3) / 1e9
         out.update({"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                     "algorithmic_bytes_per_node": bpn, "peak_source": peaks["source"]})
-    traffic = ncu_traffic(name, prec)
+    traffic = ncu_traffic(name, tag) if tag else None
     out["traffic"] = None if traffic is None else traffic * n
-    out["traffic_source"] = None if traffic is None else "profiles/ ncu dram bytes per node x N"
-    if prec == "fp64" and name in DFMA:
-        g = DFMA[name] * n / (per_launch * 1e-3) / 1e9
-        out["fp64_issue"] = {"achieved_gfma_s": g, "peak_gfma_s": DFMA_PEAK_GFMA,
-                             "frac": g / DFMA_PEAK_GFMA, "dfma_per_node": DFMA[name]}
+    out["traffic_source"] = (None if traffic is None else
+                             "profiles/ncu_%s_%s.md: ncu DRAM bytes per node x N" % (name, tag))
+    fmas = _kernel_fmas(hv).get(name)
+    if prec == "fp64" and fmas and peaks.get("fma_rates"):
+        g = fmas * n / (per_launch * 1e-3)
+        if arith == "dfma":
+            pk = peaks["fma_rates"]["fp64"]
+            out["fp64_issue"] = {"achieved_gfma_s": g / 1e9, "peak_gfma_s": pk / 1e9,
+                                 "frac": g / pk, "fma_per_node": fmas,
+                                 "peak_source": "mft_measure_fma_rate (this run)"}
+        else:
+            pk = peaks["fma_rates"]["fp32"] / 12.0
+            out["fp32_issue"] = {"achieved_gproducts_s": g / 1e9,
+                                 "peak_gproducts_s": pk / 1e9, "frac": g / pk,
+                                 "products_per_node": fmas,
+                                 "note": "double-word product + compensated sum = 12 FP32 "
+                                         "operations; peak = measured FP32 FMA rate / 12"}
     return out
 
 
-def ncu_traffic(kernel, prec):
+def ncu_traffic(kernel, tag):
     """DRAM bytes per node of one launch from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / ("ncu_%s_%s.md" % (kernel, prec))
+    f = ROOT / "profiles" / ("ncu_%s_%s.md" % (kernel, tag))
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -627,31 +685,51 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def cpu_baseline_oracle(n_side, max_steps, nthreads, min_seconds=10.0, single_seconds=4.0):
-    """The oracle's rhs! + SSP-RK3 on the host cores over a bounded number of steps, with
-    all `nthreads` cores and with one (the reference's own SpMV and flux loops are
-    serial).  The operators are built once, with all cores, outside the timed regions.
-    Returns {threads: (node-rhs/s, seconds, steps)}."""
+def oracle_problem(workload, side, nthreads):
+    """The same workload in the oracle (-O3 timing build): KNN, weights, operators (and
+    lap' lap for the hyperviscosity), outside any timed region."""
     from oracle import oracle as O
     from meshfree_gb300 import workloads as W
-    pts, per, h = W.vortex_cloud(n_side)
+    O.select_build("speed")
+    if workload == "vortex":
+        pts, per, h = W.vortex_cloud(side)
+        u0 = W.isentropic_vortex(pts, 0.0)
+    else:
+        pts, h = W.riemann_cloud(side)
+        per = (1.0, 1.0)
+        u0 = W.riemann_ic(pts)
     n = pts.shape[0]
-    idx, _, _, davg = O.knn(pts, K_STENCIL, period=per, nthreads=nthreads)
+    idx, _, dmin, davg = O.knn(pts, K_STENCIL, period=per, nthreads=nthreads)
     rowptr = np.arange(n + 1, dtype=np.int64) * K_STENCIL
     w = O.weights(pts, rowptr, idx.ravel(), period=per, nthreads=nthreads)
     ops = O.operators_from_stencils(n, rowptr, idx.ravel(), w)
-    semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=(O.SRC_RV,), h=davg)
-    u0 = W.isentropic_vortex(pts, 0.0)
+    kw = {}
+    srcs = [O.SRC_RV]
+    if HV[workload]:
+        w2 = O.weights(pts, rowptr, idx.ravel(), period=per, deriv_order=2, nthreads=nthreads)
+        lap = O.csr_add(O.operators_from_stencils(n, rowptr, idx.ravel(), w2))
+        kw = {"hv": O.ata(lap, nthreads=nthreads), "hv_gamma": 1.0 * dmin ** 4.5}
+        srcs.append(O.SRC_HV_TOMINEC)
+    semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=tuple(srcs), h=davg, **kw)
+    return O, semi, u0, DT_FACTOR[workload] * h, n
+
+
+def cpu_baseline_oracle(workload, side, max_steps, nthreads, min_seconds=10.0,
+                        single_seconds=4.0):
+    """The oracle's rhs! + SSP-RK3 (-O3 build) on the host cores over a bounded number of
+    steps, with all `nthreads` cores and with one (the reference's own SpMV and flux loops
+    are serial).  Returns {threads: (node-rhs/s, seconds, steps)}."""
+    O, semi, u0, dt, n = oracle_problem(workload, side, nthreads)
     out = {}
     for nt, budget in ((nthreads, min_seconds), (1, single_seconds)):
         hist = O.History(semi, 3)
         t0 = time.perf_counter()
-        O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, 1, history=hist, nthreads=nt)  # warm-up
+        O.ssprk33(semi, u0, 0.0, dt, 1, history=hist, nthreads=nt)  # warm-up
         per_step = (time.perf_counter() - t0) / 1.33    # 4 rhs! evaluations in a 1-step call
-        done = int(min(max_steps, max(2, budget / per_step)))   # a sample of ~budget s
+        done = int(min(max_steps, max(1, budget / per_step)))   # a sample of ~budget s
         hist = O.History(semi, 3)
         t0 = time.perf_counter()
-        O.ssprk33(semi, u0, 0.0, DT_FACTOR * h, done, history=hist, nthreads=nt)
+        O.ssprk33(semi, u0, 0.0, dt, done, history=hist, nthreads=nt)
         sec = time.perf_counter() - t0
         out[nt] = (n * RHS_PER_STEP * done / sec, sec, done)
     return out
@@ -662,18 +740,8 @@ def run_reference(args):
     if rank != 0:
         return
     nthreads = os.cpu_count() or 1
-    n = args.n_side ** 2
-    from oracle import oracle as O
-    from meshfree_gb300 import workloads as W
-    pts, per, h = W.vortex_cloud(args.n_side)
-    idx, _, _, davg = O.knn(pts, K_STENCIL, period=per, nthreads=nthreads)
-    rowptr = np.arange(n + 1, dtype=np.int64) * K_STENCIL
-    w = O.weights(pts, rowptr, idx.ravel(), period=per, nthreads=nthreads)
-    ops = O.operators_from_stencils(n, rowptr, idx.ravel(), w)
-    semi = O.Semi(pts, ops, eq="euler", gamma=1.4, sources=(O.SRC_RV,), h=davg)
-    u0 = W.isentropic_vortex(pts, 0.0)
+    O, semi, u0, dt, n = oracle_problem(args.workload, args.side, nthreads)
     hist = O.History(semi, 3)
-    dt = DT_FACTOR * h
     u, t = O.ssprk33(semi, u0, 0.0, dt, args.warmup, history=hist, nthreads=nthreads)
     t0 = time.perf_counter()
     O.ssprk33(semi, u, t, dt, args.steps, history=hist, nthreads=nthreads)
@@ -684,31 +752,59 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3 / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_dict(n, "fp64"),
+        "config": config_dict(args.workload, n, "fp64"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": "full workload, %d SSP-RK3 steps after %d warm-up"
-                                   % (args.steps, args.warmup)},
+                                   % (args.steps, args.warmup),
+                         "build": _oracle_flags()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "C restatement of the reference rhs! (Julia is not installed); OpenMP over rows",
     }
     print(json.dumps(line), flush=True)
 
 
-def config_dict(n, prec):
-    return {"workload": "2D Euler isentropic vortex, periodic [-5,5]^2, N=%d jittered nodes, "
-                        "PHS r^3 + degree-3 polynomials, k=%d, residual viscosity + history "
-                        "(order 3), SSP-RK3 dt=0.2h; one step = 3 rhs! evaluations" % (n, K_STENCIL),
-            "nodes": n, "stencil": K_STENCIL, "precision": prec,
-            "l2": "inputs larger than L2 (operator arrays ~%d MB)" % (n * K_STENCIL * 40 // 2 ** 20),
+def _oracle_flags():
+    from oracle import build as B
+    return B.flags("speed")
+
+
+def config_dict(workload, n, prec, arith="dw"):
+    if workload == "vortex":
+        wl = ("2D Euler isentropic vortex, periodic [-5,5]^2, N=%d jittered nodes, PHS r^3 + "
+              "degree-3 polynomials, k=%d, residual viscosity + history (order 3), SSP-RK3 "
+              "dt=0.2h; one step = 3 rhs! evaluations" % (n, K_STENCIL))
+    else:
+        wl = ("2D Euler four-quadrant Riemann problem, periodic unit square, N=%d jittered nodes, "
+              "PHS r^3 + degree-3 polynomials, k=%d, residual viscosity + history (order 3) + "
+              "Tominec hyperviscosity (c=1), SSP-RK3 dt=0.1h; one step = 3 rhs! evaluations"
+              % (n, K_STENCIL))
+    return {"workload": wl, "nodes": n, "stencil": K_STENCIL, "precision": prec,
+            "fp64_gather_arithmetic": arith if prec == "fp64" else None,
+            "l2": "inputs larger than L2 (operator arrays ~%d MB)"
+                  % (n * K_STENCIL * (60 if HV[workload] else 40) // 2 ** 20),
             "parallelism": "replicas"}
+
+
+def timed_workload(args, workload, side, prec, arith, local, pg, clocks=None):
+    """Build + the timed region of one workload/form: value, per-kernel profile, end state."""
+    semi, dom, u0, dt, n = build_problem(workload, side, prec, local, arith)
+    ms, prof, clk, u_end, ms_prof = timed_steps(dom.ctx, u0, dt, args.warmup, args.steps, pg,
+                                                clocks)
+    ms = max_over_ranks(pg, ms)
+    return dict(semi=semi, dom=dom, u0=u0, dt=dt, n=n, ms=ms, prof=prof, clk=clk, u=u_end,
+                ms_prof=ms_prof, value=n * RHS_PER_STEP * args.steps / (ms * 1e-3))
+
+
+def _kernels(prof):
+    return {k: {"ms": v[0], "launches": v[1], "us_per_launch": v[0] / v[1] * 1e3}
+            for k, v in prof.items()}
 
 
 def run_fp32(args, local, peaks):
     """The FP32-apply form alone on the headline workload, with the gather mapping chosen
     by --gather (profiling runs of the FP32 kernels)."""
     from meshfree_gb300 import _lib as L
-    n = args.n_side ** 2
-    _, dom, u0, dt = build_problem(args.n_side, "fp32", local)
+    semi, dom, u0, dt, n = build_problem(args.workload, args.side, "fp32", local)
     ctx = dom.ctx
     ctx.set_option(L.OPT_GATHER, {"auto": L.GATHER_AUTO, "thread": L.GATHER_THREAD,
                                   "staged": L.GATHER_STAGED}[args.gather])
@@ -717,15 +813,71 @@ def run_fp32(args, local, peaks):
            "ms_per_step": ms / args.steps, "gather": args.gather,
            "mapping": {"fwd_gather": ctx.get_option(L.OPT_TUNED_FWD),
                        "rev_gather": ctx.get_option(L.OPT_TUNED_REV)},
-           "kernels_us": {k: v[0] / v[1] * 1e3 for k, v in prof.items()},
-           "roofline": roofline(prof, n, "fp32", peaks)}
+           "kernels": _kernels(prof),
+           "roofline": roofline(prof, n, "fp32", HV[args.workload], peaks,
+                                tag="fp32_" + args.workload)}
     ctx.close()
     return out
+
+
+def run_one_form(args, local, peaks, prec, arith):
+    """One form of the headline workload alone (profiling runs)."""
+    r = timed_workload(args, args.workload, args.side, prec, arith, local, None)
+    out = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
+           "kernels": _kernels(r["prof"]),
+           "roofline": roofline(r["prof"], r["n"], prec, HV[args.workload], peaks, arith,
+                                tag="%s%s_%s" % (prec, arith if prec == "fp64" else "",
+                                                 args.workload))}
+    r["dom"].ctx.close()
+    return out
+
+
+def run_vortex(args, local, peaks):
+    """The isentropic vortex (N = side^2, RV + history): the FP64 form (double-word
+    gathers) and the FP32-apply form, their throughput over the timed steps, and each one's
+    L2 density error against the exact vortex at t = 1 (this workload's own accuracy
+    check), stepped with per-step graphs."""
+    side = args.vortex_side
+    out = {}
+    for prec in ("fp64", "fp32"):
+        r = timed_workload(args, "vortex", side, prec, "auto", local, None)
+        ctx, dt, n = r["dom"].ctx, r["dt"], r["n"]
+        nsteps = int(round(1.0 / dt))
+        ctx.history_init(3)
+        ctx.set_state(r["u0"], 0.0)
+        ctx.region_begin()
+        ctx.ssprk33(dt, nsteps, use_graph=True)
+        ms_t1 = ctx.region_end()
+        u, t = ctx.get_state()
+        from meshfree_gb300 import workloads as W
+        ex = W.isentropic_vortex(r["semi"].domain.points, t)
+        l2 = float(np.linalg.norm(u[0] - ex[0]) / np.linalg.norm(ex[0]))
+        out[prec] = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
+                     "kernels": _kernels(r["prof"]),
+                     "roofline": roofline(r["prof"], n, prec, False, peaks, "dw",
+                                          tag="%s_vortex" % ("fp64dw" if prec == "fp64" else prec)),
+                     "path_roofline": path_roofline(r["value"], prec, False, peaks),
+                     "to_t1": {"steps": nsteps, "t": t, "ms": ms_t1,
+                               "l2_density_err_vs_exact": l2}}
+        ctx.close()
+    out["workload"] = config_dict("vortex", side * side, "fp64")["workload"]
+    out["fp32_speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def fma_rates(local):
+    from meshfree_gb300 import _lib as L
+    ctx = L.Context(local)
+    r = {"fp64": ctx.fma_rate(0), "fp32": ctx.fma_rate(1)}
+    ctx.close()
+    return r
 
 
 def run_ours(args):
     ws, rank, local, pg = dist_setup()
     peaks = load_peaks()
+    peaks["fma_rates"] = fma_rates(local)
+    hv = HV[args.workload]
     if args.only != "all":           # one auxiliary measurement alone (profiling runs)
         if rank == 0:
             legs = {"adjoint": lambda: run_adjoint(args, local, peaks),
@@ -733,50 +885,64 @@ def run_ours(args):
                     "weights": lambda: run_weights(args, local),
                     "igr": lambda: run_igr(args, local),
                     "fp32": lambda: run_fp32(args, local, peaks),
-                    "setup": lambda: run_setup(args, local)}
+                    "dfma": lambda: run_one_form(args, local, peaks, "fp64", "dfma"),
+                    "vortex": lambda: run_vortex(args, local, peaks),
+                    "setup": lambda: run_setup(args, local),
+                    "rates": lambda: {k: v / 1e9 for k, v in peaks["fma_rates"].items()}}
             leg = legs[args.only]()
             print(json.dumps({args.only: leg}), flush=True)
         return
-    n = args.n_side ** 2
-    semi, domain, u0, dt = build_problem(args.n_side, "fp64", local)
-    ctx = domain.ctx
+    # headline: the FP64 form (double-word gathers) of the workload
     clocks = Clocks(local) if rank == 0 else None
-    ms, prof, clk, u64, ms_prof = timed_steps(ctx, u0, dt, args.warmup, args.steps, pg, clocks)
-    ms_max = max_over_ranks(pg, ms)
-    value = n * RHS_PER_STEP * args.steps * ws / (ms_max * 1e-3)
-    launches = sum(v[1] for v in prof.values())
-    roof = roofline(prof, n, "fp64", peaks)
+    r64 = timed_workload(args, args.workload, args.side, "fp64", "auto", local, pg, clocks)
+    n = r64["n"]
+    value = r64["value"] * ws
+    launches = sum(v[1] for v in r64["prof"].values())
+    tag = "fp64dw_" + args.workload
+    roof = roofline(r64["prof"], n, "fp64", hv, peaks, "dw", tag=tag)
+
+    # the same workload with FP64 fused multiply-adds in the gathers
+    rd = timed_workload(args, args.workload, args.side, "fp64", "dfma", local, pg)
+    dfma = {"value": rd["value"] * ws, "unit": UNIT, "ms_per_step": rd["ms"] / args.steps,
+            "dw_speedup": r64["value"] / rd["value"],
+            "dw_vs_dfma_rel_l2_after_steps": [
+                float(np.linalg.norm(r64["u"][v] - rd["u"][v]) / np.linalg.norm(rd["u"][v]))
+                for v in range(4)],
+            "kernels": _kernels(rd["prof"]),
+            "roofline": roofline(rd["prof"], n, "fp64", hv, peaks, "dfma",
+                                 tag="fp64dfma_" + args.workload)}
+    rd["dom"].ctx.close()
 
     # FP32-apply form on the same workload and steps
-    semi32, dom32, _, _ = build_problem(args.n_side, "fp32", local)
-    ms32, prof32, _, u32, _ = timed_steps(dom32.ctx, u0, dt, args.warmup, args.steps, pg)
+    r32 = timed_workload(args, args.workload, args.side, "fp32", "auto", local, pg)
     from meshfree_gb300 import _lib as L
-    mapping = {"fwd_gather": dom32.ctx.get_option(L.OPT_TUNED_FWD),
-               "rev_gather": dom32.ctx.get_option(L.OPT_TUNED_REV)}
-    ms32_max = max_over_ranks(pg, ms32)
-    # same number of steps from u0 in both forms: L2 density error of FP32 vs FP64
+    mapping = {"fwd_gather": r32["dom"].ctx.get_option(L.OPT_TUNED_FWD),
+               "rev_gather": r32["dom"].ctx.get_option(L.OPT_TUNED_REV)}
+    u32, u64 = r32["u"], r64["u"]
     l2 = float(np.linalg.norm(u32[0] - u64[0]) / np.linalg.norm(u64[0]))
     linf = float(np.abs(u32[0] - u64[0]).max() / np.abs(u64[0]).max())
-    value32 = n * RHS_PER_STEP * args.steps * ws / (ms32_max * 1e-3)
-    roof32 = roofline(prof32, n, "fp32", peaks)
-    dom32.ctx.close()
+    value32 = r32["value"] * ws
+    roof32 = roofline(r32["prof"], n, "fp32", hv, peaks, tag="fp32_" + args.workload)
+    r32["dom"].ctx.close()
 
     # end to end through the host entry point: every step uploads u from pinned host
     # memory and downloads the new state
     import torch
+    ctx = r64["dom"].ctx
     pinned = torch.empty((4, n), dtype=torch.float64, pin_memory=True)
     uh = pinned.numpy()
-    uh[:] = u0
+    uh[:] = r64["u0"]
     ctx.history_init(3)
-    t = ctx.ssprk33_host(uh, 0.0, dt, 1)
+    t = ctx.ssprk33_host(uh, 0.0, r64["dt"], 1)
     barrier(pg)
     ctx.region_begin()
     for _ in range(args.steps):
-        t = ctx.ssprk33_host(uh, t, dt, 1)
+        t = ctx.ssprk33_host(uh, t, r64["dt"], 1)
     ms_e2e = max_over_ranks(pg, ctx.region_end())
     e2e = n * RHS_PER_STEP * args.steps * ws / (ms_e2e * 1e-3)
     ctx.close()
 
+    vortex = run_vortex(args, local, peaks) if args.vortex_side > 0 and rank == 0 else None
     ens = run_ensemble(args, local, pg) if args.ens_members > 0 else None
     adj = run_adjoint(args, local, peaks) if args.adj_side > 0 and rank == 0 else None
     rie = run_riemann(args, local) if args.riemann_side > 0 and rank == 0 else None
@@ -787,12 +953,13 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        res = cpu_baseline_oracle(args.n_side, 400, nthreads)
+        res = cpu_baseline_oracle(args.workload, args.side, 400, nthreads)
         v, sec, cpu_steps = res[nthreads]
         v1, sec1, steps1 = res[1]
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": "full N=%d, %d SSP-RK3 steps (%.1f s), oracle rhs! with OpenMP"
                          % (n, cpu_steps, sec),
+               "build": _oracle_flags(),
                "single_thread": {"value": v1, "unit": UNIT, "cores": 1,
                                  "sample": "full N=%d, %d SSP-RK3 steps (%.1f s)"
                                            % (n, steps1, sec1)}}
@@ -800,28 +967,30 @@ def run_ours(args):
         return
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": r64["ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_dict(n, "fp64"),
+        "config": config_dict(args.workload, n, "fp64", "dw"),
         "roofline": roof,
-        "path_roofline": path_roofline(value, "fp64", peaks),
+        "path_roofline": path_roofline(value / ws, "fp64", hv, peaks),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * n * 8,
                 "d2h_bytes_per_step": 4 * n * 8, "entry_point": "mft_ssprk33_host"},
         "gpu_launches": launches,
         "timing": "value: per-step CUDA graphs; kernels/roofline: same steps launched "
-                  "directly with CUDA events (%.3f ms/step)" % (ms_prof / args.steps),
-        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()},
-        "clocks": clk,
+                  "directly with CUDA events (%.3f ms/step)" % (r64["ms_prof"] / args.steps),
+        "kernels": _kernels(r64["prof"]),
+        "clocks": r64["clk"],
+        "fma_rates_per_s": peaks["fma_rates"],
+        "fp64_dfma": dfma,
         "fp32_apply": {"value": value32, "unit": UNIT, "speedup_vs_fp64": value32 / value,
                        "l2_density_err_vs_fp64": l2, "linf_density_err_vs_fp64": linf,
                        "steps": args.steps, "roofline": roof32,
-                       "path_roofline": path_roofline(value32, "fp32", peaks),
-                       "autotuned_mapping": mapping,
-                       "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof32.items()}},
+                       "path_roofline": path_roofline(value32 / ws, "fp32", hv, peaks),
+                       "autotuned_mapping": mapping, "kernels": _kernels(r32["prof"])},
+        "vortex": vortex,
         "ensemble": ens,
         "adjoint": adj,
-        "riemann": rie,
+        "riemann_to_t02": rie,
         "weights_batch": wts,
         "igr": igr,
         "setup": setup,

@@ -37,7 +37,7 @@ enum {
   MFT_ERR_CUDA = 2,        /* CUDA runtime error (message in mft_last_error) */
   MFT_ERR_STATE = 3,       /* call out of order (e.g. rhs before operators) */
   MFT_ERR_SINGULAR = 4,    /* a local saddle-point system had an exactly zero pivot */
-  MFT_ERR_NONFINITE = 5,   /* the device produced NaN/Inf (flag word set by kernels) */
+  MFT_ERR_NONFINITE = 5,   /* a du or stage value became NaN/Inf (outputs still written) */
   MFT_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
   MFT_ERR_UNSUPPORTED = 7, /* configuration not provided by this engine */
   MFT_ERR_NOMEM = 8        /* device or host allocation failed */
@@ -212,8 +212,16 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
  * MFT_GATHER_THREAD (one node per thread, direct loads), MFT_GATHER_STAGED (one warp
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
  * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
-enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2 };
+enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
+       MFT_OPT_FP64_ARITH = 3 };
 enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2 };
+/* MFT_OPT_FP64_ARITH: how the FP64 form's operator gathers form their sums of products.
+ * MFT_ARITH_DFMA: FP64 fused multiply-adds.  MFT_ARITH_DW: double-word FP32 arithmetic
+ * (weights, fluxes and neighbour states as unevaluated float pairs h + l, error-free
+ * products and sums on the FP32 pipe, ~48-bit significands; per-node values, the
+ * viscosity and the stage combination stay FP64); 2D Euler only, other equations use
+ * DFMA.  MFT_ARITH_AUTO (default) = MFT_ARITH_DW.  mft_get_option returns the setting. */
+enum { MFT_ARITH_AUTO = 0, MFT_ARITH_DFMA = 1, MFT_ARITH_DW = 2 };
 mft_status mft_set_option(mft_ctx* ctx, int option, int value);
 /* Reads an option; MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV return the mapping the
  * autotuner chose for the most recent forward / transpose gather configuration
@@ -227,6 +235,12 @@ mft_status mft_get_option(mft_ctx* ctx, int option, int* value);
  * reads the word as every staged gather's caller does.  Returns MFT_ERR_TIMEOUT (the
  * expected outcome) with the context still usable. */
 mft_status mft_selftest_bounded_wait(mft_ctx* ctx, int polls);
+
+/* Arithmetic-rate probe (no counterpart in the reference): the FMA throughput of the
+ * context's GPU, kind 0 = FP64 fused multiply-adds, 1 = FP32 ones, per second (many
+ * independent chains on every SM, best of three timed launches).  It is the
+ * denominator of the FP64-issue roofline that the benchmark reports. */
+mft_status mft_measure_fma_rate(mft_ctx* ctx, int kind, double* per_second);
 
 /* ---------------------------------------------------------------- rhs! */
 

@@ -276,6 +276,12 @@ void ensure_work(mft_ctx* c) {
     c->mean.alloc(8);
     c->norms.alloc(8);
   }
+  if (use_dw(c)) {
+    c->Fdw.alloc((size_t)n * 2 * V);
+    c->udw.alloc(nv);
+    c->tdw.alloc((size_t)n * 2 * V);
+    c->qdw.alloc(nv);
+  }
   if (c->precision == MFT_PREC_FP32) {
     for (auto* b : {&c->U32[0], &c->U32[1], &c->U32[2], &c->U32[3]}) b->alloc(nv);
     c->du_p32.alloc(nv);
@@ -300,6 +306,9 @@ void ensure_device_ops(mft_ctx* c) {
   // gathers keep node order, which keeps a warp's neighbours close in L1.
   const int rev_window = c->precision == MFT_PREC_FP64 ? kRevWindow : 0;
   if (c->rev.n == c->n && c->rev.window != rev_window) c->dev_dirty = true;
+  // double-word operator values are placed only while that form is in use
+  const bool dw = use_dw(c);
+  if (dw && !c->fwdw[0].p) c->dev_dirty = true;
   if (!c->dev_dirty) return;
   c->graph_valid = false;
   cudaStream_t s = c->stream;
@@ -318,6 +327,7 @@ void ensure_device_ops(mft_ctx* c) {
   for (int k = 0; k < kSlots; ++k) {
     if (!c->have_val[k]) {
       c->fw[k].release(); c->rw[k].release(); c->fw32[k].release(); c->rw32[k].release();
+      c->fwdw[k].release(); c->rwdw[k].release();
       continue;
     }
     const std::vector<double>& v = c->val[k];
@@ -328,8 +338,18 @@ void ensure_device_ops(mft_ctx* c) {
     c->rw32[k].alloc(c->rev.n_elems);
     for (auto* b : {&c->fw[k], &c->rw[k]}) b->zero(s);
     for (auto* b : {&c->fw32[k], &c->rw32[k]}) b->zero(s);
-    launch_scatter_values((int64_t)v.size(), c->fwd_pos.p, d_v.p, c->fw[k].p, c->fw32[k].p, s);
-    launch_scatter_values((int64_t)v.size(), c->rev_pos.p, d_v.p, c->rw[k].p, c->rw32[k].p, s);
+    if (dw) {
+      c->fwdw[k].alloc(c->fwd.n_elems);
+      c->rwdw[k].alloc(c->rev.n_elems);
+      for (auto* b : {&c->fwdw[k], &c->rwdw[k]}) b->zero(s);
+    } else {
+      c->fwdw[k].release();
+      c->rwdw[k].release();
+    }
+    launch_scatter_values((int64_t)v.size(), c->fwd_pos.p, d_v.p, c->fw[k].p, c->fw32[k].p,
+                          c->fwdw[k].p, s);
+    launch_scatter_values((int64_t)v.size(), c->rev_pos.p, d_v.p, c->rw[k].p, c->rw32[k].p,
+                          c->rwdw[k].p, s);
   }
   MFT_CUDA(cudaStreamSynchronize(s));
   c->dev_dirty = false;
@@ -468,6 +488,8 @@ void launch_fwd(mft_ctx* c, const FwdArgs& a) {
     c->last_fwd_choice = ch;
     if (ch > 0 && launch_fwd_f32_tma(a, ch, c->kerr.p, c->stream)) return;
     launch_fwd_f32(a, c->stream);
+  } else if (use_dw(c)) {
+    launch_fwd_dw(a, c->stream);
   } else {
     launch_fwd_f64(a, c->stream);
   }
@@ -478,6 +500,8 @@ void launch_rev(mft_ctx* c, const RevArgs& a) {
     c->last_rev_choice = ch;
     if (ch > 0 && launch_rev_f32_tma(a, ch, c->kerr.p, c->stream)) return;
     launch_rev_f32(a, c->stream);
+  } else if (use_dw(c)) {
+    launch_rev_dw(a, c->stream);
   } else {
     launch_rev_f64(a, c->stream);
   }
@@ -498,6 +522,8 @@ static void check_kernel_errors(mft_ctx* c) {
   if (e != 0) {
     c->kerr.zero(c->stream);
     MFT_CUDA(cudaStreamSynchronize(c->stream));
+    if (e == MFT_ERR_NONFINITE)
+      throw mft::Error(e, "the state or du became NaN or infinite (outputs were written)");
     throw mft::Error(e, "a device wait gave up (bulk-copy completion not observed)");
   }
 }
@@ -526,12 +552,17 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   const int64_t n = c->n;
   const int V = c->nvars;
   const bool f32 = c->precision == MFT_PREC_FP32;
+  const bool dw = use_dw(c);
   MFT_REQUIRE(!f32 || us32, MFT_ERR_STATE, "FP32 apply needs the FP32 state shadow");
+  MFT_REQUIRE(!dw || (c->Fdw.p && c->udw.p && c->tdw.p && c->qdw.p && c->fwdw[0].p &&
+                      c->rwdw[0].p),
+              MFT_ERR_STATE, "double-word work buffers not allocated");
 
   BcDev bc{c->d_tag.p, c->d_slot.p, c->d_normal.p, c->d_dvals.p};
   Epilogue ep = ep_in;
   ep.bc = bc;
   ep.has_bc = c->nb > 0;
+  ep.err = c->kerr.p;
   ep.u_s = us;
   ep.fused = f32 ? 1 : 0;
   ep.cdt = ep.kind == kStage2 ? 0.25 * ep.dt : ep.kind == kStage3 ? (2.0 / 3.0) * ep.dt : ep.dt;
@@ -631,8 +662,12 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ep.xadd = c->igr_add.p;
   }
 
-  // 2. flux per node (FP64 Euler)
-  if (!f32 && c->eq == MFT_EQ_EULER2D) {
+  // 2. flux per node (FP64 Euler; double-word pairs of the flux and the state for the
+  // double-word gathers)
+  if (dw) {
+    ProfScope ps(c, MFT_K_FLUX);
+    launch_prep_euler_dw(n, c->gamma, us, c->Fdw.p, c->udw.p, s);
+  } else if (!f32 && c->eq == MFT_EQ_EULER2D) {
     ProfScope ps(c, MFT_K_FLUX);
     launch_flux_f64(n, c->eq, V, c->gamma, us, c->F.p, s);
   }
@@ -669,6 +704,14 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   fa.q32 = c->q32.p;
   fa.final_epilogue = (iv < 0 && !tominec);
   fa.ep = ep;
+  if (dw) {
+    for (int d = 0; d < 3; ++d) fa.wdw[d] = d < c->dim ? c->fwdw[d].p : nullptr;
+    fa.wldw = wl_slot >= 0 ? c->fwdw[wl_slot].p : nullptr;
+    fa.Fdw = c->Fdw.p;
+    fa.udw = c->udw.p;
+    fa.tdw = c->tdw.p;
+    fa.qdw = c->qdw.p;
+  }
   {
     ProfScope ps(c, MFT_K_FWD);
     launch_fwd(c, fa);
@@ -690,6 +733,12 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   ra.q32 = c->q32.p;
   ra.s = c->t.p;
   ra.s32 = c->t32.p;
+  if (dw) {
+    for (int d = 0; d < 3; ++d) ra.wdw[d] = d < c->dim ? c->rwdw[d].p : nullptr;
+    ra.wldw = tominec ? c->rwdw[kSlotLap].p : nullptr;
+    ra.sdw = c->tdw.p;
+    ra.qdw = c->qdw.p;
+  }
 
   double* dp = c->du_p.p;
   float* dp32 = c->du_p32.p;
@@ -737,8 +786,9 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ea.norms = c->nseg > 0 ? c->seg_norms.p : c->norms.p;
     ea.seg_id = c->nseg > 0 ? c->d_seg_id.p : nullptr;
     ea.seg_h = c->nseg > 0 ? c->d_seg_h.p : nullptr;
-    ea.t = f32 ? nullptr : c->t.p;
+    ea.t = (f32 || dw) ? nullptr : c->t.p;
     ea.t32 = f32 ? c->t32.p : nullptr;
+    ea.tdw = dw ? c->tdw.p : nullptr;
     ea.eps = c->eps.p;
     ea.tab = c->capturing ? c->d_tab.p : nullptr;
     ea.ctr = c->d_ctr.p;
@@ -1202,6 +1252,11 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
       c->fsal_valid = false;
       for (int& k : c->tuned_fwd) k = -1;
       for (int& k : c->tuned_rev) k = -1;
+    } else if (option == MFT_OPT_FP64_ARITH) {
+      MFT_REQUIRE(value >= MFT_ARITH_AUTO && value <= MFT_ARITH_DW, MFT_ERR_ARG,
+                  "unknown FP64 arithmetic");
+      c->fp64_arith = value;
+      c->fsal_valid = false;
     } else {
       throw mft::Error(MFT_ERR_ARG, "unknown option");
     }
@@ -1227,6 +1282,7 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     if (option == MFT_OPT_GATHER) *value = c->gather_mode;
     else if (option == MFT_OPT_TUNED_FWD) *value = c->last_fwd_choice;
     else if (option == MFT_OPT_TUNED_REV) *value = c->last_rev_choice;
+    else if (option == MFT_OPT_FP64_ARITH) *value = c->fp64_arith;
     else throw mft::Error(MFT_ERR_ARG, "unknown option");
   });
 }

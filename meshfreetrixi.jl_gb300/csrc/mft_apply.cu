@@ -19,6 +19,7 @@
 #include <cmath>
 
 #include "mft_device.cuh"
+#include "mft_dw.cuh"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -617,6 +618,18 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
       for (int k = 0; k < 2 * V; ++k) a.t[i * 2 * V + k] = dmul(eps, a.t[i * 2 * V + k]);
     }
   }
+  if (a.tdw) {
+    // s = eps * t in double-word arithmetic (eps split once per node)
+    const float2 e2 = dw::split(eps);
+    float4* t4 = reinterpret_cast<float4*>(a.tdw) + i * V;
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const float4 x = t4[q];
+      const float2 lo = dw::mul(e2, make_float2(x.x, x.y));
+      const float2 hi = dw::mul(e2, make_float2(x.z, x.w));
+      t4[q] = make_float4(lo.x, lo.y, hi.x, hi.y);
+    }
+  }
   if (a.t32) {
     const float e32 = __double2float_rn(eps);
 #pragma unroll
@@ -759,12 +772,13 @@ __global__ void k_differs(const double* __restrict__ a, const double* __restrict
 
 __global__ void k_scatter_values(int64_t nnz, const int64_t* __restrict__ pos,
                                  const double* __restrict__ v, double* __restrict__ out,
-                                 float* __restrict__ out32) {
+                                 float* __restrict__ out32, float2* __restrict__ outdw) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= nnz) return;
   const int64_t p = pos[e];
   out[p] = v[e];
   if (out32) out32[p] = __double2float_rn(v[e]);
+  if (outdw) outdw[p] = dw::split(v[e]);
 }
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
@@ -774,9 +788,9 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 // ====================================================================== launchers
 
 void launch_scatter_values(int64_t nnz, const int64_t* pos, const double* v, double* out,
-                           float* out32, cudaStream_t s) {
+                           float* out32, float2* outdw, cudaStream_t s) {
   if (nnz <= 0) return;
-  k_scatter_values<<<grid_for(nnz, 256), 256, 0, s>>>(nnz, pos, v, out, out32);
+  k_scatter_values<<<grid_for(nnz, 256), 256, 0, s>>>(nnz, pos, v, out, out32, outdw);
   MFT_LAUNCH_CHECK();
 }
 

@@ -51,6 +51,7 @@ struct mft_ctx {
   mft::DBuf<int64_t> fwd_pos, rev_pos;  // CSR entry -> ELL element
   mft::DBuf<double> fw[kSlots], rw[kSlots];
   mft::DBuf<float> fw32[kSlots], rw32[kSlots];
+  mft::DBuf<float2> fwdw[kSlots], rwdw[kSlots];  // double-word pairs (FP64 form, Euler)
 
   // physics
   int eq = -1;
@@ -81,6 +82,7 @@ struct mft_ctx {
   std::vector<double> src_par;
   int precision = MFT_PREC_FP64;
   int gather_mode = MFT_GATHER_AUTO;
+  int fp64_arith = MFT_ARITH_AUTO;
   int tuned_fwd[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   int tuned_rev[4] = {-1, -1, -1, -1};
   int last_fwd_choice = -1, last_rev_choice = -1;
@@ -90,6 +92,7 @@ struct mft_ctx {
   mft::DBuf<float> U32[4];
   mft::DBuf<double> F, du_p, du_p2, t, q, hvf, eps, approx_du, soa, soa2, work_u, work_du;
   mft::DBuf<float> du_p32, du_p2_32, t32, q32, work_u32, work_du32;
+  mft::DBuf<float2> Fdw, udw, tdw, qdw;  // double-word FP64 form: per-node pairs
   mft::DBuf<double> red_partial, mean, norms;
   mft::DBuf<unsigned> red_counter;
   mft::DBuf<int> flag;
@@ -174,6 +177,12 @@ struct ProfScope {
 }  // namespace mft
 
 namespace mft {
+// The FP64 form's gathers run in double-word FP32 arithmetic (2D Euler; the
+// MFT_OPT_FP64_ARITH option); otherwise in FP64 fused multiply-adds.
+inline bool use_dw(const mft_ctx* c) {
+  return c->precision == MFT_PREC_FP64 && c->fp64_arith != MFT_ARITH_DFMA &&
+         c->eq == MFT_EQ_EULER2D && c->nvars == 4;
+}
 // Builds (if needed) the device ELL layouts and operator values.
 void ensure_device_ops(mft_ctx* c);
 // One rhs! evaluation on the AoS state `us` (device), with the given epilogue.

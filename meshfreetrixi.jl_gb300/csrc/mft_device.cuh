@@ -158,6 +158,15 @@ static __device__ __forceinline__ void finish_node(const Epilogue& ep, int64_t i
       }
       break;
   }
+  // non-finite outputs raise MFT_ERR_NONFINITE in the error word (the exponent field
+  // of NaN and infinity is all ones; a rare atomic, no cost on the normal path)
+  if (ep.err) {
+    bool bad = false;
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+      bad |= ((__double_as_longlong(o[v]) >> 52) & 0x7FF) == 0x7FF;
+    if (bad) atomicMax(ep.err, (int)MFT_ERR_NONFINITE);
+  }
 #pragma unroll
   for (int v = 0; v < V; ++v) ep.out[i * V + v] = o[v];
   if (ep.out32) {

@@ -1,0 +1,84 @@
+// Double-word FP32 arithmetic ("double-float": a value is an unevaluated sum h + l of two
+// floats with |l| <= ulp(h) / 2, 48 significand bits) for the FP64 form's gathers.
+//
+// On this part an FP64 fused multiply-add issues at 1/74 of the FP32 rate, and the FP64
+// gathers are bound by it.  The sums of products those gathers form are evaluated here
+// on the FP32 pipe with error-free transformations instead:
+//   * the exact product of the high parts by an FMA:  p = RN(a_h b_h),
+//     e = a_h b_h - p exactly = fma(a_h, b_h, -p)  (Dekker 1971, with an FMA);
+//   * the cross terms a_h b_l + a_l b_h folded into e (a_l b_l < 2^-48 |ab| is dropped);
+//   * the exact sum of the running high part and p by Knuth's TwoSum (branch-free),
+//     whose rounding error joins e in a float carry.
+// This is the compensated dot product "Dot2" of Ogita, Rump and Oishi (SIAM J. Sci.
+// Comput. 26(6), 2005) on double-word inputs (Joldes, Muller and Popescu, ACM TOMS
+// 44(2), 2017).  With u = 2^-24, a length-n sum of products carries the inputs' split
+// error (< 3 u^2 sum |a_i b_i|) and the carry's own rounding, at most gamma_n^2
+// sum |a_i b_i| with gamma_n = n u / (1 - n u) when every rounding error has the same
+// sign and its largest size (n = 35: 4.4e-12 of the condition scale sum |a_i b_i|);
+// errors of mixed sign give about sqrt(n) u^2 of it (~2e-14).  The result is rounded
+// once to FP64.  Every operation is an explicitly rounded intrinsic, so no contraction
+// or reassociation by the compiler can break the error-free steps.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mft {
+namespace dw {
+
+// x -> (h, l): h = RN32(x), l = RN32(x - h) (x - h is exact in FP64).
+static __device__ __forceinline__ float2 split(double x) {
+  const float h = __double2float_rn(x);
+  const float l = __double2float_rn(__dsub_rn(x, (double)h));
+  return make_float2(h, l);
+}
+
+static __device__ __forceinline__ double value(float2 a) {
+  return __dadd_rn((double)a.x, (double)a.y);
+}
+
+// Running sum of products: s is the float running sum, c the float carry of every
+// rounding error (products and sums).
+struct Acc {
+  float s, c;
+};
+
+static __device__ __forceinline__ Acc zero() { return Acc{0.f, 0.f}; }
+
+// acc += a * b (a, b double-word)
+static __device__ __forceinline__ void fma_acc(Acc& acc, float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float t = __fadd_rn(acc.s, p);
+  const float bp = __fsub_rn(t, acc.s);
+  const float err = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  acc.s = t;
+  acc.c = __fadd_rn(acc.c, __fadd_rn(err, e));
+}
+
+// The accumulated value rounded once to FP64.
+static __device__ __forceinline__ double to_double(const Acc& a) {
+  return __dadd_rn((double)a.s, (double)a.c);
+}
+
+// The accumulated value as a normalised double-word pair (TwoSum of s and c).
+static __device__ __forceinline__ float2 to_pair(const Acc& a) {
+  const float t = __fadd_rn(a.s, a.c);
+  const float bp = __fsub_rn(t, a.s);
+  const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(a.c, bp));
+  return make_float2(t, err);
+}
+
+// a * b for a double-word a and b, normalised (|e| <= ulp(p), so Fast2Sum is exact).
+static __device__ __forceinline__ float2 mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  const float t = __fadd_rn(p, e);
+  return make_float2(t, __fsub_rn(e, __fsub_rn(t, p)));
+}
+
+}  // namespace dw
+}  // namespace mft

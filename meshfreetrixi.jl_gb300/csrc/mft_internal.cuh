@@ -130,6 +130,9 @@ struct Epilogue {
   // (stage 2) or 2 dt / 3 (stage 3)
   int fused;
   double cdt;
+  // device error word: MFT_ERR_NONFINITE is raised into it (atomic max, so a timeout
+  // code stays) when a written du or stage value is NaN or infinite; null: no check
+  int* err;
 };
 
 // ------------------------------------------------------------------ launchers
@@ -138,10 +141,11 @@ struct Epilogue {
 void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaStream_t s);
 void launch_soa_from_aos(const double* aos, double* soa, int64_t n, int V, cudaStream_t s);
 void launch_aos_to_f32(const double* aos, float* a32, int64_t count, cudaStream_t s);
-// out[pos[e]] = v[e] (and out32[pos[e]] = (float) v[e] when out32 is not null): the
-// operator values of structure entry e placed at their sliced-ELL element.
+// out[pos[e]] = v[e] (and out32[pos[e]] = (float) v[e] when out32 is not null, and
+// outdw[pos[e]] = the double-word pair of v[e] when outdw is not null): the operator
+// values of structure entry e placed at their sliced-ELL element.
 void launch_scatter_values(int64_t nnz, const int64_t* pos, const double* v, double* out,
-                           float* out32, cudaStream_t s);
+                           float* out32, float2* outdw, cudaStream_t s);
 
 // One pointer per variable (pinned host memory mapped for the device, or device memory).
 struct VarPtrs {
@@ -185,8 +189,21 @@ struct FwdArgs {
   float* du_p32;
   int final_epilogue;   // 1: du is final here, apply BC2 + epilogue instead of writing du_p
   Epilogue ep;
+  // FP64 form in double-word arithmetic (Euler): weights, fluxes and states as (h, l)
+  // float pairs; t and q are written as pairs, du_p / hvf in FP64
+  const float2* wdw[3];
+  const float2* wldw;
+  const float2* Fdw;    // n x 2V pairs
+  const float2* udw;    // n x V pairs
+  float2* tdw;          // n x 2V pairs
+  float2* qdw;          // n x V pairs
 };
 void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
+// Double-word forms (mft_apply_dw.cu): per-node flux and state pairs, forward gather,
+// transpose gather.
+void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
+                          cudaStream_t s);
+void launch_fwd_dw(const FwdArgs& a, cudaStream_t s);
 void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 
 // Reductions for the residual viscosity normalisation (last-block-done pattern).
@@ -226,6 +243,7 @@ struct EpsArgs {
   double* t;               // n x 2V, scaled in place to eps*t
   double* eps;             // n (diagnostic copy)
   float* t32;              // FP32 path: scaled in place
+  float2* tdw;             // double-word FP64 form: n x 2V pairs, scaled in place
 };
 void launch_eps(const EpsArgs& a, cudaStream_t s);
 void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double* u, int mode,
@@ -258,8 +276,13 @@ struct RevArgs {
   double* du_p_out;
   float* du_p_out32;
   Epilogue ep;
+  const float2* wdw[3];  // double-word FP64 form: weights on the reverse layout
+  const float2* wldw;
+  const float2* sdw;     // n x 2V pairs (eps * t)
+  const float2* qdw;     // n x V pairs
 };
 void launch_rev_f64(const RevArgs& a, cudaStream_t s);
+void launch_rev_dw(const RevArgs& a, cudaStream_t s);
 void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 // Bulk-copy-staged FP32 gathers (Euler); return false when the case is not covered.
 // chunk: slots staged per bulk copy (4 or 8).

@@ -22,7 +22,8 @@ SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER, SRC_IGR = 0, 1, 2, 3, 4
 OP_GRAD, OP_LAP, OP_HV = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 LIM_DENSITY, LIM_PRESSURE = 0, 1
-OPT_GATHER, OPT_TUNED_FWD, OPT_TUNED_REV = 0, 1, 2
+OPT_GATHER, OPT_TUNED_FWD, OPT_TUNED_REV, OPT_FP64_ARITH = 0, 1, 2, 3
+ARITH_AUTO, ARITH_DFMA, ARITH_DW = 0, 1, 2
 GATHER_AUTO, GATHER_THREAD, GATHER_STAGED = 0, 1, 2
 
 # Every entry point of include/meshfree_gb300.h with (restype, argtypes).
@@ -52,6 +53,7 @@ SIGNATURES = {
     "mft_set_segments": (I32, [VP, I32, VP, VP]),
     "mft_get_option": (I32, [VP, I32, C.POINTER(I32)]),
     "mft_selftest_bounded_wait": (I32, [VP, I32]),
+    "mft_measure_fma_rate": (I32, [VP, I32, C.POINTER(DBL)]),
     "mft_rhs": (I32, [VP, VP, VP, I32, DBL]),
     "mft_rhs_device": (I32, [VP, VP, VP, DBL]),
     "mft_set_state": (I32, [VP, VP, I32, DBL]),
@@ -248,6 +250,12 @@ class Context:
         """Runs the bounded-wait self-test; returns its status code (MFT_ERR_TIMEOUT is
         the expected outcome) without raising."""
         return int(self.lib.mft_selftest_bounded_wait(self.h, polls))
+
+    def fma_rate(self, kind):
+        """FMAs per second of this GPU: kind 0 FP64, 1 FP32 (mft_measure_fma_rate)."""
+        r = C.c_double()
+        self.check(self.lib.mft_measure_fma_rate(self.h, kind, C.byref(r)))
+        return r.value
 
     # rhs! / stepping ----------------------------------------------------
     def rhs(self, du, u, t):

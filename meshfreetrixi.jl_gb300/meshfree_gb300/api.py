@@ -80,9 +80,12 @@ def PointCloudBasis(element_type, polydeg, approximation_type=None, nv=None):
 @dataclass
 class RBFFDEngineGB300:
     """The GB300 engine (the reference's RBFFDEngineCUDA slot).  precision is
-    "fp64" (FP64 weights, states and sums) or "fp32" (FP32 apply, FP64 RK)."""
+    "fp64" (FP64 weights, states and sums) or "fp32" (FP32 apply, FP64 RK).
+    fp64_arith: how the FP64 form's gathers form their sums of products -- "auto"
+    (= "dw"), "dw" (double-word FP32 arithmetic, 2D Euler) or "dfma" (FP64 FMAs)."""
     device: int = 0
     precision: str = "fp64"
+    fp64_arith: str = "auto"
 
 
 @dataclass
@@ -369,6 +372,8 @@ class SemidiscretizationHyperbolic:
         domain.operator(L.OP_GRAD, b.approximation_type.Nrbf, b.N, 1)
         ctx.set_equations(equations.kind, equations.params())
         ctx.set_precision(L.PREC_FP32 if solver.engine.precision == "fp32" else L.PREC_FP64)
+        ctx.set_option(L.OPT_FP64_ARITH, {"auto": L.ARITH_AUTO, "dw": L.ARITH_DW,
+                                          "dfma": L.ARITH_DFMA}[solver.engine.fp64_arith])
         kinds, ptr, idx, nrm = [], [0], [], []
         self._dirichlet = []
         for name, bc in self.boundary_conditions.items():

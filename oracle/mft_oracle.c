@@ -768,50 +768,83 @@ void mfto_spmv_t_accum(const mfto_csr* a, double alpha, const double* x, double*
 
 /* lap' * lap as SparseArrays.spmatmul forms it: H[i,j] = sum over ascending k
  * of lap[k,i]*lap[k,j] (first product assigned, the rest added). */
-int mfto_ata(const mfto_csr* a, int64_t* hrp, int32_t* hci, double* hval) {
-  int64_t n = a->n;
-  int64_t* mark = (int64_t*)malloc((size_t)n * sizeof(int64_t));
-  int64_t* pos = (int64_t*)malloc((size_t)n * sizeof(int64_t));
-  double* acc = (double*)malloc((size_t)n * sizeof(double));
-  int32_t* cols = (int32_t*)malloc((size_t)n * sizeof(int32_t));
-  if (!mark || !pos || !acc || !cols) { free(mark); free(pos); free(acc); free(cols); return -2; }
-  for (int64_t i = 0; i < n; ++i) mark[i] = -1;
+/* CSC view of a CSR matrix by a counting sort: each column lists its rows ascending. */
+void mfto_csr_to_csc(int64_t n, const int64_t* rp, const int32_t* ci, const double* val,
+                     int64_t* cp, int32_t* ri, double* valt) {
+  for (int64_t j = 0; j <= n; ++j) cp[j] = 0;
+  for (int64_t p = 0; p < rp[n]; ++p) cp[ci[p] + 1] += 1;
+  for (int64_t j = 0; j < n; ++j) cp[j + 1] += cp[j];
+  int64_t* next = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+  for (int64_t j = 0; j < n; ++j) next[j] = cp[j];
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t p = rp[i]; p < rp[i + 1]; ++p) {
+      const int64_t q = next[ci[p]]++;
+      ri[q] = (int32_t)i;
+      valt[q] = val[p];
+    }
+  free(next);
+}
+
+static int cmp_i32(const void* x, const void* y) {
+  const int32_t a = *(const int32_t*)x, b = *(const int32_t*)y;
+  return (a > b) - (a < b);
+}
+
+/* lap' * lap: row i of the product accumulates lap[k, i] * lap[k, j] over the stored
+ * entries k of column i in ascending order, then over row k's entries (SparseArrays'
+ * spmatmul order for each entry).  Rows are independent, so they run in parallel; the
+ * per-row order and hence every value is the same for any thread count.  hci == NULL:
+ * count pass (hrp filled); otherwise fill pass (hrp from the count pass). */
+int mfto_ata(const mfto_csr* a, int64_t* hrp, int32_t* hci, double* hval, int nthreads) {
+  const int64_t n = a->n;
+  int failed = 0;
   if (!hci) hrp[0] = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    int64_t cnt = 0;
-    for (int64_t p = a->cp[i]; p < a->cp[i + 1]; ++p) {
-      int32_t k = a->ri[p];
-      double aki = a->valt[p];
-      for (int64_t q = a->rp[k]; q < a->rp[k + 1]; ++q) {
-        int32_t j = a->ci[q];
-        double prod = aki * a->val[q];
-        if (mark[j] != i) {
-          mark[j] = i;
-          pos[j] = cnt;
-          cols[cnt++] = j;
-          acc[j] = prod;
+#pragma omp parallel num_threads(nthreads_or_default(nthreads))
+  {
+    int64_t* mark = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+    double* acc = (double*)malloc((size_t)n * sizeof(double));
+    int32_t* cols = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    if (!mark || !acc || !cols) {
+#pragma omp atomic write
+      failed = 1;
+    } else {
+      for (int64_t i = 0; i < n; ++i) mark[i] = -1;
+#pragma omp for schedule(dynamic, 256)
+      for (int64_t i = 0; i < n; ++i) {
+        int64_t cnt = 0;
+        for (int64_t p = a->cp[i]; p < a->cp[i + 1]; ++p) {
+          const int32_t k = a->ri[p];
+          const double aki = a->valt[p];
+          for (int64_t q = a->rp[k]; q < a->rp[k + 1]; ++q) {
+            const int32_t j = a->ci[q];
+            const double prod = aki * a->val[q];
+            if (mark[j] != i) {
+              mark[j] = i;
+              cols[cnt++] = j;
+              acc[j] = prod;
+            } else {
+              acc[j] = acc[j] + prod;
+            }
+          }
+        }
+        if (!hci) {
+          hrp[i + 1] = cnt;
         } else {
-          acc[j] = acc[j] + prod;
+          qsort(cols, (size_t)cnt, sizeof(int32_t), cmp_i32);
+          for (int64_t m = 0; m < cnt; ++m) {
+            hci[hrp[i] + m] = cols[m];
+            hval[hrp[i] + m] = acc[cols[m]];
+          }
         }
       }
     }
-    if (!hci) {
-      hrp[i + 1] = hrp[i] + cnt;
-    } else {
-      /* sort columns ascending (insertion sort of small lists) */
-      for (int64_t m = 1; m < cnt; ++m) {
-        int32_t v = cols[m];
-        int64_t l = m - 1;
-        while (l >= 0 && cols[l] > v) { cols[l + 1] = cols[l]; --l; }
-        cols[l + 1] = v;
-      }
-      for (int64_t m = 0; m < cnt; ++m) {
-        hci[hrp[i] + m] = cols[m];
-        hval[hrp[i] + m] = acc[cols[m]];
-      }
-    }
+    free(mark);
+    free(acc);
+    free(cols);
   }
-  free(mark); free(pos); free(acc); free(cols);
+  if (failed) return -2;
+  if (!hci)
+    for (int64_t i = 0; i < n; ++i) hrp[i + 1] += hrp[i];
   return 0;
 }
 

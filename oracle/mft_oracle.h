@@ -170,7 +170,9 @@ void mfto_spmv_t_accum(const mfto_csr* a, double alpha, const double* x, double*
 /* H = A' * A as SparseArrays spmatmul forms it (per entry: ascending k, product
  * then add).  Two-call protocol: with hcol == NULL only hrp (n+1) is filled;
  * the second call fills hci/hval.  Columns ascending within a row. */
-int mfto_ata(const mfto_csr* a, int64_t* hrp, int32_t* hci, double* hval);
+int mfto_ata(const mfto_csr* a, int64_t* hrp, int32_t* hci, double* hval, int nthreads);
+void mfto_csr_to_csc(int64_t n, const int64_t* rp, const int32_t* ci, const double* val,
+                     int64_t* cp, int32_t* ri, double* valt);
 
 /* A16  time_deriv_weights!  history.jl:131-152:  w = scale * (A' \ b). */
 int mfto_time_deriv_weights(int m, const double* t, double* w);

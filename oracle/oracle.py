@@ -98,8 +98,10 @@ def lib():
             getattr(L, name).argtypes = [C.POINTER(_Csr), C.c_double, F64P, F64P, C.c_int]
         L.mfto_spmv.restype = None
         L.mfto_spmv.argtypes = [C.POINTER(_Csr), F64P, F64P, C.c_int]
+        L.mfto_csr_to_csc.restype = None
+        L.mfto_csr_to_csc.argtypes = [C.c_int64, I64P, I32P, F64P, I64P, I32P, F64P]
         L.mfto_ata.restype = C.c_int
-        L.mfto_ata.argtypes = [C.POINTER(_Csr), I64P, C.c_void_p, C.c_void_p]
+        L.mfto_ata.argtypes = [C.POINTER(_Csr), I64P, C.c_void_p, C.c_void_p, C.c_int]
         L.mfto_time_deriv_weights.restype = C.c_int
         L.mfto_time_deriv_weights.argtypes = [C.c_int, F64P, F64P]
         _lib = L
@@ -249,19 +251,40 @@ def csr_from_triplets(n, rows, cols, vals):
                 out[m] = acc
             r, c, v = r[starts], c[starts], out
     rp = np.zeros(n + 1, dtype=np.int64)
-    np.add.at(rp, r + 1, 1)
-    rp = np.cumsum(rp)
-    order_t = np.lexsort((r, c))
-    cp = np.zeros(n + 1, dtype=np.int64)
-    np.add.at(cp, c + 1, 1)
-    cp = np.cumsum(cp)
-    return Csr(n, rp, c.astype(np.int32), np.ascontiguousarray(v), cp,
-               r[order_t].astype(np.int32), np.ascontiguousarray(v[order_t]))
+    rp[1:] = np.cumsum(np.bincount(r, minlength=n))
+    return csr_from_sorted(n, rp, c.astype(np.int32), np.ascontiguousarray(v))
+
+
+def csr_from_sorted(n, rp, ci, val):
+    """Csr from CSR arrays whose rows hold ascending, distinct columns; the CSC view lists
+    each column's rows ascending (a stable sort of the columns keeps row order)."""
+    rp = np.ascontiguousarray(rp, dtype=np.int64)
+    ci = np.ascontiguousarray(ci, dtype=np.int32)
+    val = np.ascontiguousarray(val, dtype=np.float64)
+    cp = np.empty(n + 1, dtype=np.int64)
+    ri = np.empty(ci.size, dtype=np.int32)
+    valt = np.empty(ci.size, dtype=np.float64)
+    lib().mfto_csr_to_csc(n, rp, ci, val, cp, ri, valt)
+    return Csr(n, rp, ci, val, cp, ri, valt)
 
 
 def operators_from_stencils(n, rowptr, stencil, w):
-    """compute_operators.jl:443-452: one CSR per derivative direction."""
-    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(rowptr))
+    """compute_operators.jl:443-452: one CSR per derivative direction (sparse(...) of the
+    stencil triplets).  Stencils of one size without repeated nodes are sorted row by row;
+    anything else goes through the general triplet path, which sums duplicates."""
+    sizes = np.diff(rowptr)
+    if n > 0 and np.all(sizes == sizes[0]):
+        k = int(sizes[0])
+        st = np.asarray(stencil, dtype=np.int64).reshape(n, k)
+        order = np.argsort(st, axis=1, kind="stable")
+        cs = np.take_along_axis(st, order, axis=1)
+        if k < 2 or np.all(cs[:, 1:] != cs[:, :-1]):
+            base = (np.arange(n, dtype=np.int64) * k)[:, None]
+            perm = (base + order).ravel()
+            ci = cs.ravel().astype(np.int32)
+            return [csr_from_sorted(n, np.asarray(rowptr, dtype=np.int64).copy(), ci,
+                                    np.ascontiguousarray(w[perm, d])) for d in range(w.shape[1])]
+    rows = np.repeat(np.arange(n, dtype=np.int64), sizes)
     return [csr_from_triplets(n, rows, stencil, w[:, d]) for d in range(w.shape[1])]
 
 
@@ -272,22 +295,21 @@ def csr_add(ops):
     for o in ops[1:]:
         assert np.array_equal(o.ci, base.ci) and np.array_equal(o.rp, base.rp)
         val = val + o.val
-    n = base.n
-    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(base.rp))
-    return csr_from_triplets(n, rows, base.ci, val)
+    return csr_from_sorted(base.n, base.rp.copy(), base.ci.copy(), val)
 
 
-def ata(a: Csr) -> Csr:
-    """lap' * lap with SparseArrays' per-entry accumulation order."""
+def ata(a: Csr, nthreads=8) -> Csr:
+    """lap' * lap with SparseArrays' per-entry accumulation order (rows in parallel)."""
     L = lib()
     hrp = np.zeros(a.n + 1, dtype=np.int64)
-    L.mfto_ata(C.byref(a.cstruct()), hrp, None, None)
+    if L.mfto_ata(C.byref(a.cstruct()), hrp, None, None, nthreads):
+        raise MemoryError("mfto_ata")
     nnz = int(hrp[-1])
     hci = np.empty(nnz, dtype=np.int32)
     hval = np.empty(nnz, dtype=np.float64)
-    L.mfto_ata(C.byref(a.cstruct()), hrp, hci.ctypes.data, hval.ctypes.data)
-    rows = np.repeat(np.arange(a.n, dtype=np.int64), np.diff(hrp))
-    return csr_from_triplets(a.n, rows, hci, hval)
+    if L.mfto_ata(C.byref(a.cstruct()), hrp, hci.ctypes.data, hval.ctypes.data, nthreads):
+        raise MemoryError("mfto_ata")
+    return csr_from_sorted(a.n, hrp, hci, hval)
 
 
 def spmv(a: Csr, x, nthreads=8):

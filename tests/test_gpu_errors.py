@@ -70,3 +70,27 @@ def test_bounded_wait_reports_timeout_and_context_survives(gpu_lib):
     ctx.rhs(du, u.copy(), 0.0)
     assert np.isfinite(du).all()
     ctx.close()
+
+
+def test_nonfinite_state_is_reported(gpu_lib):
+    """A NaN in the state handed to rhs! (and to SSP-RK3 stepping, direct and graph
+    replay) makes the call return MFT_ERR_NONFINITE: the stage epilogue flags NaN or
+    infinite outputs in the device error word, which the host reads at the end of the
+    call.  The outputs are still written, the word is cleared, and the context keeps
+    working with a finite state."""
+    L, W, ctx, pts = _ctx()
+    u = W.isentropic_vortex(pts, 0.0)
+    bad = u.copy()
+    bad[0, 5] = float("nan")
+    du = np.empty_like(u)
+    assert _code(lambda: ctx.rhs(du, bad.copy(), 0.0)) == L.MFT_ERR_NONFINITE
+    assert np.isnan(du).any()
+    ctx.rhs(du, u.copy(), 0.0)
+    assert np.isfinite(du).all()
+    for graph in (False, True):
+        ctx.set_state(bad, 0.0)
+        assert _code(lambda: ctx.ssprk33(1e-3, 2, use_graph=graph)) == L.MFT_ERR_NONFINITE
+        ctx.set_state(u, 0.0)
+        ctx.ssprk33(1e-3, 2, use_graph=graph)
+        assert np.isfinite(ctx.get_state()[0]).all()
+    ctx.close()

@@ -4,7 +4,9 @@ The operators are produced by the oracle and handed to the GPU through the 1-bas
 CSC entry point (mft_load_csc), as the reference's SparseMatrixCSC would be.
 Tolerance (FP64): per variable, max_i |du_gpu - du_ref| <= 1e-12 * max_i s_i with
 the condition scale s = |D||F| + sum_d |D_d|'(|eps| |D_d||u|) + gamma |lap|'|lap||u|
-(+ gamma |H||u|); states mutated by strong BCs must agree bit for bit.
+(+ gamma |H||u|); states mutated by strong BCs must agree bit for bit.  The Euler cases
+run with both arithmetics of the FP64 form's gathers: double-word FP32 ("dw", the
+default) and FP64 fused multiply-adds ("dfma"), under the same tolerance.
 """
 import numpy as np
 import pytest
@@ -41,7 +43,11 @@ def cyl_ops(oracle, cyl):
     return dict(ops=ops, lap=lap, H_tom=H_tom, H_fly=H_fly)
 
 
-def _setup(oracle, gpu_lib, cyl, cyl_ops, case, eq="euler", success_iter=0, approx_du=None):
+ARITH = ["dw", "dfma"]
+
+
+def _setup(oracle, gpu_lib, cyl, cyl_ops, case, eq="euler", success_iter=0, approx_du=None,
+           arith="auto"):
     from meshfree_gb300 import _lib as L
     pts = cyl["positions"]
     n = pts.shape[0]
@@ -71,6 +77,8 @@ def _setup(oracle, gpu_lib, cyl, cyl_ops, case, eq="euler", success_iter=0, appr
     if approx_du is not None:
         semi.approx_du[:] = approx_du.ravel()
     ctx = L.Context(0)
+    ctx.set_option(L.OPT_FP64_ARITH, {"auto": L.ARITH_AUTO, "dw": L.ARITH_DW,
+                                      "dfma": L.ARITH_DFMA}[arith])
     ctx.set_points(pts)
     load_ops_into(ctx, cyl_ops["ops"],
                   lap=cyl_ops["lap"] if "tominec" in srcs else None,
@@ -117,16 +125,18 @@ def _check(semi, ctx, u0, ops, srcs, hv, hv_gamma, eq="euler", lap_op=None):
     return err
 
 
+@pytest.mark.parametrize("arith", ARITH)
 @pytest.mark.parametrize("case", list(CASES))
-def test_rhs_euler_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, case):
+def test_rhs_euler_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, case, arith):
     pts = cyl["positions"]
     u0 = ic_bumpy(pts)
-    semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, case)
+    semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, case, arith=arith)
     _check(semi, ctx, u0, cyl_ops["ops"], CASES[case], hv, g, lap_op=cyl_ops["lap"])
 
 
+@pytest.mark.parametrize("arith", ARITH)
 @pytest.mark.parametrize("case", ["rv", "rv_tominec", "tominec_rv", "flyer_rv"])
-def test_rhs_residual_viscosity_active(oracle, gpu_lib, cyl, cyl_ops, case):
+def test_rhs_residual_viscosity_active(oracle, gpu_lib, cyl, cyl_ops, case, arith):
     """success_iter > 0: eps = min(eps_rv, eps_uw) from a history estimate."""
     pts = cyl["positions"]
     u0 = ic_bumpy(pts)
@@ -135,7 +145,7 @@ def test_rhs_residual_viscosity_active(oracle, gpu_lib, cyl, cyl_ops, case):
     rng = np.random.default_rng(5)
     approx = np.ascontiguousarray(du_plain * (1 + 0.05 * rng.standard_normal(du_plain.shape)))
     semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, case, success_iter=3,
-                              approx_du=approx)
+                              approx_du=approx, arith=arith)
     _check(semi, ctx, u0, cyl_ops["ops"], CASES[case], hv, g, lap_op=cyl_ops["lap"])
 
 

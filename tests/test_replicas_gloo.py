@@ -55,7 +55,7 @@ def test_reference_arm_prints_on_rank_zero_only():
     checking the early return with a tiny workload)."""
     code = (
         "import sys; sys.path.insert(0, %r); sys.argv = ['bench.py', '--impl', 'reference', "
-        "'--n-side', '16', '--steps', '1', '--warmup', '1']; import bench; bench.main()"
+        "'--side', '16', '--steps', '1', '--warmup', '1']; import bench; bench.main()"
         % str(ROOT))
     outs = _launch(code)
     lines = [[json.loads(x) for x in o.splitlines() if x.startswith("{")] for o in outs]
