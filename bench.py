@@ -76,7 +76,7 @@ def parse():
                     help="members of the ensemble measurement (0 skips it)")
     ap.add_argument("--only", default="all",
                     choices=["all", "adjoint", "riemann", "weights", "igr", "fp32", "setup",
-                             "rates", "dfma", "vortex"],
+                             "rates", "dw", "dfma", "vortex"],
                     help="run one auxiliary measurement alone")
     ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
@@ -850,7 +850,7 @@ def run_vortex(args, local, peaks):
         ms_t1 = ctx.region_end()
         u, t = ctx.get_state()
         from meshfree_gb300 import workloads as W
-        ex = W.isentropic_vortex(r["semi"].domain.points, t)
+        ex = W.isentropic_vortex(r["dom"].pd.points, t)
         l2 = float(np.linalg.norm(u[0] - ex[0]) / np.linalg.norm(ex[0]))
         out[prec] = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
                      "kernels": _kernels(r["prof"]),
@@ -885,6 +885,7 @@ def run_ours(args):
                     "weights": lambda: run_weights(args, local),
                     "igr": lambda: run_igr(args, local),
                     "fp32": lambda: run_fp32(args, local, peaks),
+                    "dw": lambda: run_one_form(args, local, peaks, "fp64", "dw"),
                     "dfma": lambda: run_one_form(args, local, peaks, "fp64", "dfma"),
                     "vortex": lambda: run_vortex(args, local, peaks),
                     "setup": lambda: run_setup(args, local),

@@ -213,7 +213,11 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
  * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
-       MFT_OPT_FP64_ARITH = 3 };
+       MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4 };
+/* MFT_OPT_LAYOUT_ORDER: 1 (default) assigns the operator rows to threads along a Morton
+ * curve of the node coordinates, so that a warp's 32 rows are a compact patch whose
+ * neighbours overlap; 0 keeps node order.  Results are identical either way (every row
+ * keeps its own summation order); only the memory locality of the gathers changes. */
 enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2 };
 /* MFT_OPT_FP64_ARITH: how the FP64 form's operator gathers form their sums of products.
  * MFT_ARITH_DFMA: FP64 fused multiply-adds.  MFT_ARITH_DW: double-word FP32 arithmetic

@@ -140,10 +140,11 @@ __global__ void __launch_bounds__(kBlock) k_adj_f64(AdjArgs a) {
 template <int V, bool BC>
 __global__ void __launch_bounds__(kBlock) k_lap_masked(int64_t n, EllView ell, const double* wl,
                                                        const double* lam, BcDev bc, double* q) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= n) return;
-  const int64_t base = ell.slice_off[i >> 5] + (i & 31);
-  const int len = ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= n) return;
+  const int64_t i = ell_node(ell, r);
+  const int64_t base = ell.slice_off[r >> 5] + (r & 31);
+  const int len = ell.row_len[r];
   double acc[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) acc[v] = 0;

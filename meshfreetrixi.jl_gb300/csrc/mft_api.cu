@@ -44,14 +44,17 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 // ---------------------------------------------------------------- ELL layout
 
 // Builds a sliced ELL over rows of a CSR-like structure.  pos[e] receives the
-// ELL element of structure entry e.  With window > 0 the rows are ordered by length,
-// longest first, inside each run of `window` consecutive rows (stable, so rows stay
-// near their neighbours in memory): the 32 rows of a slice then have nearly equal
-// lengths and the lanes of a warp finish together.
+// ELL element of structure entry e.  Layout row r holds node base[r] (base: a spatial
+// order of the nodes, see morton_order; null: node r).  With window > 0 the rows are
+// then ordered by length, longest first, inside each run of `window` consecutive rows
+// (stable, so rows stay near their neighbours): the 32 rows of a slice then have nearly
+// equal lengths and the lanes of a warp finish together.
 void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& cols,
-               EllBuf& ell, std::vector<int64_t>& pos, cudaStream_t s, int window = 0) {
+               EllBuf& ell, std::vector<int64_t>& pos, cudaStream_t s, int window = 0,
+               const std::vector<int32_t>* base = nullptr) {
   std::vector<int32_t> order(n);
-  std::iota(order.begin(), order.end(), 0);
+  if (base) order = *base;
+  else std::iota(order.begin(), order.end(), 0);
   if (window > 0) {
 #pragma omp parallel for schedule(static)
     for (int64_t w0 = 0; w0 < n; w0 += window) {
@@ -104,11 +107,52 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   ell.n_elems = ne;
   ell.max_len = maxlen;
   ell.window = window;
+  ell.ordered = base != nullptr;
   ell.slice_off.upload(soff, s);
   ell.row_len.upload(rlen, s);
   ell.col.upload(col, s);
-  if (window > 0) ell.perm.upload(order, s);
+  if (window > 0 || base) ell.perm.upload(order, s);
   else ell.perm.release();
+}
+
+// Layout order of the nodes along a Morton (Z-order) curve of their coordinates: the 32
+// rows of a slice are then a compact patch of the cloud instead of a strip of node
+// numbers, so the neighbours the slice gathers overlap more and are found in L1 more
+// often.  Coordinates are quantised over the cloud's bounding box to 31 bits per axis
+// (2D) or 21 (3D) and their bits interleaved; ties keep node order.  Only which thread forms which
+// row changes: every row's sum keeps its own order, so the results are unchanged.
+std::vector<int32_t> morton_order(int dim, int64_t n, const std::vector<double>& xyz) {
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d) {
+    lo[d] = hi[d] = n ? xyz[d] : 0.0;
+    for (int64_t i = 1; i < n; ++i) {
+      lo[d] = std::min(lo[d], xyz[i * dim + d]);
+      hi[d] = std::max(hi[d], xyz[i * dim + d]);
+    }
+  }
+  const int bits = dim == 1 ? 62 : (dim == 2 ? 31 : 21);
+  const double top = (double)((1ull << bits) - 1);
+  std::vector<uint64_t> key(n);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    uint64_t k = 0;
+    uint64_t q[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+      const double span = hi[d] - lo[d];
+      double x = span > 0 ? (xyz[i * dim + d] - lo[d]) / span * top : 0.0;
+      if (!(x >= 0)) x = 0;
+      if (x > top) x = top;
+      q[d] = (uint64_t)x;
+    }
+    for (int b = bits - 1; b >= 0; --b)
+      for (int d = 0; d < dim; ++d) k = (k << 1) | ((q[d] >> b) & 1ull);
+    key[i] = k;
+  }
+  std::vector<int32_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  return order;
 }
 
 }  // namespace
@@ -306,6 +350,8 @@ void ensure_device_ops(mft_ctx* c) {
   // gathers keep node order, which keeps a warp's neighbours close in L1.
   const int rev_window = c->precision == MFT_PREC_FP64 ? kRevWindow : 0;
   if (c->rev.n == c->n && c->rev.window != rev_window) c->dev_dirty = true;
+  const bool spatial = c->layout_order == 1 && !c->xyz.empty();
+  if (c->fwd.n == c->n && c->fwd.ordered != spatial) c->dev_dirty = true;
   // double-word operator values are placed only while that form is in use
   const bool dw = use_dw(c);
   if (dw && !c->fwdw[0].p) c->dev_dirty = true;
@@ -313,10 +359,13 @@ void ensure_device_ops(mft_ctx* c) {
   c->graph_valid = false;
   cudaStream_t s = c->stream;
   std::vector<int64_t> pos;
-  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s);
+  std::vector<int32_t> zorder;
+  if (spatial) zorder = morton_order(c->dim, c->n, c->xyz);
+  const std::vector<int32_t>* base = spatial ? &zorder : nullptr;
+  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base);
   c->fwd_pos.upload(pos, s);
   std::vector<int64_t> rpos_csc;
-  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window);
+  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base);
   std::vector<int64_t> rpos(rpos_csc.size());
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < (int64_t)rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
@@ -704,6 +753,38 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   fa.q32 = c->q32.p;
   fa.final_epilogue = (iv < 0 && !tominec);
   fa.ep = ep;
+  // viscosity arguments (used by the viscosity kernel, or formed in the double-word
+  // forward gather's epilogue when the viscosity's partial du is complete there)
+  EpsArgs ea{};
+  if (iv >= 0) {
+    const int kind = c->src_kind[iv];
+    const double* par = &c->src_par[iv * 4];
+    ea.n = n;
+    ea.eq = c->eq;
+    ea.V = V;
+    ea.kind = kind;
+    ea.gamma = c->gamma;
+    ea.ax = c->adv[0];
+    ea.ay = c->adv[1];
+    ea.c_rv = kind == MFT_SRC_RV ? par[0] : 0.0;
+    ea.c_uw = kind == MFT_SRC_RV ? par[1] : par[0];
+    ea.h = kind == MFT_SRC_RV ? par[2] : par[1];
+    ea.success_iter = c->success_iter;
+    ea.u = us;
+    ea.u32 = f32 ? us32 : nullptr;
+    ea.hvf = nullptr;
+    ea.approx_du = c->approx_du.p;
+    ea.norms = c->nseg > 0 ? c->seg_norms.p : c->norms.p;
+    ea.seg_id = c->nseg > 0 ? c->d_seg_id.p : nullptr;
+    ea.seg_h = c->nseg > 0 ? c->d_seg_h.p : nullptr;
+    ea.t = (f32 || dw) ? nullptr : c->t.p;
+    ea.t32 = f32 ? c->t32.p : nullptr;
+    ea.tdw = dw ? c->tdw.p : nullptr;
+    ea.eps = c->eps.p;
+    ea.tab = c->capturing ? c->d_tab.p : nullptr;
+    ea.ctr = c->d_ctr.p;
+  }
+  const bool fuse_eps = dw && iv >= 0 && !(tominec && hv_first);
   if (dw) {
     for (int d = 0; d < 3; ++d) fa.wdw[d] = d < c->dim ? c->fwdw[d].p : nullptr;
     fa.wldw = wl_slot >= 0 ? c->fwdw[wl_slot].p : nullptr;
@@ -711,6 +792,15 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     fa.udw = c->udw.p;
     fa.tdw = c->tdw.p;
     fa.qdw = c->qdw.p;
+  }
+  if (fuse_eps) {
+    // the norms of the residual viscosity must be complete before the gather
+    if (forked) MFT_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+    else if (c->src_kind[iv] == MFT_SRC_RV) rv_norms(s);
+    fa.fuse_eps = 1;
+    fa.ea = ea;
+    fa.ea.du_p = c->du_p.p;
+    prepare_eps(fa.ea);
   }
   {
     ProfScope ps(c, MFT_K_FWD);
@@ -760,38 +850,11 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     dp32 = c->du_p2_32.p;
   }
 
-  if (iv >= 0) {
-    const int kind = c->src_kind[iv];
-    const double* par = &c->src_par[iv * 4];
+  if (iv >= 0 && !fuse_eps) {
     if (forked) MFT_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
-    else if (kind == MFT_SRC_RV) rv_norms(s);
-    EpsArgs ea{};
-    ea.n = n;
-    ea.eq = c->eq;
-    ea.V = V;
-    ea.kind = kind;
-    ea.gamma = c->gamma;
-    ea.ax = c->adv[0];
-    ea.ay = c->adv[1];
-    ea.c_rv = kind == MFT_SRC_RV ? par[0] : 0.0;
-    ea.c_uw = kind == MFT_SRC_RV ? par[1] : par[0];
-    ea.h = kind == MFT_SRC_RV ? par[2] : par[1];
-    ea.success_iter = c->success_iter;
-    ea.u = us;
-    ea.u32 = f32 ? us32 : nullptr;
+    else if (c->src_kind[iv] == MFT_SRC_RV) rv_norms(s);
     ea.du_p = f32 ? nullptr : dp;
     ea.du_p32 = f32 ? dp32 : nullptr;
-    ea.hvf = nullptr;
-    ea.approx_du = c->approx_du.p;
-    ea.norms = c->nseg > 0 ? c->seg_norms.p : c->norms.p;
-    ea.seg_id = c->nseg > 0 ? c->d_seg_id.p : nullptr;
-    ea.seg_h = c->nseg > 0 ? c->d_seg_h.p : nullptr;
-    ea.t = (f32 || dw) ? nullptr : c->t.p;
-    ea.t32 = f32 ? c->t32.p : nullptr;
-    ea.tdw = dw ? c->tdw.p : nullptr;
-    ea.eps = c->eps.p;
-    ea.tab = c->capturing ? c->d_tab.p : nullptr;
-    ea.ctr = c->d_ctr.p;
     ProfScope ps(c, MFT_K_EPS);
     launch_eps(ea, s);
   }
@@ -1252,6 +1315,10 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
       c->fsal_valid = false;
       for (int& k : c->tuned_fwd) k = -1;
       for (int& k : c->tuned_rev) k = -1;
+    } else if (option == MFT_OPT_LAYOUT_ORDER) {
+      MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG, "layout order: 0 node order, 1 Morton");
+      c->layout_order = value;
+      c->fsal_valid = false;
     } else if (option == MFT_OPT_FP64_ARITH) {
       MFT_REQUIRE(value >= MFT_ARITH_AUTO && value <= MFT_ARITH_DW, MFT_ERR_ARG,
                   "unknown FP64 arithmetic");
@@ -1283,6 +1350,7 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_TUNED_FWD) *value = c->last_fwd_choice;
     else if (option == MFT_OPT_TUNED_REV) *value = c->last_rev_choice;
     else if (option == MFT_OPT_FP64_ARITH) *value = c->fp64_arith;
+    else if (option == MFT_OPT_LAYOUT_ORDER) *value = c->layout_order;
     else throw mft::Error(MFT_ERR_ARG, "unknown option");
   });
 }

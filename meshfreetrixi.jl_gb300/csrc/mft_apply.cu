@@ -20,6 +20,7 @@
 
 #include "mft_device.cuh"
 #include "mft_dw.cuh"
+#include "mft_eps.cuh"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -118,10 +119,11 @@ __global__ void k_flux_euler(int64_t n, double g, const double* __restrict__ u,
 // the flux divergence (6 when t is formed: d rho/dt reuses t).
 template <bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(kBlock) k_fwd_euler_f64(FwdArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
   const double* __restrict__ wxp = a.w[0];
   const double* __restrict__ wyp = a.w[1];
@@ -194,10 +196,11 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_f64(FwdArgs a) {
 // Scalar advection (V = 1), FP64: flux a_d * u evaluated at the neighbour.
 template <bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(kBlock) k_fwd_adv_f64(FwdArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   double f = 0, tx = 0, ty = 0, q = 0;
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
@@ -239,22 +242,6 @@ __device__ void block_sum(double* v) {
       v[k] = x;
     }
   }
-}
-
-__device__ __forceinline__ int jl_isless(double a, double b) {
-  if (isnan(a)) return 0;
-  if (isnan(b)) return 1;
-  if (a < b) return 1;
-  if (a > b) return 0;
-  return signbit(a) && !signbit(b);
-}
-__device__ __forceinline__ double jl_max(double a, double b) {
-  if (isnan(a) || isnan(b)) return a + b;
-  return jl_isless(a, b) ? b : a;
-}
-__device__ __forceinline__ double jl_min(double a, double b) {
-  if (isnan(a) || isnan(b)) return a + b;
-  return jl_isless(b, a) ? b : a;
 }
 
 // Sum of u per variable; the last block to finish reduces the block partials with a
@@ -489,123 +476,11 @@ __global__ void __launch_bounds__(kBlock) k_lexmax_seg(const int64_t* __restrict
 
 // ------------------------------------------------------------------ viscosity
 
-// Julia's max for arguments that are +0 or larger, or NaN (NaN propagates as a + b):
-// without NaN the larger value is the larger IEEE bit pattern, so no FP64 comparison
-// is issued.
-__device__ __forceinline__ double jl_max_nonneg(double a, double b) {
-  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-  const long long inf = 0x7FF0000000000000LL;
-  if ((ia & 0x7FFFFFFFFFFFFFFFLL) > inf || (ib & 0x7FFFFFFFFFFFFFFFLL) > inf) return a + b;
-  return ib > ia ? b : a;
-}
-
-// isnan(x) || isinf(x) on the exponent bits
-__device__ __forceinline__ bool not_finite(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7FF) == 0x7FF;
-}
-
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= a.n) return;
-  const int sg = a.seg_id ? a.seg_id[i] : 0;
-  const double h = a.seg_h ? a.seg_h[sg] : a.h;
-  const double* __restrict__ norms = a.norms + (a.seg_id ? sg * 2 * V : 0);
-  const int si = a.tab ? a.tab[*a.ctr].si_eps : a.success_iter;
-  const bool rv = a.kind == MFT_SRC_RV && si != 0;
-  double eps_rv = 0.0;
-  bool rv_finite = false;
-  if (rv) {
-    // residual / norm with the norms' reciprocals (written by k_lexmax after the norms);
-    // r >= 0 and the reciprocals are positive, so every qv is +0 or larger, or NaN
-    // node records as 16-byte vectors (V = 4)
-    double dpv[V], adv[V];
-    if (V == 4) {
-      const double2* dp2 = reinterpret_cast<const double2*>(a.du_p) + i * 2;
-      const double2* ad2 = reinterpret_cast<const double2*>(a.approx_du) + i * 2;
-      const double2 d0 = dp2[0], d1 = dp2[1], a0 = ad2[0], a1 = ad2[1];
-      dpv[0] = d0.x; dpv[1 % V] = d0.y; dpv[2 % V] = d1.x; dpv[3 % V] = d1.y;
-      adv[0] = a0.x; adv[1 % V] = a0.y; adv[2 % V] = a1.x; adv[3 % V] = a1.y;
-    } else {
-      dpv[0] = a.du_p[i];
-      adv[0] = a.approx_du[i];
-    }
-    double mr = 0.0;
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-      double dp = dpv[v];
-      if (a.hvf) dp = dadd(dp, a.hvf[i * V + v]);
-      const double r = fabs(dsub(adv[v], dp));
-      const double qv = dmul(r, norms[V + v]);
-      mr = v == 0 ? qv : jl_max_nonneg(mr, qv);
-    }
-    const double rvc = a.seg_h ? dmul(dmul(0.5, a.c_rv), dmul(h, h)) : a.rv_coef;
-    eps_rv = dmul(rvc, mr);
-    rv_finite = !not_finite(eps_rv);
-  }
-  double eps;
-  double rho = 0.0, m1 = 0.0, m2 = 0.0, en = 0.0;
-  if (V == 4) {
-    const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
-    const double2 ub = reinterpret_cast<const double2*>(a.u)[i * 2 + 1];
-    rho = ua.x; m1 = ua.y; m2 = ub.x; en = ub.y;
-  }
-  const double uwc = a.seg_h ? dmul(dmul(a.c_uw, 0.5), h) : a.uw_coef;
-  // Decided without forming eps_uw: the computed eps_uw = uwc (speed + c) is at least
-  // uwc |m| / rho (1 - 5 u) (c >= 0, no cancellation in speed; u = 2^-53), so
-  // (eps_rv rho)^2 < uwc^2 (1 - 1e-12) / (1 + 1e-12) |m|^2, evaluated in FP64 with a
-  // normal, finite right side, proves eps_rv < eps_uw and update_visc!'s min is eps_rv.
-  // This skips the division and the two square roots wherever the residual viscosity is
-  // the smaller one (smooth flow).  A NaN energy, or a density so small that 1 / rho
-  // overflows (0 * inf in a velocity), would make eps_uw NaN: no shortcut then.  Every
-  // comparison is on bit patterns of values >= 0 (or NaN, which fails them), so the
-  // test issues only five products and one sum on the FP64 pipe.
-  bool done = false;
-  const double kb = a.seg_h ? dmul(dmul(uwc, uwc), (1.0 - 1e-12) / (1.0 + 1e-12)) : a.uw_bound;
-  const long long bits_rho = __double_as_longlong(rho);
-  const long long bits_en = __double_as_longlong(en) & 0x7FFFFFFFFFFFFFFFLL;
-  if (V == 4 && rv_finite && bits_rho >= 0x01A56E1FC2F8F359LL /* 1e-300 */ &&
-      __double_as_longlong(uwc) > 0 && bits_en <= 0x7FF0000000000000LL) {
-    const double er = dmul(eps_rv, rho);
-    const double lhs = dmul(er, er);
-    const double rhs = dmul(kb, dadd(dmul(m1, m1), dmul(m2, m2)));
-    const long long bl = __double_as_longlong(lhs), br = __double_as_longlong(rhs);
-    if (br >= 0x03B8F2B061AEA072LL /* 1e-290 */ && br <= 0x7FE0000000000000LL /* 2^1023 */ &&
-        bl < br) {
-      eps = eps_rv;
-      done = true;
-    }
-  }
-  if (!done) {
-    double eps_uw;
-    if (V == 4) {
-      // one reciprocal instead of three divisions (FP64 division is a long sequence on
-      // this part); results differ from the divisions by at most an ulp
-      const double rinv = ddiv(1.0, rho);
-      const double v1 = dmul(m1, rinv), v2 = dmul(m2, rinv);
-      const double p =
-          dmul(dsub(a.gamma, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
-      const double speed = sqrt(dadd(dmul(v1, v1), dmul(v2, v2)));
-      double c;
-      if (p < 0.0 || rho < 0.0) c = 0.0;
-      else c = sqrt(dmul(dmul(a.gamma, p), rinv));
-      eps_uw = dmul(uwc, dadd(speed, c));
-    } else if (a.seg_h) {
-      const double an = sqrt(dadd(dmul(a.ax, a.ax), dmul(a.ay, a.ay)));
-      eps_uw = dmul(uwc, an);
-    } else {
-      eps_uw = a.uw_adv;
-    }
-    if (rv) {
-      if (!rv_finite) eps = not_finite(eps_uw) ? 2.220446049250313e-16 : eps_uw;
-      else eps = jl_min(eps_rv, eps_uw);
-    } else if (a.kind == MFT_SRC_RV) {
-      // success_iter == 0: update_visc! takes eps_uw (or eps() when it is not finite)
-      eps = not_finite(eps_uw) ? 2.220446049250313e-16 : eps_uw;
-    } else {
-      eps = eps_uw;
-    }
-  }
+  const double eps = visc::eps_value<V>(a, i, nullptr);
   if (a.eps) a.eps[i] = eps;
   if (a.t) {
     if (V == 4) {
@@ -909,9 +784,7 @@ void launch_lexmax_seg(int nseg, const int64_t* off, int per, int V, const doubl
   MFT_LAUNCH_CHECK();
 }
 
-void launch_eps(const EpsArgs& args, cudaStream_t s) {
-  if (args.n <= 0) return;
-  EpsArgs a = args;
+void prepare_eps(EpsArgs& a) {
   // host IEEE double arithmetic without contraction: the same values the per-node
   // products give
   a.uw_coef = (a.c_uw * 0.5) * a.h;
@@ -923,6 +796,12 @@ void launch_eps(const EpsArgs& args, cudaStream_t s) {
   a.gm1_32 = (float)(a.gamma - 1.0);
   a.uw_coef32 = ((float)a.c_uw * 0.5f) * h32;
   a.rv_coef32 = ((0.5f * (float)a.c_rv) * h32) * h32;
+}
+
+void launch_eps(const EpsArgs& args, cudaStream_t s) {
+  if (args.n <= 0) return;
+  EpsArgs a = args;
+  prepare_eps(a);
   if (a.du_p32) {
     launch_eps_f32(a, s);
     return;

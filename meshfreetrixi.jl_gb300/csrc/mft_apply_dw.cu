@@ -12,6 +12,7 @@
 
 #include "mft_device.cuh"
 #include "mft_dw.cuh"
+#include "mft_eps.cuh"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -25,32 +26,33 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 static __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
 static __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
-// Per node: the Euler flux pair in FP64 (the textbook flux of k_flux_euler, one
-// reciprocal for both velocities) and the state, both stored as double-word pairs:
-// F[i] = (Fx_0..3, Fy_0..3), U[i] = (u_0..3), 8 floats per 4 values.
-__global__ void k_prep_euler_dw(int64_t n, double g, const double* __restrict__ u,
+// Per node: the state as double-word pairs and the Euler flux pair evaluated from them in
+// double-word arithmetic (the textbook flux, one reciprocal for both velocities; each
+// operation is accurate to about 2 u^2 of its operands, u = 2^-24), stored as pairs:
+// F[i] = (Fx_0..3, Fy_0..3), U[i] = (u_0..3), 8 floats per 4 values.  gm1 = gamma - 1 as
+// a pair.  The only FP64 operations are the four splits of the state.
+__global__ void k_prep_euler_dw(int64_t n, float2 gm1, const double* __restrict__ u,
                                 float4* __restrict__ F, float4* __restrict__ U) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double2* ui = reinterpret_cast<const double2*>(u) + i * 2;
   const double2 a = ui[0], b = ui[1];
-  const double rho = a.x, m1 = a.y, m2 = b.x, en = b.y;
-  const double rinv = ddiv(1.0, rho);
-  const double v1 = dmul(m1, rinv), v2 = dmul(m2, rinv);
-  const double p = dmul(dsub(g, 1.0), dsub(en, dmul(0.5, dadd(dmul(m1, v1), dmul(m2, v2)))));
-  const double ep = dadd(en, p);
-  const float2 fx0 = dw::split(m1), fx1 = dw::split(dadd(dmul(m1, v1), p));
-  const float2 fx2 = dw::split(dmul(m1, v2)), fx3 = dw::split(dmul(ep, v1));
-  const float2 fy0 = dw::split(m2), fy1 = dw::split(dmul(m2, v1));
-  const float2 fy2 = dw::split(dadd(dmul(m2, v2), p)), fy3 = dw::split(dmul(ep, v2));
+  const float2 rho = dw::split(a.x), m1 = dw::split(a.y), m2 = dw::split(b.x);
+  const float2 en = dw::split(b.y);
+  const float2 r = dw::recip(rho);
+  const float2 v1 = dw::mul(m1, r), v2 = dw::mul(m2, r);
+  const float2 a1 = dw::mul(m1, v1), a2 = dw::mul(m2, v2);
+  const float2 p = dw::mul(gm1, dw::add(en, dw::neg(dw::scale2(dw::add(a1, a2), 0.5f))));
+  const float2 ep = dw::add(en, p);
+  const float2 fx1 = dw::add(a1, p), fx2 = dw::mul(m1, v2), fx3 = dw::mul(ep, v1);
+  const float2 fy1 = dw::mul(m2, v1), fy2 = dw::add(a2, p), fy3 = dw::mul(ep, v2);
   float4* Fi = F + i * 4;
-  Fi[0] = make_float4(fx0.x, fx0.y, fx1.x, fx1.y);
+  Fi[0] = make_float4(m1.x, m1.y, fx1.x, fx1.y);
   Fi[1] = make_float4(fx2.x, fx2.y, fx3.x, fx3.y);
-  Fi[2] = make_float4(fy0.x, fy0.y, fy1.x, fy1.y);
+  Fi[2] = make_float4(m2.x, m2.y, fy1.x, fy1.y);
   Fi[3] = make_float4(fy2.x, fy2.y, fy3.x, fy3.y);
-  const float2 u0 = dw::split(rho), u1 = fx0, u2 = fy0, u3 = dw::split(en);
-  U[i * 2] = make_float4(u0.x, u0.y, u1.x, u1.y);
-  U[i * 2 + 1] = make_float4(u2.x, u2.y, u3.x, u3.y);
+  U[i * 2] = make_float4(rho.x, rho.y, m1.x, m1.y);
+  U[i * 2 + 1] = make_float4(m2.x, m2.y, en.x, en.y);
 }
 
 // Forward gather (Euler), one node per thread over the sliced ELL: the flux divergence
@@ -59,10 +61,11 @@ __global__ void k_prep_euler_dw(int64_t n, double g, const double* __restrict__ 
 // 32-byte state record (both one or two 256-bit loads), 8-byte weights.
 template <bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(kBlock) k_fwd_euler_dw(FwdArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
   const float2* __restrict__ wxp = a.wdw[0];
   const float2* __restrict__ wyp = a.wdw[1];
@@ -124,6 +127,16 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_dw(FwdArgs a) {
     float2 x[4], y[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) { x[v] = dw::to_pair(tx[v]); y[v] = dw::to_pair(ty[v]); }
+    if (a.fuse_eps) {
+      // the viscosity of this node (FP64, as k_eps forms it from the partial du held
+      // here) and s = eps * t written in place of t; this FP64 work overlaps the FP32
+      // gathers of other warps
+      const double eps = visc::eps_value<4>(a.ea, i, du);
+      if (a.ea.eps) a.ea.eps[i] = eps;
+      const float2 e2 = dw::split(eps);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { x[v] = dw::mul(e2, x[v]); y[v] = dw::mul(e2, y[v]); }
+    }
     t4[0] = make_float4(x[0].x, x[0].y, x[1].x, x[1].y);
     t4[1] = make_float4(x[2].x, x[2].y, x[3].x, x[3].y);
     t4[2] = make_float4(y[0].x, y[0].y, y[1].x, y[1].y);
@@ -215,7 +228,10 @@ __global__ void __launch_bounds__(kBlock) k_rev_euler_dw(RevArgs a) {
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s) {
   if (n <= 0) return;
-  k_prep_euler_dw<<<grid_for(n, 256), 256, 0, s>>>(n, gamma, u, reinterpret_cast<float4*>(F),
+  const double gm1 = gamma - 1.0;
+  const float h = (float)gm1;
+  const float2 gm1dw = make_float2(h, (float)(gm1 - (double)h));
+  k_prep_euler_dw<<<grid_for(n, 256), 256, 0, s>>>(n, gm1dw, u, reinterpret_cast<float4*>(F),
                                                    reinterpret_cast<float4*>(U));
   MFT_LAUNCH_CHECK();
 }

@@ -16,10 +16,11 @@ using namespace dev;
 
 template <bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
   const float* __restrict__ wxp = a.w32[0];
   const float* __restrict__ wyp = a.w32[1];
@@ -63,10 +64,11 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
 
 template <bool WT, bool WQ, int FLY>
 __global__ void __launch_bounds__(kBlock) k_fwd_adv_f32(FwdArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   const float ax = (float)a.ax, ay = (float)a.ay;
   float f = 0, tx = 0, ty = 0, q = 0;
 #pragma unroll 4

@@ -110,8 +110,9 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
   int buf = 0;
   int len_next = row_len_at(a.ell, a.n, first, lane, nslices);
   for (int64_t s = first; s < nslices; s += stride) {
-    const int64_t i = (s << 5) + lane;
-    const bool valid = i < a.n;
+    const int64_t r = (s << 5) + lane;  // layout row
+    const bool valid = r < a.n;
+    const int64_t i = valid ? ell_node(a.ell, r) : 0;
     const int len = len_next;
     len_next = row_len_at(a.ell, a.n, s + stride, lane, nslices);
     if (valid && a.final_epilogue) prefetch_epilogue(a.ep, i);

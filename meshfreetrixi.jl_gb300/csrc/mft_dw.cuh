@@ -80,5 +80,37 @@ static __device__ __forceinline__ float2 mul(float2 a, float2 b) {
   return make_float2(t, __fsub_rn(e, __fsub_rn(t, p)));
 }
 
+// a + b for double-word a and b: TwoSum of the high parts, the low parts added to its
+// error, renormalised (absolute error about 2 u^2 (|a| + |b|)).
+static __device__ __forceinline__ float2 add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  const float t = __fadd_rn(s, e);
+  return make_float2(t, __fsub_rn(e, __fsub_rn(t, s)));
+}
+
+static __device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// a * 2^k for a power of two c = 2^k (exact)
+static __device__ __forceinline__ float2 scale2(float2 a, float c) {
+  return make_float2(__fmul_rn(a.x, c), __fmul_rn(a.y, c));
+}
+
+// 1 / a for a double-word a: the correctly rounded FP32 reciprocal y of a_h and one
+// Newton step y + y (1 - a y) with 1 - a y formed exactly up to the low-order product
+// (relative error about 2 u^2).
+static __device__ __forceinline__ float2 recip(float2 a) {
+  const float y = __frcp_rn(a.x);
+  const float p = __fmul_rn(a.x, y);
+  float ep = fmaf(a.x, y, -p);
+  ep = fmaf(a.y, y, ep);
+  const float d = __fsub_rn(__fsub_rn(1.0f, p), ep);
+  const float c = __fmul_rn(y, d);
+  const float t = __fadd_rn(y, c);
+  return make_float2(t, __fsub_rn(c, __fsub_rn(t, y)));
+}
+
 }  // namespace dw
 }  // namespace mft

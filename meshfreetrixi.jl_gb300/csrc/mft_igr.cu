@@ -79,18 +79,19 @@ __global__ void k_igr_prim(int64_t n, const double* __restrict__ u, double* prim
 
 // b, x = 0, r = b, u_old = 0 and the initial residual norm.
 __global__ void __launch_bounds__(kBlock) k_igr_rhs(IgrArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
   double rr = 0.0;
-  if (i < a.n) {
-    const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-    const int len = a.ell.row_len[i];
+  if (r < a.n) {
+    const int64_t i = ell_node(a.ell, r);
+    const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+    const int len = a.ell.row_len[r];
     double dxr = 0, dxv1 = 0, dxv2 = 0, dyv1 = 0, dyv2 = 0;
     for (int j = 0; j < len; ++j) {
       const int64_t p = base + ((int64_t)j << 5);
       const int64_t c = __ldg(a.ell.col + p);
       const double wx = __ldg(a.wx + p), wy = __ldg(a.wy + p);
-      const double r = a.prim[c * 3], v1 = a.prim[c * 3 + 1], v2 = a.prim[c * 3 + 2];
-      dxr = fma(wx, r, dxr);
+      const double rc = a.prim[c * 3], v1 = a.prim[c * 3 + 1], v2 = a.prim[c * 3 + 2];
+      dxr = fma(wx, rc, dxr);
       dxv1 = fma(wx, v1, dxv1);
       dxv2 = fma(wx, v2, dxv2);
       dyv1 = fma(wy, v1, dyv1);
@@ -127,10 +128,11 @@ __global__ void k_igr_newdir(IgrArgs a, const double* uo, double* un) {
 // t1 = rinv (Dx u_new), t2 = rinv (Dy u_new)
 __global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un) {
   if (a.sc->done) return;
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   double sx = 0.0, sy = 0.0;
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
@@ -146,11 +148,12 @@ __global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un)
 // c = rinv u_new - alpha (Dx t1 + Dy t2); alpha_cg = res^2 / (u_new . c)
 __global__ void __launch_bounds__(kBlock) k_igr_op(IgrArgs a, const double* un) {
   if (a.sc->done) return;
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
   double uc = 0.0;
-  if (i < a.n) {
-    const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-    const int len = a.ell.row_len[i];
+  if (r < a.n) {
+    const int64_t i = ell_node(a.ell, r);
+    const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+    const int len = a.ell.row_len[r];
     double sx = 0.0, sy = 0.0;
     const double2* __restrict__ t2 = reinterpret_cast<const double2*>(a.t);
     for (int j = 0; j < len; ++j) {
@@ -196,10 +199,11 @@ __global__ void __launch_bounds__(kBlock) k_igr_update(IgrArgs a, const double* 
 
 // add = (-(Dx sigma), -(Dy sigma)) for the momentum rows of du
 __global__ void __launch_bounds__(kBlock) k_igr_flux(IgrArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
-  const int64_t base = a.ell.slice_off[i >> 5] + (i & 31);
-  const int len = a.ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
   double sx = 0.0, sy = 0.0;
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);

@@ -86,12 +86,13 @@ struct EllBuf {
   int64_t n = 0, n_elems = 0;
   int max_len = 0;
   int window = 0;  // rows sorted by length inside windows of this many rows (0: none)
+  bool ordered = false;  // rows start from a spatial (Morton) order of the nodes
   DBuf<int64_t> slice_off;
   DBuf<int32_t> row_len;
   DBuf<int32_t> col;
   DBuf<int32_t> perm;
   EllView view() const {
-    return EllView{n, slice_off.p, row_len.p, col.p, window > 0 ? perm.p : nullptr};
+    return EllView{n, slice_off.p, row_len.p, col.p, (window > 0 || ordered) ? perm.p : nullptr};
   }
 };
 
@@ -163,6 +164,42 @@ void launch_bc_pass1(int64_t nb, const int32_t* bnode, int V, int eq, BcDev bc, 
 void launch_flux_f64(int64_t n, int eq, int V, double gamma, const double* u, double* F,
                      cudaStream_t s);
 
+struct EpsArgs {
+  int64_t n;
+  int eq, V, kind;  // kind: MFT_SRC_RV or MFT_SRC_UPWIND
+  double gamma, ax, ay, c_rv, c_uw, h;
+  int success_iter;
+  const struct StepParams* tab;  // graph mode: success_iter = tab[*ctr].si_eps
+  const int* ctr;
+  const int* seg_id;       // ensembles: segment of each node (null: one problem)
+  const double* seg_h;     // ensembles: dx_avg per segment; norms hold 2V per segment
+  // Node-independent factors, formed by launch_eps in the kernel's operation order
+  // (one problem only; with seg_h the kernel forms them per node):
+  double uw_coef;          // (c_uw * 0.5) * h
+  double uw_adv;           // advection: uw_coef * sqrt(ax^2 + ay^2)
+  double rv_coef;          // (0.5 * c_rv) * (h * h)
+  double uw_bound;         // uw_coef^2 (1 - 1e-12) / (1 + 1e-12): the eps_uw bound's factor
+  // FP32 form: the FP32 shadow of u and the FP32 factors, formed by launch_eps in the
+  // FP32 kernel's operation order
+  const float* u32;
+  float gamma32, gm1_32;   // (float) gamma, (float)(gamma - 1)
+  float uw_coef32;         // ((float) c_uw * 0.5f) * (float) h
+  float rv_coef32;         // ((0.5f * (float) c_rv) * (float) h) * (float) h
+  const double* u;
+  const double* du_p;
+  const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)
+  const double* hvf;       // added to du_p when the Flyer term precedes RV (else null)
+  const double* approx_du; // n x V
+  const double* norms;     // V
+  double* t;               // n x 2V, scaled in place to eps*t
+  double* eps;             // n (diagnostic copy)
+  float* t32;              // FP32 path: scaled in place
+  float2* tdw;             // double-word FP64 form: n x 2V pairs, scaled in place
+};
+// Node-independent factors of EpsArgs (uw_coef, uw_adv, rv_coef, uw_bound and the FP32
+// ones), formed on the host in the kernels' operation order.
+void prepare_eps(EpsArgs& a);
+
 struct FwdArgs {
   int64_t n;
   EllView ell;
@@ -197,6 +234,10 @@ struct FwdArgs {
   const float2* udw;    // n x V pairs
   float2* tdw;          // n x 2V pairs
   float2* qdw;          // n x V pairs
+  // double-word form with a viscosity source: the viscosity is formed in the epilogue
+  // (ea, whose norms must be ready at launch) and t is written as s = eps * t
+  int fuse_eps;
+  EpsArgs ea;
 };
 void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 // Double-word forms (mft_apply_dw.cu): per-node flux and state pairs, forward gather,
@@ -213,38 +254,6 @@ void launch_lexmax(int64_t n, int V, const double* u, const double* mean, int ma
                    double* partial, unsigned* counter, double* norms, int nblocks,
                    cudaStream_t s);
 
-struct EpsArgs {
-  int64_t n;
-  int eq, V, kind;  // kind: MFT_SRC_RV or MFT_SRC_UPWIND
-  double gamma, ax, ay, c_rv, c_uw, h;
-  int success_iter;
-  const struct StepParams* tab;  // graph mode: success_iter = tab[*ctr].si_eps
-  const int* ctr;
-  const int* seg_id;       // ensembles: segment of each node (null: one problem)
-  const double* seg_h;     // ensembles: dx_avg per segment; norms hold 2V per segment
-  // Node-independent factors, formed by launch_eps in the kernel's operation order
-  // (one problem only; with seg_h the kernel forms them per node):
-  double uw_coef;          // (c_uw * 0.5) * h
-  double uw_adv;           // advection: uw_coef * sqrt(ax^2 + ay^2)
-  double rv_coef;          // (0.5 * c_rv) * (h * h)
-  double uw_bound;         // uw_coef^2 (1 - 1e-12) / (1 + 1e-12): the eps_uw bound's factor
-  // FP32 form: the FP32 shadow of u and the FP32 factors, formed by launch_eps in the
-  // FP32 kernel's operation order
-  const float* u32;
-  float gamma32, gm1_32;   // (float) gamma, (float)(gamma - 1)
-  float uw_coef32;         // ((float) c_uw * 0.5f) * (float) h
-  float rv_coef32;         // ((0.5f * (float) c_rv) * (float) h) * (float) h
-  const double* u;
-  const double* du_p;
-  const float* du_p32;     // FP32 apply: partial du in FP32 (du_p is then null)
-  const double* hvf;       // added to du_p when the Flyer term precedes RV (else null)
-  const double* approx_du; // n x V
-  const double* norms;     // V
-  double* t;               // n x 2V, scaled in place to eps*t
-  double* eps;             // n (diagnostic copy)
-  float* t32;              // FP32 path: scaled in place
-  float2* tdw;             // double-word FP64 form: n x 2V pairs, scaled in place
-};
 void launch_eps(const EpsArgs& a, cudaStream_t s);
 void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double* u, int mode,
                      double* partial, unsigned* counter, double* mean, cudaStream_t s);

@@ -29,10 +29,11 @@ static __device__ __forceinline__ double zs_variable(int variable, double g, con
 __global__ void __launch_bounds__(kBlock) k_zs_limit(int64_t n, EllView ell, const double* u,
                                                     int variable, double threshold, double g,
                                                     double* loc) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= n) return;
-  const int64_t base = ell.slice_off[i >> 5] + (i & 31);
-  const int len = ell.row_len[i];
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= n) return;
+  const int64_t i = ell_node(ell, r);
+  const int64_t base = ell.slice_off[r >> 5] + (r & 31);
+  const int len = ell.row_len[r];
   double vmin = INFINITY;
   for (int j = 0; j < len; ++j) {
     const int64_t c = __ldg(ell.col + base + ((int64_t)j << 5));
