@@ -58,9 +58,12 @@ enum { MFT_SRC_RV = 0, MFT_SRC_UPWIND = 1, MFT_SRC_HV_TOMINEC = 2, MFT_SRC_HV_FL
  * MFT_OP_HV holds a ready hyperviscosity operator sum_d D_d^(2k) (Flyer HV). */
 enum { MFT_OP_GRAD = 0, MFT_OP_LAP = 1, MFT_OP_HV = 2 };
 
-/* Arithmetic of the operator apply.  FP64: FP64 weights, states and sums.
- * FP32: weights generated in FP64 and stored FP32, FP32 states and sums in the
- * apply; the SSP-RK stage combination stays FP64 with compensated sums. */
+/* Arithmetic of the operator apply.  FP64: FP64 weights and states, sums accurate to
+ * FP64 (double-word FP32 or FP64 fused multiply-adds, see MFT_OPT_FP64_ARITH).
+ * FP32: weights generated in FP64 and stored FP32, FP32 states and sums in the apply;
+ * the state stays FP64 and the SSP-RK stage combination is evaluated in FP64 (the FP64
+ * state carries the low-order part that a compensated FP32 state would keep, so no
+ * separate compensation term is formed). */
 enum { MFT_PREC_FP64 = 0, MFT_PREC_FP32 = 1 };
 
 /* ---------------------------------------------------------------- context */
@@ -213,7 +216,13 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
  * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
-       MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4 };
+       MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5 };
+/* MFT_OPT_DW_VARIANT: kernel variant of the double-word gathers -- 0 one stencil entry
+ * per loop iteration, 1 two entries per iteration with registers capped at six blocks per
+ * SM, 2 two entries uncapped, 3 software-pipelined (indices two entries ahead, weights and
+ * neighbour records one ahead);
+ * -1 (default) lets the autotuner time them at the first launch of each configuration.
+ * MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV then report the variant in use. */
 /* MFT_OPT_LAYOUT_ORDER: 1 (default) assigns the operator rows to threads along a Morton
  * curve of the node coordinates, so that a warp's 32 rows are a compact patch whose
  * neighbours overlap; 0 keeps node order.  Results are identical either way (every row
@@ -228,9 +237,9 @@ enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2 };
 enum { MFT_ARITH_AUTO = 0, MFT_ARITH_DFMA = 1, MFT_ARITH_DW = 2 };
 mft_status mft_set_option(mft_ctx* ctx, int option, int value);
 /* Reads an option; MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV return the mapping the
- * autotuner chose for the most recent forward / transpose gather configuration
- * (0 = one node per thread, 4 or 8 = staged with that many slots per bulk copy,
- * -1 = not tuned yet). */
+ * autotuner chose for the most recent forward / transpose gather launch: FP32 form
+ * 0 = one node per thread, 4 or 8 = staged with that many slots per bulk copy; FP64
+ * form with double-word gathers: the kernel variant 0..3; -1 = not tuned yet. */
 mft_status mft_get_option(mft_ctx* ctx, int option, int* value);
 
 /* Self-test of the bounded-wait error path (no fault involved): one warp waits on a

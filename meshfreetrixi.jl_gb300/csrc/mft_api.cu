@@ -404,6 +404,8 @@ void ensure_device_ops(mft_ctx* c) {
   c->dev_dirty = false;
   for (int &k : c->tuned_fwd) k = -1;
   for (int &k : c->tuned_rev) k = -1;
+  for (int &k : c->tuned_fwd_dw) k = -1;
+  for (int &k : c->tuned_rev_dw) k = -1;
 }
 
 static void ensure_bcs(mft_ctx* c) {
@@ -469,14 +471,17 @@ static void refresh_dirichlet(mft_ctx* c, double t) {
 
 static const int kGatherChoices[3] = {0, 4, 8};
 
+// Times launch(choice) for every choice (a warm-up launch, then the best of 3 CUDA-event
+// timed launches) and returns the fastest choice.
 template <class Launch>
-static int tune_gather(mft_ctx* c, Launch&& launch) {
+static int tune_choices(mft_ctx* c, const int* choices, int nchoice, Launch&& launch) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   MFT_CUDA(cudaEventCreate(&e0));
   MFT_CUDA(cudaEventCreate(&e1));
-  int best = 0;
+  int best = choices[0];
   float best_ms = 1e30f;
-  for (int choice : kGatherChoices) {
+  for (int q = 0; q < nchoice; ++q) {
+    const int choice = choices[q];
     launch(choice);
     float t = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
@@ -496,6 +501,18 @@ static int tune_gather(mft_ctx* c, Launch&& launch) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return best;
+}
+
+template <class Launch>
+static int tune_gather(mft_ctx* c, Launch&& launch) {
+  return tune_choices(c, kGatherChoices, 3, launch);
+}
+
+template <class Launch>
+static int tune_variants(mft_ctx* c, int nvariants, Launch&& launch) {
+  int choices[8];
+  for (int k = 0; k < nvariants && k < 8; ++k) choices[k] = k;
+  return tune_choices(c, choices, nvariants, launch);
 }
 
 static int fwd_choice(mft_ctx* c, const FwdArgs& a) {
@@ -531,6 +548,39 @@ static int rev_choice(mft_ctx* c, const RevArgs& a) {
   return c->tuned_rev[key];
 }
 
+// The double-word gathers have four kernel variants (plain or software-pipelined loop,
+// with or without a register cap); with MFT_OPT_DW_VARIANT < 0 (default) the first
+// launch of each configuration outside a graph capture times them on the live inputs and
+// keeps the fastest until the operators change.
+static int dw_fwd_choice(mft_ctx* c, const FwdArgs& a) {
+  if (c->dw_variant >= 0) return c->dw_variant;
+  const int key = (a.want_t ? 1 : 0) + (a.want_q ? 2 : 0) + 4 * a.flyer;
+  if (c->tuned_fwd_dw[key] < 0) {
+    if (c->capturing) return 0;
+    FwdArgs probe = a;
+    probe.final_epilogue = 0;  // timing launches write only scratch outputs
+    c->tuned_fwd_dw[key] = tune_variants(c, kDwVariants, [&](int v) {
+      launch_fwd_dw(probe, v, c->stream);
+    });
+  }
+  return c->tuned_fwd_dw[key];
+}
+
+static int dw_rev_choice(mft_ctx* c, const RevArgs& a) {
+  if (c->dw_variant >= 0) return c->dw_variant;
+  const int key = (a.rv ? 1 : 0) + (a.lap ? 2 : 0);
+  if (c->tuned_rev_dw[key] < 0) {
+    if (c->capturing) return 0;
+    RevArgs probe = a;
+    probe.final_epilogue = 0;
+    probe.du_p_out = c->du_p2.p == a.du_p ? c->work_du.p : c->du_p2.p;
+    c->tuned_rev_dw[key] = tune_variants(c, kDwVariants, [&](int v) {
+      launch_rev_dw(probe, v, c->stream);
+    });
+  }
+  return c->tuned_rev_dw[key];
+}
+
 void launch_fwd(mft_ctx* c, const FwdArgs& a) {
   if (c->precision == MFT_PREC_FP32) {
     const int ch = fwd_choice(c, a);
@@ -538,7 +588,9 @@ void launch_fwd(mft_ctx* c, const FwdArgs& a) {
     if (ch > 0 && launch_fwd_f32_tma(a, ch, c->kerr.p, c->stream)) return;
     launch_fwd_f32(a, c->stream);
   } else if (use_dw(c)) {
-    launch_fwd_dw(a, c->stream);
+    const int v = dw_fwd_choice(c, a);
+    c->last_fwd_choice = v;
+    launch_fwd_dw(a, v, c->stream);
   } else {
     launch_fwd_f64(a, c->stream);
   }
@@ -550,7 +602,9 @@ void launch_rev(mft_ctx* c, const RevArgs& a) {
     if (ch > 0 && launch_rev_f32_tma(a, ch, c->kerr.p, c->stream)) return;
     launch_rev_f32(a, c->stream);
   } else if (use_dw(c)) {
-    launch_rev_dw(a, c->stream);
+    const int v = dw_rev_choice(c, a);
+    c->last_rev_choice = v;
+    launch_rev_dw(a, v, c->stream);
   } else {
     launch_rev_f64(a, c->stream);
   }
@@ -1315,6 +1369,11 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
       c->fsal_valid = false;
       for (int& k : c->tuned_fwd) k = -1;
       for (int& k : c->tuned_rev) k = -1;
+    } else if (option == MFT_OPT_DW_VARIANT) {
+      MFT_REQUIRE(value >= -1 && value < kDwVariants, MFT_ERR_ARG,
+                  "double-word gather variant: -1 (tuned) or 0..3");
+      c->dw_variant = value;
+      c->fsal_valid = false;
     } else if (option == MFT_OPT_LAYOUT_ORDER) {
       MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG, "layout order: 0 node order, 1 Morton");
       c->layout_order = value;
@@ -1351,6 +1410,7 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_TUNED_REV) *value = c->last_rev_choice;
     else if (option == MFT_OPT_FP64_ARITH) *value = c->fp64_arith;
     else if (option == MFT_OPT_LAYOUT_ORDER) *value = c->layout_order;
+    else if (option == MFT_OPT_DW_VARIANT) *value = c->dw_variant;
     else throw mft::Error(MFT_ERR_ARG, "unknown option");
   });
 }

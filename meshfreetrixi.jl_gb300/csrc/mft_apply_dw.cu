@@ -55,21 +55,71 @@ __global__ void k_prep_euler_dw(int64_t n, float2 gm1, const double* __restrict_
   U[i * 2 + 1] = make_float4(m2.x, m2.y, en.x, en.y);
 }
 
+// One stencil entry of the forward gather: weights and the neighbour's flux and state
+// records, requested together.
+struct FwdEntry {
+  float2 wx, wy, wl;
+  F8 fa, fb, uu;
+};
+
+template <bool WT, bool WQ, int FLY>
+static __device__ __forceinline__ FwdEntry fwd_load(const FwdArgs& a, const float* F,
+                                                    const float* U, int64_t p, int64_t c) {
+  FwdEntry e;
+  e.wx = __ldg(a.wdw[0] + p);
+  e.wy = __ldg(a.wdw[1] + p);
+  e.fa = ldg_f8(F + c * 16);
+  e.fb = ldg_f8(F + c * 16 + 8);
+  if (WT || WQ || FLY) e.uu = ldg_f8(U + c * 8);
+  if (WQ || FLY) e.wl = __ldg(a.wldw + p);
+  return e;
+}
+
+template <bool WT, bool WQ, int FLY>
+static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, dw::Acc* tx,
+                                                 dw::Acc* ty, dw::Acc* q) {
+  const float2 Fx[4] = {lo2(e.fa.lo), hi2(e.fa.lo), lo2(e.fa.hi), hi2(e.fa.hi)};
+  const float2 Fy[4] = {lo2(e.fb.lo), hi2(e.fb.lo), lo2(e.fb.hi), hi2(e.fb.hi)};
+#pragma unroll
+  for (int v = WT ? 1 : 0; v < 4; ++v) {
+    // Fx[0] = m1, Fy[0] = m2: with t formed, the rho row is tx1 + ty2
+    dw::fma_acc(f[v], e.wx, Fx[v]);
+    dw::fma_acc(f[v], e.wy, Fy[v]);
+  }
+  if (WT || WQ || FLY) {
+    const float2 uc[4] = {lo2(e.uu.lo), hi2(e.uu.lo), lo2(e.uu.hi), hi2(e.uu.hi)};
+    if (WT) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        dw::fma_acc(tx[v], e.wx, uc[v]);
+        dw::fma_acc(ty[v], e.wy, uc[v]);
+      }
+    }
+    if (WQ || FLY) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) dw::fma_acc(q[v], e.wl, uc[v]);
+    }
+  }
+}
+
 // Forward gather (Euler), one node per thread over the sliced ELL: the flux divergence
 // -sum_j (Dx F_x + Dy F_y), t = (Dx u, Dy u) (WT), q = lap u (WQ) or the Flyer term
 // H u (FLY), as in k_fwd_euler_f64.  Per stencil entry: a 64-byte flux record and a
 // 32-byte state record (both one or two 256-bit loads), 8-byte weights.
-template <bool WT, bool WQ, int FLY>
-__global__ void __launch_bounds__(kBlock) k_fwd_euler_dw(FwdArgs a) {
+// PIPE = 0: one entry per loop iteration; PIPE = 2: two (the compiler overlaps their
+// loads); PIPE = 1: software pipeline -- the column index is loaded two entries ahead and
+// the weights and records one entry ahead, so that the gathers of entry j + 1 are in flight while entry j is
+// accumulated (the gathers are latency-bound: most samples stall on their results).
+// MINB: minimum resident blocks per SM requested from the compiler (register cap).
+// The variants form the same sums in the same order; the autotuner picks one.
+template <bool WT, bool WQ, int FLY, int PIPE, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
-  const float2* __restrict__ wxp = a.wdw[0];
-  const float2* __restrict__ wyp = a.wdw[1];
-  const float2* __restrict__ wlp = a.wldw;
   const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
   const float* __restrict__ U = reinterpret_cast<const float*>(a.udw);
   dw::Acc f[4], tx[4], ty[4], q[4];
@@ -77,35 +127,31 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_dw(FwdArgs a) {
   for (int v = 0; v < 4; ++v) {
     f[v] = dw::zero(); tx[v] = dw::zero(); ty[v] = dw::zero(); q[v] = dw::zero();
   }
-#pragma unroll 2
-  for (int j = 0; j < len; ++j) {
-    const int64_t p = base + ((int64_t)j << 5);
-    const int64_t c = __ldg(col + p);
-    const float2 wx = __ldg(wxp + p), wy = __ldg(wyp + p);
-    const F8 fa = ldg_f8(F + c * 16), fb = ldg_f8(F + c * 16 + 8);
-    const float2 Fx[4] = {lo2(fa.lo), hi2(fa.lo), lo2(fa.hi), hi2(fa.hi)};
-    const float2 Fy[4] = {lo2(fb.lo), hi2(fb.lo), lo2(fb.hi), hi2(fb.hi)};
-#pragma unroll
-    for (int v = WT ? 1 : 0; v < 4; ++v) {
-      // Fx[0] = m1, Fy[0] = m2: with t formed, the rho row is tx1 + ty2
-      dw::fma_acc(f[v], wx, Fx[v]);
-      dw::fma_acc(f[v], wy, Fy[v]);
+  if (PIPE == 0) {
+#pragma unroll 1
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(col + p);
+      fwd_accum<WT, WQ, FLY>(fwd_load<WT, WQ, FLY>(a, F, U, p, c), f, tx, ty, q);
     }
-    if (WT || WQ || FLY) {
-      const F8 uu = ldg_f8(U + c * 8);
-      const float2 uc[4] = {lo2(uu.lo), hi2(uu.lo), lo2(uu.hi), hi2(uu.hi)};
-      if (WT) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          dw::fma_acc(tx[v], wx, uc[v]);
-          dw::fma_acc(ty[v], wy, uc[v]);
-        }
-      }
-      if (WQ || FLY) {
-        const float2 wl = __ldg(wlp + p);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) dw::fma_acc(q[v], wl, uc[v]);
-      }
+  } else if (PIPE == 2) {
+#pragma unroll 2
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(col + p);
+      fwd_accum<WT, WQ, FLY>(fwd_load<WT, WQ, FLY>(a, F, U, p, c), f, tx, ty, q);
+    }
+  } else if (len > 0) {
+    int64_t c_next = len > 1 ? (int64_t)__ldg(col + base + 32) : 0;
+    FwdEntry cur = fwd_load<WT, WQ, FLY>(a, F, U, base, __ldg(col + base));
+    for (int j = 0; j < len; ++j) {
+      const int64_t p1 = base + ((int64_t)(j + 1) << 5);
+      const int64_t c2 = j + 2 < len ? (int64_t)__ldg(col + p1 + 32) : 0;
+      FwdEntry nxt;
+      if (j + 1 < len) nxt = fwd_load<WT, WQ, FLY>(a, F, U, p1, c_next);
+      fwd_accum<WT, WQ, FLY>(cur, f, tx, ty, q);
+      cur = nxt;
+      c_next = c2;
     }
   }
   double du[4];
@@ -164,11 +210,53 @@ __global__ void __launch_bounds__(kBlock) k_fwd_euler_dw(FwdArgs a) {
   }
 }
 
+// One entry of the transpose gather: weights and the neighbour's s = eps t and q records.
+struct RevEntry {
+  float2 wx, wy, wl;
+  F8 xa, ya, qq;
+};
+
+template <bool RV, bool LAP>
+static __device__ __forceinline__ RevEntry rev_load(const RevArgs& a, const float* S,
+                                                    const float* Q, int64_t p, int64_t c) {
+  RevEntry e;
+  if (RV) {
+    e.wx = __ldg(a.wdw[0] + p);
+    e.wy = __ldg(a.wdw[1] + p);
+    e.xa = ldg_f8(S + c * 16);
+    e.ya = ldg_f8(S + c * 16 + 8);
+  }
+  if (LAP) {
+    e.wl = __ldg(a.wldw + p);
+    e.qq = ldg_f8(Q + c * 8);
+  }
+  return e;
+}
+
+template <bool RV, bool LAP>
+static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx, dw::Acc* sy,
+                                                 dw::Acc* sl) {
+  if (RV) {
+    const float2 X[4] = {lo2(e.xa.lo), hi2(e.xa.lo), lo2(e.xa.hi), hi2(e.xa.hi)};
+    const float2 Y[4] = {lo2(e.ya.lo), hi2(e.ya.lo), lo2(e.ya.hi), hi2(e.ya.hi)};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      dw::fma_acc(sx[v], e.wx, X[v]);
+      dw::fma_acc(sy[v], e.wy, Y[v]);
+    }
+  }
+  if (LAP) {
+    const float2 Z[4] = {lo2(e.qq.lo), hi2(e.qq.lo), lo2(e.qq.hi), hi2(e.qq.hi)};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) dw::fma_acc(sl[v], e.wl, Z[v]);
+  }
+}
+
 // Transpose gather (Euler) over the reverse adjacency, as k_rev_f64:
 // du_i = du_p_i - sum_j (Dx[j,i] s_x[j] + Dy[j,i] s_y[j]) - gamma sum_j lap[j,i] q[j],
-// with s = eps * t and q as double-word pairs.
-template <bool RV, bool LAP>
-__global__ void __launch_bounds__(kBlock) k_rev_euler_dw(RevArgs a) {
+// with s = eps * t and q as double-word pairs.  PIPE and MINB as for k_fwd_euler_dw.
+template <bool RV, bool LAP, int PIPE, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) k_rev_euler_dw(RevArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
@@ -176,30 +264,35 @@ __global__ void __launch_bounds__(kBlock) k_rev_euler_dw(RevArgs a) {
   const int len = a.ell.row_len[r];
   const float* __restrict__ S = reinterpret_cast<const float*>(a.sdw);
   const float* __restrict__ Q = reinterpret_cast<const float*>(a.qdw);
+  const int32_t* __restrict__ col = a.ell.col;
   dw::Acc sx[4], sy[4], sl[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) { sx[v] = dw::zero(); sy[v] = dw::zero(); sl[v] = dw::zero(); }
-#pragma unroll 2
-  for (int j = 0; j < len; ++j) {
-    const int64_t p = base + ((int64_t)j << 5);
-    const int64_t c = __ldg(a.ell.col + p);
-    if (RV) {
-      const float2 wx = __ldg(a.wdw[0] + p), wy = __ldg(a.wdw[1] + p);
-      const F8 xa = ldg_f8(S + c * 16), ya = ldg_f8(S + c * 16 + 8);
-      const float2 X[4] = {lo2(xa.lo), hi2(xa.lo), lo2(xa.hi), hi2(xa.hi)};
-      const float2 Y[4] = {lo2(ya.lo), hi2(ya.lo), lo2(ya.hi), hi2(ya.hi)};
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        dw::fma_acc(sx[v], wx, X[v]);
-        dw::fma_acc(sy[v], wy, Y[v]);
-      }
+  if (PIPE == 0) {
+#pragma unroll 1
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(col + p);
+      rev_accum<RV, LAP>(rev_load<RV, LAP>(a, S, Q, p, c), sx, sy, sl);
     }
-    if (LAP) {
-      const float2 wl = __ldg(a.wldw + p);
-      const F8 qq = ldg_f8(Q + c * 8);
-      const float2 Z[4] = {lo2(qq.lo), hi2(qq.lo), lo2(qq.hi), hi2(qq.hi)};
-#pragma unroll
-      for (int v = 0; v < 4; ++v) dw::fma_acc(sl[v], wl, Z[v]);
+  } else if (PIPE == 2) {
+#pragma unroll 2
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(col + p);
+      rev_accum<RV, LAP>(rev_load<RV, LAP>(a, S, Q, p, c), sx, sy, sl);
+    }
+  } else if (len > 0) {
+    int64_t c_next = len > 1 ? (int64_t)__ldg(col + base + 32) : 0;
+    RevEntry cur = rev_load<RV, LAP>(a, S, Q, base, __ldg(col + base));
+    for (int j = 0; j < len; ++j) {
+      const int64_t p1 = base + ((int64_t)(j + 1) << 5);
+      const int64_t c2 = j + 2 < len ? (int64_t)__ldg(col + p1 + 32) : 0;
+      RevEntry nxt;
+      if (j + 1 < len) nxt = rev_load<RV, LAP>(a, S, Q, p1, c_next);
+      rev_accum<RV, LAP>(cur, sx, sy, sl);
+      cur = nxt;
+      c_next = c2;
     }
   }
   double du[4];
@@ -236,7 +329,34 @@ void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, f
   MFT_LAUNCH_CHECK();
 }
 
-void launch_fwd_dw(const FwdArgs& a, cudaStream_t s) {
+namespace {
+
+// Kernel variants: 0 = one entry per loop iteration (fewest registers, most resident
+// warps), 1 = two entries per iteration with the register count capped at six blocks per
+// SM, 2 = two entries per iteration uncapped, 3 = software pipeline.
+template <bool WT, bool WQ, int FLY>
+void fwd_variant(const FwdArgs& a, int variant, unsigned g, cudaStream_t s) {
+  switch (variant) {
+    case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6><<<g, kBlock, 0, s>>>(a); break;
+    case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1><<<g, kBlock, 0, s>>>(a); break;
+    case 3: k_fwd_euler_dw<WT, WQ, FLY, 1, 1><<<g, kBlock, 0, s>>>(a); break;
+    default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1><<<g, kBlock, 0, s>>>(a); break;
+  }
+}
+
+template <bool RV, bool LAP>
+void rev_variant(const RevArgs& a, int variant, unsigned g, cudaStream_t s) {
+  switch (variant) {
+    case 1: k_rev_euler_dw<RV, LAP, 2, 6><<<g, kBlock, 0, s>>>(a); break;
+    case 2: k_rev_euler_dw<RV, LAP, 2, 1><<<g, kBlock, 0, s>>>(a); break;
+    case 3: k_rev_euler_dw<RV, LAP, 1, 1><<<g, kBlock, 0, s>>>(a); break;
+    default: k_rev_euler_dw<RV, LAP, 0, 1><<<g, kBlock, 0, s>>>(a); break;
+  }
+}
+
+}  // namespace
+
+void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s) {
   if (a.n <= 0) return;
   MFT_REQUIRE(a.V == 4, MFT_ERR_UNSUPPORTED, "double-word gathers: 2D Euler only");
   MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
@@ -244,28 +364,28 @@ void launch_fwd_dw(const FwdArgs& a, cudaStream_t s) {
   const unsigned g = grid_for(a.n, kBlock);
   const bool wt = a.want_t != 0, wq = a.want_q != 0;
   if (a.flyer == 0) {
-    if (wt && wq) k_fwd_euler_dw<true, true, 0><<<g, kBlock, 0, s>>>(a);
-    else if (wt) k_fwd_euler_dw<true, false, 0><<<g, kBlock, 0, s>>>(a);
-    else if (wq) k_fwd_euler_dw<false, true, 0><<<g, kBlock, 0, s>>>(a);
-    else k_fwd_euler_dw<false, false, 0><<<g, kBlock, 0, s>>>(a);
+    if (wt && wq) fwd_variant<true, true, 0>(a, variant, g, s);
+    else if (wt) fwd_variant<true, false, 0>(a, variant, g, s);
+    else if (wq) fwd_variant<false, true, 0>(a, variant, g, s);
+    else fwd_variant<false, false, 0>(a, variant, g, s);
   } else if (a.flyer == 1) {
-    if (wt) k_fwd_euler_dw<true, false, 1><<<g, kBlock, 0, s>>>(a);
-    else k_fwd_euler_dw<false, false, 1><<<g, kBlock, 0, s>>>(a);
+    if (wt) fwd_variant<true, false, 1>(a, variant, g, s);
+    else fwd_variant<false, false, 1>(a, variant, g, s);
   } else {
-    if (wt) k_fwd_euler_dw<true, false, 2><<<g, kBlock, 0, s>>>(a);
-    else k_fwd_euler_dw<false, false, 2><<<g, kBlock, 0, s>>>(a);
+    if (wt) fwd_variant<true, false, 2>(a, variant, g, s);
+    else fwd_variant<false, false, 2>(a, variant, g, s);
   }
   MFT_LAUNCH_CHECK();
 }
 
-void launch_rev_dw(const RevArgs& a, cudaStream_t s) {
+void launch_rev_dw(const RevArgs& a, int variant, cudaStream_t s) {
   if (a.n <= 0) return;
   MFT_REQUIRE(a.V == 4, MFT_ERR_UNSUPPORTED, "double-word gathers: 2D Euler only");
   const unsigned g = grid_for(a.n, kBlock);
-  if (a.rv && a.lap) k_rev_euler_dw<true, true><<<g, kBlock, 0, s>>>(a);
-  else if (a.rv) k_rev_euler_dw<true, false><<<g, kBlock, 0, s>>>(a);
-  else if (a.lap) k_rev_euler_dw<false, true><<<g, kBlock, 0, s>>>(a);
-  else k_rev_euler_dw<false, false><<<g, kBlock, 0, s>>>(a);
+  if (a.rv && a.lap) rev_variant<true, true>(a, variant, g, s);
+  else if (a.rv) rev_variant<true, false>(a, variant, g, s);
+  else if (a.lap) rev_variant<false, true>(a, variant, g, s);
+  else rev_variant<false, false>(a, variant, g, s);
   MFT_LAUNCH_CHECK();
 }
 

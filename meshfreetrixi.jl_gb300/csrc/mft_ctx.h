@@ -87,6 +87,9 @@ struct mft_ctx {
   int tuned_fwd[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   int tuned_rev[4] = {-1, -1, -1, -1};
   int last_fwd_choice = -1, last_rev_choice = -1;
+  int tuned_fwd_dw[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  int tuned_rev_dw[4] = {-1, -1, -1, -1};
+  int dw_variant = -1;   // double-word gather variant: -1 autotuned, else forced
 
   // work buffers (AoS n x V unless noted)
   mft::DBuf<double> U[4];  // u_n, stage 1, stage 2, stage 3

@@ -244,7 +244,9 @@ void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 // transpose gather.
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s);
-void launch_fwd_dw(const FwdArgs& a, cudaStream_t s);
+// variant: 0..3, the kernel variants the autotuner chooses among (same sums, same order)
+constexpr int kDwVariants = 4;
+void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s);
 void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 
 // Reductions for the residual viscosity normalisation (last-block-done pattern).
@@ -291,7 +293,7 @@ struct RevArgs {
   const float2* qdw;     // n x V pairs
 };
 void launch_rev_f64(const RevArgs& a, cudaStream_t s);
-void launch_rev_dw(const RevArgs& a, cudaStream_t s);
+void launch_rev_dw(const RevArgs& a, int variant, cudaStream_t s);
 void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 // Bulk-copy-staged FP32 gathers (Euler); return false when the case is not covered.
 // chunk: slots staged per bulk copy (4 or 8).

@@ -127,11 +127,73 @@ def _bc_pass_complex(semi, dirichlet, du, u):
             u[2, ii] = s2
 
 
+JL_EPS = 2.220446049250313e-16
+
+
+def _cabs(z):
+    """|x| continued to complex arguments as sign(Re z) z: the derivative of |x| away
+    from x = 0 (its branch frozen by the real part)."""
+    return np.where(z.real < 0, -z, z)
+
+
+def _visc_complex(semi, kind, du, u):
+    """The viscosity source (update_upwind_visc!, update_residual_visc!, update_visc!
+    and its application, hyperviscosity.jl:246-409; the oracle's visc_source) on complex
+    states, every selection (the min in update_visc!, the maximum over variables, the
+    lexicographic ode_maximum, |.|) decided by the real parts as the real evaluation
+    decides it.  du holds the partial du the source reads; the source is added to it."""
+    from oracle.oracle import SRC_RV
+    s = semi.s
+    n, V = semi.n, semi.nvars
+    h = s.h
+    if V == 4:
+        rho, m1, m2, en = u
+        v1, v2 = m1 / rho, m2 / rho
+        p = (s.gamma - 1.0) * (en - 0.5 * (m1 * v1 + m2 * v2))
+        speed = np.sqrt(v1 * v1 + v2 * v2)
+        bad = (p.real < 0.0) | (rho.real < 0.0)
+        c = np.where(bad, 0.0, np.sqrt(np.where(bad, 1.0, s.gamma * p / rho)))
+        eps_uw = s.c_uw * 0.5 * h * (speed + c)
+    else:
+        a2 = sum(s.adv[d] * s.adv[d] for d in range(semi.dim))
+        eps_uw = np.full(n, s.c_uw * 0.5 * h * np.sqrt(a2), dtype=np.complex128)
+    eps = eps_uw
+    if kind == SRC_RV and s.success_iter != 0:
+        denom = float(n * V) if s.mean_mode == 0 else float(n)
+        mean = np.array([u[v].sum() / denom for v in range(V)])
+        loc = _cabs(u - mean[:, None])
+        if s.max_mode == 0:
+            keys = loc.real.T
+            best = 0
+            for i in range(1, n):           # max(a, b) = isless(b, a) ? a : b; ties: later
+                if not tuple(keys[i]) < tuple(keys[best]):
+                    best = i
+            nrm = loc[:, best].copy()
+        else:
+            nrm = np.array([loc[v, np.flatnonzero(loc[v].real == loc[v].real.max())[-1]]
+                            for v in range(V)])
+        nrm = np.where(nrm.real == 0.0, JL_EPS, nrm)
+        ad = semi.approx_du.reshape(V, n)
+        q = _cabs(ad - du) / nrm[:, None]
+        mr = q[0].copy()
+        for v in range(1, V):               # jl_max: ties take the later argument
+            mr = np.where(q[v].real >= mr.real, q[v], mr)
+        eps_rv = 0.5 * s.c_rv * (h * h) * mr
+        take_uw = eps_uw.real < eps_rv.real
+        eps = np.where(take_uw, eps_uw, eps_rv)
+    for j, op in enumerate(semi.ops):
+        A = op.to_scipy()
+        for v in range(V):
+            du[v] -= A.T @ (eps * (A @ u[v]))
+    return du
+
+
 def rhs_complex(semi, u, t=0.0, return_state=False):
-    """rhs!(u, t) of an oracle Semi without viscosity or IGR sources, for real or
-    complex u (nvars, n); u is not mutated.  With return_state, also the state as the
-    BC pass leaves it (rhs! mutates u at boundary nodes)."""
-    from oracle.oracle import SRC_HV_FLYER, SRC_HV_TOMINEC
+    """rhs!(u, t) of an oracle Semi without the IGR source, for real or complex u
+    (nvars, n); u is not mutated.  With return_state, also the state as the BC pass
+    leaves it (rhs! mutates u at boundary nodes).  Viscosity sources freeze their
+    selections at the real parts (derivatives away from selection ties)."""
+    from oracle.oracle import SRC_HV_FLYER, SRC_HV_TOMINEC, SRC_RV, SRC_UPWIND
     u = np.array(u, dtype=np.complex128)
     du = np.zeros_like(u)
     dv = semi.dirichlet_values(t)
@@ -146,7 +208,10 @@ def rhs_complex(semi, u, t=0.0, return_state=False):
             du[v] -= A @ f[v]
     srcs = [int(k) for k in semi.src[:semi.s.n_src]]
     for k in srcs:
-        assert k in (SRC_HV_TOMINEC, SRC_HV_FLYER), "viscosity / IGR sources: no derivative"
+        if k in (SRC_RV, SRC_UPWIND):
+            du = _visc_complex(semi, k, du, u)
+            continue
+        assert k in (SRC_HV_TOMINEC, SRC_HV_FLYER), "IGR source: no derivative"
         H = semi.hv.to_scipy()
         for v in range(semi.nvars):
             du[v] -= semi.s.hv_gamma * (H @ u[v])
