@@ -318,9 +318,14 @@ mft_status mft_limit(mft_ctx* ctx, double* const* u, int nvars);
  * the reference corresponds: MeshfreeTrixi.jl differentiates rhs! only through
  * ForwardDiff.jl duals; these entry points are what a ChainRulesCore rrule for
  * rhs! and for solve() would call.  Covered: 2D Euler and linear advection, the
- * strong BCs (Dirichlet, slip wall, do-nothing), the hyperviscosity sources, FP64.
- * A residual-viscosity or upwind-viscosity source gives MFT_ERR_UNSUPPORTED (its
- * viscosity is a maximum over the field). */
+ * strong BCs (Dirichlet, slip wall, do-nothing), the hyperviscosity sources, the
+ * residual-viscosity and upwind-viscosity sources (differentiated with their selections
+ * -- min(eps_rv, eps_uw), the maximum over variables, the row of ode_maximum, |.| --
+ * frozen as the forward evaluation takes them: the derivative away from ties; approx_du
+ * and success_iter are inputs, as mft_set_rv_state leaves them), FP64.  A viscosity
+ * source after a hyperviscosity source, or in an ensemble, gives MFT_ERR_UNSUPPORTED.
+ * The recorded trajectory does not run the HistoryCallback: its residual viscosity uses
+ * the approx_du and success_iter in place when recording starts. */
 
 /* out = (d rhs!(u, t) / du)^T lam with host StructArray-style arrays (nvars pointers
  * of length n).  u is not mutated. */

@@ -8,6 +8,7 @@
 // operator stored as a sliced ELL), fused with the flux-Jacobian-transpose product
 // at the gathering node and with the SSP-RK3 adjoint stage combination.
 #include "mft_device.cuh"
+#include "mft_dw.cuh"
 
 namespace mft {
 namespace {
@@ -53,6 +54,64 @@ static __device__ __forceinline__ void project_row(const BcDev& bc, int64_t i, d
   }
 }
 
+// The node part of the adjoint at node i from the gathered sums gx = Dx^T M2 lam,
+// gy = Dy^T M2 lam and gh (the hyperviscosity term): flux-Jacobian-transpose product,
+// the SSP-RK3 adjoint stage combination and the BC projection.
+template <int V, bool EULER, bool BC, int HV>
+static __device__ __forceinline__ void adj_finish(const AdjArgs& a, int64_t i, const double* gx,
+                                                  const double* gy, const double* gh) {
+  double r[V];
+  if constexpr (EULER) {
+    double uu[4];
+    load_row<4>(a.u, i, uu);
+    if (BC && a.bc.tag[i] == 2) slip(a.bc.normal + 2 * (int64_t)a.bc.slot[i], uu);
+    double ub[4];
+    euler_flux_vjp(a.gamma, uu, gx, gy, ub);
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = -ub[v];
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = -(a.ax * gx[v] + a.ay * gy[v]);
+  }
+  if (a.xadd) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = r[v] + a.xadd[i * V + v];
+  }
+  if constexpr (HV != 0) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) r[v] = fma(-a.hv_gamma, gh[v], r[v]);
+  }
+  double o[V];
+  if (a.kind == kAdjPlain) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) o[v] = r[v];
+  } else {
+    double li[V];
+    load_row<V>(a.lam, i, li);
+    if (a.kind == kAdjStage3) {
+      const double c3 = 2.0 / 3.0, cr = 2.0 * a.dt / 3.0;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        o[v] = c3 * li[v] + cr * r[v];
+        a.acc[i * V + v] = div3(li[v]);
+      }
+    } else if (a.kind == kAdjStage2) {
+      const double cr = 0.25 * a.dt;
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        o[v] = 0.25 * li[v] + cr * r[v];
+        a.acc[i * V + v] = a.acc[i * V + v] + 0.75 * li[v];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) o[v] = (a.acc[i * V + v] + li[v]) + a.dt * r[v];
+    }
+  }
+  if (BC) project_row<V>(a.bc, i, o);
+#pragma unroll
+  for (int v = 0; v < V; ++v) a.out[i * V + v] = o[v];
+}
+
 template <int V, bool EULER, bool BC, int HV>
 __global__ void __launch_bounds__(kBlock) k_adj_f64(AdjArgs a) {
   const int64_t row = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
@@ -88,52 +147,66 @@ __global__ void __launch_bounds__(kBlock) k_adj_f64(AdjArgs a) {
       for (int v = 0; v < V; ++v) gh[v] = fma(wh, qq[v], gh[v]);
     }
   }
-  double r[V];
-  if constexpr (EULER) {
-    double uu[4];
-    load_row<4>(a.u, i, uu);
-    if (BC && a.bc.tag[i] == 2) slip(a.bc.normal + 2 * (int64_t)a.bc.slot[i], uu);
-    double ub[4];
-    euler_flux_vjp(a.gamma, uu, gx, gy, ub);
+  adj_finish<V, EULER, BC, HV>(a, i, gx, gy, gh);
+}
+
+// M2 lam as double-word pairs (n x 4 pairs): the cotangent the double-word adjoint
+// gather reads, masked once per node instead of once per stencil entry.
+template <bool BC>
+__global__ void k_lam_pairs(int64_t n, const double* __restrict__ lam, BcDev bc,
+                            float4* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double l[4];
+  load_row<4>(lam, i, l);
+  if (BC) mask_rows<4>(bc, i, l);
+  const float2 a = dw::split(l[0]), b = dw::split(l[1]), c = dw::split(l[2]),
+               d = dw::split(l[3]);
+  out[i * 2] = make_float4(a.x, a.y, b.x, b.y);
+  out[i * 2 + 1] = make_float4(c.x, c.y, d.x, d.y);
+}
+
+// The adjoint gather of 2D Euler in double-word FP32 arithmetic (as the forward form's
+// gathers; the sums over the reverse adjacency in pairs, the node part in FP64).  HV 0
+// (no hyperviscosity) or 2 (Flyer, whose term gathers the same M2 lam).
+template <bool BC, int HV>
+__global__ void __launch_bounds__(kBlock) k_adj_dw(AdjArgs a) {
+  const int64_t row = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (row >= a.n) return;
+  const int64_t i = ell_node(a.ell, row);
+  const int64_t base = a.ell.slice_off[row >> 5] + (row & 31);
+  const int len = a.ell.row_len[row];
+  const float* __restrict__ L = reinterpret_cast<const float*>(a.lamdw);
+  dw::Acc gx[4], gy[4], gh[4];
 #pragma unroll
-    for (int v = 0; v < V; ++v) r[v] = -ub[v];
-  } else {
+  for (int v = 0; v < 4; ++v) { gx[v] = dw::zero(); gy[v] = dw::zero(); gh[v] = dw::zero(); }
+#pragma unroll 2
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(a.ell.col + p);
+    const float2 wx = __ldg(a.wdw[0] + p), wy = __ldg(a.wdw[1] + p);
+    const F8 ll = ldg_f8(L + c * 8);
+    const float2 l[4] = {make_float2(ll.lo.x, ll.lo.y), make_float2(ll.lo.z, ll.lo.w),
+                         make_float2(ll.hi.x, ll.hi.y), make_float2(ll.hi.z, ll.hi.w)};
 #pragma unroll
-    for (int v = 0; v < V; ++v) r[v] = -(a.ax * gx[v] + a.ay * gy[v]);
-  }
-  if constexpr (HV != 0) {
+    for (int v = 0; v < 4; ++v) {
+      dw::fma_acc(gx[v], wx, l[v]);
+      dw::fma_acc(gy[v], wy, l[v]);
+    }
+    if constexpr (HV == 2) {
+      const float2 wh = __ldg(a.whdw + p);
 #pragma unroll
-    for (int v = 0; v < V; ++v) r[v] = fma(-a.hv_gamma, gh[v], r[v]);
-  }
-  double o[V];
-  if (a.kind == kAdjPlain) {
-#pragma unroll
-    for (int v = 0; v < V; ++v) o[v] = r[v];
-  } else {
-    double li[V];
-    load_row<V>(a.lam, i, li);
-    if (a.kind == kAdjStage3) {
-      const double c3 = 2.0 / 3.0, cr = 2.0 * a.dt / 3.0;
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        o[v] = c3 * li[v] + cr * r[v];
-        a.acc[i * V + v] = div3(li[v]);
-      }
-    } else if (a.kind == kAdjStage2) {
-      const double cr = 0.25 * a.dt;
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        o[v] = 0.25 * li[v] + cr * r[v];
-        a.acc[i * V + v] = a.acc[i * V + v] + 0.75 * li[v];
-      }
-    } else {
-#pragma unroll
-      for (int v = 0; v < V; ++v) o[v] = (a.acc[i * V + v] + li[v]) + a.dt * r[v];
+      for (int v = 0; v < 4; ++v) dw::fma_acc(gh[v], wh, l[v]);
     }
   }
-  if (BC) project_row<V>(a.bc, i, o);
+  double gxd[4], gyd[4], ghd[4];
 #pragma unroll
-  for (int v = 0; v < V; ++v) a.out[i * V + v] = o[v];
+  for (int v = 0; v < 4; ++v) {
+    gxd[v] = dw::to_double(gx[v]);
+    gyd[v] = dw::to_double(gy[v]);
+    ghd[v] = HV ? dw::to_double(gh[v]) : 0.0;
+  }
+  adj_finish<4, true, BC, HV>(a, i, gxd, gyd, ghd);
 }
 
 // q_i = sum_j lap[i,j] (M2 lam)_j over the forward sliced ELL.
@@ -195,6 +268,27 @@ void launch_adj_f64(const AdjArgs& a, cudaStream_t s) {
   } else {
     if (a.has_bc) adj_hv<1, false, true>(a, s);
     else adj_hv<1, false, false>(a, s);
+  }
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, cudaStream_t s) {
+  if (a.n <= 0) return;
+  MFT_REQUIRE(a.V == 4 && a.eq == MFT_EQ_EULER2D && a.hv != 1, MFT_ERR_UNSUPPORTED,
+              "double-word adjoint gather: 2D Euler without Tominec hyperviscosity");
+  const unsigned gn = grid_for(a.n, 256);
+  if (a.has_bc) k_lam_pairs<true><<<gn, 256, 0, s>>>(a.n, a.lam, a.bc, reinterpret_cast<float4*>(lam_pairs));
+  else k_lam_pairs<false><<<gn, 256, 0, s>>>(a.n, a.lam, a.bc, reinterpret_cast<float4*>(lam_pairs));
+  MFT_LAUNCH_CHECK();
+  AdjArgs b = a;
+  b.lamdw = lam_pairs;
+  const unsigned g = grid_for(a.n, kBlock);
+  if (a.has_bc) {
+    if (a.hv == 2) k_adj_dw<true, 2><<<g, kBlock, 0, s>>>(b);
+    else k_adj_dw<true, 0><<<g, kBlock, 0, s>>>(b);
+  } else {
+    if (a.hv == 2) k_adj_dw<false, 2><<<g, kBlock, 0, s>>>(b);
+    else k_adj_dw<false, 0><<<g, kBlock, 0, s>>>(b);
   }
   MFT_LAUNCH_CHECK();
 }

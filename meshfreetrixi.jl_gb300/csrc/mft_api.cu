@@ -1981,20 +1981,34 @@ namespace {
 
 // Hyperviscosity mode of the adjoint (0 none, 1 Tominec, 2 Flyer) and its gamma;
 // viscosity sources have no adjoint.
-int adj_hv_mode(mft_ctx* c, double* gamma) {
+// The hyperviscosity mode of the adjoint (0 none, 1 Tominec, 2 Flyer) and whether a
+// residual/upwind viscosity source is present (its selections are differentiated frozen,
+// see mft_adjoint_visc.cu).  A viscosity source must come before any hyperviscosity
+// source (its partial du is then the flux divergence alone) and needs one problem (no
+// ensemble segments).
+int adj_hv_mode(mft_ctx* c, double* gamma, bool* visc = nullptr) {
   int mode = 0;
+  bool has_visc = false;
   *gamma = 0.0;
   for (size_t k = 0; k < c->src_kind.size(); ++k) {
     const int kind = c->src_kind[k];
-    MFT_REQUIRE(kind != MFT_SRC_RV && kind != MFT_SRC_UPWIND, MFT_ERR_UNSUPPORTED,
-                "adjoint: residual/upwind viscosity has no adjoint (its viscosity is a "
-                "maximum over the field)");
     MFT_REQUIRE(kind != MFT_SRC_IGR, MFT_ERR_UNSUPPORTED,
                 "adjoint: the IGR source (an iterative solve) has no adjoint");
+    if (kind == MFT_SRC_RV || kind == MFT_SRC_UPWIND) {
+      MFT_REQUIRE(!has_visc, MFT_ERR_UNSUPPORTED, "more than one viscosity source");
+      MFT_REQUIRE(mode == 0, MFT_ERR_UNSUPPORTED,
+                  "adjoint: a viscosity source after a hyperviscosity source (the residual "
+                  "would include the hyperviscosity term) is not provided");
+      MFT_REQUIRE(c->nseg == 0, MFT_ERR_UNSUPPORTED,
+                  "adjoint: viscosity sources of ensembles are not provided");
+      has_visc = true;
+      continue;
+    }
     MFT_REQUIRE(mode == 0, MFT_ERR_UNSUPPORTED, "more than one hyperviscosity source");
     mode = kind == MFT_SRC_HV_TOMINEC ? 1 : 2;
     *gamma = c->src_par[k * 4];
   }
+  if (visc) *visc = has_visc;
   return mode;
 }
 
@@ -2015,13 +2029,33 @@ void ensure_adj_work(mft_ctx* c) {
   c->adj_q.alloc(nv);
 }
 
-// out = stage combination `kind` of (d rhs!/du)^T lam at state u (n x V AoS, device).
+// out = stage combination `kind` of (d rhs!/du)^T lam at state u (n x V AoS, device) and
+// time t (the Dirichlet values of the BC pass, which the viscosity source sees).
 void eval_rhs_adjoint(mft_ctx* c, const double* u, const double* lam, int kind, double dt,
-                      double* acc, double* out) {
+                      double* acc, double* out, double t) {
   ensure_device_ops(c);
   ensure_bcs(c);
   double hv_gamma = 0.0;
-  const int hv = adj_hv_mode(c, &hv_gamma);
+  bool visc = false;
+  const int hv = adj_hv_mode(c, &hv_gamma, &visc);
+  const double* xadd = nullptr;
+  if (visc) {
+    // a forward evaluation at u gives the viscosity, its partial du and norms and the
+    // BC-corrected state; then the viscosity source's transpose product
+    const size_t nv = (size_t)c->n * c->nvars;
+    c->adj_ubc.alloc(nv);
+    c->adj_du.alloc(nv);
+    c->adj_xadd.alloc(nv);
+    MFT_CUDA(cudaMemcpyAsync(c->adj_ubc.p, u, nv * sizeof(double), cudaMemcpyDeviceToDevice,
+                             c->stream));
+    Epilogue ef{};
+    ef.kind = kOutDu;
+    ef.out = c->adj_du.p;
+    eval_rhs(c, c->adj_ubc.p, nullptr, t, ef);
+    ProfScope ps(c, MFT_K_ADJ);
+    visc_adjoint_terms(c, c->adj_ubc.p, lam, c->adj_xadd.p);
+    xadd = c->adj_xadd.p;
+  }
   if (hv == 1) MFT_REQUIRE(c->have_val[kSlotLap], MFT_ERR_STATE, "Tominec HV needs MFT_OP_LAP");
   if (hv == 2) MFT_REQUIRE(c->have_val[kSlotHv], MFT_ERR_STATE, "Flyer HV needs MFT_OP_HV");
   MFT_REQUIRE(out != lam, MFT_ERR_ARG, "adjoint output aliases its input");
@@ -2055,8 +2089,18 @@ void eval_rhs_adjoint(mft_ctx* c, const double* u, const double* lam, int kind, 
   a.dt = dt;
   a.acc = acc;
   a.out = out;
+  a.xadd = xadd;
   ProfScope ps(c, MFT_K_ADJ);
-  launch_adj_f64(a, s);
+  if (use_dw(c) && hv != 1) {
+    ensure_device_ops(c);
+    a.wdw[0] = c->rwdw[0].p;
+    a.wdw[1] = c->rwdw[1].p;
+    a.whdw = hv == 2 ? c->rwdw[kSlotHv].p : nullptr;
+    c->adj_lamdw.alloc((size_t)c->n * 4);
+    launch_adj_dw(a, c->adj_lamdw.p, s);
+  } else {
+    launch_adj_f64(a, s);
+  }
 }
 
 // Time of the first stage of step k as the FSAL integrator evaluates it.
@@ -2139,16 +2183,18 @@ void ssprk33_adjoint_sweep(mft_ctx* c, double* L) {
   double* A = c->adj_lam[1].p;
   double* B = c->adj_lam[2].p;
   double* acc = c->adj_acc.p;
-  auto back = [&](const double* x, const double* s1, const double* s2) {
-    eval_rhs_adjoint(c, s2, L, kAdjStage3, dt, acc, A);
-    eval_rhs_adjoint(c, s1, A, kAdjStage2, dt, acc, B);
-    eval_rhs_adjoint(c, x, B, kAdjStage1, dt, acc, L);
+  const double t0 = c->adj_t0;
+  auto back = [&](int k, const double* x, const double* s1, const double* s2) {
+    const double t = t0 + k * dt;
+    eval_rhs_adjoint(c, s2, L, kAdjStage3, dt, acc, A, t + 0.5 * dt);
+    eval_rhs_adjoint(c, s1, A, kAdjStage2, dt, acc, B, t + dt);
+    eval_rhs_adjoint(c, x, B, kAdjStage1, dt, acc, L, stage1_time(t0, dt, k));
   };
   double* st = c->adj_store.p;
   if (E == 0) {
     for (int k = N - 1; k >= 0; --k) {
       const double* x = st + (size_t)3 * k * nv;
-      back(x, x + nv, x + 2 * nv);
+      back(k, x, x + nv, x + 2 * nv);
     }
     return;
   }
@@ -2163,7 +2209,7 @@ void ssprk33_adjoint_sweep(mft_ctx* c, double* L) {
     }
     for (int k = b - 1; k >= a; --k) {
       const double* x = st + (size_t)3 * (k - a) * nv;
-      back(x, x + nv, x + 2 * nv);
+      back(k, x, x + nv, x + 2 * nv);
     }
   }
 }
@@ -2189,7 +2235,6 @@ void ssprk33_adjoint_soa(mft_ctx* c, double* lam_soa) {
 
 mft_status mft_rhs_adjoint(mft_ctx* c, double* const* out, const double* const* lam,
                            const double* const* u, int nvars, double t) {
-  (void)t;
   return guarded(c, [&] {
     check_adjoint_ready(c);
     MFT_REQUIRE(out && lam && u && nvars == c->nvars, MFT_ERR_ARG, "bad arrays or nvars");
@@ -2207,7 +2252,8 @@ mft_status mft_rhs_adjoint(mft_ctx* c, double* const* out, const double* const* 
     }
     launch_aos_from_soa(c->soa.p, c->work_u.p, n, V, s);
     launch_aos_from_soa(c->soa2.p, c->adj_lam[0].p, n, V, s);
-    eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p);
+    eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p,
+                     t);
     launch_soa_from_aos(c->adj_lam[1].p, c->soa.p, n, V, s);
     for (int v = 0; v < V; ++v)
       MFT_CUDA(cudaMemcpyAsync(out[v], c->soa.p + (size_t)v * n, n * sizeof(double),
@@ -2218,7 +2264,6 @@ mft_status mft_rhs_adjoint(mft_ctx* c, double* const* out, const double* const* 
 
 mft_status mft_rhs_adjoint_device(mft_ctx* c, double* out, const double* lam, const double* u,
                                   double t) {
-  (void)t;
   return guarded(c, [&] {
     check_adjoint_ready(c);
     MFT_REQUIRE(out && lam && u, MFT_ERR_ARG, "NULL device array");
@@ -2230,7 +2275,8 @@ mft_status mft_rhs_adjoint_device(mft_ctx* c, double* out, const double* lam, co
     cudaStream_t s = c->stream;
     launch_aos_from_soa(u, c->work_u.p, n, V, s);
     launch_aos_from_soa(lam, c->adj_lam[0].p, n, V, s);
-    eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p);
+    eval_rhs_adjoint(c, c->work_u.p, c->adj_lam[0].p, kAdjPlain, 0.0, nullptr, c->adj_lam[1].p,
+                     t);
     launch_soa_from_aos(c->adj_lam[1].p, out, n, V, s);
     check_kernel_errors(c);
   });

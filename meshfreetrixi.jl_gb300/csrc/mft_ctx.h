@@ -139,6 +139,11 @@ struct mft_ctx {
 
   // adjoint: recorded trajectory (checkpoints, or every stage state) and cotangents
   mft::DBuf<double> adj_lam[3], adj_acc, adj_q, adj_store, adj_ckpt;
+  mft::DBuf<float2> adj_lamdw;  // M2 lam as double-word pairs (double-word adjoint gather)
+  // viscosity-source adjoint: forward state and du, the added transpose product, the
+  // norm cotangents and the ode_maximum rows
+  mft::DBuf<double> adj_ubc, adj_du, adj_xadd, adj_nbar;
+  mft::DBuf<int> adj_jstar;
   bool adj_valid = false;
   double adj_t0 = 0.0, adj_dt = 0.0;
   int adj_nsteps = 0, adj_every = 0;
@@ -203,4 +208,6 @@ void knn_device(mft_ctx* c, int k, std::vector<int32_t>& idx, std::vector<double
 void weights_device(mft_ctx* c, int rbf_pow, int polydeg, int deriv_order,
                     std::vector<double>& w_out, double* max_resid);
 void weights_batch(mft_ctx* c, int ngroups, const mft_weight_group* groups, double* max_resid);
+// The viscosity source's part of the adjoint of rhs! (mft_adjoint_visc.cu).
+void visc_adjoint_terms(mft_ctx* c, const double* u_bc, const double* lam, double* out);
 }  // namespace mft

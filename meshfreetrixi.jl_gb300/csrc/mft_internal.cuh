@@ -327,8 +327,16 @@ struct AdjArgs {
   double dt;
   double* acc;         // n x V stage accumulator (stage kinds)
   double* out;         // n x V
+  const double* xadd;  // n x V added to the transpose product before the stage
+                       // combination (the viscosity source's part), or null
+  // double-word gathers (2D Euler, FP64 form): weights on the reverse layout as pairs
+  const float2* wdw[2];
+  const float2* whdw;
+  const float2* lamdw;  // M2 lam as pairs (set by launch_adj_dw)
 };
 void launch_adj_f64(const AdjArgs& a, cudaStream_t s);
+// The same product with the sums in double-word arithmetic; lam_pairs: n x 4 pair scratch.
+void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, cudaStream_t s);
 // q_i = sum_j lap[i,j] (M2 lam)_j over the forward layout (Tominec adjoint).
 void launch_lap_masked(int64_t n, EllView fwd, const double* wl, const double* lam, int V,
                        BcDev bc, int has_bc, double* q, cudaStream_t s);

@@ -141,3 +141,25 @@ def test_trajectory_adjoint_matches_forward_mode(oracle, cyl, cyl_ops, case):
     lhs = float(np.sum(lamT * trajectory_jvp_complex(semi, u0, v, dt, nsteps)))
     rhs = float(np.sum(lam0 * v))
     assert abs(lhs - rhs) / abs(rhs) < TOL, (lhs, rhs)
+
+
+@pytest.mark.parametrize("src,si", [("upwind", 0), ("rv", 0), ("rv", 3)])
+def test_restatement_with_viscosity_equals_oracle_rhs(oracle, cyl, cyl_ops, src, si):
+    """The complex-step restatement with a viscosity source (every selection taken on
+    the real parts) has the oracle's rhs! as its real part."""
+    pts = cyl["positions"]
+    kind = oracle.SRC_RV if src == "rv" else oracle.SRC_UPWIND
+    bcs = cyl_bcs(cyl, lambda x, t: ic_gradient(x, t).T)
+    semi = oracle.Semi(pts, cyl_ops["ops"], eq="euler", gamma=GAMMA, bcs=bcs, sources=(kind,),
+                       c_rv=1.0, c_uw=1.0, h=float(cyl["dx"][1]))
+    u = ic_bumpy(pts)
+    if si:
+        plain = oracle.Semi(pts, cyl_ops["ops"], eq="euler", gamma=GAMMA, bcs=bcs)
+        du = plain.rhs(u.copy(), 0.0)
+        semi.approx_du[:] = (du * (1 + 0.05 * np.random.default_rng(5).standard_normal(
+            du.shape))).ravel()
+        semi.s.success_iter = si
+    ref = semi.rhs(u.copy(), 0.0)
+    got = rhs_complex(semi, u)
+    assert np.abs(got.imag).max() == 0.0
+    assert np.abs(got.real - ref).max() <= 1e-13 * np.abs(ref).max()
