@@ -584,6 +584,7 @@ def run_adjoint(args, local, peaks):
             "adjoint_sweep_over_forward": ms_adj / ms_fwd,
             "store_all_stages": {"record_ms": ms_rec0, "adjoint_sweep_ms": ms_adj0,
                                  "adjoint_sweep_over_forward": ms_adj0 / ms_fwd,
+                                 "gradient_over_forward": (ms_rec0 + ms_adj0) / ms_fwd,
                                  "stored_bytes": 3 * nsteps * 4 * n * 8,
                                  "max_abs_diff_vs_checkpointed": float(np.abs(grad0 - grad).max())},
             "fd_check": {"directional_fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(ad),

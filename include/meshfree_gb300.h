@@ -220,7 +220,8 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
 /* MFT_OPT_DW_VARIANT: kernel variant of the double-word gathers -- 0 one stencil entry
  * per loop iteration, 1 two entries per iteration with registers capped at six blocks per
  * SM, 2 two entries uncapped, 3 software-pipelined (indices two entries ahead, weights and
- * neighbour records one ahead);
+ * neighbour records one ahead), 4 and 5 = 1 and 2 with each warp's streamed index and
+ * weight arrays prefetched into L2 eight slots ahead (one bulk prefetch per array);
  * -1 (default) lets the autotuner time them at the first launch of each configuration.
  * MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV then report the variant in use. */
 /* MFT_OPT_LAYOUT_ORDER: 1 (default) assigns the operator rows to threads along a Morton
@@ -239,7 +240,7 @@ mft_status mft_set_option(mft_ctx* ctx, int option, int value);
 /* Reads an option; MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV return the mapping the
  * autotuner chose for the most recent forward / transpose gather launch: FP32 form
  * 0 = one node per thread, 4 or 8 = staged with that many slots per bulk copy; FP64
- * form with double-word gathers: the kernel variant 0..3; -1 = not tuned yet. */
+ * form with double-word gathers: the kernel variant 0..5; -1 = not tuned yet. */
 mft_status mft_get_option(mft_ctx* ctx, int option, int* value);
 
 /* Self-test of the bounded-wait error path (no fault involved): one warp waits on a

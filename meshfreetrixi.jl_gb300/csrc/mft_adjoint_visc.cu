@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <cmath>
+
 #include "mft_ctx.h"
 #include "mft_device.cuh"
 
@@ -45,7 +47,7 @@ struct ViscAdj {
   BcDev bc;
   int has_bc;
   int V, kind, si, mean_mode, max_mode, euler;
-  double gamma, uwc, K;
+  double gamma, uwc, K, uw_adv;
   double* ebar;         // n
   double* sl;           // n x 2V: eps o D_d l
   double* xadd;         // n x V
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(kBlock) k_visc_adj_node(ViscAdj a) {
     const double c = (p < 0.0 || rho < 0.0) ? 0.0 : sqrt(a.gamma * p / rho);
     eps_uw = a.uwc * (sqrt(v1 * v1 + v2 * v2) + c);
   } else {
-    eps_uw = 1.0;  // constant (advection): no derivative, finite
+    eps_uw = a.uw_adv;  // advection: uwc |a|, independent of the state
   }
   const bool uw_finite = isfinite(eps_uw);
   int branch = uw_finite ? 1 : 0;  // 0 none, 1 upwind, 2 residual
@@ -270,6 +272,7 @@ void visc_adjoint_terms(mft_ctx* c, const double* u_bc, const double* lam, doubl
   a.gamma = c->gamma;
   a.uwc = (c_uw * 0.5) * h;
   a.K = (0.5 * c_rv) * (h * h);
+  a.uw_adv = a.uwc * std::sqrt(c->adv[0] * c->adv[0] + c->adv[1] * c->adv[1]);
   // scratch: ebar in hvf (n), eps o D l in t (n x 2V), xadd in work_du, mu in q,
   // nbar per node in du_p2; the argmax row in d_ctr's neighbour word
   a.ebar = c->hvf.p;

@@ -1371,7 +1371,7 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
       for (int& k : c->tuned_rev) k = -1;
     } else if (option == MFT_OPT_DW_VARIANT) {
       MFT_REQUIRE(value >= -1 && value < kDwVariants, MFT_ERR_ARG,
-                  "double-word gather variant: -1 (tuned) or 0..3");
+                  "double-word gather variant: -1 (tuned) or 0..5");
       c->dw_variant = value;
       c->fsal_valid = false;
     } else if (option == MFT_OPT_LAYOUT_ORDER) {

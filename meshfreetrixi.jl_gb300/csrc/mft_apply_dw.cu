@@ -14,6 +14,7 @@
 #include "mft_dw.cuh"
 #include "mft_eps.cuh"
 #include "mft_internal.cuh"
+#include "mft_tma.cuh"
 
 namespace mft {
 
@@ -24,6 +25,28 @@ using namespace dev;
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 static __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+
+// The streamed arrays of a warp's slice (column indices and up to three weight arrays,
+// read once per launch) requested into L2 a chunk of kPfSlots slots at a time by one
+// lane, ahead of the slots the warp gathers (the weights otherwise arrive from DRAM on
+// each slot's critical path).  The range stays inside the slice.
+constexpr int kPfSlots = 8;
+struct SliceArrays {
+  const void* arr[4];
+  int esize[4];
+  int narr;
+};
+static __device__ __forceinline__ void prefetch_chunk(const SliceArrays& sa, int64_t s_lo,
+                                                      int64_t s_hi, int chunk) {
+  const int64_t e0 = s_lo + (int64_t)chunk * kPfSlots * 32;
+  if (e0 >= s_hi) return;
+  const int64_t ne = min((int64_t)kPfSlots * 32, s_hi - e0);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (k < sa.narr)
+      tma::bulk_prefetch_l2(static_cast<const char*>(sa.arr[k]) + e0 * sa.esize[k],
+                            (uint32_t)(ne * sa.esize[k]));
+}
 static __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
 // Per node: the state as double-word pairs and the Euler flux pair evaluated from them in
@@ -112,7 +135,7 @@ static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, 
 // accumulated (the gathers are latency-bound: most samples stall on their results).
 // MINB: minimum resident blocks per SM requested from the compiler (register cap).
 // The variants form the same sums in the same order; the autotuner picks one.
-template <bool WT, bool WQ, int FLY, int PIPE, int MINB>
+template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF>
 __global__ void __launch_bounds__(kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
   if (r >= a.n) return;
@@ -135,8 +158,23 @@ __global__ void __launch_bounds__(kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
       fwd_accum<WT, WQ, FLY>(fwd_load<WT, WQ, FLY>(a, F, U, p, c), f, tx, ty, q);
     }
   } else if (PIPE == 2) {
+    SliceArrays sa{};
+    int64_t s_lo = 0, s_hi = 0;
+    const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
+    if (pf_lane) {
+      sa.arr[0] = col; sa.esize[0] = 4;
+      sa.arr[1] = a.wdw[0]; sa.esize[1] = 8;
+      sa.arr[2] = a.wdw[1]; sa.esize[2] = 8;
+      sa.arr[3] = a.wldw; sa.esize[3] = 8;
+      sa.narr = (WQ || FLY) ? 4 : 3;
+      s_lo = a.ell.slice_off[r >> 5];
+      s_hi = a.ell.slice_off[(r >> 5) + 1];
+      prefetch_chunk(sa, s_lo, s_hi, 0);
+      prefetch_chunk(sa, s_lo, s_hi, 1);
+    }
 #pragma unroll 2
     for (int j = 0; j < len; ++j) {
+      if (pf_lane && (j % kPfSlots) == 0) prefetch_chunk(sa, s_lo, s_hi, j / kPfSlots + 2);
       const int64_t p = base + ((int64_t)j << 5);
       const int64_t c = __ldg(col + p);
       fwd_accum<WT, WQ, FLY>(fwd_load<WT, WQ, FLY>(a, F, U, p, c), f, tx, ty, q);
@@ -255,7 +293,7 @@ static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx,
 // Transpose gather (Euler) over the reverse adjacency, as k_rev_f64:
 // du_i = du_p_i - sum_j (Dx[j,i] s_x[j] + Dy[j,i] s_y[j]) - gamma sum_j lap[j,i] q[j],
 // with s = eps * t and q as double-word pairs.  PIPE and MINB as for k_fwd_euler_dw.
-template <bool RV, bool LAP, int PIPE, int MINB>
+template <bool RV, bool LAP, int PIPE, int MINB, bool PREF>
 __global__ void __launch_bounds__(kBlock, MINB) k_rev_euler_dw(RevArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (r >= a.n) return;
@@ -276,8 +314,23 @@ __global__ void __launch_bounds__(kBlock, MINB) k_rev_euler_dw(RevArgs a) {
       rev_accum<RV, LAP>(rev_load<RV, LAP>(a, S, Q, p, c), sx, sy, sl);
     }
   } else if (PIPE == 2) {
+    SliceArrays sa{};
+    int64_t s_lo = 0, s_hi = 0;
+    const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
+    if (pf_lane) {
+      int k = 0;
+      sa.arr[k] = col; sa.esize[k++] = 4;
+      if (RV) { sa.arr[k] = a.wdw[0]; sa.esize[k++] = 8; sa.arr[k] = a.wdw[1]; sa.esize[k++] = 8; }
+      if (LAP) { sa.arr[k] = a.wldw; sa.esize[k++] = 8; }
+      sa.narr = k;
+      s_lo = a.ell.slice_off[r >> 5];
+      s_hi = a.ell.slice_off[(r >> 5) + 1];
+      prefetch_chunk(sa, s_lo, s_hi, 0);
+      prefetch_chunk(sa, s_lo, s_hi, 1);
+    }
 #pragma unroll 2
     for (int j = 0; j < len; ++j) {
+      if (pf_lane && (j % kPfSlots) == 0) prefetch_chunk(sa, s_lo, s_hi, j / kPfSlots + 2);
       const int64_t p = base + ((int64_t)j << 5);
       const int64_t c = __ldg(col + p);
       rev_accum<RV, LAP>(rev_load<RV, LAP>(a, S, Q, p, c), sx, sy, sl);
@@ -333,24 +386,29 @@ namespace {
 
 // Kernel variants: 0 = one entry per loop iteration (fewest registers, most resident
 // warps), 1 = two entries per iteration with the register count capped at six blocks per
-// SM, 2 = two entries per iteration uncapped, 3 = software pipeline.
+// SM, 2 = two entries per iteration uncapped, 3 = software pipeline, 4 = variant 1 with
+// the slice's streamed arrays prefetched into L2 ahead of use, 5 = variant 2 with it.
 template <bool WT, bool WQ, int FLY>
 void fwd_variant(const FwdArgs& a, int variant, unsigned g, cudaStream_t s) {
   switch (variant) {
-    case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6><<<g, kBlock, 0, s>>>(a); break;
-    case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1><<<g, kBlock, 0, s>>>(a); break;
-    case 3: k_fwd_euler_dw<WT, WQ, FLY, 1, 1><<<g, kBlock, 0, s>>>(a); break;
-    default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1><<<g, kBlock, 0, s>>>(a); break;
+    case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false><<<g, kBlock, 0, s>>>(a); break;
+    case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, false><<<g, kBlock, 0, s>>>(a); break;
+    case 3: k_fwd_euler_dw<WT, WQ, FLY, 1, 1, false><<<g, kBlock, 0, s>>>(a); break;
+    case 4: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, true><<<g, kBlock, 0, s>>>(a); break;
+    case 5: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, true><<<g, kBlock, 0, s>>>(a); break;
+    default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
 
 template <bool RV, bool LAP>
 void rev_variant(const RevArgs& a, int variant, unsigned g, cudaStream_t s) {
   switch (variant) {
-    case 1: k_rev_euler_dw<RV, LAP, 2, 6><<<g, kBlock, 0, s>>>(a); break;
-    case 2: k_rev_euler_dw<RV, LAP, 2, 1><<<g, kBlock, 0, s>>>(a); break;
-    case 3: k_rev_euler_dw<RV, LAP, 1, 1><<<g, kBlock, 0, s>>>(a); break;
-    default: k_rev_euler_dw<RV, LAP, 0, 1><<<g, kBlock, 0, s>>>(a); break;
+    case 1: k_rev_euler_dw<RV, LAP, 2, 6, false><<<g, kBlock, 0, s>>>(a); break;
+    case 2: k_rev_euler_dw<RV, LAP, 2, 1, false><<<g, kBlock, 0, s>>>(a); break;
+    case 3: k_rev_euler_dw<RV, LAP, 1, 1, false><<<g, kBlock, 0, s>>>(a); break;
+    case 4: k_rev_euler_dw<RV, LAP, 2, 6, true><<<g, kBlock, 0, s>>>(a); break;
+    case 5: k_rev_euler_dw<RV, LAP, 2, 1, true><<<g, kBlock, 0, s>>>(a); break;
+    default: k_rev_euler_dw<RV, LAP, 0, 1, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
 

@@ -50,6 +50,12 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// Requests [p, p + bytes) into L2 with one bulk prefetch (nothing to wait for); p must be
+// 16-byte aligned and bytes a multiple of 16, the range inside one allocation.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // L2 policy for data read once per launch (the streamed operator arrays): evicted first,
 // so that it does not push the reused node arrays (states, gathered records) out of L2.
 __device__ __forceinline__ uint64_t policy_evict_first() {

@@ -165,12 +165,16 @@ def test_rhs_adjoint_dot_product_with_gpu_fd(oracle, gpu_lib, cyl, cyl_ops, case
     assert abs(lhs - rhs) / abs(rhs) < 1e-7, (lhs, rhs)
 
 
-def test_rhs_adjoint_rejects_residual_viscosity(oracle, gpu_lib, cyl, cyl_ops):
-    from meshfree_gb300._lib import MFTError
-    _semi, ctx, _hv, _g = _setup(oracle, gpu_lib, cyl, cyl_ops, "rv")
+def test_rhs_adjoint_rejects_viscosity_after_hyperviscosity(oracle, gpu_lib, cyl, cyl_ops):
+    """The residual viscosity's partial du would include the hyperviscosity term, whose
+    adjoint the viscosity path does not route: MFT_ERR_UNSUPPORTED (the viscosity sources
+    before or without hyperviscosity are covered in test_gpu_adjoint_visc.py)."""
+    from meshfree_gb300._lib import MFTError, MFT_ERR_UNSUPPORTED
+    _semi, ctx, _hv, _g = _setup(oracle, gpu_lib, cyl, cyl_ops, "tominec_rv")
     u = ic_bumpy(cyl["positions"])
-    with pytest.raises(MFTError):
+    with pytest.raises(MFTError) as e:
         ctx.rhs_adjoint(u, u)
+    assert e.value.code == MFT_ERR_UNSUPPORTED
 
 
 def _trajectory(oracle, gpu_lib, cyl, cyl_ops, vortex, case):
