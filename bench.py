@@ -80,6 +80,9 @@ def parse():
                     help="run one auxiliary measurement alone")
     ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
+    ap.add_argument("--dw-variant", type=int, default=-1,
+                    help="double-word gather kernel variant of the dw/dfma measurements "
+                         "(-1: autotuned; 0..5 fixed, e.g. for profiling one kernel)")
     ap.add_argument("--igr", type=int, default=1, help="1 runs the IGR-source measurement")
     ap.add_argument("--setup", type=int, default=1,
                     help="1 runs the set-up measurement (KNN and weights of the vortex cloud)")
@@ -786,9 +789,12 @@ def config_dict(workload, n, prec, arith="dw"):
             "parallelism": "replicas"}
 
 
-def timed_workload(args, workload, side, prec, arith, local, pg, clocks=None):
+def timed_workload(args, workload, side, prec, arith, local, pg, clocks=None, dw_variant=-1):
     """Build + the timed region of one workload/form: value, per-kernel profile, end state."""
     semi, dom, u0, dt, n = build_problem(workload, side, prec, local, arith)
+    if dw_variant >= 0:
+        from meshfree_gb300 import _lib as L
+        dom.ctx.set_option(L.OPT_DW_VARIANT, dw_variant)
     ms, prof, clk, u_end, ms_prof = timed_steps(dom.ctx, u0, dt, args.warmup, args.steps, pg,
                                                 clocks)
     ms = max_over_ranks(pg, ms)
@@ -823,8 +829,12 @@ def run_fp32(args, local, peaks):
 
 def run_one_form(args, local, peaks, prec, arith):
     """One form of the headline workload alone (profiling runs)."""
-    r = timed_workload(args, args.workload, args.side, prec, arith, local, None)
+    r = timed_workload(args, args.workload, args.side, prec, arith, local, None,
+                       dw_variant=args.dw_variant)
+    from meshfree_gb300 import _lib as L
     out = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
+           "variant": {"fwd_gather": r["dom"].ctx.get_option(L.OPT_TUNED_FWD),
+                       "rev_gather": r["dom"].ctx.get_option(L.OPT_TUNED_REV)},
            "kernels": _kernels(r["prof"]),
            "roofline": roofline(r["prof"], r["n"], prec, HV[args.workload], peaks, arith,
                                 tag="%s%s_%s" % (prec, arith if prec == "fp64" else "",
@@ -902,6 +912,9 @@ def run_ours(args):
     launches = sum(v[1] for v in r64["prof"].values())
     tag = "fp64dw_" + args.workload
     roof = roofline(r64["prof"], n, "fp64", hv, peaks, "dw", tag=tag)
+    from meshfree_gb300 import _lib as L
+    dw_variant = {"fwd_gather": r64["dom"].ctx.get_option(L.OPT_TUNED_FWD),
+                  "rev_gather": r64["dom"].ctx.get_option(L.OPT_TUNED_REV)}
 
     # the same workload with FP64 fused multiply-adds in the gathers
     rd = timed_workload(args, args.workload, args.side, "fp64", "dfma", local, pg)
@@ -983,6 +996,7 @@ def run_ours(args):
         "kernels": _kernels(r64["prof"]),
         "clocks": r64["clk"],
         "fma_rates_per_s": peaks["fma_rates"],
+        "dw_gather_variant": dw_variant,
         "fp64_dfma": dfma,
         "fp32_apply": {"value": value32, "unit": UNIT, "speedup_vs_fp64": value32 / value,
                        "l2_density_err_vs_fp64": l2, "linf_density_err_vs_fp64": linf,
