@@ -850,8 +850,10 @@ def run_vortex(args, local, peaks):
     check), stepped with per-step graphs."""
     side = args.vortex_side
     out = {}
+    ends = {}
     for prec in ("fp64", "fp32"):
         r = timed_workload(args, "vortex", side, prec, "auto", local, None)
+        ends[prec] = r["u"]
         ctx, dt, n = r["dom"].ctx, r["dt"], r["n"]
         nsteps = int(round(1.0 / dt))
         ctx.history_init(3)
@@ -873,6 +875,12 @@ def run_vortex(args, local, peaks):
         ctx.close()
     out["workload"] = config_dict("vortex", side * side, "fp64")["workload"]
     out["fp32_speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # the FP32 form's density against the FP64 form after the same timed steps (the
+    # FP64 form equals the oracle's trajectory to 1e-10 on this workload: the -m gpu
+    # full-size tests)
+    d32, d64 = ends["fp32"][0], ends["fp64"][0]
+    out["fp32_l2_density_err_vs_fp64"] = float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))
+    out["fp32_steps_compared"] = args.warmup + args.steps
     return out
 
 
