@@ -121,7 +121,10 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
 // often.  Coordinates are quantised over the cloud's bounding box to 31 bits per axis
 // (2D) or 21 (3D) and their bits interleaved; ties keep node order.  Only which thread forms which
 // row changes: every row's sum keeps its own order, so the results are unchanged.
-std::vector<int32_t> morton_order(int dim, int64_t n, const std::vector<double>& xyz) {
+// With ensemble members (seg_off, nseg > 0) the curve runs inside each member in turn, so
+// that a warp's rows stay in one member (the members of an ensemble may overlap in space).
+std::vector<int32_t> morton_order(int dim, int64_t n, const std::vector<double>& xyz,
+                                  const std::vector<int64_t>& seg_off = {}) {
   double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
   for (int d = 0; d < dim; ++d) {
     lo[d] = hi[d] = n ? xyz[d] : 0.0;
@@ -150,8 +153,14 @@ std::vector<int32_t> morton_order(int dim, int64_t n, const std::vector<double>&
   }
   std::vector<int32_t> order(n);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  if (seg_off.size() >= 2) {
+    for (size_t m = 0; m + 1 < seg_off.size(); ++m)
+      std::stable_sort(order.begin() + seg_off[m], order.begin() + seg_off[m + 1],
+                       [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  } else {
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  }
   return order;
 }
 
@@ -360,7 +369,9 @@ void ensure_device_ops(mft_ctx* c) {
   cudaStream_t s = c->stream;
   std::vector<int64_t> pos;
   std::vector<int32_t> zorder;
-  if (spatial) zorder = morton_order(c->dim, c->n, c->xyz);
+  if (spatial)
+    zorder = morton_order(c->dim, c->n, c->xyz,
+                          c->nseg > 0 ? c->seg_off : std::vector<int64_t>{});
   const std::vector<int32_t>* base = spatial ? &zorder : nullptr;
   build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base);
   c->fwd_pos.upload(pos, s);
@@ -1422,6 +1433,8 @@ mft_status mft_set_segments(mft_ctx* c, int nseg, const int64_t* offsets, const 
     MFT_REQUIRE(nseg >= 0 && nseg <= 1 << 20, MFT_ERR_ARG, "nseg out of range");
     set_device(c);
     c->fsal_valid = false;
+    // the spatial row order keeps members contiguous, so it follows the segments
+    if (c->layout_order == 1 && (nseg > 0 || c->nseg > 0)) c->dev_dirty = true;
     if (nseg == 0) {
       c->nseg = 0;
       return;
