@@ -659,6 +659,7 @@ static void ensure_igr(mft_ctx* c) {
 }
 
 void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_in) {
+  NvtxRange rng_rhs("rhs!");
   ensure_device_ops(c);
   ensure_bcs(c);
   refresh_dirichlet(c, t);
@@ -683,6 +684,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
 
   // 1. strong BCs, pass 1 (mutates u)
   if (c->nb > 0) {
+    NvtxRange rng("boundary flux");
     ProfScope ps(c, MFT_K_BC);
     launch_bc_pass1(c->nb, c->d_bnode.p, V, c->eq, bc, us, us32, s);
   }
@@ -738,6 +740,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   };
   bool forked = false;
   if (iv >= 0 && c->src_kind[iv] == MFT_SRC_RV && !c->prof_on) {
+    NvtxRange rng("source terms");
     MFT_CUDA(cudaEventRecord(c->ev_fork, s));
     MFT_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
     rv_norms(c->stream2);
@@ -770,6 +773,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ia.counter = c->igr_counter.p;
     ia.sc = c->igr_sc.p;
     {
+      NvtxRange rng("source terms");
       ProfScope ps(c, MFT_K_IGR);
       launch_igr(ia, us, s);
     }
@@ -779,9 +783,11 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   // 2. flux per node (FP64 Euler; double-word pairs of the flux and the state for the
   // double-word gathers)
   if (dw) {
+    NvtxRange rng("calc fluxes");
     ProfScope ps(c, MFT_K_FLUX);
     launch_prep_euler_dw(n, c->gamma, us, c->Fdw.p, c->udw.p, s);
   } else if (!f32 && c->eq == MFT_EQ_EULER2D) {
+    NvtxRange rng("calc fluxes");
     ProfScope ps(c, MFT_K_FLUX);
     launch_flux_f64(n, c->eq, V, c->gamma, us, c->F.p, s);
   }
@@ -868,6 +874,8 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     prepare_eps(fa.ea);
   }
   {
+    // the forward gather: the flux divergence (and the fused viscosity when formed here)
+    NvtxRange rng("calc fluxes");
     ProfScope ps(c, MFT_K_FWD);
     launch_fwd(c, fa);
   }
@@ -909,6 +917,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     r1.du_p_out = c->du_p2.p;
     r1.du_p_out32 = c->du_p2_32.p;
     r1.ep = ep;
+    NvtxRange rng("source terms");
     ProfScope ps(c, MFT_K_REV_LAP);
     launch_rev(c, r1);
     dp = c->du_p2.p;
@@ -920,6 +929,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     else if (c->src_kind[iv] == MFT_SRC_RV) rv_norms(s);
     ea.du_p = f32 ? nullptr : dp;
     ea.du_p32 = f32 ? dp32 : nullptr;
+    NvtxRange rng("source terms");
     ProfScope ps(c, MFT_K_EPS);
     launch_eps(ea, s);
   }
@@ -933,6 +943,9 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   r2.final_epilogue = 1;
   r2.du_p_out = nullptr;
   r2.ep = ep;
+  // the transpose gather applies the viscosity and hyperviscosity sources; its epilogue
+  // is pass 2 of the boundary conditions and the stage combination
+  NvtxRange rng("source terms");
   ProfScope ps(c, MFT_K_REV);
   launch_rev(c, r2);
 }
@@ -1017,6 +1030,7 @@ void history_push(mft_ctx* c, double t, const double* u_aos, int success_iter) {
   if (success_iter > 0)
     MFT_REQUIRE(time_deriv_weights(m, c->hist_t.data(), w) == 0, MFT_ERR_SINGULAR,
                 "time_deriv_weights: singular Vandermonde system");
+  NvtxRange rng("history");
   ProfScope ps(c, MFT_K_HISTORY);
   if (success_iter <= 0) {
     MFT_CUDA(cudaMemcpyAsync(c->hist[c->hist_head].p, u_aos, nv * sizeof(double),
@@ -1609,6 +1623,7 @@ void apply_limiter(mft_ctx* c, double* u, float* u32) {
               "the positivity limiter needs the 2D Euler equations");
   c->lim_buf.alloc((size_t)c->n * 4);
   for (int q = 0; q < c->lim_n; ++q) {
+    NvtxRange rng("positivity limiter");
     ProfScope ps(c, MFT_K_LIMITER);
     launch_zs_limiter(c->n, c->fwd.view(), c->lim_var[q], c->lim_thr[q], c->gamma, u, u32,
                       c->lim_buf.p, c->stream);
