@@ -22,6 +22,7 @@
 #ifndef MESHFREE_GB300_H
 #define MESHFREE_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -294,6 +295,22 @@ mft_status mft_set_rv_state(mft_ctx* ctx, const double* const* approx_du, int nv
 
 /* Viscosity of the last RV/upwind source evaluation (host, n values). */
 mft_status mft_get_viscosity(mft_ctx* ctx, double* eps);
+
+/* ---------------------------------------------------------------- checkpoint / resume
+ * The time-integration state of a context as one byte image, so that a run can stop and
+ * resume bit for bit: t, the device state u_n, the pending first SSP-RK3 stage (first
+ * same as last), the step-time origin, and the HistoryCallback's ring (times, states,
+ * approx_du, success_iter).  The reference writes solution files only
+ * (src/callbacks_step/save_solution_vtk.jl:158-194) and has no restart; this has no
+ * counterpart there.  The operators, BCs, sources, options and limiter are not in the
+ * image: the resuming context is set up as the saving one was (a pending stage from
+ * another precision or gather arithmetic is dropped and recomputed).  The image starts
+ * with the 8 bytes "MFTCKPT\0", is in host byte order and ends with an FNV-1a 64-bit hash
+ * of the bytes before it; mft_checkpoint_load returns MFT_ERR_ARG for a truncated,
+ * corrupted or foreign image, or one of another problem size, and changes nothing then. */
+mft_status mft_checkpoint_size(mft_ctx* ctx, size_t* bytes);
+mft_status mft_checkpoint_save(mft_ctx* ctx, void* buf, size_t bytes);
+mft_status mft_checkpoint_load(mft_ctx* ctx, const void* buf, size_t bytes);
 
 /* ---------------------------------------------------------------- positivity limiter
  * PositivityPreservingLimiterZhangShu(; thresholds, variables)

@@ -1566,6 +1566,7 @@ mft_status mft_set_state(mft_ctx* c, const double* const* u, int nvars, double t
     c->t_state = t;
     c->state_valid = true;
     c->fsal_valid = false;
+    c->origin_valid = false;
   });
 }
 
@@ -1585,28 +1586,37 @@ mft_status mft_get_state(mft_ctx* c, double* const* u, int nvars, double* t) {
   });
 }
 
+namespace {
+
+// Ring of approx_order + 1 zeroed states (approx_order -1 releases the ring).
+void history_setup(mft_ctx* c, int approx_order) {
+  c->graph_valid = false;
+  c->hist_order = approx_order;
+  c->hist_t.assign(approx_order + 1, 0.0);
+  const size_t nv = (size_t)c->n * c->nvars;
+  for (int k = 0; k < 8; ++k) {
+    if (k <= approx_order) {
+      c->hist[k].alloc(nv);
+      c->hist[k].zero(c->stream);
+    } else {
+      c->hist[k].release();
+    }
+  }
+  c->hist_w.alloc(16);
+  c->hist_head = 0;
+  c->success_iter = 0;
+  c->fsal_valid = false;
+  MFT_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+}  // namespace
+
 mft_status mft_history_init(mft_ctx* c, int approx_order) {
   return guarded(c, [&] {
-    c->graph_valid = false;
     check_state_ready(c);
     MFT_REQUIRE(approx_order >= 0 && approx_order <= 7, MFT_ERR_ARG, "approx_order out of range");
     set_device(c);
-    c->hist_order = approx_order;
-    c->hist_t.assign(approx_order + 1, 0.0);
-    const size_t nv = (size_t)c->n * c->nvars;
-    for (int k = 0; k < 8; ++k) {
-      if (k <= approx_order) {
-        c->hist[k].alloc(nv);
-        c->hist[k].zero(c->stream);
-      } else {
-        c->hist[k].release();
-      }
-    }
-    c->hist_w.alloc(16);
-    c->hist_head = 0;
-    c->success_iter = 0;
-    c->fsal_valid = false;
-    MFT_CUDA(cudaStreamSynchronize(c->stream));
+    history_setup(c, approx_order);
   });
 }
 
@@ -1676,16 +1686,35 @@ void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3) {
   apply_limiter(c, c->U[1].p, shadow(c, 1));
 }
 
+// Step times are formed as t_origin + k dt, k counted from the first step of size dt
+// after the state was set (or dt changed), as OrdinaryDiffEq's fixed-step loop forms
+// them; so a run split over several calls, or resumed from a checkpoint, takes the same
+// times bit for bit as one call.
+void sync_origin(mft_ctx* c, double dt) {
+  if (!c->origin_valid || c->origin_dt != dt ||
+      c->t_state != c->t_origin + (double)c->origin_steps * dt) {
+    c->origin_valid = true;
+    c->t_origin = c->t_state;
+    c->origin_dt = dt;
+    c->origin_steps = 0;
+  }
+}
+
+double step_time(const mft_ctx* c, double dt, int64_t k) {
+  return c->t_origin + (double)(c->origin_steps + k) * dt;
+}
+
 void ssprk33_direct(mft_ctx* c, double dt, int nsteps) {
-  const double t0 = c->t_state;
+  sync_origin(c, dt);
   for (int k = 0; k < nsteps; ++k) {
-    enqueue_step(c, dt, t0 + k * dt, 0, 3);
-    const double tn = t0 + (k + 1) * dt;
+    enqueue_step(c, dt, step_time(c, dt, k), 0, 3);
+    const double tn = step_time(c, dt, k + 1);
     std::swap(c->U[0].p, c->U[3].p);
     std::swap(c->U32[0].p, c->U32[3].p);
     c->t_state = tn;
     if (c->hist_order >= 0) history_push(c, tn, c->U[0].p, c->success_iter + 1);
   }
+  c->origin_steps += nsteps;
 }
 
 // One SSP-RK3 step captured as a CUDA graph, once with u_n in U0 and once with u_n in
@@ -1735,13 +1764,13 @@ void ssprk33_graph(mft_ctx* c, double dt, int nsteps) {
   const int slots = c->hist_order + 1;
   // host-side bookkeeping of the HistoryCallback for the whole batch
   std::vector<StepParams> tab(nsteps);
-  const double t0 = c->t_state;
+  sync_origin(c, dt);
   for (int k = 0; k < nsteps; ++k) {
     StepParams& sp = tab[k];
     memset(&sp, 0, sizeof(sp));
     sp.si_eps = c->success_iter;
     if (c->hist_order >= 0) {
-      const double tn = t0 + (k + 1) * dt;
+      const double tn = step_time(c, dt, k + 1);
       for (int q = slots - 1; q > 0; --q) c->hist_t[q] = c->hist_t[q - 1];
       c->hist_t[0] = tn;
       c->hist_head = (c->hist_head + slots - 1) % slots;
@@ -1789,7 +1818,8 @@ void ssprk33_graph(mft_ctx* c, double dt, int nsteps) {
     std::swap(c->U[0].p, c->U[3].p);
     std::swap(c->U32[0].p, c->U32[3].p);
   }
-  c->t_state = t0 + nsteps * dt;
+  c->t_state = step_time(c, dt, nsteps);
+  c->origin_steps += nsteps;
 }
 
 void ssprk33_run(mft_ctx* c, double dt, int nsteps, bool use_graph = false) {
@@ -1899,6 +1929,193 @@ mft_status mft_set_rv_state(mft_ctx* c, const double* const* approx_du, int nvar
     c->success_iter = success_iter;
     c->fsal_valid = false;
     MFT_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+// ---------------------------------------------------------------- checkpoint / resume
+
+namespace {
+
+// Image layout (host byte order; both supported hosts are little-endian):
+//   CkptHeader, u_n (n x nvars node-major FP64), the pending first stage when fsal = 1
+//   (u_n + dt f(u_n), same shape), the history ring newest first (hist_order + 1
+//   states), approx_du, then the FNV-1a 64-bit hash of everything before it.
+struct CkptHeader {
+  char magic[8];
+  uint32_t version;
+  uint32_t header_bytes;
+  int64_t n;
+  int32_t nvars;
+  int32_t hist_order;  // -1: no HistoryCallback
+  int32_t success_iter;
+  int32_t fsal;
+  int32_t form;  // precision * 4 + (double-word gathers): the form the pending stage came from
+  int32_t reserved;
+  double t;
+  double fsal_dt;
+  double t_origin, origin_dt;
+  int64_t origin_steps;
+  int32_t origin_valid;
+  int32_t reserved2;
+  double hist_t[8];
+};
+static_assert(sizeof(CkptHeader) == 160, "checkpoint header layout");
+constexpr char kCkptMagic[8] = {'M', 'F', 'T', 'C', 'K', 'P', 'T', '\0'};
+constexpr uint32_t kCkptVersion = 1;
+
+uint64_t fnv1a64(const unsigned char* p, size_t n) {
+  uint64_t h = 14695981039346656037ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+int ckpt_form(const mft_ctx* c) { return c->precision * 4 + (use_dw(c) ? 1 : 0); }
+
+size_t ckpt_bytes(const mft_ctx* c) {
+  const size_t nvb = (size_t)c->n * c->nvars * sizeof(double);
+  const size_t slots = c->hist_order >= 0 ? (size_t)c->hist_order + 1 : 0;
+  return sizeof(CkptHeader) + nvb * (1 + (c->fsal_valid ? 1 : 0) + slots + 1) + 8;
+}
+
+}  // namespace
+
+mft_status mft_checkpoint_size(mft_ctx* c, size_t* bytes) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(bytes, MFT_ERR_ARG, "NULL size pointer");
+    MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "no device state to checkpoint");
+    *bytes = ckpt_bytes(c);
+  });
+}
+
+mft_status mft_checkpoint_save(mft_ctx* c, void* buf, size_t bytes) {
+  return guarded(c, [&] {
+    MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "no device state to checkpoint");
+    MFT_REQUIRE(buf, MFT_ERR_ARG, "NULL checkpoint buffer");
+    const size_t need = ckpt_bytes(c);
+    MFT_REQUIRE(bytes >= need, MFT_ERR_ARG,
+                "checkpoint buffer too small: " + std::to_string(need) + " bytes needed");
+    set_device(c);
+    cudaStream_t s = c->stream;
+    unsigned char* out = static_cast<unsigned char*>(buf);
+    CkptHeader h{};
+    memcpy(h.magic, kCkptMagic, 8);
+    h.version = kCkptVersion;
+    h.header_bytes = sizeof(CkptHeader);
+    h.n = c->n;
+    h.nvars = c->nvars;
+    h.hist_order = c->hist_order;
+    h.success_iter = c->success_iter;
+    h.fsal = c->fsal_valid ? 1 : 0;
+    h.form = ckpt_form(c);
+    h.t = c->t_state;
+    h.fsal_dt = c->fsal_dt;
+    h.t_origin = c->t_origin;
+    h.origin_dt = c->origin_dt;
+    h.origin_steps = c->origin_steps;
+    h.origin_valid = c->origin_valid ? 1 : 0;
+    const int slots = c->hist_order + 1;
+    for (int k = 0; k < slots && k < 8; ++k) h.hist_t[k] = c->hist_t[k];
+    memcpy(out, &h, sizeof(h));
+    size_t off = sizeof(h);
+    const size_t nvb = (size_t)c->n * c->nvars * sizeof(double);
+    auto d2h = [&](const double* src) {
+      MFT_CUDA(cudaMemcpyAsync(out + off, src, nvb, cudaMemcpyDeviceToHost, s));
+      off += nvb;
+    };
+    d2h(c->U[0].p);
+    if (c->fsal_valid) d2h(c->U[1].p);
+    for (int k = 0; k < slots; ++k) d2h(c->hist[(c->hist_head + k) % slots].p);
+    d2h(c->approx_du.p);
+    MFT_CUDA(cudaStreamSynchronize(s));
+    const uint64_t hash = fnv1a64(out, off);
+    memcpy(out + off, &hash, 8);
+  });
+}
+
+mft_status mft_checkpoint_load(mft_ctx* c, const void* buf, size_t bytes) {
+  return guarded(c, [&] {
+    check_state_ready(c);
+    MFT_REQUIRE(buf, MFT_ERR_ARG, "NULL checkpoint buffer");
+    MFT_REQUIRE(bytes >= sizeof(CkptHeader) + 8, MFT_ERR_ARG, "checkpoint image truncated");
+    const unsigned char* in = static_cast<const unsigned char*>(buf);
+    CkptHeader h;
+    memcpy(&h, in, sizeof(h));
+    MFT_REQUIRE(memcmp(h.magic, kCkptMagic, 8) == 0, MFT_ERR_ARG, "not a checkpoint image");
+    MFT_REQUIRE(h.version == kCkptVersion && h.header_bytes == sizeof(CkptHeader), MFT_ERR_ARG,
+                "unsupported checkpoint version");
+    MFT_REQUIRE(h.n == c->n && h.nvars == c->nvars, MFT_ERR_ARG,
+                "checkpoint of another problem size (n " + std::to_string(h.n) + ", nvars " +
+                    std::to_string(h.nvars) + ")");
+    MFT_REQUIRE(h.hist_order >= -1 && h.hist_order <= 7 && h.success_iter >= 0 &&
+                    (h.fsal == 0 || h.fsal == 1),
+                MFT_ERR_ARG, "corrupt checkpoint header");
+    const size_t nvb = (size_t)c->n * c->nvars * sizeof(double);
+    const int slots = h.hist_order + 1;
+    const size_t need = sizeof(CkptHeader) + nvb * (1 + h.fsal + slots + 1) + 8;
+    MFT_REQUIRE(bytes == need, MFT_ERR_ARG,
+                "checkpoint image is " + std::to_string(bytes) + " bytes, expected " +
+                    std::to_string(need));
+    uint64_t hash = 0;
+    memcpy(&hash, in + need - 8, 8);
+    MFT_REQUIRE(hash == fnv1a64(in, need - 8), MFT_ERR_ARG, "checkpoint checksum mismatch");
+    set_device(c);
+    ensure_work(c);
+    if (h.hist_order != c->hist_order) history_setup(c, h.hist_order);
+    cudaStream_t s = c->stream;
+    size_t off = sizeof(h);
+    auto h2d = [&](double* dst) {
+      MFT_CUDA(cudaMemcpyAsync(dst, in + off, nvb, cudaMemcpyHostToDevice, s));
+      off += nvb;
+    };
+    h2d(c->U[0].p);
+    // the pending first stage is kept only for the form that computed it
+    const bool fsal = h.fsal == 1 && h.form == ckpt_form(c);
+    if (h.fsal == 1) {
+      if (fsal) h2d(c->U[1].p);
+      else off += nvb;
+    }
+    for (int k = 0; k < slots; ++k) h2d(c->hist[k].p);
+    h2d(c->approx_du.p);
+    const int64_t nv = c->n * c->nvars;
+    if (c->precision == MFT_PREC_FP32) {
+      launch_aos_to_f32(c->U[0].p, c->U32[0].p, nv, s);
+      if (fsal) launch_aos_to_f32(c->U[1].p, c->U32[1].p, nv, s);
+    }
+    MFT_CUDA(cudaStreamSynchronize(s));
+    c->hist_head = 0;
+    for (int k = 0; k < slots; ++k) c->hist_t[k] = h.hist_t[k];
+    c->success_iter = h.success_iter;
+    c->t_state = h.t;
+    c->state_valid = true;
+    c->fsal_valid = fsal;
+    c->fsal_dt = h.fsal_dt;
+    c->origin_valid = h.origin_valid != 0;
+    c->t_origin = h.t_origin;
+    c->origin_dt = h.origin_dt;
+    c->origin_steps = h.origin_steps;
+    c->graph_valid = false;
+    if (fsal) {
+      // With the pending stage kept, the next step starts without a direct rhs!: one
+      // rhs! on a copy of u_n builds the device layouts and times the gather variants
+      // now, outside the first step's graph capture (its outputs are scratch).
+      MFT_CUDA(cudaMemcpyAsync(c->work_u.p, c->U[0].p, nvb, cudaMemcpyDeviceToDevice, s));
+      float* w32 = nullptr;
+      if (c->precision == MFT_PREC_FP32) {
+        launch_aos_to_f32(c->work_u.p, c->work_u32.p, nv, s);
+        w32 = c->work_u32.p;
+      }
+      Epilogue ep{};
+      ep.kind = kStage1;
+      ep.dt = c->fsal_dt;
+      ep.out = c->U[2].p;
+      ep.out32 = shadow(c, 2);
+      eval_rhs(c, c->work_u.p, w32, c->t_state, ep);
+      MFT_CUDA(cudaStreamSynchronize(s));
+      check_kernel_errors(c);
+    }
   });
 }
 

@@ -109,6 +109,10 @@ struct mft_ctx {
   bool state_valid = false;
   bool fsal_valid = false;
   double fsal_dt = 0.0;
+  // step times are t_origin + k dt, k counted from the origin while dt stays the same
+  bool origin_valid = false;
+  double t_origin = 0.0, origin_dt = 0.0;
+  int64_t origin_steps = 0;
 
   // history ring (HistoryCallback)
   int hist_order = -1;

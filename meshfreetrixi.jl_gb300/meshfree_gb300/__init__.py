@@ -7,6 +7,7 @@ from .api import (  # noqa: F401
     Point1D, Point2D, Point3D, PointCloudBasis, PositivityPreservingLimiterZhangShu, density, pressure, PointCloudDomain, PointCloudDomain_from_medusa,
     PointCloudEnsemble, PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
     SemidiscretizationHyperbolic, SourceHyperviscosityFlyer, SourceHyperviscosityTominec, SourceIGR,
-    SourceResidualViscosityTominec, SourceTerms, SourceUpwindViscosityTominec, SSPRK33,
-    boundary_condition_slip_wall, rhs_, rhs_adjoint_, semidiscretize, solve, solve_adjoint)
+    SaveCheckpointCallback, SourceResidualViscosityTominec, SourceTerms,
+    SourceUpwindViscosityTominec, SSPRK33, boundary_condition_slip_wall, load_checkpoint, rhs_,
+    rhs_adjoint_, save_checkpoint, semidiscretize, solve, solve_adjoint)
 from .medusa import read_medusa_file  # noqa: F401

@@ -72,6 +72,9 @@ SIGNATURES = {
     "mft_ssprk33_adjoint": (I32, [VP, VP, I32]),
     "mft_ssprk33_adjoint_device": (I32, [VP, VP]),
     "mft_get_viscosity": (I32, [VP, VP]),
+    "mft_checkpoint_size": (I32, [VP, C.POINTER(C.c_size_t)]),
+    "mft_checkpoint_save": (I32, [VP, VP, C.c_size_t]),
+    "mft_checkpoint_load": (I32, [VP, VP, C.c_size_t]),
     "mft_profile": (I32, [VP, I32]),
     "mft_profile_get": (I32, [VP, I32, C.POINTER(DBL), C.POINTER(I64), C.POINTER(C.c_char_p)]),
     "mft_region": (I32, [VP, I32, C.POINTER(DBL)]),
@@ -357,6 +360,21 @@ class Context:
         eps = np.empty(self.n)
         self.check(self.lib.mft_get_viscosity(self.h, _p(eps)))
         return eps
+
+    def checkpoint(self):
+        """The time-integration state (t, u, pending first stage, history ring) as bytes
+        (mft_checkpoint_save)."""
+        size = C.c_size_t(0)
+        self.check(self.lib.mft_checkpoint_size(self.h, C.byref(size)))
+        buf = (C.c_ubyte * size.value)()
+        self.check(self.lib.mft_checkpoint_save(self.h, buf, size.value))
+        return bytes(buf)
+
+    def restore(self, image):
+        """Loads an image from checkpoint() into this context (mft_checkpoint_load)."""
+        image = bytes(image)
+        buf = (C.c_ubyte * len(image)).from_buffer_copy(image)
+        self.check(self.lib.mft_checkpoint_load(self.h, buf, len(image)))
 
     def sync(self):
         self.check(self.lib.mft_sync(self.h))

@@ -10,6 +10,7 @@ Node indices are 0-based.  Every numerical step runs in the CUDA library.
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 from typing import Callable
 
@@ -452,6 +453,31 @@ class HistoryCallback:
     approx_order: int
 
 
+@dataclass
+class SaveCheckpointCallback:
+    """Writes the integrator state (t, u, the pending first stage, the history ring) to
+    `path` every `interval` steps and at the end of solve, overwriting the file
+    (mft_checkpoint_save).  solve(..., resume_from=path) continues from such a file bit
+    for bit.  The reference has no restart files (save_solution_vtk.jl writes output)."""
+    interval: int
+    path: str
+
+
+def save_checkpoint(semi, path):
+    """The device integrator state of semi's context into the file at path."""
+    data = semi.domain.ctx.checkpoint()
+    tmp = str(path) + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(data)
+    os.replace(tmp, path)
+
+
+def load_checkpoint(semi, path):
+    """Loads a file written by save_checkpoint into semi's context (same problem set-up)."""
+    with open(path, "rb") as f:
+        semi.domain.ctx.restore(f.read())
+
+
 class SSPRK33:
     """Shu-Osher SSP-RK3 with first-same-as-last stage reuse; SSPRK33(stage_limiter!)
     applies the limiter after every stage, as OrdinaryDiffEq does."""
@@ -502,24 +528,40 @@ class ODESolution:
     nsteps: int
 
 
-def solve(ode, alg=None, dt=None, callback=None, save_everystep=False):
-    """Fixed-step SSPRK33 on the device from tspan[0] to tspan[1]."""
+def solve(ode, alg=None, dt=None, callback=None, save_everystep=False, resume_from=None):
+    """Fixed-step SSPRK33 on the device from tspan[0] to tspan[1]; with resume_from (a
+    file of SaveCheckpointCallback / save_checkpoint) from the state and time held there
+    to tspan[1]."""
     assert dt is not None and dt > 0
     semi = ode.p
     ctx = semi.domain.ctx
     t0, t1 = ode.tspan
     cbs = callback if isinstance(callback, (list, tuple)) else ([callback] if callback else [])
-    ctx.set_state(ode.u0, t0)
     lim = getattr(alg, "stage_limiter", None)
     if lim is not None:
         lim.configure(ctx)
     else:
         ctx.set_limiter([], [])
-    for cb in cbs:
-        if isinstance(cb, HistoryCallback):
-            ctx.history_init(cb.approx_order)
-    nfull = int(math.floor((t1 - t0) / dt + 1e-9))
-    ctx.ssprk33(dt, nfull)
+    if resume_from is not None:
+        load_checkpoint(semi, resume_from)
+        t0 = ctx.get_state()[1]
+    else:
+        ctx.set_state(ode.u0, t0)
+        for cb in cbs:
+            if isinstance(cb, HistoryCallback):
+                ctx.history_init(cb.approx_order)
+    ckpt = [cb for cb in cbs if isinstance(cb, SaveCheckpointCallback)]
+    nfull = max(int(math.floor((t1 - t0) / dt + 1e-9)), 0)
+    if ckpt:
+        every = max(int(ckpt[0].interval), 1)
+        done = 0
+        while done < nfull:
+            k = min(every, nfull - done)
+            ctx.ssprk33(dt, k)
+            done += k
+            save_checkpoint(semi, ckpt[0].path)
+    else:
+        ctx.ssprk33(dt, nfull)
     steps = nfull
     rest = (t1 - t0) - nfull * dt
     if rest > 1e-12 * dt:
