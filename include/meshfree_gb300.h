@@ -217,13 +217,24 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
  * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
-       MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5 };
+       MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
+       MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8 };
+/* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups (256 layout rows each) of
+ * the double-word form's layouts, MFT_OPT_HALO_STAGED_FWD / _REV = how many of them have
+ * their neighbour records staged in shared memory by DW variants 6-8 (the others gather
+ * directly); 0 before the first evaluation in that form. */
 /* MFT_OPT_DW_VARIANT: kernel variant of the double-word gathers -- 0 one stencil entry
  * per loop iteration, 1 two entries per iteration with registers capped at six blocks per
  * SM, 2 two entries uncapped, 3 software-pipelined (indices two entries ahead, weights and
  * neighbour records one ahead), 4 and 5 = 1 and 2 with each warp's streamed index and
- * weight arrays prefetched into L2 eight slots ahead (one bulk prefetch per array);
+ * weight arrays prefetched into L2 eight slots ahead (one bulk prefetch per array),
+ * 6 and 7 = 0 and 2 with the distinct neighbour records of each group of 256 layout rows
+ * staged in shared memory by coalesced asynchronous copies and read from there (16-bit
+ * positions instead of the 32-bit indices; a group with more than 640 distinct
+ * neighbours gathers directly; registers capped at three blocks per SM), 8 = 7 capped at
+ * four blocks per SM;
  * -1 (default) lets the autotuner time them at the first launch of each configuration.
+ * Every variant forms the same sums in the same order (bit-identical results).
  * MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV then report the variant in use. */
 /* MFT_OPT_LAYOUT_ORDER: 1 (default) assigns the operator rows to threads along a Morton
  * curve of the node coordinates, so that a warp's 32 rows are a compact patch whose

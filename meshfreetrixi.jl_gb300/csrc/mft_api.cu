@@ -49,9 +49,11 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 // then ordered by length, longest first, inside each run of `window` consecutive rows
 // (stable, so rows stay near their neighbours): the 32 rows of a slice then have nearly
 // equal lengths and the lanes of a warp finish together.
+// With halo, the neighbour halos of the row groups are built too (kHaloRows rows each:
+// distinct columns ascending, and each element's position among them).
 void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& cols,
                EllBuf& ell, std::vector<int64_t>& pos, cudaStream_t s, int window = 0,
-               const std::vector<int32_t>* base = nullptr) {
+               const std::vector<int32_t>* base = nullptr, bool halo = false) {
   std::vector<int32_t> order(n);
   if (base) order = *base;
   else std::iota(order.begin(), order.end(), 0);
@@ -113,6 +115,60 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   ell.col.upload(col, s);
   if (window > 0 || base) ell.perm.upload(order, s);
   else ell.perm.release();
+  if (!halo) {
+    ell.halo_off.release();
+    ell.halo_col.release();
+    ell.lcol.release();
+    ell.halo_groups = ell.halo_staged = 0;
+    ell.halo_stride = 0;
+    return;
+  }
+  static_assert(kHaloRows % kSlice == 0, "halo groups are whole slices");
+  const int64_t ng = (n + kHaloRows - 1) / kHaloRows;
+  std::vector<std::vector<int32_t>> lists(ng);
+  std::vector<uint16_t> lcol(ne, 0);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t g = 0; g < ng; ++g) {
+    std::vector<int32_t>& h = lists[g];
+    const int64_t r0 = g * kHaloRows, r1 = std::min<int64_t>(n, r0 + kHaloRows);
+    for (int64_t r = r0; r < r1; ++r) {
+      const int64_t node = order[r];
+      h.insert(h.end(), cols.begin() + rowptr[node], cols.begin() + rowptr[node] + rlen[r]);
+    }
+    std::sort(h.begin(), h.end());
+    h.erase(std::unique(h.begin(), h.end()), h.end());
+    if ((int64_t)h.size() > kHaloMax) {
+      h.clear();
+      continue;
+    }
+    for (int64_t r = r0; r < r1; ++r) {
+      const int64_t sl = r / kSlice, lane = r % kSlice;
+      for (int j = 0; j < rlen[r]; ++j) {
+        const int64_t e = soff[sl] + (int64_t)j * kSlice + lane;
+        lcol[e] = (uint16_t)(std::lower_bound(h.begin(), h.end(), col[e]) - h.begin());
+      }
+    }
+  }
+  std::vector<int32_t> hoff(ng + 1, 0);
+  int64_t staged = 0;
+  int stride = 0;
+  for (int64_t g = 0; g < ng; ++g) {
+    hoff[g + 1] = hoff[g] + (int32_t)lists[g].size();
+    staged += lists[g].empty() ? 0 : 1;
+    stride = std::max(stride, (int)lists[g].size());
+  }
+  std::vector<int32_t> hcol(hoff[ng]);
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < ng; ++g)
+    std::copy(lists[g].begin(), lists[g].end(), hcol.begin() + hoff[g]);
+  ell.halo_off.upload(hoff, s);
+  ell.halo_col.upload(hcol, s);
+  ell.lcol.upload(lcol, s);
+  ell.halo_groups = ng;
+  ell.halo_staged = staged;
+  ell.halo_stride = stride;
+  // the host vectors leave scope before the copies are done
+  MFT_CUDA(cudaStreamSynchronize(s));
 }
 
 // Layout order of the nodes along a Morton (Z-order) curve of their coordinates: the 32
@@ -364,6 +420,8 @@ void ensure_device_ops(mft_ctx* c) {
   // double-word operator values are placed only while that form is in use
   const bool dw = use_dw(c);
   if (dw && !c->fwdw[0].p) c->dev_dirty = true;
+  // neighbour halos of the row groups, for the double-word gathers' staged variants
+  if (dw && !c->fwd.halo_off.p) c->dev_dirty = true;
   if (!c->dev_dirty) return;
   c->graph_valid = false;
   cudaStream_t s = c->stream;
@@ -373,10 +431,10 @@ void ensure_device_ops(mft_ctx* c) {
     zorder = morton_order(c->dim, c->n, c->xyz,
                           c->nseg > 0 ? c->seg_off : std::vector<int64_t>{});
   const std::vector<int32_t>* base = spatial ? &zorder : nullptr;
-  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base);
+  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, dw);
   c->fwd_pos.upload(pos, s);
   std::vector<int64_t> rpos_csc;
-  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base);
+  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, dw);
   std::vector<int64_t> rpos(rpos_csc.size());
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < (int64_t)rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
@@ -1436,6 +1494,9 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_FP64_ARITH) *value = c->fp64_arith;
     else if (option == MFT_OPT_LAYOUT_ORDER) *value = c->layout_order;
     else if (option == MFT_OPT_DW_VARIANT) *value = c->dw_variant;
+    else if (option == MFT_OPT_HALO_STAGED_FWD) *value = (int)c->fwd.halo_staged;
+    else if (option == MFT_OPT_HALO_STAGED_REV) *value = (int)c->rev.halo_staged;
+    else if (option == MFT_OPT_HALO_GROUPS) *value = (int)c->fwd.halo_groups;
     else throw mft::Error(MFT_ERR_ARG, "unknown option");
   });
 }

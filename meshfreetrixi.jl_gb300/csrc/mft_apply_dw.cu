@@ -10,6 +10,10 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "mft_device.cuh"
 #include "mft_dw.cuh"
 #include "mft_eps.cuh"
@@ -48,6 +52,38 @@ static __device__ __forceinline__ void prefetch_chunk(const SliceArrays& sa, int
                             (uint32_t)(ne * sa.esize[k]));
 }
 static __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+// 16-byte asynchronous copy global -> shared (bypasses registers), and the wait for all
+// of this thread's copies.
+static __device__ __forceinline__ void cp_async16(float4* smem, const float4* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+static __device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Stages the neighbour records of this block's row group (the group's halo list) into
+// shared memory: NCH 16-byte chunks per record, chunk k of list entry q at
+// sm[k * ell.halo_stride + q] (chunk-major, so that lanes reading one chunk of different
+// records spread over the banks).  chunk(k, c) is the address of chunk k of node c's
+// record.  Consecutive threads copy consecutive chunks of one record, so each record
+// arrives in whole sectors.  Returns false (nothing staged) when the group has no list.
+// Every thread of the block must call it (it ends with a block barrier).
+template <int NCH, int BS, typename Chunk>
+static __device__ __forceinline__ bool stage_halo(const EllView& ell, float4* sm, Chunk chunk) {
+  const int h0 = __ldg(ell.halo_off + blockIdx.x);
+  const int nh = __ldg(ell.halo_off + blockIdx.x + 1) - h0;
+  if (nh <= 0) return false;  // block-uniform
+  for (int q = threadIdx.x; q < nh * NCH; q += BS) {
+    const int rec = q / NCH, k = q - rec * NCH;
+    cp_async16(sm + k * ell.halo_stride + rec,
+               chunk(k, (int64_t)__ldg(ell.halo_col + h0 + rec)));
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  return true;
+}
 
 // Per node: the state as double-word pairs and the Euler flux pair evaluated from them in
 // double-word arithmetic (the textbook flux, one reciprocal for both velocities; each
@@ -98,6 +134,26 @@ static __device__ __forceinline__ FwdEntry fwd_load(const FwdArgs& a, const floa
   return e;
 }
 
+// The same entry with the neighbour's records read from the staged halo (lc: position
+// of the neighbour in the group's list).
+template <bool WT, bool WQ, int FLY>
+static __device__ __forceinline__ FwdEntry fwd_load_halo(const FwdArgs& a, const float4* sm,
+                                                         int hs, int64_t p, int lc) {
+  FwdEntry e;
+  e.wx = __ldg(a.wdw[0] + p);
+  e.wy = __ldg(a.wdw[1] + p);
+  e.fa.lo = sm[lc];
+  e.fa.hi = sm[hs + lc];
+  e.fb.lo = sm[2 * hs + lc];
+  e.fb.hi = sm[3 * hs + lc];
+  if (WT || WQ || FLY) {
+    e.uu.lo = sm[4 * hs + lc];
+    e.uu.hi = sm[5 * hs + lc];
+  }
+  if (WQ || FLY) e.wl = __ldg(a.wldw + p);
+  return e;
+}
+
 template <bool WT, bool WQ, int FLY>
 static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, dw::Acc* tx,
                                                  dw::Acc* ty, dw::Acc* q) {
@@ -135,22 +191,48 @@ static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, 
 // accumulated (the gathers are latency-bound: most samples stall on their results).
 // MINB: minimum resident blocks per SM requested from the compiler (register cap).
 // The variants form the same sums in the same order; the autotuner picks one.
-template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF>
-__global__ void __launch_bounds__(kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
-  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+// HALO: blocks of kHaloRows rows (one row group) first stage the group's neighbour
+// records in shared memory and read them from there (groups without a list gather
+// directly); PIPE 0 or 2 then sets the loop's unrolling.
+template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO>
+__global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
+  constexpr int BS = HALO ? kHaloRows : kBlock;
+  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
+  const float* __restrict__ U = reinterpret_cast<const float*>(a.udw);
+  extern __shared__ float4 hsm[];
+  bool staged = false;
+  if (HALO) {
+    const float4* F4 = reinterpret_cast<const float4*>(a.Fdw);
+    const float4* U4 = reinterpret_cast<const float4*>(a.udw);
+    staged = stage_halo<(WT || WQ || FLY) ? 6 : 4, BS>(
+        a.ell, hsm, [&](int k, int64_t c) { return k < 4 ? F4 + c * 4 + k : U4 + c * 2 + (k - 4); });
+  }
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
-  const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
-  const float* __restrict__ U = reinterpret_cast<const float*>(a.udw);
   dw::Acc f[4], tx[4], ty[4], q[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     f[v] = dw::zero(); tx[v] = dw::zero(); ty[v] = dw::zero(); q[v] = dw::zero();
   }
-  if (PIPE == 0) {
+  const uint16_t* __restrict__ lcol = a.ell.lcol;
+  const int hs = a.ell.halo_stride;
+  if (HALO && staged && PIPE == 2) {
+#pragma unroll 2
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      fwd_accum<WT, WQ, FLY>(fwd_load_halo<WT, WQ, FLY>(a, hsm, hs, p, __ldg(lcol + p)), f, tx, ty, q);
+    }
+  } else if (HALO && staged) {
+#pragma unroll 1
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      fwd_accum<WT, WQ, FLY>(fwd_load_halo<WT, WQ, FLY>(a, hsm, hs, p, __ldg(lcol + p)), f, tx, ty, q);
+    }
+  } else if (PIPE == 0) {
 #pragma unroll 1
     for (int j = 0; j < len; ++j) {
       const int64_t p = base + ((int64_t)j << 5);
@@ -272,6 +354,27 @@ static __device__ __forceinline__ RevEntry rev_load(const RevArgs& a, const floa
 }
 
 template <bool RV, bool LAP>
+static __device__ __forceinline__ RevEntry rev_load_halo(const RevArgs& a, const float4* sm,
+                                                         int hs, int64_t p, int lc) {
+  RevEntry e;
+  constexpr int kq = RV ? 4 : 0;  // first chunk of the q record
+  if (RV) {
+    e.wx = __ldg(a.wdw[0] + p);
+    e.wy = __ldg(a.wdw[1] + p);
+    e.xa.lo = sm[lc];
+    e.xa.hi = sm[hs + lc];
+    e.ya.lo = sm[2 * hs + lc];
+    e.ya.hi = sm[3 * hs + lc];
+  }
+  if (LAP) {
+    e.wl = __ldg(a.wldw + p);
+    e.qq.lo = sm[kq * hs + lc];
+    e.qq.hi = sm[(kq + 1) * hs + lc];
+  }
+  return e;
+}
+
+template <bool RV, bool LAP>
 static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx, dw::Acc* sy,
                                                  dw::Acc* sl) {
   if (RV) {
@@ -293,20 +396,45 @@ static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx,
 // Transpose gather (Euler) over the reverse adjacency, as k_rev_f64:
 // du_i = du_p_i - sum_j (Dx[j,i] s_x[j] + Dy[j,i] s_y[j]) - gamma sum_j lap[j,i] q[j],
 // with s = eps * t and q as double-word pairs.  PIPE and MINB as for k_fwd_euler_dw.
-template <bool RV, bool LAP, int PIPE, int MINB, bool PREF>
-__global__ void __launch_bounds__(kBlock, MINB) k_rev_euler_dw(RevArgs a) {
-  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+template <bool RV, bool LAP, int PIPE, int MINB, bool PREF, bool HALO>
+__global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_dw(RevArgs a) {
+  constexpr int BS = HALO ? kHaloRows : kBlock;
+  constexpr int NCH = (RV ? 4 : 0) + (LAP ? 2 : 0);
+  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;
+  const float* __restrict__ S = reinterpret_cast<const float*>(a.sdw);
+  const float* __restrict__ Q = reinterpret_cast<const float*>(a.qdw);
+  extern __shared__ float4 hsm[];
+  bool staged = false;
+  if (HALO && NCH > 0) {
+    const float4* S4 = reinterpret_cast<const float4*>(a.sdw);
+    const float4* Q4 = reinterpret_cast<const float4*>(a.qdw);
+    staged = stage_halo<NCH, BS>(a.ell, hsm, [&](int k, int64_t c) {
+      return (RV && k < 4) ? S4 + c * 4 + k : Q4 + c * 2 + (k - (RV ? 4 : 0));
+    });
+  }
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
-  const float* __restrict__ S = reinterpret_cast<const float*>(a.sdw);
-  const float* __restrict__ Q = reinterpret_cast<const float*>(a.qdw);
   const int32_t* __restrict__ col = a.ell.col;
   dw::Acc sx[4], sy[4], sl[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) { sx[v] = dw::zero(); sy[v] = dw::zero(); sl[v] = dw::zero(); }
-  if (PIPE == 0) {
+  const uint16_t* __restrict__ lcol = a.ell.lcol;
+  const int hs = a.ell.halo_stride;
+  if (HALO && staged && PIPE == 2) {
+#pragma unroll 2
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      rev_accum<RV, LAP>(rev_load_halo<RV, LAP>(a, hsm, hs, p, __ldg(lcol + p)), sx, sy, sl);
+    }
+  } else if (HALO && staged) {
+#pragma unroll 1
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      rev_accum<RV, LAP>(rev_load_halo<RV, LAP>(a, hsm, hs, p, __ldg(lcol + p)), sx, sy, sl);
+    }
+  } else if (PIPE == 0) {
 #pragma unroll 1
     for (int j = 0; j < len; ++j) {
       const int64_t p = base + ((int64_t)j << 5);
@@ -387,28 +515,63 @@ namespace {
 // Kernel variants: 0 = one entry per loop iteration (fewest registers, most resident
 // warps), 1 = two entries per iteration with the register count capped at six blocks per
 // SM, 2 = two entries per iteration uncapped, 3 = software pipeline, 4 = variant 1 with
-// the slice's streamed arrays prefetched into L2 ahead of use, 5 = variant 2 with it.
+// the slice's streamed arrays prefetched into L2 ahead of use, 5 = variant 2 with it,
+// 6 / 7 = neighbour records staged per row group in shared memory (one / two entries per
+// iteration, registers capped at three blocks of kHaloRows per SM), 8 = variant 7 capped
+// at four blocks.  Without halos
+// (not built) the staged variants run as variant 2.
+// A staged launch: kHaloRows threads per block, NCH chunks of the layout's longest list
+// in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
+// kernel and device).
+template <typename Args>
+void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStream_t s) {
+  const size_t smem = (size_t)nch * a.ell.halo_stride * sizeof(float4);
+  if (smem > 48 * 1024) {
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    int dev = 0;
+    MFT_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.insert({reinterpret_cast<const void*>(k), dev}).second)
+      MFT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(6 * kHaloMax * sizeof(float4))));
+  }
+  k<<<grid_for(n, kHaloRows), kHaloRows, smem, s>>>(a);
+}
+
 template <bool WT, bool WQ, int FLY>
-void fwd_variant(const FwdArgs& a, int variant, unsigned g, cudaStream_t s) {
+void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
+  const unsigned g = grid_for(n, kBlock);
+  constexpr int nch = (WT || WQ || FLY) ? 6 : 4;
+  if (variant >= 6 && !a.ell.halo_off) variant = 2;
   switch (variant) {
-    case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false><<<g, kBlock, 0, s>>>(a); break;
-    case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, false><<<g, kBlock, 0, s>>>(a); break;
-    case 3: k_fwd_euler_dw<WT, WQ, FLY, 1, 1, false><<<g, kBlock, 0, s>>>(a); break;
-    case 4: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, true><<<g, kBlock, 0, s>>>(a); break;
-    case 5: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, true><<<g, kBlock, 0, s>>>(a); break;
-    default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false><<<g, kBlock, 0, s>>>(a); break;
+    case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 3: k_fwd_euler_dw<WT, WQ, FLY, 1, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 4: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, true, false><<<g, kBlock, 0, s>>>(a); break;
+    case 5: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, true, false><<<g, kBlock, 0, s>>>(a); break;
+    case 6: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 0, 3, false, true>, a, nch, n, s); break;
+    case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true>, a, nch, n, s); break;
+    case 8: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 4, false, true>, a, nch, n, s); break;
+    default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
 
 template <bool RV, bool LAP>
-void rev_variant(const RevArgs& a, int variant, unsigned g, cudaStream_t s) {
+void rev_variant(const RevArgs& a, int variant, int64_t n, cudaStream_t s) {
+  const unsigned g = grid_for(n, kBlock);
+  constexpr int nch = (RV ? 4 : 0) + (LAP ? 2 : 0);
+  if (variant >= 6 && !a.ell.halo_off) variant = 2;
   switch (variant) {
-    case 1: k_rev_euler_dw<RV, LAP, 2, 6, false><<<g, kBlock, 0, s>>>(a); break;
-    case 2: k_rev_euler_dw<RV, LAP, 2, 1, false><<<g, kBlock, 0, s>>>(a); break;
-    case 3: k_rev_euler_dw<RV, LAP, 1, 1, false><<<g, kBlock, 0, s>>>(a); break;
-    case 4: k_rev_euler_dw<RV, LAP, 2, 6, true><<<g, kBlock, 0, s>>>(a); break;
-    case 5: k_rev_euler_dw<RV, LAP, 2, 1, true><<<g, kBlock, 0, s>>>(a); break;
-    default: k_rev_euler_dw<RV, LAP, 0, 1, false><<<g, kBlock, 0, s>>>(a); break;
+    case 1: k_rev_euler_dw<RV, LAP, 2, 6, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 2: k_rev_euler_dw<RV, LAP, 2, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 3: k_rev_euler_dw<RV, LAP, 1, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 4: k_rev_euler_dw<RV, LAP, 2, 6, true, false><<<g, kBlock, 0, s>>>(a); break;
+    case 5: k_rev_euler_dw<RV, LAP, 2, 1, true, false><<<g, kBlock, 0, s>>>(a); break;
+    case 6: launch_staged(k_rev_euler_dw<RV, LAP, 0, 3, false, true>, a, nch, n, s); break;
+    case 7: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, false, true>, a, nch, n, s); break;
+    case 8: launch_staged(k_rev_euler_dw<RV, LAP, 2, 4, false, true>, a, nch, n, s); break;
+    default: k_rev_euler_dw<RV, LAP, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
 
@@ -419,19 +582,19 @@ void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s) {
   MFT_REQUIRE(a.V == 4, MFT_ERR_UNSUPPORTED, "double-word gathers: 2D Euler only");
   MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
               "Flyer and Tominec hyperviscosity together are not supported");
-  const unsigned g = grid_for(a.n, kBlock);
+  const int64_t n = a.n;
   const bool wt = a.want_t != 0, wq = a.want_q != 0;
   if (a.flyer == 0) {
-    if (wt && wq) fwd_variant<true, true, 0>(a, variant, g, s);
-    else if (wt) fwd_variant<true, false, 0>(a, variant, g, s);
-    else if (wq) fwd_variant<false, true, 0>(a, variant, g, s);
-    else fwd_variant<false, false, 0>(a, variant, g, s);
+    if (wt && wq) fwd_variant<true, true, 0>(a, variant, n, s);
+    else if (wt) fwd_variant<true, false, 0>(a, variant, n, s);
+    else if (wq) fwd_variant<false, true, 0>(a, variant, n, s);
+    else fwd_variant<false, false, 0>(a, variant, n, s);
   } else if (a.flyer == 1) {
-    if (wt) fwd_variant<true, false, 1>(a, variant, g, s);
-    else fwd_variant<false, false, 1>(a, variant, g, s);
+    if (wt) fwd_variant<true, false, 1>(a, variant, n, s);
+    else fwd_variant<false, false, 1>(a, variant, n, s);
   } else {
-    if (wt) fwd_variant<true, false, 2>(a, variant, g, s);
-    else fwd_variant<false, false, 2>(a, variant, g, s);
+    if (wt) fwd_variant<true, false, 2>(a, variant, n, s);
+    else fwd_variant<false, false, 2>(a, variant, n, s);
   }
   MFT_LAUNCH_CHECK();
 }
@@ -439,11 +602,11 @@ void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s) {
 void launch_rev_dw(const RevArgs& a, int variant, cudaStream_t s) {
   if (a.n <= 0) return;
   MFT_REQUIRE(a.V == 4, MFT_ERR_UNSUPPORTED, "double-word gathers: 2D Euler only");
-  const unsigned g = grid_for(a.n, kBlock);
-  if (a.rv && a.lap) rev_variant<true, true>(a, variant, g, s);
-  else if (a.rv) rev_variant<true, false>(a, variant, g, s);
-  else if (a.lap) rev_variant<false, true>(a, variant, g, s);
-  else rev_variant<false, false>(a, variant, g, s);
+  const int64_t n = a.n;
+  if (a.rv && a.lap) rev_variant<true, true>(a, variant, n, s);
+  else if (a.rv) rev_variant<true, false>(a, variant, n, s);
+  else if (a.lap) rev_variant<false, true>(a, variant, n, s);
+  else rev_variant<false, false>(a, variant, n, s);
   MFT_LAUNCH_CHECK();
 }
 

@@ -74,12 +74,25 @@ constexpr int kSlice = 32;
 
 // Row r of the layout holds node perm[r]'s row (perm null: node r).  slice_off and
 // row_len are indexed by layout row; everything per node by perm[r].
+// Neighbour halos of row groups: for each group of kHaloRows consecutive layout rows, the
+// distinct nodes its rows gather (ascending), at most kHaloMax of them, and per ELL
+// element the element's position in its group's list.  A gather kernel stages a group's
+// neighbour records into shared memory once with coalesced copies and reads them from
+// there, instead of one scattered global load per element.  Groups with more distinct
+// neighbours have an empty list and gather directly.
+constexpr int kHaloRows = 256;
+constexpr int kHaloMax = 640;
+
 struct EllView {
   int64_t n;
   const int64_t* slice_off;
   const int32_t* row_len;
   const int32_t* col;
   const int32_t* perm;
+  const int32_t* halo_off;   // groups + 1 offsets into halo_col (null: no halos built)
+  const int32_t* halo_col;   // the groups' neighbour lists
+  const uint16_t* lcol;      // per ELL element: position in its group's list
+  int halo_stride;           // longest list (shared-memory stride of a staged chunk)
 };
 
 struct EllBuf {
@@ -91,8 +104,14 @@ struct EllBuf {
   DBuf<int32_t> row_len;
   DBuf<int32_t> col;
   DBuf<int32_t> perm;
+  DBuf<int32_t> halo_off, halo_col;
+  DBuf<uint16_t> lcol;
+  int64_t halo_groups = 0, halo_staged = 0;  // groups, and groups with a list
+  int halo_stride = 0;
   EllView view() const {
-    return EllView{n, slice_off.p, row_len.p, col.p, (window > 0 || ordered) ? perm.p : nullptr};
+    return EllView{n,         slice_off.p, row_len.p,
+                   col.p,     (window > 0 || ordered) ? perm.p : nullptr,
+                   halo_off.p, halo_col.p, lcol.p,    halo_stride};
   }
 };
 
@@ -245,7 +264,7 @@ void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s);
 // variant: 0..5, the kernel variants the autotuner chooses among (same sums, same order)
-constexpr int kDwVariants = 6;
+constexpr int kDwVariants = 9;
 void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s);
 void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 
