@@ -416,11 +416,16 @@ def run_weights(args, local):
                                      % (s2.size + s3.size)}}
 
 
+CURVE_POINTS = 16
+
+
 def run_riemann(args, local):
     """Four-quadrant Riemann problem on the unit square, periodic (N = side^2 jittered
     nodes), residual viscosity + Tominec hyperviscosity (c = 1), SSP-RK3 with dt = 0.1 h
-    to t = 0.2, in the FP64 form and the FP32-apply form: throughput of both and the FP32
-    density error at t = 0.2.  (With open edges, one-sided stencils grow unstable boundary
+    to t = 0.2, in the FP64 form and the FP32-apply form: throughput of both, the FP32
+    density error at t = 0.2, and the relative L2 density difference from the FP64 run at
+    16 times along the way for the FP32 form and for the FP64 form started from a
+    rounding-size perturbation of u0.  (With open edges, one-sided stencils grow unstable boundary
     modes at this resolution; the periodic square keeps the run bounded.)"""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
@@ -431,6 +436,8 @@ def run_riemann(args, local):
     nsteps = int(round(0.2 / dt))
     eq = M.CompressibleEulerEquations2D(1.4)
     out = {}
+    curves = {}
+    snaps = []
     # fp64p: the FP64 form from u0 perturbed by seeded relative noise of FP32 rounding size,
     # which measures how strongly this discontinuous flow amplifies such differences
     for prec in ("fp64", "fp32", "fp64p"):
@@ -452,12 +459,28 @@ def run_riemann(args, local):
         ctx.ssprk33(dt, 3, use_graph=True)          # warm-up (autotune, graph capture)
         ctx.history_init(3)
         ctx.set_state(u0, 0.0)
-        ctx.region_begin()
-        ctx.ssprk33(dt, nsteps, use_graph=True)
-        ms = ctx.region_end()
+        # the run in chunks (the same steps and times as one call), the density read back
+        # between chunks outside the timed regions: difference-versus-time curves
+        ms = 0.0
+        done = 0
+        curve = []
+        for ch in range(CURVE_POINTS):
+            k = (nsteps * (ch + 1)) // CURVE_POINTS - done
+            ctx.region_begin()
+            ctx.ssprk33(dt, k, use_graph=True)
+            ms += ctx.region_end()
+            done += k
+            uc, tc = ctx.get_state()
+            if prec == "fp64":
+                snaps.append(uc[0].copy())
+                curve.append(tc)
+            else:
+                ref = snaps[ch]
+                curve.append(float(np.linalg.norm(uc[0] - ref) / np.linalg.norm(ref)))
         u, t = ctx.get_state()
         ctx.close()
         out[prec] = (ms, u, t)
+        curves[prec] = curve
     ms64, u64, t64 = out["fp64"]
     ms32, u32, _ = out["fp32"]
     v64 = n * RHS_PER_STEP * nsteps / (ms64 * 1e-3)
@@ -480,7 +503,9 @@ def run_riemann(args, local):
                                                  / np.linalg.norm(u64[0])),
                 "linf_density_diff_vs_fp64": float(np.abs(out["fp64p"][1][0] - u64[0]).max()
                                                    / np.abs(u64[0]).max())},
-            "density_range_fp64": [float(u64[0].min()), float(u64[0].max())]}
+            "density_range_fp64": [float(u64[0].min()), float(u64[0].max())],
+            "l2_density_diff_vs_time": {"t": curves["fp64"], "fp32_apply": curves["fp32"],
+                                        "fp64_perturbed": curves["fp64p"]}}
 
 
 def run_igr(args, local):
