@@ -78,7 +78,7 @@ def parse():
                     choices=["all", "adjoint", "riemann", "weights", "igr", "fp32", "setup",
                              "rates", "dw", "dfma", "vortex"],
                     help="run one auxiliary measurement alone")
-    ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged"],
+    ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged", "halo"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
     ap.add_argument("--dw-variant", type=int, default=-1,
                     help="double-word gather kernel variant of the dw/dfma measurements "
@@ -839,7 +839,8 @@ def run_fp32(args, local, peaks):
     semi, dom, u0, dt, n = build_problem(args.workload, args.side, "fp32", local)
     ctx = dom.ctx
     ctx.set_option(L.OPT_GATHER, {"auto": L.GATHER_AUTO, "thread": L.GATHER_THREAD,
-                                  "staged": L.GATHER_STAGED}[args.gather])
+                                  "staged": L.GATHER_STAGED,
+                                  "halo": L.GATHER_HALO}[args.gather])
     ms, prof, _, _, ms_prof = timed_steps(ctx, u0, dt, args.warmup, args.steps, None)
     out = {"value": n * RHS_PER_STEP * args.steps / (ms * 1e-3), "unit": UNIT,
            "ms_per_step": ms / args.steps, "gather": args.gather,

@@ -215,7 +215,9 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
 /* Engine options.  MFT_OPT_GATHER selects the mapping of the FP32 operator gathers:
  * MFT_GATHER_THREAD (one node per thread, direct loads), MFT_GATHER_STAGED (one warp
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
- * bulk copies), or MFT_GATHER_AUTO (default; staged for the FP32 Euler form). */
+ * bulk copies), MFT_GATHER_HALO (one node per thread, each group of 256 layout rows
+ * staging its distinct neighbour records in shared memory first), or MFT_GATHER_AUTO
+ * (default: the autotuner times the three on the live inputs). */
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
        MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8 };
@@ -232,7 +234,8 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
  * staged in shared memory by coalesced asynchronous copies and read from there (16-bit
  * positions instead of the 32-bit indices; a group with more than 640 distinct
  * neighbours gathers directly; registers capped at three blocks per SM), 8 = 7 capped at
- * four blocks per SM;
+ * four blocks per SM, 9 and 11 = staged with four and three entries per iteration, 10 = 7
+ * with the streamed position and weight arrays prefetched into L2 as in 4;
  * -1 (default) lets the autotuner time them at the first launch of each configuration.
  * Every variant forms the same sums in the same order (bit-identical results).
  * MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV then report the variant in use. */
@@ -240,7 +243,7 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
  * curve of the node coordinates, so that a warp's 32 rows are a compact patch whose
  * neighbours overlap; 0 keeps node order.  Results are identical either way (every row
  * keeps its own summation order); only the memory locality of the gathers changes. */
-enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2 };
+enum { MFT_GATHER_AUTO = 0, MFT_GATHER_THREAD = 1, MFT_GATHER_STAGED = 2, MFT_GATHER_HALO = 3 };
 /* MFT_OPT_FP64_ARITH: how the FP64 form's operator gathers form their sums of products.
  * MFT_ARITH_DFMA: FP64 fused multiply-adds.  MFT_ARITH_DW: double-word FP32 arithmetic
  * (weights, fluxes and neighbour states as unevaluated float pairs h + l, error-free

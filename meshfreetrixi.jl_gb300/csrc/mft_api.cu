@@ -420,8 +420,10 @@ void ensure_device_ops(mft_ctx* c) {
   // double-word operator values are placed only while that form is in use
   const bool dw = use_dw(c);
   if (dw && !c->fwdw[0].p) c->dev_dirty = true;
-  // neighbour halos of the row groups, for the double-word gathers' staged variants
-  if (dw && !c->fwd.halo_off.p) c->dev_dirty = true;
+  // neighbour halos of the row groups, for the staged gathers (double-word and FP32
+  // Euler forms)
+  const bool halo = dw || (c->precision == MFT_PREC_FP32 && c->eq == MFT_EQ_EULER2D);
+  if (halo && !c->fwd.halo_off.p) c->dev_dirty = true;
   if (!c->dev_dirty) return;
   c->graph_valid = false;
   cudaStream_t s = c->stream;
@@ -431,10 +433,10 @@ void ensure_device_ops(mft_ctx* c) {
     zorder = morton_order(c->dim, c->n, c->xyz,
                           c->nseg > 0 ? c->seg_off : std::vector<int64_t>{});
   const std::vector<int32_t>* base = spatial ? &zorder : nullptr;
-  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, dw);
+  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, halo);
   c->fwd_pos.upload(pos, s);
   std::vector<int64_t> rpos_csc;
-  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, dw);
+  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, halo);
   std::vector<int64_t> rpos(rpos_csc.size());
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < (int64_t)rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
@@ -531,14 +533,16 @@ static void refresh_dirichlet(mft_ctx* c, double t) {
 
 // ---------------------------------------------------------------- gather autotuner
 //
-// The FP32 Euler gathers have three mappings: one node per thread with direct loads
-// (choice 0) and one warp per 32-row slice with the slice's indices/weights staged in
-// shared memory by bulk copies, 4 or 8 slots per copy (choices 4, 8).  With
+// The FP32 Euler gathers have four mappings: one node per thread with direct loads
+// (choice 0), one node per thread with each 256-row group's neighbour records staged in
+// shared memory (choice 1, mft_halo.cuh), and one warp per 32-row slice with the slice's
+// indices/weights staged in shared memory by bulk copies, 4 or 8 slots per copy (choices
+// 4, 8).  With
 // MFT_GATHER_AUTO the first launch of each kernel configuration times every mapping on
 // the live inputs (CUDA events, best of 3 after a warm-up) and keeps the fastest for this
 // context until the operators change.
 
-static const int kGatherChoices[3] = {0, 4, 8};
+static const int kGatherChoices[4] = {0, 1, 4, 8};
 
 // Times launch(choice) for every choice (a warm-up launch, then the best of 3 CUDA-event
 // timed launches) and returns the fastest choice.
@@ -574,28 +578,41 @@ static int tune_choices(mft_ctx* c, const int* choices, int nchoice, Launch&& la
 
 template <class Launch>
 static int tune_gather(mft_ctx* c, Launch&& launch) {
-  return tune_choices(c, kGatherChoices, 3, launch);
+  return tune_choices(c, kGatherChoices, 4, launch);
 }
 
 template <class Launch>
 static int tune_variants(mft_ctx* c, int nvariants, Launch&& launch) {
-  int choices[8];
-  for (int k = 0; k < nvariants && k < 8; ++k) choices[k] = k;
-  return tune_choices(c, choices, nvariants, launch);
+  constexpr int kMax = 16;
+  static_assert(kDwVariants <= kMax, "tuner choice table");
+  int choices[kMax];
+  const int nv = std::min(nvariants, kMax);
+  for (int k = 0; k < nv; ++k) choices[k] = k;
+  return tune_choices(c, choices, nv, launch);
+}
+
+static void launch_fwd_f32_choice(mft_ctx* c, const FwdArgs& a, int ch) {
+  if (ch == 1 && launch_fwd_f32_halo(a, c->stream)) return;
+  if (ch > 1 && launch_fwd_f32_tma(a, ch, c->kerr.p, c->stream)) return;
+  launch_fwd_f32(a, c->stream);
+}
+
+static void launch_rev_f32_choice(mft_ctx* c, const RevArgs& a, int ch) {
+  if (ch == 1 && launch_rev_f32_halo(a, c->stream)) return;
+  if (ch > 1 && launch_rev_f32_tma(a, ch, c->kerr.p, c->stream)) return;
+  launch_rev_f32(a, c->stream);
 }
 
 static int fwd_choice(mft_ctx* c, const FwdArgs& a) {
   if (a.V != 4) return 0;
   if (c->gather_mode == MFT_GATHER_THREAD) return 0;
   if (c->gather_mode == MFT_GATHER_STAGED) return 8;
+  if (c->gather_mode == MFT_GATHER_HALO) return 1;
   const int key = (a.want_t ? 1 : 0) + (a.want_q ? 2 : 0) + 4 * a.flyer;
   if (c->tuned_fwd[key] < 0) {
     FwdArgs probe = a;
     probe.final_epilogue = 0;  // timing launches write only scratch outputs
-    c->tuned_fwd[key] = tune_gather(c, [&](int ch) {
-      if (ch == 0 || !launch_fwd_f32_tma(probe, ch, c->kerr.p, c->stream))
-        launch_fwd_f32(probe, c->stream);
-    });
+    c->tuned_fwd[key] = tune_gather(c, [&](int ch) { launch_fwd_f32_choice(c, probe, ch); });
   }
   return c->tuned_fwd[key];
 }
@@ -604,15 +621,13 @@ static int rev_choice(mft_ctx* c, const RevArgs& a) {
   if (a.V != 4) return 0;
   if (c->gather_mode == MFT_GATHER_THREAD) return 0;
   if (c->gather_mode == MFT_GATHER_STAGED) return 8;
+  if (c->gather_mode == MFT_GATHER_HALO) return 1;
   const int key = (a.rv ? 1 : 0) + (a.lap ? 2 : 0);
   if (c->tuned_rev[key] < 0) {
     RevArgs probe = a;
     probe.final_epilogue = 0;
     probe.du_p_out32 = c->du_p2_32.p == a.du_p32 ? c->work_du32.p : c->du_p2_32.p;
-    c->tuned_rev[key] = tune_gather(c, [&](int ch) {
-      if (ch == 0 || !launch_rev_f32_tma(probe, ch, c->kerr.p, c->stream))
-        launch_rev_f32(probe, c->stream);
-    });
+    c->tuned_rev[key] = tune_gather(c, [&](int ch) { launch_rev_f32_choice(c, probe, ch); });
   }
   return c->tuned_rev[key];
 }
@@ -654,8 +669,7 @@ void launch_fwd(mft_ctx* c, const FwdArgs& a) {
   if (c->precision == MFT_PREC_FP32) {
     const int ch = fwd_choice(c, a);
     c->last_fwd_choice = ch;
-    if (ch > 0 && launch_fwd_f32_tma(a, ch, c->kerr.p, c->stream)) return;
-    launch_fwd_f32(a, c->stream);
+    launch_fwd_f32_choice(c, a, ch);
   } else if (use_dw(c)) {
     const int v = dw_fwd_choice(c, a);
     c->last_fwd_choice = v;
@@ -668,8 +682,7 @@ void launch_rev(mft_ctx* c, const RevArgs& a) {
   if (c->precision == MFT_PREC_FP32) {
     const int ch = rev_choice(c, a);
     c->last_rev_choice = ch;
-    if (ch > 0 && launch_rev_f32_tma(a, ch, c->kerr.p, c->stream)) return;
-    launch_rev_f32(a, c->stream);
+    launch_rev_f32_choice(c, a, ch);
   } else if (use_dw(c)) {
     const int v = dw_rev_choice(c, a);
     c->last_rev_choice = v;
@@ -1446,7 +1459,7 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
   return guarded(c, [&] {
     c->graph_valid = false;
     if (option == MFT_OPT_GATHER) {
-      MFT_REQUIRE(value >= MFT_GATHER_AUTO && value <= MFT_GATHER_STAGED, MFT_ERR_ARG,
+      MFT_REQUIRE(value >= MFT_GATHER_AUTO && value <= MFT_GATHER_HALO, MFT_ERR_ARG,
                   "unknown gather mapping");
       c->gather_mode = value;
       c->fsal_valid = false;

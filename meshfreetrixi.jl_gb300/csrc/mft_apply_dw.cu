@@ -17,6 +17,7 @@
 #include "mft_device.cuh"
 #include "mft_dw.cuh"
 #include "mft_eps.cuh"
+#include "mft_halo.cuh"
 #include "mft_internal.cuh"
 #include "mft_tma.cuh"
 
@@ -53,37 +54,6 @@ static __device__ __forceinline__ void prefetch_chunk(const SliceArrays& sa, int
 }
 static __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
-// 16-byte asynchronous copy global -> shared (bypasses registers), and the wait for all
-// of this thread's copies.
-static __device__ __forceinline__ void cp_async16(float4* smem, const float4* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-static __device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
-
-// Stages the neighbour records of this block's row group (the group's halo list) into
-// shared memory: NCH 16-byte chunks per record, chunk k of list entry q at
-// sm[k * ell.halo_stride + q] (chunk-major, so that lanes reading one chunk of different
-// records spread over the banks).  chunk(k, c) is the address of chunk k of node c's
-// record.  Consecutive threads copy consecutive chunks of one record, so each record
-// arrives in whole sectors.  Returns false (nothing staged) when the group has no list.
-// Every thread of the block must call it (it ends with a block barrier).
-template <int NCH, int BS, typename Chunk>
-static __device__ __forceinline__ bool stage_halo(const EllView& ell, float4* sm, Chunk chunk) {
-  const int h0 = __ldg(ell.halo_off + blockIdx.x);
-  const int nh = __ldg(ell.halo_off + blockIdx.x + 1) - h0;
-  if (nh <= 0) return false;  // block-uniform
-  for (int q = threadIdx.x; q < nh * NCH; q += BS) {
-    const int rec = q / NCH, k = q - rec * NCH;
-    cp_async16(sm + k * ell.halo_stride + rec,
-               chunk(k, (int64_t)__ldg(ell.halo_col + h0 + rec)));
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  return true;
-}
 
 // Per node: the state as double-word pairs and the Euler flux pair evaluated from them in
 // double-word arithmetic (the textbook flux, one reciprocal for both velocities; each
@@ -220,15 +190,25 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
   }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (HALO && staged && PIPE == 2) {
-#pragma unroll 2
-    for (int j = 0; j < len; ++j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      fwd_accum<WT, WQ, FLY>(fwd_load_halo<WT, WQ, FLY>(a, hsm, hs, p, __ldg(lcol + p)), f, tx, ty, q);
+  if (HALO && staged) {
+    SliceArrays sa{};
+    int64_t s_lo = 0, s_hi = 0;
+    const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
+    if (pf_lane) {
+      sa.arr[0] = lcol; sa.esize[0] = 2;
+      sa.arr[1] = a.wdw[0]; sa.esize[1] = 8;
+      sa.arr[2] = a.wdw[1]; sa.esize[2] = 8;
+      sa.arr[3] = a.wldw; sa.esize[3] = 8;
+      sa.narr = (WQ || FLY) ? 4 : 3;
+      s_lo = a.ell.slice_off[r >> 5];
+      s_hi = a.ell.slice_off[(r >> 5) + 1];
+      prefetch_chunk(sa, s_lo, s_hi, 0);
+      prefetch_chunk(sa, s_lo, s_hi, 1);
     }
-  } else if (HALO && staged) {
-#pragma unroll 1
+    constexpr int UNR = PIPE < 1 ? 1 : PIPE;
+#pragma unroll UNR
     for (int j = 0; j < len; ++j) {
+      if (pf_lane && (j % kPfSlots) == 0) prefetch_chunk(sa, s_lo, s_hi, j / kPfSlots + 2);
       const int64_t p = base + ((int64_t)j << 5);
       fwd_accum<WT, WQ, FLY>(fwd_load_halo<WT, WQ, FLY>(a, hsm, hs, p, __ldg(lcol + p)), f, tx, ty, q);
     }
@@ -239,7 +219,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
       const int64_t c = __ldg(col + p);
       fwd_accum<WT, WQ, FLY>(fwd_load<WT, WQ, FLY>(a, F, U, p, c), f, tx, ty, q);
     }
-  } else if (PIPE == 2) {
+  } else if (PIPE == 2 || (HALO && PIPE > 2)) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -422,15 +402,25 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
   for (int v = 0; v < 4; ++v) { sx[v] = dw::zero(); sy[v] = dw::zero(); sl[v] = dw::zero(); }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (HALO && staged && PIPE == 2) {
-#pragma unroll 2
-    for (int j = 0; j < len; ++j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      rev_accum<RV, LAP>(rev_load_halo<RV, LAP>(a, hsm, hs, p, __ldg(lcol + p)), sx, sy, sl);
+  if (HALO && staged) {
+    SliceArrays sa{};
+    int64_t s_lo = 0, s_hi = 0;
+    const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
+    if (pf_lane) {
+      int k = 0;
+      sa.arr[k] = lcol; sa.esize[k++] = 2;
+      if (RV) { sa.arr[k] = a.wdw[0]; sa.esize[k++] = 8; sa.arr[k] = a.wdw[1]; sa.esize[k++] = 8; }
+      if (LAP) { sa.arr[k] = a.wldw; sa.esize[k++] = 8; }
+      sa.narr = k;
+      s_lo = a.ell.slice_off[r >> 5];
+      s_hi = a.ell.slice_off[(r >> 5) + 1];
+      prefetch_chunk(sa, s_lo, s_hi, 0);
+      prefetch_chunk(sa, s_lo, s_hi, 1);
     }
-  } else if (HALO && staged) {
-#pragma unroll 1
+    constexpr int UNR = PIPE < 1 ? 1 : PIPE;
+#pragma unroll UNR
     for (int j = 0; j < len; ++j) {
+      if (pf_lane && (j % kPfSlots) == 0) prefetch_chunk(sa, s_lo, s_hi, j / kPfSlots + 2);
       const int64_t p = base + ((int64_t)j << 5);
       rev_accum<RV, LAP>(rev_load_halo<RV, LAP>(a, hsm, hs, p, __ldg(lcol + p)), sx, sy, sl);
     }
@@ -441,7 +431,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
       const int64_t c = __ldg(col + p);
       rev_accum<RV, LAP>(rev_load<RV, LAP>(a, S, Q, p, c), sx, sy, sl);
     }
-  } else if (PIPE == 2) {
+  } else if (PIPE == 2 || (HALO && PIPE > 2)) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -518,7 +508,8 @@ namespace {
 // the slice's streamed arrays prefetched into L2 ahead of use, 5 = variant 2 with it,
 // 6 / 7 = neighbour records staged per row group in shared memory (one / two entries per
 // iteration, registers capped at three blocks of kHaloRows per SM), 8 = variant 7 capped
-// at four blocks.  Without halos
+// at four blocks, 9 / 11 = staged with four / three entries per iteration, 10 = variant 7
+// with the streamed position and weight arrays prefetched into L2 (as variant 4).  Without halos
 // (not built) the staged variants run as variant 2.
 // A staged launch: kHaloRows threads per block, NCH chunks of the layout's longest list
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
@@ -553,6 +544,9 @@ void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 6: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 0, 3, false, true>, a, nch, n, s); break;
     case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true>, a, nch, n, s); break;
     case 8: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 4, false, true>, a, nch, n, s); break;
+    case 9: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 4, 3, false, true>, a, nch, n, s); break;
+    case 10: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, true, true>, a, nch, n, s); break;
+    case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true>, a, nch, n, s); break;
     default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
@@ -571,6 +565,9 @@ void rev_variant(const RevArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 6: launch_staged(k_rev_euler_dw<RV, LAP, 0, 3, false, true>, a, nch, n, s); break;
     case 7: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, false, true>, a, nch, n, s); break;
     case 8: launch_staged(k_rev_euler_dw<RV, LAP, 2, 4, false, true>, a, nch, n, s); break;
+    case 9: launch_staged(k_rev_euler_dw<RV, LAP, 4, 3, false, true>, a, nch, n, s); break;
+    case 10: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, true, true>, a, nch, n, s); break;
+    case 11: launch_staged(k_rev_euler_dw<RV, LAP, 3, 3, false, true>, a, nch, n, s); break;
     default: k_rev_euler_dw<RV, LAP, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }

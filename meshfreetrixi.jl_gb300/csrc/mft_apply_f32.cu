@@ -6,6 +6,7 @@
 #include <math.h>
 
 #include "mft_device.cuh"
+#include "mft_halo.cuh"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -14,31 +15,48 @@ namespace {
 
 using namespace dev;
 
-template <bool WT, bool WQ, int FLY>
-__global__ void __launch_bounds__(kBlock) k_fwd_euler_f32(FwdArgs a) {
-  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+// HALO: one block per row group (kHaloRows rows) first stages the group's neighbour
+// states in shared memory (mft_halo.cuh) and reads them from there; groups without a list
+// load them directly.  The sums are the same in the same order either way.
+template <bool WT, bool WQ, int FLY, bool HALO = false>
+__global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_fwd_euler_f32(FwdArgs a) {
+  constexpr int BS = HALO ? kHaloRows : kBlock;
+  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
+  extern __shared__ float4 hsm[];
+  bool staged = false;
+  if (HALO) staged = stage_halo<1, BS>(a.ell, hsm, [&](int, int64_t c) { return U4 + c; });
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
+  const uint16_t* __restrict__ lcol = a.ell.lcol;
   const float* __restrict__ wxp = a.w32[0];
   const float* __restrict__ wyp = a.w32[1];
   const float* __restrict__ wlp = a.wl32;
-  const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
   const float gm1 = a.gm1_32;
   float f[4] = {0, 0, 0, 0}, tx[4] = {0, 0, 0, 0}, ty[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
-#pragma unroll 4
-  for (int j = 0; j < len; ++j) {
-    const int64_t p = base + ((int64_t)j << 5);
-    const int c = __ldg(col + p);
+  auto entry = [&](int64_t p, const float4 uc) {
     const float wx = __ldg(wxp + p), wy = __ldg(wyp + p);
-    const float4 uc = __ldg(U4 + c);
     euler_accum_f32<WT>(gm1, uc, wx, wy, f, tx, ty);
     if (WQ || FLY) {
       const float wl = __ldg(wlp + p);
       q[0] = fmaf(wl, uc.x, q[0]); q[1] = fmaf(wl, uc.y, q[1]);
       q[2] = fmaf(wl, uc.z, q[2]); q[3] = fmaf(wl, uc.w, q[3]);
+    }
+  };
+  if (HALO && staged) {
+#pragma unroll 4
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      entry(p, hsm[__ldg(lcol + p)]);
+    }
+  } else {
+#pragma unroll 4
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      entry(p, __ldg(U4 + __ldg(col + p)));
     }
   }
   const float hg = a.hg32;
@@ -181,25 +199,47 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
   }
 }
 
-template <int V, bool RV, bool LAP>
-__global__ void __launch_bounds__(kBlock) k_rev_f32(RevArgs a) {
-  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+// HALO (V = 4 only): staged neighbour records as in k_fwd_euler_f32 -- s = eps t (two
+// chunks) and q (one chunk).
+template <int V, bool RV, bool LAP, bool HALO = false>
+__global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_rev_f32(RevArgs a) {
+  static_assert(!HALO || V == 4, "staged transpose gather: 2D Euler");
+  constexpr int BS = HALO ? kHaloRows : kBlock;
+  constexpr int NCH = (RV ? 2 : 0) + (LAP ? 1 : 0);
+  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  extern __shared__ float4 hsm[];
+  bool staged = false;
+  if (HALO && NCH > 0) {
+    const float4* S4 = reinterpret_cast<const float4*>(a.s32);
+    const float4* Q4 = reinterpret_cast<const float4*>(a.q32);
+    staged = stage_halo<NCH, BS>(a.ell, hsm, [&](int k, int64_t c) {
+      return (RV && k < 2) ? S4 + c * 2 + k : Q4 + c;
+    });
+  }
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
+  const int hs = a.ell.halo_stride;
   float sx[V], sy[V], sl[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) { sx[v] = 0.f; sy[v] = 0.f; sl[v] = 0.f; }
 #pragma unroll 4
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
-    const int c = __ldg(a.ell.col + p);
+    const int c = (HALO && staged) ? (int)__ldg(a.ell.lcol + p) : __ldg(a.ell.col + p);
     if (RV) {
       const float wx = __ldg(a.w32[0] + p), wy = __ldg(a.w32[1] + p);
       if (V == 4) {
-        const F8 st = ldg_f8(a.s32 + (int64_t)c * 8);
-        const float4 xs = st.lo, ys = st.hi;
+        float4 xs, ys;
+        if (HALO && staged) {
+          xs = hsm[c];
+          ys = hsm[hs + c];
+        } else {
+          const F8 st = ldg_f8(a.s32 + (int64_t)c * 8);
+          xs = st.lo;
+          ys = st.hi;
+        }
         sx[0] = fmaf(wx, xs.x, sx[0]); sx[1] = fmaf(wx, xs.y, sx[1]);
         sx[2] = fmaf(wx, xs.z, sx[2]); sx[3] = fmaf(wx, xs.w, sx[3]);
         sy[0] = fmaf(wy, ys.x, sy[0]); sy[1] = fmaf(wy, ys.y, sy[1]);
@@ -213,7 +253,9 @@ __global__ void __launch_bounds__(kBlock) k_rev_f32(RevArgs a) {
     if (LAP) {
       const float wl = __ldg(a.wl32 + p);
       if (V == 4) {
-        const float4 qq = __ldg(reinterpret_cast<const float4*>(a.q32) + c);
+        const float4 qq = (HALO && staged)
+                              ? hsm[(RV ? 2 : 0) * hs + c]
+                              : __ldg(reinterpret_cast<const float4*>(a.q32) + c);
         sl[0] = fmaf(wl, qq.x, sl[0]); sl[1] = fmaf(wl, qq.y, sl[1]);
         sl[2] = fmaf(wl, qq.z, sl[2]); sl[3] = fmaf(wl, qq.w, sl[3]);
       } else {
@@ -278,6 +320,35 @@ void launch_fwd_f32(const FwdArgs& args, cudaStream_t s) {
   MFT_LAUNCH_CHECK();
 }
 
+bool launch_fwd_f32_halo(const FwdArgs& args, cudaStream_t s) {
+  if (args.n <= 0) return true;
+  if (args.V != 4 || !args.ell.halo_off) return false;
+  FwdArgs a = args;
+  a.gm1_32 = (float)(a.gamma - 1.0);
+  a.hg32 = (float)a.hv_gamma;
+  MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
+              "Flyer and Tominec hyperviscosity together are not supported");
+  const unsigned g = grid_for(a.n, kHaloRows);
+  const size_t smem = (size_t)a.ell.halo_stride * sizeof(float4);
+  const bool wt = a.want_t != 0, wq = a.want_q != 0;
+#define MFT_FWD32H(WT, WQ, FLY) k_fwd_euler_f32<WT, WQ, FLY, true><<<g, kHaloRows, smem, s>>>(a)
+  if (a.flyer == 0) {
+    if (wt && wq) MFT_FWD32H(true, true, 0);
+    else if (wt) MFT_FWD32H(true, false, 0);
+    else if (wq) MFT_FWD32H(false, true, 0);
+    else MFT_FWD32H(false, false, 0);
+  } else if (a.flyer == 1) {
+    if (wt) MFT_FWD32H(true, false, 1);
+    else MFT_FWD32H(false, false, 1);
+  } else {
+    if (wt) MFT_FWD32H(true, false, 2);
+    else MFT_FWD32H(false, false, 2);
+  }
+#undef MFT_FWD32H
+  MFT_LAUNCH_CHECK();
+  return true;
+}
+
 void launch_eps_f32(const EpsArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
   if (a.V == 4) k_eps_f32<4><<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
@@ -302,6 +373,21 @@ void launch_rev_f32(const RevArgs& args, cudaStream_t s) {
     else k_rev_f32<1, false, false><<<g, kBlock, 0, s>>>(a);
   }
   MFT_LAUNCH_CHECK();
+}
+
+bool launch_rev_f32_halo(const RevArgs& args, cudaStream_t s) {
+  if (args.n <= 0) return true;
+  if (args.V != 4 || !args.ell.halo_off) return false;
+  RevArgs a = args;
+  a.hg32 = (float)a.hv_gamma;
+  const unsigned g = grid_for(a.n, kHaloRows);
+  const size_t smem = (size_t)3 * a.ell.halo_stride * sizeof(float4);
+  if (a.rv && a.lap) k_rev_f32<4, true, true, true><<<g, kHaloRows, smem, s>>>(a);
+  else if (a.rv) k_rev_f32<4, true, false, true><<<g, kHaloRows, smem, s>>>(a);
+  else if (a.lap) k_rev_f32<4, false, true, true><<<g, kHaloRows, smem, s>>>(a);
+  else k_rev_f32<4, false, false, true><<<g, kHaloRows, smem, s>>>(a);
+  MFT_LAUNCH_CHECK();
+  return true;
 }
 
 }  // namespace mft

@@ -1,0 +1,45 @@
+// Shared-memory staging of a row group's neighbour records (the halos of EllView): used by
+// the staged variants of the gathers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mft_internal.cuh"
+
+namespace mft {
+namespace {
+
+// 16-byte asynchronous copy global -> shared (bypasses registers), and the wait for all
+// of this thread's copies.
+static __device__ __forceinline__ void cp_async16(float4* smem, const float4* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+static __device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Stages the neighbour records of this block's row group (the group's halo list) into
+// shared memory: NCH 16-byte chunks per record, chunk k of list entry q at
+// sm[k * ell.halo_stride + q] (chunk-major, so that lanes reading one chunk of different
+// records spread over the banks).  chunk(k, c) is the address of chunk k of node c's
+// record.  Consecutive threads copy consecutive chunks of one record, so each record
+// arrives in whole sectors.  Returns false (nothing staged) when the group has no list.
+// Every thread of the block must call it (it ends with a block barrier).
+template <int NCH, int BS, typename Chunk>
+__device__ __forceinline__ bool stage_halo(const EllView& ell, float4* sm, Chunk chunk) {
+  const int h0 = __ldg(ell.halo_off + blockIdx.x);
+  const int nh = __ldg(ell.halo_off + blockIdx.x + 1) - h0;
+  if (nh <= 0) return false;  // block-uniform
+  for (int q = threadIdx.x; q < nh * NCH; q += BS) {
+    const int rec = q / NCH, k = q - rec * NCH;
+    cp_async16(sm + k * ell.halo_stride + rec,
+               chunk(k, (int64_t)__ldg(ell.halo_col + h0 + rec)));
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  return true;
+}
+
+}  // namespace
+}  // namespace mft

@@ -264,7 +264,7 @@ void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s);
 // variant: 0..5, the kernel variants the autotuner chooses among (same sums, same order)
-constexpr int kDwVariants = 9;
+constexpr int kDwVariants = 12;
 void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s);
 void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 
@@ -316,6 +316,9 @@ void launch_rev_dw(const RevArgs& a, int variant, cudaStream_t s);
 void launch_rev_f32(const RevArgs& a, cudaStream_t s);
 // Bulk-copy-staged FP32 gathers (Euler); return false when the case is not covered.
 // chunk: slots staged per bulk copy (4 or 8).
+// The staged (halo) FP32 gathers: false when the layout has no halos or V != 4.
+bool launch_fwd_f32_halo(const FwdArgs& a, cudaStream_t s);
+bool launch_rev_f32_halo(const RevArgs& a, cudaStream_t s);
 bool launch_fwd_f32_tma(const FwdArgs& a, int chunk, int* err, cudaStream_t s);
 bool launch_rev_f32_tma(const RevArgs& a, int chunk, int* err, cudaStream_t s);
 // One warp's bounded wait on an mbarrier that nothing completes (error-path self-test).

@@ -26,7 +26,7 @@ OPT_GATHER, OPT_TUNED_FWD, OPT_TUNED_REV, OPT_FP64_ARITH, OPT_LAYOUT_ORDER = 0, 
 OPT_DW_VARIANT = 5
 OPT_HALO_STAGED_FWD, OPT_HALO_STAGED_REV, OPT_HALO_GROUPS = 6, 7, 8
 ARITH_AUTO, ARITH_DFMA, ARITH_DW = 0, 1, 2
-GATHER_AUTO, GATHER_THREAD, GATHER_STAGED = 0, 1, 2
+GATHER_AUTO, GATHER_THREAD, GATHER_STAGED, GATHER_HALO = 0, 1, 2, 3
 
 # Every entry point of include/meshfree_gb300.h with (restype, argtypes).
 VP = C.c_void_p

@@ -1,6 +1,7 @@
-"""FP32-apply form: the bulk-copy-staged gathers against the one-node-per-thread
-gathers (same operations in the same order, so bit-identical), and against the FP64
-oracle (condition-scaled error within FP32 rounding)."""
+"""FP32-apply form: the bulk-copy-staged gathers and the halo-staged gathers (neighbour
+records of each 256-row group in shared memory) against the one-node-per-thread gathers
+(same operations in the same order, so bit-identical), and against the FP64 oracle
+(condition-scaled error within FP32 rounding)."""
 import numpy as np
 import pytest
 
@@ -19,14 +20,15 @@ def test_fp32_staged_equals_thread_and_tracks_fp64(oracle, gpu_lib, cyl, cyl_ops
     semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, case)
     ctx.set_precision(L.PREC_FP32)
     out = {}
-    for mode in (L.GATHER_THREAD, L.GATHER_STAGED, L.GATHER_AUTO):
+    for mode in (L.GATHER_THREAD, L.GATHER_STAGED, L.GATHER_HALO, L.GATHER_AUTO):
         ctx.set_option(L.OPT_GATHER, mode)
         du = np.empty_like(u0)
         u = u0.copy()
         ctx.rhs(du, u, 0.0)
         out[mode] = (du, u)
-    assert ctx.get_option(L.OPT_TUNED_FWD) in (0, 4, 8)
-    for mode in (L.GATHER_STAGED, L.GATHER_AUTO):
+    assert ctx.get_option(L.OPT_TUNED_FWD) in (0, 1, 4, 8)
+    assert ctx.get_option(L.OPT_HALO_STAGED_FWD) > 0
+    for mode in (L.GATHER_STAGED, L.GATHER_HALO, L.GATHER_AUTO):
         assert np.array_equal(out[L.GATHER_THREAD][0], out[mode][0])
         assert np.array_equal(out[L.GATHER_THREAD][1], out[mode][1])
     u_ref = u0.copy()
@@ -57,11 +59,13 @@ def test_fp32_staged_equals_thread_large(gpu_lib):
     ctx = domain.ctx
     u0 = semi.compute_coefficients(0.0)
     res = {}
-    for mode in (L.GATHER_THREAD, L.GATHER_STAGED, L.GATHER_AUTO):
+    for mode in (L.GATHER_THREAD, L.GATHER_STAGED, L.GATHER_HALO, L.GATHER_AUTO):
         ctx.set_option(L.OPT_GATHER, mode)
         ctx.history_init(3)
         ctx.set_state(u0, 0.0)
         ctx.ssprk33(0.2 * h, 4)
         res[mode] = ctx.get_state()[0]
     assert np.array_equal(res[L.GATHER_THREAD], res[L.GATHER_STAGED])
+    assert np.array_equal(res[L.GATHER_THREAD], res[L.GATHER_HALO])
     assert np.array_equal(res[L.GATHER_THREAD], res[L.GATHER_AUTO])
+    assert ctx.get_option(L.OPT_HALO_STAGED_FWD) == ctx.get_option(L.OPT_HALO_GROUPS)
