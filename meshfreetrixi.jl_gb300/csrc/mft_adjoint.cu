@@ -9,6 +9,7 @@
 // at the gathering node and with the SSP-RK3 adjoint stage combination.
 #include "mft_device.cuh"
 #include "mft_dw.cuh"
+#include "mft_halo.cuh"
 
 namespace mft {
 namespace {
@@ -169,23 +170,39 @@ __global__ void k_lam_pairs(int64_t n, const double* __restrict__ lam, BcDev bc,
 // The adjoint gather of 2D Euler in double-word FP32 arithmetic (as the forward form's
 // gathers; the sums over the reverse adjacency in pairs, the node part in FP64).  HV 0
 // (no hyperviscosity) or 2 (Flyer, whose term gathers the same M2 lam).
-template <bool BC, int HV>
-__global__ void __launch_bounds__(kBlock) k_adj_dw(AdjArgs a) {
-  const int64_t row = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+// HALO: blocks of one row group stage the group's neighbour cotangent pairs in shared
+// memory first (mft_halo.cuh); same sums, same order.
+template <bool BC, int HV, bool HALO>
+__global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_adj_dw(AdjArgs a) {
+  constexpr int BS = HALO ? kHaloRows : kBlock;
+  const int64_t row = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const float* __restrict__ L = reinterpret_cast<const float*>(a.lamdw);
+  extern __shared__ float4 hsm[];
+  bool staged = false;
+  if (HALO) {
+    const float4* L4 = reinterpret_cast<const float4*>(a.lamdw);
+    staged = stage_halo<2, BS>(a.ell, hsm, [&](int k, int64_t c) { return L4 + c * 2 + k; });
+  }
   if (row >= a.n) return;
   const int64_t i = ell_node(a.ell, row);
   const int64_t base = a.ell.slice_off[row >> 5] + (row & 31);
   const int len = a.ell.row_len[row];
-  const float* __restrict__ L = reinterpret_cast<const float*>(a.lamdw);
+  const int hs = a.ell.halo_stride;
   dw::Acc gx[4], gy[4], gh[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) { gx[v] = dw::zero(); gy[v] = dw::zero(); gh[v] = dw::zero(); }
 #pragma unroll 2
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
-    const int64_t c = __ldg(a.ell.col + p);
     const float2 wx = __ldg(a.wdw[0] + p), wy = __ldg(a.wdw[1] + p);
-    const F8 ll = ldg_f8(L + c * 8);
+    F8 ll;
+    if (HALO && staged) {
+      const int lc = __ldg(a.ell.lcol + p);
+      ll.lo = hsm[lc];
+      ll.hi = hsm[hs + lc];
+    } else {
+      ll = ldg_f8(L + (int64_t)__ldg(a.ell.col + p) * 8);
+    }
     const float2 l[4] = {make_float2(ll.lo.x, ll.lo.y), make_float2(ll.lo.z, ll.lo.w),
                          make_float2(ll.hi.x, ll.hi.y), make_float2(ll.hi.z, ll.hi.w)};
 #pragma unroll
@@ -272,7 +289,7 @@ void launch_adj_f64(const AdjArgs& a, cudaStream_t s) {
   MFT_LAUNCH_CHECK();
 }
 
-void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, cudaStream_t s) {
+void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, bool staged, cudaStream_t s) {
   if (a.n <= 0) return;
   MFT_REQUIRE(a.V == 4 && a.eq == MFT_EQ_EULER2D && a.hv != 1, MFT_ERR_UNSUPPORTED,
               "double-word adjoint gather: 2D Euler without Tominec hyperviscosity");
@@ -282,13 +299,25 @@ void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, cudaStream_t s) {
   MFT_LAUNCH_CHECK();
   AdjArgs b = a;
   b.lamdw = lam_pairs;
-  const unsigned g = grid_for(a.n, kBlock);
-  if (a.has_bc) {
-    if (a.hv == 2) k_adj_dw<true, 2><<<g, kBlock, 0, s>>>(b);
-    else k_adj_dw<true, 0><<<g, kBlock, 0, s>>>(b);
+  if (staged && a.ell.halo_off) {
+    const unsigned g = grid_for(a.n, kHaloRows);
+    const size_t smem = (size_t)2 * a.ell.halo_stride * sizeof(float4);
+    if (a.has_bc) {
+      if (a.hv == 2) k_adj_dw<true, 2, true><<<g, kHaloRows, smem, s>>>(b);
+      else k_adj_dw<true, 0, true><<<g, kHaloRows, smem, s>>>(b);
+    } else {
+      if (a.hv == 2) k_adj_dw<false, 2, true><<<g, kHaloRows, smem, s>>>(b);
+      else k_adj_dw<false, 0, true><<<g, kHaloRows, smem, s>>>(b);
+    }
   } else {
-    if (a.hv == 2) k_adj_dw<false, 2><<<g, kBlock, 0, s>>>(b);
-    else k_adj_dw<false, 0><<<g, kBlock, 0, s>>>(b);
+    const unsigned g = grid_for(a.n, kBlock);
+    if (a.has_bc) {
+      if (a.hv == 2) k_adj_dw<true, 2, false><<<g, kBlock, 0, s>>>(b);
+      else k_adj_dw<true, 0, false><<<g, kBlock, 0, s>>>(b);
+    } else {
+      if (a.hv == 2) k_adj_dw<false, 2, false><<<g, kBlock, 0, s>>>(b);
+      else k_adj_dw<false, 0, false><<<g, kBlock, 0, s>>>(b);
+    }
   }
   MFT_LAUNCH_CHECK();
 }

@@ -2416,7 +2416,10 @@ void eval_rhs_adjoint(mft_ctx* c, const double* u, const double* lam, int kind, 
     a.wdw[1] = c->rwdw[1].p;
     a.whdw = hv == 2 ? c->rwdw[kSlotHv].p : nullptr;
     c->adj_lamdw.alloc((size_t)c->n * 4);
-    launch_adj_dw(a, c->adj_lamdw.p, s);
+    // staged unless a fixed direct variant of the double-word gathers is requested
+    const bool staged = !(c->dw_variant >= 0 && c->dw_variant < 6);
+    a.ell = c->rev.view();
+    launch_adj_dw(a, c->adj_lamdw.p, staged, s);
   } else {
     launch_adj_f64(a, s);
   }

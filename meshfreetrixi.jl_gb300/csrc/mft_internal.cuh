@@ -357,8 +357,9 @@ struct AdjArgs {
   const float2* lamdw;  // M2 lam as pairs (set by launch_adj_dw)
 };
 void launch_adj_f64(const AdjArgs& a, cudaStream_t s);
-// The same product with the sums in double-word arithmetic; lam_pairs: n x 4 pair scratch.
-void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, cudaStream_t s);
+// The same product with the sums in double-word arithmetic; lam_pairs: n x 4 pair scratch;
+// staged: each row group's neighbour pairs staged in shared memory (when halos exist).
+void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, bool staged, cudaStream_t s);
 // q_i = sum_j lap[i,j] (M2 lam)_j over the forward layout (Tominec adjoint).
 void launch_lap_masked(int64_t n, EllView fwd, const double* wl, const double* lam, int V,
                        BcDev bc, int has_bc, double* q, cudaStream_t s);

@@ -96,6 +96,22 @@ def test_rhs_adjoint_euler_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, case):
     assert np.all(err <= TOL), err
 
 
+@pytest.mark.parametrize("case", ["plain", "flyer"])
+def test_rhs_adjoint_staged_equals_direct(oracle, gpu_lib, cyl, cyl_ops, case):
+    """The double-word adjoint gather with each row group's cotangent pairs staged in
+    shared memory (default) and read directly (a direct variant forced): bit-identical."""
+    from meshfree_gb300 import _lib as L
+    semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, case, arith="dw")
+    u = ic_bumpy(cyl["positions"])
+    lam = np.random.default_rng(2).standard_normal(u.shape)
+    staged = ctx.rhs_adjoint(lam, u)
+    assert ctx.get_option(L.OPT_HALO_STAGED_REV) > 0
+    ctx.set_option(L.OPT_DW_VARIANT, 2)
+    direct = ctx.rhs_adjoint(lam, u)
+    assert np.array_equal(staged, direct)
+    ctx.close()
+
+
 def test_rhs_adjoint_advection_matches_oracle(oracle, gpu_lib, cyl, cyl_ops):
     semi, ctx, hv, g = _setup(oracle, gpu_lib, cyl, cyl_ops, "tominec", eq="advection")
     x = cyl["positions"]
