@@ -174,14 +174,13 @@ __global__ void k_lam_pairs(int64_t n, const double* __restrict__ lam, BcDev bc,
 // memory first (mft_halo.cuh); same sums, same order.
 template <bool BC, int HV, bool HALO>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_adj_dw(AdjArgs a) {
-  constexpr int BS = HALO ? kHaloRows : kBlock;
-  const int64_t row = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const int64_t row = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float* __restrict__ L = reinterpret_cast<const float*>(a.lamdw);
   extern __shared__ float4 hsm[];
   bool staged = false;
   if (HALO) {
     const float4* L4 = reinterpret_cast<const float4*>(a.lamdw);
-    staged = stage_halo<2, BS>(a.ell, hsm, [&](int k, int64_t c) { return L4 + c * 2 + k; });
+    staged = stage_halo<2>(a.ell, hsm, [&](int k, int64_t c) { return L4 + c * 2 + k; });
   }
   if (row >= a.n) return;
   const int64_t i = ell_node(a.ell, row);
@@ -300,14 +299,15 @@ void launch_adj_dw(const AdjArgs& a, float2* lam_pairs, bool staged, cudaStream_
   AdjArgs b = a;
   b.lamdw = lam_pairs;
   if (staged && a.ell.halo_off) {
-    const unsigned g = grid_for(a.n, kHaloRows);
+    const int rows = a.ell.halo_rows;
+    const unsigned g = grid_for(a.n, rows);
     const size_t smem = (size_t)2 * a.ell.halo_stride * sizeof(float4);
     if (a.has_bc) {
-      if (a.hv == 2) k_adj_dw<true, 2, true><<<g, kHaloRows, smem, s>>>(b);
-      else k_adj_dw<true, 0, true><<<g, kHaloRows, smem, s>>>(b);
+      if (a.hv == 2) k_adj_dw<true, 2, true><<<g, rows, smem, s>>>(b);
+      else k_adj_dw<true, 0, true><<<g, rows, smem, s>>>(b);
     } else {
-      if (a.hv == 2) k_adj_dw<false, 2, true><<<g, kHaloRows, smem, s>>>(b);
-      else k_adj_dw<false, 0, true><<<g, kHaloRows, smem, s>>>(b);
+      if (a.hv == 2) k_adj_dw<false, 2, true><<<g, rows, smem, s>>>(b);
+      else k_adj_dw<false, 0, true><<<g, rows, smem, s>>>(b);
     }
   } else {
     const unsigned g = grid_for(a.n, kBlock);

@@ -49,11 +49,11 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 // then ordered by length, longest first, inside each run of `window` consecutive rows
 // (stable, so rows stay near their neighbours): the 32 rows of a slice then have nearly
 // equal lengths and the lanes of a warp finish together.
-// With halo, the neighbour halos of the row groups are built too (kHaloRows rows each:
-// distinct columns ascending, and each element's position among them).
+// With halo_rows > 0, the neighbour halos of the row groups are built too (halo_rows rows
+// each: distinct columns ascending, and each element's position among them).
 void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& cols,
                EllBuf& ell, std::vector<int64_t>& pos, cudaStream_t s, int window = 0,
-               const std::vector<int32_t>* base = nullptr, bool halo = false) {
+               const std::vector<int32_t>* base = nullptr, int halo_rows = 0) {
   std::vector<int32_t> order(n);
   if (base) order = *base;
   else std::iota(order.begin(), order.end(), 0);
@@ -115,22 +115,24 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   ell.col.upload(col, s);
   if (window > 0 || base) ell.perm.upload(order, s);
   else ell.perm.release();
-  if (!halo) {
+  if (halo_rows <= 0) {
     ell.halo_off.release();
     ell.halo_col.release();
     ell.lcol.release();
     ell.halo_groups = ell.halo_staged = 0;
     ell.halo_stride = 0;
+    ell.halo_rows = 0;
     return;
   }
-  static_assert(kHaloRows % kSlice == 0, "halo groups are whole slices");
-  const int64_t ng = (n + kHaloRows - 1) / kHaloRows;
+  MFT_REQUIRE(halo_rows % kSlice == 0 && halo_rows <= kHaloRows, MFT_ERR_STATE,
+              "halo groups must be whole slices of at most kHaloRows rows");
+  const int64_t ng = (n + halo_rows - 1) / halo_rows;
   std::vector<std::vector<int32_t>> lists(ng);
   std::vector<uint16_t> lcol(ne, 0);
 #pragma omp parallel for schedule(dynamic, 16)
   for (int64_t g = 0; g < ng; ++g) {
     std::vector<int32_t>& h = lists[g];
-    const int64_t r0 = g * kHaloRows, r1 = std::min<int64_t>(n, r0 + kHaloRows);
+    const int64_t r0 = g * halo_rows, r1 = std::min<int64_t>(n, r0 + halo_rows);
     for (int64_t r = r0; r < r1; ++r) {
       const int64_t node = order[r];
       h.insert(h.end(), cols.begin() + rowptr[node], cols.begin() + rowptr[node] + rlen[r]);
@@ -167,6 +169,7 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   ell.halo_groups = ng;
   ell.halo_staged = staged;
   ell.halo_stride = stride;
+  ell.halo_rows = halo_rows;
   // the host vectors leave scope before the copies are done
   MFT_CUDA(cudaStreamSynchronize(s));
 }
@@ -424,6 +427,11 @@ void ensure_device_ops(mft_ctx* c) {
   // Euler forms)
   const bool halo = dw || (c->precision == MFT_PREC_FP32 && c->eq == MFT_EQ_EULER2D);
   if (halo && !c->fwd.halo_off.p) c->dev_dirty = true;
+  // 256-row groups when that still gives every SM several blocks, else 128
+  int nsm = 0;
+  MFT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+  const int halo_rows = !halo ? 0 : (c->n / kHaloRows >= 4 * (int64_t)nsm ? kHaloRows : kHaloRows / 2);
+  if (halo && c->fwd.halo_rows != halo_rows) c->dev_dirty = true;
   if (!c->dev_dirty) return;
   c->graph_valid = false;
   cudaStream_t s = c->stream;
@@ -433,10 +441,10 @@ void ensure_device_ops(mft_ctx* c) {
     zorder = morton_order(c->dim, c->n, c->xyz,
                           c->nseg > 0 ? c->seg_off : std::vector<int64_t>{});
   const std::vector<int32_t>* base = spatial ? &zorder : nullptr;
-  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, halo);
+  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, halo_rows);
   c->fwd_pos.upload(pos, s);
   std::vector<int64_t> rpos_csc;
-  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, halo);
+  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, halo_rows);
   std::vector<int64_t> rpos(rpos_csc.size());
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < (int64_t)rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];

@@ -161,13 +161,12 @@ static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, 
 // accumulated (the gathers are latency-bound: most samples stall on their results).
 // MINB: minimum resident blocks per SM requested from the compiler (register cap).
 // The variants form the same sums in the same order; the autotuner picks one.
-// HALO: blocks of kHaloRows rows (one row group) first stage the group's neighbour
+// HALO: blocks of one row group (ell.halo_rows rows) first stage the group's neighbour
 // records in shared memory and read them from there (groups without a list gather
 // directly); PIPE 0 or 2 then sets the loop's unrolling.
 template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
-  constexpr int BS = HALO ? kHaloRows : kBlock;
-  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
   const float* __restrict__ U = reinterpret_cast<const float*>(a.udw);
   extern __shared__ float4 hsm[];
@@ -175,7 +174,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
   if (HALO) {
     const float4* F4 = reinterpret_cast<const float4*>(a.Fdw);
     const float4* U4 = reinterpret_cast<const float4*>(a.udw);
-    staged = stage_halo<(WT || WQ || FLY) ? 6 : 4, BS>(
+    staged = stage_halo<(WT || WQ || FLY) ? 6 : 4>(
         a.ell, hsm, [&](int k, int64_t c) { return k < 4 ? F4 + c * 4 + k : U4 + c * 2 + (k - 4); });
   }
   if (r >= a.n) return;
@@ -378,9 +377,8 @@ static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx,
 // with s = eps * t and q as double-word pairs.  PIPE and MINB as for k_fwd_euler_dw.
 template <bool RV, bool LAP, int PIPE, int MINB, bool PREF, bool HALO>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_dw(RevArgs a) {
-  constexpr int BS = HALO ? kHaloRows : kBlock;
   constexpr int NCH = (RV ? 4 : 0) + (LAP ? 2 : 0);
-  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;
+  const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float* __restrict__ S = reinterpret_cast<const float*>(a.sdw);
   const float* __restrict__ Q = reinterpret_cast<const float*>(a.qdw);
   extern __shared__ float4 hsm[];
@@ -388,7 +386,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
   if (HALO && NCH > 0) {
     const float4* S4 = reinterpret_cast<const float4*>(a.sdw);
     const float4* Q4 = reinterpret_cast<const float4*>(a.qdw);
-    staged = stage_halo<NCH, BS>(a.ell, hsm, [&](int k, int64_t c) {
+    staged = stage_halo<NCH>(a.ell, hsm, [&](int k, int64_t c) {
       return (RV && k < 4) ? S4 + c * 4 + k : Q4 + c * 2 + (k - (RV ? 4 : 0));
     });
   }
@@ -511,7 +509,7 @@ namespace {
 // at four blocks, 9 / 11 = staged with four / three entries per iteration, 10 = variant 7
 // with the streamed position and weight arrays prefetched into L2 (as variant 4).  Without halos
 // (not built) the staged variants run as variant 2.
-// A staged launch: kHaloRows threads per block, NCH chunks of the layout's longest list
+// A staged launch: one block per row group, NCH chunks of the layout's longest list
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
 // kernel and device).
 template <typename Args>
@@ -527,7 +525,8 @@ void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStrea
       MFT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(6 * kHaloMax * sizeof(float4))));
   }
-  k<<<grid_for(n, kHaloRows), kHaloRows, smem, s>>>(a);
+  const int rows = a.ell.halo_rows;
+  k<<<grid_for(n, rows), rows, smem, s>>>(a);
 }
 
 template <bool WT, bool WQ, int FLY>

@@ -15,17 +15,16 @@ namespace {
 
 using namespace dev;
 
-// HALO: one block per row group (kHaloRows rows) first stages the group's neighbour
+// HALO: one block per row group (ell.halo_rows rows) first stages the group's neighbour
 // states in shared memory (mft_halo.cuh) and reads them from there; groups without a list
 // load them directly.  The sums are the same in the same order either way.
 template <bool WT, bool WQ, int FLY, bool HALO = false>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_fwd_euler_f32(FwdArgs a) {
-  constexpr int BS = HALO ? kHaloRows : kBlock;
-  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float4* __restrict__ U4 = reinterpret_cast<const float4*>(a.u32);
   extern __shared__ float4 hsm[];
   bool staged = false;
-  if (HALO) staged = stage_halo<1, BS>(a.ell, hsm, [&](int, int64_t c) { return U4 + c; });
+  if (HALO) staged = stage_halo<1>(a.ell, hsm, [&](int, int64_t c) { return U4 + c; });
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
@@ -204,15 +203,14 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
 template <int V, bool RV, bool LAP, bool HALO = false>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_rev_f32(RevArgs a) {
   static_assert(!HALO || V == 4, "staged transpose gather: 2D Euler");
-  constexpr int BS = HALO ? kHaloRows : kBlock;
   constexpr int NCH = (RV ? 2 : 0) + (LAP ? 1 : 0);
-  const int64_t r = blockIdx.x * (int64_t)BS + threadIdx.x;  // layout row
+  const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   extern __shared__ float4 hsm[];
   bool staged = false;
   if (HALO && NCH > 0) {
     const float4* S4 = reinterpret_cast<const float4*>(a.s32);
     const float4* Q4 = reinterpret_cast<const float4*>(a.q32);
-    staged = stage_halo<NCH, BS>(a.ell, hsm, [&](int k, int64_t c) {
+    staged = stage_halo<NCH>(a.ell, hsm, [&](int k, int64_t c) {
       return (RV && k < 2) ? S4 + c * 2 + k : Q4 + c;
     });
   }
@@ -328,10 +326,11 @@ bool launch_fwd_f32_halo(const FwdArgs& args, cudaStream_t s) {
   a.hg32 = (float)a.hv_gamma;
   MFT_REQUIRE(!(a.flyer && a.want_q), MFT_ERR_UNSUPPORTED,
               "Flyer and Tominec hyperviscosity together are not supported");
-  const unsigned g = grid_for(a.n, kHaloRows);
+  const int rows = a.ell.halo_rows;
+  const unsigned g = grid_for(a.n, rows);
   const size_t smem = (size_t)a.ell.halo_stride * sizeof(float4);
   const bool wt = a.want_t != 0, wq = a.want_q != 0;
-#define MFT_FWD32H(WT, WQ, FLY) k_fwd_euler_f32<WT, WQ, FLY, true><<<g, kHaloRows, smem, s>>>(a)
+#define MFT_FWD32H(WT, WQ, FLY) k_fwd_euler_f32<WT, WQ, FLY, true><<<g, rows, smem, s>>>(a)
   if (a.flyer == 0) {
     if (wt && wq) MFT_FWD32H(true, true, 0);
     else if (wt) MFT_FWD32H(true, false, 0);
@@ -380,12 +379,13 @@ bool launch_rev_f32_halo(const RevArgs& args, cudaStream_t s) {
   if (args.V != 4 || !args.ell.halo_off) return false;
   RevArgs a = args;
   a.hg32 = (float)a.hv_gamma;
-  const unsigned g = grid_for(a.n, kHaloRows);
+  const int rows = a.ell.halo_rows;
+  const unsigned g = grid_for(a.n, rows);
   const size_t smem = (size_t)3 * a.ell.halo_stride * sizeof(float4);
-  if (a.rv && a.lap) k_rev_f32<4, true, true, true><<<g, kHaloRows, smem, s>>>(a);
-  else if (a.rv) k_rev_f32<4, true, false, true><<<g, kHaloRows, smem, s>>>(a);
-  else if (a.lap) k_rev_f32<4, false, true, true><<<g, kHaloRows, smem, s>>>(a);
-  else k_rev_f32<4, false, false, true><<<g, kHaloRows, smem, s>>>(a);
+  if (a.rv && a.lap) k_rev_f32<4, true, true, true><<<g, rows, smem, s>>>(a);
+  else if (a.rv) k_rev_f32<4, true, false, true><<<g, rows, smem, s>>>(a);
+  else if (a.lap) k_rev_f32<4, false, true, true><<<g, rows, smem, s>>>(a);
+  else k_rev_f32<4, false, false, true><<<g, rows, smem, s>>>(a);
   MFT_LAUNCH_CHECK();
   return true;
 }

@@ -25,13 +25,14 @@ static __device__ __forceinline__ void cp_async_wait_all() {
 // records spread over the banks).  chunk(k, c) is the address of chunk k of node c's
 // record.  Consecutive threads copy consecutive chunks of one record, so each record
 // arrives in whole sectors.  Returns false (nothing staged) when the group has no list.
-// Every thread of the block must call it (it ends with a block barrier).
-template <int NCH, int BS, typename Chunk>
+// Every thread of the block must call it (it ends with a block barrier); the block is one
+// group (blockDim.x = ell.halo_rows).
+template <int NCH, typename Chunk>
 __device__ __forceinline__ bool stage_halo(const EllView& ell, float4* sm, Chunk chunk) {
   const int h0 = __ldg(ell.halo_off + blockIdx.x);
   const int nh = __ldg(ell.halo_off + blockIdx.x + 1) - h0;
   if (nh <= 0) return false;  // block-uniform
-  for (int q = threadIdx.x; q < nh * NCH; q += BS) {
+  for (int q = threadIdx.x; q < nh * NCH; q += blockDim.x) {
     const int rec = q / NCH, k = q - rec * NCH;
     cp_async16(sm + k * ell.halo_stride + rec,
                chunk(k, (int64_t)__ldg(ell.halo_col + h0 + rec)));

@@ -74,13 +74,14 @@ constexpr int kSlice = 32;
 
 // Row r of the layout holds node perm[r]'s row (perm null: node r).  slice_off and
 // row_len are indexed by layout row; everything per node by perm[r].
-// Neighbour halos of row groups: for each group of kHaloRows consecutive layout rows, the
+// Neighbour halos of row groups: for each group of halo_rows consecutive layout rows (256,
+// or 128 when 256-row groups would leave SMs idle), the
 // distinct nodes its rows gather (ascending), at most kHaloMax of them, and per ELL
 // element the element's position in its group's list.  A gather kernel stages a group's
 // neighbour records into shared memory once with coalesced copies and reads them from
 // there, instead of one scattered global load per element.  Groups with more distinct
 // neighbours have an empty list and gather directly.
-constexpr int kHaloRows = 256;
+constexpr int kHaloRows = 256;  // largest group (and block) size
 constexpr int kHaloMax = 640;
 
 struct EllView {
@@ -93,6 +94,7 @@ struct EllView {
   const int32_t* halo_col;   // the groups' neighbour lists
   const uint16_t* lcol;      // per ELL element: position in its group's list
   int halo_stride;           // longest list (shared-memory stride of a staged chunk)
+  int halo_rows;             // rows per group (= threads per block of a staged launch)
 };
 
 struct EllBuf {
@@ -108,10 +110,11 @@ struct EllBuf {
   DBuf<uint16_t> lcol;
   int64_t halo_groups = 0, halo_staged = 0;  // groups, and groups with a list
   int halo_stride = 0;
+  int halo_rows = 0;
   EllView view() const {
     return EllView{n,         slice_off.p, row_len.p,
                    col.p,     (window > 0 || ordered) ? perm.p : nullptr,
-                   halo_off.p, halo_col.p, lcol.p,    halo_stride};
+                   halo_off.p, halo_col.p, lcol.p,    halo_stride, halo_rows};
   }
 };
 
