@@ -555,6 +555,9 @@ def run_adjoint(args, local, peaks):
     semi = M.SemidiscretizationHyperbolic(dom, M.CompressibleEulerEquations2D(1.4),
                                           lambda x, t, e: W.isentropic_vortex(x, t), solver)
     ctx = dom.ctx
+    if args.dw_variant >= 0:
+        from meshfree_gb300 import _lib as L
+        ctx.set_option(L.OPT_DW_VARIANT, args.dw_variant)
     u0 = semi.compute_coefficients(0.0)
     rng = np.random.default_rng(20)
     target = W.isentropic_vortex(pts, T)[0] + 1e-3 * rng.standard_normal(n)
