@@ -90,6 +90,8 @@ def parse():
                     help="stencils of the batched-weights measurement (0 skips it)")
     ap.add_argument("--riemann-side", type=int, default=1024,
                     help="nodes per side of the Riemann FP32/FP64 run to t = 0.2 (0 skips it)")
+    ap.add_argument("--igr-arith", default="both", choices=["both", "dw", "dfma"],
+                    help="gather arithmetic(s) of the IGR measurement")
     ap.add_argument("--vortex-side", type=int, default=512,
                     help="nodes per side of the vortex measurement (0 skips it)")
     ap.add_argument("--adj-steps", type=int, default=500,
@@ -513,30 +515,42 @@ def run_igr(args, local):
     rhs! evaluation): SSP-RK3 steps with graphs, against the same steps without it."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
+    from meshfree_gb300 import _lib as L
     pts, per, h = W.vortex_cloud(args.vortex_side or SIDES["vortex"])
     n = pts.shape[0]
-    basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
-    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64"))
-    dom = M.PointCloudDomain(solver, pts, period=per)
     eq = M.CompressibleEulerEquations2D(1.4)
     ic = lambda x, t, e: W.isentropic_vortex(x, t)
-    out = {}
-    for name, src in (("plain", M.SourceTerms()),
-                      ("igr", M.SourceTerms(igr=M.SourceIGR(solver, eq, dom, alpha=h * h)))):
-        semi = M.SemidiscretizationHyperbolic(dom, eq, ic, solver, source_terms=src)
-        u0 = semi.compute_coefficients(0.0)
-        ctx = dom.ctx
-        ctx.set_state(u0, 0.0)
-        ctx.ssprk33(DT_FACTOR["vortex"] * h, 2, use_graph=True)
-        ctx.set_state(u0, 0.0)
-        ctx.region_begin()
-        ctx.ssprk33(DT_FACTOR["vortex"] * h, args.steps, use_graph=True)
-        out[name] = ctx.region_end() / args.steps
-    ctx.close()
-    return {"workload": "isentropic vortex N=%d, k=%d, SourceIGR alpha=h^2, <= 20 CG iterations "
-                        "per rhs!, SSP-RK3 graphs" % (n, K_STENCIL),
-            "ms_per_step": out["igr"], "ms_per_step_without_igr": out["plain"],
-            "igr_ms_per_rhs": (out["igr"] - out["plain"]) / RHS_PER_STEP}
+    res = {}
+    for arith in (("dw", "dfma") if args.igr_arith == "both" else (args.igr_arith,)):
+        basis = M.PointCloudBasis(M.Point2D(), 3, nv=K_STENCIL)
+        solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64",
+                                                               fp64_arith=arith))
+        dom = M.PointCloudDomain(solver, pts, period=per)
+        out = {}
+        for name, src in (("plain", M.SourceTerms()),
+                          ("igr", M.SourceTerms(igr=M.SourceIGR(solver, eq, dom, alpha=h * h)))):
+            semi = M.SemidiscretizationHyperbolic(dom, eq, ic, solver, source_terms=src)
+            u0 = semi.compute_coefficients(0.0)
+            ctx = dom.ctx
+            ctx.set_state(u0, 0.0)
+            ctx.ssprk33(DT_FACTOR["vortex"] * h, 2, use_graph=True)
+            ctx.set_state(u0, 0.0)
+            ctx.region_begin()
+            ctx.ssprk33(DT_FACTOR["vortex"] * h, args.steps, use_graph=True)
+            out[name] = ctx.region_end() / args.steps
+        iters = ctx.get_option(L.OPT_IGR_ITERS)
+        ctx.close()
+        res[arith] = {"ms_per_step": out["igr"], "ms_per_step_without_igr": out["plain"],
+                      "igr_ms_per_rhs": (out["igr"] - out["plain"]) / RHS_PER_STEP,
+                      "cg_iterations_last_solve": iters}
+    first = next(iter(res))
+    out = {"workload": "isentropic vortex N=%d, k=%d, SourceIGR alpha=h^2, <= 20 CG iterations "
+                       "per rhs!, SSP-RK3 graphs" % (n, K_STENCIL),
+           "fp64_gather_arithmetic": first}
+    out.update(res[first])
+    if "dfma" in res and first != "dfma":
+        out["fp64_fma_gathers"] = res["dfma"]
+    return out
 
 
 def run_adjoint(args, local, peaks):

@@ -220,7 +220,10 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
  * (default: the autotuner times the three on the live inputs). */
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
-       MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8 };
+       MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8,
+       MFT_OPT_IGR_ITERS = 9 };
+/* Read-only MFT_OPT_IGR_ITERS: conjugate-gradient iterations of the last IGR solve
+ * (-1 before the first). */
 /* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups (256 layout rows each) of
  * the double-word form's layouts, MFT_OPT_HALO_STAGED_FWD / _REV = how many of them have
  * their neighbour records staged in shared memory by DW variants 6-8 (the others gather

@@ -1533,6 +1533,17 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_HALO_STAGED_FWD) *value = (int)c->fwd.halo_staged;
     else if (option == MFT_OPT_HALO_STAGED_REV) *value = (int)c->rev.halo_staged;
     else if (option == MFT_OPT_HALO_GROUPS) *value = (int)c->fwd.halo_groups;
+    else if (option == MFT_OPT_IGR_ITERS) {
+      // CG iterations of the last IGR solve (-1: none yet)
+      *value = -1;
+      if (c->igr_sc.p) {
+        set_device(c);
+        IgrScalars sc{};
+        MFT_CUDA(cudaStreamSynchronize(c->stream));
+        MFT_CUDA(cudaMemcpy(&sc, c->igr_sc.p, sizeof(sc), cudaMemcpyDeviceToHost));
+        *value = sc.iter;
+      }
+    }
     else throw mft::Error(MFT_ERR_ARG, "unknown option");
   });
 }
