@@ -735,12 +735,6 @@ static void ensure_igr(mft_ctx* c) {
     c->igr_counter.zero(c->stream);
   }
   c->igr_sc.alloc(1);
-  if (use_dw(c)) {
-    c->igr_primdw.alloc(n * 3);
-    c->igr_undw.alloc(n);
-    c->igr_tdw.alloc(n * 2);
-    c->igr_xdw.alloc(n);
-  }
 }
 
 void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_in) {
@@ -857,15 +851,6 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ia.partial = c->igr_partial.p;
     ia.counter = c->igr_counter.p;
     ia.sc = c->igr_sc.p;
-    ia.dw = dw ? 1 : 0;
-    if (dw) {
-      ia.wxdw = c->fwdw[0].p;
-      ia.wydw = c->fwdw[1].p;
-      ia.primdw = c->igr_primdw.p;
-      ia.undw = c->igr_undw.p;
-      ia.tdw = c->igr_tdw.p;
-      ia.xdw = c->igr_xdw.p;
-    }
     {
       NvtxRange rng("source terms");
       ProfScope ps(c, MFT_K_IGR);

@@ -135,7 +135,6 @@ struct mft_ctx {
       igr_partial;
   mft::DBuf<unsigned> igr_counter;
   mft::DBuf<mft::IgrScalars> igr_sc;
-  mft::DBuf<float2> igr_primdw, igr_undw, igr_tdw, igr_xdw;
 
   // Zhang-Shu positivity limiter after every SSP-RK3 stage (variables in order)
   int lim_n = 0;

@@ -11,14 +11,9 @@
 // device memory; once converged, the remaining kernels return at entry, so one rhs!
 // evaluation is a fixed launch sequence that a CUDA graph can hold.  Reductions are
 // block partials finished by the last block in a fixed order (deterministic).
-// In the FP64 form with double-word gathers (DW) the four operator gathers form their sums
-// in double-word FP32 arithmetic (mft_dw.cuh) from pair copies of the weights and of the
-// gathered node values, which the producing kernels write beside their FP64 outputs; the
-// per-node arithmetic and the CG scalars stay FP64.
 #include <cfloat>
 
 #include "mft_device.cuh"
-#include "mft_dw.cuh"
 
 namespace mft {
 namespace {
@@ -72,25 +67,17 @@ __device__ bool last_block_total(double x, double* partial, unsigned* counter, d
 }
 
 // prim = (rho, v1, v2), rinv = 1 / rho
-__global__ void k_igr_prim(int64_t n, const double* __restrict__ u, double* prim, double* rinv,
-                           float2* primdw) {
+__global__ void k_igr_prim(int64_t n, const double* __restrict__ u, double* prim, double* rinv) {
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= n) return;
   const double rho = u[i * 4], m1 = u[i * 4 + 1], m2 = u[i * 4 + 2];
-  const double v1 = ddiv(m1, rho), v2 = ddiv(m2, rho);
   prim[i * 3] = rho;
-  prim[i * 3 + 1] = v1;
-  prim[i * 3 + 2] = v2;
+  prim[i * 3 + 1] = ddiv(m1, rho);
+  prim[i * 3 + 2] = ddiv(m2, rho);
   rinv[i] = ddiv(1.0, rho);
-  if (primdw) {
-    primdw[i * 3] = dw::split(rho);
-    primdw[i * 3 + 1] = dw::split(v1);
-    primdw[i * 3 + 2] = dw::split(v2);
-  }
 }
 
 // b, x = 0, r = b, u_old = 0 and the initial residual norm.
-template <bool DW>
 __global__ void __launch_bounds__(kBlock) k_igr_rhs(IgrArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
   double rr = 0.0;
@@ -99,37 +86,16 @@ __global__ void __launch_bounds__(kBlock) k_igr_rhs(IgrArgs a) {
     const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
     const int len = a.ell.row_len[r];
     double dxr = 0, dxv1 = 0, dxv2 = 0, dyv1 = 0, dyv2 = 0;
-    if (DW) {
-      dw::Acc s[5] = {dw::zero(), dw::zero(), dw::zero(), dw::zero(), dw::zero()};
-#pragma unroll 2
-      for (int j = 0; j < len; ++j) {
-        const int64_t p = base + ((int64_t)j << 5);
-        const int64_t c = __ldg(a.ell.col + p);
-        const float2 wx = __ldg(a.wxdw + p), wy = __ldg(a.wydw + p);
-        const float2 rc = a.primdw[c * 3], v1 = a.primdw[c * 3 + 1], v2 = a.primdw[c * 3 + 2];
-        dw::fma_acc(s[0], wx, rc);
-        dw::fma_acc(s[1], wx, v1);
-        dw::fma_acc(s[2], wx, v2);
-        dw::fma_acc(s[3], wy, v1);
-        dw::fma_acc(s[4], wy, v2);
-      }
-      dxr = dw::to_double(s[0]);
-      dxv1 = dw::to_double(s[1]);
-      dxv2 = dw::to_double(s[2]);
-      dyv1 = dw::to_double(s[3]);
-      dyv2 = dw::to_double(s[4]);
-    } else {
-      for (int j = 0; j < len; ++j) {
-        const int64_t p = base + ((int64_t)j << 5);
-        const int64_t c = __ldg(a.ell.col + p);
-        const double wx = __ldg(a.wx + p), wy = __ldg(a.wy + p);
-        const double rc = a.prim[c * 3], v1 = a.prim[c * 3 + 1], v2 = a.prim[c * 3 + 2];
-        dxr = fma(wx, rc, dxr);
-        dxv1 = fma(wx, v1, dxv1);
-        dxv2 = fma(wx, v2, dxv2);
-        dyv1 = fma(wy, v1, dyv1);
-        dyv2 = fma(wy, v2, dyv2);
-      }
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(a.ell.col + p);
+      const double wx = __ldg(a.wx + p), wy = __ldg(a.wy + p);
+      const double rc = a.prim[c * 3], v1 = a.prim[c * 3 + 1], v2 = a.prim[c * 3 + 2];
+      dxr = fma(wx, rc, dxr);
+      dxv1 = fma(wx, v1, dxv1);
+      dxv2 = fma(wx, v2, dxv2);
+      dyv1 = fma(wy, v1, dyv1);
+      dyv2 = fma(wy, v2, dyv2);
     }
     const double tr = dadd(dxr, dyv1);
     const double tsq = dadd(dadd(dmul(dxv1, dxv1), dmul(dmul(2.0, dyv1), dxv2)), dmul(dyv2, dyv2));
@@ -156,13 +122,10 @@ __global__ void k_igr_newdir(IgrArgs a, const double* uo, double* un) {
   if (a.sc->done) return;
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
   if (i >= a.n) return;
-  const double v = dadd(a.r[i], dmul(a.sc->beta, uo[i]));
-  un[i] = v;
-  if (a.dw) a.undw[i] = dw::split(v);
+  un[i] = dadd(a.r[i], dmul(a.sc->beta, uo[i]));
 }
 
 // t1 = rinv (Dx u_new), t2 = rinv (Dy u_new)
-template <bool DW>
 __global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un) {
   if (a.sc->done) return;
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
@@ -171,22 +134,6 @@ __global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un)
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   double sx = 0.0, sy = 0.0;
-  if (DW) {
-    dw::Acc ax = dw::zero(), ay = dw::zero();
-#pragma unroll 4
-    for (int j = 0; j < len; ++j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      const float2 uc = a.undw[__ldg(a.ell.col + p)];
-      dw::fma_acc(ax, __ldg(a.wxdw + p), uc);
-      dw::fma_acc(ay, __ldg(a.wydw + p), uc);
-    }
-    sx = dw::to_double(ax);
-    sy = dw::to_double(ay);
-    const double t1 = dmul(a.rinv[i], sx), t2 = dmul(a.rinv[i], sy);
-    a.tdw[i * 2] = dw::split(t1);
-    a.tdw[i * 2 + 1] = dw::split(t2);
-    return;
-  }
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
     const int64_t c = __ldg(a.ell.col + p);
@@ -199,7 +146,6 @@ __global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un)
 }
 
 // c = rinv u_new - alpha (Dx t1 + Dy t2); alpha_cg = res^2 / (u_new . c)
-template <bool DW>
 __global__ void __launch_bounds__(kBlock) k_igr_op(IgrArgs a, const double* un) {
   if (a.sc->done) return;
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
@@ -209,27 +155,13 @@ __global__ void __launch_bounds__(kBlock) k_igr_op(IgrArgs a, const double* un) 
     const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
     const int len = a.ell.row_len[r];
     double sx = 0.0, sy = 0.0;
-    if (DW) {
-      dw::Acc ax = dw::zero(), ay = dw::zero();
-      const float4* __restrict__ t4 = reinterpret_cast<const float4*>(a.tdw);
-#pragma unroll 4
-      for (int j = 0; j < len; ++j) {
-        const int64_t p = base + ((int64_t)j << 5);
-        const float4 tc = t4[__ldg(a.ell.col + p)];  // (t1, t2) pairs in one 16-byte load
-        dw::fma_acc(ax, __ldg(a.wxdw + p), make_float2(tc.x, tc.y));
-        dw::fma_acc(ay, __ldg(a.wydw + p), make_float2(tc.z, tc.w));
-      }
-      sx = dw::to_double(ax);
-      sy = dw::to_double(ay);
-    } else {
-      const double2* __restrict__ t2 = reinterpret_cast<const double2*>(a.t);
-      for (int j = 0; j < len; ++j) {
-        const int64_t p = base + ((int64_t)j << 5);
-        const int64_t c = __ldg(a.ell.col + p);
-        const double2 tc = t2[c];  // (t1, t2) of the neighbour in one 16-byte load
-        sx = fma(__ldg(a.wx + p), tc.x, sx);
-        sy = fma(__ldg(a.wy + p), tc.y, sy);
-      }
+    const double2* __restrict__ t2 = reinterpret_cast<const double2*>(a.t);
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(a.ell.col + p);
+      const double2 tc = t2[c];  // (t1, t2) of the neighbour in one 16-byte load
+      sx = fma(__ldg(a.wx + p), tc.x, sx);
+      sy = fma(__ldg(a.wy + p), tc.y, sy);
     }
     const double ci = dsub(dmul(a.rinv[i], un[i]), dmul(a.alpha, dadd(sx, sy)));
     a.c[i] = ci;
@@ -265,14 +197,7 @@ __global__ void __launch_bounds__(kBlock) k_igr_update(IgrArgs a, const double* 
   }
 }
 
-// sigma as pairs for the double-word flux gather
-__global__ void k_igr_xsplit(IgrArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i < a.n) a.xdw[i] = dw::split(a.x[i]);
-}
-
 // add = (-(Dx sigma), -(Dy sigma)) for the momentum rows of du
-template <bool DW>
 __global__ void __launch_bounds__(kBlock) k_igr_flux(IgrArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
   if (r >= a.n) return;
@@ -280,24 +205,11 @@ __global__ void __launch_bounds__(kBlock) k_igr_flux(IgrArgs a) {
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   double sx = 0.0, sy = 0.0;
-  if (DW) {
-    dw::Acc ax = dw::zero(), ay = dw::zero();
-#pragma unroll 4
-    for (int j = 0; j < len; ++j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      const float2 xc = a.xdw[__ldg(a.ell.col + p)];
-      dw::fma_acc(ax, __ldg(a.wxdw + p), xc);
-      dw::fma_acc(ay, __ldg(a.wydw + p), xc);
-    }
-    sx = dw::to_double(ax);
-    sy = dw::to_double(ay);
-  } else {
-    for (int j = 0; j < len; ++j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      const int64_t c = __ldg(a.ell.col + p);
-      sx = fma(__ldg(a.wx + p), a.x[c], sx);
-      sy = fma(__ldg(a.wy + p), a.x[c], sy);
-    }
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(a.ell.col + p);
+    sx = fma(__ldg(a.wx + p), a.x[c], sx);
+    sy = fma(__ldg(a.wy + p), a.x[c], sy);
   }
   a.add[i * 2] = -sx;
   a.add[i * 2 + 1] = -sy;
@@ -308,35 +220,23 @@ __global__ void __launch_bounds__(kBlock) k_igr_flux(IgrArgs a) {
 void launch_igr(const IgrArgs& a, const double* u, cudaStream_t s) {
   if (a.n <= 0) return;
   const unsigned g = (unsigned)((a.n + kBlock - 1) / kBlock);
-  const bool dwf = a.dw != 0;
-  MFT_REQUIRE(!dwf || (a.wxdw && a.wydw && a.primdw && a.undw && a.tdw && a.xdw), MFT_ERR_STATE,
-              "IGR double-word buffers not set");
-  k_igr_prim<<<g, kBlock, 0, s>>>(a.n, u, a.prim, a.rinv, dwf ? a.primdw : nullptr);
+  k_igr_prim<<<g, kBlock, 0, s>>>(a.n, u, a.prim, a.rinv);
   MFT_LAUNCH_CHECK();
-  if (dwf) k_igr_rhs<true><<<g, kBlock, 0, s>>>(a);
-  else k_igr_rhs<false><<<g, kBlock, 0, s>>>(a);
+  k_igr_rhs<<<g, kBlock, 0, s>>>(a);
   MFT_LAUNCH_CHECK();
   for (int it = 0; it < a.maxiter; ++it) {
     const double* uo = (it & 1) ? a.u1 : a.u0;
     double* un = (it & 1) ? a.u0 : a.u1;
     k_igr_newdir<<<g, kBlock, 0, s>>>(a, uo, un);
     MFT_LAUNCH_CHECK();
-    if (dwf) k_igr_dir<true><<<g, kBlock, 0, s>>>(a, un);
-    else k_igr_dir<false><<<g, kBlock, 0, s>>>(a, un);
+    k_igr_dir<<<g, kBlock, 0, s>>>(a, un);
     MFT_LAUNCH_CHECK();
-    if (dwf) k_igr_op<true><<<g, kBlock, 0, s>>>(a, un);
-    else k_igr_op<false><<<g, kBlock, 0, s>>>(a, un);
+    k_igr_op<<<g, kBlock, 0, s>>>(a, un);
     MFT_LAUNCH_CHECK();
     k_igr_update<<<g, kBlock, 0, s>>>(a, un);
     MFT_LAUNCH_CHECK();
   }
-  if (dwf) {
-    k_igr_xsplit<<<g, kBlock, 0, s>>>(a);
-    MFT_LAUNCH_CHECK();
-    k_igr_flux<true><<<g, kBlock, 0, s>>>(a);
-  } else {
-    k_igr_flux<false><<<g, kBlock, 0, s>>>(a);
-  }
+  k_igr_flux<<<g, kBlock, 0, s>>>(a);
   MFT_LAUNCH_CHECK();
 }
 

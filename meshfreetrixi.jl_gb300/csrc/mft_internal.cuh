@@ -400,15 +400,6 @@ struct IgrArgs {
   double* partial;      // one double per block
   unsigned* counter;
   IgrScalars* sc;
-  // double-word form (2D Euler, FP64 form with double-word gathers): the four gathers
-  // form their sums from pair copies of the weights and of the gathered node values
-  int dw;
-  const float2* wxdw;   // D_x, D_y pairs on the forward layout
-  const float2* wydw;
-  float2* primdw;       // n x 3
-  float2* undw;         // n: the current CG direction
-  float2* tdw;          // n x 2
-  float2* xdw;          // n: sigma, split before the flux gather
 };
 // Full IGR pipeline on the Euler state u (n x 4 AoS): prim, right-hand side, CG, flux.
 void launch_igr(const IgrArgs& a, const double* u, cudaStream_t s);

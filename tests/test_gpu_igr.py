@@ -1,6 +1,5 @@
 """GPU IGR source (SourceIGR) against the oracle: rhs! with the regularisation (a
-conjugate-gradient solve per evaluation) and a short SSP-RK3 trajectory, with the CG's
-operator gathers in double-word arithmetic (the FP64 form's default) and in FP64 FMAs.  Both sides
+conjugate-gradient solve per evaluation) and a short SSP-RK3 trajectory.  Both sides
 run the same CG iteration count unless a residual lands within rounding of the
 tolerance; rounding differences in the CG stay below 1e-9 of max |du| (asserted)."""
 import numpy as np
@@ -11,7 +10,7 @@ from helpers import GAMMA, load_ops_into, stencil_ops
 pytestmark = pytest.mark.gpu
 
 
-def _setup(oracle, alpha_h2=1.0, arith="auto"):
+def _setup(oracle, alpha_h2=1.0):
     from meshfree_gb300 import _lib as L
     from meshfree_gb300 import workloads as W
     pts, per, h = W.vortex_cloud(32, seed=3)
@@ -21,8 +20,6 @@ def _setup(oracle, alpha_h2=1.0, arith="auto"):
     semi = oracle.Semi(pts, ops, eq="euler", gamma=GAMMA, sources=[oracle.SRC_IGR],
                        igr_alpha=alpha, igr_maxiter=20)
     ctx = L.Context(0)
-    ctx.set_option(L.OPT_FP64_ARITH, {"auto": L.ARITH_AUTO, "dw": L.ARITH_DW,
-                                      "dfma": L.ARITH_DFMA}[arith])
     ctx.set_points(pts)
     load_ops_into(ctx, ops)
     ctx.set_equations(L.EQ_EULER2D, [GAMMA])
@@ -31,11 +28,10 @@ def _setup(oracle, alpha_h2=1.0, arith="auto"):
     return semi, ctx, pts, h
 
 
-@pytest.mark.parametrize("arith", ["dw", "dfma"])
 @pytest.mark.parametrize("alpha_h2", [1.0, 20.0])
-def test_rhs_igr_matches_oracle(oracle, gpu_lib, alpha_h2, arith):
+def test_rhs_igr_matches_oracle(oracle, gpu_lib, alpha_h2):
     from meshfree_gb300 import workloads as W
-    semi, ctx, pts, _h = _setup(oracle, alpha_h2, arith)
+    semi, ctx, pts, _h = _setup(oracle, alpha_h2)
     u = W.isentropic_vortex(pts, 0.0)
     ref = semi.rhs(u.copy(), 0.0)
     got = np.empty_like(u)
@@ -50,10 +46,9 @@ def test_rhs_igr_matches_oracle(oracle, gpu_lib, alpha_h2, arith):
     assert np.array_equal(plain[0], got[0]) and np.array_equal(plain[3], got[3])
 
 
-@pytest.mark.parametrize("arith", ["dw", "dfma"])
-def test_igr_trajectory_matches_oracle(oracle, gpu_lib, arith):
+def test_igr_trajectory_matches_oracle(oracle, gpu_lib):
     from meshfree_gb300 import workloads as W
-    semi, ctx, pts, h = _setup(oracle, arith=arith)
+    semi, ctx, pts, h = _setup(oracle)
     u0 = W.isentropic_vortex(pts, 0.0)
     dt, nsteps = 0.1 * h, 5
     ref, _ = oracle.ssprk33(semi, u0, 0.0, dt, nsteps)
