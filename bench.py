@@ -90,8 +90,9 @@ def parse():
                     help="stencils of the batched-weights measurement (0 skips it)")
     ap.add_argument("--riemann-side", type=int, default=1024,
                     help="nodes per side of the Riemann FP32/FP64 run to t = 0.2 (0 skips it)")
-    ap.add_argument("--igr-arith", default="both", choices=["both", "dw", "dfma"],
-                    help="gather arithmetic(s) of the IGR measurement")
+    ap.add_argument("--igr-arith", default="dw", choices=["both", "dw", "dfma"],
+                    help="engine form(s) of the IGR measurement (the CG itself runs in FP64 "
+                         "fused multiply-adds in both)")
     ap.add_argument("--vortex-side", type=int, default=512,
                     help="nodes per side of the vortex measurement (0 skips it)")
     ap.add_argument("--adj-steps", type=int, default=500,
