@@ -221,9 +221,10 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
        MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8,
-       MFT_OPT_IGR_ITERS = 9 };
+       MFT_OPT_IGR_ITERS = 9, MFT_OPT_ADJ_EVERY = 10 };
 /* Read-only MFT_OPT_IGR_ITERS: conjugate-gradient iterations of the last IGR solve
- * (-1 before the first). */
+ * (-1 before the first).  Read-only MFT_OPT_ADJ_EVERY: the checkpoint interval of the last
+ * mft_ssprk33_record (0: every stage state stored). */
 /* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups (256 layout rows each) of
  * the double-word form's layouts, MFT_OPT_HALO_STAGED_FWD / _REV = how many of them have
  * their neighbour records staged in shared memory by DW variants 6-8 (the others gather
@@ -374,7 +375,10 @@ mft_status mft_rhs_adjoint_device(mft_ctx* ctx, double* out, const double* lam, 
 /* Advances the device state nsteps SSP-RK3 steps of size dt (the same arithmetic as
  * mft_ssprk33) and records the trajectory for mft_ssprk33_adjoint: the state every
  * `every` steps (the stage states are recomputed from these checkpoints during the
- * reverse sweep), or every stage state of every step when every == 0. */
+ * reverse sweep), or every stage state of every step when every == 0.  every == -1 picks:
+ * every stage state when they take at most half of the free device memory (the sweep then
+ * recomputes nothing), else checkpoints every ceil(sqrt(nsteps / 3)) steps; the choice is
+ * read back through MFT_OPT_ADJ_EVERY. */
 mft_status mft_ssprk33_record(mft_ctx* ctx, double dt, int nsteps, int every);
 
 /* Reverse sweep over the recorded trajectory.  On entry lam (host StructArray-style)

@@ -58,18 +58,33 @@ static __device__ __forceinline__ void project_row(const BcDev& bc, int64_t i, d
 // The node part of the adjoint at node i from the gathered sums gx = Dx^T M2 lam,
 // gy = Dy^T M2 lam and gh (the hyperviscosity term): flux-Jacobian-transpose product,
 // the SSP-RK3 adjoint stage combination and the BC projection.
+// gxp / gyp (double-word path): the gathered sums as pairs, from which the Jacobian product
+// is formed in double-word arithmetic (gx / gy unused then).
 template <int V, bool EULER, bool BC, int HV>
 static __device__ __forceinline__ void adj_finish(const AdjArgs& a, int64_t i, const double* gx,
-                                                  const double* gy, const double* gh) {
+                                                  const double* gy, const double* gh,
+                                                  const float2* gxp = nullptr,
+                                                  const float2* gyp = nullptr) {
   double r[V];
   if constexpr (EULER) {
     double uu[4];
     load_row<4>(a.u, i, uu);
     if (BC && a.bc.tag[i] == 2) slip(a.bc.normal + 2 * (int64_t)a.bc.slot[i], uu);
-    double ub[4];
-    euler_flux_vjp(a.gamma, uu, gx, gy, ub);
+    if (gxp) {
+      const double gm1 = a.gamma - 1.0;
+      const float2 g2 = dw::split(gm1);
+      const float2 up[4] = {dw::split(uu[0]), dw::split(uu[1]), dw::split(uu[2]),
+                            dw::split(uu[3])};
+      float2 ub[4];
+      dw::euler_flux_vjp(g2, up, gxp, gyp, ub);
 #pragma unroll
-    for (int v = 0; v < V; ++v) r[v] = -ub[v];
+      for (int v = 0; v < V; ++v) r[v] = -dw::value(ub[v]);
+    } else {
+      double ub[4];
+      euler_flux_vjp(a.gamma, uu, gx, gy, ub);
+#pragma unroll
+      for (int v = 0; v < V; ++v) r[v] = -ub[v];
+    }
   } else {
 #pragma unroll
     for (int v = 0; v < V; ++v) r[v] = -(a.ax * gx[v] + a.ay * gy[v]);
@@ -215,14 +230,16 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_adj_dw(AdjArgs a)
       for (int v = 0; v < 4; ++v) dw::fma_acc(gh[v], wh, l[v]);
     }
   }
-  double gxd[4], gyd[4], ghd[4];
+  // the Jacobian product in double-word arithmetic from the sums as pairs
+  float2 gxp[4], gyp[4];
+  double ghd[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    gxd[v] = dw::to_double(gx[v]);
-    gyd[v] = dw::to_double(gy[v]);
+    gxp[v] = dw::to_pair(gx[v]);
+    gyp[v] = dw::to_pair(gy[v]);
     ghd[v] = HV ? dw::to_double(gh[v]) : 0.0;
   }
-  adj_finish<4, true, BC, HV>(a, i, gxd, gyd, ghd);
+  adj_finish<4, true, BC, HV>(a, i, nullptr, nullptr, ghd, gxp, gyp);
 }
 
 // q_i = sum_j lap[i,j] (M2 lam)_j over the forward sliced ELL.

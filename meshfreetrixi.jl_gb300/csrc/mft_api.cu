@@ -1518,6 +1518,7 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_HALO_STAGED_FWD) *value = (int)c->fwd.halo_staged;
     else if (option == MFT_OPT_HALO_STAGED_REV) *value = (int)c->rev.halo_staged;
     else if (option == MFT_OPT_HALO_GROUPS) *value = (int)c->fwd.halo_groups;
+    else if (option == MFT_OPT_ADJ_EVERY) *value = c->adj_every;
     else if (option == MFT_OPT_IGR_ITERS) {
       // CG iterations of the last IGR solve (-1: none yet)
       *value = -1;
@@ -2627,10 +2628,20 @@ mft_status mft_ssprk33_record(mft_ctx* c, double dt, int nsteps, int every) {
   return guarded(c, [&] {
     MFT_REQUIRE(c->state_valid, MFT_ERR_STATE, "call mft_set_state first");
     MFT_REQUIRE(nsteps >= 1, MFT_ERR_ARG, "nsteps < 1");
-    MFT_REQUIRE(every >= 0, MFT_ERR_ARG, "every < 0");
+    MFT_REQUIRE(every >= -1, MFT_ERR_ARG, "every < -1");
     MFT_REQUIRE(dt > 0 && isfinite(dt), MFT_ERR_ARG, "dt must be positive and finite");
     check_adjoint_ready(c);
     set_device(c);
+    if (every == -1) {
+      // every stage state when they fit in half of the device memory free (counting what
+      // the previous recording holds), which spares the sweep its recomputation; else
+      // checkpoints every ~sqrt(nsteps / 3) steps (the least memory)
+      size_t free_b = 0, total_b = 0;
+      MFT_CUDA(cudaMemGetInfo(&free_b, &total_b));
+      const double avail = (double)free_b + 8.0 * (double)(c->adj_store.n + c->adj_ckpt.n);
+      const double need = 3.0 * nsteps * (double)c->n * c->nvars * 8.0;
+      every = need <= 0.5 * avail ? 0 : std::max(1, (int)ceil(sqrt(nsteps / 3.0)));
+    }
     ssprk33_record(c, dt, nsteps, every);
     check_kernel_errors(c);
   });

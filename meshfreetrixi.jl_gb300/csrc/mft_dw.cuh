@@ -112,5 +112,26 @@ static __device__ __forceinline__ float2 recip(float2 a) {
   return make_float2(t, __fsub_rn(c, __fsub_rn(t, y)));
 }
 
+// The Euler flux-Jacobian-transpose product ub = J_Fx(u)^T gx + J_Fy(u)^T gy (as
+// euler_flux_vjp in FP64) in double-word arithmetic: u as pairs, gx / gy as pairs,
+// gm1 = gamma - 1 as a pair; each operation is accurate to about 2 u^2 of its operands.
+static __device__ __forceinline__ void euler_flux_vjp(float2 gm1, const float2* u,
+                                                      const float2* gx, const float2* gy,
+                                                      float2* ub) {
+  const float2 rho = u[0], m1 = u[1], m2 = u[2], en = u[3];
+  const float2 ri = recip(rho);
+  const float2 v1 = mul(m1, ri), v2 = mul(m2, ri);
+  const float2 p = mul(gm1, add(en, neg(scale2(add(mul(m1, v1), mul(m2, v2)), 0.5f))));
+  const float2 ep = add(en, p);
+  const float2 pb = add(add(gx[1], mul(gx[3], v1)), add(gy[2], mul(gy[3], v2)));
+  const float2 hp = scale2(mul(gm1, pb), 0.5f);
+  const float2 v1b = add(add(mul(gx[1], m1), mul(gx[3], ep)), add(mul(gy[1], m2), neg(mul(hp, m1))));
+  const float2 v2b = add(add(mul(gx[2], m1), mul(gy[2], m2)), add(mul(gy[3], ep), neg(mul(hp, m2))));
+  ub[0] = neg(mul(add(mul(v1b, v1), mul(v2b, v2)), ri));
+  ub[1] = add(add(add(gx[0], mul(gx[1], v1)), add(mul(gx[2], v2), neg(mul(hp, v1)))), mul(v1b, ri));
+  ub[2] = add(add(add(gy[0], mul(gy[1], v1)), add(mul(gy[2], v2), neg(mul(hp, v2)))), mul(v2b, ri));
+  ub[3] = add(add(mul(gx[3], v1), mul(gy[3], v2)), mul(gm1, pb));
+}
+
 }  // namespace dw
 }  // namespace mft

@@ -571,11 +571,13 @@ def solve(ode, alg=None, dt=None, callback=None, save_everystep=False, resume_fr
     return ODESolution(u, t, steps)
 
 
-def solve_adjoint(ode, dt, dJdu, checkpoint_every=0):
+def solve_adjoint(ode, dt, dJdu, checkpoint_every=-1):
     """Gradient of an objective of the final state w.r.t. the initial state: SSP-RK3
     from tspan[0] to tspan[1] in steps of dt (which must divide the span), recorded
-    with a checkpoint every `checkpoint_every` steps (0 keeps every stage state), then
-    the reverse sweep from dJdu(u(T)).  Returns (ODESolution, dJ/du0)."""
+    with a checkpoint every `checkpoint_every` steps (0 keeps every stage state; -1, the
+    default, keeps every stage state when they fit in half of the free device memory and
+    checkpoints otherwise), then the reverse sweep from dJdu(u(T)).  Returns
+    (ODESolution, dJ/du0)."""
     semi = ode.p
     ctx = semi.domain.ctx
     t0, t1 = ode.tspan
