@@ -216,12 +216,17 @@ def test_trajectory_adjoint_matches_oracle(oracle, gpu_lib, cyl, cyl_ops, vortex
     lamT = np.zeros_like(uT_o)
     lamT[0] = uT_o[0] - target
     ref = oracle.ssprk33_adjoint(semi, rec, dt, lamT)
+    from meshfree_gb300 import _lib as L
     grads, states = {}, {}
-    for every in (0, 2, 4):
+    for every in (0, 2, 4, -1):
         ctx.set_state(u0, 0.0)
         ctx.ssprk33_record(dt, nsteps, every)
+        if every == -1:
+            # the default policy stores every stage state of so small a problem
+            assert ctx.get_option(L.OPT_ADJ_EVERY) == 0
         states[every] = ctx.get_state()[0]
         grads[every] = ctx.ssprk33_adjoint(lamT)
+    assert np.array_equal(grads[0], grads[-1])
     # the recording integrator is the plain one
     ctx.set_state(u0, 0.0)
     ctx.ssprk33(dt, nsteps, use_graph=False)
