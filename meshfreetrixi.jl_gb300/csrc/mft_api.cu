@@ -380,9 +380,14 @@ void ensure_work(mft_ctx* c) {
     c->kerr.alloc(1);
     c->kerr.zero(c->stream);
   }
-  if (c->red_blocks == 0) {
-    c->red_blocks = 512;
-    c->red_partial.alloc((size_t)c->red_blocks * 8);
+  // the norm reductions: about four nodes per thread of 128-thread blocks, so that the
+  // loads of a large cloud fill every SM
+  const int rb = (int)std::min<int64_t>(4096, std::max<int64_t>(64, (n + 511) / 512));
+  if (c->red_blocks != rb) {
+    c->red_blocks = rb;
+    c->red_partial.alloc((size_t)rb * 8);
+  }
+  if (!c->red_counter.p) {
     c->red_counter.alloc(2);
     c->red_counter.zero(c->stream);
     c->mean.alloc(8);
