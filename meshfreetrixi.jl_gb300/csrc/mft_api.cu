@@ -380,9 +380,9 @@ void ensure_work(mft_ctx* c) {
     c->kerr.alloc(1);
     c->kerr.zero(c->stream);
   }
-  // the norm reductions: about four nodes per thread of 128-thread blocks, so that the
-  // loads of a large cloud fill every SM
-  const int rb = (int)std::min<int64_t>(4096, std::max<int64_t>(64, (n + 511) / 512));
+  // the norm reductions: 512 blocks (measured on the 1M cloud: 2048 blocks of four nodes
+  // per thread take 37 µs for the mean instead of 25, the per-block combine dominating)
+  const int rb = 512;
   if (c->red_blocks != rb) {
     c->red_blocks = rb;
     c->red_partial.alloc((size_t)rb * 8);
