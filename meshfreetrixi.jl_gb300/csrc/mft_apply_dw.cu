@@ -10,8 +10,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
-#include <map>
 #include <mutex>
+#include <set>
 #include <utility>
 
 #include "mft_device.cuh"
@@ -163,10 +163,8 @@ static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, 
 // The variants form the same sums in the same order; the autotuner picks one.
 // HALO: blocks of one row group (ell.halo_rows rows) first stage the group's neighbour
 // records in shared memory and read them from there (groups without a list gather
-// directly); PIPE 0 or 2 then sets the loop's unrolling.  WST > 0 (staged groups): the
-// weights and positions stream through a per-warp WST-slot ring (WarpRing) instead of
-// being loaded at use.
-template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO, int WST = 0>
+// directly); PIPE 0 or 2 then sets the loop's unrolling.
+template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
   const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
@@ -179,12 +177,10 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
     staged = stage_halo<(WT || WQ || FLY) ? 6 : 4>(
         a.ell, hsm, [&](int k, int64_t c) { return k < 4 ? F4 + c * 4 + k : U4 + c * 2 + (k - 4); });
   }
-  const bool active = r < a.n;
-  // a pipelined warp keeps its rows past n in the ring's issue / wait steps
-  if (!active && !(WST > 0 && staged)) return;
-  const int64_t i = active ? ell_node(a.ell, r) : 0;
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
-  const int len = active ? a.ell.row_len[r] : 0;
+  const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
   dw::Acc f[4], tx[4], ty[4], q[4];
 #pragma unroll
@@ -193,44 +189,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
   }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (WST > 0 && staged) {
-    constexpr int NA = (WQ || FLY) ? 3 : 2;
-    constexpr int NCH = (WT || WQ || FLY) ? 6 : 4;
-    const float2* arrays[3] = {a.wdw[0], a.wdw[1], a.wldw};
-    WarpRing<NA, (WST > 0 ? WST : 1)> ring;
-    ring.ring = hsm + NCH * hs + (threadIdx.x >> 5) * ((WST > 0 ? WST : 1) * ring.kSlot);
-    ring.s0 = a.ell.slice_off[r >> 5];
-    ring.m = (int)((a.ell.slice_off[(r >> 5) + 1] - ring.s0) >> 5);
-    ring.lane = threadIdx.x & 31;
-    ring.arrays = arrays;
-    ring.lcol = lcol;
-#pragma unroll
-    for (int st = 0; st < WST - 1; ++st) ring.issue(st);
-#pragma unroll 1
-    for (int j = 0; j < ring.m; ++j) {
-      ring.issue(j + WST - 1);
-      cp_async_wait_group<(WST > 0 ? WST - 1 : 0)>();
-      __syncwarp();
-      if (j < len) {
-        const int lc = ring.pos(j);
-        FwdEntry e;
-        e.wx = ring.weight(j, 0);
-        e.wy = ring.weight(j, 1);
-        if (WQ || FLY) e.wl = ring.weight(j, 2);
-        e.fa.lo = hsm[lc];
-        e.fa.hi = hsm[hs + lc];
-        e.fb.lo = hsm[2 * hs + lc];
-        e.fb.hi = hsm[3 * hs + lc];
-        if (WT || WQ || FLY) {
-          e.uu.lo = hsm[4 * hs + lc];
-          e.uu.hi = hsm[5 * hs + lc];
-        }
-        fwd_accum<WT, WQ, FLY>(e, f, tx, ty, q);
-      }
-      __syncwarp();
-    }
-    if (!active) return;
-  } else if (HALO && staged) {
+  if (HALO && staged) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -416,7 +375,7 @@ static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx,
 // Transpose gather (Euler) over the reverse adjacency, as k_rev_f64:
 // du_i = du_p_i - sum_j (Dx[j,i] s_x[j] + Dy[j,i] s_y[j]) - gamma sum_j lap[j,i] q[j],
 // with s = eps * t and q as double-word pairs.  PIPE and MINB as for k_fwd_euler_dw.
-template <bool RV, bool LAP, int PIPE, int MINB, bool PREF, bool HALO, int WST = 0>
+template <bool RV, bool LAP, int PIPE, int MINB, bool PREF, bool HALO>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_dw(RevArgs a) {
   constexpr int NCH = (RV ? 4 : 0) + (LAP ? 2 : 0);
   const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
@@ -431,57 +390,17 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
       return (RV && k < 4) ? S4 + c * 4 + k : Q4 + c * 2 + (k - (RV ? 4 : 0));
     });
   }
-  const bool active = r < a.n;
-  if (!active && !(WST > 0 && staged)) return;
-  const int64_t i = active ? ell_node(a.ell, r) : 0;
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
-  const int len = active ? a.ell.row_len[r] : 0;
+  const int len = a.ell.row_len[r];
   const int32_t* __restrict__ col = a.ell.col;
   dw::Acc sx[4], sy[4], sl[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) { sx[v] = dw::zero(); sy[v] = dw::zero(); sl[v] = dw::zero(); }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (WST > 0 && staged) {
-    constexpr int NA = (RV ? 2 : 0) + (LAP ? 1 : 0);
-    constexpr int kq = RV ? 4 : 0;
-    const float2* arrays[3] = {RV ? a.wdw[0] : a.wldw, RV ? a.wdw[1] : a.wldw, a.wldw};
-    WarpRing<(NA > 0 ? NA : 1), (WST > 0 ? WST : 1)> ring;
-    ring.ring = hsm + NCH * hs + (threadIdx.x >> 5) * ((WST > 0 ? WST : 1) * ring.kSlot);
-    ring.s0 = a.ell.slice_off[r >> 5];
-    ring.m = (int)((a.ell.slice_off[(r >> 5) + 1] - ring.s0) >> 5);
-    ring.lane = threadIdx.x & 31;
-    ring.arrays = arrays;
-    ring.lcol = lcol;
-#pragma unroll
-    for (int st = 0; st < WST - 1; ++st) ring.issue(st);
-#pragma unroll 1
-    for (int j = 0; j < ring.m; ++j) {
-      ring.issue(j + WST - 1);
-      cp_async_wait_group<(WST > 0 ? WST - 1 : 0)>();
-      __syncwarp();
-      if (j < len) {
-        const int lc = ring.pos(j);
-        RevEntry e;
-        if (RV) {
-          e.wx = ring.weight(j, 0);
-          e.wy = ring.weight(j, 1);
-          e.xa.lo = hsm[lc];
-          e.xa.hi = hsm[hs + lc];
-          e.ya.lo = hsm[2 * hs + lc];
-          e.ya.hi = hsm[3 * hs + lc];
-        }
-        if (LAP) {
-          e.wl = ring.weight(j, RV ? 2 : 0);
-          e.qq.lo = hsm[kq * hs + lc];
-          e.qq.hi = hsm[(kq + 1) * hs + lc];
-        }
-        rev_accum<RV, LAP>(e, sx, sy, sl);
-      }
-      __syncwarp();
-    }
-    if (!active) return;
-  } else if (HALO && staged) {
+  if (HALO && staged) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -588,32 +507,25 @@ namespace {
 // 6 / 7 = neighbour records staged per row group in shared memory (one / two entries per
 // iteration, registers capped at three blocks of kHaloRows per SM), 8 = variant 7 capped
 // at four blocks, 9 / 11 = staged with four / three entries per iteration, 10 = variant 7
-// with the streamed position and weight arrays prefetched into L2 (as variant 4), 12 / 13
-// = staged with the weights and positions streamed through a per-warp shared-memory ring
-// four / eight slots ahead (asynchronous copies; three / two blocks per SM).  Without halos
+// with the streamed position and weight arrays prefetched into L2 (as variant 4).  Without halos
 // (not built) the staged variants run as variant 2.
 // A staged launch: one block per row group, NCH chunks of the layout's longest list
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
 // kernel and device).
-// ring_slot4: float4 per slot of the per-warp weight ring (0 without one), wst: its slots.
 template <typename Args>
-void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStream_t s,
-                   int ring_slot4 = 0, int wst = 0) {
-  const int rows = a.ell.halo_rows;
-  const size_t smem = ((size_t)nch * a.ell.halo_stride +
-                       (size_t)(rows / 32) * wst * ring_slot4) * sizeof(float4);
+void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStream_t s) {
+  const size_t smem = (size_t)nch * a.ell.halo_stride * sizeof(float4);
   if (smem > 48 * 1024) {
     static std::mutex mu;
-    static std::map<std::pair<const void*, int>, size_t> opted;
+    static std::set<std::pair<const void*, int>> done;
     int dev = 0;
     MFT_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lock(mu);
-    size_t& cur = opted[{reinterpret_cast<const void*>(k), dev}];
-    if (smem > cur) {
-      MFT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      cur = smem;
-    }
+    if (done.insert({reinterpret_cast<const void*>(k), dev}).second)
+      MFT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(6 * kHaloMax * sizeof(float4))));
   }
+  const int rows = a.ell.halo_rows;
   k<<<grid_for(n, rows), rows, smem, s>>>(a);
 }
 
@@ -621,7 +533,6 @@ template <bool WT, bool WQ, int FLY>
 void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
   const unsigned g = grid_for(n, kBlock);
   constexpr int nch = (WT || WQ || FLY) ? 6 : 4;
-  constexpr int nslot = 16 * ((WQ || FLY) ? 3 : 2) + 4;
   if (variant >= 6 && !a.ell.halo_off) variant = 2;
   switch (variant) {
     case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false, false><<<g, kBlock, 0, s>>>(a); break;
@@ -635,12 +546,6 @@ void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 9: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 4, 3, false, true>, a, nch, n, s); break;
     case 10: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, true, true>, a, nch, n, s); break;
     case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true>, a, nch, n, s); break;
-    case 12:
-      launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 0, 3, false, true, 4>, a, nch, n, s, nslot, 4);
-      break;
-    case 13:
-      launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 0, 2, false, true, 8>, a, nch, n, s, nslot, 8);
-      break;
     default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
@@ -649,7 +554,6 @@ template <bool RV, bool LAP>
 void rev_variant(const RevArgs& a, int variant, int64_t n, cudaStream_t s) {
   const unsigned g = grid_for(n, kBlock);
   constexpr int nch = (RV ? 4 : 0) + (LAP ? 2 : 0);
-  constexpr int nslot = 16 * ((RV ? 2 : 0) + (LAP ? 1 : 0) > 0 ? (RV ? 2 : 0) + (LAP ? 1 : 0) : 1) + 4;
   if (variant >= 6 && !a.ell.halo_off) variant = 2;
   switch (variant) {
     case 1: k_rev_euler_dw<RV, LAP, 2, 6, false, false><<<g, kBlock, 0, s>>>(a); break;
@@ -663,12 +567,6 @@ void rev_variant(const RevArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 9: launch_staged(k_rev_euler_dw<RV, LAP, 4, 3, false, true>, a, nch, n, s); break;
     case 10: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, true, true>, a, nch, n, s); break;
     case 11: launch_staged(k_rev_euler_dw<RV, LAP, 3, 3, false, true>, a, nch, n, s); break;
-    case 12:
-      launch_staged(k_rev_euler_dw<RV, LAP, 0, 3, false, true, 4>, a, nch, n, s, nslot, 4);
-      break;
-    case 13:
-      launch_staged(k_rev_euler_dw<RV, LAP, 0, 2, false, true, 8>, a, nch, n, s, nslot, 8);
-      break;
     default: k_rev_euler_dw<RV, LAP, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }

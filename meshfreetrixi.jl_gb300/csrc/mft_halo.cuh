@@ -18,52 +18,6 @@ static __device__ __forceinline__ void cp_async16(float4* smem, const float4* gm
 static __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
-static __device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-// Waits until at most N of this thread's committed copy groups are still in flight.
-template <int N>
-static __device__ __forceinline__ void cp_async_wait_group() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-// Per-warp ring of the streamed arrays of a sliced-ELL gather: for slot j of the warp's
-// slice, NA double-word weight arrays (32 lanes x 8 bytes = 16 chunks each) and the 16-bit
-// positions (32 x 2 bytes = 4 chunks), copied into shared memory WST - 1 slots ahead of
-// use, so that their DRAM latency is covered without registers.  Slot layout (float4):
-// [array a: 16 chunks] x NA, then the positions.  Every lane of the warp takes part in
-// every issue / wait (rows past n included: their slice exists, padded).
-template <int NA, int WST>
-struct WarpRing {
-  static constexpr int kSlot = 16 * NA + 4;  // float4 per slot
-  float4* ring;
-  int64_t s0;    // first ELL element of the slice
-  int m;         // slots of the slice
-  int lane;
-  const float2* const* arrays;
-  const uint16_t* lcol;
-  __device__ __forceinline__ void issue(int j) {
-    if (j < m) {
-      float4* dst = ring + (j % WST) * kSlot;
-      const int64_t e0 = s0 + ((int64_t)j << 5);
-#pragma unroll
-      for (int q = lane; q < kSlot; q += 32) {
-        const float4* src = q < 16 * NA
-                                ? reinterpret_cast<const float4*>(arrays[q >> 4] + e0) + (q & 15)
-                                : reinterpret_cast<const float4*>(lcol + e0) + (q - 16 * NA);
-        cp_async16(dst + q, src);
-      }
-    }
-    cp_async_commit();
-  }
-  // weight pair of array a and the position of this lane in slot j (after wait + sync)
-  __device__ __forceinline__ float2 weight(int j, int a) const {
-    return reinterpret_cast<const float2*>(ring + (j % WST) * kSlot)[a * 32 + lane];
-  }
-  __device__ __forceinline__ int pos(int j) const {
-    return reinterpret_cast<const uint16_t*>(ring + (j % WST) * kSlot + 16 * NA)[lane];
-  }
-};
 
 // Stages the neighbour records of this block's row group (the group's halo list) into
 // shared memory: NCH 16-byte chunks per record, chunk k of list entry q at
