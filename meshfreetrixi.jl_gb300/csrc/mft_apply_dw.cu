@@ -189,42 +189,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
   }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (HALO && staged && PIPE == 1) {
-    // the position and weights of entry j + 1 are loaded while entry j accumulates
-    struct W { float2 wx, wy, wl; int lc; };
-    auto wload = [&](int j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      W w;
-      w.lc = __ldg(lcol + p);
-      w.wx = __ldg(a.wdw[0] + p);
-      w.wy = __ldg(a.wdw[1] + p);
-      if (WQ || FLY) w.wl = __ldg(a.wldw + p);
-      return w;
-    };
-    if (len > 0) {
-      W cur = wload(0);
-#pragma unroll 1
-      for (int j = 0; j < len; ++j) {
-        W nxt;
-        if (j + 1 < len) nxt = wload(j + 1);
-        FwdEntry e;
-        e.wx = cur.wx;
-        e.wy = cur.wy;
-        if (WQ || FLY) e.wl = cur.wl;
-        const int lc = cur.lc;
-        e.fa.lo = hsm[lc];
-        e.fa.hi = hsm[hs + lc];
-        e.fb.lo = hsm[2 * hs + lc];
-        e.fb.hi = hsm[3 * hs + lc];
-        if (WT || WQ || FLY) {
-          e.uu.lo = hsm[4 * hs + lc];
-          e.uu.hi = hsm[5 * hs + lc];
-        }
-        fwd_accum<WT, WQ, FLY>(e, f, tx, ty, q);
-        cur = nxt;
-      }
-    }
-  } else if (HALO && staged) {
+  if (HALO && staged) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -253,7 +218,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
       const int64_t c = __ldg(col + p);
       fwd_accum<WT, WQ, FLY>(fwd_load<WT, WQ, FLY>(a, F, U, p, c), f, tx, ty, q);
     }
-  } else if (PIPE == 2 || (HALO && PIPE != 0)) {
+  } else if (PIPE == 2 || (HALO && PIPE > 2)) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -435,46 +400,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
   for (int v = 0; v < 4; ++v) { sx[v] = dw::zero(); sy[v] = dw::zero(); sl[v] = dw::zero(); }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (HALO && staged && PIPE == 1) {
-    struct W { float2 wx, wy, wl; int lc; };
-    auto wload = [&](int j) {
-      const int64_t p = base + ((int64_t)j << 5);
-      W w;
-      w.lc = __ldg(lcol + p);
-      if (RV) {
-        w.wx = __ldg(a.wdw[0] + p);
-        w.wy = __ldg(a.wdw[1] + p);
-      }
-      if (LAP) w.wl = __ldg(a.wldw + p);
-      return w;
-    };
-    if (len > 0) {
-      constexpr int kq = RV ? 4 : 0;
-      W cur = wload(0);
-#pragma unroll 1
-      for (int j = 0; j < len; ++j) {
-        W nxt;
-        if (j + 1 < len) nxt = wload(j + 1);
-        RevEntry e;
-        const int lc = cur.lc;
-        if (RV) {
-          e.wx = cur.wx;
-          e.wy = cur.wy;
-          e.xa.lo = hsm[lc];
-          e.xa.hi = hsm[hs + lc];
-          e.ya.lo = hsm[2 * hs + lc];
-          e.ya.hi = hsm[3 * hs + lc];
-        }
-        if (LAP) {
-          e.wl = cur.wl;
-          e.qq.lo = hsm[kq * hs + lc];
-          e.qq.hi = hsm[(kq + 1) * hs + lc];
-        }
-        rev_accum<RV, LAP>(e, sx, sy, sl);
-        cur = nxt;
-      }
-    }
-  } else if (HALO && staged) {
+  if (HALO && staged) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -503,7 +429,7 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
       const int64_t c = __ldg(col + p);
       rev_accum<RV, LAP>(rev_load<RV, LAP>(a, S, Q, p, c), sx, sy, sl);
     }
-  } else if (PIPE == 2 || (HALO && PIPE != 0)) {
+  } else if (PIPE == 2 || (HALO && PIPE > 2)) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
     const bool pf_lane = PREF && (threadIdx.x & 31) == 0;
@@ -581,9 +507,7 @@ namespace {
 // 6 / 7 = neighbour records staged per row group in shared memory (one / two entries per
 // iteration, registers capped at three blocks of kHaloRows per SM), 8 = variant 7 capped
 // at four blocks, 9 / 11 = staged with four / three entries per iteration, 10 = variant 7
-// with the streamed position and weight arrays prefetched into L2 (as variant 4), 12 =
-// staged with the position and weights of the next entry loaded while the current one
-// accumulates.  Without halos
+// with the streamed position and weight arrays prefetched into L2 (as variant 4).  Without halos
 // (not built) the staged variants run as variant 2.
 // A staged launch: one block per row group, NCH chunks of the layout's longest list
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
@@ -622,7 +546,6 @@ void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 9: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 4, 3, false, true>, a, nch, n, s); break;
     case 10: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, true, true>, a, nch, n, s); break;
     case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true>, a, nch, n, s); break;
-    case 12: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 1, 3, false, true>, a, nch, n, s); break;
     default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
@@ -644,7 +567,6 @@ void rev_variant(const RevArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 9: launch_staged(k_rev_euler_dw<RV, LAP, 4, 3, false, true>, a, nch, n, s); break;
     case 10: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, true, true>, a, nch, n, s); break;
     case 11: launch_staged(k_rev_euler_dw<RV, LAP, 3, 3, false, true>, a, nch, n, s); break;
-    case 12: launch_staged(k_rev_euler_dw<RV, LAP, 1, 3, false, true>, a, nch, n, s); break;
     default: k_rev_euler_dw<RV, LAP, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
