@@ -215,9 +215,9 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
 /* Engine options.  MFT_OPT_GATHER selects the mapping of the FP32 operator gathers:
  * MFT_GATHER_THREAD (one node per thread, direct loads), MFT_GATHER_STAGED (one warp
  * per 32-node slice with the slice's indices and weights streamed into shared memory by
- * bulk copies), MFT_GATHER_HALO (one node per thread, each group of 256 layout rows
- * staging its distinct neighbour records in shared memory first), or MFT_GATHER_AUTO
- * (default: the autotuner times the three on the live inputs). */
+ * bulk copies), MFT_GATHER_HALO (one node per thread, each group of 256 (or 128)
+ * layout rows staging its distinct neighbour records in shared memory first), or
+ * MFT_GATHER_AUTO (default: the autotuner times the three on the live inputs). */
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
        MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8,
@@ -225,17 +225,18 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
 /* Read-only MFT_OPT_IGR_ITERS: conjugate-gradient iterations of the last IGR solve
  * (-1 before the first).  Read-only MFT_OPT_ADJ_EVERY: the checkpoint interval of the last
  * mft_ssprk33_record (0: every stage state stored). */
-/* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups (256 layout rows each) of
- * the double-word form's layouts, MFT_OPT_HALO_STAGED_FWD / _REV = how many of them have
- * their neighbour records staged in shared memory by DW variants 6-8 (the others gather
- * directly); 0 before the first evaluation in that form. */
+/* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups of the staged layouts (256
+ * layout rows each, or 128 when 256-row groups would give every SM fewer than four),
+ * MFT_OPT_HALO_STAGED_FWD / _REV = how many of them have their neighbour records staged
+ * in shared memory by the staged gathers (the others gather directly); 0 before the first
+ * evaluation in the double-word or FP32 Euler form. */
 /* MFT_OPT_DW_VARIANT: kernel variant of the double-word gathers -- 0 one stencil entry
  * per loop iteration, 1 two entries per iteration with registers capped at six blocks per
  * SM, 2 two entries uncapped, 3 software-pipelined (indices two entries ahead, weights and
  * neighbour records one ahead), 4 and 5 = 1 and 2 with each warp's streamed index and
  * weight arrays prefetched into L2 eight slots ahead (one bulk prefetch per array),
- * 6 and 7 = 0 and 2 with the distinct neighbour records of each group of 256 layout rows
- * staged in shared memory by coalesced asynchronous copies and read from there (16-bit
+ * 6 and 7 = 0 and 2 with the distinct neighbour records of each group of 256 (or 128)
+ * layout rows staged in shared memory by coalesced asynchronous copies and read from there (16-bit
  * positions instead of the 32-bit indices; a group with more than 640 distinct
  * neighbours gathers directly; registers capped at three blocks per SM), 8 = 7 capped at
  * four blocks per SM, 9 and 11 = staged with four and three entries per iteration, 10 = 7
