@@ -240,7 +240,9 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
  * positions instead of the 32-bit indices; a group with more than 640 distinct
  * neighbours gathers directly; registers capped at three blocks per SM), 8 = 7 capped at
  * four blocks per SM, 9 and 11 = staged with four and three entries per iteration, 10 = 7
- * with the streamed position and weight arrays prefetched into L2 as in 4;
+ * with the streamed position and weight arrays prefetched into L2 as in 4, 12 = 7 with L2
+ * eviction-priority hints (streamed arrays evict-first, the intermediates the transpose
+ * gather reads back evict-last);
  * -1 (default) lets the autotuner time them at the first launch of each configuration.
  * Every variant forms the same sums in the same order (bit-identical results).
  * MFT_OPT_TUNED_FWD / MFT_OPT_TUNED_REV then report the variant in use. */

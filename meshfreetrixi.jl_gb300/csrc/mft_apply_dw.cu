@@ -106,12 +106,13 @@ static __device__ __forceinline__ FwdEntry fwd_load(const FwdArgs& a, const floa
 
 // The same entry with the neighbour's records read from the staged halo (lc: position
 // of the neighbour in the group's list).
-template <bool WT, bool WQ, int FLY>
+template <bool WT, bool WQ, int FLY, bool HINT = false>
 static __device__ __forceinline__ FwdEntry fwd_load_halo(const FwdArgs& a, const float4* sm,
-                                                         int hs, int64_t p, int lc) {
+                                                         int hs, int64_t p, int lc,
+                                                         uint64_t pol = 0) {
   FwdEntry e;
-  e.wx = __ldg(a.wdw[0] + p);
-  e.wy = __ldg(a.wdw[1] + p);
+  e.wx = HINT ? ldg_hint(a.wdw[0] + p, pol) : __ldg(a.wdw[0] + p);
+  e.wy = HINT ? ldg_hint(a.wdw[1] + p, pol) : __ldg(a.wdw[1] + p);
   e.fa.lo = sm[lc];
   e.fa.hi = sm[hs + lc];
   e.fb.lo = sm[2 * hs + lc];
@@ -120,7 +121,7 @@ static __device__ __forceinline__ FwdEntry fwd_load_halo(const FwdArgs& a, const
     e.uu.lo = sm[4 * hs + lc];
     e.uu.hi = sm[5 * hs + lc];
   }
-  if (WQ || FLY) e.wl = __ldg(a.wldw + p);
+  if (WQ || FLY) e.wl = HINT ? ldg_hint(a.wldw + p, pol) : __ldg(a.wldw + p);
   return e;
 }
 
@@ -163,8 +164,10 @@ static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, 
 // The variants form the same sums in the same order; the autotuner picks one.
 // HALO: blocks of one row group (ell.halo_rows rows) first stage the group's neighbour
 // records in shared memory and read them from there (groups without a list gather
-// directly); PIPE 0 or 2 then sets the loop's unrolling.
-template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO>
+// directly); PIPE 0 or 2 then sets the loop's unrolling.  HINT: the staged loop reads the
+// streamed positions and weights with an L2 evict-first policy and the epilogue writes t,
+// q and the partial du with evict-last, which the transpose gather reads next.
+template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO, bool HINT = false>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
   const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
@@ -205,11 +208,13 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
       prefetch_chunk(sa, s_lo, s_hi, 1);
     }
     constexpr int UNR = PIPE < 1 ? 1 : PIPE;
+    const uint64_t pol = HINT ? l2_evict_first() : 0;
 #pragma unroll UNR
     for (int j = 0; j < len; ++j) {
       if (pf_lane && (j % kPfSlots) == 0) prefetch_chunk(sa, s_lo, s_hi, j / kPfSlots + 2);
       const int64_t p = base + ((int64_t)j << 5);
-      fwd_accum<WT, WQ, FLY>(fwd_load_halo<WT, WQ, FLY>(a, hsm, hs, p, __ldg(lcol + p)), f, tx, ty, q);
+      const int lc = HINT ? ldg_hint(lcol + p, pol) : __ldg(lcol + p);
+      fwd_accum<WT, WQ, FLY>(fwd_load_halo<WT, WQ, FLY, HINT>(a, hsm, hs, p, lc, pol), f, tx, ty, q);
     }
   } else if (PIPE == 0) {
 #pragma unroll 1
@@ -282,18 +287,34 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
 #pragma unroll
       for (int v = 0; v < 4; ++v) { x[v] = dw::mul(e2, x[v]); y[v] = dw::mul(e2, y[v]); }
     }
-    t4[0] = make_float4(x[0].x, x[0].y, x[1].x, x[1].y);
-    t4[1] = make_float4(x[2].x, x[2].y, x[3].x, x[3].y);
-    t4[2] = make_float4(y[0].x, y[0].y, y[1].x, y[1].y);
-    t4[3] = make_float4(y[2].x, y[2].y, y[3].x, y[3].y);
+    const float4 o[4] = {make_float4(x[0].x, x[0].y, x[1].x, x[1].y),
+                         make_float4(x[2].x, x[2].y, x[3].x, x[3].y),
+                         make_float4(y[0].x, y[0].y, y[1].x, y[1].y),
+                         make_float4(y[2].x, y[2].y, y[3].x, y[3].y)};
+    if (HINT) {
+      const uint64_t keep = l2_evict_last();
+#pragma unroll
+      for (int k = 0; k < 4; ++k) st_hint(t4 + k, o[k], keep);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) t4[k] = o[k];
+    }
   }
   if (WQ) {
     float4* q4 = reinterpret_cast<float4*>(a.qdw) + i * 2;
     float2 x[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) x[v] = dw::to_pair(q[v]);
-    q4[0] = make_float4(x[0].x, x[0].y, x[1].x, x[1].y);
-    q4[1] = make_float4(x[2].x, x[2].y, x[3].x, x[3].y);
+    const float4 o0 = make_float4(x[0].x, x[0].y, x[1].x, x[1].y);
+    const float4 o1 = make_float4(x[2].x, x[2].y, x[3].x, x[3].y);
+    if (HINT) {
+      const uint64_t keep = l2_evict_last();
+      st_hint(q4, o0, keep);
+      st_hint(q4 + 1, o1, keep);
+    } else {
+      q4[0] = o0;
+      q4[1] = o1;
+    }
   }
   if (FLY == 2) {
     double2* h2 = reinterpret_cast<double2*>(a.hvf) + i * 2;
@@ -304,8 +325,14 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
     finish_node<4>(a.ep, i, du);
   } else {
     double2* d2 = reinterpret_cast<double2*>(a.du_p) + i * 2;
-    d2[0] = make_double2(du[0], du[1]);
-    d2[1] = make_double2(du[2], du[3]);
+    if (HINT) {
+      const uint64_t keep = l2_evict_last();
+      st_hint(d2, make_double2(du[0], du[1]), keep);
+      st_hint(d2 + 1, make_double2(du[2], du[3]), keep);
+    } else {
+      d2[0] = make_double2(du[0], du[1]);
+      d2[1] = make_double2(du[2], du[3]);
+    }
   }
 }
 
@@ -332,21 +359,22 @@ static __device__ __forceinline__ RevEntry rev_load(const RevArgs& a, const floa
   return e;
 }
 
-template <bool RV, bool LAP>
+template <bool RV, bool LAP, bool HINT = false>
 static __device__ __forceinline__ RevEntry rev_load_halo(const RevArgs& a, const float4* sm,
-                                                         int hs, int64_t p, int lc) {
+                                                         int hs, int64_t p, int lc,
+                                                         uint64_t pol = 0) {
   RevEntry e;
   constexpr int kq = RV ? 4 : 0;  // first chunk of the q record
   if (RV) {
-    e.wx = __ldg(a.wdw[0] + p);
-    e.wy = __ldg(a.wdw[1] + p);
+    e.wx = HINT ? ldg_hint(a.wdw[0] + p, pol) : __ldg(a.wdw[0] + p);
+    e.wy = HINT ? ldg_hint(a.wdw[1] + p, pol) : __ldg(a.wdw[1] + p);
     e.xa.lo = sm[lc];
     e.xa.hi = sm[hs + lc];
     e.ya.lo = sm[2 * hs + lc];
     e.ya.hi = sm[3 * hs + lc];
   }
   if (LAP) {
-    e.wl = __ldg(a.wldw + p);
+    e.wl = HINT ? ldg_hint(a.wldw + p, pol) : __ldg(a.wldw + p);
     e.qq.lo = sm[kq * hs + lc];
     e.qq.hi = sm[(kq + 1) * hs + lc];
   }
@@ -375,7 +403,7 @@ static __device__ __forceinline__ void rev_accum(const RevEntry& e, dw::Acc* sx,
 // Transpose gather (Euler) over the reverse adjacency, as k_rev_f64:
 // du_i = du_p_i - sum_j (Dx[j,i] s_x[j] + Dy[j,i] s_y[j]) - gamma sum_j lap[j,i] q[j],
 // with s = eps * t and q as double-word pairs.  PIPE and MINB as for k_fwd_euler_dw.
-template <bool RV, bool LAP, int PIPE, int MINB, bool PREF, bool HALO>
+template <bool RV, bool LAP, int PIPE, int MINB, bool PREF, bool HALO, bool HINT = false>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_dw(RevArgs a) {
   constexpr int NCH = (RV ? 4 : 0) + (LAP ? 2 : 0);
   const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
@@ -416,11 +444,13 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
       prefetch_chunk(sa, s_lo, s_hi, 1);
     }
     constexpr int UNR = PIPE < 1 ? 1 : PIPE;
+    const uint64_t pol = HINT ? l2_evict_first() : 0;
 #pragma unroll UNR
     for (int j = 0; j < len; ++j) {
       if (pf_lane && (j % kPfSlots) == 0) prefetch_chunk(sa, s_lo, s_hi, j / kPfSlots + 2);
       const int64_t p = base + ((int64_t)j << 5);
-      rev_accum<RV, LAP>(rev_load_halo<RV, LAP>(a, hsm, hs, p, __ldg(lcol + p)), sx, sy, sl);
+      const int lc = HINT ? ldg_hint(lcol + p, pol) : __ldg(lcol + p);
+      rev_accum<RV, LAP>(rev_load_halo<RV, LAP, HINT>(a, hsm, hs, p, lc, pol), sx, sy, sl);
     }
   } else if (PIPE == 0) {
 #pragma unroll 1
@@ -507,7 +537,9 @@ namespace {
 // 6 / 7 = neighbour records staged per row group in shared memory (one / two entries per
 // iteration, registers capped at three blocks of kHaloRows per SM), 8 = variant 7 capped
 // at four blocks, 9 / 11 = staged with four / three entries per iteration, 10 = variant 7
-// with the streamed position and weight arrays prefetched into L2 (as variant 4).  Without halos
+// with the streamed position and weight arrays prefetched into L2 (as variant 4), 12 =
+// variant 7 with L2 eviction-priority hints (streamed arrays evict-first; the forward
+// gather's t, q and partial du evict-last for the transpose gather).  Without halos
 // (not built) the staged variants run as variant 2.
 // A staged launch: one block per row group, NCH chunks of the layout's longest list
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
@@ -546,6 +578,7 @@ void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 9: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 4, 3, false, true>, a, nch, n, s); break;
     case 10: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, true, true>, a, nch, n, s); break;
     case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true>, a, nch, n, s); break;
+    case 12: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, true>, a, nch, n, s); break;
     default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }
@@ -567,6 +600,7 @@ void rev_variant(const RevArgs& a, int variant, int64_t n, cudaStream_t s) {
     case 9: launch_staged(k_rev_euler_dw<RV, LAP, 4, 3, false, true>, a, nch, n, s); break;
     case 10: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, true, true>, a, nch, n, s); break;
     case 11: launch_staged(k_rev_euler_dw<RV, LAP, 3, 3, false, true>, a, nch, n, s); break;
+    case 12: launch_staged(k_rev_euler_dw<RV, LAP, 2, 3, false, true, true>, a, nch, n, s); break;
     default: k_rev_euler_dw<RV, LAP, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
   }
 }

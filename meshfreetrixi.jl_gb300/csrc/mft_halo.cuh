@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 #include "mft_internal.cuh"
 
@@ -17,6 +18,43 @@ static __device__ __forceinline__ void cp_async16(float4* smem, const float4* gm
 }
 static __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// L2 eviction-priority hints (createpolicy + .L2::cache_hint): evict_first for the streamed
+// operator arrays, read once per launch, and evict_last for the intermediates a gather
+// writes for the next one (t, q, the partial du), so that the stream does not push the
+// intermediates out of L2 before they are read back.
+static __device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+static __device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+static __device__ __forceinline__ float2 ldg_hint(const float2* ptr, uint64_t pol) {
+  float2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;\n"
+      : "=f"(v.x), "=f"(v.y)
+      : "l"(ptr), "l"(pol));
+  return v;
+}
+static __device__ __forceinline__ int ldg_hint(const uint16_t* ptr, uint64_t pol) {
+  unsigned short v;
+  asm("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;\n" : "=h"(v) : "l"(ptr), "l"(pol));
+  return (int)v;
+}
+static __device__ __forceinline__ void st_hint(float4* ptr, float4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;\n"
+               ::"l"(ptr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol)
+               : "memory");
+}
+static __device__ __forceinline__ void st_hint(double2* ptr, double2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;\n"
+               ::"l"(ptr), "d"(v.x), "d"(v.y), "l"(pol)
+               : "memory");
 }
 
 // Stages the neighbour records of this block's row group (the group's halo list) into

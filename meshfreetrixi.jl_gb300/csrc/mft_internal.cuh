@@ -267,7 +267,7 @@ void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s);
 // variant: 0..5, the kernel variants the autotuner chooses among (same sums, same order)
-constexpr int kDwVariants = 12;
+constexpr int kDwVariants = 13;
 void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s);
 void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 

@@ -1,8 +1,8 @@
-"""The kernel variants of the double-word gathers (MFT_OPT_DW_VARIANT 0-11) form the same
+"""The kernel variants of the double-word gathers (MFT_OPT_DW_VARIANT 0-12) form the same
 sums in the same order, so one rhs! is bit-identical across them: the 2D Euler
 four-quadrant Riemann problem with residual viscosity (history estimate set) and Tominec
 hyperviscosity, which runs the forward gather with t and q and the transpose gather with
-both terms.  Three layouts exercise the staged variants (6-11): every row group's
+both terms.  Three layouts exercise the staged variants (6-12): every row group's
 neighbour records staged (Morton row order), none (a shuffled node order kept as the
 layout order: each group of rows then gathers from thousands of nodes), and a mix (a
 32 x 32 cloud in row order with its second half shuffled: the groups of the first half
@@ -53,7 +53,7 @@ def test_dw_variants_bit_identical(gpu_lib, layout):
     rng = np.random.default_rng(9)
     ctx.set_rv_state(du0 * (1.0 + 0.05 * rng.standard_normal(du0.shape)), 2)
     ref = None
-    for v in range(12):
+    for v in range(13):
         ctx.set_option(L.OPT_DW_VARIANT, v)
         du = np.empty_like(u0)
         ctx.rhs(du, u0.copy(), 0.0)
