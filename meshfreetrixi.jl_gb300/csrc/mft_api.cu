@@ -963,17 +963,7 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ProfScope ps(c, MFT_K_FWD);
     launch_fwd(c, fa);
   }
-  auto fire_after_visc = [&]() {
-    if (c->after_visc) {
-      const std::function<void()>* h = c->after_visc;
-      c->after_visc = nullptr;
-      (*h)();
-    }
-  };
-  if (fa.final_epilogue) {
-    fire_after_visc();
-    return;
-  }
+  if (fa.final_epilogue) return;
 
   RevArgs ra{};
   ra.n = n;
@@ -1039,7 +1029,6 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   r2.ep = ep;
   // the transpose gather applies the viscosity and hyperviscosity sources; its epilogue
   // is pass 2 of the boundary conditions and the stage combination
-  fire_after_visc();
   NvtxRange rng("source terms");
   ProfScope ps(c, MFT_K_REV);
   launch_rev(c, r2);
@@ -1183,15 +1172,11 @@ mft_status mft_ctx_create(mft_ctx** out, int device, int flags) {
       cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_tab, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_hfork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_hjoin, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_tab, cudaEventDisableTiming) != cudaSuccess) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
-    if (c->ev_tab) cudaEventDestroy(c->ev_tab);
-    if (c->ev_hfork) cudaEventDestroy(c->ev_hfork);
     delete c;
     return MFT_ERR_CUDA;
   }
@@ -1213,8 +1198,6 @@ mft_status mft_ctx_destroy(mft_ctx* c) {
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->ev_tab) cudaEventDestroy(c->ev_tab);
-  if (c->ev_hfork) cudaEventDestroy(c->ev_hfork);
-  if (c->ev_hjoin) cudaEventDestroy(c->ev_hjoin);
   if (c->h_tab) cudaFreeHost(c->h_tab);
   if (c->h_kerr) cudaFreeHost(c->h_kerr);
   for (auto& p : c->prof_pending) {
@@ -1776,8 +1759,7 @@ void fsal_eval(mft_ctx* c, double dt) {
 
 // Stages 2, 3 and the next step's first stage from u_n in buffer `un` (stage-3 state
 // into `u3`); `t` is the step start time.
-void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3,
-                  const std::function<void()>* stage1_after_visc = nullptr) {
+void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3) {
   Epilogue e2{};
   e2.kind = kStage2;
   e2.dt = dt;
@@ -1799,9 +1781,7 @@ void enqueue_step(mft_ctx* c, double dt, double t, int iu_n, int iu_3,
   e1.dt = dt;
   e1.out = c->U[1].p;
   e1.out32 = shadow(c, 1);
-  c->after_visc = stage1_after_visc;
   eval_rhs(c, c->U[iu_3].p, shadow(c, iu_3), t + dt, e1);
-  c->after_visc = nullptr;
   apply_limiter(c, c->U[1].p, shadow(c, 1));
 }
 
@@ -1851,35 +1831,13 @@ void capture_step_graphs(mft_ctx* c, double dt) {
     MFT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     c->capturing = true;
     try {
-      // The history push of u_{n+1} writes approx_du and a ring slot; the next step's first
-      // stage reads approx_du only in its viscosity, so the push runs on the side stream
-      // beside that stage's transpose gather and joins before the step ends.  Only without
-      // strong BCs: the stage epilogue re-projects u_{n+1} at slip walls, which the push
-      // must read afterwards.
-      const bool overlap = c->hist_order >= 0 && c->nb == 0;
-      bool hist_launched = false;
-      const std::function<void()> hist = [&]() {
-        MFT_CUDA(cudaEventRecord(c->ev_hfork, c->stream));
-        MFT_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_hfork, 0));
+      enqueue_step(c, dt, 0.0, iu_n, iu_3);
+      if (c->hist_order >= 0) {
         const double* ring[8];
         for (int k = 0; k < slots; ++k) ring[k] = c->hist[k].p;
         launch_history_dev((int64_t)c->n * c->nvars, c->U[iu_3].p, ring, slots, c->d_tab.p,
                            c->d_ctr.p, c->approx_du.p, c->precision == MFT_PREC_FP32,
-                           c->stream2);
-        MFT_CUDA(cudaEventRecord(c->ev_hjoin, c->stream2));
-        hist_launched = true;
-      };
-      enqueue_step(c, dt, 0.0, iu_n, iu_3, overlap ? &hist : nullptr);
-      if (c->hist_order >= 0) {
-        if (hist_launched) {
-          MFT_CUDA(cudaStreamWaitEvent(c->stream, c->ev_hjoin, 0));
-        } else {
-          const double* ring[8];
-          for (int k = 0; k < slots; ++k) ring[k] = c->hist[k].p;
-          launch_history_dev((int64_t)c->n * c->nvars, c->U[iu_3].p, ring, slots, c->d_tab.p,
-                             c->d_ctr.p, c->approx_du.p, c->precision == MFT_PREC_FP32,
-                             c->stream);
-        }
+                           c->stream);
       }
       launch_step_advance(c->d_ctr.p, c->stream);
     } catch (...) {

@@ -4,7 +4,6 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
-#include <functional>
 #include <string>
 #include <vector>
 
@@ -170,10 +169,6 @@ struct mft_ctx {
   // side stream for the residual-viscosity reductions (overlap with the gathers)
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  cudaEvent_t ev_hfork = nullptr, ev_hjoin = nullptr;  // history push beside the last gather
-  // called once by the next rhs! evaluation when the work that reads approx_du (the
-  // viscosity) has been enqueued, before its last gather (graph capture of a step)
-  const std::function<void()>* after_visc = nullptr;
 
   // timing
   bool prof_on = false;
