@@ -192,11 +192,6 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
   }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (HINT && a.fuse_eps) {
-    // the epilogue's viscosity reads the node's state and history estimate
-    prefetch_l2(a.ea.u + i * 4);
-    prefetch_l2(a.ea.approx_du + i * 4);
-  }
   if (HALO && staged) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
@@ -433,14 +428,6 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
   for (int v = 0; v < 4; ++v) { sx[v] = dw::zero(); sy[v] = dw::zero(); sl[v] = dw::zero(); }
   const uint16_t* __restrict__ lcol = a.ell.lcol;
   const int hs = a.ell.halo_stride;
-  if (HINT) {
-    // the epilogue's partial du and stage states
-    prefetch_l2(a.du_p + i * 4);
-    if (a.final_epilogue) {
-      prefetch_l2(a.ep.u_s + i * 4);
-      if (a.ep.kind == kStage2 || a.ep.kind == kStage3) prefetch_l2(a.ep.u_n + i * 4);
-    }
-  }
   if (HALO && staged) {
     SliceArrays sa{};
     int64_t s_lo = 0, s_hi = 0;
@@ -552,8 +539,7 @@ namespace {
 // at four blocks, 9 / 11 = staged with four / three entries per iteration, 10 = variant 7
 // with the streamed position and weight arrays prefetched into L2 (as variant 4), 12 =
 // variant 7 with L2 eviction-priority hints (streamed arrays evict-first; the forward
-// gather's t, q and partial du evict-last for the transpose gather) and the epilogue's
-// per-node inputs requested into L2 when the row starts.  Without halos
+// gather's t, q and partial du evict-last for the transpose gather).  Without halos
 // (not built) the staged variants run as variant 2.
 // A staged launch: one block per row group, NCH chunks of the layout's longest list
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per

@@ -57,12 +57,6 @@ static __device__ __forceinline__ void st_hint(double2* ptr, double2 v, uint64_t
                : "memory");
 }
 
-// Requests the line holding p into L2 (no register result): the per-node inputs of a
-// gather's epilogue are requested when the row starts, so they arrive while it gathers.
-static __device__ __forceinline__ void prefetch_l2(const void* p) {
-  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
-}
-
 // Stages the neighbour records of this block's row group (the group's halo list) into
 // shared memory: NCH 16-byte chunks per record, chunk k of list entry q at
 // sm[k * ell.halo_stride + q] (chunk-major, so that lanes reading one chunk of different
