@@ -27,6 +27,32 @@ def jittered_grid(nx, ny, lo=(0.0, 0.0), hi=(1.0, 1.0), jitter=0.25, seed=SEED):
     return np.ascontiguousarray(np.stack([x, y], axis=1)), (hx, hy)
 
 
+def jittered_grid3(n, lo=0.0, hi=1.0, jitter=0.25, seed=SEED):
+    """Cell-centred n x n x n grid on the cube [lo, hi]^3 with uniform jitter of
+    +-jitter*h per axis (x fastest)."""
+    g = rng(seed)
+    h = (hi - lo) / n
+    i, j, k = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    base = np.stack([k.ravel(), j.ravel(), i.ravel()], axis=1)
+    pts = lo + (base + 0.5) * h + g.uniform(-jitter * h, jitter * h, base.shape)
+    return np.ascontiguousarray(pts), h
+
+
+def euler3d_wave(x, gamma=1.4):
+    """A smooth 3D Euler state on the periodic unit cube: density and pressure waves with
+    a swirling velocity (every component varies in every direction)."""
+    tp = 2.0 * np.pi
+    s = [np.sin(tp * x[:, d]) for d in range(3)]
+    c = [np.cos(tp * x[:, d]) for d in range(3)]
+    rho = 1.0 + 0.2 * s[0] * c[1] + 0.1 * s[2]
+    v1 = 0.3 + 0.1 * s[1] * c[2]
+    v2 = -0.2 + 0.1 * s[2] * c[0]
+    v3 = 0.1 + 0.1 * s[0] * c[1]
+    p = 1.0 + 0.1 * c[0] * s[1] * c[2]
+    e = p / (gamma - 1.0) + 0.5 * rho * (v1 * v1 + v2 * v2 + v3 * v3)
+    return np.ascontiguousarray(np.stack([rho, rho * v1, rho * v2, rho * v3, e]))
+
+
 # ------------------------------------------------------------------ scalar advection
 
 

@@ -853,6 +853,20 @@ int mfto_ata(const mfto_csr* a, int64_t* hrp, int32_t* hci, double* hval, int nt
 /* ------------------------------------------------------------------------ */
 
 static void flux_point(const mfto_semi* s, const double* uu, int d, double* f) {
+  if (s->eq == MFTO_EQ_EULER3D) {
+    /* Trixi's CompressibleEulerEquations3D flux (textbook form) in direction d */
+    double rho = uu[0], m1 = uu[1], m2 = uu[2], m3 = uu[3], en = uu[4];
+    double v1 = m1 / rho, v2 = m2 / rho, v3 = m3 / rho;
+    double p = (s->gamma - 1.0) * (en - 0.5 * (m1 * v1 + m2 * v2 + m3 * v3));
+    double m = d == 0 ? m1 : (d == 1 ? m2 : m3);
+    double vd = d == 0 ? v1 : (d == 1 ? v2 : v3);
+    f[0] = m;
+    f[1] = m * v1 + (d == 0 ? p : 0.0);
+    f[2] = m * v2 + (d == 1 ? p : 0.0);
+    f[3] = m * v3 + (d == 2 ? p : 0.0);
+    f[4] = (en + p) * vd;
+    return;
+  }
   if (s->eq == MFTO_EQ_EULER2D) {
     double rho = uu[0], m1 = uu[1], m2 = uu[2], en = uu[3];
     double v1 = m1 / rho, v2 = m2 / rho;
@@ -1118,6 +1132,14 @@ int mfto_rhs(const mfto_semi* s, double t, const double* dirichlet, double* cons
              double* const* u, double* eps_out, mfto_rv_diag* diag, int nthreads) {
   (void)t;
   int V = s->nvars;
+  /* 3D Euler: the plain flux divergence with Dirichlet / do-nothing BCs -- the reference's
+   * viscosity sources and slip walls are written for CompressibleEulerEquations2D
+   * (hyperviscosity.jl:246-329, PointCloudBCs.jl:15-21) */
+  if (s->eq == MFTO_EQ_EULER3D) {
+    if (s->n_src > 0) return -1;
+    for (int b = 0; b < s->n_bc; ++b)
+      if (s->bc_kind[b] == MFTO_BC_SLIP_WALL) return -1;
+  }
   for (int v = 0; v < V; ++v) memset(du[v], 0, (size_t)s->n * sizeof(double));
   bc_pass(s, dirichlet, du, u);
   int rc = mfto_calc_fluxes(s, du, u, nthreads);

@@ -74,7 +74,7 @@ int mfto_saddle_system(int dim, const double* x, const double* period, const int
 int mfto_bk_solve(int n, double* a, int nrhs, double* b);
 
 /* Equation kinds and boundary-condition kinds. */
-enum { MFTO_EQ_EULER2D = 0, MFTO_EQ_ADVECTION = 1 };
+enum { MFTO_EQ_EULER2D = 0, MFTO_EQ_ADVECTION = 1, MFTO_EQ_EULER3D = 2 };
 enum { MFTO_BC_DIRICHLET = 0, MFTO_BC_SLIP_WALL = 1, MFTO_BC_DO_NOTHING = 2 };
 enum { MFTO_SRC_RV = 0, MFTO_SRC_UPWIND = 1, MFTO_SRC_HV_TOMINEC = 2, MFTO_SRC_HV_FLYER = 3,
        MFTO_SRC_IGR = 4 };

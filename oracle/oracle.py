@@ -22,7 +22,7 @@ I32P = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 I64P = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 F64P = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
-EQ_EULER2D, EQ_ADVECTION = 0, 1
+EQ_EULER2D, EQ_ADVECTION, EQ_EULER3D = 0, 1, 2
 BC_DIRICHLET, BC_SLIP_WALL, BC_DO_NOTHING = 0, 1, 2
 SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER, SRC_IGR = 0, 1, 2, 3, 4
 
@@ -351,8 +351,8 @@ class Semi:
         self.points = np.ascontiguousarray(points, dtype=np.float64)
         self.n, self.dim = self.points.shape
         self.ops = list(ops)
-        self.eq = EQ_EULER2D if eq == "euler" else EQ_ADVECTION
-        self.nvars = 4 if self.eq == EQ_EULER2D else 1
+        self.eq = {"euler": EQ_EULER2D, "advection": EQ_ADVECTION, "euler3d": EQ_EULER3D}[eq]
+        self.nvars = {EQ_EULER2D: 4, EQ_ADVECTION: 1, EQ_EULER3D: 5}[self.eq]
         self.bcs = list(bcs)
         kinds, ptr, idx, nrm = [], [0], [], []
         for kind, ii, normals, _fn in self.bcs:

@@ -74,6 +74,16 @@ def flux_np(u, d, gamma=GAMMA):
     return np.stack([m2, m2 * v1, m2 * v2 + p, (e + p) * v2])
 
 
+def flux3d_np(u, d, gamma=GAMMA):
+    """CompressibleEulerEquations3D flux in direction d (textbook form)."""
+    rho, m1, m2, m3, e = u
+    v = [m1 / rho, m2 / rho, m3 / rho]
+    m = [m1, m2, m3]
+    p = (gamma - 1.0) * (e - 0.5 * (m1 * v[0] + m2 * v[1] + m3 * v[2]))
+    f = [m[d]] + [m[d] * v[k] + (p if k == d else 0.0) for k in range(3)] + [(e + p) * v[d]]
+    return np.stack(f)
+
+
 def cond_scale(ops, u, fluxes=None, eps=None, lap=None, hv_gamma=0.0, hvop=None):
     """Per-variable condition scale  |D||F| + sum_d |D_d|'(|eps| |D_d||u|)
     + gamma |lap|'|lap||u| (+ gamma |H||u|), max over nodes."""
