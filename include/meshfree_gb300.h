@@ -45,7 +45,7 @@ enum {
 };
 
 /* Equation kinds (Trixi equation types used with point clouds). */
-enum { MFT_EQ_EULER2D = 0, MFT_EQ_ADVECTION = 1 };
+enum { MFT_EQ_EULER2D = 0, MFT_EQ_ADVECTION = 1, MFT_EQ_EULER3D = 2 };
 
 /* Boundary-condition kinds (src/equations/PointCloudBCs.jl). */
 enum { MFT_BC_DIRICHLET = 0, MFT_BC_SLIP_WALL = 1, MFT_BC_DO_NOTHING = 2 };
@@ -168,9 +168,14 @@ mft_status mft_load_csc(mft_ctx* ctx, int op, int comp, int64_t n, const int64_t
 
 /* ---------------------------------------------------------------- physics */
 
-/* kind MFT_EQ_EULER2D: params[0] = gamma (CompressibleEulerEquations2D);
- * kind MFT_EQ_ADVECTION: params[0..dim-1] = advection velocity
- * (LinearScalarAdvectionEquation2D). */
+/* kind MFT_EQ_EULER2D: params[0] = gamma (CompressibleEulerEquations2D, 2D clouds);
+ * kind MFT_EQ_EULER3D: params[0] = gamma (CompressibleEulerEquations3D, 3D clouds, 5
+ * variables);  kind MFT_EQ_ADVECTION: params[0..dim-1] = advection velocity
+ * (LinearScalarAdvectionEquation2D / 3D).  On 3D clouds rhs! is the plain flux divergence
+ * (calc_fluxes! over D_x, D_y, D_z, rbfsolver.jl:247-265) with Dirichlet and do-nothing
+ * BCs, in the FP64 form (FP64 fused multiply-adds): the reference's viscosity sources,
+ * slip walls, positivity limiter and IGR are written for the 2D Euler equations, and an
+ * rhs! on a 3D cloud with any of them returns MFT_ERR_UNSUPPORTED, as does the adjoint. */
 mft_status mft_set_equations(mft_ctx* ctx, int kind, const double* params);
 
 /* Boundary conditions in the order of the reference's NamedTuple

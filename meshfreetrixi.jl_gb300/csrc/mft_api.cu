@@ -361,7 +361,7 @@ void ensure_work(mft_ctx* c) {
   MFT_REQUIRE(V > 0, MFT_ERR_STATE, "equations not set");
   const size_t nv = (size_t)n * V;
   for (auto* b : {&c->U[0], &c->U[1], &c->U[2], &c->U[3]}) b->alloc(nv);
-  c->F.alloc((size_t)n * 2 * V);
+  c->F.alloc((size_t)n * std::max(c->dim, 2) * V);
   c->du_p.alloc(nv);
   c->du_p2.alloc(nv);
   c->t.alloc((size_t)n * 2 * V);
@@ -506,6 +506,10 @@ static void ensure_bcs(mft_ctx* c) {
     for (int64_t p = c->bc_ptr[b]; p < c->bc_ptr[b + 1]; ++p) {
       const int32_t i = c->bc_idx[p];
       if (k == MFT_BC_DO_NOTHING) continue;
+      // apply_slip_velocity is written for CompressibleEulerEquations2D
+      // (PointCloudBCs.jl:15-21); scalar advection ignores slip walls
+      MFT_REQUIRE(!(k == MFT_BC_SLIP_WALL && c->eq == MFT_EQ_EULER3D), MFT_ERR_UNSUPPORTED,
+                  "slip walls: 2D Euler only");
       if (k == MFT_BC_SLIP_WALL && c->eq != MFT_EQ_EULER2D) continue;
       MFT_REQUIRE(tag[i] == 0, MFT_ERR_UNSUPPORTED,
                   "node " + std::to_string(i) + " carries two active boundary conditions");
@@ -787,6 +791,38 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
       MFT_REQUIRE(ih < 0, MFT_ERR_UNSUPPORTED, "more than one hyperviscosity source");
       ih = (int)k;
     }
+  }
+  if (c->dim == 3) {
+    // 3D clouds: the plain flux divergence (calc_fluxes! over D_x, D_y, D_z) with the
+    // strong BCs and the stage epilogue, in FP64 fused multiply-adds
+    MFT_REQUIRE(!f32, MFT_ERR_UNSUPPORTED, "3D point clouds: the FP64 form only");
+    MFT_REQUIRE(iv < 0 && ih < 0 && ig < 0, MFT_ERR_UNSUPPORTED,
+                "3D point clouds: no viscosity, hyperviscosity or IGR source (the "
+                "reference writes them for the 2D Euler equations)");
+    MFT_REQUIRE(c->have_val[2], MFT_ERR_STATE, "gradient operator component 2 not set");
+    FwdArgs fa{};
+    fa.n = n;
+    fa.ell = c->fwd.view();
+    for (int d = 0; d < 3; ++d) fa.w[d] = c->fw[d].p;
+    fa.F = c->F.p;
+    fa.u = us;
+    fa.eq = c->eq;
+    fa.V = V;
+    fa.gamma = c->gamma;
+    fa.ax = c->adv[0];
+    fa.ay = c->adv[1];
+    fa.az = c->adv[2];
+    fa.final_epilogue = 1;
+    fa.ep = ep;
+    if (c->eq == MFT_EQ_EULER3D) {
+      NvtxRange rng("calc fluxes");
+      ProfScope ps(c, MFT_K_FLUX);
+      launch_flux_euler3d(n, c->gamma, us, c->F.p, s);
+    }
+    NvtxRange rng("calc fluxes");
+    ProfScope ps(c, MFT_K_FWD);
+    launch_fwd3(fa, s);
+    return;
   }
   const bool tominec = ih >= 0 && c->src_kind[ih] == MFT_SRC_HV_TOMINEC;
   const bool flyer = ih >= 0 && c->src_kind[ih] == MFT_SRC_HV_FLYER;
@@ -1387,10 +1423,17 @@ mft_status mft_set_equations(mft_ctx* c, int kind, const double* params) {
   return guarded(c, [&] {
     c->graph_valid = false;
     MFT_REQUIRE(params, MFT_ERR_ARG, "params is NULL");
-    MFT_REQUIRE(c->dim == 2, MFT_ERR_UNSUPPORTED, "the rhs! engine covers 2D point clouds");
+    MFT_REQUIRE(c->dim == 2 || c->dim == 3, MFT_ERR_UNSUPPORTED,
+                "the rhs! engine covers 2D and 3D point clouds");
     if (kind == MFT_EQ_EULER2D) {
+      MFT_REQUIRE(c->dim == 2, MFT_ERR_ARG, "CompressibleEulerEquations2D needs a 2D cloud");
       c->eq = kind;
       c->nvars = 4;
+      c->gamma = params[0];
+    } else if (kind == MFT_EQ_EULER3D) {
+      MFT_REQUIRE(c->dim == 3, MFT_ERR_ARG, "CompressibleEulerEquations3D needs a 3D cloud");
+      c->eq = kind;
+      c->nvars = 5;
       c->gamma = params[0];
     } else if (kind == MFT_EQ_ADVECTION) {
       c->eq = kind;

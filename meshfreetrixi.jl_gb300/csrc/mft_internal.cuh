@@ -225,15 +225,15 @@ void prepare_eps(EpsArgs& a);
 struct FwdArgs {
   int64_t n;
   EllView ell;
-  const double* w[3];   // grad components (x, y)
+  const double* w[3];   // grad components (x, y, z)
   const double* wl;     // lap (Tominec) or H (Flyer) weights, or null
   const float* w32[3];
   const float* wl32;
-  const double* F;      // n x 2V fluxes (Euler FP64)
+  const double* F;      // n x 2V fluxes (Euler FP64; n x 3V on 3D clouds)
   const double* u;      // n x V state (FP64)
   const float* u32;     // n x V state (FP32 path)
   int eq, V;
-  double gamma, ax, ay;
+  double gamma, ax, ay, az;
   double hv_gamma;      // Flyer: du += -gamma * H u
   float gm1_32, hg32;   // (float)(gamma - 1), (float) hv_gamma (FP32 kernels; set by the launchers)
   int want_t;           // write t = D u (n x 2V)
@@ -262,6 +262,11 @@ struct FwdArgs {
   EpsArgs ea;
 };
 void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
+// 3D clouds (mft_apply3d.cu): per-node Euler fluxes F = (F_x, F_y, F_z) (n x 15), and the
+// plain flux divergence -sum_d D_d F_d with the stage epilogue (V = 5, Euler; V = 1,
+// advection with the flux a_d u formed at the neighbour).
+void launch_flux_euler3d(int64_t n, double gamma, const double* u, double* F, cudaStream_t s);
+void launch_fwd3(const FwdArgs& a, cudaStream_t s);
 // Double-word forms (mft_apply_dw.cu): per-node flux and state pairs, forward gather,
 // transpose gather.
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,

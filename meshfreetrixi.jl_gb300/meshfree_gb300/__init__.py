@@ -3,7 +3,8 @@ MeshfreeTrixi.jl, with a host API that mirrors the reference's point-cloud API."
 from ._lib import Context, MFTError, load  # noqa: F401
 from .api import (  # noqa: F401
     RBF, BoundaryConditionDirichlet, BoundaryConditionDoNothing, BoundaryData,
-    CompressibleEulerEquations2D, HistoryCallback, LinearScalarAdvectionEquation2D, ODEProblem,
+    CompressibleEulerEquations2D, CompressibleEulerEquations3D, HistoryCallback,
+    LinearScalarAdvectionEquation2D, LinearScalarAdvectionEquation3D, ODEProblem,
     Point1D, Point2D, Point3D, PointCloudBasis, PositivityPreservingLimiterZhangShu, density, pressure, PointCloudDomain, PointCloudDomain_from_medusa,
     PointCloudEnsemble, PointCloudSolver, PointData, PolyharmonicSpline, RBFFDEngineGB300, RBFSolver, RefPointData,
     SemidiscretizationHyperbolic, SourceHyperviscosityFlyer, SourceHyperviscosityTominec, SourceIGR,

@@ -16,7 +16,7 @@ LIB_PATH = Path(os.environ.get("MFT_LIBRARY", PKG / "lib" / "libmeshfree_gb300.s
 
 MFT_OK, MFT_ERR_ARG, MFT_ERR_CUDA, MFT_ERR_STATE, MFT_ERR_SINGULAR = 0, 1, 2, 3, 4
 MFT_ERR_NONFINITE, MFT_ERR_TIMEOUT, MFT_ERR_UNSUPPORTED, MFT_ERR_NOMEM = 5, 6, 7, 8
-EQ_EULER2D, EQ_ADVECTION = 0, 1
+EQ_EULER2D, EQ_ADVECTION, EQ_EULER3D = 0, 1, 2
 BC_DIRICHLET, BC_SLIP_WALL, BC_DO_NOTHING = 0, 1, 2
 SRC_RV, SRC_UPWIND, SRC_HV_TOMINEC, SRC_HV_FLYER, SRC_IGR = 0, 1, 2, 3, 4
 OP_GRAD, OP_LAP, OP_HV = 0, 1, 2
@@ -199,7 +199,7 @@ class Context:
     def set_equations(self, kind, params):
         p = np.ascontiguousarray(params, dtype=np.float64)
         self.check(self.lib.mft_set_equations(self.h, kind, _p(p)))
-        self.nvars = 4 if kind == EQ_EULER2D else 1
+        self.nvars = {EQ_EULER2D: 4, EQ_EULER3D: 5}.get(kind, 1)
 
     def set_bcs(self, kinds, ptr, idx, normals):
         k = np.ascontiguousarray(kinds, dtype=np.int32)

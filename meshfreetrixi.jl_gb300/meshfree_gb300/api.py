@@ -229,8 +229,42 @@ class CompressibleEulerEquations2D:
 
 
 @dataclass
+class CompressibleEulerEquations3D:
+    """Trixi's CompressibleEulerEquations3D (rho, rho v1, rho v2, rho v3, E).  On 3D clouds
+    the engine evaluates the plain flux divergence with Dirichlet / do-nothing BCs (the
+    reference's viscosity sources and slip walls are 2D-only)."""
+    gamma: float = 1.4
+    nvariables = 5
+    kind = L.EQ_EULER3D
+
+    def params(self):
+        return [self.gamma]
+
+    def cons2prim(self, u):
+        rho, m1, m2, m3, e = u
+        v1, v2, v3 = m1 / rho, m2 / rho, m3 / rho
+        p = (self.gamma - 1.0) * (e - 0.5 * (m1 * v1 + m2 * v2 + m3 * v3))
+        return np.stack([rho, v1, v2, v3, p])
+
+    def prim2cons(self, w):
+        rho, v1, v2, v3, p = w
+        return np.stack([rho, rho * v1, rho * v2, rho * v3,
+                         p / (self.gamma - 1.0) + 0.5 * rho * (v1 * v1 + v2 * v2 + v3 * v3)])
+
+
+@dataclass
 class LinearScalarAdvectionEquation2D:
     advection_velocity: tuple = (1.0, 0.5)
+    nvariables = 1
+    kind = L.EQ_ADVECTION
+
+    def params(self):
+        return list(self.advection_velocity)
+
+
+@dataclass
+class LinearScalarAdvectionEquation3D:
+    advection_velocity: tuple = (1.0, 0.5, 0.25)
     nvariables = 1
     kind = L.EQ_ADVECTION
 
