@@ -76,7 +76,7 @@ def parse():
                     help="members of the ensemble measurement (0 skips it)")
     ap.add_argument("--only", default="all",
                     choices=["all", "adjoint", "riemann", "weights", "igr", "fp32", "setup",
-                             "rates", "dw", "dfma", "vortex"],
+                             "rates", "dw", "dfma", "vortex", "euler3d"],
                     help="run one auxiliary measurement alone")
     ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged", "halo"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
@@ -84,6 +84,8 @@ def parse():
                     help="double-word gather kernel variant of the dw/dfma measurements "
                          "(-1: autotuned; 0..5 fixed, e.g. for profiling one kernel)")
     ap.add_argument("--igr", type=int, default=1, help="1 runs the IGR-source measurement")
+    ap.add_argument("--euler3d-side", type=int, default=64,
+                    help="cube side of the 3D Euler measurement (0 skips it)")
     ap.add_argument("--setup", type=int, default=1,
                     help="1 runs the set-up measurement (KNN and weights of the vortex cloud)")
     ap.add_argument("--weights-n", type=int, default=1048576,
@@ -554,6 +556,50 @@ def run_igr(args, local):
     return out
 
 
+def run_euler3d(args, local, peaks):
+    """CompressibleEulerEquations3D on a periodic jittered cube (N = side^3, PHS r^3 +
+    degree 2, k = 30): the plain flux divergence in FP64, SSP-RK3 steps with per-step
+    graphs; the gather's HBM roofline by the same convention (k indices, 3 k weights, the
+    state and the flux record of the node, the stage's u_n / u_s / out)."""
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    side = args.euler3d_side
+    pts, h = W.jittered_grid3(side, seed=11)
+    n = pts.shape[0]
+    k = 30
+    basis = M.PointCloudBasis(M.Point3D(), 2, nv=k)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(device=local, precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=(1.0, 1.0, 1.0))
+    eq = M.CompressibleEulerEquations3D(1.4)
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.euler3d_wave(x), solver)
+    ctx = dom.ctx
+    u0 = semi.compute_coefficients(0.0)
+    dt = 0.1 * h
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, args.warmup, use_graph=True)
+    ctx.region_begin()
+    ctx.ssprk33(dt, args.steps, use_graph=True)
+    ms = ctx.region_end()
+    ctx.profile(True)
+    ctx.ssprk33(dt, args.steps, use_graph=False)
+    prof = ctx.profile_report()
+    ctx.profile(False)
+    ctx.close()
+    fwd_ms, fwd_n = prof.get("fwd_gather", (0.0, 0))
+    per = fwd_ms / max(fwd_n, 1)
+    # per node: indices 4k, weights 3*8k, flux record 120 + state 40 in, stage in/out 80
+    bytes_node = 4 * k + 24 * k + 120 + 40 + 80
+    return {"workload": "CompressibleEulerEquations3D, periodic unit cube, N=%d jittered nodes, "
+                        "PHS r^3 + degree-2 polynomials, k=%d, plain flux divergence (FP64), "
+                        "SSP-RK3 dt=0.1h, per-step graphs" % (n, k),
+            "nodes": n, "value": n * RHS_PER_STEP * args.steps / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms / args.steps, "kernels": _kernels(prof),
+            "fwd_gather_gbs": bytes_node * n / (per * 1e-3) / 1e9 if fwd_n else None,
+            "fwd_gather_hbm_frac": (bytes_node * n / (per * 1e-3) / 1e9) / peaks["hbm_gbs"]
+            if fwd_n else None,
+            "algorithmic_bytes_per_node": bytes_node}
+
+
 def run_adjoint(args, local, peaks):
     """Gradient of J = 0.5 |rho(T) - rho*|^2 w.r.t. u0 for the isentropic vortex at
     N = 65,536 (T = 0.5, 500 SSP-RK3 steps; rho* the exact density at T plus seeded
@@ -959,6 +1005,7 @@ def run_ours(args):
                     "dw": lambda: run_one_form(args, local, peaks, "fp64", "dw"),
                     "dfma": lambda: run_one_form(args, local, peaks, "fp64", "dfma"),
                     "vortex": lambda: run_vortex(args, local, peaks),
+                    "euler3d": lambda: run_euler3d(args, local, peaks),
                     "setup": lambda: run_setup(args, local),
                     "rates": lambda: {k: v / 1e9 for k, v in peaks["fma_rates"].items()}}
             leg = legs[args.only]()
@@ -1023,6 +1070,7 @@ def run_ours(args):
     rie = run_riemann(args, local) if args.riemann_side > 0 and rank == 0 else None
     wts = run_weights(args, local) if args.weights_n > 0 and rank == 0 else None
     igr = run_igr(args, local) if args.igr and rank == 0 else None
+    e3d = run_euler3d(args, local, peaks) if args.euler3d_side > 0 and rank == 0 else None
     setup = run_setup(args, local) if args.setup and rank == 0 else None
 
     cpu = None
@@ -1069,6 +1117,7 @@ def run_ours(args):
         "riemann_to_t02": rie,
         "weights_batch": wts,
         "igr": igr,
+        "euler3d": e3d,
         "setup": setup,
     }
     print(json.dumps(line), flush=True)
