@@ -399,6 +399,7 @@ void ensure_work(mft_ctx* c) {
     c->tdw.alloc((size_t)n * 2 * V);
     c->qdw.alloc(nv);
   }
+  if (use_dw3(c)) c->Fdw.alloc((size_t)n * 16);  // 15 flux pairs per node, padded to 128 B
   if (c->precision == MFT_PREC_FP32) {
     for (auto* b : {&c->U32[0], &c->U32[1], &c->U32[2], &c->U32[3]}) b->alloc(nv);
     c->du_p32.alloc(nv);
@@ -426,11 +427,11 @@ void ensure_device_ops(mft_ctx* c) {
   const bool spatial = c->layout_order == 1 && !c->xyz.empty();
   if (c->fwd.n == c->n && c->fwd.ordered != spatial) c->dev_dirty = true;
   // double-word operator values are placed only while that form is in use
-  const bool dw = use_dw(c);
+  const bool dw = use_dw(c) || use_dw3(c);
   if (dw && !c->fwdw[0].p) c->dev_dirty = true;
-  // neighbour halos of the row groups, for the staged gathers (double-word and FP32
+  // neighbour halos of the row groups, for the staged gathers (double-word and FP32 2D
   // Euler forms)
-  const bool halo = dw || (c->precision == MFT_PREC_FP32 && c->eq == MFT_EQ_EULER2D);
+  const bool halo = use_dw(c) || (c->precision == MFT_PREC_FP32 && c->eq == MFT_EQ_EULER2D);
   if (halo && !c->fwd.halo_off.p) c->dev_dirty = true;
   // 256-row groups when that still gives every SM several blocks, else 128
   int nsm = 0;
@@ -814,6 +815,22 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     fa.az = c->adv[2];
     fa.final_epilogue = 1;
     fa.ep = ep;
+    if (use_dw3(c)) {
+      // double-word form: flux pairs per node, sums of double-word products
+      MFT_REQUIRE(c->Fdw.p && c->fwdw[0].p && c->fwdw[1].p && c->fwdw[2].p, MFT_ERR_STATE,
+                  "double-word 3D buffers not allocated");
+      for (int d = 0; d < 3; ++d) fa.wdw[d] = c->fwdw[d].p;
+      fa.Fdw = c->Fdw.p;
+      {
+        NvtxRange rng("calc fluxes");
+        ProfScope ps(c, MFT_K_FLUX);
+        launch_prep_euler3d_dw(n, c->gamma, us, c->Fdw.p, s);
+      }
+      NvtxRange rng("calc fluxes");
+      ProfScope ps(c, MFT_K_FWD);
+      launch_fwd3_dw(fa, s);
+      return;
+    }
     if (c->eq == MFT_EQ_EULER3D) {
       NvtxRange rng("calc fluxes");
       ProfScope ps(c, MFT_K_FLUX);
@@ -2114,7 +2131,7 @@ uint64_t fnv1a64(const unsigned char* p, size_t n) {
   return h;
 }
 
-int ckpt_form(const mft_ctx* c) { return c->precision * 4 + (use_dw(c) ? 1 : 0); }
+int ckpt_form(const mft_ctx* c) { return c->precision * 4 + (use_dw(c) || use_dw3(c) ? 1 : 0); }
 
 size_t ckpt_bytes(const mft_ctx* c) {
   const size_t nvb = (size_t)c->n * c->nvars * sizeof(double);

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "mft_device.cuh"
+#include "mft_dw.cuh"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -85,7 +86,96 @@ __global__ void __launch_bounds__(kBlock) k_fwd3_f64(FwdArgs a) {
   finish_node<V>(a.ep, i, du);
 }
 
+// Double-word form: the state split into pairs and the flux formed in double-word
+// arithmetic (one reciprocal of rho refined by a Newton step), F[i] = 16 pairs (F_x, F_y,
+// F_z, 5 each, then a zero pad).  The only FP64 operations are the five splits.
+__global__ void k_prep_euler3d_dw(int64_t n, float2 gm1, const double* __restrict__ u,
+                                  float4* __restrict__ F) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* ui = u + i * 5;
+  const float2 rho = dw::split(ui[0]), en = dw::split(ui[4]);
+  const float2 m[3] = {dw::split(ui[1]), dw::split(ui[2]), dw::split(ui[3])};
+  const float2 r = dw::recip(rho);
+  const float2 v[3] = {dw::mul(m[0], r), dw::mul(m[1], r), dw::mul(m[2], r)};
+  const float2 mv = dw::add(dw::add(dw::mul(m[0], v[0]), dw::mul(m[1], v[1])), dw::mul(m[2], v[2]));
+  const float2 p = dw::mul(gm1, dw::add(en, dw::neg(dw::scale2(mv, 0.5f))));
+  const float2 ep = dw::add(en, p);
+  float2 f[16];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    f[d * 5 + 0] = m[d];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float2 mk = dw::mul(m[d], v[k]);
+      f[d * 5 + 1 + k] = k == d ? dw::add(mk, p) : mk;
+    }
+    f[d * 5 + 4] = dw::mul(ep, v[d]);
+  }
+  f[15] = make_float2(0.f, 0.f);
+  float4* Fi = F + i * 8;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) Fi[q] = make_float4(f[2 * q].x, f[2 * q].y, f[2 * q + 1].x, f[2 * q + 1].y);
+}
+
+// du_i = -sum_j (Dx_ij F_x + Dy_ij F_y + Dz_ij F_z)(node j) as compensated sums of
+// double-word products (mft_dw.cuh), the stage epilogue in FP64.  Per stencil entry: three
+// weight pairs and the neighbour's 128-byte flux record (four 32-byte loads).
+__global__ void __launch_bounds__(kBlock) k_fwd3_dw(FwdArgs a) {
+  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+  if (r >= a.n) return;
+  const int64_t i = ell_node(a.ell, r);
+  const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
+  const int len = a.ell.row_len[r];
+  const int32_t* __restrict__ col = a.ell.col;
+  const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
+  dw::Acc f[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) f[v] = dw::zero();
+#pragma unroll 2
+  for (int j = 0; j < len; ++j) {
+    const int64_t p = base + ((int64_t)j << 5);
+    const int64_t c = __ldg(col + p);
+    const float2 w[3] = {__ldg(a.wdw[0] + p), __ldg(a.wdw[1] + p), __ldg(a.wdw[2] + p)};
+    const F8 r0 = ldg_f8(F + c * 32), r1 = ldg_f8(F + c * 32 + 8);
+    const F8 r2 = ldg_f8(F + c * 32 + 16), r3 = ldg_f8(F + c * 32 + 24);
+    const float4 q[8] = {r0.lo, r0.hi, r1.lo, r1.hi, r2.lo, r2.hi, r3.lo, r3.hi};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const int k = d * 5 + v;  // pair k of the record
+        const float4 qq = q[k >> 1];
+        const float2 fv = (k & 1) ? make_float2(qq.z, qq.w) : make_float2(qq.x, qq.y);
+        dw::fma_acc(f[v], w[d], fv);
+      }
+    }
+  }
+  double du[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) du[v] = -dw::to_double(f[v]);
+  finish_node<5>(a.ep, i, du);
+}
+
 }  // namespace
+
+void launch_prep_euler3d_dw(int64_t n, double gamma, const double* u, float2* F,
+                            cudaStream_t s) {
+  if (n <= 0) return;
+  const double gm1 = gamma - 1.0;
+  const float h = (float)gm1;
+  const float2 g2 = make_float2(h, (float)(gm1 - (double)h));
+  k_prep_euler3d_dw<<<grid_for(n, 256), 256, 0, s>>>(n, g2, u, reinterpret_cast<float4*>(F));
+  MFT_LAUNCH_CHECK();
+}
+
+void launch_fwd3_dw(const FwdArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  MFT_REQUIRE(a.V == 5 && a.Fdw && a.wdw[0] && a.wdw[1] && a.wdw[2] && a.final_epilogue,
+              MFT_ERR_STATE, "double-word 3D gather: arguments not set");
+  k_fwd3_dw<<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  MFT_LAUNCH_CHECK();
+}
 
 void launch_flux_euler3d(int64_t n, double gamma, const double* u, double* F, cudaStream_t s) {
   if (n <= 0) return;

@@ -208,6 +208,11 @@ inline bool use_dw(const mft_ctx* c) {
   return c->precision == MFT_PREC_FP64 && c->fp64_arith != MFT_ARITH_DFMA &&
          c->eq == MFT_EQ_EULER2D && c->nvars == 4;
 }
+// The 3D Euler gather in double-word arithmetic (FP64 form, MFT_OPT_FP64_ARITH not DFMA).
+inline bool use_dw3(const mft_ctx* c) {
+  return c->precision == MFT_PREC_FP64 && c->fp64_arith != MFT_ARITH_DFMA &&
+         c->eq == MFT_EQ_EULER3D && c->nvars == 5;
+}
 // Builds (if needed) the device ELL layouts and operator values.
 void ensure_device_ops(mft_ctx* c);
 // One rhs! evaluation on the AoS state `us` (device), with the given epilogue.

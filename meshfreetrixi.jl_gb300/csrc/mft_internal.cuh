@@ -267,6 +267,11 @@ void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 // advection with the flux a_d u formed at the neighbour).
 void launch_flux_euler3d(int64_t n, double gamma, const double* u, double* F, cudaStream_t s);
 void launch_fwd3(const FwdArgs& a, cudaStream_t s);
+// The same for 3D Euler in double-word arithmetic: flux pairs (n x 16 float2, the 15 of
+// F_x, F_y, F_z and one pad) and the gather over the weight pairs a.wdw[0..2].
+void launch_prep_euler3d_dw(int64_t n, double gamma, const double* u, float2* F,
+                            cudaStream_t s);
+void launch_fwd3_dw(const FwdArgs& a, cudaStream_t s);
 // Double-word forms (mft_apply_dw.cu): per-node flux and state pairs, forward gather,
 // transpose gather.
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,

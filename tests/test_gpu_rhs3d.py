@@ -1,5 +1,5 @@
 """rhs! on 3D point clouds against the oracle: CompressibleEulerEquations3D on a periodic
-jittered cube and 3D scalar advection with a time-dependent Dirichlet inflow (the plain
+jittered cube (both gather arithmetics: double-word and FP64 FMAs) and 3D scalar advection with a time-dependent Dirichlet inflow (the plain
 flux divergence of calc_fluxes! over D_x, D_y, D_z, rbfsolver.jl:247-265, with the strong
 BCs).  GPU KNN and weights (PHS r^3 + degree 2, k = 30) bit-identical to the oracle's; one
 rhs! within 1e-12 of the condition scale; SSP-RK3 trajectories within 1e-10.  The
@@ -25,11 +25,11 @@ def cube(oracle):
     return pts, h, idx, ops, w
 
 
-def _euler_semi(pts, prec="fp64", sources=None):
+def _euler_semi(pts, prec="fp64", sources=None, arith="auto"):
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
     basis = M.PointCloudBasis(M.Point3D(), DEG, nv=K)
-    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision=prec))
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision=prec, fp64_arith=arith))
     dom = M.PointCloudDomain(solver, pts, period=PER)
     eq = M.CompressibleEulerEquations3D(GAMMA)
     semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.euler3d_wave(x), solver,
@@ -37,10 +37,11 @@ def _euler_semi(pts, prec="fp64", sources=None):
     return M, dom, semi
 
 
-def test_euler3d_rhs_and_steps_match_oracle(oracle, gpu_lib, cube):
+@pytest.mark.parametrize("arith", ["dw", "dfma"])
+def test_euler3d_rhs_and_steps_match_oracle(oracle, gpu_lib, cube, arith):
     from meshfree_gb300 import workloads as W
     pts, h, idx, ops, _w = cube
-    M, dom, semi = _euler_semi(pts)
+    M, dom, semi = _euler_semi(pts, arith=arith)
     assert np.array_equal(dom.pd.neighbors, idx)
     osemi = oracle.Semi(pts, ops, eq="euler3d", gamma=GAMMA)
     u0 = W.euler3d_wave(pts)
