@@ -1,7 +1,7 @@
 """rhs! on 3D point clouds against the oracle: CompressibleEulerEquations3D on a periodic
-jittered cube (both gather arithmetics: double-word and FP64 FMAs) and 3D scalar advection with a time-dependent Dirichlet inflow (the plain
-flux divergence of calc_fluxes! over D_x, D_y, D_z, rbfsolver.jl:247-265, with the strong
-BCs).  GPU KNN and weights (PHS r^3 + degree 2, k = 30) bit-identical to the oracle's; one
+jittered cube (both gather arithmetics: double-word and FP64 FMAs) and 3D scalar advection
+with a time-dependent Dirichlet inflow (the plain flux divergence of calc_fluxes! over
+D_x, D_y, D_z, rbfsolver.jl:247-265, with the strong BCs).  GPU KNN and weights (PHS r^3 + degree 2, k = 30) bit-identical to the oracle's; one
 rhs! within 1e-12 of the condition scale; SSP-RK3 trajectories within 1e-10.  The
 combinations the reference writes only for 2D Euler (viscosity sources, slip walls) and
 the FP32 form and adjoint are refused with MFT_ERR_UNSUPPORTED."""
