@@ -558,9 +558,10 @@ def run_igr(args, local):
 
 def run_euler3d(args, local, peaks):
     """CompressibleEulerEquations3D on a periodic jittered cube (N = side^3, PHS r^3 +
-    degree 2, k = 30): the plain flux divergence in FP64, SSP-RK3 steps with per-step
-    graphs; the gather's HBM roofline by the same convention (k indices, 3 k weights, the
-    state and the flux record of the node, the stage's u_n / u_s / out)."""
+    degree 2, k = 30): the plain flux divergence in the FP64 form (double-word gathers),
+    SSP-RK3 steps with per-step graphs; the gather's HBM roofline by the same convention
+    (k indices, 3 k weights, the state and the flux record of the node, the stage's
+    u_n / u_s / out)."""
     import meshfree_gb300 as M
     from meshfree_gb300 import workloads as W
     side = args.euler3d_side
@@ -590,7 +591,8 @@ def run_euler3d(args, local, peaks):
     # per node: indices 4k, weights 3*8k, flux record 120 + state 40 in, stage in/out 80
     bytes_node = 4 * k + 24 * k + 120 + 40 + 80
     return {"workload": "CompressibleEulerEquations3D, periodic unit cube, N=%d jittered nodes, "
-                        "PHS r^3 + degree-2 polynomials, k=%d, plain flux divergence (FP64), "
+                        "PHS r^3 + degree-2 polynomials, k=%d, plain flux divergence (FP64 form, "
+                        "double-word gathers), "
                         "SSP-RK3 dt=0.1h, per-step graphs" % (n, k),
             "nodes": n, "value": n * RHS_PER_STEP * args.steps / (ms * 1e-3), "unit": UNIT,
             "ms_per_step": ms / args.steps, "kernels": _kernels(prof),
