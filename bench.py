@@ -80,6 +80,8 @@ def parse():
                     help="run one auxiliary measurement alone")
     ap.add_argument("--gather", default="auto", choices=["auto", "thread", "staged", "halo"],
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
+    ap.add_argument("--halo-rows", type=int, default=0, choices=[0, 128, 256],
+                    help="rows per staged group of the dw/dfma/fp32 measurements (0: automatic)")
     ap.add_argument("--dw-variant", type=int, default=-1,
                     help="double-word gather kernel variant of the dw/dfma measurements "
                          "(-1: autotuned; 0..5 fixed, e.g. for profiling one kernel)")
@@ -891,9 +893,11 @@ def config_dict(workload, n, prec, arith="dw"):
 def timed_workload(args, workload, side, prec, arith, local, pg, clocks=None, dw_variant=-1):
     """Build + the timed region of one workload/form: value, per-kernel profile, end state."""
     semi, dom, u0, dt, n = build_problem(workload, side, prec, local, arith)
+    from meshfree_gb300 import _lib as L
     if dw_variant >= 0:
-        from meshfree_gb300 import _lib as L
         dom.ctx.set_option(L.OPT_DW_VARIANT, dw_variant)
+    if getattr(args, "halo_rows", 0):
+        dom.ctx.set_option(L.OPT_HALO_ROWS, args.halo_rows)
     ms, prof, clk, u_end, ms_prof = timed_steps(dom.ctx, u0, dt, args.warmup, args.steps, pg,
                                                 clocks)
     ms = max_over_ranks(pg, ms)
@@ -935,6 +939,7 @@ def run_one_form(args, local, peaks, prec, arith):
     out = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
            "variant": {"fwd_gather": r["dom"].ctx.get_option(L.OPT_TUNED_FWD),
                        "rev_gather": r["dom"].ctx.get_option(L.OPT_TUNED_REV)},
+           "halo_rows": r["dom"].ctx.get_option(L.OPT_HALO_ROWS),
            "kernels": _kernels(r["prof"]),
            "roofline": roofline(r["prof"], r["n"], prec, HV[args.workload], peaks, arith,
                                 tag="%s%s_%s" % (prec, arith if prec == "fp64" else "",

@@ -226,7 +226,11 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
        MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8,
-       MFT_OPT_IGR_ITERS = 9, MFT_OPT_ADJ_EVERY = 10 };
+       MFT_OPT_IGR_ITERS = 9, MFT_OPT_ADJ_EVERY = 10, MFT_OPT_HALO_ROWS = 11 };
+/* MFT_OPT_HALO_ROWS: layout rows per staged group (= threads per block of the staged
+ * gathers): 0 (default) picks 256, or 128 when 256-row groups would give every SM fewer
+ * than four; 128 or 256 fixes it (the layouts are rebuilt).  Read back: the size in use
+ * (0 when no staged layout is built). */
 /* Read-only MFT_OPT_IGR_ITERS: conjugate-gradient iterations of the last IGR solve
  * (-1 before the first).  Read-only MFT_OPT_ADJ_EVERY: the checkpoint interval of the last
  * mft_ssprk33_record (0: every stage state stored). */

@@ -436,7 +436,11 @@ void ensure_device_ops(mft_ctx* c) {
   // 256-row groups when that still gives every SM several blocks, else 128
   int nsm = 0;
   MFT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-  const int halo_rows = !halo ? 0 : (c->n / kHaloRows >= 4 * (int64_t)nsm ? kHaloRows : kHaloRows / 2);
+  const int halo_rows =
+      !halo ? 0
+            : (c->halo_rows_opt > 0
+                   ? c->halo_rows_opt
+                   : (c->n / kHaloRows >= 4 * (int64_t)nsm ? kHaloRows : kHaloRows / 2));
   if (halo && c->fwd.halo_rows != halo_rows) c->dev_dirty = true;
   if (!c->dev_dirty) return;
   c->graph_valid = false;
@@ -1543,6 +1547,11 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
                   "double-word gather variant: -1 (tuned) or 0..5");
       c->dw_variant = value;
       c->fsal_valid = false;
+    } else if (option == MFT_OPT_HALO_ROWS) {
+      MFT_REQUIRE(value == 0 || value == 128 || value == 256, MFT_ERR_ARG,
+                  "halo rows: 0 (automatic), 128 or 256");
+      c->halo_rows_opt = value;
+      c->fsal_valid = false;
     } else if (option == MFT_OPT_LAYOUT_ORDER) {
       MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG, "layout order: 0 node order, 1 Morton");
       c->layout_order = value;
@@ -1584,6 +1593,7 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_HALO_STAGED_REV) *value = (int)c->rev.halo_staged;
     else if (option == MFT_OPT_HALO_GROUPS) *value = (int)c->fwd.halo_groups;
     else if (option == MFT_OPT_ADJ_EVERY) *value = c->adj_every;
+    else if (option == MFT_OPT_HALO_ROWS) *value = c->fwd.halo_rows;
     else if (option == MFT_OPT_IGR_ITERS) {
       // CG iterations of the last IGR solve (-1: none yet)
       *value = -1;
