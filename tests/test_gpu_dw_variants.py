@@ -72,3 +72,36 @@ def test_dw_variants_bit_identical(gpu_lib, layout):
     else:
         assert 0 < staged[0] < groups and 0 < staged[1] < groups
     ctx.close()
+
+
+@pytest.mark.parametrize("case", ["rv_tominec", "tominec_rv", "rv_flyer", "upwind"])
+def test_dw_variants_bit_identical_with_bcs(oracle, gpu_lib, cyl, case):
+    """The same on the reference's cylinder fixture with its strong BCs (Dirichlet inlet,
+    do-nothing outlet, slip walls) and the source orderings, a history estimate set."""
+    from helpers import ic_bumpy, stencil_ops
+    from test_gpu_rhs import _setup
+    from meshfree_gb300 import _lib as L
+    pts = cyl["positions"]
+    ops, _ = stencil_ops(oracle, pts, cyl["knn"], rbf_pow=3)
+    lap_parts, _ = stencil_ops(oracle, pts, cyl["knn"], rbf_pow=3, order=2)
+    lap = oracle.csr_add(lap_parts)
+    fly_parts, _ = stencil_ops(oracle, pts, cyl["knn"], rbf_pow=5, order=4)
+    cyl_ops = dict(ops=ops, lap=lap, H_tom=oracle.ata(lap), H_fly=oracle.csr_add(fly_parts))
+    u0 = ic_bumpy(pts)
+    rng = np.random.default_rng(3)
+    approx = u0 * 0.1 * rng.standard_normal(u0.shape)
+    semi, ctx, _hv, _g = _setup(oracle, gpu_lib, cyl, cyl_ops, case, success_iter=2,
+                                approx_du=approx, arith="dw")
+    ref = None
+    for v in range(13):
+        ctx.set_option(L.OPT_DW_VARIANT, v)
+        du = np.empty_like(u0)
+        u = u0.copy()
+        ctx.rhs(du, u, 0.0)
+        if ref is None:
+            ref = (du, u)
+        else:
+            assert np.array_equal(du, ref[0]), (v, np.abs(du - ref[0]).max())
+            assert np.array_equal(u, ref[1])
+    assert ctx.get_option(L.OPT_HALO_STAGED_FWD) > 0
+    ctx.close()
