@@ -82,6 +82,9 @@ def parse():
                     help="FP32 gather mapping of the fp32 measurement (auto: autotuned)")
     ap.add_argument("--halo-rows", type=int, default=0, choices=[0, 128, 256],
                     help="rows per staged group of the dw/dfma/fp32 measurements (0: automatic)")
+    ap.add_argument("--entry-order", type=int, default=1, choices=[0, 1],
+                    help="entry order inside the staged rows: 1 bank-spreading (default), "
+                         "0 ascending columns")
     ap.add_argument("--dw-variant", type=int, default=-1,
                     help="double-word gather kernel variant of the dw/dfma measurements "
                          "(-1: autotuned; 0..5 fixed, e.g. for profiling one kernel)")
@@ -898,11 +901,20 @@ def timed_workload(args, workload, side, prec, arith, local, pg, clocks=None, dw
         dom.ctx.set_option(L.OPT_DW_VARIANT, dw_variant)
     if getattr(args, "halo_rows", 0):
         dom.ctx.set_option(L.OPT_HALO_ROWS, args.halo_rows)
+    dom.ctx.set_option(L.OPT_ENTRY_ORDER, getattr(args, "entry_order", 1))
     ms, prof, clk, u_end, ms_prof = timed_steps(dom.ctx, u0, dt, args.warmup, args.steps, pg,
                                                 clocks)
     ms = max_over_ranks(pg, ms)
     return dict(semi=semi, dom=dom, u0=u0, dt=dt, n=n, ms=ms, prof=prof, clk=clk, u=u_end,
                 ms_prof=ms_prof, value=n * RHS_PER_STEP * args.steps / (ms * 1e-3))
+
+
+def bank_counts(ctx):
+    """Serialised shared-memory accesses per quarter-warp record load of the staged
+    gathers' layouts (1.0 = conflict-free), as counted when the layouts were built."""
+    from meshfree_gb300 import _lib as L
+    return {"fwd_gather": ctx.get_option(L.OPT_BANK_FWD) / 1000.0,
+            "rev_gather": ctx.get_option(L.OPT_BANK_REV) / 1000.0}
 
 
 def _kernels(prof):
@@ -919,11 +931,13 @@ def run_fp32(args, local, peaks):
     ctx.set_option(L.OPT_GATHER, {"auto": L.GATHER_AUTO, "thread": L.GATHER_THREAD,
                                   "staged": L.GATHER_STAGED,
                                   "halo": L.GATHER_HALO}[args.gather])
+    ctx.set_option(L.OPT_ENTRY_ORDER, args.entry_order)
     ms, prof, _, _, ms_prof = timed_steps(ctx, u0, dt, args.warmup, args.steps, None)
     out = {"value": n * RHS_PER_STEP * args.steps / (ms * 1e-3), "unit": UNIT,
            "ms_per_step": ms / args.steps, "gather": args.gather,
            "mapping": {"fwd_gather": ctx.get_option(L.OPT_TUNED_FWD),
                        "rev_gather": ctx.get_option(L.OPT_TUNED_REV)},
+           "entry_order": args.entry_order, "smem_accesses_per_quarter_load": bank_counts(ctx),
            "kernels": _kernels(prof),
            "roofline": roofline(prof, n, "fp32", HV[args.workload], peaks,
                                 tag="fp32_" + args.workload)}
@@ -940,6 +954,8 @@ def run_one_form(args, local, peaks, prec, arith):
            "variant": {"fwd_gather": r["dom"].ctx.get_option(L.OPT_TUNED_FWD),
                        "rev_gather": r["dom"].ctx.get_option(L.OPT_TUNED_REV)},
            "halo_rows": r["dom"].ctx.get_option(L.OPT_HALO_ROWS),
+           "entry_order": args.entry_order,
+           "smem_accesses_per_quarter_load": bank_counts(r["dom"].ctx),
            "kernels": _kernels(r["prof"]),
            "roofline": roofline(r["prof"], r["n"], prec, HV[args.workload], peaks, arith,
                                 tag="%s%s_%s" % (prec, arith if prec == "fp64" else "",

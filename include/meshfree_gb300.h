@@ -226,7 +226,16 @@ mft_status mft_set_segments(mft_ctx* ctx, int nseg, const int64_t* offsets, cons
 enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
        MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8,
-       MFT_OPT_IGR_ITERS = 9, MFT_OPT_ADJ_EVERY = 10, MFT_OPT_HALO_ROWS = 11 };
+       MFT_OPT_IGR_ITERS = 9, MFT_OPT_ADJ_EVERY = 10, MFT_OPT_HALO_ROWS = 11,
+       MFT_OPT_ENTRY_ORDER = 12, MFT_OPT_BANK_FWD = 13, MFT_OPT_BANK_REV = 14 };
+/* MFT_OPT_ENTRY_ORDER: order of the entries inside the rows of the staged row groups
+ * (which is the order each row's sum runs in, for every gather variant of that layout):
+ * 1 (default) spreads the shared-memory reads of the 8 lanes of each quarter-warp over
+ * the bank groups, slot by slot; 0 keeps the structure's (ascending-column) order.  The
+ * layouts are rebuilt on change; sums differ between the two in the last bits only.
+ * Read-only MFT_OPT_BANK_FWD / _REV: for the staged forward / transpose gathers' layout,
+ * the mean number of serialised shared-memory accesses per quarter-warp record load
+ * (1000 = conflict-free), counted on the host when the layout is built; 0 before. */
 /* MFT_OPT_HALO_ROWS: layout rows per staged group (= threads per block of the staged
  * gathers): 0 (default) picks 256, or 128 when 256-row groups would give every SM fewer
  * than four; 128 or 256 fixes it (the layouts are rebuilt).  Read back: the size in use

@@ -43,6 +43,76 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 
 // ---------------------------------------------------------------- ELL layout
 
+// Entry order inside the rows of a staged row group.  A staged gather reads, at each
+// slot, one neighbour record per lane from shared memory with 16-byte loads; the 8 lanes
+// of a quarter-warp are served together, and records in the same bank group (their
+// position in the group's list mod 8) at different positions are served one after
+// another.  In ascending-column order the 8 lanes' positions fall into bank groups at
+// random (about 1.8 serialised accesses per quarter-warp load on a Morton-ordered cloud).
+// A row's sum may run in any order that every gather of that layout shares, so the
+// entries of each quarter-warp's rows are ordered slot by slot: the rows with the fewest
+// bank groups left choose first, each an entry in a bank group no other lane of the
+// quarter takes at this slot -- of the free groups the one with the most entries left
+// over the quarter's rows, so that crowded groups spread over all slots; a row without a
+// free group takes an entry another lane reads at this slot (one address is served
+// once), else one from its fullest group.  rows: the quarter's layout rows (at most 8);
+// lists: per row its entries' list positions, in CSR order; out: per row and slot the
+// CSR offset (within the row) placed there.
+static void spread_quarter(int nrows, const std::vector<int32_t>* lists,
+                           std::vector<int32_t>* out) {
+  std::vector<std::pair<int32_t, int32_t>> bucket[8][8];  // [row][bank group]: (pos, offset)
+  int left[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < nrows; ++k) {
+    out[k].assign(lists[k].size(), 0);
+    left[k] = (int)lists[k].size();
+    for (int32_t j = 0; j < (int32_t)lists[k].size(); ++j)
+      bucket[k][lists[k][j] & 7].emplace_back(lists[k][j], j);
+  }
+  for (int slot = 0;; ++slot) {
+    int act[8], na = 0, nfree[8];
+    int demand[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < nrows; ++k) {
+      if (left[k] == 0) continue;
+      act[na++] = k;
+      nfree[k] = 0;
+      for (int g = 0; g < 8; ++g) {
+        demand[g] += (int)bucket[k][g].size();
+        nfree[k] += bucket[k][g].empty() ? 0 : 1;
+      }
+    }
+    if (na == 0) break;
+    for (int a = 1; a < na; ++a)  // fewest choices first (stable)
+      for (int b = a; b > 0 && nfree[act[b]] < nfree[act[b - 1]]; --b) std::swap(act[b], act[b - 1]);
+    unsigned used = 0;
+    int32_t chosen[8];
+    int nch = 0;
+    for (int a = 0; a < na; ++a) {
+      const int k = act[a];
+      int g = -1;
+      for (int x = 0; x < 8; ++x)
+        if (!bucket[k][x].empty() && !(used >> x & 1u) && (g < 0 || demand[x] > demand[g])) g = x;
+      size_t at = 0;
+      if (g < 0) {
+        for (int x = 0; x < 8 && g < 0; ++x)
+          for (size_t e = 0; e < bucket[k][x].size() && g < 0; ++e)
+            for (int c = 0; c < nch; ++c)
+              if (bucket[k][x][e].first == chosen[c]) { g = x; at = e; break; }
+        if (g < 0) {
+          for (int x = 0; x < 8; ++x)
+            if (!bucket[k][x].empty() && (g < 0 || bucket[k][x].size() > bucket[k][g].size())) g = x;
+          at = 0;
+        }
+      }
+      const std::pair<int32_t, int32_t> ent = bucket[k][g][at];
+      bucket[k][g].erase(bucket[k][g].begin() + (std::ptrdiff_t)at);
+      used |= 1u << g;
+      chosen[nch++] = ent.first;
+      out[k][slot] = ent.second;
+      --left[k];
+    }
+  }
+}
+
 // Builds a sliced ELL over rows of a CSR-like structure.  pos[e] receives the
 // ELL element of structure entry e.  Layout row r holds node base[r] (base: a spatial
 // order of the nodes, see morton_order; null: node r).  With window > 0 the rows are
@@ -50,10 +120,13 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 // (stable, so rows stay near their neighbours): the 32 rows of a slice then have nearly
 // equal lengths and the lanes of a warp finish together.
 // With halo_rows > 0, the neighbour halos of the row groups are built too (halo_rows rows
-// each: distinct columns ascending, and each element's position among them).
+// each: distinct columns ascending, and each element's position among them), and with
+// spread the rows of the staged groups take their entries in the bank-spreading order of
+// spread_quarter (else, and in the other groups, in structure order).
 void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<int32_t>& cols,
                EllBuf& ell, std::vector<int64_t>& pos, cudaStream_t s, int window = 0,
-               const std::vector<int32_t>* base = nullptr, int halo_rows = 0) {
+               const std::vector<int32_t>* base = nullptr, int halo_rows = 0,
+               bool spread = false) {
   std::vector<int32_t> order(n);
   if (base) order = *base;
   else std::iota(order.begin(), order.end(), 0);
@@ -86,8 +159,52 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
     soff[sl + 1] += soff[sl];
   }
   const int64_t ne = soff[nsl];
+  // neighbour halos: per group the distinct columns its rows gather, ascending
+  const bool halos = halo_rows > 0;
+  if (halos)
+    MFT_REQUIRE(halo_rows % kSlice == 0 && halo_rows <= kHaloRows, MFT_ERR_STATE,
+                "halo groups must be whole slices of at most kHaloRows rows");
+  const int64_t ng = halos ? (n + halo_rows - 1) / halo_rows : 0;
+  std::vector<std::vector<int32_t>> lists(ng);
+  // eorder[rowptr[node] + slot]: the CSR offset placed at that slot of the node's row
+  std::vector<int32_t> eorder;
+  if (halos && spread) eorder.resize(rowptr[n]);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t g = 0; g < ng; ++g) {
+    std::vector<int32_t>& h = lists[g];
+    const int64_t r0 = g * halo_rows, r1 = std::min<int64_t>(n, r0 + halo_rows);
+    for (int64_t r = r0; r < r1; ++r) {
+      const int64_t node = order[r];
+      h.insert(h.end(), cols.begin() + rowptr[node], cols.begin() + rowptr[node] + rlen[r]);
+    }
+    std::sort(h.begin(), h.end());
+    h.erase(std::unique(h.begin(), h.end()), h.end());
+    if ((int64_t)h.size() > kHaloMax) h.clear();
+    if (!spread) continue;
+    std::vector<int32_t> qlists[8], qout[8];
+    for (int64_t r = r0; r < r1; r += 8) {
+      const int nr = (int)std::min<int64_t>(8, r1 - r);
+      for (int k = 0; k < nr; ++k) {
+        const int64_t node = order[r + k];
+        const int32_t* rc = cols.data() + rowptr[node];
+        qlists[k].resize(rlen[r + k]);
+        for (int j = 0; j < rlen[r + k]; ++j)
+          qlists[k][j] = h.empty() ? 0
+                                   : (int32_t)(std::lower_bound(h.begin(), h.end(), rc[j]) - h.begin());
+      }
+      if (h.empty()) {  // gathered directly: structure order
+        for (int k = 0; k < nr; ++k)
+          for (int j = 0; j < rlen[r + k]; ++j) eorder[rowptr[order[r + k]] + j] = j;
+        continue;
+      }
+      spread_quarter(nr, qlists, qout);
+      for (int k = 0; k < nr; ++k)
+        std::copy(qout[k].begin(), qout[k].end(), eorder.begin() + rowptr[order[r + k]]);
+    }
+  }
   std::vector<int32_t> col(ne);
   pos.assign(rowptr[n], 0);
+  const bool reorder = !eorder.empty();
 #pragma omp parallel for schedule(static)
   for (int64_t sl = 0; sl < nsl; ++sl) {
     const int m = (int)((soff[sl + 1] - soff[sl]) / kSlice);
@@ -97,8 +214,9 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
       for (int j = 0; j < m; ++j) {
         const int64_t e = soff[sl] + (int64_t)j * kSlice + lane;
         if (r < n && j < rlen[r]) {
-          col[e] = cols[rowptr[node] + j];
-          pos[rowptr[node] + j] = e;
+          const int64_t src = rowptr[node] + (reorder ? eorder[rowptr[node] + j] : j);
+          col[e] = cols[src];
+          pos[src] = e;
         } else {
           col[e] = (int32_t)(r < n ? node : 0);  // padding: a valid index, never read
         }
@@ -115,7 +233,9 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
   ell.col.upload(col, s);
   if (window > 0 || base) ell.perm.upload(order, s);
   else ell.perm.release();
-  if (halo_rows <= 0) {
+  ell.spread = halos && spread;
+  ell.bank_milli = 0;
+  if (!halos) {
     ell.halo_off.release();
     ell.halo_col.release();
     ell.lcol.release();
@@ -124,25 +244,15 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
     ell.halo_rows = 0;
     return;
   }
-  MFT_REQUIRE(halo_rows % kSlice == 0 && halo_rows <= kHaloRows, MFT_ERR_STATE,
-              "halo groups must be whole slices of at most kHaloRows rows");
-  const int64_t ng = (n + halo_rows - 1) / halo_rows;
-  std::vector<std::vector<int32_t>> lists(ng);
   std::vector<uint16_t> lcol(ne, 0);
+  // shared-memory accesses of the staged groups: per quarter-warp load, the largest number
+  // of distinct positions in one bank group (summed, and the loads counted)
+  std::vector<int64_t> acc_sum(ng, 0), acc_cnt(ng, 0);
 #pragma omp parallel for schedule(dynamic, 16)
   for (int64_t g = 0; g < ng; ++g) {
-    std::vector<int32_t>& h = lists[g];
+    const std::vector<int32_t>& h = lists[g];
+    if (h.empty()) continue;
     const int64_t r0 = g * halo_rows, r1 = std::min<int64_t>(n, r0 + halo_rows);
-    for (int64_t r = r0; r < r1; ++r) {
-      const int64_t node = order[r];
-      h.insert(h.end(), cols.begin() + rowptr[node], cols.begin() + rowptr[node] + rlen[r]);
-    }
-    std::sort(h.begin(), h.end());
-    h.erase(std::unique(h.begin(), h.end()), h.end());
-    if ((int64_t)h.size() > kHaloMax) {
-      h.clear();
-      continue;
-    }
     for (int64_t r = r0; r < r1; ++r) {
       const int64_t sl = r / kSlice, lane = r % kSlice;
       for (int j = 0; j < rlen[r]; ++j) {
@@ -150,15 +260,35 @@ void build_ell(int64_t n, const std::vector<int64_t>& rowptr, const std::vector<
         lcol[e] = (uint16_t)(std::lower_bound(h.begin(), h.end(), col[e]) - h.begin());
       }
     }
+    for (int64_t r = r0; r < r1; r += 8) {
+      const int64_t sl = r / kSlice;
+      const int m = (int)((soff[sl + 1] - soff[sl]) / kSlice);
+      for (int j = 0; j < m; ++j) {
+        int32_t q[8];
+        int nq = 0;
+        for (int64_t x = r; x < std::min<int64_t>(r + 8, r1); ++x)
+          if (j < rlen[x]) q[nq++] = lcol[soff[sl] + (int64_t)j * kSlice + x % kSlice];
+        if (nq == 0) continue;
+        std::sort(q, q + nq);
+        int per[8] = {0, 0, 0, 0, 0, 0, 0, 0}, worst = 0;
+        for (int a = 0; a < nq; ++a)
+          if (a == 0 || q[a] != q[a - 1]) worst = std::max(worst, ++per[q[a] & 7]);
+        acc_sum[g] += worst;
+        acc_cnt[g] += 1;
+      }
+    }
   }
   std::vector<int32_t> hoff(ng + 1, 0);
-  int64_t staged = 0;
+  int64_t staged = 0, wsum = 0, wcnt = 0;
   int stride = 0;
   for (int64_t g = 0; g < ng; ++g) {
     hoff[g + 1] = hoff[g] + (int32_t)lists[g].size();
     staged += lists[g].empty() ? 0 : 1;
     stride = std::max(stride, (int)lists[g].size());
+    wsum += acc_sum[g];
+    wcnt += acc_cnt[g];
   }
+  ell.bank_milli = wcnt ? (int)((1000 * wsum + wcnt / 2) / wcnt) : 0;
   std::vector<int32_t> hcol(hoff[ng]);
 #pragma omp parallel for schedule(static)
   for (int64_t g = 0; g < ng; ++g)
@@ -442,6 +572,8 @@ void ensure_device_ops(mft_ctx* c) {
                    ? c->halo_rows_opt
                    : (c->n / kHaloRows >= 4 * (int64_t)nsm ? kHaloRows : kHaloRows / 2));
   if (halo && c->fwd.halo_rows != halo_rows) c->dev_dirty = true;
+  const bool spread = halo && c->entry_order == 1;
+  if (halo && c->fwd.spread != spread) c->dev_dirty = true;
   if (!c->dev_dirty) return;
   c->graph_valid = false;
   cudaStream_t s = c->stream;
@@ -451,10 +583,10 @@ void ensure_device_ops(mft_ctx* c) {
     zorder = morton_order(c->dim, c->n, c->xyz,
                           c->nseg > 0 ? c->seg_off : std::vector<int64_t>{});
   const std::vector<int32_t>* base = spatial ? &zorder : nullptr;
-  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, halo_rows);
+  build_ell(c->n, c->rp, c->ci, c->fwd, pos, s, 0, base, halo_rows, spread);
   c->fwd_pos.upload(pos, s);
   std::vector<int64_t> rpos_csc;
-  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, halo_rows);
+  build_ell(c->n, c->cp, c->ri, c->rev, rpos_csc, s, rev_window, base, halo_rows, spread);
   std::vector<int64_t> rpos(rpos_csc.size());
 #pragma omp parallel for schedule(static)
   for (int64_t p = 0; p < (int64_t)rpos_csc.size(); ++p) rpos[c->csc2csr[p]] = rpos_csc[p];
@@ -1552,6 +1684,11 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
                   "halo rows: 0 (automatic), 128 or 256");
       c->halo_rows_opt = value;
       c->fsal_valid = false;
+    } else if (option == MFT_OPT_ENTRY_ORDER) {
+      MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG,
+                  "entry order: 0 structure order, 1 bank-spreading");
+      c->entry_order = value;
+      c->fsal_valid = false;
     } else if (option == MFT_OPT_LAYOUT_ORDER) {
       MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG, "layout order: 0 node order, 1 Morton");
       c->layout_order = value;
@@ -1594,6 +1731,9 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_HALO_GROUPS) *value = (int)c->fwd.halo_groups;
     else if (option == MFT_OPT_ADJ_EVERY) *value = c->adj_every;
     else if (option == MFT_OPT_HALO_ROWS) *value = c->fwd.halo_rows;
+    else if (option == MFT_OPT_ENTRY_ORDER) *value = c->entry_order;
+    else if (option == MFT_OPT_BANK_FWD) *value = c->fwd.bank_milli;
+    else if (option == MFT_OPT_BANK_REV) *value = c->rev.bank_milli;
     else if (option == MFT_OPT_IGR_ITERS) {
       // CG iterations of the last IGR solve (-1: none yet)
       *value = -1;

@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(kBlock) k_eps(EpsArgs a) {
 
 // du_i = du_p_i - sum_{j: i in stencil(j)} (Dx[j,i] s_x[j] + Dy[j,i] s_y[j])
 //               - gamma * sum_j lap[j,i] q[j]
-// over the reverse adjacency (CSC column i), ascending j.
+// over the reverse adjacency (CSC column i), in the layout's entry order.
 template <int V, bool RV, bool LAP>
 __global__ void __launch_bounds__(kBlock) k_rev_f64(RevArgs a) {
   const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row

@@ -5,8 +5,9 @@
 // neighbour states are read as double-word pairs (h, l) -- 8 bytes per value, the
 // footprint of an FP64 value -- and the products and sums run on the FP32 pipe with
 // error-free transformations; per-node values (the stage epilogue, the viscosity) stay
-// in FP64.  Accumulation order per row is the layout's ascending-column order, as in the
-// FP64 kernels.
+// in FP64.  Accumulation order per row is the layout's entry order (ascending columns, or
+// in the rows of staged groups the bank-spreading order of build_ell), shared by every
+// variant.
 #include <cuda_runtime.h>
 #include <math.h>
 

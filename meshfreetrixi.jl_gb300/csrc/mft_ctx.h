@@ -86,6 +86,7 @@ struct mft_ctx {
   int fp64_arith = MFT_ARITH_AUTO;
   int layout_order = 1;  // 1: operator layout rows in Morton order of the nodes
   int halo_rows_opt = 0;  // rows per staged group: 0 automatic, else 128 or 256
+  int entry_order = 1;    // staged rows: 1 bank-spreading entry order, 0 structure order
   int tuned_fwd[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   int tuned_rev[4] = {-1, -1, -1, -1};
   int last_fwd_choice = -1, last_rev_choice = -1;

@@ -80,7 +80,8 @@ constexpr int kSlice = 32;
 // element the element's position in its group's list.  A gather kernel stages a group's
 // neighbour records into shared memory once with coalesced copies and reads them from
 // there, instead of one scattered global load per element.  Groups with more distinct
-// neighbours have an empty list and gather directly.
+// neighbours have an empty list and gather directly.  The rows of the groups with a list
+// may take their entries in a bank-spreading order (build_ell, spread).
 constexpr int kHaloRows = 256;  // largest group (and block) size
 constexpr int kHaloMax = 640;
 
@@ -111,6 +112,8 @@ struct EllBuf {
   int64_t halo_groups = 0, halo_staged = 0;  // groups, and groups with a list
   int halo_stride = 0;
   int halo_rows = 0;
+  bool spread = false;  // staged rows in the bank-spreading entry order
+  int bank_milli = 0;   // staged loads: serialised accesses per quarter-warp load x 1000
   EllView view() const {
     return EllView{n,         slice_off.p, row_len.p,
                    col.p,     (window > 0 || ordered) ? perm.p : nullptr,

@@ -105,3 +105,41 @@ def test_dw_variants_bit_identical_with_bcs(oracle, gpu_lib, cyl, case):
             assert np.array_equal(u, ref[1])
     assert ctx.get_option(L.OPT_HALO_STAGED_FWD) > 0
     ctx.close()
+
+
+def test_entry_order_spreads_banks_and_keeps_the_sums(gpu_lib):
+    """The bank-spreading entry order of the staged rows (MFT_OPT_ENTRY_ORDER 1, the
+    default) against the structure order (0): fewer serialised shared-memory accesses per
+    quarter-warp load in both staged layouts (as counted when they are built), and one
+    rhs! that differs only by the rounding of the reordered sums (within 1e-12 of each
+    variable's largest |du|); under either order every variant gives the same bits."""
+    from meshfree_gb300 import workloads as W
+    pts, h = W.riemann_cloud(96)
+    L, dom, semi = _problem(pts, 1)
+    ctx = dom.ctx
+    u0 = W.riemann_ic(pts)
+    du0 = np.empty_like(u0)
+    ctx.rhs(du0, u0.copy(), 0.0)
+    ctx.set_rv_state(du0 * 1.01, 2)
+    out, banks = {}, {}
+    for order in (0, 1):
+        ctx.set_option(L.OPT_ENTRY_ORDER, order)
+        ref = None
+        for v in (0, 7, 11):
+            ctx.set_option(L.OPT_DW_VARIANT, v)
+            du = np.empty_like(u0)
+            ctx.rhs(du, u0.copy(), 0.0)
+            if ref is None:
+                ref = du
+            else:
+                assert np.array_equal(du, ref), (order, v)
+        out[order] = ref
+        banks[order] = (ctx.get_option(L.OPT_BANK_FWD), ctx.get_option(L.OPT_BANK_REV))
+        assert ctx.get_option(L.OPT_ENTRY_ORDER) == order
+    assert all(b >= 1000 for b in banks[0] + banks[1]), banks
+    assert banks[1][0] < 0.8 * banks[0][0] and banks[1][1] < 0.8 * banks[0][1], banks
+    scale = np.abs(out[0]).max(axis=1, keepdims=True)
+    assert np.all(np.abs(out[1] - out[0]) <= 1e-12 * scale)
+    with pytest.raises(L.MFTError):
+        ctx.set_option(L.OPT_ENTRY_ORDER, 2)
+    ctx.close()

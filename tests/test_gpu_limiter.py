@@ -1,9 +1,10 @@
 """GPU Zhang-Shu positivity limiter against the oracle.
 
-The device sums a node's stencil mean in its operator row order (ascending node index);
-fed that same order, the oracle gives bit-identical states.  In the reference's stencil
-order (by distance) the mean differs by rounding only: 1e-14 relative.  A limited
-SSP-RK3 trajectory matches the oracle's SSPRK33(stage_limiter!) to 1e-10."""
+The device sums a node's stencil mean in its operator layout's entry order: ascending node
+index with MFT_OPT_ENTRY_ORDER 0, where the oracle fed that same order gives bit-identical
+states.  In the default bank-spreading order, and against the reference's stencil order
+(by distance), the mean differs by rounding only: 1e-14 relative.  A limited SSP-RK3
+trajectory matches the oracle's SSPRK33(stage_limiter!) to 1e-10."""
 import numpy as np
 import pytest
 
@@ -24,15 +25,18 @@ def _domain(n=32):
     return M, semi, dom, pts, h
 
 
-@pytest.mark.parametrize("order", ["row", "stencil"])
+@pytest.mark.parametrize("order", ["row", "spread", "stencil"])
 def test_limit_matches_oracle(oracle, gpu_lib, order):
+    from meshfree_gb300 import _lib as L
     M, semi, dom, pts, _h = _domain()
+    if order == "row":
+        dom.ctx.set_option(L.OPT_ENTRY_ORDER, 0)
     lim = M.PositivityPreservingLimiterZhangShu(thresholds=(0.05, 0.05),
                                                 variables=(M.density, M.pressure))
     u0 = dip_state(pts)
     got = lim(u0.copy(), semi)
     nb = dom.pd.neighbors
-    cols = np.sort(nb, axis=1) if order == "row" else nb
+    cols = np.sort(nb, axis=1) if order in ("row", "spread") else nb
     rp = np.arange(pts.shape[0] + 1, dtype=np.int64) * nb.shape[1]
     ref = u0.copy()
     oracle.stage_limiter(rp, cols.ravel(), [oracle.LIM_DENSITY, oracle.LIM_PRESSURE],
