@@ -85,6 +85,9 @@ def parse():
     ap.add_argument("--entry-order", type=int, default=1, choices=[0, 1],
                     help="entry order inside the staged rows: 1 bank-spreading (default), "
                          "0 ascending columns")
+    ap.add_argument("--fuse-flux", type=int, default=1, choices=[0, 1],
+                    help="1: the staged double-word forward gather forms the flux records "
+                         "while staging (no flux kernel) when it can; 0: never")
     ap.add_argument("--dw-variant", type=int, default=-1,
                     help="double-word gather kernel variant of the dw/dfma measurements "
                          "(-1: autotuned; 0..5 fixed, e.g. for profiling one kernel)")
@@ -902,6 +905,7 @@ def timed_workload(args, workload, side, prec, arith, local, pg, clocks=None, dw
     if getattr(args, "halo_rows", 0):
         dom.ctx.set_option(L.OPT_HALO_ROWS, args.halo_rows)
     dom.ctx.set_option(L.OPT_ENTRY_ORDER, getattr(args, "entry_order", 1))
+    dom.ctx.set_option(L.OPT_FUSE_FLUX, getattr(args, "fuse_flux", 1))
     ms, prof, clk, u_end, ms_prof = timed_steps(dom.ctx, u0, dt, args.warmup, args.steps, pg,
                                                 clocks)
     ms = max_over_ranks(pg, ms)
@@ -956,6 +960,7 @@ def run_one_form(args, local, peaks, prec, arith):
            "halo_rows": r["dom"].ctx.get_option(L.OPT_HALO_ROWS),
            "entry_order": args.entry_order,
            "smem_accesses_per_quarter_load": bank_counts(r["dom"].ctx),
+           "flux_records_formed_in_gather": r["dom"].ctx.get_option(L.OPT_FLUX_FUSED),
            "kernels": _kernels(r["prof"]),
            "roofline": roofline(r["prof"], r["n"], prec, HV[args.workload], peaks, arith,
                                 tag="%s%s_%s" % (prec, arith if prec == "fp64" else "",
@@ -1045,6 +1050,10 @@ def run_ours(args):
     from meshfree_gb300 import _lib as L
     dw_variant = {"fwd_gather": r64["dom"].ctx.get_option(L.OPT_TUNED_FWD),
                   "rev_gather": r64["dom"].ctx.get_option(L.OPT_TUNED_REV)}
+    dw_layout = {"entry_order": args.entry_order,
+                 "smem_accesses_per_quarter_load": bank_counts(r64["dom"].ctx),
+                 "flux_records_formed_in_gather": r64["dom"].ctx.get_option(L.OPT_FLUX_FUSED),
+                 "halo_rows": r64["dom"].ctx.get_option(L.OPT_HALO_ROWS)}
 
     # the same workload with FP64 fused multiply-adds in the gathers
     rd = timed_workload(args, args.workload, args.side, "fp64", "dfma", local, pg)
@@ -1128,6 +1137,7 @@ def run_ours(args):
         "clocks": r64["clk"],
         "fma_rates_per_s": peaks["fma_rates"],
         "dw_gather_variant": dw_variant,
+        "dw_layout": dw_layout,
         "fp64_dfma": dfma,
         "fp32_apply": {"value": value32, "unit": UNIT, "speedup_vs_fp64": value32 / value,
                        "l2_density_err_vs_fp64": l2, "linf_density_err_vs_fp64": linf,

@@ -227,7 +227,14 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
        MFT_OPT_FP64_ARITH = 3, MFT_OPT_LAYOUT_ORDER = 4, MFT_OPT_DW_VARIANT = 5,
        MFT_OPT_HALO_STAGED_FWD = 6, MFT_OPT_HALO_STAGED_REV = 7, MFT_OPT_HALO_GROUPS = 8,
        MFT_OPT_IGR_ITERS = 9, MFT_OPT_ADJ_EVERY = 10, MFT_OPT_HALO_ROWS = 11,
-       MFT_OPT_ENTRY_ORDER = 12, MFT_OPT_BANK_FWD = 13, MFT_OPT_BANK_REV = 14 };
+       MFT_OPT_ENTRY_ORDER = 12, MFT_OPT_BANK_FWD = 13, MFT_OPT_BANK_REV = 14,
+       MFT_OPT_FUSE_FLUX = 15, MFT_OPT_FLUX_FUSED = 16 };
+/* MFT_OPT_FUSE_FLUX (default 1): in the double-word form, when every row group is staged
+ * and the forward gather's variant is 7, 11 or 12, that gather forms each staged
+ * neighbour's state and flux pairs from the FP64 state while staging, and the separate
+ * flux kernel (which writes those pairs for every node) is skipped; 0 always runs it.  The
+ * results are the same bits either way.  Read-only MFT_OPT_FLUX_FUSED: 1 when the last
+ * evaluation formed the pairs in the gather. */
 /* MFT_OPT_ENTRY_ORDER: order of the entries inside the rows of the staged row groups
  * (which is the order each row's sum runs in, for every gather variant of that layout):
  * 1 (default) spreads the shared-memory reads of the 8 lanes of each quarter-warp over

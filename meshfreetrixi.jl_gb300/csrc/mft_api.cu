@@ -797,7 +797,11 @@ static int dw_fwd_choice(mft_ctx* c, const FwdArgs& a) {
     if (c->capturing) return 0;
     FwdArgs probe = a;
     probe.final_epilogue = 0;  // timing launches write only scratch outputs
+    // with fused staging possible, an unfused variant is timed with the flux kernel it
+    // needs (which rewrites the same pairs)
     c->tuned_fwd_dw[key] = tune_variants(c, kDwVariants, [&](int v) {
+      if (probe.fuse_flux && !dw_fwd_fuses(v))
+        launch_prep_euler_dw(probe.n, c->gamma, probe.ustate, c->Fdw.p, c->udw.p, c->stream);
       launch_fwd_dw(probe, v, c->stream);
     });
   }
@@ -863,6 +867,8 @@ static void check_kernel_errors(mft_ctx* c) {
     MFT_CUDA(cudaStreamSynchronize(c->stream));
     if (e == MFT_ERR_NONFINITE)
       throw mft::Error(e, "the state or du became NaN or infinite (outputs were written)");
+    if (e == MFT_ERR_STATE)
+      throw mft::Error(e, "a fused staged gather met a row group without a staged list");
     throw mft::Error(e, "a device wait gave up (bulk-copy completion not observed)");
   }
 }
@@ -1054,11 +1060,23 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   }
 
   // 2. flux per node (FP64 Euler; double-word pairs of the flux and the state for the
-  // double-word gathers)
+  // double-word gathers).  The staged double-word forward variants 7, 11 and 12 can form
+  // those records while staging when every row group is staged; once such a variant is
+  // the chosen one the flux kernel is skipped (it still runs in the evaluation that tunes,
+  // whose unfused variants read its pairs).
+  const int fwd_flyer = flyer ? ((iv < 0 || hv_first) ? 1 : 2) : 0;
+  const int fwd_key = (iv >= 0 ? 1 : 0) + (tominec ? 2 : 0) + 4 * fwd_flyer;
+  const bool fuse_ok = dw && c->fuse_flux && c->fwd.halo_groups > 0 &&
+                       c->fwd.halo_staged == c->fwd.halo_groups;
+  const int fwd_known = c->dw_variant >= 0 ? c->dw_variant : c->tuned_fwd_dw[fwd_key];
+  const bool skip_flux = fuse_ok && fwd_known >= 0 && dw_fwd_fuses(fwd_known);
+  c->last_flux_fused = skip_flux ? 1 : 0;
   if (dw) {
-    NvtxRange rng("calc fluxes");
-    ProfScope ps(c, MFT_K_FLUX);
-    launch_prep_euler_dw(n, c->gamma, us, c->Fdw.p, c->udw.p, s);
+    if (!skip_flux) {
+      NvtxRange rng("calc fluxes");
+      ProfScope ps(c, MFT_K_FLUX);
+      launch_prep_euler_dw(n, c->gamma, us, c->Fdw.p, c->udw.p, s);
+    }
   } else if (!f32 && c->eq == MFT_EQ_EULER2D) {
     NvtxRange rng("calc fluxes");
     ProfScope ps(c, MFT_K_FLUX);
@@ -1087,7 +1105,11 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
   fa.hv_gamma = hv_gamma;
   fa.want_t = iv >= 0;
   fa.want_q = tominec;
-  fa.flyer = flyer ? ((iv < 0 || hv_first) ? 1 : 2) : 0;
+  fa.flyer = fwd_flyer;
+  fa.fuse_flux = fuse_ok ? 1 : 0;
+  fa.ustate = us;
+  fa.gm1dw = gm1_pair(c->gamma);
+  fa.err = c->kerr.p;
   fa.du_p = c->du_p.p;
   fa.t = c->t.p;
   fa.q = c->q.p;
@@ -1684,6 +1706,11 @@ mft_status mft_set_option(mft_ctx* c, int option, int value) {
                   "halo rows: 0 (automatic), 128 or 256");
       c->halo_rows_opt = value;
       c->fsal_valid = false;
+    } else if (option == MFT_OPT_FUSE_FLUX) {
+      MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG, "fuse flux: 0 or 1");
+      c->fuse_flux = value;
+      c->fsal_valid = false;
+      for (int& k : c->tuned_fwd_dw) k = -1;  // the tuner times the flux kernel by it
     } else if (option == MFT_OPT_ENTRY_ORDER) {
       MFT_REQUIRE(value == 0 || value == 1, MFT_ERR_ARG,
                   "entry order: 0 structure order, 1 bank-spreading");
@@ -1732,6 +1759,8 @@ mft_status mft_get_option(mft_ctx* c, int option, int* value) {
     else if (option == MFT_OPT_ADJ_EVERY) *value = c->adj_every;
     else if (option == MFT_OPT_HALO_ROWS) *value = c->fwd.halo_rows;
     else if (option == MFT_OPT_ENTRY_ORDER) *value = c->entry_order;
+    else if (option == MFT_OPT_FUSE_FLUX) *value = c->fuse_flux;
+    else if (option == MFT_OPT_FLUX_FUSED) *value = c->last_flux_fused;
     else if (option == MFT_OPT_BANK_FWD) *value = c->fwd.bank_milli;
     else if (option == MFT_OPT_BANK_REV) *value = c->rev.bank_milli;
     else if (option == MFT_OPT_IGR_ITERS) {

@@ -58,15 +58,13 @@ static __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z,
 
 // Per node: the state as double-word pairs and the Euler flux pair evaluated from them in
 // double-word arithmetic (the textbook flux, one reciprocal for both velocities; each
-// operation is accurate to about 2 u^2 of its operands, u = 2^-24), stored as pairs:
-// F[i] = (Fx_0..3, Fy_0..3), U[i] = (u_0..3), 8 floats per 4 values.  gm1 = gamma - 1 as
-// a pair.  The only FP64 operations are the four splits of the state.
-__global__ void k_prep_euler_dw(int64_t n, float2 gm1, const double* __restrict__ u,
-                                float4* __restrict__ F, float4* __restrict__ U) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double2* ui = reinterpret_cast<const double2*>(u) + i * 2;
-  const double2 a = ui[0], b = ui[1];
+// operation is accurate to about 2 u^2 of its operands, u = 2^-24), as the records the
+// forward gather reads: F = (Fx_0..3, Fy_0..3) in four float4 (Fx_0 = m1, Fy_0 = m2),
+// U = (u_0..3) in two, 8 floats per 4 values.  gm1 = gamma - 1 as a pair.  The only FP64
+// operations are the four splits of the state.  Shared by the flux kernel and the staged
+// gathers that form the records while staging, so both give the same bits.
+static __device__ __forceinline__ void euler_records(double2 a, double2 b, float2 gm1,
+                                                     float4* F, float4* U) {
   const float2 rho = dw::split(a.x), m1 = dw::split(a.y), m2 = dw::split(b.x);
   const float2 en = dw::split(b.y);
   const float2 r = dw::recip(rho);
@@ -76,13 +74,59 @@ __global__ void k_prep_euler_dw(int64_t n, float2 gm1, const double* __restrict_
   const float2 ep = dw::add(en, p);
   const float2 fx1 = dw::add(a1, p), fx2 = dw::mul(m1, v2), fx3 = dw::mul(ep, v1);
   const float2 fy1 = dw::mul(m2, v1), fy2 = dw::add(a2, p), fy3 = dw::mul(ep, v2);
+  F[0] = make_float4(m1.x, m1.y, fx1.x, fx1.y);
+  F[1] = make_float4(fx2.x, fx2.y, fx3.x, fx3.y);
+  F[2] = make_float4(m2.x, m2.y, fy1.x, fy1.y);
+  F[3] = make_float4(fy2.x, fy2.y, fy3.x, fy3.y);
+  U[0] = make_float4(rho.x, rho.y, m1.x, m1.y);
+  U[1] = make_float4(m2.x, m2.y, en.x, en.y);
+}
+
+__global__ void k_prep_euler_dw(int64_t n, float2 gm1, const double* __restrict__ u,
+                                float4* __restrict__ F, float4* __restrict__ U) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2* ui = reinterpret_cast<const double2*>(u) + i * 2;
+  float4 f[4], uu[2];
+  euler_records(ui[0], ui[1], gm1, f, uu);
   float4* Fi = F + i * 4;
-  Fi[0] = make_float4(m1.x, m1.y, fx1.x, fx1.y);
-  Fi[1] = make_float4(fx2.x, fx2.y, fx3.x, fx3.y);
-  Fi[2] = make_float4(m2.x, m2.y, fy1.x, fy1.y);
-  Fi[3] = make_float4(fy2.x, fy2.y, fy3.x, fy3.y);
-  U[i * 2] = make_float4(rho.x, rho.y, m1.x, m1.y);
-  U[i * 2 + 1] = make_float4(m2.x, m2.y, en.x, en.y);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) Fi[k] = f[k];
+  U[i * 2] = uu[0];
+  U[i * 2 + 1] = uu[1];
+}
+
+// Staging with the records formed on the fly: each thread reads the FP64 states of list
+// entries q and q + blockDim.x (both loads in flight together), forms their records
+// (euler_records) and writes the NCH chunks of each into shared memory at k * stride + q,
+// the layout stage_halo's copies give.  Returns false for a group without a list.
+template <int NCH>
+static __device__ __forceinline__ bool stage_halo_records(const EllView& ell, float4* sm,
+                                                          const double* __restrict__ u,
+                                                          float2 gm1) {
+  const int h0 = __ldg(ell.halo_off + blockIdx.x);
+  const int nh = __ldg(ell.halo_off + blockIdx.x + 1) - h0;
+  if (nh <= 0) return false;  // block-uniform
+  const int hs = ell.halo_stride;
+  const double2* __restrict__ u2 = reinterpret_cast<const double2*>(u);
+  for (int q0 = threadIdx.x; q0 < nh; q0 += 2 * blockDim.x) {
+    const int q1 = q0 + blockDim.x;
+    const int64_t c0 = __ldg(ell.halo_col + h0 + q0);
+    const int64_t c1 = q1 < nh ? (int64_t)__ldg(ell.halo_col + h0 + q1) : c0;
+    const double2 a0 = __ldg(u2 + c0 * 2), b0 = __ldg(u2 + c0 * 2 + 1);
+    const double2 a1 = __ldg(u2 + c1 * 2), b1 = __ldg(u2 + c1 * 2 + 1);
+    float4 rec[6];
+    euler_records(a0, b0, gm1, rec, rec + 4);
+#pragma unroll
+    for (int k = 0; k < NCH; ++k) sm[k * hs + q0] = rec[k];
+    if (q1 < nh) {
+      euler_records(a1, b1, gm1, rec, rec + 4);
+#pragma unroll
+      for (int k = 0; k < NCH; ++k) sm[k * hs + q1] = rec[k];
+    }
+  }
+  __syncthreads();
+  return true;
 }
 
 // One stencil entry of the forward gather: weights and the neighbour's flux and state
@@ -167,18 +211,29 @@ static __device__ __forceinline__ void fwd_accum(const FwdEntry& e, dw::Acc* f, 
 // records in shared memory and read them from there (groups without a list gather
 // directly); PIPE 0 or 2 then sets the loop's unrolling.  HINT: the staged loop reads the
 // streamed positions and weights with an L2 evict-first policy and the epilogue writes t,
-// q and the partial du with evict-last, which the transpose gather reads next.
-template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO, bool HINT = false>
+// q and the partial du with evict-last, which the transpose gather reads next.  FUSE: the
+// staged records are formed from the FP64 state while staging (stage_halo_records), so
+// the flux kernel's pairs are not read; launched only when every group is staged (a group
+// without a list sets MFT_ERR_STATE in *a.err and its rows are not written).
+template <bool WT, bool WQ, int FLY, int PIPE, int MINB, bool PREF, bool HALO, bool HINT = false,
+          bool FUSE = false>
 __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_dw(FwdArgs a) {
   const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
   const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
   const float* __restrict__ U = reinterpret_cast<const float*>(a.udw);
   extern __shared__ float4 hsm[];
   bool staged = false;
-  if (HALO) {
+  constexpr int kNch = (WT || WQ || FLY) ? 6 : 4;
+  if (HALO && FUSE) {
+    staged = stage_halo_records<kNch>(a.ell, hsm, a.ustate, a.gm1dw);
+    if (!staged) {
+      if (threadIdx.x == 0) atomicExch(a.err, MFT_ERR_STATE);
+      return;
+    }
+  } else if (HALO) {
     const float4* F4 = reinterpret_cast<const float4*>(a.Fdw);
     const float4* U4 = reinterpret_cast<const float4*>(a.udw);
-    staged = stage_halo<(WT || WQ || FLY) ? 6 : 4>(
+    staged = stage_halo<kNch>(
         a.ell, hsm, [&](int k, int64_t c) { return k < 4 ? F4 + c * 4 + k : U4 + c * 2 + (k - 4); });
   }
   if (r >= a.n) return;
@@ -518,13 +573,19 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_rev_euler_d
 
 }  // namespace
 
+float2 gm1_pair(double gamma) {
+  const double gm1 = gamma - 1.0;
+  const float h = (float)gm1;
+  return make_float2(h, (float)(gm1 - (double)h));
+}
+
+bool dw_fwd_fuses(int variant) { return variant == 7 || variant == 11 || variant == 12; }
+
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s) {
   if (n <= 0) return;
-  const double gm1 = gamma - 1.0;
-  const float h = (float)gm1;
-  const float2 gm1dw = make_float2(h, (float)(gm1 - (double)h));
-  k_prep_euler_dw<<<grid_for(n, 256), 256, 0, s>>>(n, gm1dw, u, reinterpret_cast<float4*>(F),
+  k_prep_euler_dw<<<grid_for(n, 256), 256, 0, s>>>(n, gm1_pair(gamma), u,
+                                                   reinterpret_cast<float4*>(F),
                                                    reinterpret_cast<float4*>(U));
   MFT_LAUNCH_CHECK();
 }
@@ -567,6 +628,15 @@ void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
   const unsigned g = grid_for(n, kBlock);
   constexpr int nch = (WT || WQ || FLY) ? 6 : 4;
   if (variant >= 6 && !a.ell.halo_off) variant = 2;
+  if (a.fuse_flux && a.ell.halo_off && dw_fwd_fuses(variant)) {
+    MFT_REQUIRE(a.ustate && a.err, MFT_ERR_STATE, "fused staging needs the state and error word");
+    switch (variant) {
+      case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, false, true>, a, nch, n, s); break;
+      case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true, false, true>, a, nch, n, s); break;
+      default: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, true, true>, a, nch, n, s); break;
+    }
+    return;
+  }
   switch (variant) {
     case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false, false><<<g, kBlock, 0, s>>>(a); break;
     case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, false, false><<<g, kBlock, 0, s>>>(a); break;

@@ -87,6 +87,8 @@ struct mft_ctx {
   int layout_order = 1;  // 1: operator layout rows in Morton order of the nodes
   int halo_rows_opt = 0;  // rows per staged group: 0 automatic, else 128 or 256
   int entry_order = 1;    // staged rows: 1 bank-spreading entry order, 0 structure order
+  int fuse_flux = 1;      // staged double-word forward gathers may form the flux records
+  int last_flux_fused = 0;  // the last evaluation did (and skipped the flux kernel)
   int tuned_fwd[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   int tuned_rev[4] = {-1, -1, -1, -1};
   int last_fwd_choice = -1, last_rev_choice = -1;

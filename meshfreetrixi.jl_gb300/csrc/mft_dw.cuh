@@ -22,18 +22,36 @@
 
 #include <cuda_runtime.h>
 
+#include "mft_fpbits.h"
+
 namespace mft {
 namespace dw {
 
+// (double)f, exact, on the integer pipe where the result is normal or zero.
+static __device__ __forceinline__ double f2d(float f) {
+  uint32_t hi, lo;
+  if (fpbits::f2d_words(__float_as_uint(f), &hi, &lo))
+    return __hiloint2double((int)hi, (int)lo);
+  return (double)f;
+}
+
+// RN32(x), on the integer pipe where the result is a normal float or zero.
+static __device__ __forceinline__ float d2f(double x) {
+  uint32_t r;
+  if (fpbits::d2f_bits((uint32_t)__double2hiint(x), (uint32_t)__double2loint(x), &r))
+    return __uint_as_float(r);
+  return __double2float_rn(x);
+}
+
 // x -> (h, l): h = RN32(x), l = RN32(x - h) (x - h is exact in FP64).
 static __device__ __forceinline__ float2 split(double x) {
-  const float h = __double2float_rn(x);
-  const float l = __double2float_rn(__dsub_rn(x, (double)h));
+  const float h = d2f(x);
+  const float l = d2f(__dsub_rn(x, f2d(h)));
   return make_float2(h, l);
 }
 
 static __device__ __forceinline__ double value(float2 a) {
-  return __dadd_rn((double)a.x, (double)a.y);
+  return __dadd_rn(f2d(a.x), f2d(a.y));
 }
 
 // Running sum of products: s is the float running sum, c the float carry of every
@@ -59,7 +77,7 @@ static __device__ __forceinline__ void fma_acc(Acc& acc, float2 a, float2 b) {
 
 // The accumulated value rounded once to FP64.
 static __device__ __forceinline__ double to_double(const Acc& a) {
-  return __dadd_rn((double)a.s, (double)a.c);
+  return __dadd_rn(f2d(a.s), f2d(a.c));
 }
 
 // The accumulated value as a normalised double-word pair (TwoSum of s and c).

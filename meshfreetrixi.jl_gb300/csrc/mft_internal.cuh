@@ -263,6 +263,14 @@ struct FwdArgs {
   // (ea, whose norms must be ready at launch) and t is written as s = eps * t
   int fuse_eps;
   EpsArgs ea;
+  // double-word staged gathers: with fuse_flux the groups' state and flux pairs are formed
+  // while staging, from ustate (the FP64 state after BC pass 1) and gm1dw (gamma - 1 as a
+  // pair), instead of read from Fdw / udw (which the flux kernel then need not write).
+  // Only when every row group is staged; a block of a group without a list sets *err.
+  int fuse_flux;
+  const double* ustate;
+  float2 gm1dw;
+  int* err;
 };
 void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 // 3D clouds (mft_apply3d.cu): per-node Euler fluxes F = (F_x, F_y, F_z) (n x 15), and the
@@ -279,9 +287,14 @@ void launch_fwd3_dw(const FwdArgs& a, cudaStream_t s);
 // transpose gather.
 void launch_prep_euler_dw(int64_t n, double gamma, const double* u, float2* F, float2* U,
                           cudaStream_t s);
-// variant: 0..5, the kernel variants the autotuner chooses among (same sums, same order)
+// variant: 0..12, the kernel variants the autotuner chooses among (same sums, same order)
 constexpr int kDwVariants = 13;
 void launch_fwd_dw(const FwdArgs& a, int variant, cudaStream_t s);
+// Whether forward variant `variant` forms the flux pairs while staging when a.fuse_flux
+// is set (the staged variants 7, 11 and 12).
+bool dw_fwd_fuses(int variant);
+// The pairs of gamma - 1 (h = RN32(gamma - 1), l = RN32 of the remainder).
+float2 gm1_pair(double gamma);
 void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 
 // Reductions for the residual viscosity normalisation (last-block-done pattern).

@@ -27,6 +27,7 @@ OPT_DW_VARIANT = 5
 OPT_HALO_STAGED_FWD, OPT_HALO_STAGED_REV, OPT_HALO_GROUPS, OPT_IGR_ITERS = 6, 7, 8, 9
 OPT_ADJ_EVERY, OPT_HALO_ROWS = 10, 11
 OPT_ENTRY_ORDER, OPT_BANK_FWD, OPT_BANK_REV = 12, 13, 14
+OPT_FUSE_FLUX, OPT_FLUX_FUSED = 15, 16
 ARITH_AUTO, ARITH_DFMA, ARITH_DW = 0, 1, 2
 GATHER_AUTO, GATHER_THREAD, GATHER_STAGED, GATHER_HALO = 0, 1, 2, 3
 

@@ -143,3 +143,70 @@ def test_entry_order_spreads_banks_and_keeps_the_sums(gpu_lib):
     with pytest.raises(L.MFTError):
         ctx.set_option(L.OPT_ENTRY_ORDER, 2)
     ctx.close()
+
+
+def test_fused_flux_records_are_bit_identical(gpu_lib):
+    """With every row group staged, the forward variants 7, 11 and 12 form the neighbours'
+    state and flux pairs while staging and the flux kernel is skipped
+    (MFT_OPT_FUSE_FLUX 1, the default; MFT_OPT_FLUX_FUSED reads back 1): the same bits as
+    with the flux kernel (MFT_OPT_FUSE_FLUX 0) and as an unfused variant, for forced
+    variants and for the autotuned choice, over several evaluations and an SSP-RK3 run
+    (graph-replayed steps).  With groups left unstaged (a half-shuffled layout) nothing is
+    fused."""
+    from meshfree_gb300 import workloads as W
+    pts, h = W.riemann_cloud(96)
+    L, dom, semi = _problem(pts, 1)
+    ctx = dom.ctx
+    u0 = W.riemann_ic(pts)
+    du0 = np.empty_like(u0)
+    ctx.rhs(du0, u0.copy(), 0.0)
+    ctx.set_rv_state(du0 * 1.01, 2)
+
+    def rhs():
+        du = np.empty_like(u0)
+        ctx.rhs(du, u0.copy(), 0.0)
+        return du
+
+    ctx.set_option(L.OPT_DW_VARIANT, 6)
+    ref = rhs()
+    assert ctx.get_option(L.OPT_FLUX_FUSED) == 0
+    for fuse in (1, 0):
+        ctx.set_option(L.OPT_FUSE_FLUX, fuse)
+        for v in (7, 11, 12, -1):
+            ctx.set_option(L.OPT_DW_VARIANT, v)
+            for _ in range(3 if v == -1 else 2):
+                assert np.array_equal(rhs(), ref), (fuse, v)
+            if v >= 0:
+                assert ctx.get_option(L.OPT_FLUX_FUSED) == fuse
+    # trajectories: graph-replayed steps with the fused and the unfused forward variant
+    out = []
+    for v in (7, 8):
+        ctx.set_option(L.OPT_FUSE_FLUX, 1)
+        ctx.set_option(L.OPT_DW_VARIANT, v)
+        ctx.set_state(u0, 0.0)
+        ctx.history_init(2)
+        ctx.ssprk33(0.05 * h, 6)
+        out.append(ctx.get_state()[0])
+    assert np.array_equal(out[0], out[1])
+    ctx.close()
+    # groups without a list (a 32 x 32 cloud in node order, second half shuffled): the
+    # forced variant 7 runs unfused
+    pts2, _ = W.riemann_cloud(32)
+    n = pts2.shape[0]
+    rng = np.random.default_rng(4)
+    perm = np.arange(n)
+    perm[n // 2:] = n // 2 + rng.permutation(n - n // 2)
+    pts2 = np.ascontiguousarray(pts2[perm])
+    L, dom, semi = _problem(pts2, 0)
+    ctx = dom.ctx
+    u2 = W.riemann_ic(pts2)
+    ctx.set_option(L.OPT_DW_VARIANT, 7)
+    du = np.empty_like(u2)
+    ctx.rhs(du, u2.copy(), 0.0)
+    assert ctx.get_option(L.OPT_HALO_STAGED_FWD) < ctx.get_option(L.OPT_HALO_GROUPS)
+    assert ctx.get_option(L.OPT_FLUX_FUSED) == 0
+    ctx.set_option(L.OPT_DW_VARIANT, 6)
+    du6 = np.empty_like(u2)
+    ctx.rhs(du6, u2.copy(), 0.0)
+    assert np.array_equal(du, du6)
+    ctx.close()
