@@ -1004,7 +1004,8 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
       }
       ProfScope ps(c, MFT_K_LEXMAX);
       launch_lexmax_seg(c->nseg, c->d_seg_off.p, kSegBlocks, V, us, c->seg_mean.p, mode,
-                        c->seg_partial.p, c->seg_counter.p + c->nseg, c->seg_norms.p, st);
+                        c->seg_partial.p, c->seg_counter.p + c->nseg, c->seg_norms.p, st,
+                        !c->prof_on);
     } else {
       const double denom = mode == 0 ? (double)n * V : (double)n;
       {
@@ -1014,11 +1015,16 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
       }
       ProfScope ps(c, MFT_K_LEXMAX);
       launch_lexmax(n, V, us, c->mean.p, mode, c->red_partial.p, c->red_counter.p + 1,
-                    c->norms.p, c->red_blocks, st);
+                    c->norms.p, c->red_blocks, st, !c->prof_on);
     }
   };
+  // With the viscosity formed in the double-word forward gather's epilogue, the norms run
+  // on this stream right before that gather, which is launched as their programmatic
+  // dependent: its staging and sums overlap the reductions and only its epilogue waits.
+  // Otherwise they run on the side stream beside the flux kernel and the forward gather.
+  const bool fuse_eps = dw && iv >= 0 && !(tominec && hv_first);
   bool forked = false;
-  if (iv >= 0 && c->src_kind[iv] == MFT_SRC_RV && !c->prof_on) {
+  if (iv >= 0 && c->src_kind[iv] == MFT_SRC_RV && !c->prof_on && !fuse_eps) {
     NvtxRange rng("source terms");
     MFT_CUDA(cudaEventRecord(c->ev_fork, s));
     MFT_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
@@ -1150,7 +1156,6 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     ea.tab = c->capturing ? c->d_tab.p : nullptr;
     ea.ctr = c->d_ctr.p;
   }
-  const bool fuse_eps = dw && iv >= 0 && !(tominec && hv_first);
   if (dw) {
     for (int d = 0; d < 3; ++d) fa.wdw[d] = d < c->dim ? c->fwdw[d].p : nullptr;
     fa.wldw = wl_slot >= 0 ? c->fwdw[wl_slot].p : nullptr;
@@ -1160,9 +1165,13 @@ void eval_rhs(mft_ctx* c, double* us, float* us32, double t, const Epilogue& ep_
     fa.qdw = c->qdw.p;
   }
   if (fuse_eps) {
-    // the norms of the residual viscosity must be complete before the gather
-    if (forked) MFT_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
-    else if (c->src_kind[iv] == MFT_SRC_RV) rv_norms(s);
+    // the norms of the residual viscosity must be complete before the gather's epilogue
+    if (c->src_kind[iv] == MFT_SRC_RV) {
+      rv_norms(s);
+      // not while profiling (events between the launches) nor when this launch tunes
+      // the variant (timing launches would sit between the reductions and the gather)
+      fa.pdl = (!c->prof_on && fwd_known >= 0) ? 1 : 0;
+    }
     fa.fuse_eps = 1;
     fa.ea = ea;
     fa.ea.du_p = c->du_p.p;

@@ -223,33 +223,71 @@ __global__ void __launch_bounds__(kBlock) k_fwd_adv_f64(FwdArgs a) {
 
 // ------------------------------------------------------------------ reductions
 
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWarps = kBlock / 32;
+
+// The warp's totals of V FP64 partial sums per lane.  For V = 4 the lanes first
+// reduce-scatter (lanes 16 apart exchange half of their sums, then lanes 8 apart half of
+// the rest), so that each FP64 addition of those steps serves two or four sums; then each
+// group of 8 lanes finishes its sum with a shuffle tree.  Afterwards lane l holds the
+// total of sum l >> 3 (V = 4) or of the only sum (V = 1).  Six full-warp additions for
+// four sums instead of twenty; a fixed order, so the result is deterministic.
 template <int V>
-__device__ void block_sum(double* v) {
-  __shared__ double sh[V][kBlock / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+__device__ __forceinline__ double warp_sum_scatter(const double* v, int lane) {
+  static_assert(V == 1 || V == 4, "one or four sums");
+  double k;
+  if (V == 4) {
+    const bool hi16 = (lane & 16) != 0;
+    double a0 = hi16 ? v[2 % V] : v[0], a1 = hi16 ? v[3 % V] : v[1 % V];
+    const double s0 = hi16 ? v[0] : v[2 % V], s1 = hi16 ? v[1 % V] : v[3 % V];
+    a0 = dadd(a0, __shfl_xor_sync(kFull, s0, 16));
+    a1 = dadd(a1, __shfl_xor_sync(kFull, s1, 16));
+    const bool hi8 = (lane & 8) != 0;
+    k = hi8 ? a1 : a0;
+    k = dadd(k, __shfl_xor_sync(kFull, hi8 ? a0 : a1, 8));
 #pragma unroll
-  for (int k = 0; k < V; ++k) {
-    double x = v[k];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[k][wid] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+    for (int o = 4; o > 0; o >>= 1) k = dadd(k, __shfl_xor_sync(kFull, k, o));
+  } else {
+    k = v[0];
 #pragma unroll
-    for (int k = 0; k < V; ++k) {
-      double x = sh[k][0];
-      for (int w = 1; w < kBlock / 32; ++w) x += sh[k][w];
-      v[k] = x;
-    }
+    for (int o = 16; o > 0; o >>= 1) k = dadd(k, __shfl_xor_sync(kFull, k, o));
   }
+  return k;
 }
 
-// Sum of u per variable; the last block to finish reduces the block partials with a
-// fixed strided-then-tree order (deterministic) and writes mean = sum / denom.
+// Block totals of V partial sums per thread: lane k < V of warp 0 returns total k (other
+// threads return 0).  The warps' totals are combined by warp 0 with a shuffle tree.
 template <int V>
+__device__ double block_sum_lanes(const double* v) {
+  static_assert(kWarps * V <= 32, "one warp combines the warps' totals");
+  __shared__ double sh[V * kWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const double k = warp_sum_scatter<V>(v, lane);
+  if ((lane & (V == 4 ? 7 : 31)) == 0) sh[(V == 4 ? lane >> 3 : 0) * kWarps + wid] = k;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    double x = lane < V * kWarps ? sh[lane] : 0.0;  // lane = sum * kWarps + warp
+#pragma unroll
+    for (int o = kWarps / 2; o > 0; o >>= 1) x = dadd(x, __shfl_xor_sync(kFull, x, o));
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const double t = __shfl_sync(kFull, x, q * kWarps);
+      if (lane == q) r = t;
+    }
+  }
+  __syncthreads();
+  return r;
+}
+
+// Sum of u per variable; the last block to finish reduces the block partials in a fixed
+// order (deterministic) and writes mean = sum / denom.  A grid launched after this one
+// with launch_k(pdl) may start at once (it waits for the means with pdl_wait).
+template <int V, bool VEC>
 __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __restrict__ u,
                                                  double denom, double* partial,
                                                  unsigned* counter, double* mean) {
+  pdl_trigger();
   double acc[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) acc[k] = 0.0;
@@ -258,32 +296,40 @@ __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __rest
 #pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kBlock) {
+    if (VEC && V == 4) {
+      const double2* u2 = reinterpret_cast<const double2*>(u) + i * 2;
+      const double2 a = __ldg(u2), b = __ldg(u2 + 1);
+      acc[0] = dadd(acc[0], a.x); acc[1 % V] = dadd(acc[1 % V], a.y);
+      acc[2 % V] = dadd(acc[2 % V], b.x); acc[3 % V] = dadd(acc[3 % V], b.y);
+    } else {
 #pragma unroll
-    for (int k = 0; k < V; ++k) acc[k] += u[i * V + k];
+      for (int k = 0; k < V; ++k) acc[k] = dadd(acc[k], u[i * V + k]);
+    }
   }
-  block_sum<V>(acc);
+  const double tot = block_sum_lanes<V>(acc);
   __shared__ int last;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    double t[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = acc[k];
-    __threadfence();
-    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    for (int k = 0; k < V; ++k) t[k] = __shfl_sync(kFull, tot, k);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = t[k];
+      __threadfence();
+      last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
 #pragma unroll
   for (int k = 0; k < V; ++k) acc[k] = 0.0;
-#pragma unroll 4
   for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock)
 #pragma unroll
-    for (int k = 0; k < V; ++k) acc[k] += __ldcg(partial + b * V + k);
-  block_sum<V>(acc);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < V; ++k) mean[k] = acc[k] / denom;
-    *counter = 0u;
-  }
+    for (int k = 0; k < V; ++k) acc[k] = dadd(acc[k], __ldcg(partial + b * V + k));
+  const double all = block_sum_lanes<V>(acc);
+  if (threadIdx.x < V) mean[threadIdx.x] = all / denom;
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
 // ode_maximum(|u - mean|) (mpi.jl:61-81): lexicographic Base.isless order on vectors
@@ -292,6 +338,8 @@ __global__ void __launch_bounds__(kBlock) k_mean(int64_t n, const double* __rest
 // component orders like its value (NaN above +Inf, as Base.isless does): the maximum
 // is taken on 64-bit integer keys.
 typedef unsigned long long u64;
+// |x| as a bit pattern: the sign bit cleared (fabs, without an FP64 instruction)
+constexpr u64 kAbsMask = 0x7FFFFFFFFFFFFFFFull;
 
 template <int V>
 __device__ __forceinline__ bool key_less(const u64* a, const u64* b) {
@@ -315,38 +363,82 @@ __device__ __forceinline__ void key_max_into(u64* a, const u64* b, int max_mode)
   }
 }
 
+// The block's maximum key (integer shuffles and one exchange through shared memory);
+// valid in lane 0 of warp 0.  The maximum is a value, not a position: any order gives it.
 template <int V>
 __device__ void block_keymax(u64* best, int max_mode) {
-  __shared__ u64 sh[kBlock][V];
+  __shared__ u64 sh[kWarps][V];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < V; ++k) sh[threadIdx.x][k] = best[k];
-  __syncthreads();
-  for (int s = kBlock / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) key_max_into<V>(sh[threadIdx.x], sh[threadIdx.x + s], max_mode);
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    u64 c[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) c[k] = __shfl_xor_sync(kFull, best[k], o);
+    key_max_into<V>(best, c, max_mode);
   }
+  if (lane == 0)
 #pragma unroll
-  for (int k = 0; k < V; ++k) best[k] = sh[0][k];
+    for (int k = 0; k < V; ++k) sh[wid][k] = best[k];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) best[k] = lane < kWarps ? sh[lane][k] : 0ull;
+#pragma unroll
+    for (int o = kWarps / 2; o > 0; o >>= 1) {
+      u64 c[V];
+#pragma unroll
+      for (int k = 0; k < V; ++k) c[k] = __shfl_xor_sync(kFull, best[k], o);
+      key_max_into<V>(best, c, max_mode);
+    }
+  }
   __syncthreads();
 }
 
+// The norms from the maximum key (warp 0; lane k < V writes component k).
 template <int V>
+__device__ __forceinline__ void write_norms(const u64* best, double* norms) {
+  const int lane = threadIdx.x & 31;
+  double v = 0.0;
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    const double t = __longlong_as_double((long long)__shfl_sync(kFull, best[k], 0));
+    if (lane == k) v = t;
+  }
+  if (lane < V) {
+    const double nv = v == 0.0 ? 2.220446049250313e-16 : v;
+    norms[lane] = nv;
+    norms[V + lane] = 1.0 / nv;
+  }
+}
+
+template <int V, bool VEC>
 __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __restrict__ u,
                                                    const double* __restrict__ mean, int max_mode,
                                                    double* partial, unsigned* counter,
                                                    double* norms) {
+  pdl_trigger();
+  pdl_wait();  // the means (k_mean, which this grid may overlap)
   double m[V];
   u64 best[V];
 #pragma unroll
-  for (int k = 0; k < V; ++k) { m[k] = mean[k]; best[k] = 0ull; }
+  for (int k = 0; k < V; ++k) { m[k] = __ldcg(mean + k); best[k] = 0ull; }
   // Threads without nodes keep the all-zero key, the smallest possible: it can only
   // tie with a real all-zero vector, which has the same value.
 #pragma unroll 4
   for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kBlock) {
+    double uv[V];
+    if (VEC && V == 4) {
+      const double2* u2 = reinterpret_cast<const double2*>(u) + i * 2;
+      const double2 a = __ldg(u2), b = __ldg(u2 + 1);
+      uv[0] = a.x; uv[1 % V] = a.y; uv[2 % V] = b.x; uv[3 % V] = b.y;
+    } else {
+#pragma unroll
+      for (int k = 0; k < V; ++k) uv[k] = u[i * V + k];
+    }
     u64 x[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) x[k] = (u64)__double_as_longlong(fabs(dsub(u[i * V + k], m[k])));
+    for (int k = 0; k < V; ++k) x[k] = (u64)__double_as_longlong(dsub(uv[k], m[k])) & kAbsMask;
     key_max_into<V>(best, x, max_mode);
   }
   block_keymax<V>(best, max_mode);
@@ -362,7 +454,6 @@ __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __re
   __threadfence();
 #pragma unroll
   for (int k = 0; k < V; ++k) best[k] = 0ull;
-#pragma unroll 4
   for (unsigned b = threadIdx.x; b < gridDim.x; b += kBlock) {
     u64 c[V];
 #pragma unroll
@@ -370,25 +461,19 @@ __global__ void __launch_bounds__(kBlock) k_lexmax(int64_t n, const double* __re
     key_max_into<V>(best, c, max_mode);
   }
   block_keymax<V>(best, max_mode);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const double v = __longlong_as_double((long long)best[k]);
-      norms[k] = v == 0.0 ? 2.220446049250313e-16 : v;
-      norms[V + k] = 1.0 / norms[k];
-    }
-    *counter = 0u;
-  }
+  if (threadIdx.x < 32) write_norms<V>(best, norms);
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
 // Segmented versions for ensembles: segment s owns nodes [off[s], off[s+1]) and is
 // reduced by `per` blocks (blockIdx.x = s * per + part); the last block of a segment
-// finishes it with the same strided-then-tree order as above.
+// finishes it in the same fixed order as above.
 template <int V>
 __global__ void __launch_bounds__(kBlock) k_mean_seg(const int64_t* __restrict__ off, int per,
                                                      const double* __restrict__ u, int mode,
                                                      double* partial, unsigned* counter,
                                                      double* mean) {
+  pdl_trigger();
   const int sg = blockIdx.x / per, part = blockIdx.x % per;
   const int64_t lo = off[sg], hi = off[sg + 1];
   double acc[V];
@@ -396,15 +481,20 @@ __global__ void __launch_bounds__(kBlock) k_mean_seg(const int64_t* __restrict__
   for (int k = 0; k < V; ++k) acc[k] = 0.0;
   for (int64_t i = lo + (int64_t)part * kBlock + threadIdx.x; i < hi; i += (int64_t)per * kBlock) {
 #pragma unroll
-    for (int k = 0; k < V; ++k) acc[k] += u[i * V + k];
+    for (int k = 0; k < V; ++k) acc[k] = dadd(acc[k], u[i * V + k]);
   }
-  block_sum<V>(acc);
+  const double tot = block_sum_lanes<V>(acc);
   __shared__ int last;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    double t[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = acc[k];
-    __threadfence();
-    last = (atomicAdd(counter + sg, 1u) == (unsigned)per - 1);
+    for (int k = 0; k < V; ++k) t[k] = __shfl_sync(kFull, tot, k);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < V; ++k) partial[blockIdx.x * V + k] = t[k];
+      __threadfence();
+      last = (atomicAdd(counter + sg, 1u) == (unsigned)per - 1);
+    }
   }
   __syncthreads();
   if (!last) return;
@@ -413,14 +503,13 @@ __global__ void __launch_bounds__(kBlock) k_mean_seg(const int64_t* __restrict__
   for (int k = 0; k < V; ++k) acc[k] = 0.0;
   for (int b = threadIdx.x; b < per; b += kBlock)
 #pragma unroll
-    for (int k = 0; k < V; ++k) acc[k] += __ldcg(partial + (sg * per + b) * V + k);
-  block_sum<V>(acc);
-  if (threadIdx.x == 0) {
+    for (int k = 0; k < V; ++k) acc[k] = dadd(acc[k], __ldcg(partial + (sg * per + b) * V + k));
+  const double all = block_sum_lanes<V>(acc);
+  if (threadIdx.x < V) {
     const double denom = mode == 0 ? (double)(hi - lo) * V : (double)(hi - lo);
-#pragma unroll
-    for (int k = 0; k < V; ++k) mean[sg * V + k] = acc[k] / denom;
-    counter[sg] = 0u;
+    mean[sg * V + threadIdx.x] = all / denom;
   }
+  if (threadIdx.x == 0) counter[sg] = 0u;
 }
 
 template <int V>
@@ -429,16 +518,18 @@ __global__ void __launch_bounds__(kBlock) k_lexmax_seg(const int64_t* __restrict
                                                        const double* __restrict__ mean,
                                                        int max_mode, double* partial,
                                                        unsigned* counter, double* norms) {
+  pdl_trigger();
+  pdl_wait();  // the means (k_mean_seg)
   const int sg = blockIdx.x / per, part = blockIdx.x % per;
   const int64_t lo = off[sg], hi = off[sg + 1];
   double m[V];
   u64 best[V];
 #pragma unroll
-  for (int k = 0; k < V; ++k) { m[k] = mean[sg * V + k]; best[k] = 0ull; }
+  for (int k = 0; k < V; ++k) { m[k] = __ldcg(mean + sg * V + k); best[k] = 0ull; }
   for (int64_t i = lo + (int64_t)part * kBlock + threadIdx.x; i < hi; i += (int64_t)per * kBlock) {
     u64 x[V];
 #pragma unroll
-    for (int k = 0; k < V; ++k) x[k] = (u64)__double_as_longlong(fabs(dsub(u[i * V + k], m[k])));
+    for (int k = 0; k < V; ++k) x[k] = (u64)__double_as_longlong(dsub(u[i * V + k], m[k])) & kAbsMask;
     key_max_into<V>(best, x, max_mode);
   }
   block_keymax<V>(best, max_mode);
@@ -462,16 +553,8 @@ __global__ void __launch_bounds__(kBlock) k_lexmax_seg(const int64_t* __restrict
     key_max_into<V>(best, c, max_mode);
   }
   block_keymax<V>(best, max_mode);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const double v = __longlong_as_double((long long)best[k]);
-      const double nv = v == 0.0 ? 2.220446049250313e-16 : v;
-      norms[sg * 2 * V + k] = nv;
-      norms[sg * 2 * V + V + k] = 1.0 / nv;
-    }
-    counter[sg] = 0u;
-  }
+  if (threadIdx.x < 32) write_norms<V>(best, norms + sg * 2 * V);
+  if (threadIdx.x == 0) counter[sg] = 0u;
 }
 
 // ------------------------------------------------------------------ viscosity
@@ -750,19 +833,26 @@ void launch_fwd_f64(const FwdArgs& a, cudaStream_t s) {
 
 void launch_mean(int64_t n, int V, const double* u, double denom, double* partial,
                  unsigned* counter, double* mean, int nblocks, cudaStream_t s) {
-  if (V == 4) k_mean<4><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
-  else k_mean<1><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
+  const bool vec = (reinterpret_cast<uintptr_t>(u) & 15) == 0;
+  if (V == 4 && vec) k_mean<4, true><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
+  else if (V == 4) k_mean<4, false><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
+  else k_mean<1, false><<<nblocks, kBlock, 0, s>>>(n, u, denom, partial, counter, mean);
   MFT_LAUNCH_CHECK();
 }
 
 void launch_lexmax(int64_t n, int V, const double* u, const double* mean, int max_mode,
                    double* partial, unsigned* counter, double* norms, int nblocks,
-                   cudaStream_t s) {
-  if (V == 4)
-    k_lexmax<4><<<nblocks, kBlock, 0, s>>>(n, u, mean, max_mode, partial, counter, norms);
+                   cudaStream_t s, bool pdl) {
+  const bool vec = (reinterpret_cast<uintptr_t>(u) & 15) == 0;
+  if (V == 4 && vec)
+    launch_k(k_lexmax<4, true>, nblocks, kBlock, 0, s, pdl, n, u, mean, max_mode, partial,
+             counter, norms);
+  else if (V == 4)
+    launch_k(k_lexmax<4, false>, nblocks, kBlock, 0, s, pdl, n, u, mean, max_mode, partial,
+             counter, norms);
   else
-    k_lexmax<1><<<nblocks, kBlock, 0, s>>>(n, u, mean, max_mode, partial, counter, norms);
-  MFT_LAUNCH_CHECK();
+    launch_k(k_lexmax<1, false>, nblocks, kBlock, 0, s, pdl, n, u, mean, max_mode, partial,
+             counter, norms);
 }
 
 void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double* u, int mode,
@@ -775,13 +865,14 @@ void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double*
 
 void launch_lexmax_seg(int nseg, const int64_t* off, int per, int V, const double* u,
                        const double* mean, int max_mode, double* partial, unsigned* counter,
-                       double* norms, cudaStream_t s) {
+                       double* norms, cudaStream_t s, bool pdl) {
   if (nseg <= 0) return;
   if (V == 4)
-    k_lexmax_seg<4><<<nseg * per, kBlock, 0, s>>>(off, per, u, mean, max_mode, partial, counter, norms);
+    launch_k(k_lexmax_seg<4>, nseg * per, kBlock, 0, s, pdl, off, per, u, mean, max_mode,
+             partial, counter, norms);
   else
-    k_lexmax_seg<1><<<nseg * per, kBlock, 0, s>>>(off, per, u, mean, max_mode, partial, counter, norms);
-  MFT_LAUNCH_CHECK();
+    launch_k(k_lexmax_seg<1>, nseg * per, kBlock, 0, s, pdl, off, per, u, mean, max_mode,
+             partial, counter, norms);
 }
 
 void prepare_eps(EpsArgs& a) {

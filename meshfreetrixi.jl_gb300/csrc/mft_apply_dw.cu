@@ -336,7 +336,9 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock, MINB) k_fwd_euler_d
     if (a.fuse_eps) {
       // the viscosity of this node (FP64, as k_eps forms it from the partial du held
       // here) and s = eps * t written in place of t; this FP64 work overlaps the FP32
-      // gathers of other warps
+      // gathers of other warps.  The norms come from the reductions this grid may have
+      // been launched beside (launch_k with a.pdl): wait for them here, not earlier.
+      pdl_wait();
       const double eps = visc::eps_value<4>(a.ea, i, du);
       if (a.ea.eps) a.ea.eps[i] = eps;
       const float2 e2 = dw::split(eps);
@@ -607,7 +609,8 @@ namespace {
 // in dynamic shared memory (above 48 KB that needs a per-kernel opt-in, made once per
 // kernel and device).
 template <typename Args>
-void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStream_t s) {
+void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStream_t s,
+                   bool pdl = false) {
   const size_t smem = (size_t)nch * a.ell.halo_stride * sizeof(float4);
   if (smem > 48 * 1024) {
     static std::mutex mu;
@@ -620,37 +623,38 @@ void launch_staged(void (*k)(Args), const Args& a, int nch, int64_t n, cudaStrea
                                     (int)(6 * kHaloMax * sizeof(float4))));
   }
   const int rows = a.ell.halo_rows;
-  k<<<grid_for(n, rows), rows, smem, s>>>(a);
+  launch_k(k, grid_for(n, rows), rows, smem, s, pdl, a);
 }
 
 template <bool WT, bool WQ, int FLY>
 void fwd_variant(const FwdArgs& a, int variant, int64_t n, cudaStream_t s) {
   const unsigned g = grid_for(n, kBlock);
   constexpr int nch = (WT || WQ || FLY) ? 6 : 4;
+  const bool pdl = a.pdl != 0;
   if (variant >= 6 && !a.ell.halo_off) variant = 2;
   if (a.fuse_flux && a.ell.halo_off && dw_fwd_fuses(variant)) {
     MFT_REQUIRE(a.ustate && a.err, MFT_ERR_STATE, "fused staging needs the state and error word");
     switch (variant) {
-      case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, false, true>, a, nch, n, s); break;
-      case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true, false, true>, a, nch, n, s); break;
-      default: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, true, true>, a, nch, n, s); break;
+      case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, false, true>, a, nch, n, s, pdl); break;
+      case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true, false, true>, a, nch, n, s, pdl); break;
+      default: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, true, true>, a, nch, n, s, pdl); break;
     }
     return;
   }
   switch (variant) {
-    case 1: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false, false><<<g, kBlock, 0, s>>>(a); break;
-    case 2: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
-    case 3: k_fwd_euler_dw<WT, WQ, FLY, 1, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
-    case 4: k_fwd_euler_dw<WT, WQ, FLY, 2, 6, true, false><<<g, kBlock, 0, s>>>(a); break;
-    case 5: k_fwd_euler_dw<WT, WQ, FLY, 2, 1, true, false><<<g, kBlock, 0, s>>>(a); break;
-    case 6: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 0, 3, false, true>, a, nch, n, s); break;
-    case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true>, a, nch, n, s); break;
-    case 8: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 4, false, true>, a, nch, n, s); break;
-    case 9: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 4, 3, false, true>, a, nch, n, s); break;
-    case 10: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, true, true>, a, nch, n, s); break;
-    case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true>, a, nch, n, s); break;
-    case 12: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, true>, a, nch, n, s); break;
-    default: k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false><<<g, kBlock, 0, s>>>(a); break;
+    case 1: launch_k(k_fwd_euler_dw<WT, WQ, FLY, 2, 6, false, false>, g, kBlock, 0, s, pdl, a); break;
+    case 2: launch_k(k_fwd_euler_dw<WT, WQ, FLY, 2, 1, false, false>, g, kBlock, 0, s, pdl, a); break;
+    case 3: launch_k(k_fwd_euler_dw<WT, WQ, FLY, 1, 1, false, false>, g, kBlock, 0, s, pdl, a); break;
+    case 4: launch_k(k_fwd_euler_dw<WT, WQ, FLY, 2, 6, true, false>, g, kBlock, 0, s, pdl, a); break;
+    case 5: launch_k(k_fwd_euler_dw<WT, WQ, FLY, 2, 1, true, false>, g, kBlock, 0, s, pdl, a); break;
+    case 6: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 0, 3, false, true>, a, nch, n, s, pdl); break;
+    case 7: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true>, a, nch, n, s, pdl); break;
+    case 8: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 4, false, true>, a, nch, n, s, pdl); break;
+    case 9: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 4, 3, false, true>, a, nch, n, s, pdl); break;
+    case 10: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, true, true>, a, nch, n, s, pdl); break;
+    case 11: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 3, 3, false, true>, a, nch, n, s, pdl); break;
+    case 12: launch_staged(k_fwd_euler_dw<WT, WQ, FLY, 2, 3, false, true, true>, a, nch, n, s, pdl); break;
+    default: launch_k(k_fwd_euler_dw<WT, WQ, FLY, 0, 1, false, false>, g, kBlock, 0, s, pdl, a); break;
   }
 }
 

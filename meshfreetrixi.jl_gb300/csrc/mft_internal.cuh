@@ -31,6 +31,33 @@ struct Error : std::runtime_error {
 
 #define MFT_LAUNCH_CHECK() MFT_CUDA(cudaGetLastError())
 
+// Programmatic dependent launch.  A grid launched with launch_k(..., pdl = true) may start
+// while the previous kernel in its stream still runs, once every block of that kernel has
+// executed pdl_trigger() (or exited); before reading anything that kernel writes it must
+// execute pdl_wait(), which returns when that kernel has completed and its writes are
+// visible (at once for a grid launched without the attribute).  Everything earlier in the
+// stream has completed before the previous kernel started, as with plain launches.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     bool pdl, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  MFT_CUDA(cudaLaunchKernelEx(&cfg, k, args...));
+}
+
 // Owning device buffer (cudaMalloc / cudaFree).
 template <class T>
 struct DBuf {
@@ -271,6 +298,9 @@ struct FwdArgs {
   const double* ustate;
   float2 gm1dw;
   int* err;
+  // launched as a programmatic dependent of the norm reductions just before it (the
+  // viscosity epilogue waits for them; the staging and the sums do not)
+  int pdl;
 };
 void launch_fwd_f64(const FwdArgs& a, cudaStream_t s);
 // 3D clouds (mft_apply3d.cu): per-node Euler fluxes F = (F_x, F_y, F_z) (n x 15), and the
@@ -300,16 +330,17 @@ void launch_fwd_f32(const FwdArgs& a, cudaStream_t s);
 // Reductions for the residual viscosity normalisation (last-block-done pattern).
 void launch_mean(int64_t n, int V, const double* u, double denom, double* partial,
                  unsigned* counter, double* mean, int nblocks, cudaStream_t s);
+// pdl: launched as a programmatic dependent of the k_mean launch just before it
 void launch_lexmax(int64_t n, int V, const double* u, const double* mean, int max_mode,
                    double* partial, unsigned* counter, double* norms, int nblocks,
-                   cudaStream_t s);
+                   cudaStream_t s, bool pdl = false);
 
 void launch_eps(const EpsArgs& a, cudaStream_t s);
 void launch_mean_seg(int nseg, const int64_t* off, int per, int V, const double* u, int mode,
                      double* partial, unsigned* counter, double* mean, cudaStream_t s);
 void launch_lexmax_seg(int nseg, const int64_t* off, int per, int V, const double* u,
                        const double* mean, int max_mode, double* partial, unsigned* counter,
-                       double* norms, cudaStream_t s);
+                       double* norms, cudaStream_t s, bool pdl = false);
 void launch_eps_f32(const EpsArgs& a, cudaStream_t s);
 
 struct RevArgs {
