@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
 
 template <int CH, bool RV, bool LAP>
 __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* err) {
+  constexpr int kRevBatch = CH < 4 ? CH : 4;
   constexpr int NARR = 1 + (RV ? 2 : 0) + (LAP ? 1 : 0);
   __shared__ __align__(128) unsigned char sbuf[kTmaWarps][2][NARR][CH * 128];
   __shared__ __align__(8) uint64_t bars[kTmaWarps][2];
@@ -240,38 +241,44 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
       phase[buf] ^= 1u;
       pending[buf] = false;
       const int* scol = reinterpret_cast<const int*>(sbuf[w][buf][0]);
+      const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][RV ? 1 : 0]);
+      const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][RV ? 2 : 0]);
+      const float* swl = reinterpret_cast<const float*>(sbuf[w][buf][NARR - 1]);
       const int j0 = c * CH;
-      if (RV) {
-        const float* swx = reinterpret_cast<const float*>(sbuf[w][buf][1]);
-        const float* swy = reinterpret_cast<const float*>(sbuf[w][buf][2]);
-        F8 st[CH];
+      // batches of kRevBatch slots: both records of every slot of a batch are requested
+      // before any is accumulated (one latency per batch, few registers held); each
+      // accumulator still takes its slots in order
 #pragma unroll
-        for (int k = 0; k < CH; ++k)
-          if (j0 + k < len) st[k] = ldg_f8(a.s32 + (int64_t)scol[k * 32 + lane] * 8);
+      for (int k0 = 0; k0 < CH; k0 += kRevBatch) {
+        F8 st[kRevBatch];
+        float4 qs[kRevBatch];
 #pragma unroll
-        for (int k = 0; k < CH; ++k)
-          if (j0 + k < len) {
-            const float wx = swx[k * 32 + lane], wy = swy[k * 32 + lane];
+        for (int k = 0; k < kRevBatch; ++k) {
+          const int kk = k0 + k;
+          if (j0 + kk < len) {
+            const int64_t cc = scol[kk * 32 + lane];
+            if (RV) st[k] = ldg_f8(a.s32 + cc * 8);
+            if (LAP) qs[k] = __ldg(Q4 + cc);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kRevBatch; ++k) {
+          const int kk = k0 + k;
+          if (j0 + kk >= len) continue;
+          if (RV) {
+            const float wx = swx[kk * 32 + lane], wy = swy[kk * 32 + lane];
             const float4 xs = st[k].lo, ys = st[k].hi;
             sx[0] = fmaf(wx, xs.x, sx[0]); sx[1] = fmaf(wx, xs.y, sx[1]);
             sx[2] = fmaf(wx, xs.z, sx[2]); sx[3] = fmaf(wx, xs.w, sx[3]);
             sy[0] = fmaf(wy, ys.x, sy[0]); sy[1] = fmaf(wy, ys.y, sy[1]);
             sy[2] = fmaf(wy, ys.z, sy[2]); sy[3] = fmaf(wy, ys.w, sy[3]);
           }
-      }
-      if (LAP) {
-        const float* swl = reinterpret_cast<const float*>(sbuf[w][buf][NARR - 1]);
-        float4 qs[CH];
-#pragma unroll
-        for (int k = 0; k < CH; ++k)
-          if (j0 + k < len) qs[k] = __ldg(Q4 + scol[k * 32 + lane]);
-#pragma unroll
-        for (int k = 0; k < CH; ++k)
-          if (j0 + k < len) {
-            const float wl = swl[k * 32 + lane];
+          if (LAP) {
+            const float wl = swl[kk * 32 + lane];
             sl[0] = fmaf(wl, qs[k].x, sl[0]); sl[1] = fmaf(wl, qs[k].y, sl[1]);
             sl[2] = fmaf(wl, qs[k].z, sl[2]); sl[3] = fmaf(wl, qs[k].w, sl[3]);
           }
+        }
       }
       __syncwarp();
       if (iss.s < nslices) {
