@@ -61,7 +61,7 @@ __global__ void k_vars_from_aos(const double* __restrict__ aos, VarPtrs dst, int
 }
 __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t count) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < count) b[i] = __double2float_rn(a[i]);
+  if (i < count) b[i] = fpconv::d2f(a[i]);
 }
 
 // ------------------------------------------------------------------ BC pass 1
@@ -84,7 +84,7 @@ __global__ void k_bc_pass1(int64_t nb, const int32_t* __restrict__ bnode, int V,
     return;
   }
   if (u32)
-    for (int v = 0; v < V; ++v) u32[i * V + v] = __double2float_rn(u[i * V + v]);
+    for (int v = 0; v < V; ++v) u32[i * V + v] = fpconv::d2f(u[i * V + v]);
 }
 
 // ------------------------------------------------------------------ flux
@@ -735,7 +735,7 @@ __global__ void k_scatter_values(int64_t nnz, const int64_t* __restrict__ pos,
   if (e >= nnz) return;
   const int64_t p = pos[e];
   out[p] = v[e];
-  if (out32) out32[p] = __double2float_rn(v[e]);
+  if (out32) out32[p] = fpconv::d2f(v[e]);
   if (outdw) outdw[p] = dw::split(v[e]);
 }
 

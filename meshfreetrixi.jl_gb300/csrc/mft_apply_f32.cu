@@ -70,9 +70,10 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_fwd_euler_f32(Fwd
   }
   if (WQ) reinterpret_cast<float4*>(a.q32)[i] = make_float4(q[0], q[1], q[2], q[3]);
   if (FLY == 2)
-    for (int v = 0; v < 4; ++v) a.hvf[i * 4 + v] = (double)(-hg * q[v]);
+    for (int v = 0; v < 4; ++v) a.hvf[i * 4 + v] = fpconv::f2d(-hg * q[v]);
   if (a.final_epilogue) {
-    double d[4] = {du[0], du[1], du[2], du[3]};
+    double d[4] = {fpconv::f2d(du[0]), fpconv::f2d(du[1]), fpconv::f2d(du[2]),
+                   fpconv::f2d(du[3])};
     finish_node<4>(a.ep, i, d);
   } else {
     reinterpret_cast<float4*>(a.du_p32)[i] = make_float4(du[0], du[1], du[2], du[3]);
@@ -103,9 +104,9 @@ __global__ void __launch_bounds__(kBlock) k_fwd_adv_f32(FwdArgs a) {
   if (FLY == 1) du = fmaf(-hg, q, du);
   if (WT) { a.t32[i * 2] = tx; a.t32[i * 2 + 1] = ty; }
   if (WQ) a.q32[i] = q;
-  if (FLY == 2) a.hvf[i] = (double)(-hg * q);
+  if (FLY == 2) a.hvf[i] = fpconv::f2d(-hg * q);
   if (a.final_epilogue) {
-    double d[1] = {du};
+    double d[1] = {fpconv::f2d(du)};
     finish_node<1>(a.ep, i, d);
   } else {
     a.du_p32[i] = du;
@@ -157,17 +158,17 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
       const double2 a0 = reinterpret_cast<const double2*>(a.approx_du)[i * 2];
       const double2 a1 = reinterpret_cast<const double2*>(a.approx_du)[i * 2 + 1];
       dpv[0] = d4.x; dpv[1 % V] = d4.y; dpv[2 % V] = d4.z; dpv[3 % V] = d4.w;
-      adv[0] = (float)a0.x; adv[1 % V] = (float)a0.y; adv[2 % V] = (float)a1.x;
-      adv[3 % V] = (float)a1.y;
+      adv[0] = fpconv::d2f(a0.x); adv[1 % V] = fpconv::d2f(a0.y);
+      adv[2 % V] = fpconv::d2f(a1.x); adv[3 % V] = fpconv::d2f(a1.y);
     } else {
       dpv[0] = a.du_p32[i];
-      adv[0] = (float)a.approx_du[i];
+      adv[0] = fpconv::d2f(a.approx_du[i]);
     }
     float mr = 0.0f;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
       float dp = dpv[v];
-      if (a.hvf) dp += (float)a.hvf[i * V + v];
+      if (a.hvf) dp += fpconv::d2f(a.hvf[i * V + v]);
       const float r = fabsf(adv[v] - dp);
       const float rn = a.seg_id ? (float)a.norms[sg * 2 * V + V + v] : s_rnorm[v];
       const float qv = r * rn;
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
   } else {
     eps = eps_uw;
   }
-  if (a.eps) a.eps[i] = (double)eps;
+  if (a.eps) a.eps[i] = fpconv::f2d(eps);
   if (V == 4) {
     float4* t4 = reinterpret_cast<float4*>(a.t32) + i * 2;
     float4 x = t4[0], y = t4[1];
@@ -269,13 +270,13 @@ __global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_rev_f32(RevArgs a
     float d = dp32[i * V + v];
     if (RV) d = (d - sx[v]) - sy[v];
     if (LAP) d = fmaf(-hg, sl[v], d);
-    if (a.hvf) d += (float)a.hvf[i * V + v];
+    if (a.hvf) d += fpconv::d2f(a.hvf[i * V + v]);
     du[v] = d;
   }
   if (a.final_epilogue) {
     double d[V];
 #pragma unroll
-    for (int v = 0; v < V; ++v) d[v] = du[v];
+    for (int v = 0; v < V; ++v) d[v] = fpconv::f2d(du[v]);
     finish_node<V>(a.ep, i, d);
   } else {
     float* out = a.du_p_out32;

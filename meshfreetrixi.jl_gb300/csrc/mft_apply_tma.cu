@@ -169,9 +169,10 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_fwd_euler_f32_tma(FwdArgs a,
     }
     if (WQ) reinterpret_cast<float4*>(a.q32)[i] = make_float4(q[0], q[1], q[2], q[3]);
     if (FLY == 2)
-      for (int v = 0; v < 4; ++v) a.hvf[i * 4 + v] = (double)(-hg * q[v]);
+      for (int v = 0; v < 4; ++v) a.hvf[i * 4 + v] = fpconv::f2d(-hg * q[v]);
     if (a.final_epilogue) {
-      double d[4] = {du[0], du[1], du[2], du[3]};
+      double d[4] = {fpconv::f2d(du[0]), fpconv::f2d(du[1]), fpconv::f2d(du[2]),
+                     fpconv::f2d(du[3])};
       finish_node<4>(a.ep, i, d);
     } else {
       reinterpret_cast<float4*>(a.du_p32)[i] = make_float4(du[0], du[1], du[2], du[3]);
@@ -295,11 +296,12 @@ __global__ void __launch_bounds__(32 * kTmaWarps) k_rev_f32_tma(RevArgs a, int* 
       float d = a.du_p32[i * 4 + v];
       if (RV) d = (d - sx[v]) - sy[v];
       if (LAP) d = fmaf(-hg, sl[v], d);
-      if (a.hvf) d += (float)a.hvf[i * 4 + v];
+      if (a.hvf) d += fpconv::d2f(a.hvf[i * 4 + v]);
       du[v] = d;
     }
     if (a.final_epilogue) {
-      double d[4] = {du[0], du[1], du[2], du[3]};
+      double d[4] = {fpconv::f2d(du[0]), fpconv::f2d(du[1]), fpconv::f2d(du[2]),
+                     fpconv::f2d(du[3])};
       finish_node<4>(a.ep, i, d);
     } else {
 #pragma unroll

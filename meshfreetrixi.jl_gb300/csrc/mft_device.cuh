@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "mft_fpbits.h"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -171,7 +172,7 @@ static __device__ __forceinline__ void finish_node(const Epilogue& ep, int64_t i
   for (int v = 0; v < V; ++v) ep.out[i * V + v] = o[v];
   if (ep.out32) {
 #pragma unroll
-    for (int v = 0; v < V; ++v) ep.out32[i * V + v] = __double2float_rn(o[v]);
+    for (int v = 0; v < V; ++v) ep.out32[i * V + v] = fpconv::d2f(o[v]);
   }
 }
 

@@ -27,21 +27,8 @@
 namespace mft {
 namespace dw {
 
-// (double)f, exact, on the integer pipe where the result is normal or zero.
-static __device__ __forceinline__ double f2d(float f) {
-  uint32_t hi, lo;
-  if (fpbits::f2d_words(__float_as_uint(f), &hi, &lo))
-    return __hiloint2double((int)hi, (int)lo);
-  return (double)f;
-}
-
-// RN32(x), on the integer pipe where the result is a normal float or zero.
-static __device__ __forceinline__ float d2f(double x) {
-  uint32_t r;
-  if (fpbits::d2f_bits((uint32_t)__double2hiint(x), (uint32_t)__double2loint(x), &r))
-    return __uint_as_float(r);
-  return __double2float_rn(x);
-}
+using fpconv::d2f;
+using fpconv::f2d;
 
 // x -> (h, l): h = RN32(x), l = RN32(x - h) (x - h is exact in FP64).
 static __device__ __forceinline__ float2 split(double x) {

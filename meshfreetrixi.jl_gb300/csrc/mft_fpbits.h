@@ -4,8 +4,10 @@
 // 1/74 of the FP32 rate.  Splitting an FP64 value into a double-word pair takes three of
 // them and one subtraction; the staged forward gather that forms its neighbours' flux
 // records splits four state values per record at the start of every block, where the
-// block's FP64 work is not hidden behind other warps.  Here the conversions are formed
-// from the IEEE-754 bit fields with 32-bit integer operations, leaving the subtraction:
+// block's FP64 work is not hidden behind other warps; the FP32-apply form converts its
+// partial du to FP64 and every new state to its FP32 shadow in the stage epilogues.  Here
+// the conversions are formed from the IEEE-754 bit fields with 32-bit integer operations
+// (fpconv::f2d / d2f below, the same bits as the hardware conversions):
 //   * float -> double is exact: the exponent is rebiased (127 -> 1023) and the 23-bit
 //     significand moved to the top of the 52-bit one;
 //   * double -> float rounds to nearest, ties to even: the 52-bit significand is cut to
@@ -68,6 +70,24 @@ MFT_FPBITS_FN bool d2f_bits(uint32_t hi, uint32_t lo, uint32_t* out) {
 }
 
 }  // namespace fpbits
+
+#if defined(__CUDACC__)
+namespace fpconv {
+// (double)f, exact, on the integer pipe where the result is normal or zero.
+static __device__ __forceinline__ double f2d(float f) {
+  uint32_t hi, lo;
+  if (fpbits::f2d_words(__float_as_uint(f), &hi, &lo)) return __hiloint2double((int)hi, (int)lo);
+  return (double)f;
+}
+// RN32(x), on the integer pipe where the result is a normal float or zero.
+static __device__ __forceinline__ float d2f(double x) {
+  uint32_t r;
+  if (fpbits::d2f_bits((uint32_t)__double2hiint(x), (uint32_t)__double2loint(x), &r))
+    return __uint_as_float(r);
+  return __double2float_rn(x);
+}
+}  // namespace fpconv
+#endif
 }  // namespace mft
 
 #undef MFT_FPBITS_FN
