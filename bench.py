@@ -991,16 +991,22 @@ def run_vortex(args, local, peaks):
         from meshfree_gb300 import workloads as W
         ex = W.isentropic_vortex(r["dom"].pd.points, t)
         l2 = float(np.linalg.norm(u[0] - ex[0]) / np.linalg.norm(ex[0]))
+        from meshfree_gb300 import _lib as L
         out[prec] = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / args.steps,
+                     "mapping": {"fwd_gather": ctx.get_option(L.OPT_TUNED_FWD),
+                                 "rev_gather": ctx.get_option(L.OPT_TUNED_REV)},
                      "kernels": _kernels(r["prof"]),
                      "roofline": roofline(r["prof"], n, prec, False, peaks, "dw",
                                           tag="%s_vortex" % ("fp64dw" if prec == "fp64" else prec)),
                      "path_roofline": path_roofline(r["value"], prec, False, peaks),
                      "to_t1": {"steps": nsteps, "t": t, "ms": ms_t1,
+                               "value": n * RHS_PER_STEP * nsteps / (ms_t1 * 1e-3),
                                "l2_density_err_vs_exact": l2}}
         ctx.close()
     out["workload"] = config_dict("vortex", side * side, "fp64")["workload"]
     out["fp32_speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # the same ratio over the runs to t = 1 (~256 steps each, a longer timed region)
+    out["fp32_speedup_vs_fp64_to_t1"] = out["fp32"]["to_t1"]["value"] / out["fp64"]["to_t1"]["value"]
     # the FP32 form's density against the FP64 form after the same timed steps (the
     # FP64 form equals the oracle's trajectory to 1e-10 on this workload: the -m gpu
     # full-size tests)
