@@ -882,6 +882,7 @@ void prepare_eps(EpsArgs& a) {
   a.uw_adv = a.uw_coef * std::sqrt(a.ax * a.ax + a.ay * a.ay);
   a.rv_coef = (0.5 * a.c_rv) * (a.h * a.h);
   a.uw_bound = a.uw_coef * a.uw_coef * ((1.0 - 1e-12) / (1.0 + 1e-12));
+  a.gg1 = a.gamma * (a.gamma - 1.0);
   const float h32 = (float)a.h;
   a.gamma32 = (float)a.gamma;
   a.gm1_32 = (float)(a.gamma - 1.0);

@@ -111,15 +111,19 @@ static __device__ __forceinline__ double eps_value(const EpsArgs& a, int64_t i,
     rho = ua.x; m1 = ua.y; m2 = ub.x; en = ub.y;
   }
   const double uwc = a.seg_h ? dmul(dmul(a.c_uw, 0.5), h) : a.uw_coef;
-  // Decided without forming eps_uw: the computed eps_uw = uwc (speed + c) is at least
-  // uwc |m| / rho (1 - 5 u) (c >= 0, no cancellation in speed; u = 2^-53), so
-  // (eps_rv rho)^2 < uwc^2 (1 - 1e-12) / (1 + 1e-12) |m|^2, evaluated in FP64 with a
-  // normal, finite right side, proves eps_rv < eps_uw and update_visc!'s min is eps_rv.
-  // This skips the reciprocal and the two square roots wherever the residual viscosity
-  // is the smaller one (smooth flow).  A NaN energy, or a density so small that 1 / rho
-  // overflows (0 * inf in a velocity), would make eps_uw NaN: no shortcut then.  Every
-  // comparison is on bit patterns of values >= 0 (or NaN, which fails them), so the
-  // test issues only five products and one sum on the FP64 pipe.
+  // Decided without forming eps_uw: speed + c >= sqrt(speed^2 + c^2), so in exact
+  // arithmetic (rho eps_uw)^2 >= uwc^2 (|m|^2 + gamma p rho) with
+  // p rho = (gamma - 1) (E rho - |m|^2 / 2).  The pressure term is counted only where
+  // |m|^2 <= E rho: the difference then keeps at least half of E rho (a few ulps of
+  // error), and p > 0, so the computed c is that of the formula; elsewhere the bound
+  // uses the speed alone (c >= 0).  The computed eps_uw is within ~20 u of the exact one
+  // (u = 2^-53), so (eps_rv rho)^2 < uwc^2 (1 - 1e-12) / (1 + 1e-12) w, evaluated in FP64
+  // with a normal, finite right side, proves eps_rv < eps_uw and update_visc!'s min is
+  // eps_rv.  This skips the reciprocal and the two square roots wherever the residual
+  // viscosity is the smaller one (smooth flow, and still flow: with the sound speed in the
+  // bound a node at rest qualifies too).  A NaN energy, or a density so small that
+  // 1 / rho overflows (0 * inf in a velocity), would make eps_uw NaN: no shortcut then.
+  // The final comparison is on bit patterns of values >= 0 (or NaN, which fails it).
   bool done = false;
   const double kb = a.seg_h ? dmul(dmul(uwc, uwc), (1.0 - 1e-12) / (1.0 + 1e-12)) : a.uw_bound;
   const long long bits_rho = __double_as_longlong(rho);
@@ -128,7 +132,11 @@ static __device__ __forceinline__ double eps_value(const EpsArgs& a, int64_t i,
       __double_as_longlong(uwc) > 0 && bits_en <= 0x7FF0000000000000LL) {
     const double er = dmul(eps_rv, rho);
     const double lhs = dmul(er, er);
-    const double rhs = dmul(kb, dadd(dmul(m1, m1), dmul(m2, m2)));
+    const double mm = dadd(dmul(m1, m1), dmul(m2, m2));
+    const double erho = dmul(en, rho);
+    double w = mm;
+    if (mm <= erho) w = dadd(mm, dmul(a.gg1, dsub(erho, dmul(0.5, mm))));
+    const double rhs = dmul(kb, w);
     const long long bl = __double_as_longlong(lhs), br = __double_as_longlong(rhs);
     if (br >= 0x03B8F2B061AEA072LL /* 1e-290 */ && br <= 0x7FE0000000000000LL /* 2^1023 */ &&
         bl < br) {

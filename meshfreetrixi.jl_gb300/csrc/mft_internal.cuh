@@ -231,6 +231,7 @@ struct EpsArgs {
   double uw_adv;           // advection: uw_coef * sqrt(ax^2 + ay^2)
   double rv_coef;          // (0.5 * c_rv) * (h * h)
   double uw_bound;         // uw_coef^2 (1 - 1e-12) / (1 + 1e-12): the eps_uw bound's factor
+  double gg1;              // gamma (gamma - 1): the sound speed's part of that bound
   // FP32 form: the FP32 shadow of u and the FP32 factors, formed by launch_eps in the
   // FP32 kernel's operation order
   const float* u32;
