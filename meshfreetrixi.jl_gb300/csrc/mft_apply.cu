@@ -59,6 +59,43 @@ __global__ void k_vars_from_aos(const double* __restrict__ aos, VarPtrs dst, int
 #pragma unroll
   for (int v = 0; v < V; ++v) dst.p[v][i] = aos[i * V + v];
 }
+// The same for V = 4 with two nodes per thread and 16-byte accesses to the caller's
+// arrays (host memory read or written over the host link: fewer, wider requests).  The
+// caller checks that every array is 16-byte aligned; an odd last node is taken singly.
+__global__ void k_aos_from_vars4x2(VarPtrs src, double* __restrict__ aos, int64_t n) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = 2 * j;
+  if (i >= n) return;
+  if (i + 1 < n) {
+    double2 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = reinterpret_cast<const double2*>(src.p[k])[j];
+    double2* o = reinterpret_cast<double2*>(aos) + i * 2;
+    o[0] = make_double2(v[0].x, v[1].x);
+    o[1] = make_double2(v[2].x, v[3].x);
+    o[2] = make_double2(v[0].y, v[1].y);
+    o[3] = make_double2(v[2].y, v[3].y);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) aos[i * 4 + k] = src.p[k][i];
+  }
+}
+__global__ void k_vars_from_aos4x2(const double* __restrict__ aos, VarPtrs dst, int64_t n) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = 2 * j;
+  if (i >= n) return;
+  if (i + 1 < n) {
+    const double2* a = reinterpret_cast<const double2*>(aos) + i * 2;
+    const double2 a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
+    reinterpret_cast<double2*>(dst.p[0])[j] = make_double2(a0.x, a2.x);
+    reinterpret_cast<double2*>(dst.p[1])[j] = make_double2(a0.y, a2.y);
+    reinterpret_cast<double2*>(dst.p[2])[j] = make_double2(a1.x, a3.x);
+    reinterpret_cast<double2*>(dst.p[3])[j] = make_double2(a1.y, a3.y);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) dst.p[k][i] = aos[i * 4 + k];
+  }
+}
 __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t count) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < count) b[i] = fpconv::d2f(a[i]);
@@ -757,10 +794,17 @@ void launch_aos_from_soa(const double* soa, double* aos, int64_t n, int V, cudaS
   k_aos_from_soa<<<grid_for(n, 256), 256, 0, s>>>(soa, aos, n, V);
   MFT_LAUNCH_CHECK();
 }
+static bool aligned16(const VarPtrs& v, int nv) {
+  for (int k = 0; k < nv; ++k)
+    if (reinterpret_cast<uintptr_t>(v.p[k]) & 15) return false;
+  return true;
+}
 void launch_aos_from_vars(const VarPtrs& src, double* aos, int64_t n, int V, cudaStream_t s) {
   if (n <= 0) return;
   MFT_REQUIRE(V == 1 || V == 4, MFT_ERR_UNSUPPORTED, "1 or 4 variables");
-  if (V == 4) k_aos_from_vars<4><<<grid_for(n, 256), 256, 0, s>>>(src, aos, n);
+  if (V == 4 && aligned16(src, 4))
+    k_aos_from_vars4x2<<<grid_for((n + 1) / 2, 256), 256, 0, s>>>(src, aos, n);
+  else if (V == 4) k_aos_from_vars<4><<<grid_for(n, 256), 256, 0, s>>>(src, aos, n);
   else k_aos_from_vars<1><<<grid_for(n, 256), 256, 0, s>>>(src, aos, n);
   MFT_LAUNCH_CHECK();
 }
@@ -768,7 +812,9 @@ void launch_vars_from_aos(const double* aos, const VarPtrs& dst, int64_t n, int 
                           cudaStream_t s) {
   if (n <= 0) return;
   MFT_REQUIRE(V == 1 || V == 4, MFT_ERR_UNSUPPORTED, "1 or 4 variables");
-  if (V == 4) k_vars_from_aos<4><<<grid_for(n, 256), 256, 0, s>>>(aos, dst, n);
+  if (V == 4 && aligned16(dst, 4))
+    k_vars_from_aos4x2<<<grid_for((n + 1) / 2, 256), 256, 0, s>>>(aos, dst, n);
+  else if (V == 4) k_vars_from_aos<4><<<grid_for(n, 256), 256, 0, s>>>(aos, dst, n);
   else k_vars_from_aos<1><<<grid_for(n, 256), 256, 0, s>>>(aos, dst, n);
   MFT_LAUNCH_CHECK();
 }

@@ -278,3 +278,56 @@ def test_graph_steps_equal_direct_steps_odd_count(gpu_lib):
         res.append(ctx.get_state())
     assert res[0][1] == res[1][1]
     assert np.array_equal(res[0][0], res[1][0])
+
+
+class _Rows:
+    """Per-variable arrays handed to the host entry point as separate rows."""
+
+    def __init__(self, rows):
+        self.rows = rows
+        self.shape = (len(rows), rows[0].shape[0])
+
+    def __iter__(self):
+        return iter(self.rows)
+
+
+def test_host_entry_point_odd_node_count_pinned_layouts(gpu_lib):
+    """An odd node count (39 x 39 vortex, 1,521 nodes) through pinned caller arrays: four
+    separately allocated rows (16-byte aligned: the two-nodes-per-thread layout kernels,
+    the last node taken singly) and one 2D array (its odd rows start 8 bytes off: the
+    one-node-per-thread kernels) give device stepping's states bit for bit."""
+    torch = pytest.importorskip("torch")
+    import meshfree_gb300 as M
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(39)
+    n = pts.shape[0]
+    assert n % 2 == 1
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom))
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                          solver, source_terms=src)
+    ctx = dom.ctx
+    u0 = semi.compute_coefficients(0.0)
+    dt = 0.2 * h
+    ctx.history_init(3)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, 3)
+    u_dev, t_dev = ctx.get_state()
+    rows = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    for v in range(4):
+        rows[v][:] = u0[v]
+    assert all(r.ctypes.data % 16 == 0 for r in rows)
+    whole = torch.empty((4, n), dtype=torch.float64, pin_memory=True).numpy()
+    whole[:] = u0
+    assert whole[1].ctypes.data % 16 == 8
+    for u in (_Rows(rows), whole):
+        ctx.history_init(3)
+        t = 0.0
+        for _ in range(3):
+            t = ctx.ssprk33_host(u, t, dt, 1)
+        assert t == t_dev
+        got = np.stack([np.array(r, copy=True) for r in u])
+        assert np.array_equal(got, u_dev)
