@@ -121,19 +121,34 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
   // FP64 -> FP32 conversions run on the FP64 pipe of this part: the state comes from its
   // FP32 shadow (the same rounded values), the node-independent factors from the launch
   // and, for one problem, the norms' reciprocals are converted once per block.
+  // V = 4: the node's records (state, partial du, approx_du, t) are requested before the
+  // block reads the norms and meets its barrier, so one memory latency covers them all.
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  const bool valid = i < a.n;
+  float4 q4 = {}, d4 = {}, tx4 = {}, ty4 = {};
+  double2 a0 = {}, a1 = {};
+  if (V == 4 && valid) {
+    if (a.u32) q4 = reinterpret_cast<const float4*>(a.u32)[i];
+    if (a.kind == MFT_SRC_RV) {
+      d4 = reinterpret_cast<const float4*>(a.du_p32)[i];
+      a0 = reinterpret_cast<const double2*>(a.approx_du)[i * 2];
+      a1 = reinterpret_cast<const double2*>(a.approx_du)[i * 2 + 1];
+    }
+    const float4* t4 = reinterpret_cast<const float4*>(a.t32) + i * 2;
+    tx4 = t4[0];
+    ty4 = t4[1];
+  }
   __shared__ float s_rnorm[V];
   if (!a.seg_id && threadIdx.x < V) s_rnorm[threadIdx.x] = (float)a.norms[V + threadIdx.x];
   __syncthreads();
-  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
-  if (i >= a.n) return;
+  if (!valid) return;
   const int sg = a.seg_id ? a.seg_id[i] : 0;
   const float h = a.seg_h ? (float)a.seg_h[sg] : (float)a.h;
   float eps_uw;
   if (V == 4) {
     float rho, m1, m2, en;
     if (a.u32) {
-      const float4 q = reinterpret_cast<const float4*>(a.u32)[i];
-      rho = q.x; m1 = q.y; m2 = q.z; en = q.w;
+      rho = q4.x; m1 = q4.y; m2 = q4.z; en = q4.w;
     } else {
       const double2 ua = reinterpret_cast<const double2*>(a.u)[i * 2];
       const double2 ub = reinterpret_cast<const double2*>(a.u)[i * 2 + 1];
@@ -154,9 +169,6 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
     // node records as 16-byte vectors (V = 4): du_p32 one float4, approx_du two double2
     float dpv[V], adv[V];
     if (V == 4) {
-      const float4 d4 = reinterpret_cast<const float4*>(a.du_p32)[i];
-      const double2 a0 = reinterpret_cast<const double2*>(a.approx_du)[i * 2];
-      const double2 a1 = reinterpret_cast<const double2*>(a.approx_du)[i * 2 + 1];
       dpv[0] = d4.x; dpv[1 % V] = d4.y; dpv[2 % V] = d4.z; dpv[3 % V] = d4.w;
       adv[0] = fpconv::d2f(a0.x); adv[1 % V] = fpconv::d2f(a0.y);
       adv[2 % V] = fpconv::d2f(a1.x); adv[3 % V] = fpconv::d2f(a1.y);
@@ -188,7 +200,7 @@ __global__ void __launch_bounds__(kBlock) k_eps_f32(EpsArgs a) {
   if (a.eps) a.eps[i] = fpconv::f2d(eps);
   if (V == 4) {
     float4* t4 = reinterpret_cast<float4*>(a.t32) + i * 2;
-    float4 x = t4[0], y = t4[1];
+    float4 x = tx4, y = ty4;
     x.x *= eps; x.y *= eps; x.z *= eps; x.w *= eps;
     y.x *= eps; y.y *= eps; y.z *= eps; y.w *= eps;
     t4[0] = x;
