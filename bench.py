@@ -596,8 +596,9 @@ def run_euler3d(args, local, peaks):
     ctx.close()
     fwd_ms, fwd_n = prof.get("fwd_gather", (0.0, 0))
     per = fwd_ms / max(fwd_n, 1)
-    # per node: indices 4k, weights 3*8k, flux record 120 + state 40 in, stage in/out 80
-    bytes_node = 4 * k + 24 * k + 120 + 40 + 80
+    # per node: indices 4k, weights 3*8k, flux record 96 (its 12 distinct values) + state
+    # 40 in, stage in/out 80
+    bytes_node = 4 * k + 24 * k + 96 + 40 + 80
     return {"workload": "CompressibleEulerEquations3D, periodic unit cube, N=%d jittered nodes, "
                         "PHS r^3 + degree-2 polynomials, k=%d, plain flux divergence (FP64 form, "
                         "double-word gathers), "

@@ -529,7 +529,7 @@ void ensure_work(mft_ctx* c) {
     c->tdw.alloc((size_t)n * 2 * V);
     c->qdw.alloc(nv);
   }
-  if (use_dw3(c)) c->Fdw.alloc((size_t)n * 16);  // 15 flux pairs per node, padded to 128 B
+  if (use_dw3(c)) c->Fdw.alloc((size_t)n * 12);  // the 12 distinct flux pairs of a node
   if (c->precision == MFT_PREC_FP32) {
     for (auto* b : {&c->U32[0], &c->U32[1], &c->U32[2], &c->U32[3]}) b->alloc(nv);
     c->du_p32.alloc(nv);
@@ -559,18 +559,22 @@ void ensure_device_ops(mft_ctx* c) {
   // double-word operator values are placed only while that form is in use
   const bool dw = use_dw(c) || use_dw3(c);
   if (dw && !c->fwdw[0].p) c->dev_dirty = true;
-  // neighbour halos of the row groups, for the staged gathers (double-word and FP32 2D
-  // Euler forms)
-  const bool halo = use_dw(c) || (c->precision == MFT_PREC_FP32 && c->eq == MFT_EQ_EULER2D);
+  // neighbour halos of the row groups, for the staged gathers (double-word 2D and 3D Euler
+  // forms, FP32 2D Euler form)
+  const bool halo = use_dw(c) || use_dw3(c) ||
+                    (c->precision == MFT_PREC_FP32 && c->eq == MFT_EQ_EULER2D);
   if (halo && !c->fwd.halo_off.p) c->dev_dirty = true;
   // 256-row groups when that still gives every SM several blocks, else 128
   int nsm = 0;
   MFT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+  // 3D clouds: 128-row groups (a 256-row group of a jittered cube gathers ~850 distinct
+  // neighbours, beyond kHaloMax; a 128-row group ~520)
   const int halo_rows =
       !halo ? 0
             : (c->halo_rows_opt > 0
                    ? c->halo_rows_opt
-                   : (c->n / kHaloRows >= 4 * (int64_t)nsm ? kHaloRows : kHaloRows / 2));
+                   : (c->dim == 3 || c->n / kHaloRows < 4 * (int64_t)nsm ? kHaloRows / 2
+                                                                         : kHaloRows));
   if (halo && c->fwd.halo_rows != halo_rows) c->dev_dirty = true;
   const bool spread = halo && c->entry_order == 1;
   if (halo && c->fwd.spread != spread) c->dev_dirty = true;

@@ -7,8 +7,12 @@
 // kernels.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <set>
+
 #include "mft_device.cuh"
 #include "mft_dw.cuh"
+#include "mft_halo.cuh"
 #include "mft_internal.cuh"
 
 namespace mft {
@@ -87,8 +91,14 @@ __global__ void __launch_bounds__(kBlock) k_fwd3_f64(FwdArgs a) {
 }
 
 // Double-word form: the state split into pairs and the flux formed in double-word
-// arithmetic (one reciprocal of rho refined by a Newton step), F[i] = 16 pairs (F_x, F_y,
-// F_z, 5 each, then a zero pad).  The only FP64 operations are the five splits.
+// arithmetic (one reciprocal of rho refined by a Newton step).  The momentum flux is
+// symmetric, so the 15 flux components hold 12 distinct values, each formed once and
+// stored as one pair: F[i] = 6 float4 =
+//   (m1, m2), (m3, m1 v1 + p), (m2 v2 + p, m3 v3 + p), (m1 v2, m1 v3), (m2 v3, (E+p) v1),
+//   ((E+p) v2, (E+p) v3)
+// (96 bytes), and F_x = (m1, m1 v1 + p, m1 v2, m1 v3, (E+p) v1), F_y = (m2, m1 v2,
+// m2 v2 + p, m2 v3, (E+p) v2), F_z = (m3, m1 v3, m2 v3, m3 v3 + p, (E+p) v3).  The only
+// FP64 operations are the five splits.
 __global__ void k_prep_euler3d_dw(int64_t n, float2 gm1, const double* __restrict__ u,
                                   float4* __restrict__ F) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -101,54 +111,82 @@ __global__ void k_prep_euler3d_dw(int64_t n, float2 gm1, const double* __restric
   const float2 mv = dw::add(dw::add(dw::mul(m[0], v[0]), dw::mul(m[1], v[1])), dw::mul(m[2], v[2]));
   const float2 p = dw::mul(gm1, dw::add(en, dw::neg(dw::scale2(mv, 0.5f))));
   const float2 ep = dw::add(en, p);
-  float2 f[16];
+  const float2 xx = dw::add(dw::mul(m[0], v[0]), p), yy = dw::add(dw::mul(m[1], v[1]), p);
+  const float2 zz = dw::add(dw::mul(m[2], v[2]), p);
+  const float2 xy = dw::mul(m[0], v[1]), xz = dw::mul(m[0], v[2]), yz = dw::mul(m[1], v[2]);
+  const float2 ex = dw::mul(ep, v[0]), ey = dw::mul(ep, v[1]), ez = dw::mul(ep, v[2]);
+  float4* Fi = F + i * 6;
+  Fi[0] = make_float4(m[0].x, m[0].y, m[1].x, m[1].y);
+  Fi[1] = make_float4(m[2].x, m[2].y, xx.x, xx.y);
+  Fi[2] = make_float4(yy.x, yy.y, zz.x, zz.y);
+  Fi[3] = make_float4(xy.x, xy.y, xz.x, xz.y);
+  Fi[4] = make_float4(yz.x, yz.y, ex.x, ex.y);
+  Fi[5] = make_float4(ey.x, ey.y, ez.x, ez.y);
+}
+
+static __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+static __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+// One stencil entry: the three weight pairs against the record's 15 flux components.
+static __device__ __forceinline__ void accum3(dw::Acc* f, const float2* w, const float4* q) {
+  const float2 m1 = lo2(q[0]), m2 = hi2(q[0]), m3 = lo2(q[1]), xx = hi2(q[1]);
+  const float2 yy = lo2(q[2]), zz = hi2(q[2]), xy = lo2(q[3]), xz = hi2(q[3]);
+  const float2 yz = lo2(q[4]), ex = hi2(q[4]), ey = lo2(q[5]), ez = hi2(q[5]);
+  const float2 fx[5] = {m1, xx, xy, xz, ex};
+  const float2 fy[5] = {m2, xy, yy, yz, ey};
+  const float2 fz[5] = {m3, xz, yz, zz, ez};
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    f[d * 5 + 0] = m[d];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float2 mk = dw::mul(m[d], v[k]);
-      f[d * 5 + 1 + k] = k == d ? dw::add(mk, p) : mk;
-    }
-    f[d * 5 + 4] = dw::mul(ep, v[d]);
+  for (int v = 0; v < 5; ++v) {
+    dw::fma_acc(f[v], w[0], fx[v]);
+    dw::fma_acc(f[v], w[1], fy[v]);
+    dw::fma_acc(f[v], w[2], fz[v]);
   }
-  f[15] = make_float2(0.f, 0.f);
-  float4* Fi = F + i * 8;
-#pragma unroll
-  for (int q = 0; q < 8; ++q) Fi[q] = make_float4(f[2 * q].x, f[2 * q].y, f[2 * q + 1].x, f[2 * q + 1].y);
 }
 
 // du_i = -sum_j (Dx_ij F_x + Dy_ij F_y + Dz_ij F_z)(node j) as compensated sums of
 // double-word products (mft_dw.cuh), the stage epilogue in FP64.  Per stencil entry: three
-// weight pairs and the neighbour's 128-byte flux record (four 32-byte loads).
-__global__ void __launch_bounds__(kBlock) k_fwd3_dw(FwdArgs a) {
-  const int64_t r = blockIdx.x * (int64_t)kBlock + threadIdx.x;  // layout row
+// weight pairs and the neighbour's 96-byte flux record.  HALO: one block per row group
+// (ell.halo_rows rows) first stages the group's neighbour records in shared memory (six
+// 16-byte chunks each, mft_halo.cuh) and reads them from there; a group without a list
+// gathers directly.  Both read the same records in the same order: the same sums.
+template <bool HALO>
+__global__ void __launch_bounds__(HALO ? kHaloRows : kBlock) k_fwd3_dw(FwdArgs a) {
+  const int64_t r = blockIdx.x * (int64_t)(HALO ? (int)blockDim.x : kBlock) + threadIdx.x;
+  const float4* __restrict__ F4 = reinterpret_cast<const float4*>(a.Fdw);
+  extern __shared__ float4 hsm3[];
+  bool staged = false;
+  if (HALO) staged = stage_halo<6>(a.ell, hsm3, [&](int k, int64_t c) { return F4 + c * 6 + k; });
   if (r >= a.n) return;
   const int64_t i = ell_node(a.ell, r);
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
-  const int32_t* __restrict__ col = a.ell.col;
-  const float* __restrict__ F = reinterpret_cast<const float*>(a.Fdw);
+  const int hs = a.ell.halo_stride;
   dw::Acc f[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) f[v] = dw::zero();
+  if (HALO && staged) {
+    const uint16_t* __restrict__ lcol = a.ell.lcol;
 #pragma unroll 2
-  for (int j = 0; j < len; ++j) {
-    const int64_t p = base + ((int64_t)j << 5);
-    const int64_t c = __ldg(col + p);
-    const float2 w[3] = {__ldg(a.wdw[0] + p), __ldg(a.wdw[1] + p), __ldg(a.wdw[2] + p)};
-    const F8 r0 = ldg_f8(F + c * 32), r1 = ldg_f8(F + c * 32 + 8);
-    const F8 r2 = ldg_f8(F + c * 32 + 16), r3 = ldg_f8(F + c * 32 + 24);
-    const float4 q[8] = {r0.lo, r0.hi, r1.lo, r1.hi, r2.lo, r2.hi, r3.lo, r3.hi};
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int lc = __ldg(lcol + p);
+      const float2 w[3] = {__ldg(a.wdw[0] + p), __ldg(a.wdw[1] + p), __ldg(a.wdw[2] + p)};
+      float4 q[6];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
+      for (int k = 0; k < 6; ++k) q[k] = hsm3[k * hs + lc];
+      accum3(f, w, q);
+    }
+  } else {
+    const int32_t* __restrict__ col = a.ell.col;
+#pragma unroll 2
+    for (int j = 0; j < len; ++j) {
+      const int64_t p = base + ((int64_t)j << 5);
+      const int64_t c = __ldg(col + p);
+      const float2 w[3] = {__ldg(a.wdw[0] + p), __ldg(a.wdw[1] + p), __ldg(a.wdw[2] + p)};
+      float4 q[6];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const int k = d * 5 + v;  // pair k of the record
-        const float4 qq = q[k >> 1];
-        const float2 fv = (k & 1) ? make_float2(qq.z, qq.w) : make_float2(qq.x, qq.y);
-        dw::fma_acc(f[v], w[d], fv);
-      }
+      for (int k = 0; k < 6; ++k) q[k] = __ldg(F4 + c * 6 + k);
+      accum3(f, w, q);
     }
   }
   double du[5];
@@ -173,7 +211,25 @@ void launch_fwd3_dw(const FwdArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
   MFT_REQUIRE(a.V == 5 && a.Fdw && a.wdw[0] && a.wdw[1] && a.wdw[2] && a.final_epilogue,
               MFT_ERR_STATE, "double-word 3D gather: arguments not set");
-  k_fwd3_dw<<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  if (a.ell.halo_off && a.ell.halo_rows > 0) {
+    // one block per row group, six chunks of the longest list in dynamic shared memory
+    // (above 48 KB a per-kernel opt-in, made once per device)
+    const size_t smem = (size_t)6 * a.ell.halo_stride * sizeof(float4);
+    if (smem > 48 * 1024) {
+      static std::mutex mu;
+      static std::set<int> done;
+      int dev = 0;
+      MFT_CUDA(cudaGetDevice(&dev));
+      std::lock_guard<std::mutex> lock(mu);
+      if (done.insert(dev).second)
+        MFT_CUDA(cudaFuncSetAttribute(k_fwd3_dw<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(6 * kHaloMax * sizeof(float4))));
+    }
+    const int rows = a.ell.halo_rows;
+    k_fwd3_dw<true><<<grid_for(a.n, rows), rows, smem, s>>>(a);
+  } else {
+    k_fwd3_dw<false><<<grid_for(a.n, kBlock), kBlock, 0, s>>>(a);
+  }
   MFT_LAUNCH_CHECK();
 }
 
