@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(kBlock) k_igr_dir(IgrArgs a, const double* un)
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   double sx = 0.0, sy = 0.0;
+#pragma unroll 4
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
     const int64_t c = __ldg(a.ell.col + p);
@@ -156,6 +157,7 @@ __global__ void __launch_bounds__(kBlock) k_igr_op(IgrArgs a, const double* un) 
     const int len = a.ell.row_len[r];
     double sx = 0.0, sy = 0.0;
     const double2* __restrict__ t2 = reinterpret_cast<const double2*>(a.t);
+#pragma unroll 4
     for (int j = 0; j < len; ++j) {
       const int64_t p = base + ((int64_t)j << 5);
       const int64_t c = __ldg(a.ell.col + p);
@@ -205,6 +207,7 @@ __global__ void __launch_bounds__(kBlock) k_igr_flux(IgrArgs a) {
   const int64_t base = a.ell.slice_off[r >> 5] + (r & 31);
   const int len = a.ell.row_len[r];
   double sx = 0.0, sy = 0.0;
+#pragma unroll 4
   for (int j = 0; j < len; ++j) {
     const int64_t p = base + ((int64_t)j << 5);
     const int64_t c = __ldg(a.ell.col + p);
