@@ -244,17 +244,17 @@ enum { MFT_OPT_GATHER = 0, MFT_OPT_TUNED_FWD = 1, MFT_OPT_TUNED_REV = 2,
  * the mean number of serialised shared-memory accesses per quarter-warp record load
  * (1000 = conflict-free), counted on the host when the layout is built; 0 before. */
 /* MFT_OPT_HALO_ROWS: layout rows per staged group (= threads per block of the staged
- * gathers): 0 (default) picks 256, or 128 when 256-row groups would give every SM fewer
- * than four; 128 or 256 fixes it (the layouts are rebuilt).  Read back: the size in use
+ * gathers): 0 (default) picks 256, or 128 on 3D clouds and when 256-row groups would give
+ * every SM fewer than four; 128 or 256 fixes it (the layouts are rebuilt).  Read back: the size in use
  * (0 when no staged layout is built). */
 /* Read-only MFT_OPT_IGR_ITERS: conjugate-gradient iterations of the last IGR solve
  * (-1 before the first).  Read-only MFT_OPT_ADJ_EVERY: the checkpoint interval of the last
  * mft_ssprk33_record (0: every stage state stored). */
-/* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups of the staged layouts (256
- * layout rows each, or 128 when 256-row groups would give every SM fewer than four),
- * MFT_OPT_HALO_STAGED_FWD / _REV = how many of them have their neighbour records staged
- * in shared memory by the staged gathers (the others gather directly); 0 before the first
- * evaluation in the double-word or FP32 Euler form. */
+/* Read-only (mft_get_option): MFT_OPT_HALO_GROUPS = row groups of the staged layouts
+ * (MFT_OPT_HALO_ROWS layout rows each), MFT_OPT_HALO_STAGED_FWD / _REV = how many of them
+ * have their neighbour records staged in shared memory by the staged gathers (the others
+ * gather directly); 0 before the first evaluation in the double-word (2D or 3D Euler) or
+ * FP32 2D Euler form. */
 /* MFT_OPT_DW_VARIANT: kernel variant of the double-word gathers -- 0 one stencil entry
  * per loop iteration, 1 two entries per iteration with registers capped at six blocks per
  * SM, 2 two entries uncapped, 3 software-pipelined (indices two entries ahead, weights and
