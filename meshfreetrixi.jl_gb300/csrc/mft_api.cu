@@ -60,7 +60,11 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 // CSR offset (within the row) placed there.
 static void spread_quarter(int nrows, const std::vector<int32_t>* lists,
                            std::vector<int32_t>* out) {
-  std::vector<std::pair<int32_t, int32_t>> bucket[8][8];  // [row][bank group]: (pos, offset)
+  // [row][bank group]: (pos, offset); per host thread, kept between calls (no allocation
+  // per quarter once the capacities have grown)
+  thread_local std::vector<std::pair<int32_t, int32_t>> bucket[8][8];
+  for (auto& row : bucket)
+    for (auto& b : row) b.clear();
   int left[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int k = 0; k < nrows; ++k) {
     out[k].assign(lists[k].size(), 0);
