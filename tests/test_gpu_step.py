@@ -331,3 +331,45 @@ def test_host_entry_point_odd_node_count_pinned_layouts(gpu_lib):
         assert t == t_dev
         got = np.stack([np.array(r, copy=True) for r in u])
         assert np.array_equal(got, u_dev)
+
+
+@pytest.mark.parametrize("mode", ["graph", "direct", "limited"])
+def test_host_entry_point_several_steps_per_call(gpu_lib, mode):
+    """Pinned caller arrays with three SSP-RK3 steps per host call (graph-replayed steps,
+    directly launched steps while profiling, and a stage limiter on density and pressure
+    after every stage): two calls equal six device steps bit for bit (vortex with residual
+    viscosity and history)."""
+    torch = pytest.importorskip("torch")
+    import meshfree_gb300 as M
+    from meshfree_gb300 import _lib as L
+    from meshfree_gb300 import workloads as W
+    pts, per, h = W.vortex_cloud(40)
+    basis = M.PointCloudBasis(M.Point2D(), 3, nv=35)
+    solver = M.PointCloudSolver(basis, M.RBFFDEngineGB300(precision="fp64"))
+    dom = M.PointCloudDomain(solver, pts, period=per)
+    eq = M.CompressibleEulerEquations2D(1.4)
+    src = M.SourceTerms(rv=M.SourceResidualViscosityTominec(solver, eq, dom))
+    semi = M.SemidiscretizationHyperbolic(dom, eq, lambda x, t, e: W.isentropic_vortex(x, t),
+                                          solver, source_terms=src)
+    ctx = dom.ctx
+    if mode == "limited":
+        ctx.set_limiter([L.LIM_DENSITY, L.LIM_PRESSURE], [0.05, 0.05])
+    u0 = semi.compute_coefficients(0.0)
+    dt = 0.2 * h
+    ctx.history_init(3)
+    ctx.set_state(u0, 0.0)
+    ctx.ssprk33(dt, 6, use_graph=(mode != "direct"))
+    u_dev, t_dev = ctx.get_state()
+    u = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    u[:] = u0
+    ctx.history_init(3)
+    if mode == "direct":
+        ctx.profile(True)  # profiled steps are launched directly
+    t = 0.0
+    for _ in range(2):
+        t = ctx.ssprk33_host(u, t, dt, 3)
+    if mode == "direct":
+        ctx.profile(False)
+    assert t == t_dev
+    assert np.array_equal(u, u_dev)
+    ctx.close()
