@@ -48,16 +48,17 @@ void set_device(mft_ctx* c) { MFT_CUDA(cudaSetDevice(c->device)); }
 // of a quarter-warp are served together, and records in the same bank group (their
 // position in the group's list mod 8) at different positions are served one after
 // another.  In ascending-column order the 8 lanes' positions fall into bank groups at
-// random (about 1.8 serialised accesses per quarter-warp load on a Morton-ordered cloud).
-// A row's sum may run in any order that every gather of that layout shares, so the
-// entries of each quarter-warp's rows are ordered slot by slot: the rows with the fewest
-// bank groups left choose first, each an entry in a bank group no other lane of the
-// quarter takes at this slot -- of the free groups the one with the most entries left
-// over the quarter's rows, so that crowded groups spread over all slots; a row without a
-// free group takes an entry another lane reads at this slot (one address is served
-// once), else one from its fullest group.  rows: the quarter's layout rows (at most 8);
-// lists: per row its entries' list positions, in CSR order; out: per row and slot the
-// CSR offset (within the row) placed there.
+// random (2.1 serialised accesses per quarter-warp load in the forward layout of a
+// Morton-ordered jittered cloud, 2.4 in the transpose layout).  A row's sum may run in any
+// order that every gather of that layout shares, so the entries of each quarter-warp's
+// rows are ordered slot by slot: the rows with the fewest bank groups left choose first,
+// each an entry in a bank group no other lane of the quarter takes at this slot -- of the
+// free groups the one with the most entries left over the quarter's rows, so that crowded
+// groups spread over all slots; a row without a free group takes an entry another lane
+// reads at this slot (one address is served once), else one from its fullest group
+// (1.09 and 1.21 accesses per load then).  nrows: the quarter's rows (at most 8); lists:
+// per row its entries' list positions, in CSR order; out: per row and slot the CSR offset
+// (within the row) placed there.
 static void spread_quarter(int nrows, const std::vector<int32_t>* lists,
                            std::vector<int32_t>* out) {
   // [row][bank group]: (pos, offset); per host thread, kept between calls (no allocation
